@@ -1,0 +1,66 @@
+"""Pins of the FP64 oracle against the reference's own known answers (no GPU).
+
+* ci-tests/full_test.py: final <m> and E_tot on examples/ellipsoid.msh, seed 2, for the
+  5-point and the 1-point Gauss builds, tolerance 1e-5 (the test's own threshold).
+* unit-tests/ut_readMesh.cpp: ellipsoid node/tet/triangle counts and the four
+  controlTriangles error messages on unit-tests/meshes/bad_cuboid_{1..4}.msh.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import fgo
+from oracle import mesh as om
+
+
+def _gold(golden_dir):
+    return json.load(open(os.path.join(golden_dir, "golden.json")))
+
+
+@pytest.mark.parametrize("one_point", [False, True])
+def test_full_test_golden(golden_dir, one_point):
+    g = _gold(golden_dir)["full_test"]
+    msh = om.read_msh(os.path.join(golden_dir, g["mesh"]))
+    m = om.setup(msh, [g["volume_region"]], [], g["length_unit"], Ms=[795774.7])
+    regs = [fgo.make_region(), fgo.make_region(K=g["K"], uk=g["uk"])]
+    o = fgo.Oracle(m, regs, one_gauss_point=one_point)
+    o.set_state(np.tile(g["initial_magnetization"], (len(m["xyz"]), 1)))
+    Hext = np.array(g["Bext"]) / fgo.MU0
+    rows, nsteps, _ = o.time_integration(g["seed"], g["final_time"], g["min_dt"], g["max_dt"],
+                                         g["evol_time_step"], g["max_du"], Hext)
+    exp = g["expected_1pt" if one_point else "expected_5pt"]
+    last = rows[-1]
+    assert abs(last[0] - g["final_time"]) < 1e-20
+    m_err = np.linalg.norm(np.array(exp["m"]) - last[1:4])
+    e_err = abs((last[7] - exp["E_tot"]) / exp["E_tot"])
+    assert m_err < g["threshold"], (last[1:4], exp["m"])
+    assert e_err < g["threshold"], (last[7], exp["E_tot"])
+    assert len(rows) == round(g["final_time"] / g["evol_time_step"]) + 1
+
+
+def test_ellipsoid_counts(golden_dir):
+    g = _gold(golden_dir)
+    msh = om.read_msh(os.path.join(golden_dir, "ellipsoid.msh"))
+    c = g["ellipsoid_counts"]
+    assert msh["nodes"].shape[0] == c["nodes"]
+    ntet = sum(len(b[4]) for b in msh["blocks"] if b[3] == 4)
+    ntri = sum(len(b[4]) for b in msh["blocks"] if b[3] == 2)
+    assert (ntet, ntri) == (c["tets"], c["tris"])
+    # with the surface declared in the settings, the file's triangles are used as they are
+    m = om.setup(msh, ["ellipsoid_volume"], ["ellipsoid_surface"], 1e-9, Ms=[8e5])
+    assert len(m["tris"]) == c["tris"] and len(m["surf_names"]) == 2
+    # without it, controlTriangles recreates exactly the same boundary
+    m2 = om.setup(msh, ["ellipsoid_volume"], [], 1e-9, Ms=[8e5])
+    assert len(m2["tris"]) == c["tris"] and m2["surf_names"][1] == "surface(ellipsoid_volume)"
+    assert np.all(np.abs(m2["dMs"]) == 8e5)
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4])
+def test_bad_cuboid_messages(golden_dir, k):
+    g = _gold(golden_dir)
+    msh = om.read_msh(os.path.join(golden_dir, f"bad_cuboid_{k}.msh"))
+    with pytest.raises(om.MeshError) as e:
+        om.setup(msh, ["whole_volume"], ["whole_surface"], 1.0, Ms=[8e5])
+    assert str(e.value) == g["bad_cuboid_errors"][k - 1]
