@@ -1,0 +1,242 @@
+"""ctypes binding of the fggpu C ABI (include/fggpu.h).
+
+``Context`` mirrors the reference's per-step sequence (src/time_integration.cpp:193-231):
+``step`` = base_projection + prepareElements + solve, ``compute_all`` = demag of m and
+of v, energy, evolution. Arrays are numpy host arrays in the caller's node numbering.
+Loading fails loudly when the library has not been built: nothing here computes on
+the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+MU0 = 1.25663706127e-6
+GAMMA0 = 1.76085962784e11 * MU0
+
+FG_OK, FG_SOLVER_ITER_OVERFLOW, FG_SOLVER_CANNOT_CONVERGE, FG_ETIMEDOUT = 0, 1, 2, 3
+FG_EINVAL, FG_ECUDA, FG_ENOMEM, FG_EMESH, FG_EIO = 4, 5, 6, 7, 8
+FG_PREC_FP64, FG_PREC_FP32_REFINE = 0, 1
+FG_DEMAG_AUTO, FG_DEMAG_DIRECT, FG_DEMAG_FMM = 0, 1, 2
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def lib_path():
+    return os.path.join(_HERE, "_build", "libfggpu.so")
+
+
+class FgError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"fggpu status {status}: {msg}")
+        self.status = status
+
+
+class fg_mesh(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("n_tets", C.c_int), ("n_tris", C.c_int), ("xyz", C.c_void_p),
+                ("tet4", C.c_void_p), ("tet_region", C.c_void_p), ("tri3", C.c_void_p),
+                ("tri_region", C.c_void_p), ("tri_dMs", C.c_void_p)]
+
+
+class fg_region(C.Structure):
+    _fields_ = [("Ae", C.c_double), ("Ms", C.c_double), ("K", C.c_double), ("uk", C.c_double * 3),
+                ("K3", C.c_double), ("ex", C.c_double * 3), ("ey", C.c_double * 3), ("ez", C.c_double * 3),
+                ("alpha", C.c_double)]
+
+
+class fg_tri_region(C.Structure):
+    _fields_ = [("Ks", C.c_double), ("uk", C.c_double * 3), ("suppress_charges", C.c_int)]
+
+
+class fg_opts(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("precision", C.c_int), ("learned_guess", C.c_int),
+                ("demag", C.c_int), ("fmm_order", C.c_int), ("fmm_leaf", C.c_int), ("one_gauss_point", C.c_int),
+                ("first_order", C.c_int), ("refine_max", C.c_int), ("inner_tol", C.c_double),
+                ("verbose", C.c_int)]
+
+
+class fg_step_report(C.Structure):
+    _fields_ = [("status", C.c_int), ("iters", C.c_int), ("refinements", C.c_int), ("guess_accepted", C.c_int),
+                ("vmax", C.c_double), ("res", C.c_double), ("rhsn", C.c_double), ("res0", C.c_double),
+                ("res0_fallback", C.c_double)]
+
+
+StepReport = dict
+
+_dp = C.POINTER(C.c_double)
+_lib = None
+
+# every symbol include/fggpu.h declares, with (restype, argtypes)
+SIGNATURES = {
+    "fg_opts_default": (None, [C.POINTER(fg_opts)]),
+    "fg_strerror": (C.c_char_p, [C.c_int]),
+    "fg_last_error": (C.c_char_p, [C.c_void_p]),
+    "fg_create": (C.c_int, [C.POINTER(fg_mesh), C.POINTER(fg_region), C.c_int, C.POINTER(fg_tri_region), C.c_int,
+                            C.POINTER(fg_opts), C.POINTER(C.c_void_p)]),
+    "fg_destroy": (None, [C.c_void_p]),
+    "fg_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fg_step": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, C.c_double, C.POINTER(fg_step_report)]),
+    "fg_compute_all": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "fg_get_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fg_demag": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+    "fg_energy": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "fg_average": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+    "fg_debug_system": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fg_debug_apply": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "fg_timings": (C.c_int, [C.c_void_p, _dp]),
+}
+
+
+def fg_lib():
+    """Load libfggpu.so (raises when it has not been built)."""
+    global _lib
+    if _lib is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            raise ImportError(f"{path} is missing: build it with `python -m feellgood_gb300.build` "
+                              "(there is no CPU fallback)")
+        L = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def make_region(Ae=1e-11, Ms=795774.7, K=0.0, uk=(0, 0, 1), K3=0.0, ex=(1, 0, 0), ey=(0, 1, 0), ez=(0, 0, 1),
+                alpha=0.5, **_):
+    r = fg_region()
+    r.Ae, r.Ms, r.K, r.K3, r.alpha = Ae, Ms, K, K3, alpha
+    for name, v in (("uk", uk), ("ex", ex), ("ey", ey), ("ez", ez)):
+        v = np.asarray(v, float)
+        getattr(r, name)[:] = list(v / np.linalg.norm(v))
+    return r
+
+
+def make_tri_region(Ks=0.0, uk=(0, 0, 1), suppress_charges=False, **_):
+    r = fg_tri_region()
+    r.Ks = Ks
+    v = np.asarray(uk, float)
+    r.uk[:] = list(v / np.linalg.norm(v))
+    r.suppress_charges = int(bool(suppress_charges))
+    return r
+
+
+class Context:
+    """One mesh (or batch) resident on the GPU; see include/fggpu.h."""
+
+    def __init__(self, mesh, regions, tri_regions=None, **opts):
+        L = fg_lib()
+        self.L = L
+        self._keep = []
+        xyz = np.ascontiguousarray(mesh["xyz"], dtype=np.float64)
+        tets = np.ascontiguousarray(mesh["tets"], dtype=np.int32)
+        treg = np.ascontiguousarray(mesh["tet_reg"], dtype=np.int32)
+        tris = np.ascontiguousarray(mesh.get("tris", np.zeros((0, 3))), dtype=np.int32).reshape(-1, 3)
+        freg = np.ascontiguousarray(mesh.get("tri_reg", np.zeros(0)), dtype=np.int32)
+        dms = np.ascontiguousarray(mesh.get("dMs", np.zeros(0)), dtype=np.float64)
+        self._keep += [xyz, tets, treg, tris, freg, dms]
+        m = fg_mesh(len(xyz), len(tets), len(tris), _ptr(xyz), _ptr(tets), _ptr(treg), _ptr(tris), _ptr(freg),
+                    _ptr(dms))
+        regs = [r if isinstance(r, fg_region) else make_region(**r) for r in regions]
+        if tri_regions is None:
+            tri_regions = [make_tri_region() for _ in range(int(freg.max()) + 1 if len(freg) else 1)]
+        tregs = [r if isinstance(r, fg_tri_region) else make_tri_region(**r) for r in tri_regions]
+        R = (fg_region * len(regs))(*regs)
+        T = (fg_tri_region * len(tregs))(*tregs)
+        o = fg_opts()
+        L.fg_opts_default(C.byref(o))
+        for k, v in opts.items():
+            if not hasattr(o, k):
+                raise TypeError(f"unknown option {k}")
+            setattr(o, k, v)
+        self.opts = o
+        h = C.c_void_p()
+        s = L.fg_create(C.byref(m), R, len(regs), T, len(tregs), C.byref(o), C.byref(h))
+        if s != FG_OK:
+            raise FgError(s, L.fg_last_error(None).decode())
+        self.h = h
+        self.nn = len(xyz)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, s):
+        if s not in (FG_OK,):
+            raise FgError(s, self.L.fg_last_error(self.h).decode())
+
+    def set_state(self, u, v=None, phi=None, phiv=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (u, v, phi, phiv)]
+        self._check(self.L.fg_set_state(self.h, *[_ptr(a) for a in arrs]))
+
+    def get_state(self, which=1):
+        u, v = np.zeros((self.nn, 3)), np.zeros((self.nn, 3))
+        phi, phiv = np.zeros(self.nn), np.zeros(self.nn)
+        self._check(self.L.fg_get_state(self.h, which, _ptr(u), _ptr(v), _ptr(phi), _ptr(phiv)))
+        return {"u": u, "v": v, "phi": phi, "phiv": phiv}
+
+    def step(self, dt, prefactor, Hext, angle):
+        """Returns the report dict; report['status'] is FG_OK or a solver status."""
+        rep = fg_step_report()
+        H = np.ascontiguousarray(Hext, dtype=np.float64)
+        s = self.L.fg_step(self.h, dt, prefactor, _dptr(H), angle, C.byref(rep))
+        if s not in (FG_OK, FG_SOLVER_ITER_OVERFLOW, FG_SOLVER_CANNOT_CONVERGE):
+            self._check(s)
+        return {k: getattr(rep, k) for k, _ in fg_step_report._fields_}
+
+    def compute_all(self, Hext):
+        H = np.ascontiguousarray(Hext, dtype=np.float64)
+        E = np.zeros(4)
+        self._check(self.L.fg_compute_all(self.h, _dptr(H), _dptr(E)))
+        return E
+
+    def demag(self, which=0):
+        out = np.zeros(self.nn)
+        self._check(self.L.fg_demag(self.h, which, _dptr(out)))
+        return out
+
+    def energy(self, Hext):
+        H = np.ascontiguousarray(Hext, dtype=np.float64)
+        E = np.zeros(4)
+        self._check(self.L.fg_energy(self.h, _dptr(H), _dptr(E)))
+        return E
+
+    def average(self, which=0):
+        a = np.zeros(3)
+        self._check(self.L.fg_average(self.h, which, _dptr(a)))
+        return a
+
+    def debug_system(self):
+        rhs, ep, eq = np.zeros(2 * self.nn), np.zeros((self.nn, 3)), np.zeros((self.nn, 3))
+        self._check(self.L.fg_debug_system(self.h, _ptr(rhs), _ptr(ep), _ptr(eq)))
+        return rhs, ep, eq
+
+    def debug_apply(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        self._check(self.L.fg_debug_apply(self.h, _dptr(x), _dptr(y)))
+        return y
+
+    def timings(self):
+        ms = np.zeros(4)
+        self._check(self.L.fg_timings(self.h, _dptr(ms)))
+        return ms

@@ -1,0 +1,702 @@
+// C ABI of the fggpu library: context construction (once per mesh), state transfer and
+// the per-step orchestration of the device kernels. No function exits the process and
+// no exception crosses the ABI.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "fg_internal.h"
+
+namespace fg {
+void upload_rules(bool one_point);
+int fmm_build(Ctx &c);
+void fmm_free(Ctx &c);
+cudaError_t fmm_eval(Ctx &c);
+}  // namespace fg
+
+using namespace fg;
+
+struct fg_ctx {
+    Ctx c;
+    double last_c0 = 0.0;
+};
+
+static thread_local std::string g_create_error;
+
+#define CK(call)                                                                      \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess) {                                                      \
+            c.err = std::string(#call) + ": " + cudaGetErrorString(e_);               \
+            return FG_ECUDA;                                                          \
+        }                                                                             \
+    } while (0)
+
+template <typename T>
+static cudaError_t dalloc(T **p, size_t n) {
+    if (n == 0) n = 1;
+    return cudaMalloc((void **)p, n * sizeof(T));
+}
+template <typename T>
+static cudaError_t upload(T **p, const std::vector<T> &h) {
+    cudaError_t e = dalloc(p, h.size());
+    if (e != cudaSuccess) return e;
+    if (!h.empty()) e = cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return e;
+}
+
+namespace {
+
+struct Rules {
+    int npi_t, npi_f;
+    double ta[4][5], tp[5], fa[3][4], fp[4];
+};
+
+Rules make_rules(bool one) {
+    Rules r{};
+    if (one) {
+        r.npi_t = 1;
+        r.npi_f = 1;
+        for (int i = 0; i < 4; i++) r.ta[i][0] = 0.25;
+        r.tp[0] = 1.0 / 6.0;
+        for (int i = 0; i < 3; i++) r.fa[i][0] = 1.0 / 3.0;
+        r.fp[0] = 0.5;
+    } else {
+        r.npi_t = 5;
+        r.npi_f = 4;
+        const double A = 1. / 4., B = 1. / 6., C = 1. / 2., D = -2. / 15., E = 3. / 40.;
+        const double u[5] = {A, B, B, B, C}, v[5] = {A, B, B, C, B}, w[5] = {A, B, C, B, B};
+        const double p[5] = {D, E, E, E, E};
+        for (int j = 0; j < 5; j++) {
+            r.ta[0][j] = 1. - u[j] - v[j] - w[j];
+            r.ta[1][j] = u[j];
+            r.ta[2][j] = v[j];
+            r.ta[3][j] = w[j];
+            r.tp[j] = p[j];
+        }
+        const double fu[4] = {1 / 3., 1 / 5., 3 / 5., 1 / 5.}, fv[4] = {1 / 3., 1 / 5., 1 / 5., 3 / 5.};
+        const double fpds[4] = {-27 / 96., 25 / 96., 25 / 96., 25 / 96.};
+        for (int j = 0; j < 4; j++) {
+            r.fa[0][j] = 1. - fu[j] - fv[j];
+            r.fa[1][j] = fu[j];
+            r.fa[2][j] = fv[j];
+            r.fp[j] = fpds[j];
+        }
+    }
+    return r;
+}
+
+struct P3 {
+    double x, y, z;
+};
+inline P3 sub(P3 a, P3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline double dot3(P3 a, P3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline P3 cross3(P3 a, P3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double nrm(P3 a) { return std::sqrt(dot3(a, a)); }
+
+// Tri::potential geometry (src/triangle.cpp:87-125): coefficients of s_i, s_{i+1}, s_{i+2}.
+void tri_potential_coeffs(P3 p1, P3 p2, P3 p3, double surf, double out[3]) {
+    P3 p1p2 = sub(p2, p1), p1p3 = sub(p3, p1);
+    auto f = [](double x) { return std::sqrt(1.0 + x * x); };
+    double b = nrm(p1p2);
+    double t = dot3(p1p2, p1p3) / b;
+    double _2s = 2. * surf;
+    double h = _2s / b;
+    double c = (t - b) / h;
+    double r = h * f(t / h);
+    double log_1 = std::log((c * t + h + f(c) * r) / (b * (c + f(c))));
+    double xi = b * log_1 / f(c);
+    double den = b / (_2s * (1 + c * c));
+    out[0] = xi;
+    out[1] = (xi * (h + c * t) - b * (r - b)) * den;
+    out[2] = b * (r - b - c * xi) * den;
+}
+
+}  // namespace
+
+extern "C" {
+
+void fg_opts_default(fg_opts *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->tol = 1e-6;
+    o->max_iter = 700;
+    o->precision = FG_PREC_FP64;
+    o->learned_guess = 0;
+    o->demag = FG_DEMAG_AUTO;
+    o->fmm_order = 0;
+    o->fmm_leaf = 0;
+    o->one_gauss_point = 0;
+    o->first_order = 0;
+    o->refine_max = 20;
+    o->inner_tol = 1e-3;
+    o->verbose = 0;
+}
+
+const char *fg_strerror(int s) {
+    switch (s) {
+        case FG_OK: return "ok";
+        case FG_SOLVER_ITER_OVERFLOW: return "solver: iteration overflow";
+        case FG_SOLVER_CANNOT_CONVERGE: return "solver: cannot converge";
+        case FG_ETIMEDOUT: return "bounded device wait timed out";
+        case FG_EINVAL: return "invalid argument";
+        case FG_ECUDA: return "CUDA error";
+        case FG_ENOMEM: return "out of memory";
+        case FG_EMESH: return "invalid mesh";
+        case FG_EIO: return "I/O error";
+        default: return "unknown status";
+    }
+}
+
+const char *fg_last_error(const fg_ctx *ctx) { return ctx ? ctx->c.err.c_str() : g_create_error.c_str(); }
+
+static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int nreg, const fg_tri_region *tregs,
+                       int ntreg, const fg_opts *opts) {
+    Ctx &c = h->c;
+    if (opts) c.opts = *opts; else fg_opts_default(&c.opts);
+    if (!m || !regs || nreg <= 0 || m->n_nodes <= 0 || m->n_tets <= 0 || !m->xyz || !m->tet4 || !m->tet_region) {
+        c.err = "fg_create: missing mesh or region data";
+        return FG_EINVAL;
+    }
+    if (m->n_tris > 0 && (!m->tri3 || !m->tri_region || !m->tri_dMs || !tregs || ntreg <= 0)) {
+        c.err = "fg_create: triangles given without their regions";
+        return FG_EINVAL;
+    }
+    const Rules R = make_rules(c.opts.one_gauss_point != 0);
+    c.npi_t = R.npi_t;
+    c.npi_f = R.npi_f;
+    const int nn = m->n_nodes;
+    c.nn = nn;
+    c.n_tets_total = m->n_tets;
+    CK(cudaGetDevice(&c.device));
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, c.device));
+    c.nsm = prop.multiProcessorCount;
+    CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 8; k++) CK(cudaEventCreate(&c.ev[k]));
+    upload_rules(c.opts.one_gauss_point != 0);
+
+    // region table
+    std::vector<DevRegion> hreg(nreg);
+    for (int r = 0; r < nreg; r++) {
+        const fg_region &g = regs[r];
+        DevRegion &d = hreg[r];
+        std::memset(&d, 0, sizeof(d));
+        d.A = g.Ae; d.Ms = g.Ms; d.alpha = g.alpha; d.K = g.K; d.K3 = g.K3;
+        if (g.Ms > 0) {
+            d.Abis = 2.0 * g.Ae / (FG_MU0 * g.Ms);
+            d.Kbis = 2.0 * g.K / (FG_MU0 * g.Ms);
+            d.K3bis = 2.0 * g.K3 / (FG_MU0 * g.Ms);
+        }
+        for (int k = 0; k < 3; k++) {
+            d.uk[k] = g.uk[k]; d.ex[k] = g.ex[k]; d.ey[k] = g.ey[k]; d.ez[k] = g.ez[k];
+        }
+    }
+    // magnetic tetrahedra and nodes (src/mesh.h:115-131)
+    std::vector<unsigned char> mag(nn, 0);
+    std::vector<int> mtets;
+    for (int t = 0; t < m->n_tets; t++) {
+        const int r = m->tet_region[t];
+        if (r < 0 || r >= nreg) { c.err = "fg_create: tet region out of range"; return FG_EINVAL; }
+        for (int i = 0; i < 4; i++) {
+            const int v = m->tet4[4 * t + i];
+            if (v < 0 || v >= nn) { c.err = "fg_create: tet node index out of range"; return FG_EMESH; }
+        }
+        if (regs[r].Ms > 0) {
+            mtets.push_back(t);
+            for (int i = 0; i < 4; i++) mag[m->tet4[4 * t + i]] = 1;
+        }
+    }
+    c.h_mag = mag;
+    c.h_xyz.assign(m->xyz, m->xyz + 3 * (size_t)nn);
+    const int nmt = (int)mtets.size();
+    c.nmt = nmt;
+    auto P = [&](int i) { return P3{m->xyz[3 * i], m->xyz[3 * i + 1], m->xyz[3 * i + 2]}; };
+
+    // per-tet geometry: da = dadu inv(J), detJ (src/tetra.h:140-163)
+    std::vector<double> da(12 * (size_t)nmt), detJ(nmt);
+    std::vector<int4> htet(nmt);
+    std::vector<int> htreg(nmt);
+    std::vector<double> A(nn, 0.0);
+    for (int k = 0; k < nmt; k++) {
+        const int t = mtets[k];
+        const int *ind = &m->tet4[4 * t];
+        htet[k] = make_int4(ind[0], ind[1], ind[2], ind[3]);
+        htreg[k] = m->tet_region[t];
+        P3 p0 = P(ind[0]);
+        P3 a = sub(P(ind[1]), p0), b = sub(P(ind[2]), p0), cc = sub(P(ind[3]), p0);
+        double J[3][3] = {{a.x, b.x, cc.x}, {a.y, b.y, cc.y}, {a.z, b.z, cc.z}};
+        double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                     J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                     J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+        if (!(det > 0)) {
+            c.err = "fg_create: tetrahedron " + std::to_string(t) + " is flat or not positively oriented";
+            return FG_EMESH;
+        }
+        double inv[3][3];
+        inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+        inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+        inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+        inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+        inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+        inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+        inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+        inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+        inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+        const double dadu[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+        for (int i = 0; i < 4; i++)
+            for (int q = 0; q < 3; q++) {
+                double s = 0;
+                for (int mm = 0; mm < 3; mm++) s += dadu[i][mm] * inv[mm][q];
+                da[(3 * i + q) * (size_t)nmt + k] = s;
+            }
+        detJ[k] = det;
+        for (int i = 0; i < 4; i++) {
+            double aw = 0;
+            for (int g = 0; g < R.npi_t; g++) aw += R.ta[i][g] * (det * R.tp[g]);
+            A[ind[i]] += aw;
+        }
+        for (int g = 0; g < R.npi_t; g++) c.total_mag_vol += det * R.tp[g];
+    }
+    // static stiffness S_ij = sum_t Abis vol (da_i . da_j) on the node graph (with diagonal)
+    std::vector<std::vector<int>> nb(nn);
+    for (int k = 0; k < nmt; k++) {
+        const int4 I = htet[k];
+        const int ind[4] = {I.x, I.y, I.z, I.w};
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) nb[ind[i]].push_back(ind[j]);
+    }
+    std::vector<int> Sptr(nn + 1, 0);
+    for (int i = 0; i < nn; i++) {
+        auto &v = nb[i];
+        v.push_back(i);
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        Sptr[i + 1] = Sptr[i] + (int)v.size();
+    }
+    c.nnzS = Sptr[nn];
+    std::vector<int> Scol(c.nnzS);
+    for (int i = 0; i < nn; i++) std::copy(nb[i].begin(), nb[i].end(), Scol.begin() + Sptr[i]);
+    nb.clear();
+    nb.shrink_to_fit();
+    std::vector<double> Sval(c.nnzS, 0.0);
+    for (int k = 0; k < nmt; k++) {
+        const int4 I = htet[k];
+        const int ind[4] = {I.x, I.y, I.z, I.w};
+        const double Abis = hreg[htreg[k]].Abis;
+        double wsum = 0;
+        for (int g = 0; g < R.npi_t; g++) wsum += detJ[k] * R.tp[g];
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) {
+                double dd = 0;
+                for (int q = 0; q < 3; q++)
+                    dd += da[(3 * i + q) * (size_t)nmt + k] * da[(3 * j + q) * (size_t)nmt + k];
+                auto b0 = Scol.begin() + Sptr[ind[i]], e0 = Scol.begin() + Sptr[ind[i] + 1];
+                auto it = std::lower_bound(b0, e0, ind[j]);
+                Sval[it - Scol.begin()] += dd * (Abis * wsum);
+            }
+    }
+    // node -> tet-vertex slots
+    std::vector<int> inc_ptr(nn + 1, 0), inc(4 * (size_t)nmt);
+    for (int k = 0; k < nmt; k++) {
+        inc_ptr[htet[k].x + 1]++; inc_ptr[htet[k].y + 1]++; inc_ptr[htet[k].z + 1]++; inc_ptr[htet[k].w + 1]++;
+    }
+    for (int i = 0; i < nn; i++) inc_ptr[i + 1] += inc_ptr[i];
+    {
+        std::vector<int> fill(inc_ptr.begin(), inc_ptr.end() - 1);
+        for (int k = 0; k < nmt; k++) {
+            const int ind[4] = {htet[k].x, htet[k].y, htet[k].z, htet[k].w};
+            for (int i = 0; i < 4; i++) inc[fill[ind[i]]++] = 4 * k + i;
+        }
+    }
+    // magnetic triangles (src/mesh.h:127-131) and their charge/correction constants
+    std::vector<int4> htri;
+    std::vector<DevTri> htc;
+    for (int f = 0; f < m->n_tris; f++) {
+        const int *ind = &m->tri3[3 * f];
+        const int r = m->tri_region[f];
+        if (r < 0 || r >= ntreg) { c.err = "fg_create: triangle region out of range"; return FG_EINVAL; }
+        for (int i = 0; i < 3; i++)
+            if (ind[i] < 0 || ind[i] >= nn) { c.err = "fg_create: triangle node out of range"; return FG_EMESH; }
+        if (!(mag[ind[0]] && mag[ind[1]] && mag[ind[2]]) || tregs[r].suppress_charges) continue;
+        P3 p[3] = {P(ind[0]), P(ind[1]), P(ind[2])};
+        P3 nv = cross3(sub(p[1], p[0]), sub(p[2], p[0]));
+        const double surf = 0.5 * nrm(nv);
+        const double nn_ = nrm(nv);
+        DevTri T;
+        std::memset(&T, 0, sizeof(T));
+        T.n[0] = nv.x / nn_; T.n[1] = nv.y / nn_; T.n[2] = nv.z / nn_;
+        T.dMs = m->tri_dMs[f];
+        for (int g = 0; g < R.npi_f; g++) T.w[g] = 2.0 * surf * R.fp[g];
+        P3 gp[4];
+        for (int g = 0; g < R.npi_f; g++) {
+            gp[g] = {0, 0, 0};
+            for (int i = 0; i < 3; i++) {
+                gp[g].x += R.fa[i][g] * p[i].x; gp[g].y += R.fa[i][g] * p[i].y; gp[g].z += R.fa[i][g] * p[i].z;
+            }
+        }
+        for (int i = 0; i < 3; i++) {
+            double pc[3];
+            tri_potential_coeffs(p[i], p[(i + 1) % 3], p[(i + 2) % 3], surf, pc);
+            for (int k = 0; k < 3; k++) {
+                double b = 0;
+                for (int g = 0; g < R.npi_f; g++) b -= T.w[g] * R.fa[k][g] / nrm(sub(p[i], gp[g]));
+                const int rel = (k - i + 3) % 3;
+                b += 0.5 * pc[rel];
+                T.beta[3 * i + k] = b;
+            }
+        }
+        T.Ks = tregs[r].Ks;
+        for (int k = 0; k < 3; k++) T.uk[k] = tregs[r].uk[k];
+        htri.push_back(make_int4(ind[0], ind[1], ind[2], f));
+        htc.push_back(T);
+    }
+    c.nft = (int)htri.size();
+    c.nsrc = nmt * c.npi_t + c.nft * c.npi_f;
+    std::vector<double> sxyz(3 * (size_t)c.nsrc);
+    {
+        size_t s = 0;
+        for (int k = 0; k < nmt; k++) {
+            const int ind[4] = {htet[k].x, htet[k].y, htet[k].z, htet[k].w};
+            for (int g = 0; g < c.npi_t; g++, s++) {
+                double x = 0, y = 0, z = 0;
+                for (int i = 0; i < 4; i++) {
+                    P3 q = P(ind[i]);
+                    x += R.ta[i][g] * q.x; y += R.ta[i][g] * q.y; z += R.ta[i][g] * q.z;
+                }
+                sxyz[3 * s] = x; sxyz[3 * s + 1] = y; sxyz[3 * s + 2] = z;
+            }
+        }
+        for (int f = 0; f < c.nft; f++) {
+            const int ind[3] = {htri[f].x, htri[f].y, htri[f].z};
+            for (int g = 0; g < c.npi_f; g++, s++) {
+                double x = 0, y = 0, z = 0;
+                for (int i = 0; i < 3; i++) {
+                    P3 q = P(ind[i]);
+                    x += R.fa[i][g] * q.x; y += R.fa[i][g] * q.y; z += R.fa[i][g] * q.z;
+                }
+                sxyz[3 * s] = x; sxyz[3 * s + 1] = y; sxyz[3 * s + 2] = z;
+            }
+        }
+    }
+    std::vector<int> tinc_ptr(nn + 1, 0), tinc(3 * (size_t)c.nft);
+    for (int f = 0; f < c.nft; f++) { tinc_ptr[htri[f].x + 1]++; tinc_ptr[htri[f].y + 1]++; tinc_ptr[htri[f].z + 1]++; }
+    for (int i = 0; i < nn; i++) tinc_ptr[i + 1] += tinc_ptr[i];
+    {
+        std::vector<int> fill(tinc_ptr.begin(), tinc_ptr.end() - 1);
+        for (int f = 0; f < c.nft; f++) {
+            const int ind[3] = {htri[f].x, htri[f].y, htri[f].z};
+            for (int i = 0; i < 3; i++) tinc[fill[ind[i]]++] = 3 * f + i;
+        }
+    }
+    std::vector<int> mnodes;
+    double sumA = 0;
+    for (int i = 0; i < nn; i++)
+        if (mag[i]) { mnodes.push_back(i); sumA += A[i]; }
+    c.n_mag_nodes = (int)mnodes.size();
+    c.mean_A = c.n_mag_nodes ? sumA / c.n_mag_nodes : 1.0;
+
+    // uploads
+    std::vector<double> hxyz(m->xyz, m->xyz + 3 * (size_t)nn);
+    CK(upload(&c.xyz, hxyz));
+    CK(upload(&c.tet, htet));
+    CK(upload(&c.da, da));
+    CK(upload(&c.detJ, detJ));
+    CK(upload(&c.treg, htreg));
+    CK(upload(&c.regs, hreg));
+    c.nreg = nreg;
+    CK(upload(&c.mag, mag));
+    CK(upload(&c.inc_ptr, inc_ptr));
+    CK(upload(&c.inc, inc));
+    CK(upload(&c.Sptr, Sptr));
+    CK(upload(&c.Scol, Scol));
+    CK(upload(&c.Sval, Sval));
+    CK(upload(&c.A, A));
+    {
+        std::vector<float> s32(Sval.begin(), Sval.end()), a32(A.size());
+        const double sc = 1.0 / c.mean_A;
+        for (size_t i = 0; i < A.size(); i++) a32[i] = (float)(A[i] * sc);
+        (void)s32;
+        CK(upload(&c.A32, a32));
+    }
+    CK(upload(&c.tri, htri));
+    CK(upload(&c.tri_c, htc));
+    CK(upload(&c.tinc_ptr, tinc_ptr));
+    CK(upload(&c.tinc, tinc));
+    CK(upload(&c.src_xyz, sxyz));
+    CK(upload(&c.mag_nodes, mnodes));
+    for (int k = 0; k < 2; k++) {
+        CK(dalloc(&c.u[k], 3 * (size_t)nn));
+        CK(dalloc(&c.v[k], 3 * (size_t)nn));
+        CK(dalloc(&c.phi[k], nn));
+        CK(dalloc(&c.phiv[k], nn));
+        CK(cudaMemset(c.u[k], 0, 3 * sizeof(double) * nn));
+        CK(cudaMemset(c.v[k], 0, 3 * sizeof(double) * nn));
+        CK(cudaMemset(c.phi[k], 0, sizeof(double) * nn));
+        CK(cudaMemset(c.phiv[k], 0, sizeof(double) * nn));
+    }
+    CK(dalloc(&c.ep, 3 * (size_t)nn));
+    CK(dalloc(&c.eq, 3 * (size_t)nn));
+    CK(dalloc(&c.slot, 4 * (size_t)nmt));
+    CK(dalloc(&c.Dl, nn));
+    CK(dalloc(&c.rhs, 2 * (size_t)nn));
+    CK(dalloc(&c.x, 2 * (size_t)nn));
+    CK(dalloc(&c.bv, 10 * 2 * (size_t)nn));
+    CK(dalloc(&c.W, 3 * (size_t)nn));
+    c.bicg_grid = bicg_grid_size(c, false);
+    c.partial_len = 8 * std::max(c.bicg_grid, 1024);
+    CK(dalloc(&c.partial, c.partial_len));
+    CK(dalloc(&c.bar, 1));
+    CK(cudaMemset(c.bar, 0, sizeof(GridBar)));
+    CK(dalloc(&c.dres, 1));
+    CK(cudaMallocHost((void **)&c.hres, sizeof(SolveResult)));
+    CK(dalloc(&c.src_q, c.nsrc));
+    CK(dalloc(&c.tri_slot, 3 * (size_t)c.nft));
+    CK(dalloc(&c.pot, nn));
+    CK(cudaMemset(c.pot, 0, sizeof(double) * nn));
+    c.epart_blocks = std::max(1, std::min(4 * c.nsm, (nmt + 255) / 256));
+    CK(dalloc(&c.epart, 7 * (size_t)c.epart_blocks));
+    CK(cudaMallocHost((void **)&c.hepart, 7 * sizeof(double) * c.epart_blocks));
+    int demag = c.opts.demag;
+    if (demag == FG_DEMAG_AUTO) demag = ((double)c.nsrc * c.n_mag_nodes > 4e9) ? FG_DEMAG_FMM : FG_DEMAG_DIRECT;
+    c.opts.demag = demag;
+    if (demag == FG_DEMAG_FMM) {
+        int s = fmm_build(c);
+        if (s != FG_OK) return s;
+    }
+    CK(cudaDeviceSynchronize());
+    return FG_OK;
+}
+
+int fg_create(const fg_mesh *mesh, const fg_region *regions, int n_regions, const fg_tri_region *tri_regions,
+              int n_tri_regions, const fg_opts *opts, fg_ctx **out) {
+    if (!out) return FG_EINVAL;
+    *out = nullptr;
+    fg_ctx *h = new (std::nothrow) fg_ctx();
+    if (!h) return FG_ENOMEM;
+    int s;
+    try {
+        s = create_impl(h, mesh, regions, n_regions, tri_regions, n_tri_regions, opts);
+    } catch (const std::bad_alloc &) {
+        h->c.err = "host allocation failed";
+        s = FG_ENOMEM;
+    } catch (...) {
+        h->c.err = "unexpected exception";
+        s = FG_EINVAL;
+    }
+    if (s != FG_OK) {
+        g_create_error = h->c.err;
+        fg_destroy(h);
+        return s;
+    }
+    *out = h;
+    return FG_OK;
+}
+
+void fg_destroy(fg_ctx *h) {
+    if (!h) return;
+    Ctx &c = h->c;
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    void *ptrs[] = {c.xyz, c.tet, c.da, c.detJ, c.treg, c.regs, c.mag, c.inc_ptr, c.inc, c.Sptr, c.Scol, c.Sval,
+                    c.Sval32, c.A, c.A32, c.tri, c.tri_c, c.tinc_ptr, c.tinc, c.src_xyz, c.mag_nodes, c.u[0], c.u[1],
+                    c.v[0], c.v[1], c.phi[0], c.phi[1], c.phiv[0], c.phiv[1], c.ep, c.eq, c.ep32, c.eq32, c.Dl32,
+                    c.slot, c.Dl, c.rhs, c.x, c.bv, c.W, c.fv, c.partial, c.bar, c.dres, c.src_q, c.tri_slot,
+                    c.pot, c.epart};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    fmm_free(c);
+    if (c.hres) cudaFreeHost(c.hres);
+    if (c.hepart) cudaFreeHost(c.hepart);
+    for (int k = 0; k < 8; k++)
+        if (c.ev[k]) cudaEventDestroy(c.ev[k]);
+    if (c.stream) cudaStreamDestroy(c.stream);
+    delete h;
+}
+
+int fg_set_state(fg_ctx *h, const double *u, const double *v, const double *phi, const double *phiv) {
+    if (!h || !u) return FG_EINVAL;
+    Ctx &c = h->c;
+    const size_t n3 = 3 * sizeof(double) * c.nn, n1 = sizeof(double) * c.nn;
+    for (int k = 0; k < 2; k++) {
+        CK(cudaMemcpyAsync(c.u[k], u, n3, cudaMemcpyHostToDevice, c.stream));
+        if (v) CK(cudaMemcpyAsync(c.v[k], v, n3, cudaMemcpyHostToDevice, c.stream));
+        else CK(cudaMemsetAsync(c.v[k], 0, n3, c.stream));
+        if (phi) CK(cudaMemcpyAsync(c.phi[k], phi, n1, cudaMemcpyHostToDevice, c.stream));
+        else CK(cudaMemsetAsync(c.phi[k], 0, n1, c.stream));
+        if (phiv) CK(cudaMemcpyAsync(c.phiv[k], phiv, n1, cudaMemcpyHostToDevice, c.stream));
+        else CK(cudaMemsetAsync(c.phiv[k], 0, n1, c.stream));
+    }
+    CK(cudaStreamSynchronize(c.stream));
+    return FG_OK;
+}
+
+int fg_get_state(const fg_ctx *hc, int which, double *u, double *v, double *phi, double *phiv) {
+    if (!hc || which < 0 || which > 1) return FG_EINVAL;
+    fg_ctx *h = const_cast<fg_ctx *>(hc);
+    Ctx &c = h->c;
+    const size_t n3 = 3 * sizeof(double) * c.nn, n1 = sizeof(double) * c.nn;
+    if (u) CK(cudaMemcpyAsync(u, c.u[which], n3, cudaMemcpyDeviceToHost, c.stream));
+    if (v) CK(cudaMemcpyAsync(v, c.v[which], n3, cudaMemcpyDeviceToHost, c.stream));
+    if (phi) CK(cudaMemcpyAsync(phi, c.phi[which], n1, cudaMemcpyDeviceToHost, c.stream));
+    if (phiv) CK(cudaMemcpyAsync(phiv, c.phiv[which], n1, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    return FG_OK;
+}
+
+int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double basis_angle, fg_step_report *rep) {
+    if (!h || !Hext || !(dt > 0)) return FG_EINVAL;
+    Ctx &c = h->c;
+    CK(cudaEventRecord(c.ev[0], c.stream));
+    CK(launch_tet(c, dt, Hext));
+    CK(launch_node(c, basis_angle));
+    CK(cudaEventRecord(c.ev[1], c.stream));
+    h->last_c0 = prefactor * FG_THETA * dt * FG_GAMMA0;
+    if (c.opts.precision == FG_PREC_FP32_REFINE) CK(launch_mixed(c, dt, prefactor));
+    else CK(launch_bicg64(c, dt, prefactor));
+    CK(cudaEventRecord(c.ev[2], c.stream));
+    CK(cudaMemcpyAsync(c.hres, c.dres, sizeof(SolveResult), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    cudaEventElapsedTime(&c.ms[0], c.ev[0], c.ev[1]);
+    cudaEventElapsedTime(&c.ms[1], c.ev[1], c.ev[2]);
+    const SolveResult &r = *c.hres;
+    int status = FG_OK;
+    if (r.timeout) status = FG_ETIMEDOUT;
+    else if (r.status == 1) status = FG_SOLVER_ITER_OVERFLOW;
+    else if (r.status == 2 || r.fail) status = FG_SOLVER_CANNOT_CONVERGE;
+    if (rep) {
+        std::memset(rep, 0, sizeof(*rep));
+        rep->status = status;
+        rep->iters = r.nit;
+        rep->vmax = FG_GAMMA0 * std::sqrt(r.v2max);
+        rep->res = r.res;
+        rep->rhsn = r.rhsn;
+        rep->res0 = r.res0;
+        rep->res0_fallback = r.res0;
+    }
+    if (status == FG_ETIMEDOUT) {
+        c.err = "persistent solver: grid barrier timed out";
+        cudaMemsetAsync(c.bar, 0, sizeof(GridBar), c.stream);
+    }
+    return status;
+}
+
+static int demag_into(fg_ctx *h, const double *m, double *phi_out) {
+    Ctx &c = h->c;
+    CK(launch_charges(c, m));
+    if (c.opts.demag == FG_DEMAG_FMM) CK(fmm_eval(c));
+    else CK(launch_p2p_direct(c));
+    CK(launch_phi_final(c, phi_out));
+    return FG_OK;
+}
+
+static int energy_impl(fg_ctx *h, const double Hext[3], double E[4], double avg[3]) {
+    Ctx &c = h->c;
+    CK(launch_energy(c, Hext));
+    CK(cudaMemcpyAsync(c.hepart, c.epart, 7 * sizeof(double) * c.epart_blocks, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    double s[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 7; k++)
+        for (int b = 0; b < c.epart_blocks; b++) s[k] += c.hepart[k * c.epart_blocks + b];
+    if (E)
+        for (int k = 0; k < 4; k++) E[k] = s[k];
+    if (avg)
+        for (int k = 0; k < 3; k++) avg[k] = s[4 + k] / c.total_mag_vol;
+    return FG_OK;
+}
+
+int fg_compute_all(fg_ctx *h, const double Hext[3], double energies[4]) {
+    if (!h || !Hext) return FG_EINVAL;
+    Ctx &c = h->c;
+    CK(cudaEventRecord(c.ev[3], c.stream));
+    int s = demag_into(h, c.u[1], c.phi[1]);
+    if (s) return s;
+    if (!c.opts.first_order) {
+        s = demag_into(h, c.v[1], c.phiv[1]);
+        if (s) return s;
+    }
+    CK(cudaEventRecord(c.ev[4], c.stream));
+    double E[4];
+    s = energy_impl(h, Hext, E, nullptr);
+    if (s) return s;
+    if (energies)
+        for (int k = 0; k < 4; k++) energies[k] = E[k];
+    // Fem::evolution: CURRENT <- NEXT
+    const size_t n3 = 3 * sizeof(double) * c.nn, n1 = sizeof(double) * c.nn;
+    CK(cudaMemcpyAsync(c.u[0], c.u[1], n3, cudaMemcpyDeviceToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.v[0], c.v[1], n3, cudaMemcpyDeviceToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.phi[0], c.phi[1], n1, cudaMemcpyDeviceToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.phiv[0], c.phiv[1], n1, cudaMemcpyDeviceToDevice, c.stream));
+    CK(cudaEventRecord(c.ev[5], c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    cudaEventElapsedTime(&c.ms[2], c.ev[3], c.ev[4]);
+    cudaEventElapsedTime(&c.ms[3], c.ev[4], c.ev[5]);
+    return FG_OK;
+}
+
+int fg_demag(fg_ctx *h, int which, double *out) {
+    if (!h || !out || which < 0 || which > 1) return FG_EINVAL;
+    Ctx &c = h->c;
+    int s = demag_into(h, which ? c.v[1] : c.u[1], c.bv + 9 * 2 * (size_t)c.nn);
+    if (s) return s;
+    // non-magnetic nodes keep 0 in the scratch vector
+    std::vector<double> tmp(c.nn);
+    CK(cudaMemcpyAsync(out, c.bv + 9 * 2 * (size_t)c.nn, sizeof(double) * c.nn, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    for (int i = 0; i < c.nn; i++)
+        if (!c.h_mag[i]) out[i] = 0.0;
+    return FG_OK;
+}
+
+int fg_energy(fg_ctx *h, const double Hext[3], double energies[4]) {
+    if (!h || !Hext || !energies) return FG_EINVAL;
+    return energy_impl(h, Hext, energies, nullptr);
+}
+
+int fg_average(fg_ctx *h, int which, double avg[3]) {
+    if (!h || !avg || which < 0 || which > 1) return FG_EINVAL;
+    Ctx &c = h->c;
+    double zero[3] = {0, 0, 0};
+    if (which == 0) return energy_impl(h, zero, nullptr, avg);
+    // <v>: run the same reduction on the NEXT velocity field
+    std::swap(c.u[1], c.v[1]);
+    int s = energy_impl(h, zero, nullptr, avg);
+    std::swap(c.u[1], c.v[1]);
+    return s;
+}
+
+int fg_debug_system(fg_ctx *h, double *rhs, double *ep, double *eq) {
+    if (!h) return FG_EINVAL;
+    Ctx &c = h->c;
+    if (rhs) CK(cudaMemcpy(rhs, c.rhs, 2 * sizeof(double) * c.nn, cudaMemcpyDeviceToHost));
+    if (ep) CK(cudaMemcpy(ep, c.ep, 3 * sizeof(double) * c.nn, cudaMemcpyDeviceToHost));
+    if (eq) CK(cudaMemcpy(eq, c.eq, 3 * sizeof(double) * c.nn, cudaMemcpyDeviceToHost));
+    return FG_OK;
+}
+
+int fg_debug_apply(fg_ctx *h, const double *x, double *y) {
+    if (!h || !x || !y) return FG_EINVAL;
+    Ctx &c = h->c;
+    const size_t n2 = 2 * (size_t)c.nn;
+    double *dx = c.bv + 9 * n2, *dy = c.bv + 8 * n2;  // scratch: spare vector and Minv slot
+    std::vector<double> keep(n2);
+    CK(cudaMemcpy(keep.data(), dy, n2 * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(dx, x, n2 * sizeof(double), cudaMemcpyHostToDevice));
+    CK(launch_apply(c, h->last_c0, dx, dy));
+    CK(cudaMemcpyAsync(y, dy, n2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    CK(cudaMemcpy(dy, keep.data(), n2 * sizeof(double), cudaMemcpyHostToDevice));
+    return FG_OK;
+}
+
+int fg_timings(const fg_ctx *h, double ms[4]) {
+    if (!h || !ms) return FG_EINVAL;
+    for (int k = 0; k < 4; k++) ms[k] = h->c.ms[k];
+    return FG_OK;
+}
+
+}  // extern "C"

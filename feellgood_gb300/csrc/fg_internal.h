@@ -1,0 +1,186 @@
+// Internal declarations shared by the host orchestration (fg_api.cu) and the device
+// kernels (fg_kernels.cu, fg_fmm.cu, fg_mlp.cu) of the fggpu library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/fggpu.h"
+
+// Physical constants of the reference (src/config.h.in:31-32, :59).
+#define FG_MU0 1.25663706127e-6
+#define FG_GAMMA0 (1.76085962784e11 * FG_MU0)
+#define FG_THETA 0.5
+
+namespace fg {
+
+// Per-region material constants, precomputed once (Tetra::prm, src/tetra.h:86-112).
+struct DevRegion {
+    double A, Ms, alpha, Abis, K, Kbis, K3, K3bis;
+    double uk[3], ex[3], ey[3], ez[3];
+};
+
+// Per-magnetic-triangle constants for charges, self-corrections and energies.
+struct DevTri {
+    double n[3];
+    double dMs;
+    double w[4];     // Gauss weights 2*surf*pds
+    double beta[9];  // corr_i += dMs * sum_k beta[3i+k] * (m_k . n): correctionCharges + potential
+    double Ks;       // surface anisotropy constant
+    double uk[3];
+};
+
+// Result of one solve, written by the persistent BiCG kernel.
+struct SolveResult {
+    int status;     // -1 undefined, 0 converged, 1 overflow, 2 cannot converge
+    int nit;
+    int fail;       // solve() returned true
+    int timeout;
+    double res, rhsn, v2max, res0;
+};
+
+// Grid-wide barrier state of the persistent kernels (bounded wait, no hang).
+struct GridBar {
+    unsigned int count;
+    unsigned int gen;
+    int err;
+    int pad;
+};
+
+// Arguments of the FP64 BiCGSTAB persistent kernel (bicg_dir, src/algebra/bicg.h:163-234).
+struct BicgArgs {
+    int nn;
+    const int *Sptr, *Scol;
+    const double *Sval, *A, *Dl, *ep, *eq;
+    const unsigned char *mag;
+    double c0;
+    const double *b;
+    double *x, *r, *rt, *p, *v, *s, *t, *phat, *shat, *Minv, *W;
+    double *partial;
+    GridBar *bar;
+    SolveResult *res;
+    double tol;
+    int maxiter;
+    // fused node update (Node::make_evol, src/node.h:116-122)
+    double dt;
+    const double *u0;
+    double *u1, *v1;
+};
+
+// Arguments of the FP32 inner Krylov solve with FP64 refinement.
+struct MixedArgs {
+    int nn;
+    const int *Sptr, *Scol;
+    const double *Sval, *A, *Dl, *ep, *eq;
+    const float *Sval32, *A32, *Dl32, *ep32, *eq32;
+    const unsigned char *mag;
+    double c0;
+    const double *b;
+    double *x;        // FP64 solution
+    double *r64;      // FP64 residual
+    double *W64;
+    float *r, *rt, *p, *v, *s, *t, *phat, *shat, *d, *Minv, *W;
+    double *partial;
+    GridBar *bar;
+    SolveResult *res;
+    double tol, inner_tol;
+    int maxiter, refine_max;
+    double dt;
+    const double *u0;
+    double *u1, *v1;
+    double scale;  // 1/mean(A): scales the FP32 system to O(1)
+};
+
+struct Ctx {
+    int device = 0, nsm = 0;
+    cudaStream_t stream = nullptr;
+    fg_opts opts{};
+    std::string err;
+
+    int nn = 0;        // nodes
+    int nmt = 0;       // magnetic tetrahedra
+    int nft = 0;       // magnetic (charge-carrying) triangles
+    int npi_t = 5, npi_f = 4;
+    int nsrc = 0;      // Gauss-point sources
+    int n_tets_total = 0;
+    double total_mag_vol = 0;
+    double mean_A = 0;
+
+    std::vector<unsigned char> h_mag;
+    std::vector<double> h_xyz;
+
+    // device: static mesh data
+    double *xyz = nullptr;
+    int4 *tet = nullptr;        // magnetic tets
+    double *da = nullptr;       // 12 x nmt (structure of arrays)
+    double *detJ = nullptr;     // nmt
+    int *treg = nullptr;        // nmt
+    DevRegion *regs = nullptr;
+    int nreg = 0;
+    unsigned char *mag = nullptr;
+    int *inc_ptr = nullptr, *inc = nullptr;      // node -> tet slots
+    int *Sptr = nullptr, *Scol = nullptr;         // static stiffness pattern (with diagonal)
+    double *Sval = nullptr;
+    float *Sval32 = nullptr;
+    int nnzS = 0;
+    double *A = nullptr;        // lumped mass per node
+    float *A32 = nullptr;
+    int4 *tri = nullptr;        // magnetic triangles: 3 nodes + index
+    DevTri *tri_c = nullptr;
+    int *tinc_ptr = nullptr, *tinc = nullptr;    // node -> tri-vertex slots
+    double *src_xyz = nullptr;  // nsrc x 3, magTet*npi then magTri*npi_f
+    int *mag_nodes = nullptr;   // list of magnetic nodes
+    int n_mag_nodes = 0;
+
+    // device: state (interleaved xyz per node)
+    double *u[2] = {nullptr, nullptr}, *v[2] = {nullptr, nullptr};
+    double *phi[2] = {nullptr, nullptr}, *phiv[2] = {nullptr, nullptr};
+    double *ep = nullptr, *eq = nullptr;
+    float *ep32 = nullptr, *eq32 = nullptr, *Dl32 = nullptr;
+
+    // device: per step
+    double4 *slot = nullptr;    // 4 x nmt: (lumped alpha, BE)
+    double *Dl = nullptr;       // nn
+    double *rhs = nullptr, *x = nullptr;  // 2 nn
+    double *bv = nullptr;       // 10 x 2nn FP64 BiCG vectors
+    double *W = nullptr;        // 3 nn
+    float *fv = nullptr;        // FP32 vectors
+    double *partial = nullptr;  // reductions
+    int partial_len = 0;
+    GridBar *bar = nullptr;
+    SolveResult *dres = nullptr;
+    SolveResult *hres = nullptr;  // pinned
+
+    // device: demag
+    double *src_q = nullptr;
+    double *tri_slot = nullptr;  // 3 x nft corrections
+    double *pot = nullptr;       // nn
+    double *epart = nullptr;     // energy partials
+    double *hepart = nullptr;    // pinned
+    int epart_blocks = 0;
+
+    // persistent-kernel launch shapes
+    int bicg_grid = 0, bicg_block = 256;
+    int mixed_grid = 0;
+
+    // timings
+    cudaEvent_t ev[8];
+    float ms[4] = {0, 0, 0, 0};
+};
+
+// kernels (fg_kernels.cu)
+cudaError_t launch_tet(Ctx &c, double dt, const double Hext[3]);
+cudaError_t launch_node(Ctx &c, double angle);
+cudaError_t launch_bicg64(Ctx &c, double dt, double prefactor);
+cudaError_t launch_mixed(Ctx &c, double dt, double prefactor);
+cudaError_t launch_apply(Ctx &c, double c0, const double *x, double *y);
+cudaError_t launch_charges(Ctx &c, const double *m);
+cudaError_t launch_p2p_direct(Ctx &c);
+cudaError_t launch_phi_final(Ctx &c, double *phi_out);
+cudaError_t launch_energy(Ctx &c, const double Hext[3]);
+int bicg_grid_size(Ctx &c, bool mixed);
+
+}  // namespace fg

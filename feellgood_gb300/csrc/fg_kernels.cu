@@ -1,0 +1,960 @@
+// Device kernels of the per-time-step LLG update (sm_103a).
+//
+// Formulation. In Tet::integrales (src/tetra.cpp:210-307) the 12x12 matrix AE has
+// off-diagonal node couplings only through the exchange block c*vol*(da_i . da_j),
+// identical in the three Cartesian components; the magnetisation cross terms and the
+// lumped damping sit on the node diagonal. Projected with P and the row permutation
+// Perm, the 2x2 block of K coupling nodes i != j is therefore
+//     c0 * S_ij * [eq_i.ep_j  eq_i.eq_j ; ep_i.ep_j  ep_i.eq_j],
+// with S_ij = sum_t Abis_t vol_t (da_i . da_j) a STATIC scalar stiffness matrix and
+// c0 = prefactor * theta * dt * gamma0. The diagonal block of node i is
+//     [A_i  D_i ; D_i  -A_i],  A_i = sum_t sum_g a_i(g) w_g (lumped mass, static),
+//     D_i = c0 S_ii + sum_t sum_g a_i(g) w_g alpha_eff(g).
+// (u x ep = eq and u x eq = -ep for the orthonormal basis of Node::setBasis.) So the
+// per-step element work reduces to four scalars per (tet, vertex): the lumped damping
+// and the 3-vector BE, and K x needs only S, the basis and two diagonals:
+//     (K x)_i = [eq_i ; ep_i] . (c0 sum_j S_ij W_j) + diag block * x_i,
+//     W_j = x_2j ep_j + x_2j+1 eq_j.
+// The RHS is L_i = [eq_i . BE_i ; ep_i . BE_i] (Perm P BE, src/tetra.cpp:306).
+#include <cooperative_groups.h>
+
+#include <cmath>
+#include <cstdio>
+
+#include "fg_internal.h"
+
+namespace fg {
+
+__constant__ double c_ta[4][5];   // tet shape functions at Gauss points (src/tetra.h:50-80)
+__constant__ double c_tpds[5];
+__constant__ double c_fa[3][4];   // triangle rule (src/triangle.h:42-64)
+__constant__ double c_fpds[4];
+
+// ---------------------------------------------------------------------------------
+// small helpers
+
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid-wide barrier for cooperative (co-resident) launches. The wait is bounded: after
+// 2 s without progress it records FG_ETIMEDOUT and returns false; every block then
+// leaves the kernel, so no launch can hang the GPU.
+__device__ bool grid_sync(GridBar *gb) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int *vgen = &gb->gen;
+        volatile int *verr = &gb->err;
+        unsigned int g = *vgen;
+        __threadfence();
+        unsigned int arrived = atomicAdd(&gb->count, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(&gb->count, 0u);
+            __threadfence();
+            atomicAdd(&gb->gen, 1u);
+        } else {
+            unsigned long long t0 = gtimer();
+            while (*vgen == g) {
+                if (*verr) break;
+                if (gtimer() - t0 > 2000000000ull) {
+                    atomicExch(&gb->err, FG_ETIMEDOUT);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int *)&gb->err == 0;
+}
+
+// Deterministic block reduction of NV sums into partial[k*G + blockIdx.x].
+template <int NV>
+__device__ __forceinline__ void block_store(double (&val)[NV], double *partial, int G) {
+    __shared__ double sh[NV][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++)
+        for (int o = 16; o > 0; o >>= 1) val[k] += __shfl_down_sync(0xffffffffu, val[k], o);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) sh[k][warp] = val[k];
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double x = lane < nw ? sh[k][lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) partial[k * G + blockIdx.x] = x;
+        }
+    }
+    __syncthreads();
+}
+
+// Every block sums the G partials of each of the NV slots in the same fixed order.
+template <int NV>
+__device__ __forceinline__ void grid_sum(const double *partial, int G, double (&out)[NV]) {
+    __shared__ double res[NV];
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double x = 0.0;
+            for (int b = lane; b < G; b += 32) x += *(volatile const double *)&partial[k * G + b];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) res[k] = x;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; k++) out[k] = res[k];
+    __syncthreads();
+}
+
+__device__ __forceinline__ double dmax_reduce_block(double v) {
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        v = lane < nw ? sh[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    }
+    __syncthreads();
+    return v;
+}
+
+// ---------------------------------------------------------------------------------
+// Element kernel: one thread per magnetic tetrahedron. Restates the interpolation,
+// calc_alpha_eff, anisotropy and BE parts of Tet::integrales (src/tetra.cpp:47-75,
+// 171-307) and writes per vertex (lumped alpha_eff weight, BE_i) to its slot.
+
+template <int NPI>
+__global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__ tet, const double *__restrict__ da,
+                                               const double *__restrict__ detJ, const int *__restrict__ treg,
+                                               const DevRegion *__restrict__ regs, const double *__restrict__ u0,
+                                               const double *__restrict__ v0, const double *__restrict__ phi0,
+                                               const double *__restrict__ phiv0, double dt, double Hx, double Hy,
+                                               double Hz, double4 *__restrict__ slot) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nmt) return;
+    const int4 I = tet[t];
+    const int ind[4] = {I.x, I.y, I.z, I.w};
+    double d[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) d[i][k] = da[(3 * i + k) * (size_t)nmt + t];
+    const double J = detJ[t];
+    const DevRegion &R = regs[treg[t]];
+    double un[4][3], vn[4][3], ph[4], phv[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const double *pu = u0 + 3 * (size_t)ind[i];
+        const double *pv = v0 + 3 * (size_t)ind[i];
+        un[i][0] = pu[0]; un[i][1] = pu[1]; un[i][2] = pu[2];
+        vn[i][0] = pv[0]; vn[i][1] = pv[1]; vn[i][2] = pv[2];
+        ph[i] = phi0[ind[i]];
+        phv[i] = phiv0[ind[i]];
+    }
+    // constant gradients: dU[k][c] = d u_c / d x_k
+    double dU[3][3], Hd[3], Hv[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            double s = 0.0;
+#pragma unroll
+            for (int i = 0; i < 4; i++) s += d[i][k] * un[i][c];
+            dU[k][c] = s;
+        }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        double h = 0.0, hv = 0.0;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            h -= ph[i] * d[i][c];
+            hv -= phv[i] * d[i][c];
+        }
+        Hd[c] = h;
+        Hv[c] = hv;
+    }
+    const double Abis = R.Abis, alpha = R.alpha;
+    const double s_dt = FG_THETA * dt * FG_GAMMA0;
+    const double gradsq = dU[0][0] * dU[0][0] + dU[0][1] * dU[0][1] + dU[0][2] * dU[0][2] +
+                          dU[1][0] * dU[1][0] + dU[1][1] * dU[1][1] + dU[1][2] * dU[1][2] +
+                          dU[2][0] * dU[2][0] + dU[2][1] * dU[2][1] + dU[2][2] * dU[2][2];
+    const double He[3] = {Hd[0] + Hx, Hd[1] + Hy, Hd[2] + Hz};
+    double w[NPI], aeff[NPI], H[NPI][3];
+    const double reduced_dt = FG_GAMMA0 * dt;
+    const double M = 2. * alpha * 0.1 / reduced_dt;
+#pragma unroll
+    for (int g = 0; g < NPI; g++) {
+        w[g] = J * c_tpds[g];
+        double U[3], V[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            double su = 0.0, sv = 0.0;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                su += c_ta[i][g] * un[i][c];
+                sv += c_ta[i][g] * vn[i][c];
+            }
+            U[c] = su;
+            V[c] = sv;
+        }
+        double uHeff = -Abis * gradsq;
+        double Han[3] = {0.0, 0.0, 0.0};
+        if (R.K != 0.0) {
+            const double sdt = s_dt / FG_GAMMA0;
+            const double kk = R.Kbis * (R.uk[0] * (U[0] + sdt * V[0]) + R.uk[1] * (U[1] + sdt * V[1]) +
+                                        R.uk[2] * (U[2] + sdt * V[2]));
+            Han[0] += kk * R.uk[0];
+            Han[1] += kk * R.uk[1];
+            Han[2] += kk * R.uk[2];
+            const double uu = U[0] * R.uk[0] + U[1] * R.uk[1] + U[2] * R.uk[2];
+            uHeff += R.Kbis * uu * uu;
+        }
+        if (R.K3 != 0.0) {
+            const double sdt = s_dt / FG_GAMMA0;
+            const double *e[3] = {R.ex, R.ey, R.ez};
+            double ku[3], kv[3], uuu[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                ku[a] = e[a][0] * U[0] + e[a][1] * U[1] + e[a][2] * U[2];
+                kv[a] = e[a][0] * V[0] + e[a][1] * V[1] + e[a][2] * V[2];
+                uuu[a] = ku[a] * (1.0 - ku[a] * ku[a]);
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const double tmp = kv[c] * R.ex[c];  // the reference multiplies by ex here
+                const double h = uuu[0] * R.ex[c] + uuu[1] * R.ey[c] + uuu[2] * R.ez[c] +
+                                 sdt * (tmp * (1.0 - 3.0 * ku[c] * ku[c]));
+                Han[c] += -R.K3bis * h;
+            }
+            uHeff += -R.K3bis * (ku[0] * uuu[0] + ku[1] * uuu[1] + ku[2] * uuu[2]);
+        }
+        uHeff += U[0] * He[0] + U[1] * He[1] + U[2] * He[2];
+        // calc_alpha_eff (src/tetra.cpp:47-75)
+        double a;
+        if (uHeff > 0.0)
+            a = (uHeff > M) ? alpha + reduced_dt / 2. * M : alpha + reduced_dt / 2. * uHeff;
+        else
+            a = (uHeff < -M) ? alpha / (1. + reduced_dt / (2. * alpha) * M)
+                             : alpha / (1. - reduced_dt / (2. * alpha) * uHeff);
+        aeff[g] = a;
+        const double kv = s_dt / FG_GAMMA0;
+#pragma unroll
+        for (int c = 0; c < 3; c++) H[g][c] = He[c] + Han[c] + kv * Hv[c];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        double contrib = 0.0;
+#pragma unroll
+        for (int g = 0; g < NPI; g++) contrib += c_ta[i][g] * w[g] * aeff[g];
+        double ex[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) ex[c] = d[i][0] * dU[0][c] + d[i][1] * dU[1][c] + d[i][2] * dU[2][c];
+        double BE[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int g = 0; g < NPI; g++) {
+            const double ai_w = w[g] * c_ta[i][g];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                BE[c] -= w[g] * Abis * ex[c];
+                BE[c] += ai_w * H[g][c];
+            }
+        }
+        slot[4 * (size_t)t + i] = make_double4(contrib, BE[0], BE[1], BE[2]);
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Node kernel: Node::setBasis with the step's angle (src/node.h:73-102), the gather of
+// the per-vertex slots (assembly, src/solver.cpp:11-48), the RHS projection, the Jacobi
+// preconditioner (src/algebra/sparseMat.h:174-183) and the initial guess
+// (src/linear_algebra.cpp:13-24: previous v on the new basis / gamma0).
+
+__global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+                         const double4 *__restrict__ slot, const unsigned char *__restrict__ mag,
+                         const double *__restrict__ A, const double *__restrict__ u0, const double *__restrict__ v1,
+                         double cr, double sr, double *__restrict__ ep, double *__restrict__ eq,
+                         double *__restrict__ Dl, double *__restrict__ rhs, double *__restrict__ x,
+                         double *__restrict__ Minv, double *__restrict__ W) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    const double u[3] = {u0[3 * i], u0[3 * i + 1], u0[3 * i + 2]};
+    double e[3], q[3];
+    if (mag[i]) {
+        const double ax = fabs(u[0]), ay = fabs(u[1]), az = fabs(u[2]);
+        int m = 0;
+        double mv = ax;
+        if (ay < mv) { mv = ay; m = 1; }
+        if (az < mv) { m = 2; }
+        e[0] = (m == 0) - u[m] * u[0];
+        e[1] = (m == 1) - u[m] * u[1];
+        e[2] = (m == 2) - u[m] * u[2];
+        const double n = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+        e[0] /= n; e[1] /= n; e[2] /= n;
+        q[0] = u[1] * e[2] - u[2] * e[1];
+        q[1] = u[2] * e[0] - u[0] * e[2];
+        q[2] = u[0] * e[1] - u[1] * e[0];
+        double ne[3];
+        for (int c = 0; c < 3; c++) {
+            ne[c] = cr * e[c] - sr * q[c];
+            q[c] = sr * e[c] + cr * q[c];
+        }
+        e[0] = ne[0]; e[1] = ne[1]; e[2] = ne[2];
+    } else {
+        e[0] = e[1] = e[2] = q[0] = q[1] = q[2] = 0.0;
+    }
+    ep[3 * i] = e[0]; ep[3 * i + 1] = e[1]; ep[3 * i + 2] = e[2];
+    eq[3 * i] = q[0]; eq[3 * i + 1] = q[1]; eq[3 * i + 2] = q[2];
+    double dl = 0.0, be0 = 0.0, be1 = 0.0, be2 = 0.0;
+    for (int k = inc_ptr[i]; k < inc_ptr[i + 1]; k++) {
+        const double4 s = slot[inc[k]];
+        dl += s.x; be0 += s.y; be1 += s.z; be2 += s.w;
+    }
+    Dl[i] = dl;
+    if (mag[i]) {
+        rhs[2 * i] = q[0] * be0 + q[1] * be1 + q[2] * be2;
+        rhs[2 * i + 1] = e[0] * be0 + e[1] * be1 + e[2] * be2;
+        Minv[2 * i] = 1.0 / A[i];
+        Minv[2 * i + 1] = -1.0 / A[i];
+        const double vv[3] = {v1[3 * i], v1[3 * i + 1], v1[3 * i + 2]};
+        const double xp = (vv[0] * e[0] + vv[1] * e[1] + vv[2] * e[2]) / FG_GAMMA0;
+        const double xq = (vv[0] * q[0] + vv[1] * q[1] + vv[2] * q[2]) / FG_GAMMA0;
+        x[2 * i] = xp;
+        x[2 * i + 1] = xq;
+        W[3 * i] = xp * e[0] + xq * q[0];
+        W[3 * i + 1] = xp * e[1] + xq * q[1];
+        W[3 * i + 2] = xp * e[2] + xq * q[2];
+    } else {
+        rhs[2 * i] = rhs[2 * i + 1] = 0.0;
+        Minv[2 * i] = Minv[2 * i + 1] = 0.0;
+        x[2 * i] = x[2 * i + 1] = 0.0;
+        W[3 * i] = W[3 * i + 1] = W[3 * i + 2] = 0.0;
+    }
+}
+
+// (K x)_i for node i from the tangent vectors W of x (see the header comment).
+__device__ __forceinline__ void apply_row(int i, const int *__restrict__ Sptr, const int *__restrict__ Scol,
+                                          const double *__restrict__ Sval, const double *W,
+                                          const double *__restrict__ ep, const double *__restrict__ eq,
+                                          const double *__restrict__ A, const double *__restrict__ Dl, double c0,
+                                          double xp, double xq, double &y0, double &y1) {
+    // W is written by other blocks of the persistent kernel: read it through L2 (ld.cg).
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    const int k1 = Sptr[i + 1];
+    for (int k = Sptr[i]; k < k1; k++) {
+        const int j = Scol[k];
+        const double s = Sval[k];
+        a0 += s * __ldcg(W + 3 * j);
+        a1 += s * __ldcg(W + 3 * j + 1);
+        a2 += s * __ldcg(W + 3 * j + 2);
+    }
+    const double q0 = eq[3 * i], q1 = eq[3 * i + 1], q2 = eq[3 * i + 2];
+    const double e0 = ep[3 * i], e1 = ep[3 * i + 1], e2 = ep[3 * i + 2];
+    const double ai = A[i], di = Dl[i];
+    y0 = c0 * (q0 * a0 + q1 * a1 + q2 * a2) + ai * xp + di * xq;
+    y1 = c0 * (e0 * a0 + e1 * a1 + e2 * a2) + di * xp - ai * xq;
+}
+
+__device__ __forceinline__ void tangent(int i, const double *ep, const double *eq, double xp, double xq, double *W) {
+    W[3 * i] = xp * ep[3 * i] + xq * eq[3 * i];
+    W[3 * i + 1] = xp * ep[3 * i + 1] + xq * eq[3 * i + 1];
+    W[3 * i + 2] = xp * ep[3 * i + 2] + xq * eq[3 * i + 2];
+}
+
+// ---------------------------------------------------------------------------------
+// Persistent FP64 BiCGSTAB, one cooperative launch per solve. Same iteration, masks
+// and stopping logic as algebra::bicg_dir (src/algebra/bicg.h:163-234) with the
+// iteration monitor of src/algebra/iter.h:119-175; vector phases are separated by
+// bounded grid barriers and the dot products are deterministic two-level reductions.
+// On success the node update of LinAlgebra::solve (src/solver.cpp:74-88) is fused.
+
+__global__ void __launch_bounds__(256) k_bicg64(BicgArgs a) {
+    const int G = gridDim.x;
+    const int nn = a.nn;
+    const int stride = G * blockDim.x;
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    // phase 0: r = b - K x (masked), rt = r, p = r; |b|^2, |r|^2
+    {
+        double bb = 0.0, rr = 0.0;
+        for (int i = i0; i < nn; i += stride) {
+            double y0, y1;
+            const double xp = a.x[2 * i], xq = a.x[2 * i + 1];
+            apply_row(i, a.Sptr, a.Scol, a.Sval, a.W, a.ep, a.eq, a.A, a.Dl, a.c0, xp, xq, y0, y1);
+            const bool m = a.mag[i];
+            const double b0 = m ? a.b[2 * i] : 0.0, b1 = m ? a.b[2 * i + 1] : 0.0;
+            const double r0 = m ? b0 - y0 : 0.0, r1 = m ? b1 - y1 : 0.0;
+            a.r[2 * i] = r0; a.r[2 * i + 1] = r1;
+            a.rt[2 * i] = r0; a.rt[2 * i + 1] = r1;
+            a.p[2 * i] = r0; a.p[2 * i + 1] = r1;
+            bb += b0 * b0 + b1 * b1;
+            rr += r0 * r0 + r1 * r1;
+        }
+        double v2[2] = {bb, rr};
+        block_store<2>(v2, a.partial, G);
+    }
+    if (!grid_sync(a.bar)) goto timeout;
+    {
+        double s2[2];
+        grid_sum<2>(a.partial, G, s2);
+        const double rhsn = sqrt(fabs(s2[0]));
+        const double resmax = a.tol;
+        double rr = s2[1], rtr = s2[1];
+        double rho1 = 0.0, rho2 = 0.0, alpha = 0.0, beta = 0.0, omega = 0.0;
+        int status = -1, nit = 0;
+        double res = sqrt(fabs(rr));
+        const double res0 = res;
+        // iteration::finished
+        auto finished = [&](double nr) {
+            res = fabs(nr);
+            if (isnan(res)) {
+                status = 2;
+                return false;
+            }
+            const bool cv = res <= rhsn * resmax;
+            if (cv) status = 0;
+            return cv;
+        };
+        while (!finished(sqrt(fabs(rr)))) {
+            rho1 = rtr;
+            if (nit > 0) {
+                if (rho2 == 0.0 || omega == 0.0) {
+                    status = 2;
+                    break;
+                }
+                beta = (rho1 / rho2) * (alpha / omega);
+            }
+            // phase 1: p = r + beta (p - omega v); phat = M p; W = tangent(phat)
+            for (int i = i0; i < nn; i += stride) {
+                double p0 = a.p[2 * i], p1 = a.p[2 * i + 1];
+                if (nit > 0) {
+                    p0 = (p0 - omega * a.v[2 * i]) * beta + a.r[2 * i];
+                    p1 = (p1 - omega * a.v[2 * i + 1]) * beta + a.r[2 * i + 1];
+                    a.p[2 * i] = p0; a.p[2 * i + 1] = p1;
+                }
+                const double h0 = a.Minv[2 * i] * p0, h1 = a.Minv[2 * i + 1] * p1;
+                a.phat[2 * i] = h0; a.phat[2 * i + 1] = h1;
+                tangent(i, a.ep, a.eq, h0, h1, a.W);
+            }
+            if (!grid_sync(a.bar)) goto timeout;
+            // phase 2: v = K phat (masked); v . rt
+            {
+                double vr = 0.0;
+                for (int i = i0; i < nn; i += stride) {
+                    double y0, y1;
+                    apply_row(i, a.Sptr, a.Scol, a.Sval, a.W, a.ep, a.eq, a.A, a.Dl, a.c0, a.phat[2 * i],
+                              a.phat[2 * i + 1], y0, y1);
+                    if (!a.mag[i]) y0 = y1 = 0.0;
+                    a.v[2 * i] = y0; a.v[2 * i + 1] = y1;
+                    vr += y0 * a.rt[2 * i] + y1 * a.rt[2 * i + 1];
+                }
+                double v1[1] = {vr};
+                block_store<1>(v1, a.partial, G);
+            }
+            if (!grid_sync(a.bar)) goto timeout;
+            {
+                double s1[1];
+                grid_sum<1>(a.partial, G, s1);
+                alpha = rho1 / s1[0];
+            }
+            // phase 3: s = r - alpha v; shat = M s; |s|^2
+            {
+                double ss = 0.0;
+                for (int i = i0; i < nn; i += stride) {
+                    const double s0 = a.r[2 * i] + (-alpha) * a.v[2 * i];
+                    const double s1 = a.r[2 * i + 1] + (-alpha) * a.v[2 * i + 1];
+                    a.s[2 * i] = s0; a.s[2 * i + 1] = s1;
+                    ss += s0 * s0 + s1 * s1;
+                }
+                double v1[1] = {ss};
+                block_store<1>(v1, a.partial, G);
+            }
+            if (!grid_sync(a.bar)) goto timeout;
+            {
+                double s1[1];
+                grid_sum<1>(a.partial, G, s1);
+                if (finished(sqrt(fabs(s1[0])))) {
+                    for (int i = i0; i < nn; i += stride) {
+                        a.x[2 * i] += alpha * a.phat[2 * i];
+                        a.x[2 * i + 1] += alpha * a.phat[2 * i + 1];
+                    }
+                    break;
+                } else if (status == 1 || status == 2) {
+                    break;
+                }
+            }
+            // phase 4: shat = M s, W = tangent(shat) ... needs a barrier before the SpMV
+            for (int i = i0; i < nn; i += stride) {
+                const double h0 = a.Minv[2 * i] * a.s[2 * i], h1 = a.Minv[2 * i + 1] * a.s[2 * i + 1];
+                a.shat[2 * i] = h0; a.shat[2 * i + 1] = h1;
+                tangent(i, a.ep, a.eq, h0, h1, a.W);
+            }
+            if (!grid_sync(a.bar)) goto timeout;
+            // phase 5: t = K shat (masked); t.s, t.t
+            {
+                double ts = 0.0, tt = 0.0;
+                for (int i = i0; i < nn; i += stride) {
+                    double y0, y1;
+                    apply_row(i, a.Sptr, a.Scol, a.Sval, a.W, a.ep, a.eq, a.A, a.Dl, a.c0, a.shat[2 * i],
+                              a.shat[2 * i + 1], y0, y1);
+                    if (!a.mag[i]) y0 = y1 = 0.0;
+                    a.t[2 * i] = y0; a.t[2 * i + 1] = y1;
+                    ts += y0 * a.s[2 * i] + y1 * a.s[2 * i + 1];
+                    tt += y0 * y0 + y1 * y1;
+                }
+                double v2[2] = {ts, tt};
+                block_store<2>(v2, a.partial, G);
+            }
+            if (!grid_sync(a.bar)) goto timeout;
+            {
+                double s2b[2];
+                grid_sum<2>(a.partial, G, s2b);
+                omega = s2b[0] / s2b[1];
+            }
+            // phase 6: x += alpha phat + omega shat; r = s - omega t; |r|^2, rt.r
+            {
+                double r2 = 0.0, rtr2 = 0.0;
+                for (int i = i0; i < nn; i += stride) {
+#pragma unroll
+                    for (int c = 0; c < 2; c++) {
+                        const int k = 2 * i + c;
+                        double xv = a.x[k] + alpha * a.phat[k];
+                        xv += omega * a.shat[k];
+                        a.x[k] = xv;
+                        const double rv = a.s[k] - omega * a.t[k];
+                        a.r[k] = rv;
+                        r2 += rv * rv;
+                        rtr2 += a.rt[k] * rv;
+                    }
+                }
+                double v2[2] = {r2, rtr2};
+                block_store<2>(v2, a.partial, G);
+            }
+            if (!grid_sync(a.bar)) goto timeout;
+            {
+                double s2c[2];
+                grid_sum<2>(a.partial, G, s2c);
+                rr = s2c[0];
+                rtr = s2c[1];
+            }
+            rho2 = rho1;
+            nit++;
+            if (nit >= a.maxiter) status = 1;
+        }
+        // solve() epilogue: failure test, then the fused node update
+        const bool fail = (status == 1 || status == 2 || res > resmax);
+        if (!grid_sync(a.bar)) goto timeout;
+        double v2max = 0.0;
+        if (!fail) {
+            for (int i = i0; i < nn; i += stride) {
+                if (!a.mag[i]) continue;
+                const double vp = a.x[2 * i], vq = a.x[2 * i + 1];
+                const double v2 = vp * vp + vq * vq;
+                v2max = fmax(v2max, v2);
+                const double pa = vp * FG_GAMMA0, qb = vq * FG_GAMMA0;
+                double nv[3], nu[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    nv[c] = pa * a.ep[3 * i + c] + qb * a.eq[3 * i + c];
+                    nu[c] = a.u0[3 * i + c] + a.dt * nv[c];
+                }
+                const double n = sqrt(nu[0] * nu[0] + nu[1] * nu[1] + nu[2] * nu[2]);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    a.v1[3 * i + c] = nv[c];
+                    a.u1[3 * i + c] = nu[c] / n;
+                }
+            }
+        }
+        v2max = dmax_reduce_block(v2max);
+        if (threadIdx.x == 0) {
+            // v2 >= 0: the bit patterns of non-negative doubles order like the values
+            atomicMax((unsigned long long *)&a.res->v2max, (unsigned long long)__double_as_longlong(v2max));
+            if (blockIdx.x == 0) {
+                a.res->status = status;
+                a.res->nit = nit;
+                a.res->fail = fail ? 1 : 0;
+                a.res->res = res;
+                a.res->rhsn = rhsn;
+                a.res->res0 = res0;
+            }
+        }
+        return;
+    }
+timeout:
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.res->timeout = 1;
+        a.res->fail = 1;
+    }
+}
+
+// y = K x for inspection (two launches: tangent vectors, then rows).
+__global__ void k_tangent64(int nn, const double *x, const double *ep, const double *eq, double *W) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nn) tangent(i, ep, eq, x[2 * i], x[2 * i + 1], W);
+}
+__global__ void k_apply64(int nn, const int *Sptr, const int *Scol, const double *Sval, const double *W,
+                          const double *ep, const double *eq, const double *A, const double *Dl,
+                          const unsigned char *mag, double c0, const double *x, double *y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    double y0, y1;
+    apply_row(i, Sptr, Scol, Sval, W, ep, eq, A, Dl, c0, x[2 * i], x[2 * i + 1], y0, y1);
+    if (!mag[i]) y0 = y1 = 0.0;
+    y[2 * i] = y0;
+    y[2 * i + 1] = y1;
+}
+
+// ---------------------------------------------------------------------------------
+// Demag sources: Tet::charges (src/tetra.cpp:347-359), Tri::charges and the
+// self-corrections of Tri::correctionCharges + Tri::potential (src/triangle.cpp:45-125),
+// in the source order of fmm::calc_charges (src/fmm_demag.h:155-179).
+
+template <int NPI, int NPF>
+__global__ void k_charges(int nmt, int nft, const int4 *__restrict__ tet, const double *__restrict__ da,
+                          const double *__restrict__ detJ, const int *__restrict__ treg,
+                          const DevRegion *__restrict__ regs, const int4 *__restrict__ tri,
+                          const DevTri *__restrict__ tc, const double *__restrict__ m, double *__restrict__ q,
+                          double *__restrict__ tri_slot) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nmt) {
+        const int4 I = tet[k];
+        const int ind[4] = {I.x, I.y, I.z, I.w};
+        double dud = 0.0;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const double *pm = m + 3 * (size_t)ind[i];
+            dud += pm[0] * da[(3 * i) * (size_t)nmt + k] + pm[1] * da[(3 * i + 1) * (size_t)nmt + k] +
+                   pm[2] * da[(3 * i + 2) * (size_t)nmt + k];
+        }
+        const double Ms = regs[treg[k]].Ms, J = detJ[k];
+#pragma unroll
+        for (int g = 0; g < NPI; g++) q[(size_t)k * NPI + g] = -Ms * (J * c_tpds[g]) * dud;
+    } else if (k < nmt + nft) {
+        const int f = k - nmt;
+        const int4 I = tri[f];
+        const int ind[3] = {I.x, I.y, I.z};
+        const DevTri &T = tc[f];
+        double s[3];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const double *pm = m + 3 * (size_t)ind[i];
+            s[i] = pm[0] * T.n[0] + pm[1] * T.n[1] + pm[2] * T.n[2];
+        }
+        double *qq = q + (size_t)nmt * NPI + (size_t)f * NPF;
+#pragma unroll
+        for (int g = 0; g < NPF; g++) {
+            double un = c_fa[0][g] * s[0] + c_fa[1][g] * s[1] + c_fa[2][g] * s[2];
+            qq[g] = (T.dMs != 0.0) ? T.dMs * T.w[g] * un : 0.0;
+        }
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+            tri_slot[3 * (size_t)f + i] =
+                T.dMs * (T.beta[3 * i] * s[0] + T.beta[3 * i + 1] * s[1] + T.beta[3 * i + 2] * s[2]);
+    }
+}
+
+// Exact FP64 direct sum pot_i = sum_s q_s / |x_i - y_s| over all sources, tiled through
+// shared memory (one thread per magnetic node).
+__global__ void __launch_bounds__(256) k_p2p_direct64(int nt, const int *__restrict__ tnode,
+                                                      const double *__restrict__ xyz, int ns,
+                                                      const double *__restrict__ sxyz,
+                                                      const double *__restrict__ q, double *__restrict__ pot) {
+    __shared__ double4 tile[256];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double x = 0, y = 0, z = 0;
+    int node = -1;
+    if (k < nt) {
+        node = tnode[k];
+        x = xyz[3 * node];
+        y = xyz[3 * node + 1];
+        z = xyz[3 * node + 2];
+    }
+    double acc = 0.0;
+    for (int base = 0; base < ns; base += 256) {
+        const int s = base + threadIdx.x;
+        if (s < ns) tile[threadIdx.x] = make_double4(sxyz[3 * s], sxyz[3 * s + 1], sxyz[3 * s + 2], q[s]);
+        else tile[threadIdx.x] = make_double4(0, 0, 0, 0);
+        __syncthreads();
+        const int cnt = min(256, ns - base);
+        for (int j = 0; j < cnt; j++) {
+            const double4 t = tile[j];
+            const double dx = x - t.x, dy = y - t.y, dz = z - t.z;
+            acc += t.w * rsqrt(dx * dx + dy * dy + dz * dz);
+        }
+        __syncthreads();
+    }
+    if (node >= 0) pot[node] = acc;
+}
+
+// phi_i = (pot_i + corr_i) / (4 pi), src/fmm_demag.h:211-223; corr gathered per node.
+__global__ void k_phi_final(int nt, const int *__restrict__ tnode, const int *__restrict__ tinc_ptr,
+                            const int *__restrict__ tinc, const double *__restrict__ tri_slot,
+                            const double *__restrict__ pot, double *__restrict__ phi) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nt) return;
+    const int i = tnode[k];
+    double corr = 0.0;
+    for (int j = tinc_ptr[i]; j < tinc_ptr[i + 1]; j++) corr += tri_slot[tinc[j]];
+    phi[i] = (pot[i] + corr) / (4 * M_PI);
+}
+
+// ---------------------------------------------------------------------------------
+// Energies of the NEXT state and <m> (Fem::energy, src/energy.cpp:5-68; mesh::avg,
+// src/mesh.cpp:89-106). partial layout: [7][G]: E_ex, E_aniso, E_demag, E_zeeman, <m>*V.
+
+template <int NPI, int NPF>
+__global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__restrict__ tet,
+                                                const double *__restrict__ da, const double *__restrict__ detJ,
+                                                const int *__restrict__ treg, const DevRegion *__restrict__ regs,
+                                                const int4 *__restrict__ tri, const DevTri *__restrict__ tc,
+                                                const double *__restrict__ u, const double *__restrict__ phi,
+                                                double Hx, double Hy, double Hz, double *__restrict__ partial) {
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    const int stride = gridDim.x * blockDim.x;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nmt; k += stride) {
+        const int4 I = tet[k];
+        const int ind[4] = {I.x, I.y, I.z, I.w};
+        const DevRegion &R = regs[treg[k]];
+        double un[4][3], ph[4], d[4][3];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                un[i][c] = u[3 * (size_t)ind[i] + c];
+                d[i][c] = da[(3 * i + c) * (size_t)nmt + k];
+            }
+            ph[i] = phi[ind[i]];
+        }
+        double dU[3][3];
+#pragma unroll
+        for (int kk = 0; kk < 3; kk++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                double s = 0.0;
+#pragma unroll
+                for (int i = 0; i < 4; i++) s += d[i][kk] * un[i][c];
+                dU[kk][c] = s;
+            }
+        const double dens = dU[0][0] * dU[0][0] + dU[0][1] * dU[0][1] + dU[0][2] * dU[0][2] + dU[1][0] * dU[1][0] +
+                            dU[1][1] * dU[1][1] + dU[1][2] * dU[1][2] + dU[2][0] * dU[2][0] +
+                            dU[2][1] * dU[2][1] + dU[2][2] * dU[2][2];
+        const double div = dU[0][0] + dU[1][1] + dU[2][2];
+        const double J = detJ[k];
+        double ex = 0.0, dm = 0.0, an = 0.0, ze = 0.0, cub = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
+#pragma unroll
+        for (int g = 0; g < NPI; g++) {
+            const double w = J * c_tpds[g];
+            double U[3], pg = 0.0;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                double s = 0.0;
+#pragma unroll
+                for (int i = 0; i < 4; i++) s += c_ta[i][g] * un[i][c];
+                U[c] = s;
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++) pg += c_ta[i][g] * ph[i];
+            ex += w * dens;
+            dm += w * div * pg;
+            if (R.K != 0.0) {
+                const double a = R.uk[0] * U[0] + R.uk[1] * U[1] + R.uk[2] * U[2];
+                an += w * a * a;
+            }
+            if (R.K3 != 0.0) {
+                const double a0 = U[0] * R.ex[0] + U[1] * R.ex[1] + U[2] * R.ex[2];
+                const double a1 = U[0] * R.ey[0] + U[1] * R.ey[1] + U[2] * R.ey[2];
+                const double a2 = U[0] * R.ez[0] + U[1] * R.ez[1] + U[2] * R.ez[2];
+                cub += w * ((a0 * a1) * (a0 * a1) + (a1 * a2) * (a1 * a2) + (a2 * a0) * (a2 * a0));
+            }
+            ze += w * (U[0] * Hx + U[1] * Hy + U[2] * Hz);
+            mx += w * U[0];
+            my += w * U[1];
+            mz += w * U[2];
+        }
+        acc[0] += R.A * ex;
+        acc[1] += -R.K * an + R.K3 * cub;
+        acc[2] += -0.5 * FG_MU0 * R.Ms * dm;
+        acc[3] += -FG_MU0 * R.Ms * ze;
+        acc[4] += mx;
+        acc[5] += my;
+        acc[6] += mz;
+    }
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nft; f += stride) {
+        const int4 I = tri[f];
+        const int ind[3] = {I.x, I.y, I.z};
+        const DevTri &T = tc[f];
+        double an = 0.0, dm = 0.0;
+#pragma unroll
+        for (int g = 0; g < NPF; g++) {
+            double U[3], pg = 0.0;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                double s = 0.0;
+#pragma unroll
+                for (int i = 0; i < 3; i++) s += c_fa[i][g] * u[3 * (size_t)ind[i] + c];
+                U[c] = s;
+            }
+#pragma unroll
+            for (int i = 0; i < 3; i++) pg += c_fa[i][g] * phi[ind[i]];
+            if (T.Ks != 0.0) {
+                const double a = U[0] * T.uk[0] + U[1] * T.uk[1] + U[2] * T.uk[2];
+                an += T.w[g] * a * a;
+            }
+            dm += (U[0] * T.n[0] + U[1] * T.n[1] + U[2] * T.n[2]) * pg * T.w[g];
+        }
+        acc[1] += -T.Ks * an;
+        acc[2] += 0.5 * FG_MU0 * T.dMs * dm;
+    }
+    block_store<7>(acc, partial, gridDim.x);
+}
+
+// ---------------------------------------------------------------------------------
+// launch wrappers
+
+static inline int nblocks(long n, int b) { return (int)((n + b - 1) / b); }
+
+void upload_rules(bool one_point) {
+    double ta[4][5] = {{0}}, tp[5] = {0}, fa[3][4] = {{0}}, fp[4] = {0};
+    if (one_point) {
+        for (int i = 0; i < 4; i++) ta[i][0] = 0.25;
+        tp[0] = 1.0 / 6.0;
+        for (int i = 0; i < 3; i++) fa[i][0] = 1.0 / 3.0;
+        fp[0] = 0.5;
+    } else {
+        const double A = 1. / 4., B = 1. / 6., C = 1. / 2., D = -2. / 15., E = 3. / 40.;
+        const double u[5] = {A, B, B, B, C}, v[5] = {A, B, B, C, B}, w[5] = {A, B, C, B, B};
+        const double p[5] = {D, E, E, E, E};
+        for (int j = 0; j < 5; j++) {
+            ta[0][j] = 1. - u[j] - v[j] - w[j];
+            ta[1][j] = u[j];
+            ta[2][j] = v[j];
+            ta[3][j] = w[j];
+            tp[j] = p[j];
+        }
+        const double fu[4] = {1 / 3., 1 / 5., 3 / 5., 1 / 5.}, fv[4] = {1 / 3., 1 / 5., 1 / 5., 3 / 5.};
+        const double fpds[4] = {-27 / 96., 25 / 96., 25 / 96., 25 / 96.};
+        for (int j = 0; j < 4; j++) {
+            fa[0][j] = 1. - fu[j] - fv[j];
+            fa[1][j] = fu[j];
+            fa[2][j] = fv[j];
+            fp[j] = fpds[j];
+        }
+    }
+    cudaMemcpyToSymbol(c_ta, ta, sizeof(ta));
+    cudaMemcpyToSymbol(c_tpds, tp, sizeof(tp));
+    cudaMemcpyToSymbol(c_fa, fa, sizeof(fa));
+    cudaMemcpyToSymbol(c_fpds, fp, sizeof(fp));
+}
+
+cudaError_t launch_tet(Ctx &c, double dt, const double H[3]) {
+    if (c.nmt == 0) return cudaSuccess;
+    const int b = 128;
+    if (c.npi_t == 5)
+        k_tet64<5><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0], c.v[0],
+                                                          c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot);
+    else
+        k_tet64<1><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0], c.v[0],
+                                                          c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_node(Ctx &c, double angle) {
+    const double cr = std::cos(angle), sr = std::sin(angle);
+    double *bv = c.bv;
+    const long n2 = 2L * c.nn;
+    double *Minv = bv + 8 * n2;
+    k_node64<<<nblocks(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.inc_ptr, c.inc, c.slot, c.mag, c.A, c.u[0], c.v[1],
+                                                        cr, sr, c.ep, c.eq, c.Dl, c.rhs, c.x, Minv, c.W);
+    return cudaGetLastError();
+}
+
+int bicg_grid_size(Ctx &c, bool mixed) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bicg64, 256, 0);
+    (void)mixed;
+    if (per_sm < 1) per_sm = 1;
+    int g = per_sm * c.nsm;
+    const int need = nblocks(c.nn, 256);
+    if (need < g) g = need;
+    if (g < 1) g = 1;
+    return g;
+}
+
+cudaError_t launch_bicg64(Ctx &c, double dt, double prefactor) {
+    const long n2 = 2L * c.nn;
+    BicgArgs a;
+    a.nn = c.nn;
+    a.Sptr = c.Sptr; a.Scol = c.Scol; a.Sval = c.Sval;
+    a.A = c.A; a.Dl = c.Dl; a.ep = c.ep; a.eq = c.eq; a.mag = c.mag;
+    a.c0 = prefactor * FG_THETA * dt * FG_GAMMA0;
+    a.b = c.rhs; a.x = c.x;
+    double *bv = c.bv;
+    a.r = bv; a.rt = bv + n2; a.p = bv + 2 * n2; a.v = bv + 3 * n2; a.s = bv + 4 * n2; a.t = bv + 5 * n2;
+    a.phat = bv + 6 * n2; a.shat = bv + 7 * n2; a.Minv = bv + 8 * n2; a.W = c.W;
+    a.partial = c.partial; a.bar = c.bar; a.res = c.dres;
+    a.tol = c.opts.tol; a.maxiter = c.opts.max_iter;
+    a.dt = dt; a.u0 = c.u[0]; a.u1 = c.u[1]; a.v1 = c.v[1];
+    cudaError_t e = cudaMemsetAsync(c.bar, 0, sizeof(GridBar), c.stream);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(c.dres, 0, sizeof(SolveResult), c.stream);
+    if (e != cudaSuccess) return e;
+    void *args[] = {&a};
+    return cudaLaunchCooperativeKernel((void *)k_bicg64, dim3(c.bicg_grid), dim3(256), args, 0, c.stream);
+}
+
+cudaError_t launch_apply(Ctx &c, double c0, const double *x, double *y) {
+    k_tangent64<<<nblocks(c.nn, 256), 256, 0, c.stream>>>(c.nn, x, c.ep, c.eq, c.W);
+    k_apply64<<<nblocks(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.Sptr, c.Scol, c.Sval, c.W, c.ep, c.eq, c.A, c.Dl,
+                                                         c.mag, c0, x, y);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_charges(Ctx &c, const double *m) {
+    const int n = c.nmt + c.nft;
+    if (n == 0) return cudaSuccess;
+    if (c.npi_t == 5)
+        k_charges<5, 4><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs,
+                                                                c.tri, c.tri_c, m, c.src_q, c.tri_slot);
+    else
+        k_charges<1, 1><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs,
+                                                                c.tri, c.tri_c, m, c.src_q, c.tri_slot);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_p2p_direct(Ctx &c) {
+    if (c.n_mag_nodes == 0) return cudaSuccess;
+    k_p2p_direct64<<<nblocks(c.n_mag_nodes, 256), 256, 0, c.stream>>>(c.n_mag_nodes, c.mag_nodes, c.xyz, c.nsrc,
+                                                                        c.src_xyz, c.src_q, c.pot);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phi_final(Ctx &c, double *phi_out) {
+    if (c.n_mag_nodes == 0) return cudaSuccess;
+    k_phi_final<<<nblocks(c.n_mag_nodes, 256), 256, 0, c.stream>>>(c.n_mag_nodes, c.mag_nodes, c.tinc_ptr, c.tinc,
+                                                                     c.tri_slot, c.pot, phi_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_energy(Ctx &c, const double H[3]) {
+    const int G = c.epart_blocks;
+    if (c.npi_t == 5)
+        k_energy<5, 4><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
+                                                 c.u[1], c.phi[1], H[0], H[1], H[2], c.epart);
+    else
+        k_energy<1, 1><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
+                                                 c.u[1], c.phi[1], H[0], H[1], H[2], c.epart);
+    return cudaGetLastError();
+}
+
+}  // namespace fg

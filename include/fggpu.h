@@ -1,0 +1,148 @@
+/* fggpu.h — C ABI of the GB300 implementation of FeeLLGood's per-time-step LLG update.
+ *
+ * One context owns all device memory of one mesh (or of a batch of independent meshes)
+ * on one GPU and one CUDA stream. All arrays crossing this ABI are HOST arrays in the
+ * caller's node numbering; indices are 0-based. No call exits the process and no C++
+ * exception crosses the ABI: every entry point returns an FG_* status code.
+ *
+ * Reference interfaces replaced (paths in the FeeLLGood source tree):
+ *   fg_create        Fem/mesh/LinAlgebra/scal_fmm::fmm construction: src/fem.h:46-121,
+ *                    src/linear_algebra.h:40-65 (CSR shape, Dirichlet list),
+ *                    src/fmm_demag.h:64-90 (octree insertion, done once)
+ *   fg_set_state     mesh::init_distrib / mesh::readSol: src/mesh.h:221-277, src/read.cpp:199-249
+ *   fg_step          LinAlgebra::base_projection + prepareElements + solve (+ updateNode):
+ *                    src/time_integration.cpp:193-205, src/linear_algebra.cpp:3-53,
+ *                    src/solver.cpp:6-89
+ *   fg_compute_all   Fem::compute_all (demag of m and of v, energy, evolution): src/fem.h:203-224
+ *   fg_get_state     the node data read by mesh::savesol / Fem::saver: src/save.cpp:164-186
+ *   fg_demag         scal_fmm::fmm::demag for one field: src/fmm_demag.h:184-224
+ *   fg_energy        Fem::energy: src/energy.cpp:5-68
+ */
+#ifndef FGGPU_H
+#define FGGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes; 1 and 2 keep the meaning of algebra::algoStatus (src/algebra/iter.h:24-30) */
+#define FG_OK 0
+#define FG_SOLVER_ITER_OVERFLOW 1
+#define FG_SOLVER_CANNOT_CONVERGE 2
+#define FG_ETIMEDOUT 3 /* a bounded device-side wait gave up; the context stays usable */
+#define FG_EINVAL 4
+#define FG_ECUDA 5
+#define FG_ENOMEM 6
+#define FG_EMESH 7
+#define FG_EIO 8
+
+/* precision of the per-step solve */
+#define FG_PREC_FP64 0        /* plain path: every stage in FP64, as the reference */
+#define FG_PREC_FP32_REFINE 1 /* FP32 Krylov body and FP32 FMM, FP64 refinement residual */
+
+/* demagnetising-potential evaluator */
+#define FG_DEMAG_AUTO 0
+#define FG_DEMAG_DIRECT 1 /* exact tiled direct sum */
+#define FG_DEMAG_FMM 2    /* fast multipole method on a uniform octree */
+
+typedef struct fg_ctx fg_ctx;
+
+/* A set-up mesh: tetrahedra oriented (positive Jacobian, Tet::orientate), boundary and
+ * interface triangles present with their signed dMs (mesh::controlTriangles). xyz in m. */
+typedef struct {
+    int n_nodes, n_tets, n_tris;
+    const double *xyz;         /* n_nodes*3 */
+    const int32_t *tet4;       /* n_tets*4 */
+    const int32_t *tet_region; /* n_tets, index into the region table */
+    const int32_t *tri3;       /* n_tris*3 */
+    const int32_t *tri_region; /* n_tris, index into the triangle region table */
+    const double *tri_dMs;     /* n_tris */
+} fg_mesh;
+
+/* Tetra::prm subset (src/tetra.h:86-112); Ms <= 0 marks a non-magnetic region. */
+typedef struct {
+    double Ae, Ms, K, uk[3], K3, ex[3], ey[3], ez[3], alpha;
+} fg_region;
+
+/* Triangle::prm subset (src/triangle.h:69-101) */
+typedef struct {
+    double Ks, uk[3];
+    int suppress_charges;
+} fg_tri_region;
+
+typedef struct {
+    double tol;           /* BiCG relative tolerance (finite_element_solver.tolerance) */
+    int max_iter;         /* finite_element_solver.max(iter) */
+    int precision;        /* FG_PREC_* */
+    int learned_guess;    /* 1: online-trained per-node MLP proposes the initial guess */
+    int demag;            /* FG_DEMAG_* */
+    int fmm_order;        /* expansion order P of the FMM (0: default) */
+    int fmm_leaf;         /* target number of sources per leaf (0: autotuned) */
+    int one_gauss_point;  /* 1: single Gauss point rules (reference ONE_GAUSS_POINT build) */
+    int first_order;      /* 1: skip the demag of v (reference FIRST_ORDER build) */
+    int refine_max;       /* FP64 refinement sweeps in FG_PREC_FP32_REFINE */
+    double inner_tol;     /* relative tolerance of each FP32 inner solve */
+    int verbose;
+} fg_opts;
+
+typedef struct {
+    int status;         /* FG_OK, FG_SOLVER_ITER_OVERFLOW, FG_SOLVER_CANNOT_CONVERGE, FG_ETIMEDOUT */
+    int iters;          /* BiCG iterations (sum of inner iterations when refining) */
+    int refinements;    /* FP64 refinement sweeps */
+    int guess_accepted; /* 1 if the learned guess was used */
+    double vmax;        /* gamma0 * max sqrt(vp^2 + vq^2), src/solver.cpp:74-88 */
+    double res;         /* final residual norm (absolute) */
+    double rhsn;        /* masked RHS norm */
+    double res0;        /* initial residual norm of the guess used */
+    double res0_fallback; /* initial residual norm of the previous-step guess */
+} fg_step_report;
+
+void fg_opts_default(fg_opts *opts);
+const char *fg_strerror(int status);
+/* Last error message of a context (or of the last failed fg_create when ctx is NULL). */
+const char *fg_last_error(const fg_ctx *ctx);
+
+int fg_create(const fg_mesh *mesh, const fg_region *regions, int n_regions, const fg_tri_region *tri_regions,
+              int n_tri_regions, const fg_opts *opts, fg_ctx **out);
+void fg_destroy(fg_ctx *ctx);
+
+/* Sets CURRENT and NEXT node data. v, phi, phiv may be NULL (zero). */
+int fg_set_state(fg_ctx *ctx, const double *u, const double *v, const double *phi, const double *phiv);
+
+/* One attempt of a time step: tangent basis rotated by basis_angle (radians), element
+ * integrals, solve, and on success the node update into NEXT. Does not commit NEXT. */
+int fg_step(fg_ctx *ctx, double dt, double prefactor, const double Hext[3], double basis_angle,
+            fg_step_report *report);
+
+/* demag(u_NEXT) -> phi, demag(v_NEXT) -> phiv, energies of NEXT, then CURRENT <- NEXT.
+ * energies: exchange, anisotropy, demag, zeeman (src/fem.h:27-36). May be NULL. */
+int fg_compute_all(fg_ctx *ctx, const double Hext[3], double energies[4]);
+
+/* which: 0 = CURRENT, 1 = NEXT. Any output may be NULL. */
+int fg_get_state(const fg_ctx *ctx, int which, double *u, double *v, double *phi, double *phiv);
+
+/* Demag potential of the NEXT field (which: 0 = u, 1 = v) into out[n_nodes], without
+ * touching the state. */
+int fg_demag(fg_ctx *ctx, int which, double *out);
+
+/* Energies of the NEXT state for a constant applied field. */
+int fg_energy(fg_ctx *ctx, const double Hext[3], double energies[4]);
+
+/* <u_d> (which 0) or <v_d> (which 1) of NEXT over the magnetic volume, src/mesh.cpp:89-106. */
+int fg_average(fg_ctx *ctx, int which, double avg[3]);
+
+/* Inspection of the assembled system of the last fg_step, for parity tests:
+ * rhs[2n] and the basis ep/eq[3n]; y = K x for a host x[2n]. */
+int fg_debug_system(fg_ctx *ctx, double *rhs, double *ep, double *eq);
+int fg_debug_apply(fg_ctx *ctx, const double *x, double *y);
+
+/* Device time of the last fg_step / fg_compute_all phases, in ms:
+ * [0] elements, [1] solve, [2] demag, [3] energy+evolution. */
+int fg_timings(const fg_ctx *ctx, double ms[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FGGPU_H */

@@ -171,41 +171,40 @@ def control_triangles(tets, tet_reg, tris, tri_reg, vol_names, surf_names, Ms):
     all_nodes, all_reg, all_surf, all_flip = all_nodes[order], all_reg[order], all_surf[order], all_flip[order]
     change = np.any(all_nodes[1:] != all_nodes[:-1], axis=1)
     starts = np.concatenate([[0], np.nonzero(change)[0] + 1])
-    ends = np.concatenate([starts[1:], [len(all_nodes)]])
-    to_add_nodes, to_add_pairs = [], []
-    for lo, up in zip(starts, ends):
-        id_surf, n_faces, n_surf = -1, 0, 0
-        pair = [-1, -1]
-        for i in range(lo, up):
-            if all_surf[i]:
-                id_surf = int(all_reg[i])
-                n_surf += 1
-            else:
-                n_faces += 1
-                r = int(all_reg[i])
-                if r > pair[0]:
-                    pair[1] = pair[0]
-                    pair[0] = r
-                else:
-                    pair[1] = r
-        if n_surf == 0 and (n_faces == 1 or (n_faces == 2 and pair[0] != pair[1])):
-            to_add_nodes.append(all_nodes[lo])
-            to_add_pairs.append(tuple(pair))
-        if n_surf > 1:
-            raise MeshError(f"Error: bad mesh. {n_surf} instances of the same surface triangle have been found")
-        elif n_faces == 0:
+    gid = np.cumsum(np.concatenate([[0], change.astype(np.int64)]))
+    ng = len(starts)
+    n_surf = np.bincount(gid, weights=all_surf, minlength=ng).astype(np.int64)
+    n_faces = np.bincount(gid, weights=~all_surf, minlength=ng).astype(np.int64)
+    # region pair of the (at most two) tetrahedron faces: (max, min), -1 when absent
+    face_reg = np.where(all_surf, -1, all_reg)
+    rmax = np.full(ng, -1, np.int64)
+    np.maximum.at(rmax, gid, face_reg)
+    big = np.iinfo(np.int64).max
+    rmin = np.full(ng, big, np.int64)
+    np.minimum.at(rmin, gid, np.where(all_surf, big, all_reg))
+    rmin = np.where(n_faces >= 2, rmin, -1)
+    surf_reg = np.full(ng, -1, np.int64)
+    np.maximum.at(surf_reg, gid, np.where(all_surf, all_reg, -1))
+    # assertNoErrInTriangle, in the reference's order of tests, first failing group wins
+    bad = (n_surf > 1) | (n_faces == 0) | (n_faces > 2) | ((n_faces == 2) & (n_surf == 1) & (rmax == rmin))
+    if np.any(bad):
+        g = int(np.nonzero(bad)[0][0])
+        ns_, nf_, sid = int(n_surf[g]), int(n_faces[g]), int(surf_reg[g])
+        if ns_ > 1:
+            raise MeshError(f"Error: bad mesh. {ns_} instances of the same surface triangle have been found")
+        if nf_ == 0:
             raise MeshError(
-                "Error: bad mesh. A triangle which belongs to 1 surface region and no tetrahedron has been found"
-            )
-        elif n_faces > 2:
-            if n_surf == 1:
-                raise MeshError(
-                    f"Error: bad mesh. A triangular face shared by {n_faces} tetrahedrons has been found "
-                    f"in the surface region {id_surf}"
-                )
-            raise MeshError(f"Error: bad mesh. A triangular face shared by {n_faces} tetrahedrons has been found")
-        elif n_faces == 2 and n_surf == 1 and pair[0] == pair[1]:
-            raise MeshError(f"Error: bad mesh. An internal triangle has been found in the surface region {id_surf}")
+                "Error: bad mesh. A triangle which belongs to 1 surface region and no tetrahedron has been found")
+        if nf_ > 2:
+            if ns_ == 1:
+                raise MeshError(f"Error: bad mesh. A triangular face shared by {nf_} tetrahedrons has been found "
+                                f"in the surface region {sid}")
+            raise MeshError(f"Error: bad mesh. A triangular face shared by {nf_} tetrahedrons has been found")
+        raise MeshError(f"Error: bad mesh. An internal triangle has been found in the surface region {sid}")
+    add = (n_surf == 0) & ((n_faces == 1) | ((n_faces == 2) & (rmax != rmin)))
+    to_add_nodes = all_nodes[starts[add]]
+    to_add_pairs = [(int(a), int(b)) for a, b in zip(rmax[add], rmin[add])]
+    # create the missing surface regions and triangles (src/mesh.cpp:155-203)
     surf_names = list(surf_names)
     pair_to_reg = {}
     for pair in to_add_pairs:
@@ -215,7 +214,7 @@ def control_triangles(tets, tet_reg, tris, tri_reg, vol_names, surf_names, Ms):
             base = f"surface({vol_names[pair[0]]})"
         else:
             base = f"interface({vol_names[pair[0]]}, {vol_names[pair[1]]})"
-        i, name = 0, base
+        i = 0
         while True:
             name = base if i == 0 else f"{base}.{i}"
             if name not in surf_names:
@@ -223,20 +222,31 @@ def control_triangles(tets, tet_reg, tris, tri_reg, vol_names, surf_names, Ms):
             i += 1
         surf_names.append(name)
         pair_to_reg[pair] = len(surf_names) - 1
-    new_tris = np.array(to_add_nodes, dtype=np.int64).reshape(-1, 3)
+    new_tris = np.asarray(to_add_nodes, dtype=np.int64).reshape(-1, 3)
     new_reg = np.array([pair_to_reg[p] for p in to_add_pairs], dtype=np.int64)
     tris = np.concatenate([tris, new_tris]) if len(new_tris) else tris
     tri_reg = np.concatenate([np.asarray(tri_reg, dtype=np.int64), new_reg])
-    # dMs (src/mesh.cpp:218-232)
+    # dMs (src/mesh.cpp:218-232): sum of +-Ms over the tetrahedron faces matching each triangle
     ts, tflip = _basic(tris) if len(tris) else (np.zeros((0, 3), np.int64), np.zeros(0, bool))
-    key = {}
-    for i in range(len(all_nodes)):
-        if not all_surf[i]:
-            key.setdefault(tuple(all_nodes[i]), []).append((int(all_reg[i]), bool(all_flip[i])))
+    face = ~all_surf
+    fkeys = all_nodes[face]
+    n = int(max(all_nodes.max(), ts.max() if len(ts) else 0)) + 1
+
+    def key(a):
+        return (a[:, 0].astype(np.int64) * n + a[:, 1]) * n + a[:, 2]
+    fk = key(fkeys)  # already sorted (lexicographic order of the triples)
+    fms = np.asarray(Ms)[all_reg[face]]
+    fflp = all_flip[face]
     dMs = np.zeros(len(tris))
-    for f in range(len(tris)):
-        for reg, flip in key.get(tuple(ts[f]), []):
-            dMs[f] += -Ms[reg] if (tflip[f] ^ flip) else Ms[reg]
+    if len(tris):
+        tk = key(ts)
+        lo = np.searchsorted(fk, tk, side="left")
+        hi = np.searchsorted(fk, tk, side="right")
+        for off in range(int((hi - lo).max()) if len(hi) else 0):
+            sel = lo + off < hi
+            j = lo[sel] + off
+            sgn = np.where(tflip[sel] ^ fflp[j], -1.0, 1.0)
+            dMs[sel] += sgn * fms[j]
     return tris, tri_reg, dMs, surf_names
 
 

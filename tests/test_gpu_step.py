@@ -1,0 +1,138 @@
+"""GPU parity of the plain FP64 path against the FP64 oracle.
+
+Both sides start from the same state (u, v, phi, phiv) and the same basis angle. The
+GPU assembles the factorised system (static stiffness + per-step diagonals); the oracle
+assembles the reference's explicit 2x2-block CSR. Tolerances: basis 1e-14 absolute,
+RHS and K x within 1e-12 relative (same algebra, different rounding order); v within
+rel-L2 1e-9 when both solve to a relative residual of 1e-12; demag potential within
+1e-11 relative (both exact direct sums); energies within 1e-10 relative.
+"""
+import numpy as np
+import pytest
+
+import feellgood_gb300 as fg
+from oracle import fgo
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+DT = 1e-14
+DTMAX = 1e-13
+UK = (0.3, 0.2, 1.0)
+
+
+def _setup(nx=6, ny=5, nz=4, K=0.0, K3=0.0, alpha=0.5, seed=1, tol=1e-12, one_point=False, **opts):
+    m = cases.cuboid(nx, ny, nz)
+    u = cases.perturbed_state(m["xyz"], seed=seed)
+    v = cases.tangent_field(u, seed=seed + 1)
+    o = fgo.Oracle(m, cases.oracle_regions(alpha=alpha, K=K, uk=UK, K3=K3), one_gauss_point=one_point)
+    o.set_solver(tol, 5000)
+    o.set_state(u, v)
+    H = np.array([2e4, -1e4, 3e4])
+    o.compute_all(H)  # phi, phiv of (u, v), then CURRENT <- NEXT
+    st = o.get_state(0)
+    c = fg.Context(m, cases.regions(alpha=alpha, K=K, uk=UK, K3=K3), tol=tol, max_iter=5000,
+                   one_gauss_point=int(one_point), **opts)
+    c.set_state(st["u"], st["v"], st["phi"], st["phiv"])
+    return m, st, H, o, c
+
+
+def _csr_apply(rowptr, col, val, x):
+    y = np.zeros_like(x)
+    for r in range(len(x)):
+        y[r] = val[rowptr[r]:rowptr[r + 1]] @ x[col[rowptr[r]:rowptr[r + 1]]]
+    return y
+
+
+def _rel(a, b):
+    return np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b))
+
+
+@pytest.mark.parametrize("aniso", [(0.0, 0.0), (4e4, 0.0), (0.0, 2e4)])
+@pytest.mark.parametrize("one_point", [False, True])
+def test_rhs_and_operator(aniso, one_point):
+    K, K3 = aniso
+    m, st, H, o, c = _setup(K=K, K3=K3, one_point=one_point)
+    angle = 0.41
+    pref = fgo.prefactor(DT, DTMAX)
+    o.base_projection(angle)
+    o.step(DT, pref, H)
+    rowptr, col, val, rhs_o = o.export_system()
+    rep = c.step(DT, pref, H, angle)
+    assert rep["status"] == fg.FG_OK
+    rhs_g, ep, eq = c.debug_system()
+    ep_o, eq_o = o.basis()
+    assert np.max(np.abs(ep - ep_o)) < 1e-14 and np.max(np.abs(eq - eq_o)) < 1e-14
+    assert _rel(rhs_g, rhs_o) <= 1e-12
+    rng = np.random.default_rng(5)
+    for _ in range(3):
+        x = rng.normal(size=2 * len(m["xyz"]))
+        assert _rel(c.debug_apply(x), _csr_apply(rowptr, col, val, x)) <= 1e-12
+
+
+@pytest.mark.parametrize("nodes", [(6, 5, 4), (10, 10, 3)])
+def test_solve_and_update(nodes):
+    m, st, H, o, c = _setup(*nodes)
+    angle = 1.1 * 0.5
+    pref = fgo.prefactor(DT, DTMAX)
+    o.base_projection(angle)
+    ro = o.step(DT, pref, H)
+    rg = c.step(DT, pref, H, angle)
+    assert not ro["fail"] and rg["status"] == fg.FG_OK
+    so, sg = o.get_state(1), c.get_state(1)
+    assert _rel(sg["v"], so["v"]) <= 1e-9
+    assert np.max(np.abs(sg["u"] - so["u"])) <= 1e-12
+    assert abs(rg["vmax"] - ro["vmax"]) <= 1e-9 * ro["vmax"]
+    assert abs(rg["iters"] - ro["iters"]) <= 2
+    assert abs(rg["rhsn"] - ro["rhsn"]) <= 1e-12 * ro["rhsn"]
+
+
+def test_solver_failure_is_reported():
+    """max(iter)=1 forces ITER_OVERFLOW on both sides (iter.h:119-125); NEXT is not written."""
+    m, st, H, o, c = _setup(tol=1e-14)
+    o.set_solver(1e-14, 1)
+    c2 = fg.Context(m, cases.regions(), tol=1e-14, max_iter=1)
+    c2.set_state(st["u"], st["v"], st["phi"], st["phiv"])
+    pref = fgo.prefactor(DT, DTMAX)
+    o.base_projection(0.2)
+    ro = o.step(DT, pref, H)
+    rg = c2.step(DT, pref, H, 0.2)
+    assert ro["fail"] and ro["status"] == 1
+    assert rg["status"] == fg.FG_SOLVER_ITER_OVERFLOW
+    assert np.array_equal(c2.get_state(1)["u"], st["u"])
+
+
+@pytest.mark.parametrize("one_point", [False, True])
+def test_compute_all(one_point):
+    m, st, H, o, c = _setup(8, 6, 5, K=3e4, one_point=one_point)
+    pref = fgo.prefactor(DT, DTMAX)
+    o.base_projection(0.3)
+    o.step(DT, pref, H)
+    c.step(DT, pref, H, 0.3)
+    Eo = o.compute_all(H)
+    Eg = c.compute_all(H)
+    so, sg = o.get_state(0), c.get_state(0)
+    assert _rel(sg["phi"], so["phi"]) <= 1e-11
+    assert _rel(sg["phiv"], so["phiv"]) <= 1e-11
+    for k in range(4):
+        assert abs(Eg[k] - Eo[k]) <= 1e-10 * np.max(np.abs(Eo)), (k, Eg, Eo)
+    avg = c.average(0)
+    for d in range(3):
+        assert abs(avg[d] - o.avg(0, d)) <= 1e-12
+
+
+def test_bad_mesh_is_rejected():
+    m = cases.cuboid(2, 2, 2)
+    bad = dict(m)
+    t = m["tets"].copy()
+    t[0, 2], t[0, 3] = t[0, 3], t[0, 2]  # negative Jacobian
+    bad["tets"] = t
+    with pytest.raises(fg.FgError) as e:
+        fg.Context(bad, cases.regions())
+    assert e.value.status == 7
+    bad2 = dict(m)
+    t2 = m["tets"].copy()
+    t2[1, 0] = len(m["xyz"]) + 5
+    bad2["tets"] = t2
+    with pytest.raises(fg.FgError):
+        fg.Context(bad2, cases.regions())
