@@ -429,6 +429,7 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     CK(upload(&c.tinc_ptr, tinc_ptr));
     CK(upload(&c.tinc, tinc));
     CK(upload(&c.src_xyz, sxyz));
+    c.h_src_xyz = std::move(sxyz);
     CK(upload(&c.mag_nodes, mnodes));
     for (int k = 0; k < 2; k++) {
         CK(dalloc(&c.u[k], 3 * (size_t)nn));
@@ -506,7 +507,7 @@ void fg_destroy(fg_ctx *h) {
                     c.Sval32, c.A, c.A32, c.tri, c.tri_c, c.tinc_ptr, c.tinc, c.src_xyz, c.mag_nodes, c.u[0], c.u[1],
                     c.v[0], c.v[1], c.phi[0], c.phi[1], c.phiv[0], c.phiv[1], c.ep, c.eq, c.ep32, c.eq32, c.Dl32,
                     c.slot, c.Dl, c.rhs, c.x, c.bv, c.W, c.fv, c.partial, c.bar, c.dres, c.src_q, c.tri_slot,
-                    c.pot, c.epart};
+                    c.pot, c.epart, c.src_dst};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     fmm_free(c);

@@ -1,12 +1,787 @@
-// Fast multipole evaluation of the demagnetising potential (built in a later step).
+// Fast multipole evaluation of the demagnetising potential on the GPU.
+//
+// Replaces the ScalFMM octree + rotation kernel that fmm::demag calls
+// (src/fmm_demag.h:184-224: P2M, M2M, M2L, L2L, L2P of 1/r plus the P2P near field).
+// The potential computed is the same sum pot_i = sum_s q_s / |x_i - y_s| over the
+// Gauss-point sources; only the evaluator differs.
+//
+// Expansions use the scaled solid harmonics
+//   Ups_n^m(r) = (-1)^m r^n P_n^m(cos t) e^{i m p} / (n+m)!        (regular)
+//   The_n^m(r) = (-1)^m (n-m)! P_n^m(cos t) e^{i m p} / r^{n+1}     (irregular)
+// (P_n^m with the Condon-Shortley phase), for which 1/|x-y| = sum Ups_n^m*(y) The_n^m(x),
+// Ups(a+b) = sum_kl Ups_k^l(a) Ups_{n-k}^{m-l}(b) and The(x-y) = sum Ups_k^l*(y) The_{n+k}^{m+l}(x).
+// Multipoles M_n^m = sum q Ups_n^m*(y - z); locals F_n^m with phi = sum F_n^m Ups_n^m*(x - z).
+// For real charges X_n^-m = (-1)^m conj X_n^m, so each expansion is stored as (P+1)^2 reals:
+// Re X_n^0, then Re/Im X_n^m for m = 1..n. Coefficients of a cell of width w are stored
+// scaled (M/w^n, F*w^(n+1)), which makes every translation independent of the level.
+//
+// Every translation (M2L for each of the 316 cell offsets, M2M and L2L for the 8 child
+// octants) is then a fixed real 100x100 matrix, built once on the host. One kernel applies
+// them: a block owns 64 output cells, walks the operator codes, gathers the 64 input
+// expansions of that code and accumulates a register-tiled 100x100 x 100x64 product in a
+// fixed order (deterministic, no atomics).
+//
+// The octree is uniform (all leaves on one level) and built once per mesh on the host
+// (geometry is static). Interaction lists follow the one-cell separation: M2L over the
+// children of the parent's neighbours that are not adjacent, P2P over adjacent leaves.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <unordered_map>
+#include <vector>
+
 #include "fg_internal.h"
 
 namespace fg {
-int fmm_build(Ctx &c) {
-    c.err = "FMM demag is not built in this library version";
-    return FG_EINVAL;
+
+constexpr int FMM_P = 9;
+constexpr int NR = (FMM_P + 1) * (FMM_P + 1);  // reals per expansion (100)
+constexpr int NCODE_M2L = 343;                   // offsets in [-3,3]^3 (27 unused)
+constexpr int TB = 64;                           // output cells per translation block
+
+__host__ __device__ constexpr int cidx(int n, int m) { return n * (n + 1) / 2 + m; }
+// real layout: Re X_n^0 at n*n; Re/Im X_n^m (m>0) at n*n + 2m-1, n*n + 2m
+__host__ __device__ constexpr int ridx(int n, int m, int part) { return m == 0 ? n * n : n * n + 2 * m - 1 + part; }
+
+struct FmmTree {
+    int L = 0, nleaf = 0, ncell = 0, leaf0 = 0;
+    double s0 = 1, c0[3] = {0, 0, 0};
+    std::vector<int> lev_begin;
+    size_t n_m2l = 0, n_p2p_pairs = 0;
+    bool fp32 = false;
+    double eval_ms = 0;
+    // device
+    int *leaf_src = nullptr, *leaf_tgt = nullptr, *tgt_node = nullptr;
+    void *sloc = nullptr;  // 4 x nsrc: leaf-local source coordinates (T), w unused
+    void *tloc = nullptr;  // 4 x ntgt: leaf-local target coordinates (T)
+    int *leaf_ijk = nullptr;  // 3 x nleaf integer leaf coordinates
+    int *m2l_tab = nullptr;   // [ncell][343] source cell or -1
+    int *m2m_tab = nullptr;   // [ncell][8] child per octant or -1
+    int *l2l_tab = nullptr;   // [ncell][8] parent at the own octant, -1 elsewhere
+    int *near_ptr = nullptr, *near_leaf = nullptr;
+    void *M = nullptr, *F = nullptr;
+    void *op_m2l = nullptr, *op_m2m = nullptr, *op_l2l = nullptr;  // [code][NR][NR] (out x in)
+    int *dst_keep = nullptr;
+};
+
+// ---------------------------------------------------------------------------------
+// host: complex operators (checked against a direct sum in the tests)
+
+using cd = std::complex<double>;
+
+static void ups_host(double x, double y, double z, int P, std::vector<cd> &U) {
+    const double r2 = x * x + y * y + z * z;
+    U.assign((P + 1) * (P + 2) / 2, 0.0);
+    U[0] = 1.0;
+    const cd w(x, y);
+    for (int m = 0; m <= P; m++) {
+        if (m > 0) U[cidx(m, m)] = w / (2.0 * m) * U[cidx(m - 1, m - 1)];
+        if (m + 1 <= P) U[cidx(m + 1, m)] = z * U[cidx(m, m)];
+        for (int n = m + 2; n <= P; n++)
+            U[cidx(n, m)] = ((2.0 * n - 1) * z * U[cidx(n - 1, m)] - r2 * U[cidx(n - 2, m)]) / double((n + m) * (n - m));
+    }
 }
-void fmm_free(Ctx &) {}
-cudaError_t fmm_eval(Ctx &) { return cudaErrorNotSupported; }
+static void the_host(double x, double y, double z, int P, std::vector<cd> &T) {
+    const double r2 = x * x + y * y + z * z, ir2 = 1.0 / r2;
+    T.assign((P + 1) * (P + 2) / 2, 0.0);
+    T[0] = 1.0 / std::sqrt(r2);
+    const cd w(x, y);
+    for (int m = 0; m <= P; m++) {
+        if (m > 0) T[cidx(m, m)] = (2.0 * m - 1) * w * ir2 * T[cidx(m - 1, m - 1)];
+        if (m + 1 <= P) T[cidx(m + 1, m)] = (2.0 * m + 1) * z * ir2 * T[cidx(m, m)];
+        for (int n = m + 2; n <= P; n++)
+            T[cidx(n, m)] = ((2.0 * n - 1) * z * T[cidx(n - 1, m)] - double((n + m - 1) * (n - m - 1)) * T[cidx(n - 2, m)]) * ir2;
+    }
+}
+static inline cd getc(const std::vector<cd> &A, int n, int m) {
+    if (m >= 0) return A[cidx(n, m)];
+    const cd v = std::conj(A[cidx(n, -m)]);
+    return (m & 1) ? -v : v;
+}
+static void to_complex(const double *r, int P, std::vector<cd> &A) {
+    A.assign((P + 1) * (P + 2) / 2, 0.0);
+    for (int n = 0; n <= P; n++)
+        for (int m = 0; m <= n; m++) A[cidx(n, m)] = m == 0 ? cd(r[ridx(n, 0, 0)], 0) : cd(r[ridx(n, m, 0)], r[ridx(n, m, 1)]);
+}
+static void to_real(const std::vector<cd> &A, int P, double *r) {
+    for (int n = 0; n <= P; n++)
+        for (int m = 0; m <= n; m++) {
+            r[ridx(n, m, 0)] = A[cidx(n, m)].real();
+            if (m) r[ridx(n, m, 1)] = A[cidx(n, m)].imag();
+        }
+}
+// F_n^m = (-1)^n sum_kl M_k^l The_{n+k}^{m+l}(t), t = target centre - source centre (cell units)
+static void m2l_c(const std::vector<cd> &M, const std::vector<cd> &T, int P, std::vector<cd> &F) {
+    F.assign((P + 1) * (P + 2) / 2, 0.0);
+    for (int n = 0; n <= P; n++)
+        for (int m = 0; m <= n; m++) {
+            cd s = 0;
+            for (int k = 0; k <= P; k++)
+                for (int l = -k; l <= k; l++) s += getc(M, k, l) * getc(T, n + k, m + l);
+            F[cidx(n, m)] = (n & 1) ? -s : s;
+        }
+}
+// parent M from a child: M_n^m = sum conj(Ups_k^l(t)) 2^-(n-k) M_{n-k}^{m-l}, t = child - parent (parent units)
+static void m2m_c(const std::vector<cd> &M, const std::vector<cd> &U, int P, std::vector<cd> &O) {
+    O.assign((P + 1) * (P + 2) / 2, 0.0);
+    for (int n = 0; n <= P; n++)
+        for (int m = 0; m <= n; m++) {
+            cd s = 0;
+            for (int k = 0; k <= n; k++)
+                for (int l = -k; l <= k; l++)
+                    if (std::abs(m - l) <= n - k) s += std::conj(getc(U, k, l)) * std::ldexp(1.0, -(n - k)) * getc(M, n - k, m - l);
+            O[cidx(n, m)] = s;
+        }
+}
+// child F from the parent: F_k^l = sum_{n>=k} F_n^m 2^-(k+1) conj(Ups_{n-k}^{m-l}(t)), t = child - parent
+static void l2l_c(const std::vector<cd> &F, const std::vector<cd> &U, int P, std::vector<cd> &O) {
+    O.assign((P + 1) * (P + 2) / 2, 0.0);
+    for (int k = 0; k <= P; k++)
+        for (int l = 0; l <= k; l++) {
+            cd s = 0;
+            for (int n = k; n <= P; n++)
+                for (int m = -n; m <= n; m++)
+                    if (std::abs(m - l) <= n - k) s += getc(F, n, m) * std::conj(getc(U, n - k, m - l));
+            O[cidx(k, l)] = s * std::ldexp(1.0, -(k + 1));
+        }
+}
+
+// ---------------------------------------------------------------------------------
+// device
+
+template <typename T, typename Fn>
+__device__ __forceinline__ void ups_cols(T x, T y, T z, Fn &&f) {
+    constexpr int P = FMM_P;
+    const T r2 = x * x + y * y + z * z;
+    T dre = 1, dim = 0;
+#pragma unroll
+    for (int m = 0; m <= P; m++) {
+        if (m > 0) {
+            const T s = T(1) / T(2 * m);
+            const T nre = (x * dre - y * dim) * s, nim = (x * dim + y * dre) * s;
+            dre = nre;
+            dim = nim;
+        }
+        f(m, m, dre, dim);
+        T p2re = dre, p2im = dim;
+        T p1re = z * dre, p1im = z * dim;
+        if (m + 1 <= P) f(m + 1, m, p1re, p1im);
+#pragma unroll
+        for (int n = m + 2; n <= P; n++) {
+            const T a = T(2 * n - 1), b = T(1) / T((n + m) * (n - m));
+            const T cre = (a * z * p1re - r2 * p2re) * b, cim = (a * z * p1im - r2 * p2im) * b;
+            f(n, m, cre, cim);
+            p2re = p1re; p2im = p1im;
+            p1re = cre; p1im = cim;
+        }
+    }
+}
+
+template <typename T> __device__ __forceinline__ T rsqrt_t(T x);
+template <> __device__ __forceinline__ float rsqrt_t<float>(float x) { return rsqrtf(x); }
+template <> __device__ __forceinline__ double rsqrt_t<double>(double x) { return rsqrt(x); }
+
+// P2M: one block (64 threads) per leaf; each thread forms q*conj(Ups) of one source into a
+// shared tile, each coefficient is summed over the tile in a fixed order.
+template <typename T>
+__global__ void __launch_bounds__(64) k_p2m(int nleaf, const int *__restrict__ leaf_src, const T *__restrict__ sloc,
+                                            const double *__restrict__ q, int leaf0, T *__restrict__ M) {
+    constexpr int LD = 65;
+    extern __shared__ unsigned char smem_raw[];
+    T *tile = reinterpret_cast<T *>(smem_raw);  // [NR][LD]
+    const int leaf = blockIdx.x, tid = threadIdx.x;
+    const int s0 = leaf_src[leaf], s1 = leaf_src[leaf + 1];
+    T acc[2] = {0, 0};
+    for (int base = s0; base < s1; base += 64) {
+        const int s = base + tid;
+        if (s < s1) {
+            const T x = sloc[4 * (size_t)s], y = sloc[4 * (size_t)s + 1], z = sloc[4 * (size_t)s + 2];
+            const T qq = T(q[s]);
+            ups_cols<T>(x, y, z, [&](int n, int m, T re, T im) {
+                tile[ridx(n, m, 0) * LD + tid] = qq * re;
+                if (m) tile[ridx(n, m, 1) * LD + tid] = -qq * im;
+            });
+        } else {
+#pragma unroll
+            for (int j = 0; j < NR; j++) tile[j * LD + tid] = 0;
+        }
+        __syncthreads();
+        const int cnt = min(64, s1 - base);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int j = tid + 64 * h;
+            if (j < NR)
+                for (int k = 0; k < cnt; k++) acc[h] += tile[j * LD + k];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int j = tid + 64 * h;
+        if (j < NR) M[(size_t)(leaf0 + leaf) * NR + j] = acc[h];
+    }
+}
+
+// Batched translation out[c] (+)= sum_code Op[code] in[tab[c][code]] for TB=64 output cells
+// per block. 160 threads: 10 row groups (10 rows each) x 16 column groups (4 cells each).
+template <typename T>
+__global__ void __launch_bounds__(160) k_translate(int n_out, int out0, int ncode, const int *__restrict__ tab,
+                                                   const T *__restrict__ ops, const T *in, T *out,
+                                                   int accumulate) {
+    // in and out may be the same array (M2M, L2L): the cells read and written are disjoint.
+    constexpr int RT = 10, CT = 4, BLD = TB + 4;
+    extern __shared__ unsigned char smem_raw[];
+    T *AT = reinterpret_cast<T *>(smem_raw);  // [NR][NR]: AT[k*NR + row] = Op[row][k]
+    T *Bs = AT + NR * NR;                      // [NR][BLD]
+    __shared__ int srcs[TB];
+    const int tid = threadIdx.x, rg = tid / 16, cg = tid % 16;
+    const int c_begin = blockIdx.x * TB;
+    T acc[RT][CT];
+#pragma unroll
+    for (int i = 0; i < RT; i++)
+#pragma unroll
+        for (int j = 0; j < CT; j++) acc[i][j] = 0;
+    for (int code = 0; code < ncode; code++) {
+        int s = -1;
+        if (tid < TB && c_begin + tid < n_out) s = tab[(size_t)(out0 + c_begin + tid) * ncode + code];
+        if (tid < TB) srcs[tid] = s;
+        if (!__syncthreads_or(s >= 0)) continue;
+        for (int e = tid; e < NR * NR; e += blockDim.x) {
+            const int row = e / NR, k = e % NR;
+            AT[k * NR + row] = ops[(size_t)code * NR * NR + e];
+        }
+        for (int e = tid; e < NR * TB; e += blockDim.x) {
+            const int col = e / NR, k = e % NR;
+            const int sc = srcs[col];
+            Bs[k * BLD + col] = sc >= 0 ? in[(size_t)sc * NR + k] : T(0);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int k = 0; k < NR; k++) {
+            T a[RT], b[CT];
+#pragma unroll
+            for (int i = 0; i < RT; i++) a[i] = AT[k * NR + rg * RT + i];
+#pragma unroll
+            for (int j = 0; j < CT; j++) b[j] = Bs[k * BLD + cg * CT + j];
+#pragma unroll
+            for (int i = 0; i < RT; i++)
+#pragma unroll
+                for (int j = 0; j < CT; j++) acc[i][j] += a[i] * b[j];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < CT; j++) {
+        const int c = c_begin + cg * CT + j;
+        if (c >= n_out) continue;
+        T *o = out + (size_t)(out0 + c) * NR + rg * RT;
+#pragma unroll
+        for (int i = 0; i < RT; i++) o[i] = accumulate ? o[i] + acc[i][j] : acc[i][j];
+    }
+}
+
+// L2P + P2P: one warp per leaf. Sources of the adjacent leaves are spread over the lanes,
+// up to 8 targets of the leaf are held in registers; coordinates are leaf-local (leaf
+// units), so FP32 keeps the relative precision of close pairs. Per-lane FP32 partial
+// sums are reduced in a fixed order and accumulated in FP64.
+template <typename T>
+__global__ void __launch_bounds__(128) k_l2p_p2p(int nleaf, const int *__restrict__ leaf_src,
+                                                 const int *__restrict__ leaf_tgt, const int *__restrict__ tgt_node,
+                                                 const T *__restrict__ tloc, const T *__restrict__ sloc,
+                                                 const double *__restrict__ q, const int *__restrict__ leaf_ijk,
+                                                 int leaf0, double scale, const int *__restrict__ near_ptr,
+                                                 const int *__restrict__ near_leaf, const T *__restrict__ F,
+                                                 double *__restrict__ pot) {
+    constexpr int NT = 8;
+    const int lane = threadIdx.x & 31;
+    const int leaf = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (leaf >= nleaf) return;
+    const int t0 = leaf_tgt[leaf], t1 = leaf_tgt[leaf + 1];
+    if (t0 == t1) return;
+    const int li = leaf_ijk[3 * leaf], lj = leaf_ijk[3 * leaf + 1], lk = leaf_ijk[3 * leaf + 2];
+    const T *Fl = F + (size_t)(leaf0 + leaf) * NR;
+    for (int tb = t0; tb < t1; tb += NT) {
+        const int nt = min(NT, t1 - tb);
+        T tx[NT], ty[NT], tz[NT];
+        double near[NT];
+#pragma unroll
+        for (int j = 0; j < NT; j++) {
+            const int ti = tb + (j < nt ? j : 0);
+            tx[j] = tloc[4 * (size_t)ti];
+            ty[j] = tloc[4 * (size_t)ti + 1];
+            tz[j] = tloc[4 * (size_t)ti + 2];
+            near[j] = 0.0;
+        }
+        for (int e = near_ptr[leaf]; e < near_ptr[leaf + 1]; e++) {
+            const int nl = near_leaf[e];
+            const T ox = T(leaf_ijk[3 * nl] - li), oy = T(leaf_ijk[3 * nl + 1] - lj), oz = T(leaf_ijk[3 * nl + 2] - lk);
+            const int s0 = leaf_src[nl], s1 = leaf_src[nl + 1];
+            T acc[NT];
+#pragma unroll
+            for (int j = 0; j < NT; j++) acc[j] = 0;
+            for (int s = s0 + lane; s < s1; s += 32) {
+                const T sx = sloc[4 * (size_t)s] + ox, sy = sloc[4 * (size_t)s + 1] + oy,
+                        sz = sloc[4 * (size_t)s + 2] + oz;
+                const T qq = T(q[s]);
+#pragma unroll
+                for (int j = 0; j < NT; j++) {
+                    const T dx = tx[j] - sx, dy = ty[j] - sy, dz = tz[j] - sz;
+                    acc[j] += qq * rsqrt_t<T>(dx * dx + dy * dy + dz * dz);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < NT; j++) near[j] += double(acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < NT; j++)
+            for (int o = 16; o > 0; o >>= 1) near[j] += __shfl_xor_sync(0xffffffffu, near[j], o);
+        // L2P: lane j evaluates target j
+        if (lane < nt) {
+            T x = 0, y = 0, z = 0;
+            double nr = 0;
+#pragma unroll
+            for (int j = 0; j < NT; j++)
+                if (j == lane) { x = tx[j]; y = ty[j]; z = tz[j]; nr = near[j]; }
+            T far = 0;
+            ups_cols<T>(x, y, z, [&](int n, int m, T re, T im) {
+                if (m == 0) far += Fl[ridx(n, 0, 0)] * re;
+                else far += T(2) * (Fl[ridx(n, m, 0)] * re + Fl[ridx(n, m, 1)] * im);
+            });
+            pot[tgt_node[tb + lane]] = (double(far) + nr) * scale;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// host: tree construction
+
+static inline uint64_t spread3(uint64_t v) {
+    v &= 0x1fffff;
+    v = (v | v << 32) & 0x1f00000000ffffull;
+    v = (v | v << 16) & 0x1f0000ff0000ffull;
+    v = (v | v << 8) & 0x100f00f00f00f00full;
+    v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+    v = (v | v << 2) & 0x1249249249249249ull;
+    return v;
+}
+static inline uint64_t morton(int x, int y, int z) { return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2); }
+static void decode(uint64_t k, int *ijk) {
+    ijk[0] = ijk[1] = ijk[2] = 0;
+    for (int b = 0; b < 21; b++) {
+        ijk[0] |= (int)((k >> (3 * b)) & 1) << b;
+        ijk[1] |= (int)((k >> (3 * b + 1)) & 1) << b;
+        ijk[2] |= (int)((k >> (3 * b + 2)) & 1) << b;
+    }
+}
+
+template <typename T>
+static cudaError_t up(T **p, const std::vector<T> &h) {
+    cudaError_t e = cudaMalloc((void **)p, std::max<size_t>(1, h.size()) * sizeof(T));
+    if (e != cudaSuccess) return e;
+    if (!h.empty()) e = cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return e;
+}
+template <typename T>
+static cudaError_t up_as(void **p, const std::vector<double> &h, bool fp32) {
+    if (fp32) {
+        std::vector<float> f(h.begin(), h.end());
+        return up((float **)p, f);
+    }
+    return up((double **)p, h);
+}
+
+#define FCK(call)                                                                   \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            c.err = std::string("fmm: ") + #call + ": " + cudaGetErrorString(e_);   \
+            return FG_ECUDA;                                                        \
+        }                                                                           \
+    } while (0)
+
+// Operator matrices (level independent), [code][out][in], in the real layout.
+struct FmmOps {
+    std::vector<double> m2l, m2m, l2l;
+};
+static const FmmOps &fmm_ops() {
+    static FmmOps ops;
+    if (!ops.m2l.empty()) return ops;
+    const int P = FMM_P;
+    ops.m2l.assign((size_t)NCODE_M2L * NR * NR, 0.0);
+    ops.m2m.assign((size_t)8 * NR * NR, 0.0);
+    ops.l2l.assign((size_t)8 * NR * NR, 0.0);
+    std::vector<cd> T, U, in, out;
+    std::vector<double> e(NR), r(NR);
+    for (int dx = -3; dx <= 3; dx++)
+        for (int dy = -3; dy <= 3; dy++)
+            for (int dz = -3; dz <= 3; dz++) {
+                if (std::abs(dx) <= 1 && std::abs(dy) <= 1 && std::abs(dz) <= 1) continue;
+                const int code = (dx + 3) * 49 + (dy + 3) * 7 + (dz + 3);
+                the_host(dx, dy, dz, 2 * P, T);
+                for (int j = 0; j < NR; j++) {
+                    std::fill(e.begin(), e.end(), 0.0);
+                    e[j] = 1.0;
+                    to_complex(e.data(), P, in);
+                    m2l_c(in, T, P, out);
+                    to_real(out, P, r.data());
+                    for (int i = 0; i < NR; i++) ops.m2l[(size_t)code * NR * NR + (size_t)i * NR + j] = r[i];
+                }
+            }
+    for (int oc = 0; oc < 8; oc++) {
+        ups_host((oc & 1) ? 0.25 : -0.25, (oc & 2) ? 0.25 : -0.25, (oc & 4) ? 0.25 : -0.25, P, U);
+        for (int j = 0; j < NR; j++) {
+            std::fill(e.begin(), e.end(), 0.0);
+            e[j] = 1.0;
+            to_complex(e.data(), P, in);
+            m2m_c(in, U, P, out);
+            to_real(out, P, r.data());
+            for (int i = 0; i < NR; i++) ops.m2m[(size_t)oc * NR * NR + (size_t)i * NR + j] = r[i];
+            l2l_c(in, U, P, out);
+            to_real(out, P, r.data());
+            for (int i = 0; i < NR; i++) ops.l2l[(size_t)oc * NR * NR + (size_t)i * NR + j] = r[i];
+        }
+    }
+    return ops;
+}
+
+void fmm_free(Ctx &c);
+static int fmm_build_level(Ctx &c, int L);
+template <typename T>
+static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t);
+
+int fmm_build(Ctx &c) {
+    const bool fp32 = (c.opts.precision == FG_PREC_FP32_REFINE);
+    if (c.opts.fmm_order != 0 && c.opts.fmm_order != FMM_P) {
+        c.err = "fmm: only expansion order P=9 is built";
+        return FG_EINVAL;
+    }
+    const int ns = c.nsrc;
+    // root cube over sources and targets
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int s = 0; s < ns; s++)
+        for (int d = 0; d < 3; d++) {
+            lo[d] = std::min(lo[d], c.h_src_xyz[3 * s + d]);
+            hi[d] = std::max(hi[d], c.h_src_xyz[3 * s + d]);
+        }
+    for (int i = 0; i < c.nn; i++)
+        if (c.h_mag[i])
+            for (int d = 0; d < 3; d++) {
+                lo[d] = std::min(lo[d], c.h_xyz[3 * i + d]);
+                hi[d] = std::max(hi[d], c.h_xyz[3 * i + d]);
+            }
+    const double side = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2])) * (1.0 + 1e-9);
+    const double cen[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2])};
+    // candidate depths: mean sources per occupied leaf near the requested size (autotuned
+    // over a neighbourhood when fmm_leaf is 0)
+    const int n10 = 1 << 10;
+    std::vector<uint64_t> keys(ns);
+    for (int s = 0; s < ns; s++) {
+        int ijk[3];
+        for (int d = 0; d < 3; d++)
+            ijk[d] = std::min(n10 - 1, std::max(0, (int)(((c.h_src_xyz[3 * s + d] - cen[d]) / side + 0.5) * n10)));
+        keys[s] = morton(ijk[0], ijk[1], ijk[2]);
+    }
+    std::sort(keys.begin(), keys.end());
+    std::vector<double> mean(11, 0.0);
+    for (int l = 2; l <= 10; l++) {
+        const int sh = 3 * (10 - l);
+        size_t occ = 0;
+        uint64_t prev = ~0ull;
+        for (uint64_t k : keys)
+            if ((k >> sh) != prev) { occ++; prev = k >> sh; }
+        mean[l] = ns / std::max<double>(1.0, (double)occ);
+    }
+    keys.clear();
+    keys.shrink_to_fit();
+    auto closest = [&](double target) {
+        int best = 2;
+        double bd = 1e300;
+        for (int l = 2; l <= 10; l++) {
+            const double d = std::fabs(std::log(mean[l] / target));
+            if (d < bd) { bd = d; best = l; }
+        }
+        return best;
+    };
+    std::vector<int> cands;
+    if (c.opts.fmm_leaf > 0) cands.push_back(closest(c.opts.fmm_leaf));
+    else {
+        const int l0 = closest(fp32 ? 400.0 : 300.0);
+        for (int l = std::max(2, l0 - 1); l <= std::min(10, l0 + 1); l++) cands.push_back(l);
+    }
+    cudaMemsetAsync(c.src_q, 0, sizeof(double) * std::max(1, c.nsrc), c.stream);
+    int bestL = cands[0];
+    double bestms = 1e300;
+    for (size_t k = 0; k < cands.size(); k++) {
+        fmm_free(c);
+        FmmTree *t = new FmmTree();
+        c.fmm = t;
+        t->fp32 = fp32;
+        t->s0 = side;
+        for (int d = 0; d < 3; d++) t->c0[d] = cen[d];
+        int s = fmm_build_level(c, cands[k]);
+        if (s != FG_OK) return s;
+        if (cands.size() == 1) return FG_OK;
+        // autotune: time two evaluations with the current charges (values do not matter)
+        cudaEvent_t a, b;
+        FCK(cudaEventCreate(&a));
+        FCK(cudaEventCreate(&b));
+        FCK(fp32 ? fmm_eval_t<float>(c, *t) : fmm_eval_t<double>(c, *t));
+        FCK(cudaEventRecord(a, c.stream));
+        for (int r = 0; r < 2; r++) FCK(fp32 ? fmm_eval_t<float>(c, *t) : fmm_eval_t<double>(c, *t));
+        FCK(cudaEventRecord(b, c.stream));
+        FCK(cudaEventSynchronize(b));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        if (c.opts.verbose) fprintf(stderr, "fmm autotune: L=%d %.3f ms/eval\n", cands[k], ms / 2);
+        if (ms < bestms) { bestms = ms; bestL = cands[k]; }
+    }
+    fmm_free(c);
+    FmmTree *t = new FmmTree();
+    c.fmm = t;
+    t->fp32 = fp32;
+    t->s0 = side;
+    for (int d = 0; d < 3; d++) t->c0[d] = cen[d];
+    return fmm_build_level(c, bestL);
+}
+
+static int fmm_build_level(Ctx &c, int L) {
+    FmmTree *t = static_cast<FmmTree *>(c.fmm);
+    const bool fp32 = t->fp32;
+    t->L = L;
+    const int ns = c.nsrc;
+    std::vector<int> mnodes;
+    for (int i = 0; i < c.nn; i++)
+        if (c.h_mag[i]) mnodes.push_back(i);
+    const int nt = (int)mnodes.size();
+    const int nside = 1 << L;
+    auto cell_of = [&](const double *p, int *ijk) {
+        for (int d = 0; d < 3; d++)
+            ijk[d] = std::min(nside - 1, std::max(0, (int)(((p[d] - t->c0[d]) / t->s0 + 0.5) * nside)));
+        return morton(ijk[0], ijk[1], ijk[2]);
+    };
+    std::vector<std::pair<uint64_t, int>> sk(ns), tk(nt);
+    int ijk[3];
+    for (int s = 0; s < ns; s++) sk[s] = {cell_of(&c.h_src_xyz[3 * s], ijk), s};
+    for (int k = 0; k < nt; k++) tk[k] = {cell_of(&c.h_xyz[3 * mnodes[k]], ijk), mnodes[k]};
+    std::sort(sk.begin(), sk.end());
+    std::sort(tk.begin(), tk.end());
+    std::vector<uint64_t> lk;
+    {
+        std::vector<uint64_t> a, b;
+        for (auto &p : sk) if (a.empty() || a.back() != p.first) a.push_back(p.first);
+        for (auto &p : tk) if (b.empty() || b.back() != p.first) b.push_back(p.first);
+        std::set_union(a.begin(), a.end(), b.begin(), b.end(), std::back_inserter(lk));
+    }
+    const int nleaf = (int)lk.size();
+    t->nleaf = nleaf;
+    std::vector<int> leaf_src(nleaf + 1, 0), leaf_tgt(nleaf + 1, 0), leaf_ijk(3 * (size_t)nleaf);
+    {
+        size_t a = 0, b = 0;
+        for (int l = 0; l < nleaf; l++) {
+            leaf_src[l] = (int)a;
+            while (a < sk.size() && sk[a].first == lk[l]) a++;
+            leaf_tgt[l] = (int)b;
+            while (b < tk.size() && tk[b].first == lk[l]) b++;
+            decode(lk[l], &leaf_ijk[3 * (size_t)l]);
+        }
+        leaf_src[nleaf] = (int)a;
+        leaf_tgt[nleaf] = (int)b;
+    }
+    // leaf-local coordinates in leaf units
+    const double w = t->s0 / nside;
+    auto local = [&](const double *p, const int *lijk, double *o) {
+        for (int d = 0; d < 3; d++) {
+            const double cc = t->c0[d] - 0.5 * t->s0 + (lijk[d] + 0.5) * w;
+            o[d] = (p[d] - cc) / w;
+        }
+    };
+    std::vector<int> src_dst(ns), tgt_node(nt);
+    std::vector<double> sloc(4 * (size_t)ns, 0.0), tloc(4 * (size_t)nt, 0.0);
+    for (int l = 0; l < nleaf; l++) {
+        for (int k = leaf_src[l]; k < leaf_src[l + 1]; k++) {
+            src_dst[sk[k].second] = k;
+            local(&c.h_src_xyz[3 * (size_t)sk[k].second], &leaf_ijk[3 * (size_t)l], &sloc[4 * (size_t)k]);
+        }
+        for (int k = leaf_tgt[l]; k < leaf_tgt[l + 1]; k++) {
+            tgt_node[k] = tk[k].second;
+            local(&c.h_xyz[3 * (size_t)tk[k].second], &leaf_ijk[3 * (size_t)l], &tloc[4 * (size_t)k]);
+        }
+    }
+    // levels 2..L
+    std::vector<std::vector<uint64_t>> keys(L + 1);
+    keys[L] = lk;
+    for (int l = L - 1; l >= 2; l--)
+        for (uint64_t k : keys[l + 1]) {
+            const uint64_t pk = k >> 3;
+            if (keys[l].empty() || keys[l].back() != pk) keys[l].push_back(pk);
+        }
+    t->lev_begin.assign(L + 2, 0);
+    for (int l = 2; l <= L; l++) t->lev_begin[l + 1] = t->lev_begin[l] + (int)keys[l].size();
+    const int ncell = t->lev_begin[L + 1];
+    t->ncell = ncell;
+    t->leaf0 = t->lev_begin[L];
+    std::vector<std::unordered_map<uint64_t, int>> where(L + 1);
+    for (int l = 2; l <= L; l++) {
+        where[l].reserve(keys[l].size() * 2);
+        for (size_t i = 0; i < keys[l].size(); i++) where[l][keys[l][i]] = t->lev_begin[l] + (int)i;
+    }
+    std::vector<int> nsub_src(ncell, 0), nsub_tgt(ncell, 0);
+    for (int l = 0; l < nleaf; l++) {
+        nsub_src[t->leaf0 + l] = leaf_src[l + 1] - leaf_src[l];
+        nsub_tgt[t->leaf0 + l] = leaf_tgt[l + 1] - leaf_tgt[l];
+    }
+    std::vector<int> m2m_tab((size_t)ncell * 8, -1), l2l_tab((size_t)ncell * 8, -1);
+    for (int l = L; l >= 3; l--)
+        for (size_t i = 0; i < keys[l].size(); i++) {
+            const int g = t->lev_begin[l] + (int)i;
+            const int p = where[l - 1][keys[l][i] >> 3];
+            const int oc = (int)(keys[l][i] & 7);
+            nsub_src[p] += nsub_src[g];
+            nsub_tgt[p] += nsub_tgt[g];
+            if (nsub_src[g] > 0) m2m_tab[(size_t)p * 8 + oc] = g;
+            l2l_tab[(size_t)g * 8 + oc] = p;
+        }
+    // M2L table: offset = target - source (cell units), code = (dx+3)*49 + (dy+3)*7 + (dz+3)
+    std::vector<int> m2l_tab((size_t)ncell * NCODE_M2L, -1);
+    size_t nm2l = 0;
+    for (int l = 2; l <= L; l++) {
+        const int n = 1 << l;
+        for (size_t i = 0; i < keys[l].size(); i++) {
+            const int g = t->lev_begin[l] + (int)i;
+            if (nsub_tgt[g] == 0) continue;
+            decode(keys[l][i], ijk);
+            const int px = ijk[0] >> 1, py = ijk[1] >> 1, pz = ijk[2] >> 1;
+            for (int ax = 2 * (px - 1); ax <= 2 * (px + 1) + 1; ax++)
+                for (int ay = 2 * (py - 1); ay <= 2 * (py + 1) + 1; ay++)
+                    for (int az = 2 * (pz - 1); az <= 2 * (pz + 1) + 1; az++) {
+                        if (ax < 0 || ay < 0 || az < 0 || ax >= n || ay >= n || az >= n) continue;
+                        const int dx = ijk[0] - ax, dy = ijk[1] - ay, dz = ijk[2] - az;
+                        if (std::abs(dx) <= 1 && std::abs(dy) <= 1 && std::abs(dz) <= 1) continue;
+                        auto it = where[l].find(morton(ax, ay, az));
+                        if (it == where[l].end() || nsub_src[it->second] == 0) continue;
+                        m2l_tab[(size_t)g * NCODE_M2L + (dx + 3) * 49 + (dy + 3) * 7 + (dz + 3)] = it->second;
+                        nm2l++;
+                    }
+        }
+    }
+    t->n_m2l = nm2l;
+    std::vector<int> near_ptr(nleaf + 1, 0), near_leaf;
+    t->n_p2p_pairs = 0;
+    for (int lf = 0; lf < nleaf; lf++) {
+        if (leaf_tgt[lf + 1] > leaf_tgt[lf]) {
+            const int *q = &leaf_ijk[3 * (size_t)lf];
+            for (int dx = -1; dx <= 1; dx++)
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dz = -1; dz <= 1; dz++) {
+                        const int ax = q[0] + dx, ay = q[1] + dy, az = q[2] + dz;
+                        if (ax < 0 || ay < 0 || az < 0 || ax >= nside || ay >= nside || az >= nside) continue;
+                        auto it = where[L].find(morton(ax, ay, az));
+                        if (it == where[L].end()) continue;
+                        const int nl = it->second - t->leaf0;
+                        if (leaf_src[nl + 1] == leaf_src[nl]) continue;
+                        near_leaf.push_back(nl);
+                        t->n_p2p_pairs += (size_t)(leaf_src[nl + 1] - leaf_src[nl]) * (leaf_tgt[lf + 1] - leaf_tgt[lf]);
+                    }
+        }
+        near_ptr[lf + 1] = (int)near_leaf.size();
+    }
+    const FmmOps &ops = fmm_ops();
+    FCK(up(&t->leaf_src, leaf_src));
+    FCK(up(&t->leaf_tgt, leaf_tgt));
+    FCK(up(&t->tgt_node, tgt_node));
+    FCK(up(&t->leaf_ijk, leaf_ijk));
+    FCK(up(&t->m2l_tab, m2l_tab));
+    FCK(up(&t->m2m_tab, m2m_tab));
+    FCK(up(&t->l2l_tab, l2l_tab));
+    FCK(up(&t->near_ptr, near_ptr));
+    FCK(up(&t->near_leaf, near_leaf));
+    FCK(up_as<double>(&t->sloc, sloc, fp32));
+    FCK(up_as<double>(&t->tloc, tloc, fp32));
+    FCK(up_as<double>(&t->op_m2l, ops.m2l, fp32));
+    FCK(up_as<double>(&t->op_m2m, ops.m2m, fp32));
+    FCK(up_as<double>(&t->op_l2l, ops.l2l, fp32));
+    if (c.src_dst) cudaFree(c.src_dst);
+    c.src_dst = nullptr;
+    FCK(up(&c.src_dst, src_dst));
+    const size_t esz = fp32 ? sizeof(float) : sizeof(double);
+    FCK(cudaMalloc(&t->M, (size_t)ncell * NR * esz));
+    FCK(cudaMalloc(&t->F, (size_t)ncell * NR * esz));
+    FCK(cudaMemset(t->M, 0, (size_t)ncell * NR * esz));
+    FCK(cudaMemset(t->F, 0, (size_t)ncell * NR * esz));
+    const int smem_p2m = (int)(NR * 65 * esz), smem_tr = (int)((NR * NR + NR * (TB + 4)) * esz);
+    if (fp32) {
+        FCK(cudaFuncSetAttribute(k_p2m<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_p2m));
+        FCK(cudaFuncSetAttribute(k_translate<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_tr));
+    } else {
+        FCK(cudaFuncSetAttribute(k_p2m<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_p2m));
+        FCK(cudaFuncSetAttribute(k_translate<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_tr));
+    }
+    if (c.opts.verbose)
+        fprintf(stderr, "fmm: L=%d leaves=%d cells=%d m2l=%zu p2p_pairs=%zu (%s)\n", L, nleaf, ncell, t->n_m2l,
+                t->n_p2p_pairs, fp32 ? "fp32" : "fp64");
+    return FG_OK;
+}
+
+void fmm_free(Ctx &c) {
+    FmmTree *t = static_cast<FmmTree *>(c.fmm);
+    if (!t) return;
+    void *ptrs[] = {t->leaf_src, t->leaf_tgt, t->tgt_node, t->sloc, t->tloc, t->leaf_ijk, t->m2l_tab, t->m2m_tab,
+                    t->l2l_tab, t->near_ptr, t->near_leaf, t->M, t->F, t->op_m2l, t->op_m2m, t->op_l2l};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    delete t;
+    c.fmm = nullptr;
+}
+
+template <typename T>
+static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
+    const int L = t.L;
+    T *M = (T *)t.M, *F = (T *)t.F;
+    const size_t esz = sizeof(T);
+    const int smem_p2m = (int)(NR * 65 * esz), smem_tr = (int)((NR * NR + NR * (TB + 4)) * esz);
+    k_p2m<T><<<t.nleaf, 64, smem_p2m, c.stream>>>(t.nleaf, t.leaf_src, (const T *)t.sloc, c.src_q, t.leaf0, M);
+    for (int l = L - 1; l >= 2; l--) {
+        const int n = t.lev_begin[l + 1] - t.lev_begin[l];
+        if (n)
+            k_translate<T><<<(n + TB - 1) / TB, 160, smem_tr, c.stream>>>(n, t.lev_begin[l], 8, t.m2m_tab,
+                                                                            (const T *)t.op_m2m, M, M, 0);
+    }
+    k_translate<T><<<(t.ncell + TB - 1) / TB, 160, smem_tr, c.stream>>>(t.ncell, 0, NCODE_M2L, t.m2l_tab,
+                                                                          (const T *)t.op_m2l, M, F, 0);
+    for (int l = 3; l <= L; l++) {
+        const int n = t.lev_begin[l + 1] - t.lev_begin[l];
+        if (n)
+            k_translate<T><<<(n + TB - 1) / TB, 160, smem_tr, c.stream>>>(n, t.lev_begin[l], 8, t.l2l_tab,
+                                                                            (const T *)t.op_l2l, F, F, 1);
+    }
+    const double scale = 1.0 / (t.s0 / (double)(1 << L));
+    k_l2p_p2p<T><<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node,
+                                                           (const T *)t.tloc, (const T *)t.sloc, c.src_q, t.leaf_ijk,
+                                                           t.leaf0, scale, t.near_ptr, t.near_leaf, F, c.pot);
+    return cudaGetLastError();
+}
+
+cudaError_t fmm_eval(Ctx &c) {
+    FmmTree *t = static_cast<FmmTree *>(c.fmm);
+    if (!t) return cudaErrorNotSupported;
+    return t->fp32 ? fmm_eval_t<float>(c, *t) : fmm_eval_t<double>(c, *t);
+}
+
+int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p) {
+    const FmmTree *t = static_cast<const FmmTree *>(c.fmm);
+    if (!t) return FG_EINVAL;
+    *L = t->L;
+    *nleaf = t->nleaf;
+    *n_m2l = (double)t->n_m2l;
+    *n_p2p = (double)t->n_p2p_pairs;
+    return FG_OK;
+}
+
 cudaError_t launch_mixed(Ctx &, double, double) { return cudaErrorNotSupported; }
+
 }  // namespace fg

@@ -155,6 +155,9 @@ struct Ctx {
     SolveResult *hres = nullptr;  // pinned
 
     // device: demag
+    std::vector<double> h_src_xyz;  // source points (original order), host copy for the FMM tree
+    int *src_dst = nullptr;      // original source index -> storage position (FMM order)
+    void *fmm = nullptr;         // FMM tree and buffers (fg_fmm.cu)
     double *src_q = nullptr;
     double *tri_slot = nullptr;  // 3 x nft corrections
     double *pot = nullptr;       // nn

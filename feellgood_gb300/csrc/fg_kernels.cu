@@ -624,8 +624,8 @@ template <int NPI, int NPF>
 __global__ void k_charges(int nmt, int nft, const int4 *__restrict__ tet, const double *__restrict__ da,
                           const double *__restrict__ detJ, const int *__restrict__ treg,
                           const DevRegion *__restrict__ regs, const int4 *__restrict__ tri,
-                          const DevTri *__restrict__ tc, const double *__restrict__ m, double *__restrict__ q,
-                          double *__restrict__ tri_slot) {
+                          const DevTri *__restrict__ tc, const double *__restrict__ m,
+                          const int *__restrict__ dst, double *__restrict__ q, double *__restrict__ tri_slot) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < nmt) {
         const int4 I = tet[k];
@@ -639,7 +639,10 @@ __global__ void k_charges(int nmt, int nft, const int4 *__restrict__ tet, const 
         }
         const double Ms = regs[treg[k]].Ms, J = detJ[k];
 #pragma unroll
-        for (int g = 0; g < NPI; g++) q[(size_t)k * NPI + g] = -Ms * (J * c_tpds[g]) * dud;
+        for (int g = 0; g < NPI; g++) {
+            const size_t s = (size_t)k * NPI + g;
+            q[dst ? dst[s] : s] = -Ms * (J * c_tpds[g]) * dud;
+        }
     } else if (k < nmt + nft) {
         const int f = k - nmt;
         const int4 I = tri[f];
@@ -651,11 +654,11 @@ __global__ void k_charges(int nmt, int nft, const int4 *__restrict__ tet, const 
             const double *pm = m + 3 * (size_t)ind[i];
             s[i] = pm[0] * T.n[0] + pm[1] * T.n[1] + pm[2] * T.n[2];
         }
-        double *qq = q + (size_t)nmt * NPI + (size_t)f * NPF;
 #pragma unroll
         for (int g = 0; g < NPF; g++) {
             double un = c_fa[0][g] * s[0] + c_fa[1][g] * s[1] + c_fa[2][g] * s[2];
-            qq[g] = (T.dMs != 0.0) ? T.dMs * T.w[g] * un : 0.0;
+            const size_t sidx = (size_t)nmt * NPI + (size_t)f * NPF + g;
+            q[dst ? dst[sidx] : sidx] = (T.dMs != 0.0) ? T.dMs * T.w[g] * un : 0.0;
         }
 #pragma unroll
         for (int i = 0; i < 3; i++)
@@ -925,10 +928,10 @@ cudaError_t launch_charges(Ctx &c, const double *m) {
     if (n == 0) return cudaSuccess;
     if (c.npi_t == 5)
         k_charges<5, 4><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs,
-                                                                c.tri, c.tri_c, m, c.src_q, c.tri_slot);
+                                                                c.tri, c.tri_c, m, c.src_dst, c.src_q, c.tri_slot);
     else
         k_charges<1, 1><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs,
-                                                                c.tri, c.tri_c, m, c.src_q, c.tri_slot);
+                                                                c.tri, c.tri_c, m, c.src_dst, c.src_q, c.tri_slot);
     return cudaGetLastError();
 }
 
