@@ -54,7 +54,7 @@ class fg_opts(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("precision", C.c_int), ("learned_guess", C.c_int),
                 ("demag", C.c_int), ("fmm_order", C.c_int), ("fmm_leaf", C.c_int), ("one_gauss_point", C.c_int),
                 ("first_order", C.c_int), ("refine_max", C.c_int), ("inner_tol", C.c_double),
-                ("verbose", C.c_int)]
+                ("verbose", C.c_int), ("profile", C.c_int)]
 
 
 class fg_step_report(C.Structure):
@@ -86,7 +86,82 @@ SIGNATURES = {
     "fg_debug_system": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fg_debug_apply": (C.c_int, [C.c_void_p, _dp, _dp]),
     "fg_timings": (C.c_int, [C.c_void_p, _dp]),
+    "fg_counters": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "fg_mesh_load_msh": (C.c_int, [C.c_char_p, C.c_double, C.c_int, C.POINTER(C.c_char_p), _dp, C.c_int,
+                                   C.POINTER(C.c_char_p), C.POINTER(C.c_void_p)]),
+    "fg_mesh_cuboid": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                 C.c_double, C.POINTER(C.c_void_p)]),
+    "fg_mesh_view": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fg_mesh_free": (None, [C.c_void_p]),
+    "fg_mesh_last_error": (C.c_char_p, []),
+    "fg_rng_seed": (None, [C.c_uint]),
+    "fg_rng_angle": (C.c_double, []),
+    "fg_fmm_timings": (C.c_int, [C.c_void_p, _dp]),
 }
+
+
+class fg_mesh_data(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("n_tets", C.c_int), ("n_tris", C.c_int), ("xyz", C.POINTER(C.c_double)),
+                ("tet4", C.POINTER(C.c_int32)), ("tet_region", C.POINTER(C.c_int32)),
+                ("tri3", C.POINTER(C.c_int32)), ("tri_region", C.POINTER(C.c_int32)),
+                ("tri_dMs", C.POINTER(C.c_double)), ("node_index", C.POINTER(C.c_int32)),
+                ("n_vol_regions", C.c_int), ("n_surf_regions", C.c_int), ("vol_names", C.POINTER(C.c_char_p)),
+                ("surf_names", C.POINTER(C.c_char_p))]
+
+
+def _take_mesh(ptr):
+    d = C.cast(ptr, C.POINTER(fg_mesh_data)).contents
+
+    def arr(p, n, dt):
+        return np.ctypeslib.as_array(p, shape=(n,)).astype(dt).copy() if n else np.zeros(0, dt)
+    out = {
+        "xyz": arr(d.xyz, 3 * d.n_nodes, np.float64).reshape(-1, 3),
+        "tets": arr(d.tet4, 4 * d.n_tets, np.int32).reshape(-1, 4),
+        "tet_reg": arr(d.tet_region, d.n_tets, np.int32),
+        "tris": arr(d.tri3, 3 * d.n_tris, np.int32).reshape(-1, 3),
+        "tri_reg": arr(d.tri_region, d.n_tris, np.int32),
+        "dMs": arr(d.tri_dMs, d.n_tris, np.float64),
+        "node_index": arr(d.node_index, d.n_nodes, np.int64),
+        "vol_names": [d.vol_names[k].decode() for k in range(d.n_vol_regions)],
+        "surf_names": [d.surf_names[k].decode() for k in range(d.n_surf_regions)],
+    }
+    fg_lib().fg_mesh_free(ptr)
+    return out
+
+
+def rng_seed(seed):
+    fg_lib().fg_rng_seed(seed)
+
+
+def rng_angle():
+    """Next basis angle of the reference's stream (M_2_PI * U(0,1) from mt19937(rand()))."""
+    return fg_lib().fg_rng_angle()
+
+
+def load_msh(path, vol_regions, Ms, surf_regions=(), length_unit=1e-9):
+    """Read a gmsh file and run the reference's mesh set-up (C++ host code of the library).
+
+    vol_regions: names of the settings' volume regions; Ms: their saturation magnetisation."""
+    L = fg_lib()
+    vn = (C.c_char_p * max(1, len(vol_regions)))(*[n.encode() for n in vol_regions])
+    sn = (C.c_char_p * max(1, len(surf_regions)))(*[n.encode() for n in surf_regions])
+    ms = np.ascontiguousarray(Ms, dtype=np.float64)
+    out = C.c_void_p()
+    s = L.fg_mesh_load_msh(str(path).encode(), length_unit, len(vol_regions), vn, _dptr(ms), len(surf_regions), sn,
+                           C.byref(out))
+    if s != FG_OK:
+        raise FgError(s, L.fg_mesh_last_error().decode())
+    return _take_mesh(out)
+
+
+def cuboid(nx, ny, nz, lx, ly, lz, length_unit=1e-9, Ms=8e5):
+    """Structured cuboid (6 tetrahedra per cell) set up like a mesh read from a file."""
+    L = fg_lib()
+    out = C.c_void_p()
+    s = L.fg_mesh_cuboid(nx, ny, nz, lx, ly, lz, length_unit, Ms, C.byref(out))
+    if s != FG_OK:
+        raise FgError(s, L.fg_mesh_last_error().decode())
+    return _take_mesh(out)
 
 
 def fg_lib():
@@ -235,6 +310,18 @@ class Context:
         y = np.zeros_like(x)
         self._check(self.L.fg_debug_apply(self.h, _dptr(x), _dptr(y)))
         return y
+
+    def counters(self):
+        out = (C.c_longlong * 4)()
+        self._check(self.L.fg_counters(self.h, out))
+        return list(out)
+
+    def fmm_timings(self):
+        """Device ms of the FMM stages of the last evaluation (needs profile=1):
+        P2M, M2M, M2L, L2L, L2P+P2P."""
+        ms = np.zeros(5)
+        self._check(self.L.fg_fmm_timings(self.h, _dptr(ms)))
+        return ms
 
     def timings(self):
         ms = np.zeros(4)

@@ -421,7 +421,7 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
         std::vector<float> s32(Sval.begin(), Sval.end()), a32(A.size());
         const double sc = 1.0 / c.mean_A;
         for (size_t i = 0; i < A.size(); i++) a32[i] = (float)(A[i] * sc);
-        (void)s32;
+        CK(upload(&c.Sval32, s32));
         CK(upload(&c.A32, a32));
     }
     CK(upload(&c.tri, htri));
@@ -449,7 +449,12 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     CK(dalloc(&c.x, 2 * (size_t)nn));
     CK(dalloc(&c.bv, 10 * 2 * (size_t)nn));
     CK(dalloc(&c.W, 3 * (size_t)nn));
+    CK(dalloc(&c.ep32, 3 * (size_t)nn));
+    CK(dalloc(&c.eq32, 3 * (size_t)nn));
+    CK(dalloc(&c.Dl32, nn));
+    CK(dalloc(&c.fv, 23 * (size_t)nn));
     c.bicg_grid = bicg_grid_size(c, false);
+    c.mixed_grid = mixed_grid_size(c);
     c.partial_len = 8 * std::max(c.bicg_grid, 1024);
     CK(dalloc(&c.partial, c.partial_len));
     CK(dalloc(&c.bar, 1));
@@ -555,6 +560,7 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
     CK(cudaEventRecord(c.ev[0], c.stream));
     CK(launch_tet(c, dt, Hext));
     CK(launch_node(c, basis_angle));
+    c.launches += 3;
     CK(cudaEventRecord(c.ev[1], c.stream));
     h->last_c0 = prefactor * FG_THETA * dt * FG_GAMMA0;
     if (c.opts.precision == FG_PREC_FP32_REFINE) CK(launch_mixed(c, dt, prefactor));
@@ -573,6 +579,7 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
         std::memset(rep, 0, sizeof(*rep));
         rep->status = status;
         rep->iters = r.nit;
+        rep->refinements = r.nref;
         rep->vmax = FG_GAMMA0 * std::sqrt(r.v2max);
         rep->res = r.res;
         rep->rhsn = r.rhsn;
@@ -589,15 +596,25 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
 static int demag_into(fg_ctx *h, const double *m, double *phi_out) {
     Ctx &c = h->c;
     CK(launch_charges(c, m));
-    if (c.opts.demag == FG_DEMAG_FMM) CK(fmm_eval(c));
-    else CK(launch_p2p_direct(c));
+    if (c.opts.demag == FG_DEMAG_FMM) {
+        CK(fmm_eval(c));
+        int L = 0, nl = 0;
+        double a, b;
+        fmm_info(c, &L, &nl, &a, &b);
+        c.launches += 3 + 2 * (L - 2);
+    } else {
+        CK(launch_p2p_direct(c));
+        c.launches += 1;
+    }
     CK(launch_phi_final(c, phi_out));
+    c.launches += 2;
     return FG_OK;
 }
 
 static int energy_impl(fg_ctx *h, const double Hext[3], double E[4], double avg[3]) {
     Ctx &c = h->c;
     CK(launch_energy(c, Hext));
+    c.launches += 1;
     CK(cudaMemcpyAsync(c.hepart, c.epart, 7 * sizeof(double) * c.epart_blocks, cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
     double s[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -692,6 +709,24 @@ int fg_debug_apply(fg_ctx *h, const double *x, double *y) {
     CK(cudaStreamSynchronize(c.stream));
     CK(cudaMemcpy(dy, keep.data(), n2 * sizeof(double), cudaMemcpyHostToDevice));
     return FG_OK;
+}
+
+int fg_counters(const fg_ctx *h, long long out[4]) {
+    if (!h || !out) return FG_EINVAL;
+    const Ctx &c = h->c;
+    out[0] = c.launches;
+    int L = 0, nl = 0;
+    double a = 0, b = 0;
+    if (c.fmm) fmm_info(c, &L, &nl, &a, &b);
+    out[1] = L;
+    out[2] = (long long)a;
+    out[3] = (long long)b;
+    return FG_OK;
+}
+
+int fg_fmm_timings(const fg_ctx *h, double ms[5]) {
+    if (!h || !ms) return FG_EINVAL;
+    return fmm_stage_ms(h->c, ms);
 }
 
 int fg_timings(const fg_ctx *h, double ms[4]) {

@@ -53,6 +53,8 @@ struct FmmTree {
     size_t n_m2l = 0, n_p2p_pairs = 0;
     bool fp32 = false;
     double eval_ms = 0;
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    float stage_ms[5] = {0, 0, 0, 0, 0};
     // device
     int *leaf_src = nullptr, *leaf_tgt = nullptr, *tgt_node = nullptr;
     void *sloc = nullptr;  // 4 x nsrc: leaf-local source coordinates (T), w unused
@@ -721,6 +723,8 @@ static int fmm_build_level(Ctx &c, int L) {
         FCK(cudaFuncSetAttribute(k_p2m<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_p2m));
         FCK(cudaFuncSetAttribute(k_translate<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_tr));
     }
+    if (c.opts.profile)
+        for (auto &e : t->ev) FCK(cudaEventCreate(&e));
     if (c.opts.verbose)
         fprintf(stderr, "fmm: L=%d leaves=%d cells=%d m2l=%zu p2p_pairs=%zu (%s)\n", L, nleaf, ncell, t->n_m2l,
                 t->n_p2p_pairs, fp32 ? "fp32" : "fp64");
@@ -734,6 +738,8 @@ void fmm_free(Ctx &c) {
                     t->l2l_tab, t->near_ptr, t->near_leaf, t->M, t->F, t->op_m2l, t->op_m2m, t->op_l2l};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    for (auto &e : t->ev)
+        if (e) cudaEventDestroy(e);
     delete t;
     c.fmm = nullptr;
 }
@@ -744,25 +750,40 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
     T *M = (T *)t.M, *F = (T *)t.F;
     const size_t esz = sizeof(T);
     const int smem_p2m = (int)(NR * 65 * esz), smem_tr = (int)((NR * NR + NR * (TB + 4)) * esz);
+    const bool prof = c.opts.profile && t.ev[0];
+    if (prof) cudaEventRecord(t.ev[0], c.stream);
     k_p2m<T><<<t.nleaf, 64, smem_p2m, c.stream>>>(t.nleaf, t.leaf_src, (const T *)t.sloc, c.src_q, t.leaf0, M);
+    if (prof) cudaEventRecord(t.ev[1], c.stream);
     for (int l = L - 1; l >= 2; l--) {
         const int n = t.lev_begin[l + 1] - t.lev_begin[l];
         if (n)
             k_translate<T><<<(n + TB - 1) / TB, 160, smem_tr, c.stream>>>(n, t.lev_begin[l], 8, t.m2m_tab,
                                                                             (const T *)t.op_m2m, M, M, 0);
     }
+    if (prof) cudaEventRecord(t.ev[2], c.stream);
     k_translate<T><<<(t.ncell + TB - 1) / TB, 160, smem_tr, c.stream>>>(t.ncell, 0, NCODE_M2L, t.m2l_tab,
                                                                           (const T *)t.op_m2l, M, F, 0);
+    if (prof) cudaEventRecord(t.ev[3], c.stream);
     for (int l = 3; l <= L; l++) {
         const int n = t.lev_begin[l + 1] - t.lev_begin[l];
         if (n)
             k_translate<T><<<(n + TB - 1) / TB, 160, smem_tr, c.stream>>>(n, t.lev_begin[l], 8, t.l2l_tab,
                                                                             (const T *)t.op_l2l, F, F, 1);
     }
+    if (prof) cudaEventRecord(t.ev[4], c.stream);
     const double scale = 1.0 / (t.s0 / (double)(1 << L));
     k_l2p_p2p<T><<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node,
                                                            (const T *)t.tloc, (const T *)t.sloc, c.src_q, t.leaf_ijk,
                                                            t.leaf0, scale, t.near_ptr, t.near_leaf, F, c.pot);
+    if (prof) {
+        cudaEventRecord(t.ev[5], c.stream);
+        cudaEventSynchronize(t.ev[5]);
+        cudaEventElapsedTime(&t.stage_ms[0], t.ev[0], t.ev[1]);
+        cudaEventElapsedTime(&t.stage_ms[1], t.ev[1], t.ev[2]);
+        cudaEventElapsedTime(&t.stage_ms[2], t.ev[2], t.ev[3]);
+        cudaEventElapsedTime(&t.stage_ms[3], t.ev[3], t.ev[4]);
+        cudaEventElapsedTime(&t.stage_ms[4], t.ev[4], t.ev[5]);
+    }
     return cudaGetLastError();
 }
 
@@ -770,6 +791,13 @@ cudaError_t fmm_eval(Ctx &c) {
     FmmTree *t = static_cast<FmmTree *>(c.fmm);
     if (!t) return cudaErrorNotSupported;
     return t->fp32 ? fmm_eval_t<float>(c, *t) : fmm_eval_t<double>(c, *t);
+}
+
+int fmm_stage_ms(const Ctx &c, double ms[5]) {
+    const FmmTree *t = static_cast<const FmmTree *>(c.fmm);
+    if (!t) return FG_EINVAL;
+    for (int k = 0; k < 5; k++) ms[k] = t->stage_ms[k];
+    return FG_OK;
 }
 
 int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p) {
@@ -781,7 +809,5 @@ int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p) {
     *n_p2p = (double)t->n_p2p_pairs;
     return FG_OK;
 }
-
-cudaError_t launch_mixed(Ctx &, double, double) { return cudaErrorNotSupported; }
 
 }  // namespace fg

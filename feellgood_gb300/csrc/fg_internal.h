@@ -40,6 +40,8 @@ struct SolveResult {
     int fail;       // solve() returned true
     int timeout;
     double res, rhsn, v2max, res0;
+    int nref;
+    int pad;
 };
 
 // Grid-wide barrier state of the persistent kernels (bounded wait, no hang).
@@ -70,19 +72,18 @@ struct BicgArgs {
     double *u1, *v1;
 };
 
-// Arguments of the FP32 inner Krylov solve with FP64 refinement.
+// Arguments of the FP32 inner Krylov solve with FP64 iterative refinement.
 struct MixedArgs {
     int nn;
     const int *Sptr, *Scol;
-    const double *Sval, *A, *Dl, *ep, *eq;
-    const float *Sval32, *A32, *Dl32, *ep32, *eq32;
+    const double *Sval, *A, *Dl, *ep, *eq;  // FP64 operator (refinement residual)
+    const float *Sval32, *A32;              // static FP32 copies (A32 = A * scale)
+    float *ep32, *eq32, *Dl32, *Minv32;     // per-step FP32 copies, written in phase 0
     const unsigned char *mag;
     double c0;
     const double *b;
-    double *x;        // FP64 solution
-    double *r64;      // FP64 residual
-    double *W64;
-    float *r, *rt, *p, *v, *s, *t, *phat, *shat, *d, *Minv, *W;
+    double *x, *r64, *W64;
+    float *r, *rt, *p, *v, *s, *t, *phat, *shat, *d, *W32;
     double *partial;
     GridBar *bar;
     SolveResult *res;
@@ -91,7 +92,7 @@ struct MixedArgs {
     double dt;
     const double *u0;
     double *u1, *v1;
-    double scale;  // 1/mean(A): scales the FP32 system to O(1)
+    double scale;  // 1/mean(A): the FP32 system is scale*K, entries O(1)
 };
 
 struct Ctx {
@@ -172,6 +173,7 @@ struct Ctx {
     // timings
     cudaEvent_t ev[8];
     float ms[4] = {0, 0, 0, 0};
+    long long launches = 0;  // kernels launched by this context
 };
 
 // kernels (fg_kernels.cu)
@@ -185,5 +187,8 @@ cudaError_t launch_p2p_direct(Ctx &c);
 cudaError_t launch_phi_final(Ctx &c, double *phi_out);
 cudaError_t launch_energy(Ctx &c, const double Hext[3]);
 int bicg_grid_size(Ctx &c, bool mixed);
+int mixed_grid_size(Ctx &c);
+int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p);
+int fmm_stage_ms(const Ctx &c, double ms[5]);
 
 }  // namespace fg

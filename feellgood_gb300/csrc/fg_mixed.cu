@@ -1,0 +1,321 @@
+// FP32 Krylov body with FP64 iterative refinement for the per-step system (the
+// FG_PREC_FP32_REFINE path). Same operator, preconditioner and mask as the plain path
+// (bicg_dir, src/algebra/bicg.h:163-234); what changes is the arithmetic:
+//   outer loop (FP64):  r = b - K x with the FP64 operator; stop when |r| <= tol |b|,
+//                       the reference's own test (src/algebra/iter.h:144-156) applied to
+//                       the true residual;
+//   inner loop (FP32):  BiCGSTAB on (scale K) d = r/|r| from d = 0 with FP32 vectors and
+//                       operator and FP64 dot-product accumulation; scale = 1/mean(A)
+//                       keeps every FP32 quantity O(1) (raw entries are ~1e-27);
+//   x += scale |r| d in FP64.
+// One cooperative launch per solve; the node update (Node::make_evol) is fused at the end.
+#include <cmath>
+
+#include "fg_device.cuh"
+#include "fg_internal.h"
+
+namespace fg {
+
+__global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
+    const int G = gridDim.x;
+    const int nn = a.nn;
+    const int stride = G * blockDim.x;
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const float c32 = (float)(a.c0 * a.scale);
+    // phase 0: FP32 copies of the per-step operator, FP64 tangent vectors of x, |b|^2
+    {
+        double bb = 0.0;
+        for (int i = i0; i < nn; i += stride) {
+            for (int c = 0; c < 3; c++) {
+                a.ep32[3 * i + c] = (float)a.ep[3 * i + c];
+                a.eq32[3 * i + c] = (float)a.eq[3 * i + c];
+            }
+            a.Dl32[i] = (float)(a.Dl[i] * a.scale);
+            const bool m = a.mag[i];
+            a.Minv32[2 * i] = m ? 1.0f / a.A32[i] : 0.0f;
+            a.Minv32[2 * i + 1] = m ? -1.0f / a.A32[i] : 0.0f;
+            tangent<double>(i, a.ep, a.eq, a.x[2 * i], a.x[2 * i + 1], a.W64);
+            if (m) bb += a.b[2 * i] * a.b[2 * i] + a.b[2 * i + 1] * a.b[2 * i + 1];
+        }
+        double v1[1] = {bb};
+        block_store<1>(v1, a.partial, G);
+    }
+    if (!grid_sync(a.bar)) goto timeout;
+    {
+        double s1[1];
+        grid_sum<1>(a.partial, G, s1);
+        const double rhsn = sqrt(fabs(s1[0]));
+        int status = -1, nit = 0, nref = 0;
+        double res = 0.0, res0 = 0.0;
+        for (;;) {
+            // refinement residual r64 = b - K x (FP64, masked)
+            {
+                double rr = 0.0;
+                for (int i = i0; i < nn; i += stride) {
+                    double y0, y1;
+                    apply_row<double>(i, a.Sptr, a.Scol, a.Sval, a.W64, a.ep, a.eq, a.A, a.Dl, a.c0, a.x[2 * i],
+                                      a.x[2 * i + 1], y0, y1);
+                    const bool m = a.mag[i];
+                    const double r0 = m ? a.b[2 * i] - y0 : 0.0, r1 = m ? a.b[2 * i + 1] - y1 : 0.0;
+                    a.r64[2 * i] = r0;
+                    a.r64[2 * i + 1] = r1;
+                    rr += r0 * r0 + r1 * r1;
+                }
+                double v1[1] = {rr};
+                block_store<1>(v1, a.partial, G);
+            }
+            if (!grid_sync(a.bar)) goto timeout;
+            {
+                double s2[1];
+                grid_sum<1>(a.partial, G, s2);
+                res = sqrt(fabs(s2[0]));
+            }
+            if (nref == 0) res0 = res;
+            if (isnan(res)) { status = 2; break; }
+            if (res <= rhsn * a.tol) { status = 0; break; }
+            if (nref >= a.refine_max || nit >= a.maxiter) { status = 1; break; }
+            // inner FP32 BiCGSTAB on (scale K) d = r64/res, relative target
+            const double rho = res;
+            const double target = fmax(a.inner_tol, 0.3 * a.tol * rhsn / res);
+            {
+                const float inv = (float)(1.0 / rho);
+                double rr = 0.0;
+                for (int i = i0; i < nn; i += stride) {
+                    for (int c = 0; c < 2; c++) {
+                        const int k = 2 * i + c;
+                        const float rv = (float)a.r64[k] * inv;
+                        a.r[k] = rv;
+                        a.rt[k] = rv;
+                        a.p[k] = rv;
+                        a.d[k] = 0.0f;
+                        rr += (double)rv * rv;
+                    }
+                }
+                double v1[1] = {rr};
+                block_store<1>(v1, a.partial, G);
+            }
+            if (!grid_sync(a.bar)) goto timeout;
+            {
+                double s2[1];
+                grid_sum<1>(a.partial, G, s2);
+                double rr = s2[0], rtr = s2[0];
+                double rho1 = 0.0, rho2 = 0.0, alpha = 0.0, beta = 0.0, omega = 0.0;
+                int it = 0;
+                while (sqrt(rr) > target && nit < a.maxiter) {
+                    rho1 = rtr;
+                    if (it > 0) {
+                        if (rho2 == 0.0 || omega == 0.0) break;
+                        beta = (rho1 / rho2) * (alpha / omega);
+                    }
+                    const float fb = (float)beta, fo = (float)omega;
+                    for (int i = i0; i < nn; i += stride) {
+                        float p0 = a.p[2 * i], p1 = a.p[2 * i + 1];
+                        if (it > 0) {
+                            p0 = a.r[2 * i] + fb * (p0 - fo * a.v[2 * i]);
+                            p1 = a.r[2 * i + 1] + fb * (p1 - fo * a.v[2 * i + 1]);
+                            a.p[2 * i] = p0;
+                            a.p[2 * i + 1] = p1;
+                        }
+                        const float h0 = a.Minv32[2 * i] * p0, h1 = a.Minv32[2 * i + 1] * p1;
+                        a.phat[2 * i] = h0;
+                        a.phat[2 * i + 1] = h1;
+                        tangent<float>(i, a.ep32, a.eq32, h0, h1, a.W32);
+                    }
+                    if (!grid_sync(a.bar)) goto timeout;
+                    {
+                        double vr = 0.0;
+                        for (int i = i0; i < nn; i += stride) {
+                            float y0, y1;
+                            apply_row<float>(i, a.Sptr, a.Scol, a.Sval32, a.W32, a.ep32, a.eq32, a.A32, a.Dl32, c32,
+                                             a.phat[2 * i], a.phat[2 * i + 1], y0, y1);
+                            if (!a.mag[i]) y0 = y1 = 0.0f;
+                            a.v[2 * i] = y0;
+                            a.v[2 * i + 1] = y1;
+                            vr += (double)y0 * a.rt[2 * i] + (double)y1 * a.rt[2 * i + 1];
+                        }
+                        double v1[1] = {vr};
+                        block_store<1>(v1, a.partial, G);
+                    }
+                    if (!grid_sync(a.bar)) goto timeout;
+                    {
+                        double s1b[1];
+                        grid_sum<1>(a.partial, G, s1b);
+                        alpha = rho1 / s1b[0];
+                    }
+                    {
+                        const float fa = (float)alpha;
+                        double ss = 0.0;
+                        for (int i = i0; i < nn; i += stride) {
+                            const float s0 = a.r[2 * i] - fa * a.v[2 * i], s1 = a.r[2 * i + 1] - fa * a.v[2 * i + 1];
+                            a.s[2 * i] = s0;
+                            a.s[2 * i + 1] = s1;
+                            const float h0 = a.Minv32[2 * i] * s0, h1 = a.Minv32[2 * i + 1] * s1;
+                            a.shat[2 * i] = h0;
+                            a.shat[2 * i + 1] = h1;
+                            tangent<float>(i, a.ep32, a.eq32, h0, h1, a.W32);
+                            ss += (double)s0 * s0 + (double)s1 * s1;
+                        }
+                        double v1[1] = {ss};
+                        block_store<1>(v1, a.partial, G);
+                    }
+                    if (!grid_sync(a.bar)) goto timeout;
+                    {
+                        double s1c[1];
+                        grid_sum<1>(a.partial, G, s1c);
+                        if (sqrt(s1c[0]) <= target) {
+                            const float fa = (float)alpha;
+                            for (int i = i0; i < nn; i += stride) {
+                                a.d[2 * i] += fa * a.phat[2 * i];
+                                a.d[2 * i + 1] += fa * a.phat[2 * i + 1];
+                            }
+                            nit++;
+                            break;
+                        }
+                    }
+                    {
+                        double ts = 0.0, tt = 0.0;
+                        for (int i = i0; i < nn; i += stride) {
+                            float y0, y1;
+                            apply_row<float>(i, a.Sptr, a.Scol, a.Sval32, a.W32, a.ep32, a.eq32, a.A32, a.Dl32, c32,
+                                             a.shat[2 * i], a.shat[2 * i + 1], y0, y1);
+                            if (!a.mag[i]) y0 = y1 = 0.0f;
+                            a.t[2 * i] = y0;
+                            a.t[2 * i + 1] = y1;
+                            ts += (double)y0 * a.s[2 * i] + (double)y1 * a.s[2 * i + 1];
+                            tt += (double)y0 * y0 + (double)y1 * y1;
+                        }
+                        double v2[2] = {ts, tt};
+                        block_store<2>(v2, a.partial, G);
+                    }
+                    if (!grid_sync(a.bar)) goto timeout;
+                    {
+                        double s2b[2];
+                        grid_sum<2>(a.partial, G, s2b);
+                        omega = s2b[0] / s2b[1];
+                    }
+                    {
+                        const float fa = (float)alpha, fo = (float)omega;
+                        double r2 = 0.0, rtr2 = 0.0;
+                        for (int i = i0; i < nn; i += stride) {
+#pragma unroll
+                            for (int c = 0; c < 2; c++) {
+                                const int k = 2 * i + c;
+                                a.d[k] += fa * a.phat[k] + fo * a.shat[k];
+                                const float rv = a.s[k] - fo * a.t[k];
+                                a.r[k] = rv;
+                                r2 += (double)rv * rv;
+                                rtr2 += (double)a.rt[k] * rv;
+                            }
+                        }
+                        double v2[2] = {r2, rtr2};
+                        block_store<2>(v2, a.partial, G);
+                    }
+                    if (!grid_sync(a.bar)) goto timeout;
+                    {
+                        double s2c[2];
+                        grid_sum<2>(a.partial, G, s2c);
+                        rr = s2c[0];
+                        rtr = s2c[1];
+                    }
+                    rho2 = rho1;
+                    it++;
+                    nit++;
+                }
+            }
+            // x += scale * rho * d (FP64) and the tangent vectors of the new x
+            {
+                const double f = a.scale * rho;
+                for (int i = i0; i < nn; i += stride) {
+                    const double x0 = a.x[2 * i] + f * (double)a.d[2 * i];
+                    const double x1 = a.x[2 * i + 1] + f * (double)a.d[2 * i + 1];
+                    a.x[2 * i] = x0;
+                    a.x[2 * i + 1] = x1;
+                    tangent<double>(i, a.ep, a.eq, x0, x1, a.W64);
+                }
+            }
+            nref++;
+            if (!grid_sync(a.bar)) goto timeout;
+        }
+        const bool fail = (status != 0);
+        if (!grid_sync(a.bar)) goto timeout;
+        double v2max = 0.0;
+        if (!fail) {
+            for (int i = i0; i < nn; i += stride) {
+                if (!a.mag[i]) continue;
+                const double vp = a.x[2 * i], vq = a.x[2 * i + 1];
+                v2max = fmax(v2max, vp * vp + vq * vq);
+                const double pa = vp * FG_GAMMA0, qb = vq * FG_GAMMA0;
+                double nv[3], nu[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    nv[c] = pa * a.ep[3 * i + c] + qb * a.eq[3 * i + c];
+                    nu[c] = a.u0[3 * i + c] + a.dt * nv[c];
+                }
+                const double n = sqrt(nu[0] * nu[0] + nu[1] * nu[1] + nu[2] * nu[2]);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    a.v1[3 * i + c] = nv[c];
+                    a.u1[3 * i + c] = nu[c] / n;
+                }
+            }
+        }
+        v2max = dmax_reduce_block(v2max);
+        if (threadIdx.x == 0) {
+            atomicMax((unsigned long long *)&a.res->v2max, (unsigned long long)__double_as_longlong(v2max));
+            if (blockIdx.x == 0) {
+                a.res->status = status;
+                a.res->nit = nit;
+                a.res->nref = nref;
+                a.res->fail = fail ? 1 : 0;
+                a.res->res = res;
+                a.res->rhsn = rhsn;
+                a.res->res0 = res0;
+            }
+        }
+        return;
+    }
+timeout:
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.res->timeout = 1;
+        a.res->fail = 1;
+    }
+}
+
+int mixed_grid_size(Ctx &c) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed, 256, 0);
+    if (per_sm < 1) per_sm = 1;
+    int g = per_sm * c.nsm;
+    const int need = (c.nn + 255) / 256;
+    if (need < g) g = need;
+    return g < 1 ? 1 : g;
+}
+
+cudaError_t launch_mixed(Ctx &c, double dt, double prefactor) {
+    const size_t n2 = 2 * (size_t)c.nn;
+    MixedArgs a;
+    a.nn = c.nn;
+    a.Sptr = c.Sptr; a.Scol = c.Scol; a.Sval = c.Sval; a.A = c.A; a.Dl = c.Dl; a.ep = c.ep; a.eq = c.eq;
+    a.Sval32 = c.Sval32; a.A32 = c.A32;
+    a.ep32 = c.ep32; a.eq32 = c.eq32; a.Dl32 = c.Dl32;
+    float *f = c.fv;
+    a.r = f; a.rt = f + n2; a.p = f + 2 * n2; a.v = f + 3 * n2; a.s = f + 4 * n2; a.t = f + 5 * n2;
+    a.phat = f + 6 * n2; a.shat = f + 7 * n2; a.d = f + 8 * n2; a.Minv32 = f + 9 * n2; a.W32 = f + 10 * n2;
+    a.mag = c.mag;
+    a.c0 = prefactor * FG_THETA * dt * FG_GAMMA0;
+    a.b = c.rhs; a.x = c.x;
+    a.r64 = c.bv; a.W64 = c.W;
+    a.partial = c.partial; a.bar = c.bar; a.res = c.dres;
+    a.tol = c.opts.tol; a.inner_tol = c.opts.inner_tol;
+    a.maxiter = c.opts.max_iter; a.refine_max = c.opts.refine_max;
+    a.dt = dt; a.u0 = c.u[0]; a.u1 = c.u[1]; a.v1 = c.v[1];
+    a.scale = 1.0 / c.mean_A;
+    cudaError_t e = cudaMemsetAsync(c.bar, 0, sizeof(GridBar), c.stream);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(c.dres, 0, sizeof(SolveResult), c.stream);
+    if (e != cudaSuccess) return e;
+    void *args[] = {&a};
+    return cudaLaunchCooperativeKernel((void *)k_mixed, dim3(c.mixed_grid), dim3(256), args, 0, c.stream);
+}
+
+}  // namespace fg

@@ -85,6 +85,7 @@ typedef struct {
     int refine_max;       /* FP64 refinement sweeps in FG_PREC_FP32_REFINE */
     double inner_tol;     /* relative tolerance of each FP32 inner solve */
     int verbose;
+    int profile;          /* 1: record device events around every FMM stage (fg_fmm_timings) */
 } fg_opts;
 
 typedef struct {
@@ -141,6 +142,46 @@ int fg_debug_apply(fg_ctx *ctx, const double *x, double *y);
 /* Device time of the last fg_step / fg_compute_all phases, in ms:
  * [0] elements, [1] solve, [2] demag, [3] energy+evolution. */
 int fg_timings(const fg_ctx *ctx, double ms[4]);
+
+/* Counters: [0] kernels launched by the context so far, [1] FMM tree depth (0 without FMM),
+ * [2] M2L (cell, cell) pairs, [3] P2P (target, source) pairs per evaluation. */
+int fg_counters(const fg_ctx *ctx, long long out[4]);
+
+/* Device ms of the stages of the last FMM evaluation when opts.profile is set:
+ * [0] P2M, [1] M2M, [2] M2L, [3] L2L, [4] L2P + P2P. */
+int fg_fmm_timings(const fg_ctx *ctx, double ms[5]);
+
+/* ---- host-side mesh set-up (no GPU work) ----------------------------------------
+ * A set-up mesh owned by the library: the fg_mesh fields plus region names (index 0 is
+ * "__default__", as in the reference's Settings) and node_index[file node] = internal
+ * node (mesh::sortNodes). Free with fg_mesh_free.
+ *   fg_mesh_load_msh  mesh::mesh(Settings&) construction: src/mesh.h:38-135, src/read.cpp:12-197,
+ *                     src/mesh.cpp:121-367 (gmsh 2.2/4.1 ASCII, orientation, controlTriangles, sortNodes)
+ *   fg_mesh_cuboid    python-modules/meshMaker.py:440-483 (Cuboid, 6 tetrahedra per cell) followed
+ *                     by the same set-up, one volume region "volume" of saturation Ms */
+typedef struct {
+    int n_nodes, n_tets, n_tris;
+    double *xyz;
+    int32_t *tet4, *tet_region, *tri3, *tri_region;
+    double *tri_dMs;
+    int32_t *node_index;
+    int n_vol_regions, n_surf_regions;
+    char **vol_names, **surf_names;
+} fg_mesh_data;
+
+int fg_mesh_load_msh(const char *path, double length_unit, int n_vol, const char *const *vol_names,
+                     const double *vol_Ms, int n_surf, const char *const *surf_names, fg_mesh_data **out);
+int fg_mesh_cuboid(int nx, int ny, int nz, double lx, double ly, double lz, double length_unit, double Ms,
+                   fg_mesh_data **out);
+int fg_mesh_view(const fg_mesh_data *data, fg_mesh *mesh);
+void fg_mesh_free(fg_mesh_data *data);
+const char *fg_mesh_last_error(void);
+
+/* Basis-angle stream of LinAlgebra::base_projection (src/linear_algebra.cpp:3-11):
+ * fg_rng_seed = srand(seed) (src/main.cpp:211); each fg_rng_angle() = M_2_PI * U(0,1) from
+ * std::mt19937(rand()). */
+void fg_rng_seed(unsigned int seed);
+double fg_rng_angle(void);
 
 #ifdef __cplusplus
 }

@@ -136,3 +136,23 @@ def test_bad_mesh_is_rejected():
     bad2["tets"] = t2
     with pytest.raises(fg.FgError):
         fg.Context(bad2, cases.regions())
+
+
+@pytest.mark.parametrize("tol", [1e-6, 1e-10])
+def test_mixed_precision_solve(tol):
+    """FP32 Krylov body + FP64 refinement stops on the true FP64 residual at the same
+    tolerance; its v agrees with the FP64 oracle to within the tolerance's reach."""
+    m, st, H, o, c = _setup(10, 10, 4, tol=tol)
+    cm = fg.Context(m, cases.regions(), tol=tol, max_iter=5000, precision=fg.FG_PREC_FP32_REFINE)
+    cm.set_state(st["u"], st["v"], st["phi"], st["phiv"])
+    pref = fgo.prefactor(DT, DTMAX)
+    o.set_solver(1e-13, 5000)
+    o.base_projection(0.9)
+    ro = o.step(DT, pref, H)
+    rg = cm.step(DT, pref, H, 0.9)
+    assert rg["status"] == fg.FG_OK and not ro["fail"]
+    assert rg["res"] <= tol * rg["rhsn"]
+    assert rg["refinements"] >= 1
+    so, sg = o.get_state(1), cm.get_state(1)
+    assert _rel(sg["v"], so["v"]) <= 50 * tol
+    assert np.max(np.abs(np.linalg.norm(sg["u"], axis=1) - 1.0)) < 1e-14

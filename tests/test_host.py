@@ -1,0 +1,80 @@
+"""Host-side parts of the product (no GPU needed): C-ABI exports, mesh ingest and set-up.
+
+The mesh set-up of libfggpu (C++) is compared array for array with the oracle's
+restatement, and against the reference's own known answers (ellipsoid counts, the
+controlTriangles error messages of unit-tests/ut_readMesh.cpp, meshMaker.Cuboid output).
+"""
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+import feellgood_gb300 as fg
+from oracle import mesh as om
+from tests import cases
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_declared_symbol():
+    hdr = open(os.path.join(ROOT, "include", "fggpu.h")).read()
+    names = sorted(set(re.findall(r"\b(fg_[a-z_0-9]+)\s*\(", hdr)))
+    lib = fg.fg_lib()
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert len(names) >= 20
+
+
+def _same(a, b, keys=("xyz", "tets", "tet_reg", "tris", "tri_reg", "dMs")):
+    for k in keys:
+        assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), k
+
+
+@pytest.mark.parametrize("shape", [(3, 2, 2), (6, 5, 4), (4, 4, 1)])
+def test_cuboid_setup_matches_oracle(shape):
+    nx, ny, nz = shape
+    a = fg.cuboid(nx, ny, nz, 2.5 * nx, 2.5 * ny, 2.5 * nz, 1e-9, cases.MS)
+    b = cases.cuboid(nx, ny, nz)
+    _same(a, b)
+    assert a["surf_names"] == ["__default__", "surface(volume)"]
+
+
+def test_cuboid_matches_meshmaker_fixture(golden_dir):
+    """meshMaker.Cuboid((0,0,0),(7.5,5,5),3,2,2) written by the reference's generator."""
+    path = os.path.join(golden_dir, "cuboid_3x2x2.msh")
+    a = fg.load_msh(path, ["volume"], [cases.MS])       # boundary recreated by controlTriangles
+    b = fg.cuboid(3, 2, 2, 7.5, 5, 5, 1e-9, cases.MS)
+    _same(a, b)
+    c = fg.load_msh(path, ["volume"], [cases.MS], ["surface"])  # the file's own triangles
+    d = om.setup(om.read_msh(path), ["volume"], ["surface"], 1e-9, Ms=[cases.MS])
+    _same(c, d)
+    assert np.all(np.abs(c["dMs"]) == cases.MS)
+    info = json.load(open(os.path.join(golden_dir, "cuboid_20.json")))
+    e = fg.cuboid(20, 20, 20, 50, 50, 50, 1e-9, cases.MS)
+    assert (len(e["xyz"]), len(e["tets"]), len(e["tris"])) == (info["nodes"], info["tets"], info["tris"])
+
+
+def test_ellipsoid_setup_matches_oracle(golden_dir):
+    path = os.path.join(golden_dir, "ellipsoid.msh")
+    g = json.load(open(os.path.join(golden_dir, "golden.json")))["ellipsoid_counts"]
+    a = fg.load_msh(path, ["ellipsoid_volume"], [795774.7])
+    b = om.setup(om.read_msh(path), ["ellipsoid_volume"], [], 1e-9, Ms=[795774.7])
+    _same(a, b, keys=("xyz", "tets", "tet_reg", "tris", "tri_reg", "dMs", "node_index"))
+    assert (len(a["xyz"]), len(a["tets"]), len(a["tris"])) == (g["nodes"], g["tets"], g["tris"])
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4])
+def test_bad_meshes_rejected_with_reference_message(golden_dir, k):
+    msg = json.load(open(os.path.join(golden_dir, "golden.json")))["bad_cuboid_errors"][k - 1]
+    with pytest.raises(fg.FgError) as e:
+        fg.load_msh(os.path.join(golden_dir, f"bad_cuboid_{k}.msh"), ["whole_volume"], [8e5], ["whole_surface"], 1.0)
+    assert e.value.status == fg.api.FG_EMESH
+    assert str(e.value).endswith(msg)
+
+
+def test_missing_mesh_file():
+    with pytest.raises(fg.FgError) as e:
+        fg.load_msh("/nonexistent/file.msh", ["v"], [1.0])
+    assert e.value.status == fg.api.FG_EIO
