@@ -82,6 +82,7 @@ SIGNATURES = {
     "fg_get_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fg_demag": (C.c_int, [C.c_void_p, C.c_int, _dp]),
     "fg_energy": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "fg_energy_noalloc": (C.c_int, [C.c_void_p, _dp, _dp]),
     "fg_average": (C.c_int, [C.c_void_p, C.c_int, _dp]),
     "fg_debug_system": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fg_debug_apply": (C.c_int, [C.c_void_p, _dp, _dp]),
@@ -293,6 +294,13 @@ class Context:
         H = np.ascontiguousarray(Hext, dtype=np.float64)
         E = np.zeros(4)
         self._check(self.L.fg_energy(self.h, _dptr(H), _dptr(E)))
+        return E
+
+    def energy_noalloc(self, Hext):
+        """fg_energy through the entry point that allocates no device memory."""
+        H = np.ascontiguousarray(Hext, dtype=np.float64)
+        E = np.zeros(4)
+        self._check(self.L.fg_energy_noalloc(self.h, _dptr(H), _dptr(E)))
         return E
 
     def average(self, which=0):

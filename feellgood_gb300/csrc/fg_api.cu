@@ -21,11 +21,6 @@ cudaError_t fmm_eval(Ctx &c);
 
 using namespace fg;
 
-struct fg_ctx {
-    Ctx c;
-    double last_c0 = 0.0;
-};
-
 static thread_local std::string g_create_error;
 
 #define CK(call)                                                                      \

@@ -186,9 +186,16 @@ cudaError_t launch_charges(Ctx &c, const double *m);
 cudaError_t launch_p2p_direct(Ctx &c);
 cudaError_t launch_phi_final(Ctx &c, double *phi_out);
 cudaError_t launch_energy(Ctx &c, const double Hext[3]);
+cudaError_t launch_energy_into(Ctx &c, const double Hext[3], double *partial);
 int bicg_grid_size(Ctx &c, bool mixed);
 int mixed_grid_size(Ctx &c);
 int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p);
 int fmm_stage_ms(const Ctx &c, double ms[5]);
 
 }  // namespace fg
+
+// The opaque handle of the C ABI.
+struct fg_ctx {
+    fg::Ctx c;
+    double last_c0 = 0.0;
+};

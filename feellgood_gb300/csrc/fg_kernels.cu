@@ -832,4 +832,17 @@ cudaError_t launch_energy(Ctx &c, const double H[3]) {
     return cudaGetLastError();
 }
 
+// Same reduction as launch_energy with the per-block partial sums written to a caller-given
+// device buffer of at least 7 * c.epart_blocks doubles (used by fg_energy_noalloc).
+cudaError_t launch_energy_into(Ctx &c, const double H[3], double *partial) {
+    const int G = c.epart_blocks;
+    if (c.npi_t == 5)
+        k_energy<5, 4><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
+                                                 c.u[1], c.phi[1], H[0], H[1], H[2], partial);
+    else
+        k_energy<1, 1><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
+                                                 c.u[1], c.phi[1], H[0], H[1], H[2], partial);
+    return cudaGetLastError();
+}
+
 }  // namespace fg

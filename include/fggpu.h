@@ -131,6 +131,15 @@ int fg_demag(fg_ctx *ctx, int which, double *out);
 /* Energies of the NEXT state for a constant applied field. */
 int fg_energy(fg_ctx *ctx, const double Hext[3], double energies[4]);
 
+/* fg_energy for callers that cannot allocate device memory when they call (a framework
+ * that owns all device memory after start-up, or code that must not trigger the device
+ * synchronisation an allocation may cause). No counterpart in the reference. Allocates
+ * nothing: the reduction's partial sums go to a static device array of 8192 doubles shared
+ * by all calls in the process; a context needing more returns FG_EINVAL. The first call on
+ * a device looks that array up (make it before any stream capture); calls whose GPU work
+ * overlaps race on the array. Same results as fg_energy. */
+int fg_energy_noalloc(fg_ctx *ctx, const double Hext[3], double energies[4]);
+
 /* <u_d> (which 0) or <v_d> (which 1) of NEXT over the magnetic volume, src/mesh.cpp:89-106. */
 int fg_average(fg_ctx *ctx, int which, double avg[3]);
 
