@@ -184,6 +184,7 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
         std::memset(&d, 0, sizeof(d));
         d.A = g.Ae; d.Ms = g.Ms; d.alpha = g.alpha; d.K = g.K; d.K3 = g.K3;
         if (g.Ms > 0) {
+            if (g.K != 0.0 || g.K3 != 0.0) c.aniso = true;
             d.Abis = 2.0 * g.Ae / (FG_MU0 * g.Ms);
             d.Kbis = 2.0 * g.K / (FG_MU0 * g.Ms);
             d.K3bis = 2.0 * g.K3 / (FG_MU0 * g.Ms);

@@ -182,14 +182,11 @@ __device__ __forceinline__ void ups_cols(T x, T y, T z, Fn &&f) {
     }
 }
 
-template <typename T> __device__ __forceinline__ T rsqrt_t(T x);
-template <> __device__ __forceinline__ float rsqrt_t<float>(float x) { return rsqrtf(x); }
-template <> __device__ __forceinline__ double rsqrt_t<double>(double x) { return rsqrt(x); }
 
 // P2M: one block (64 threads) per leaf; each thread forms q*conj(Ups) of one source into a
 // shared tile, each coefficient is summed over the tile in a fixed order.
 template <typename T>
-__global__ void __launch_bounds__(64) k_p2m(int nleaf, const int *__restrict__ leaf_src, const T *__restrict__ sloc,
+__global__ void __launch_bounds__(64) k_p2m(int nleaf, const int *__restrict__ leaf_src, T *__restrict__ sloc,
                                             const double *__restrict__ q, int leaf0, T *__restrict__ M) {
     constexpr int LD = 65;
     extern __shared__ unsigned char smem_raw[];
@@ -202,6 +199,7 @@ __global__ void __launch_bounds__(64) k_p2m(int nleaf, const int *__restrict__ l
         if (s < s1) {
             const T x = sloc[4 * (size_t)s], y = sloc[4 * (size_t)s + 1], z = sloc[4 * (size_t)s + 2];
             const T qq = T(q[s]);
+            sloc[4 * (size_t)s + 3] = qq;  // charge beside the coordinates for the near field
             ups_cols<T>(x, y, z, [&](int n, int m, T re, T im) {
                 tile[ridx(n, m, 0) * LD + tid] = qq * re;
                 if (m) tile[ridx(n, m, 1) * LD + tid] = -qq * im;
@@ -285,19 +283,30 @@ __global__ void __launch_bounds__(160) k_translate(int n_out, int out0, int ncod
     }
 }
 
-// L2P + P2P: one warp per leaf. Sources of the adjacent leaves are spread over the lanes,
-// up to 8 targets of the leaf are held in registers; coordinates are leaf-local (leaf
-// units), so FP32 keeps the relative precision of close pairs. Per-lane FP32 partial
-// sums are reduced in a fixed order and accumulated in FP64.
+// 1/sqrt in the precision of the path (CUDA's rsqrtf / rsqrt).
+template <typename T> __device__ __forceinline__ T rsqrt_p(T x);
+template <> __device__ __forceinline__ float rsqrt_p<float>(float x) { return rsqrtf(x); }
+template <> __device__ __forceinline__ double rsqrt_p<double>(double x) { return rsqrt(x); }
+
+template <typename T> struct Vec4;
+template <> struct Vec4<float> { using type = float4; };
+template <> struct Vec4<double> { using type = double4; };
+
+// L2P + P2P: one warp per leaf. Sources of the adjacent leaves are spread over the lanes
+// (x, y, z, q in one vector load), up to NT targets of the leaf are held in registers;
+// coordinates are leaf-local (leaf units), so FP32 keeps the relative precision of close
+// pairs. Per-lane partial sums of each adjacent leaf are added in FP64, reduced over the
+// warp in a fixed order.
 template <typename T>
 __global__ void __launch_bounds__(128) k_l2p_p2p(int nleaf, const int *__restrict__ leaf_src,
                                                  const int *__restrict__ leaf_tgt, const int *__restrict__ tgt_node,
                                                  const T *__restrict__ tloc, const T *__restrict__ sloc,
-                                                 const double *__restrict__ q, const int *__restrict__ leaf_ijk,
-                                                 int leaf0, double scale, const int *__restrict__ near_ptr,
-                                                 const int *__restrict__ near_leaf, const T *__restrict__ F,
-                                                 double *__restrict__ pot) {
-    constexpr int NT = 8;
+                                                 const int *__restrict__ leaf_ijk, int leaf0, double scale,
+                                                 const int *__restrict__ near_ptr, const int *__restrict__ near_leaf,
+                                                 const T *__restrict__ F, double *__restrict__ pot) {
+    constexpr int NT = 16;
+    using V4 = typename Vec4<T>::type;
+    const V4 *__restrict__ src4 = reinterpret_cast<const V4 *>(sloc);
     const int lane = threadIdx.x & 31;
     const int leaf = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (leaf >= nleaf) return;
@@ -319,19 +328,19 @@ __global__ void __launch_bounds__(128) k_l2p_p2p(int nleaf, const int *__restric
         }
         for (int e = near_ptr[leaf]; e < near_ptr[leaf + 1]; e++) {
             const int nl = near_leaf[e];
+            // source coordinates relative to this leaf: own leaf-local + integer leaf offset
             const T ox = T(leaf_ijk[3 * nl] - li), oy = T(leaf_ijk[3 * nl + 1] - lj), oz = T(leaf_ijk[3 * nl + 2] - lk);
             const int s0 = leaf_src[nl], s1 = leaf_src[nl + 1];
             T acc[NT];
 #pragma unroll
             for (int j = 0; j < NT; j++) acc[j] = 0;
             for (int s = s0 + lane; s < s1; s += 32) {
-                const T sx = sloc[4 * (size_t)s] + ox, sy = sloc[4 * (size_t)s + 1] + oy,
-                        sz = sloc[4 * (size_t)s + 2] + oz;
-                const T qq = T(q[s]);
+                const V4 sv = src4[s];
+                const T sx = sv.x + ox, sy = sv.y + oy, sz = sv.z + oz, qq = sv.w;
 #pragma unroll
                 for (int j = 0; j < NT; j++) {
                     const T dx = tx[j] - sx, dy = ty[j] - sy, dz = tz[j] - sz;
-                    acc[j] += qq * rsqrt_t<T>(dx * dx + dy * dy + dz * dz);
+                    acc[j] += qq * rsqrt_p<T>(dx * dx + dy * dy + dz * dz);
                 }
             }
 #pragma unroll
@@ -752,7 +761,7 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
     const int smem_p2m = (int)(NR * 65 * esz), smem_tr = (int)((NR * NR + NR * (TB + 4)) * esz);
     const bool prof = c.opts.profile && t.ev[0];
     if (prof) cudaEventRecord(t.ev[0], c.stream);
-    k_p2m<T><<<t.nleaf, 64, smem_p2m, c.stream>>>(t.nleaf, t.leaf_src, (const T *)t.sloc, c.src_q, t.leaf0, M);
+    k_p2m<T><<<t.nleaf, 64, smem_p2m, c.stream>>>(t.nleaf, t.leaf_src, (T *)t.sloc, c.src_q, t.leaf0, M);
     if (prof) cudaEventRecord(t.ev[1], c.stream);
     for (int l = L - 1; l >= 2; l--) {
         const int n = t.lev_begin[l + 1] - t.lev_begin[l];
@@ -773,8 +782,8 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
     if (prof) cudaEventRecord(t.ev[4], c.stream);
     const double scale = 1.0 / (t.s0 / (double)(1 << L));
     k_l2p_p2p<T><<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node,
-                                                           (const T *)t.tloc, (const T *)t.sloc, c.src_q, t.leaf_ijk,
-                                                           t.leaf0, scale, t.near_ptr, t.near_leaf, F, c.pot);
+                                                           (const T *)t.tloc, (const T *)t.sloc, t.leaf_ijk, t.leaf0,
+                                                           scale, t.near_ptr, t.near_leaf, F, c.pot);
     if (prof) {
         cudaEventRecord(t.ev[5], c.stream);
         cudaEventSynchronize(t.ev[5]);

@@ -109,6 +109,7 @@ struct Ctx {
     int n_tets_total = 0;
     double total_mag_vol = 0;
     double mean_A = 0;
+    bool aniso = false;  // some magnetic region has K != 0 or K3 != 0
 
     std::vector<unsigned char> h_mag;
     std::vector<double> h_xyz;

@@ -176,6 +176,91 @@ __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__
     }
 }
 
+// Element kernel without anisotropy (all regions K = K3 = 0, the case of the benchmark
+// configurations). The same quantities in closed form: with no anisotropy the Gauss-point
+// fields of Tet::integrales reduce to constants per tet, so
+//   uHeff(g) = -Abis |grad u|^2 + sum_i a_i(g) (u_i . He),            He = Hd + Hext
+//   BE_i     = -Abis vol (da_i . grad) u + (sum_g w_g a_i(g)) (He + (s_dt/gamma0) Hv)
+// and v is not read (it enters integrales only through the anisotropy terms).
+template <int NPI>
+__global__ void __launch_bounds__(128) k_tet64_iso(int nmt, const int4 *__restrict__ tet, const double *__restrict__ da,
+                                                   const double *__restrict__ detJ, const int *__restrict__ treg,
+                                                   const DevRegion *__restrict__ regs, const double *__restrict__ u0,
+                                                   const double *__restrict__ phi0, const double *__restrict__ phiv0,
+                                                   double dt, double Hx, double Hy, double Hz,
+                                                   double4 *__restrict__ slot) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nmt) return;
+    const int4 I = tet[t];
+    const int ind[4] = {I.x, I.y, I.z, I.w};
+    double d[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) d[i][k] = da[(3 * i + k) * (size_t)nmt + t];
+    const double J = detJ[t];
+    const DevRegion &R = regs[treg[t]];
+    double un[4][3], ph[4], phv[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const double *pu = u0 + 3 * (size_t)ind[i];
+        un[i][0] = pu[0]; un[i][1] = pu[1]; un[i][2] = pu[2];
+        ph[i] = phi0[ind[i]];
+        phv[i] = phiv0[ind[i]];
+    }
+    double dU[3][3], Hd[3], Hv[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) dU[k][c] = d[0][k] * un[0][c] + d[1][k] * un[1][c] + d[2][k] * un[2][c] + d[3][k] * un[3][c];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        Hd[c] = -(ph[0] * d[0][c] + ph[1] * d[1][c] + ph[2] * d[2][c] + ph[3] * d[3][c]);
+        Hv[c] = -(phv[0] * d[0][c] + phv[1] * d[1][c] + phv[2] * d[2][c] + phv[3] * d[3][c]);
+    }
+    const double Abis = R.Abis, alpha = R.alpha;
+    double gradsq = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) gradsq += dU[k][c] * dU[k][c];
+    const double He[3] = {Hd[0] + Hx, Hd[1] + Hy, Hd[2] + Hz};
+    double uh[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) uh[i] = un[i][0] * He[0] + un[i][1] * He[1] + un[i][2] * He[2];
+    const double reduced_dt = FG_GAMMA0 * dt;
+    const double M = 2. * alpha * 0.1 / reduced_dt;
+    const double kv = FG_THETA * dt;  // s_dt / gamma0
+    double w[NPI], aw[4] = {0, 0, 0, 0}, contrib[4] = {0, 0, 0, 0}, vol = 0.0;
+#pragma unroll
+    for (int g = 0; g < NPI; g++) {
+        w[g] = J * c_tpds[g];
+        vol += w[g];
+        const double h = -Abis * gradsq + c_ta[0][g] * uh[0] + c_ta[1][g] * uh[1] + c_ta[2][g] * uh[2] + c_ta[3][g] * uh[3];
+        double a;
+        if (h > 0.0)
+            a = (h > M) ? alpha + reduced_dt / 2. * M : alpha + reduced_dt / 2. * h;
+        else
+            a = (h < -M) ? alpha / (1. + reduced_dt / (2. * alpha) * M) : alpha / (1. - reduced_dt / (2. * alpha) * h);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            aw[i] += c_ta[i][g] * w[g];
+            contrib[i] += c_ta[i][g] * w[g] * a;
+        }
+    }
+    const double H[3] = {He[0] + kv * Hv[0], He[1] + kv * Hv[1], He[2] + kv * Hv[2]};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        double BE[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const double ex = d[i][0] * dU[0][c] + d[i][1] * dU[1][c] + d[i][2] * dU[2][c];
+            BE[c] = -vol * Abis * ex + aw[i] * H[c];
+        }
+        slot[4 * (size_t)t + i] = make_double4(contrib[i], BE[0], BE[1], BE[2]);
+    }
+}
+
 // ---------------------------------------------------------------------------------
 // Node kernel: Node::setBasis with the step's angle (src/node.h:73-102), the gather of
 // the per-vertex slots (assembly, src/solver.cpp:11-48), the RHS projection, the Jacobi
@@ -735,6 +820,15 @@ void upload_rules(bool one_point) {
 cudaError_t launch_tet(Ctx &c, double dt, const double H[3]) {
     if (c.nmt == 0) return cudaSuccess;
     const int b = 128;
+    if (!c.aniso) {
+        if (c.npi_t == 5)
+            k_tet64_iso<5><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0],
+                                                                   c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot);
+        else
+            k_tet64_iso<1><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0],
+                                                                   c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot);
+        return cudaGetLastError();
+    }
     if (c.npi_t == 5)
         k_tet64<5><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0], c.v[0],
                                                           c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot);

@@ -1,6 +1,6 @@
 """Build recipe for the oracle's C++ restatement (test infrastructure only).
 
-Compiles oracle/fgoracle.cpp into oracle/_build/libfgoracle.so with g++ and OpenMP.
+Compiles oracle/fgoracle.cpp and oracle/fmm_cpu.cpp into oracle/_build/libfgoracle.so with g++ and OpenMP.
 Plain -O2 without fast-math, so the FP64 arithmetic follows IEEE order of operations.
 """
 import os
@@ -12,12 +12,15 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfgoracle.so")
 
 
+SOURCES = ["fgoracle.cpp", "fmm_cpu.cpp"]
+
+
 def build(force=False, quiet=True):
-    src = os.path.join(HERE, "fgoracle.cpp")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in SOURCES]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(f) for f in srcs):
         return LIB
     os.makedirs(OUT, exist_ok=True)
-    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-o", LIB + ".tmp", src]
+    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-o", LIB + ".tmp"] + srcs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         sys.stderr.write(r.stdout + r.stderr)

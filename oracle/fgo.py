@@ -58,6 +58,7 @@ def lib():
         L.fgo_create.argtypes = [C.c_int, _dp, C.c_int, _ip, _ip, C.c_int, _ip, _ip, _dp, C.c_int,
                                  C.POINTER(Region), C.c_int, C.POINTER(TriRegion), C.c_int]
         L.fgo_destroy.argtypes = [C.c_void_p]
+        L.fgo_set_demag.argtypes = [C.c_void_p, C.c_int]
         L.fgo_set_threads.argtypes = [C.c_void_p, C.c_int]
         L.fgo_max_threads.restype = C.c_int
         L.fgo_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_int]
@@ -126,6 +127,10 @@ class Oracle:
         if getattr(self, "h", None):
             self.L.fgo_destroy(self.h)
             self.h = None
+
+    def set_demag(self, levels):
+        """0: exact direct sum; > 0: CPU FMM of that depth (5 = the reference's ScalFMM tree)."""
+        self.L.fgo_set_demag(self.h, levels)
 
     def set_solver(self, tol=1e-6, maxiter=700):
         self.L.fgo_set_solver(self.h, tol, maxiter)

@@ -147,6 +147,8 @@ struct Oracle {
     double res = 0, rhsn = 1, vmax = 0;
     double E[4] = {0, 0, 0, 0};
     int nthreads = 0;
+    int fmm_levels = 0;  // 0: exact direct sum; > 0: CPU FMM with this tree depth
+    void *fmm = nullptr;
 };
 
 V3 v3(const double *p) { return {p[0], p[1], p[2]}; }
@@ -776,12 +778,39 @@ void charges(const Oracle &o, int which, const std::vector<double> &pts, std::ve
     }
 }
 
-// fmm::demag (src/fmm_demag.h:184-224) with an exact FP64 direct sum in place of the FMM.
+}  // namespace
+extern "C" void *fgo_fmm_create(int ns, const double *src, int nt, const double *tgt, int levels);
+extern "C" void fgo_fmm_destroy(void *h);
+extern "C" void fgo_fmm_eval(void *h, const double *q, double *pot);
+namespace {
+
+// fmm::demag (src/fmm_demag.h:184-224): an exact FP64 direct sum in place of ScalFMM, or
+// the CPU FMM (fmm_cpu.cpp) when fmm_levels > 0 (used to time the CPU baseline).
 void demag_direct(Oracle &o, int which) {
     std::vector<double> pts, q, corr;
     source_points(o, pts);
     charges(o, which, pts, q, corr);
     const long ns = (long)q.size();
+    if (o.fmm_levels > 0) {
+        std::vector<int> tn;
+        std::vector<double> txyz;
+        for (int i = 0; i < o.nn; i++)
+            if (o.magNode[i]) {
+                tn.push_back(i);
+                txyz.push_back(o.node[i].p.x);
+                txyz.push_back(o.node[i].p.y);
+                txyz.push_back(o.node[i].p.z);
+            }
+        if (!o.fmm) o.fmm = fgo_fmm_create((int)ns, pts.data(), (int)tn.size(), txyz.data(), o.fmm_levels);
+        std::vector<double> pot(tn.size());
+        fgo_fmm_eval(o.fmm, q.data(), pot.data());
+        for (size_t k = 0; k < tn.size(); k++) {
+            const int i = tn[k];
+            const double phi = (pot[k] + corr[i]) / (4 * M_PI);
+            if (which) o.node[i].phiv[NXT] = phi; else o.node[i].phi[NXT] = phi;
+        }
+        return;
+    }
 #pragma omp parallel for schedule(dynamic, 64)
     for (int i = 0; i < o.nn; i++) {
         if (!o.magNode[i]) continue;
@@ -984,7 +1013,19 @@ void *fgo_create(int nn, const double *xyz, int nt, const int *tet, const int *t
     return o;
 }
 
-void fgo_destroy(void *h) { delete static_cast<Oracle *>(h); }
+void fgo_destroy(void *h) {
+    Oracle *o = static_cast<Oracle *>(h);
+    if (o->fmm) fgo_fmm_destroy(o->fmm);
+    delete o;
+}
+
+// Demag evaluator: levels 0 = exact direct sum, > 0 = CPU FMM with that tree depth
+// (5 reproduces ScalFMM's NbLevels = 6 of the reference: 32^3 leaves).
+void fgo_set_demag(void *h, int levels) {
+    Oracle *o = static_cast<Oracle *>(h);
+    if (o->fmm) { fgo_fmm_destroy(o->fmm); o->fmm = nullptr; }
+    o->fmm_levels = levels;
+}
 
 void fgo_set_threads(void *h, int n) {
     static_cast<Oracle *>(h)->nthreads = n;
