@@ -151,36 +151,39 @@ def run_steps(ctx, n, H, dtmax, angles):
     return ms, reps
 
 
-def cpu_leg(mesh, u0, steps, warmup, budget_s=25.0):
-    """The oracle (CPU restatement of the reference path, FP64, OpenMP over all host cores)."""
+def cpu_leg(mesh, u0, steps, warmup, budget_s=25.0, levels=5):
+    """The oracle (CPU restatement of the reference path, FP64, OpenMP over all host cores):
+    full steps (base_projection, element integrals, 2x2-block CSR assembly, bicg_dir, update,
+    demag of m and v with the CPU FMM at the reference's tree depth, energies, evolution)."""
     from oracle import fgo
     o = fgo.Oracle({k: mesh[k] for k in ("xyz", "tets", "tet_reg", "tris", "tri_reg", "dMs")},
                    [fgo.make_region(), fgo.make_region(A=AE, Ms=MS, alpha=ALPHA)])
     cores = fgo.lib().fgo_max_threads()
     o.set_solver(TOL, MAXITER)
+    o.set_demag(levels)
     o.set_state(u0)
     H = np.zeros(3)
+    o.compute_all(H)  # also builds the FMM tree (set-up, untimed)
     fgo.srand(SEED)
-    dtmax = DT
     times = []
     t_start = time.perf_counter()
     for k in range(warmup + steps):
-        o.base_projection(fgo.draw_angle())
         t0 = time.perf_counter()
-        r = o.step(DT, prefactor(DT, dtmax), H)
+        o.base_projection(fgo.draw_angle())
+        r = o.step(DT, prefactor(DT, DT), H)
+        if r["fail"]:
+            raise RuntimeError(f"oracle solve failed: {r}")
+        o.compute_all(H)
         t1 = time.perf_counter()
         if k >= warmup:
             times.append(t1 - t0)
-        # evolution without demag (the CPU demag evaluator is not part of this sample)
-        st = o.get_state(1)
-        o.set_state(st["u"], st["v"], st["phi"], st["phiv"])
-        if time.perf_counter() - t_start > budget_s and len(times) >= 1:
+        if time.perf_counter() - t_start > budget_s and times:
             break
     per = float(np.mean(times))
     return {"value": 1.0 / per, "unit": "steps/s", "cores": cores, "kind": "port",
-            "sample": f"oracle FP64 step at 1.2M tets (element integrals + 2x2-block CSR assembly + bicg_dir + "
-                      f"update), {len(times)} steps timed; demag excluded (no CPU FMM in this sample), so this "
-                      f"overstates the CPU's steps/s"}
+            "sample": f"{len(times)} full oracle step(s) of the same film workload (1.2M tets) after {warmup} "
+                      f"warm-up: element integrals + 2x2-block CSR assembly + bicg_dir + update + demag x2 "
+                      f"(CPU FP64 FMM, P=9, 32^3-leaf tree as ScalFMM in the reference) + energies"}
 
 
 def reference_arm(args):
@@ -191,9 +194,9 @@ def reference_arm(args):
     mesh = film_mesh()
     u0 = initial_state(mesh)
     steps = max(1, min(args.steps, 3))
-    c = cpu_leg(mesh, u0, steps, min(args.warmup, 1))
+    c = cpu_leg(mesh, u0, steps, 1, budget_s=120.0)
     line = {"metric": METRIC, "value": c["value"], "unit": "steps/s", "n_gpus": args.gpus, "steps": steps,
-            "warmup": min(args.warmup, 1), "ms_per_step": 1e3 / c["value"], "higher_is_better": True,
+            "warmup": 1, "ms_per_step": 1e3 / c["value"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "film 400x400x10 nm, 2 nm grid, 1.2M tets, alpha 0.02, dt 5e-14, tol 1e-6",
                        "global_batch": 1, "seq_len": 0, "parallelism": "replicas"},

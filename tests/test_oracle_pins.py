@@ -64,3 +64,16 @@ def test_bad_cuboid_messages(golden_dir, k):
     with pytest.raises(om.MeshError) as e:
         om.setup(msh, ["whole_volume"], ["whole_surface"], 1.0, Ms=[8e5])
     assert str(e.value) == g["bad_cuboid_errors"][k - 1]
+
+
+def test_oracle_cpu_fmm_matches_direct_sum():
+    """The CPU FMM that times the CPU baseline computes the same potential as the exact sum."""
+    from tests import cases
+    m = cases.cuboid(10, 10, 3)
+    u = cases.perturbed_state(m["xyz"], seed=3, sigma=0.3)
+    o = fgo.Oracle(m, cases.oracle_regions())
+    o.set_state(u)
+    d = o.demag(0)
+    o.set_demag(3)
+    f = o.demag(0)
+    assert np.linalg.norm(f - d) / np.linalg.norm(d) < 1e-5
