@@ -54,7 +54,8 @@ class fg_opts(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("precision", C.c_int), ("learned_guess", C.c_int),
                 ("demag", C.c_int), ("fmm_order", C.c_int), ("fmm_leaf", C.c_int), ("one_gauss_point", C.c_int),
                 ("first_order", C.c_int), ("refine_max", C.c_int), ("inner_tol", C.c_double),
-                ("verbose", C.c_int), ("profile", C.c_int)]
+                ("verbose", C.c_int), ("profile", C.c_int), ("mlp_train_steps", C.c_int), ("mlp_batch", C.c_int),
+                ("mlp_lr", C.c_double)]
 
 
 class fg_step_report(C.Structure):
@@ -95,9 +96,17 @@ SIGNATURES = {
     "fg_mesh_view": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fg_mesh_free": (None, [C.c_void_p]),
     "fg_mesh_last_error": (C.c_char_p, []),
+    "fg_run": (C.c_int, [C.c_char_p, C.c_uint, C.c_int, C.c_void_p]),
+    "fg_run_last_error": (C.c_char_p, []),
+    "fg_run_request_stop": (None, []),
+    "fg_settings_dump": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int]),
     "fg_rng_seed": (None, [C.c_uint]),
     "fg_rng_angle": (C.c_double, []),
     "fg_fmm_timings": (C.c_int, [C.c_void_p, _dp]),
+    "fg_mlp_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _dp]),
+    "fg_mlp_debug_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p]),
+    "fg_mlp_nparam": (C.c_int, []),
 }
 
 
@@ -128,6 +137,32 @@ def _take_mesh(ptr):
     }
     fg_lib().fg_mesh_free(ptr)
     return out
+
+
+class fg_run_report(C.Structure):
+    _fields_ = [("status", C.c_int), ("steps", C.c_longlong), ("t", C.c_double), ("wall_s", C.c_double),
+                ("E", C.c_double * 4)]
+
+
+def run(settings_path, seed=0, verbose=False):
+    """A whole simulation from a settings file (the reference's `feellgood --seed N file`)."""
+    L = fg_lib()
+    rep = fg_run_report()
+    s = L.fg_run(str(settings_path).encode(), seed, int(verbose), C.byref(rep))
+    if s != FG_OK:
+        raise FgError(s, L.fg_run_last_error().decode())
+    return {"steps": rep.steps, "t": rep.t, "wall_s": rep.wall_s, "E": list(rep.E)}
+
+
+def settings_dump(settings_path):
+    """The parsed settings (reader check, no GPU work)."""
+    import json
+    L = fg_lib()
+    buf = C.create_string_buffer(1 << 16)
+    s = L.fg_settings_dump(str(settings_path).encode(), buf, len(buf))
+    if s != FG_OK:
+        raise FgError(s, L.fg_run_last_error().decode())
+    return json.loads(buf.value.decode())
 
 
 def rng_seed(seed):
@@ -323,6 +358,23 @@ class Context:
         out = (C.c_longlong * 4)()
         self._check(self.L.fg_counters(self.h, out))
         return list(out)
+
+    def mlp_info(self):
+        """(training steps done, last minibatch loss) of the learned guess."""
+        n = C.c_longlong()
+        loss = np.zeros(1)
+        self._check(self.L.fg_mlp_info(self.h, C.byref(n), _dptr(loss)))
+        return n.value, float(loss[0])
+
+    def mlp_debug_grad(self, feat, target):
+        """(weights, summed gradient, loss) of the GPU training kernels for given samples."""
+        feat = np.ascontiguousarray(feat, dtype=np.float32)
+        target = np.ascontiguousarray(target, dtype=np.float32)
+        n = self.L.fg_mlp_nparam()
+        w, g, loss = np.zeros(n, np.float32), np.zeros(n, np.float32), np.zeros(1, np.float32)
+        self._check(self.L.fg_mlp_debug_grad(self.h, len(feat), _ptr(feat), _ptr(target), _ptr(w), _ptr(g),
+                                             _ptr(loss)))
+        return w, g, float(loss[0])
 
     def fmm_timings(self):
         """Device ms of the FMM stages of the last evaluation (needs profile=1):

@@ -20,9 +20,13 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler"
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-I", os.path.join(HERE, "..", "include")]
 
 
+MAIN = "fg_main.cpp"  # the command-line driver, linked as an executable
+EXE = os.path.join(OUT, "fggpu")
+
+
 def _sources():
     cu = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
-    cpp = sorted(f for f in os.listdir(CSRC) if f.endswith(".cpp"))
+    cpp = sorted(f for f in os.listdir(CSRC) if f.endswith(".cpp") and f != MAIN)
     return cu, cpp
 
 
@@ -66,6 +70,11 @@ def build(force=False, verbose=False, ptxas_info=False):
         sys.stderr.write(log)
         raise RuntimeError("fggpu link failed")
     os.replace(LIB + ".tmp", LIB)
+    rc, log = _run(["g++"] + CXXFLAGS + [os.path.join(CSRC, MAIN), "-o", EXE, "-L", OUT, "-lfggpu",
+                                        "-Wl,-rpath,$ORIGIN"])
+    if rc != 0:
+        sys.stderr.write(log)
+        raise RuntimeError("fggpu driver link failed")
     return LIB
 
 

@@ -131,6 +131,9 @@ void fg_opts_default(fg_opts *o) {
     o->refine_max = 20;
     o->inner_tol = 1e-3;
     o->verbose = 0;
+    o->mlp_train_steps = 20;
+    o->mlp_batch = 16384;
+    o->mlp_lr = 1e-3;
 }
 
 const char *fg_strerror(int s) {
@@ -185,6 +188,7 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
         d.A = g.Ae; d.Ms = g.Ms; d.alpha = g.alpha; d.K = g.K; d.K3 = g.K3;
         if (g.Ms > 0) {
             if (g.K != 0.0 || g.K3 != 0.0) c.aniso = true;
+            c.ms_ref = std::max(c.ms_ref == 1.0 ? 0.0 : c.ms_ref, g.Ms);
             d.Abis = 2.0 * g.Ae / (FG_MU0 * g.Ms);
             d.Kbis = 2.0 * g.K / (FG_MU0 * g.Ms);
             d.K3bis = 2.0 * g.K3 / (FG_MU0 * g.Ms);
@@ -464,6 +468,14 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     c.epart_blocks = std::max(1, std::min(4 * c.nsm, (nmt + 255) / 256));
     CK(dalloc(&c.epart, 7 * (size_t)c.epart_blocks));
     CK(cudaMallocHost((void **)&c.hepart, 7 * sizeof(double) * c.epart_blocks));
+    if (c.opts.learned_guess) {
+        CK(dalloc(&c.heff, 3 * (size_t)nn));
+        int sm = mlp_create(c);
+        if (sm != FG_OK) {
+            c.err = "fg_create: learned-guess buffers";
+            return sm;
+        }
+    }
     int demag = c.opts.demag;
     if (demag == FG_DEMAG_AUTO) demag = ((double)c.nsrc * c.n_mag_nodes > 4e9) ? FG_DEMAG_FMM : FG_DEMAG_DIRECT;
     c.opts.demag = demag;
@@ -512,6 +524,8 @@ void fg_destroy(fg_ctx *h) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     fmm_free(c);
+    mlp_free(c);
+    if (c.heff) cudaFree(c.heff);
     if (c.hres) cudaFreeHost(c.hres);
     if (c.hepart) cudaFreeHost(c.hepart);
     for (int k = 0; k < 8; k++)
@@ -557,10 +571,13 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
     CK(launch_tet(c, dt, Hext));
     CK(launch_node(c, basis_angle));
     c.launches += 3;
-    CK(cudaEventRecord(c.ev[1], c.stream));
     h->last_c0 = prefactor * FG_THETA * dt * FG_GAMMA0;
+    const bool use_mlp = c.mlp && mlp_steps(c) >= c.opts.mlp_train_steps;
+    if (c.mlp) CK(mlp_before_solve(c, h->last_c0, use_mlp));
+    CK(cudaEventRecord(c.ev[1], c.stream));
     if (c.opts.precision == FG_PREC_FP32_REFINE) CK(launch_mixed(c, dt, prefactor));
     else CK(launch_bicg64(c, dt, prefactor));
+    c.launches += 1;
     CK(cudaEventRecord(c.ev[2], c.stream));
     CK(cudaMemcpyAsync(c.hres, c.dres, sizeof(SolveResult), cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
@@ -571,16 +588,25 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
     if (r.timeout) status = FG_ETIMEDOUT;
     else if (r.status == 1) status = FG_SOLVER_ITER_OVERFLOW;
     else if (r.status == 2 || r.fail) status = FG_SOLVER_CANNOT_CONVERGE;
+    int accepted = 0;
+    double r0m = r.res0, r0p = r.res0;
+    if (c.mlp) {
+        mlp_after_sync(c, use_mlp ? &accepted : nullptr, &r0m, &r0p, nullptr);
+        if (!use_mlp) { r0m = r.res0; r0p = r.res0; }
+        // train on this step's solution (asynchronous; its loss is read at the next sync)
+        if (status == FG_OK) CK(mlp_train(c));
+    }
     if (rep) {
         std::memset(rep, 0, sizeof(*rep));
         rep->status = status;
         rep->iters = r.nit;
         rep->refinements = r.nref;
+        rep->guess_accepted = accepted;
         rep->vmax = FG_GAMMA0 * std::sqrt(r.v2max);
         rep->res = r.res;
         rep->rhsn = r.rhsn;
         rep->res0 = r.res0;
-        rep->res0_fallback = r.res0;
+        rep->res0_fallback = use_mlp ? r0p : r.res0;
     }
     if (status == FG_ETIMEDOUT) {
         c.err = "persistent solver: grid barrier timed out";
@@ -640,6 +666,7 @@ int fg_compute_all(fg_ctx *h, const double Hext[3], double energies[4]) {
     if (energies)
         for (int k = 0; k < 4; k++) energies[k] = E[k];
     // Fem::evolution: CURRENT <- NEXT
+    if (c.mlp) CK(mlp_before_evolution(c));
     const size_t n3 = 3 * sizeof(double) * c.nn, n1 = sizeof(double) * c.nn;
     CK(cudaMemcpyAsync(c.u[0], c.u[1], n3, cudaMemcpyDeviceToDevice, c.stream));
     CK(cudaMemcpyAsync(c.v[0], c.v[1], n3, cudaMemcpyDeviceToDevice, c.stream));
@@ -719,6 +746,22 @@ int fg_counters(const fg_ctx *h, long long out[4]) {
     out[3] = (long long)b;
     return FG_OK;
 }
+
+int fg_mlp_info(const fg_ctx *h, long long *train_steps, double *last_loss) {
+    if (!h) return FG_EINVAL;
+    if (!h->c.mlp) return FG_EINVAL;
+    if (train_steps) *train_steps = mlp_steps(h->c);
+    if (last_loss) *last_loss = mlp_loss(h->c);
+    return FG_OK;
+}
+
+int fg_mlp_debug_grad(fg_ctx *h, int nsamples, const float *feat, const float *target, float *weights,
+                      float *grad, float *loss) {
+    if (!h || !h->c.mlp || !feat || !target || !weights || !grad || !loss) return FG_EINVAL;
+    return mlp_debug_grad(h->c, nsamples, feat, target, weights, grad, loss);
+}
+
+int fg_mlp_nparam(void) { return mlp_nparam(); }
 
 int fg_fmm_timings(const fg_ctx *h, double ms[5]) {
     if (!h || !ms) return FG_EINVAL;

@@ -110,6 +110,7 @@ struct Ctx {
     double total_mag_vol = 0;
     double mean_A = 0;
     bool aniso = false;  // some magnetic region has K != 0 or K3 != 0
+    double ms_ref = 1.0; // largest Ms of the magnetic regions (feature scale of the learned guess)
 
     std::vector<unsigned char> h_mag;
     std::vector<double> h_xyz;
@@ -175,6 +176,8 @@ struct Ctx {
     cudaEvent_t ev[8];
     float ms[4] = {0, 0, 0, 0};
     long long launches = 0;  // kernels launched by this context
+    void *mlp = nullptr;     // learned initial guess (fg_mlp.cu)
+    double *heff = nullptr;  // per-node BE/A (effective field), written when the learned guess is on
 };
 
 // kernels (fg_kernels.cu)
@@ -192,6 +195,16 @@ int bicg_grid_size(Ctx &c, bool mixed);
 int mixed_grid_size(Ctx &c);
 int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p);
 int fmm_stage_ms(const Ctx &c, double ms[5]);
+int mlp_create(Ctx &c);
+void mlp_free(Ctx &c);
+cudaError_t mlp_before_solve(Ctx &c, double c0, bool use);
+cudaError_t mlp_train(Ctx &c);
+void mlp_after_sync(Ctx &c, int *accepted, double *res0_mlp, double *res0_prev, double *loss);
+long long mlp_steps(const Ctx &c);
+cudaError_t mlp_before_evolution(Ctx &c);
+double mlp_loss(const Ctx &c);
+int mlp_debug_grad(Ctx &c, int nsamples, const float *hx, const float *hy, float *w_out, float *g_out, float *loss);
+int mlp_nparam();
 
 }  // namespace fg
 

@@ -272,7 +272,7 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
                          const double *__restrict__ A, const double *__restrict__ u0, const double *__restrict__ v1,
                          double cr, double sr, double *__restrict__ ep, double *__restrict__ eq,
                          double *__restrict__ Dl, double *__restrict__ rhs, double *__restrict__ x,
-                         double *__restrict__ Minv, double *__restrict__ W) {
+                         double *__restrict__ Minv, double *__restrict__ W, double *__restrict__ heff) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
     const double u[3] = {u0[3 * i], u0[3 * i + 1], u0[3 * i + 2]};
@@ -308,6 +308,12 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
         dl += s.x; be0 += s.y; be1 += s.z; be2 += s.w;
     }
     Dl[i] = dl;
+    if (heff) {  // effective field BE_i / A_i, a feature of the learned guess
+        const double ia = mag[i] ? 1.0 / A[i] : 0.0;
+        heff[3 * i] = be0 * ia;
+        heff[3 * i + 1] = be1 * ia;
+        heff[3 * i + 2] = be2 * ia;
+    }
     if (mag[i]) {
         rhs[2 * i] = q[0] * be0 + q[1] * be1 + q[2] * be2;
         rhs[2 * i + 1] = e[0] * be0 + e[1] * be1 + e[2] * be2;
@@ -844,7 +850,8 @@ cudaError_t launch_node(Ctx &c, double angle) {
     const long n2 = 2L * c.nn;
     double *Minv = bv + 8 * n2;
     k_node64<<<nblocks(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.inc_ptr, c.inc, c.slot, c.mag, c.A, c.u[0], c.v[1],
-                                                        cr, sr, c.ep, c.eq, c.Dl, c.rhs, c.x, Minv, c.W);
+                                                        cr, sr, c.ep, c.eq, c.Dl, c.rhs, c.x, Minv, c.W,
+                                                        c.mlp ? c.heff : nullptr);
     return cudaGetLastError();
 }
 

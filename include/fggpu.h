@@ -86,6 +86,9 @@ typedef struct {
     double inner_tol;     /* relative tolerance of each FP32 inner solve */
     int verbose;
     int profile;          /* 1: record device events around every FMM stage (fg_fmm_timings) */
+    int mlp_train_steps;  /* learned guess: solves that only train before the guess is proposed */
+    int mlp_batch;        /* learned guess: nodes per training minibatch */
+    double mlp_lr;        /* learned guess: Adam learning rate */
 } fg_opts;
 
 typedef struct {
@@ -156,6 +159,17 @@ int fg_timings(const fg_ctx *ctx, double ms[4]);
  * [2] M2L (cell, cell) pairs, [3] P2P (target, source) pairs per evaluation. */
 int fg_counters(const fg_ctx *ctx, long long out[4]);
 
+/* Learned guess: training steps done and the last minibatch MSE (scaled units). */
+int fg_mlp_info(const fg_ctx *ctx, long long *train_steps, double *last_loss);
+
+/* Learned guess, for gradient checks: runs the training forward/backward kernels on
+ * nsamples (a multiple of 128) caller-given feature rows (12 floats) and targets (3 floats);
+ * returns the weights used (BF16 values as float), the summed loss gradient and the mean
+ * squared loss. Parameter layout: W1[64][12], b1[64], W2[64][64], b2[64], W3[3][64], b3[3]. */
+int fg_mlp_debug_grad(fg_ctx *ctx, int nsamples, const float *feat, const float *target, float *weights,
+                      float *grad, float *loss);
+int fg_mlp_nparam(void);
+
 /* Device ms of the stages of the last FMM evaluation when opts.profile is set:
  * [0] P2M, [1] M2M, [2] M2L, [3] L2L, [4] L2P + P2P. */
 int fg_fmm_timings(const fg_ctx *ctx, double ms[5]);
@@ -191,6 +205,30 @@ const char *fg_mesh_last_error(void);
  * std::mt19937(rand()). */
 void fg_rng_seed(unsigned int seed);
 double fg_rng_angle(void);
+
+/* ---- whole simulations from a settings file (host driver around the GPU step) -----
+ * fg_run reproduces `feellgood [--seed seed] settings.yml` (src/main.cpp:204-286 and
+ * Fem::time_integration, src/time_integration.cpp:136-254): the same YAML/JSON settings
+ * keys (numbers only where the reference accepts expressions), the gmsh mesh, the
+ * TimeStepper with dt halving and max(du) rejection, <basename>.evol and
+ * <basename>_iter<N>.sol outputs in the reference's formats, "-" reads stdin.
+ * An optional "gpu:" section selects precision (fp64 | fp32_refine), learned_guess,
+ * demag (auto | direct | fmm) and one_gauss_point. */
+typedef struct {
+    int status;
+    long long steps; /* accepted time steps */
+    double t;        /* final time */
+    double wall_s;   /* wall time of the time loop */
+    double E[4];     /* last energies */
+} fg_run_report;
+
+int fg_run(const char *settings_path, unsigned int seed, int verbose, fg_run_report *report);
+const char *fg_run_last_error(void);
+/* Ask a running fg_run to stop after the current step, saving <basename>_at_exit.sol
+ * (the reference's SIGINT/SIGTERM behaviour, src/time_integration.cpp:101-134). */
+void fg_run_request_stop(void);
+/* Parsed settings as JSON (no GPU work). */
+int fg_settings_dump(const char *settings_path, char *out, int len);
 
 #ifdef __cplusplus
 }

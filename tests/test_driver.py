@@ -1,0 +1,140 @@
+"""Settings reader (CPU) and the whole-simulation driver fg_run (GPU): the reference's own
+functional test (ci-tests/full_test.py) run from its JSON settings through the product's
+driver, and the .sol write / restart round trip."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import feellgood_gb300 as fg
+
+YAML = """# a settings file in the reference's schema
+outputs:
+  directory: out/     # trailing slash is dropped
+  evol_time_step: 2e-13
+  final_time: 1e-11
+  evol_columns:
+    - t
+    - <Mx>
+    - E_tot
+  mag_config_every: false
+mesh:
+  filename: some/dir/film.msh
+  length_unit: 1e-9
+  volume_regions:
+    film:
+      Ae: 1.3e-11
+      Ms: 8e5
+      K: 1e4
+      uk: [0, 0, 2]
+      alpha_LLG: 0.02
+  surface_regions:
+    top: {Ks: 1e-3, suppress_charges: true}
+initial_magnetization: [1, 1, 0]
+Bext: [0, 0, 0.005]
+finite_element_solver:
+  max(iter): 500
+  tolerance: 1e-8
+time_integration:
+  max(du): 0.1
+  min(dt): 1e-15
+  max(dt): 1e-13
+"""
+
+
+def _full_test_settings(golden_dir, outdir, mag_config_every=False):
+    g = json.load(open(os.path.join(golden_dir, "golden.json")))["full_test"]
+    return g, {
+        "outputs": {"directory": str(outdir), "file_basename": "full_test", "evol_time_step": g["evol_time_step"],
+                    "final_time": g["final_time"], "mag_config_every": mag_config_every},
+        "mesh": {"filename": os.path.join(golden_dir, g["mesh"]), "length_unit": g["length_unit"],
+                 "volume_regions": {g["volume_region"]: {"K": g["K"], "uk": g["uk"]}}},
+        "initial_magnetization": g["initial_magnetization"],
+        "Bext": g["Bext"],
+        "time_integration": {"min(dt)": g["min_dt"], "max(dt)": g["max_dt"], "max(du)": g["max_du"]},
+    }
+
+
+def test_settings_yaml(tmp_path):
+    p = tmp_path / "s.yml"
+    p.write_text(YAML)
+    s = fg.settings_dump(p)
+    assert s["mesh"] == "some/dir/film.msh" and s["sim_name"] == "film"
+    assert s["final_time"] == 1e-11 and s["evol_time_step"] == 2e-13 and s["save_period"] == 0
+    assert s["evol_columns"] == ["t", "<Mx>", "E_tot"]
+    assert s["tol"] == 1e-8 and s["max_iter"] == 500 and s["dumax"] == 0.1 and s["dt_max"] == 1e-13
+    r = s["volume_regions"][0]
+    assert r["name"] == "film" and r["Ms"] == 8e5 and r["K"] == 1e4 and r["alpha"] == 0.02
+    assert np.allclose(r["uk"], [0, 0, 1])           # unit vectors are normalised
+    assert np.allclose(s["m0"], [2 ** -0.5, 2 ** -0.5, 0])
+    assert s["Bext"] == [0, 0, 0.005]
+    assert s["surface_regions"] == [{"name": "top", "Ks": 1e-3, "suppress_charges": True}]
+
+
+def test_settings_json_and_defaults(tmp_path, golden_dir):
+    g, st = _full_test_settings(golden_dir, tmp_path)
+    p = tmp_path / "s.json"
+    p.write_text(json.dumps(st))
+    s = fg.settings_dump(p)
+    assert s["tol"] == 1e-6 and s["max_iter"] == 700     # defaults of the reference
+    assert s["volume_regions"][0]["Ms"] == 795774.7 and s["volume_regions"][0]["alpha"] == 0.5
+    assert s["volume_regions"][0]["Ae"] == 1e-11
+    assert s["evol_columns"] == ["t", "<Mx>", "<My>", "<Mz>", "E_ex", "E_demag", "E_zeeman", "E_tot"]
+    assert s["dumax"] == g["max_du"]
+
+
+def test_settings_errors(tmp_path):
+    p = tmp_path / "bad.yml"
+    p.write_text("mesh:\n  filename: a.msh\n  volume_regions:\n    v: {Ms: 1}\nBext: [0, 0]\n")
+    with pytest.raises(fg.FgError) as e:
+        fg.settings_dump(p)
+    assert "three components" in str(e.value)
+    p.write_text("mesh:\n  filename: a.msh\n  volume_regions:\n    v: {Ms: 1}\ninitial_magnetization: [sin(x), 0, 1]\n")
+    with pytest.raises(fg.FgError):
+        fg.settings_dump(p)
+
+
+def _last_row(path):
+    rows = [l for l in open(path) if not l.startswith("#")]
+    return np.array([float(x) for x in rows[-1].split()])
+
+
+@pytest.mark.gpu
+def test_run_full_test_golden(tmp_path, golden_dir):
+    g, st = _full_test_settings(golden_dir, tmp_path)
+    p = tmp_path / "full_test.json"
+    p.write_text(json.dumps(st))
+    rep = fg.run(p, seed=g["seed"])
+    assert rep["steps"] > 0 and abs(rep["t"] - g["final_time"]) < 1e-20
+    last = _last_row(tmp_path / "full_test.evol")
+    exp = g["expected_5pt"]
+    assert np.linalg.norm(last[1:4] - np.array(exp["m"])) < g["threshold"]
+    assert abs((last[7] - exp["E_tot"]) / exp["E_tot"]) < g["threshold"]
+    hdr = [l for l in open(tmp_path / "full_test.evol") if l.startswith("## columns:")][0]
+    assert hdr.split(":", 1)[1].split() == ["t", "<Mx>", "<My>", "<Mz>", "E_ex", "E_demag", "E_zeeman", "E_tot"]
+
+
+@pytest.mark.gpu
+def test_sol_written_and_restarted(tmp_path, golden_dir):
+    g, st = _full_test_settings(golden_dir, tmp_path, mag_config_every=5)
+    st["outputs"]["final_time"] = 5e-12
+    p = tmp_path / "a.json"
+    p.write_text(json.dumps(st))
+    fg.run(p, seed=1)
+    sol = tmp_path / "full_test_iter5.sol"
+    text = open(sol).read().splitlines()
+    assert any(l.startswith("## time: ") for l in text)
+    data = np.array([[float(x) for x in l.split()] for l in text if not l.startswith("#")])
+    assert data.shape[1] == 5 and np.array_equal(data[:, 0], np.arange(len(data)))
+    assert np.allclose(np.linalg.norm(data[:, 1:4], axis=1), 1.0, atol=1e-6)
+    # restart from the snapshot: time is taken from its metadata
+    st2 = dict(st)
+    st2["initial_magnetization"] = str(sol)
+    st2["outputs"] = dict(st["outputs"], file_basename="restart", final_time=6e-12, mag_config_every=False)
+    p2 = tmp_path / "b.json"
+    p2.write_text(json.dumps(st2))
+    rep = fg.run(p2, seed=1)
+    assert abs(rep["t"] - 6e-12) < 1e-20
+    first = [l for l in open(tmp_path / "restart.evol") if not l.startswith("#")][0].split()
+    assert abs(float(first[0]) - 5e-12) < 1e-20
