@@ -64,6 +64,11 @@ class fg_step_report(C.Structure):
                 ("res0_fallback", C.c_double)]
 
 
+class fg_batch_report(C.Structure):
+    _fields_ = [("fails", C.c_int), ("first_fail", C.c_int), ("iters_max", C.c_int), ("refinements_max", C.c_int),
+                ("iters", C.c_longlong), ("refinements", C.c_longlong), ("vmax", C.c_double)]
+
+
 StepReport = dict
 
 _dp = C.POINTER(C.c_double)
@@ -107,6 +112,13 @@ SIGNATURES = {
     "fg_mlp_debug_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p]),
     "fg_mlp_nparam": (C.c_int, []),
+    "fg_batch_create": (C.c_int, [C.POINTER(fg_mesh), C.c_int, C.POINTER(fg_region), C.c_int,
+                                  C.POINTER(fg_tri_region), C.c_int, C.POINTER(fg_opts), C.POINTER(C.c_void_p)]),
+    "fg_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
+    "fg_batch_step": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(fg_step_report)]),
+    "fg_batch_compute_all": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fg_batch_run": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(fg_batch_report)]),
+    "fg_batch_run_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), _dp]),
 }
 
 
@@ -248,21 +260,30 @@ class Context:
     """One mesh (or batch) resident on the GPU; see include/fggpu.h."""
 
     def __init__(self, mesh, regions, tri_regions=None, **opts):
+        """mesh: one mesh dict, or a list of mesh dicts for a batch of independent samples
+        (fg_batch_create; the samples' nodes are concatenated in list order)."""
         L = fg_lib()
         self.L = L
         self._keep = []
-        xyz = np.ascontiguousarray(mesh["xyz"], dtype=np.float64)
-        tets = np.ascontiguousarray(mesh["tets"], dtype=np.int32)
-        treg = np.ascontiguousarray(mesh["tet_reg"], dtype=np.int32)
-        tris = np.ascontiguousarray(mesh.get("tris", np.zeros((0, 3))), dtype=np.int32).reshape(-1, 3)
-        freg = np.ascontiguousarray(mesh.get("tri_reg", np.zeros(0)), dtype=np.int32)
-        dms = np.ascontiguousarray(mesh.get("dMs", np.zeros(0)), dtype=np.float64)
-        self._keep += [xyz, tets, treg, tris, freg, dms]
-        m = fg_mesh(len(xyz), len(tets), len(tris), _ptr(xyz), _ptr(tets), _ptr(treg), _ptr(tris), _ptr(freg),
-                    _ptr(dms))
+        meshes = list(mesh) if isinstance(mesh, (list, tuple)) else [mesh]
+        self.batch = isinstance(mesh, (list, tuple))
+        cm = []
+        nfreg = 0
+        for one in meshes:
+            xyz = np.ascontiguousarray(one["xyz"], dtype=np.float64)
+            tets = np.ascontiguousarray(one["tets"], dtype=np.int32)
+            treg = np.ascontiguousarray(one["tet_reg"], dtype=np.int32)
+            tris = np.ascontiguousarray(one.get("tris", np.zeros((0, 3))), dtype=np.int32).reshape(-1, 3)
+            freg = np.ascontiguousarray(one.get("tri_reg", np.zeros(0)), dtype=np.int32)
+            dms = np.ascontiguousarray(one.get("dMs", np.zeros(0)), dtype=np.float64)
+            self._keep += [xyz, tets, treg, tris, freg, dms]
+            cm.append(fg_mesh(len(xyz), len(tets), len(tris), _ptr(xyz), _ptr(tets), _ptr(treg), _ptr(tris),
+                              _ptr(freg), _ptr(dms)))
+            if len(freg):
+                nfreg = max(nfreg, int(freg.max()) + 1)
         regs = [r if isinstance(r, fg_region) else make_region(**r) for r in regions]
         if tri_regions is None:
-            tri_regions = [make_tri_region() for _ in range(int(freg.max()) + 1 if len(freg) else 1)]
+            tri_regions = [make_tri_region() for _ in range(max(nfreg, 1))]
         tregs = [r if isinstance(r, fg_tri_region) else make_tri_region(**r) for r in tri_regions]
         R = (fg_region * len(regs))(*regs)
         T = (fg_tri_region * len(tregs))(*tregs)
@@ -274,11 +295,20 @@ class Context:
             setattr(o, k, v)
         self.opts = o
         h = C.c_void_p()
-        s = L.fg_create(C.byref(m), R, len(regs), T, len(tregs), C.byref(o), C.byref(h))
+        if self.batch:
+            M = (fg_mesh * len(cm))(*cm)
+            s = L.fg_batch_create(M, len(cm), R, len(regs), T, len(tregs), C.byref(o), C.byref(h))
+        else:
+            s = L.fg_create(C.byref(cm[0]), R, len(regs), T, len(tregs), C.byref(o), C.byref(h))
         if s != FG_OK:
             raise FgError(s, L.fg_last_error(None).decode())
         self.h = h
-        self.nn = len(xyz)
+        self.nn = sum(m.n_nodes for m in cm)
+        self.n_samples = len(cm)
+        off = np.zeros(self.n_samples + 1, dtype=np.int32)
+        ns = C.c_int()
+        self._check(L.fg_batch_info(h, C.byref(ns), _ptr(off)))
+        self.node_offsets = off
 
     def close(self):
         if getattr(self, "h", None):
@@ -304,6 +334,51 @@ class Context:
         phi, phiv = np.zeros(self.nn), np.zeros(self.nn)
         self._check(self.L.fg_get_state(self.h, which, _ptr(u), _ptr(v), _ptr(phi), _ptr(phiv)))
         return {"u": u, "v": v, "phi": phi, "phiv": phiv}
+
+    @staticmethod
+    def _sample_steps(dt, prefactor, Hext, angle, shape):
+        """(..., 6) float64 rows laid out as fg_sample_step: dt, prefactor, Hext[3], angle."""
+        a = np.empty(shape + (6,), dtype=np.float64)
+        a[..., 0] = dt
+        a[..., 1] = prefactor
+        a[..., 2:5] = Hext
+        a[..., 5] = angle
+        return np.ascontiguousarray(a)
+
+    def batch_step(self, dt, prefactor, Hext, angle):
+        """fg_batch_step; every argument broadcasts to the samples (Hext: (n_samples, 3))."""
+        ns = self.n_samples
+        a = self._sample_steps(dt, prefactor, Hext, angle, (ns,))
+        reps = (fg_step_report * ns)()
+        s = self.L.fg_batch_step(self.h, _ptr(a), reps)
+        if s == FG_ETIMEDOUT or s > FG_ETIMEDOUT:
+            self._check(s)
+        return s, [{k: getattr(r, k) for k, _ in fg_step_report._fields_} for r in reps]
+
+    def batch_compute_all(self, Hext=None, energies=True):
+        ns = self.n_samples
+        H = None if Hext is None else np.ascontiguousarray(np.broadcast_to(Hext, (ns, 3)), dtype=np.float64)
+        E = np.zeros((ns, 4)) if energies else None
+        self._check(self.L.fg_batch_compute_all(self.h, _ptr(H), _ptr(E)))
+        return E
+
+    def batch_run(self, dt, prefactor, Hext, angles):
+        """fg_batch_run over angles.shape[0] steps; angles: (n_steps, n_samples); dt, prefactor
+        and Hext broadcast to (n_steps, n_samples[, 3])."""
+        angles = np.asarray(angles, dtype=np.float64)
+        nsteps = angles.shape[0]
+        a = self._sample_steps(dt, prefactor, Hext, angles, angles.shape)
+        reps = (fg_batch_report * self.n_samples)()
+        s = self.L.fg_batch_run(self.h, nsteps, _ptr(a), reps)
+        if s == FG_ETIMEDOUT or s > FG_ETIMEDOUT:
+            self._check(s)
+        return s, [{k: getattr(r, k) for k, _ in fg_batch_report._fields_} for r in reps]
+
+    def batch_run_info(self):
+        g = C.c_int()
+        ms = C.c_double()
+        self._check(self.L.fg_batch_run_info(self.h, C.byref(g), C.byref(ms)))
+        return bool(g.value), ms.value
 
     def step(self, dt, prefactor, Hext, angle):
         """Returns the report dict; report['status'] is FG_OK or a solver status."""

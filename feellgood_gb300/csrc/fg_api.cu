@@ -157,6 +157,16 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
                        int ntreg, const fg_opts *opts) {
     Ctx &c = h->c;
     if (opts) c.opts = *opts; else fg_opts_default(&c.opts);
+    if (c.batch) {
+        // a batch runs the FP32 + refinement solver and a forest FMM (one tree per sample)
+        if (c.opts.precision != FG_PREC_FP32_REFINE || c.opts.learned_guess ||
+            c.opts.demag == FG_DEMAG_DIRECT) {
+            c.err = "fg_batch_create: a batch needs precision FG_PREC_FP32_REFINE, demag FMM and no learned guess";
+            return FG_EINVAL;
+        }
+        c.opts.demag = FG_DEMAG_FMM;
+        c.opts.profile = 0;
+    }
     if (!m || !regs || nreg <= 0 || m->n_nodes <= 0 || m->n_tets <= 0 || !m->xyz || !m->tet4 || !m->tet_region) {
         c.err = "fg_create: missing mesh or region data";
         return FG_EINVAL;
@@ -476,6 +486,10 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
             return sm;
         }
     }
+    if (c.batch) {
+        int sb = batch_setup(c, htet, htri);
+        if (sb != FG_OK) return sb;
+    }
     int demag = c.opts.demag;
     if (demag == FG_DEMAG_AUTO) demag = ((double)c.nsrc * c.n_mag_nodes > 4e9) ? FG_DEMAG_FMM : FG_DEMAG_DIRECT;
     c.opts.demag = demag;
@@ -487,12 +501,18 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     return FG_OK;
 }
 
-int fg_create(const fg_mesh *mesh, const fg_region *regions, int n_regions, const fg_tri_region *tri_regions,
-              int n_tri_regions, const fg_opts *opts, fg_ctx **out) {
+static int create_common(const fg_mesh *mesh, const fg_region *regions, int n_regions,
+                         const fg_tri_region *tri_regions, int n_tri_regions, const fg_opts *opts,
+                         std::vector<int> *node_seg, int nseg, fg_ctx **out) {
     if (!out) return FG_EINVAL;
     *out = nullptr;
     fg_ctx *h = new (std::nothrow) fg_ctx();
     if (!h) return FG_ENOMEM;
+    if (node_seg) {
+        h->c.batch = true;
+        h->c.nseg = nseg;
+        h->c.h_node_seg = std::move(*node_seg);
+    }
     int s;
     try {
         s = create_impl(h, mesh, regions, n_regions, tri_regions, n_tri_regions, opts);
@@ -512,6 +532,75 @@ int fg_create(const fg_mesh *mesh, const fg_region *regions, int n_regions, cons
     return FG_OK;
 }
 
+int fg_create(const fg_mesh *mesh, const fg_region *regions, int n_regions, const fg_tri_region *tri_regions,
+              int n_tri_regions, const fg_opts *opts, fg_ctx **out) {
+    return create_common(mesh, regions, n_regions, tri_regions, n_tri_regions, opts, nullptr, 1, out);
+}
+
+int fg_batch_create(const fg_mesh *meshes, int n_samples, const fg_region *regions, int n_regions,
+                    const fg_tri_region *tri_regions, int n_tri_regions, const fg_opts *opts, fg_ctx **out) {
+    if (!out) return FG_EINVAL;
+    *out = nullptr;
+    if (!meshes || n_samples <= 0) {
+        g_create_error = "fg_batch_create: no samples";
+        return FG_EINVAL;
+    }
+    // the samples' meshes concatenated: a block-diagonal system over disjoint node sets
+    std::vector<double> xyz, dMs;
+    std::vector<int32_t> tet4, treg, tri3, freg;
+    std::vector<int> node_seg;
+    try {
+        int off = 0;
+        for (int g = 0; g < n_samples; g++) {
+            const fg_mesh &m = meshes[g];
+            if (m.n_nodes <= 0 || m.n_tets <= 0 || !m.xyz || !m.tet4 || !m.tet_region ||
+                (m.n_tris > 0 && (!m.tri3 || !m.tri_region || !m.tri_dMs))) {
+                g_create_error = "fg_batch_create: sample " + std::to_string(g) + " has incomplete mesh data";
+                return FG_EINVAL;
+            }
+            xyz.insert(xyz.end(), m.xyz, m.xyz + 3 * (size_t)m.n_nodes);
+            for (size_t k = 0; k < 4 * (size_t)m.n_tets; k++) {
+                const int v = m.tet4[k];
+                if (v < 0 || v >= m.n_nodes) {
+                    g_create_error = "fg_batch_create: tet node index out of range in sample " + std::to_string(g);
+                    return FG_EMESH;
+                }
+                tet4.push_back(v + off);
+            }
+            treg.insert(treg.end(), m.tet_region, m.tet_region + m.n_tets);
+            for (size_t k = 0; k < 3 * (size_t)m.n_tris; k++) {
+                const int v = m.tri3[k];
+                if (v < 0 || v >= m.n_nodes) {
+                    g_create_error = "fg_batch_create: triangle node out of range in sample " + std::to_string(g);
+                    return FG_EMESH;
+                }
+                tri3.push_back(v + off);
+            }
+            if (m.n_tris > 0) {
+                freg.insert(freg.end(), m.tri_region, m.tri_region + m.n_tris);
+                dMs.insert(dMs.end(), m.tri_dMs, m.tri_dMs + m.n_tris);
+            }
+            node_seg.insert(node_seg.end(), m.n_nodes, g);
+            off += m.n_nodes;
+        }
+    } catch (const std::bad_alloc &) {
+        g_create_error = "host allocation failed";
+        return FG_ENOMEM;
+    }
+    fg_mesh u;
+    std::memset(&u, 0, sizeof(u));
+    u.n_nodes = (int)node_seg.size();
+    u.n_tets = (int)treg.size();
+    u.n_tris = (int)freg.size();
+    u.xyz = xyz.data();
+    u.tet4 = tet4.data();
+    u.tet_region = treg.data();
+    u.tri3 = u.n_tris ? tri3.data() : nullptr;
+    u.tri_region = u.n_tris ? freg.data() : nullptr;
+    u.tri_dMs = u.n_tris ? dMs.data() : nullptr;
+    return create_common(&u, regions, n_regions, tri_regions, n_tri_regions, opts, &node_seg, n_samples, out);
+}
+
 void fg_destroy(fg_ctx *h) {
     if (!h) return;
     Ctx &c = h->c;
@@ -525,6 +614,7 @@ void fg_destroy(fg_ctx *h) {
         if (p) cudaFree(p);
     fmm_free(c);
     mlp_free(c);
+    batch_free(c);
     if (c.heff) cudaFree(c.heff);
     if (c.hres) cudaFreeHost(c.hres);
     if (c.hepart) cudaFreeHost(c.hepart);
@@ -567,6 +657,10 @@ int fg_get_state(const fg_ctx *hc, int which, double *u, double *v, double *phi,
 int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double basis_angle, fg_step_report *rep) {
     if (!h || !Hext || !(dt > 0)) return FG_EINVAL;
     Ctx &c = h->c;
+    if (c.batch) {
+        c.err = "fg_step: a batch context steps with fg_batch_step";
+        return FG_EINVAL;
+    }
     CK(cudaEventRecord(c.ev[0], c.stream));
     CK(launch_tet(c, dt, Hext));
     CK(launch_node(c, basis_angle));

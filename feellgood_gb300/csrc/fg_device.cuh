@@ -91,6 +91,26 @@ __device__ __forceinline__ void grid_sum(const double *partial, int G, double (&
     __syncthreads();
 }
 
+// Sum of the partials of blocks [b0, b1) only (one sample of a batch), same fixed order.
+template <int NV>
+__device__ __forceinline__ void range_sum(const double *partial, int G, int b0, int b1, double (&out)[NV]) {
+    __shared__ double res[NV];
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double x = 0.0;
+            for (int b = b0 + lane; b < b1; b += 32) x += *(volatile const double *)&partial[k * G + b];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) res[k] = x;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; k++) out[k] = res[k];
+    __syncthreads();
+}
+
 __device__ __forceinline__ double dmax_reduce_block(double v) {
     __shared__ double sh[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

@@ -59,7 +59,8 @@ struct FmmTree {
     int *leaf_src = nullptr, *leaf_tgt = nullptr, *tgt_node = nullptr;
     void *sloc = nullptr;  // 4 x nsrc: leaf-local source coordinates (T), w unused
     void *tloc = nullptr;  // 4 x ntgt: leaf-local target coordinates (T)
-    int *leaf_ijk = nullptr;  // 3 x nleaf integer leaf coordinates
+    int *leaf_ijk = nullptr;  // 3 x nleaf integer leaf coordinates (within the leaf's own tree)
+    double *leaf_scale = nullptr;  // 1 / physical leaf width of the leaf's tree
     int *m2l_tab = nullptr;   // [ncell][343] source cell or -1
     int *m2m_tab = nullptr;   // [ncell][8] child per octant or -1
     int *l2l_tab = nullptr;   // [ncell][8] parent at the own octant, -1 elsewhere
@@ -301,7 +302,8 @@ template <typename T>
 __global__ void __launch_bounds__(128) k_l2p_p2p(int nleaf, const int *__restrict__ leaf_src,
                                                  const int *__restrict__ leaf_tgt, const int *__restrict__ tgt_node,
                                                  const T *__restrict__ tloc, const T *__restrict__ sloc,
-                                                 const int *__restrict__ leaf_ijk, int leaf0, double scale,
+                                                 const int *__restrict__ leaf_ijk, int leaf0,
+                                                 const double *__restrict__ leaf_scale,
                                                  const int *__restrict__ near_ptr, const int *__restrict__ near_leaf,
                                                  const T *__restrict__ F, double *__restrict__ pot) {
     constexpr int NT = 16;
@@ -361,7 +363,7 @@ __global__ void __launch_bounds__(128) k_l2p_p2p(int nleaf, const int *__restric
                 if (m == 0) far += Fl[ridx(n, 0, 0)] * re;
                 else far += T(2) * (Fl[ridx(n, m, 0)] * re + Fl[ridx(n, m, 1)] * im);
             });
-            pot[tgt_node[tb + lane]] = (double(far) + nr) * scale;
+            pot[tgt_node[tb + lane]] = (double(far) + nr) * leaf_scale[leaf];
         }
     }
 }
@@ -459,9 +461,42 @@ static const FmmOps &fmm_ops() {
 }
 
 void fmm_free(Ctx &c);
-static int fmm_build_level(Ctx &c, int L);
+static int fmm_build_forest(Ctx &c, int L);
 template <typename T>
 static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t);
+
+// Points of each sample (sources and target nodes) and the sample's root cube. A batch of
+// independent meshes gets one octree per sample (a forest); a single mesh is one tree.
+struct SamplePts {
+    std::vector<int> src, tgt;  // source indices, target node ids
+    double c0[3] = {0, 0, 0}, side = 1.0;
+};
+
+static std::vector<SamplePts> split_samples(const Ctx &c) {
+    const int nseg = std::max(1, c.nseg);
+    std::vector<SamplePts> S(nseg);
+    for (int s = 0; s < c.nsrc; s++) S[c.h_src_seg.empty() ? 0 : c.h_src_seg[s]].src.push_back(s);
+    for (int i = 0; i < c.nn; i++)
+        if (c.h_mag[i]) S[c.h_node_seg.empty() ? 0 : c.h_node_seg[i]].tgt.push_back(i);
+    for (auto &P : S) {
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int s : P.src)
+            for (int d = 0; d < 3; d++) {
+                lo[d] = std::min(lo[d], c.h_src_xyz[3 * (size_t)s + d]);
+                hi[d] = std::max(hi[d], c.h_src_xyz[3 * (size_t)s + d]);
+            }
+        for (int i : P.tgt)
+            for (int d = 0; d < 3; d++) {
+                lo[d] = std::min(lo[d], c.h_xyz[3 * (size_t)i + d]);
+                hi[d] = std::max(hi[d], c.h_xyz[3 * (size_t)i + d]);
+            }
+        if (P.src.empty() && P.tgt.empty()) continue;
+        P.side = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2])) * (1.0 + 1e-9);
+        if (!(P.side > 0)) P.side = 1.0;
+        for (int d = 0; d < 3; d++) P.c0[d] = 0.5 * (lo[d] + hi[d]);
+    }
+    return S;
+}
 
 int fmm_build(Ctx &c) {
     const bool fp32 = (c.opts.precision == FG_PREC_FP32_REFINE);
@@ -469,55 +504,40 @@ int fmm_build(Ctx &c) {
         c.err = "fmm: only expansion order P=9 is built";
         return FG_EINVAL;
     }
-    const int ns = c.nsrc;
-    // root cube over sources and targets
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int s = 0; s < ns; s++)
-        for (int d = 0; d < 3; d++) {
-            lo[d] = std::min(lo[d], c.h_src_xyz[3 * s + d]);
-            hi[d] = std::max(hi[d], c.h_src_xyz[3 * s + d]);
+    const std::vector<SamplePts> S = split_samples(c);
+    // mean number of sources per occupied leaf at each depth, over all samples
+    std::vector<double> occ(11, 0.0);
+    for (const SamplePts &P : S) {
+        const int n10 = 1 << 10;
+        std::vector<uint64_t> keys;
+        keys.reserve(P.src.size());
+        for (int s : P.src) {
+            int ijk[3];
+            for (int d = 0; d < 3; d++)
+                ijk[d] = std::min(n10 - 1, std::max(0, (int)(((c.h_src_xyz[3 * (size_t)s + d] - P.c0[d]) / P.side + 0.5) * n10)));
+            keys.push_back(morton(ijk[0], ijk[1], ijk[2]));
         }
-    for (int i = 0; i < c.nn; i++)
-        if (c.h_mag[i])
-            for (int d = 0; d < 3; d++) {
-                lo[d] = std::min(lo[d], c.h_xyz[3 * i + d]);
-                hi[d] = std::max(hi[d], c.h_xyz[3 * i + d]);
-            }
-    const double side = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2])) * (1.0 + 1e-9);
-    const double cen[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2])};
-    // candidate depths: mean sources per occupied leaf near the requested size (autotuned
-    // over a neighbourhood when fmm_leaf is 0)
-    const int n10 = 1 << 10;
-    std::vector<uint64_t> keys(ns);
-    for (int s = 0; s < ns; s++) {
-        int ijk[3];
-        for (int d = 0; d < 3; d++)
-            ijk[d] = std::min(n10 - 1, std::max(0, (int)(((c.h_src_xyz[3 * s + d] - cen[d]) / side + 0.5) * n10)));
-        keys[s] = morton(ijk[0], ijk[1], ijk[2]);
+        std::sort(keys.begin(), keys.end());
+        for (int l = 2; l <= 10; l++) {
+            const int sh = 3 * (10 - l);
+            uint64_t prev = ~0ull;
+            for (uint64_t k : keys)
+                if ((k >> sh) != prev) { occ[l] += 1; prev = k >> sh; }
+        }
     }
-    std::sort(keys.begin(), keys.end());
-    std::vector<double> mean(11, 0.0);
-    for (int l = 2; l <= 10; l++) {
-        const int sh = 3 * (10 - l);
-        size_t occ = 0;
-        uint64_t prev = ~0ull;
-        for (uint64_t k : keys)
-            if ((k >> sh) != prev) { occ++; prev = k >> sh; }
-        mean[l] = ns / std::max<double>(1.0, (double)occ);
-    }
-    keys.clear();
-    keys.shrink_to_fit();
     auto closest = [&](double target) {
         int best = 2;
         double bd = 1e300;
         for (int l = 2; l <= 10; l++) {
-            const double d = std::fabs(std::log(mean[l] / target));
+            const double mean = c.nsrc / std::max(1.0, occ[l]);
+            const double d = std::fabs(std::log(mean / target));
             if (d < bd) { bd = d; best = l; }
         }
         return best;
     };
     std::vector<int> cands;
-    if (c.opts.fmm_leaf > 0) cands.push_back(closest(c.opts.fmm_leaf));
+    if (c.opts.fmm_leaf < 0) cands.push_back(std::min(10, std::max(2, -c.opts.fmm_leaf)));  // fixed depth
+    else if (c.opts.fmm_leaf > 0) cands.push_back(closest(c.opts.fmm_leaf));
     else {
         const int l0 = closest(fp32 ? 400.0 : 300.0);
         for (int l = std::max(2, l0 - 1); l <= std::min(10, l0 + 1); l++) cands.push_back(l);
@@ -530,9 +550,7 @@ int fmm_build(Ctx &c) {
         FmmTree *t = new FmmTree();
         c.fmm = t;
         t->fp32 = fp32;
-        t->s0 = side;
-        for (int d = 0; d < 3; d++) t->c0[d] = cen[d];
-        int s = fmm_build_level(c, cands[k]);
+        int s = fmm_build_forest(c, cands[k]);
         if (s != FG_OK) return s;
         if (cands.size() == 1) return FG_OK;
         // autotune: time two evaluations with the current charges (values do not matter)
@@ -555,157 +573,186 @@ int fmm_build(Ctx &c) {
     FmmTree *t = new FmmTree();
     c.fmm = t;
     t->fp32 = fp32;
-    t->s0 = side;
-    for (int d = 0; d < 3; d++) t->c0[d] = cen[d];
-    return fmm_build_level(c, bestL);
+    return fmm_build_forest(c, bestL);
 }
 
-static int fmm_build_level(Ctx &c, int L) {
+// Per-sample octree of depth L (host vectors, sample-local indices).
+struct TreeH {
+    std::vector<uint64_t> leaf_keys;
+    std::vector<std::vector<uint64_t>> keys;  // per level
+    std::vector<std::pair<uint64_t, int>> sk, tk;  // (leaf key, source index / node id), sorted
+    std::vector<int> leaf_src, leaf_tgt;           // CSR over sk / tk
+};
+
+static int fmm_build_forest(Ctx &c, int L) {
     FmmTree *t = static_cast<FmmTree *>(c.fmm);
     const bool fp32 = t->fp32;
     t->L = L;
-    const int ns = c.nsrc;
-    std::vector<int> mnodes;
-    for (int i = 0; i < c.nn; i++)
-        if (c.h_mag[i]) mnodes.push_back(i);
-    const int nt = (int)mnodes.size();
     const int nside = 1 << L;
-    auto cell_of = [&](const double *p, int *ijk) {
-        for (int d = 0; d < 3; d++)
-            ijk[d] = std::min(nside - 1, std::max(0, (int)(((p[d] - t->c0[d]) / t->s0 + 0.5) * nside)));
-        return morton(ijk[0], ijk[1], ijk[2]);
-    };
-    std::vector<std::pair<uint64_t, int>> sk(ns), tk(nt);
-    int ijk[3];
-    for (int s = 0; s < ns; s++) sk[s] = {cell_of(&c.h_src_xyz[3 * s], ijk), s};
-    for (int k = 0; k < nt; k++) tk[k] = {cell_of(&c.h_xyz[3 * mnodes[k]], ijk), mnodes[k]};
-    std::sort(sk.begin(), sk.end());
-    std::sort(tk.begin(), tk.end());
-    std::vector<uint64_t> lk;
-    {
+    const std::vector<SamplePts> SP = split_samples(c);
+    const int nseg = (int)SP.size();
+    t->s0 = SP[0].side;
+    for (int d = 0; d < 3; d++) t->c0[d] = SP[0].c0[d];
+    std::vector<TreeH> T(nseg);
+    for (int g = 0; g < nseg; g++) {
+        const SamplePts &P = SP[g];
+        TreeH &H = T[g];
+        auto cell_of = [&](const double *p) {
+            int ijk[3];
+            for (int d = 0; d < 3; d++) ijk[d] = std::min(nside - 1, std::max(0, (int)(((p[d] - P.c0[d]) / P.side + 0.5) * nside)));
+            return morton(ijk[0], ijk[1], ijk[2]);
+        };
+        for (int s : P.src) H.sk.push_back({cell_of(&c.h_src_xyz[3 * (size_t)s]), s});
+        for (int i : P.tgt) H.tk.push_back({cell_of(&c.h_xyz[3 * (size_t)i]), i});
+        std::sort(H.sk.begin(), H.sk.end());
+        std::sort(H.tk.begin(), H.tk.end());
         std::vector<uint64_t> a, b;
-        for (auto &p : sk) if (a.empty() || a.back() != p.first) a.push_back(p.first);
-        for (auto &p : tk) if (b.empty() || b.back() != p.first) b.push_back(p.first);
-        std::set_union(a.begin(), a.end(), b.begin(), b.end(), std::back_inserter(lk));
+        for (auto &p : H.sk) if (a.empty() || a.back() != p.first) a.push_back(p.first);
+        for (auto &p : H.tk) if (b.empty() || b.back() != p.first) b.push_back(p.first);
+        std::set_union(a.begin(), a.end(), b.begin(), b.end(), std::back_inserter(H.leaf_keys));
+        H.leaf_src.assign(H.leaf_keys.size() + 1, 0);
+        H.leaf_tgt.assign(H.leaf_keys.size() + 1, 0);
+        size_t ia = 0, ib = 0;
+        for (size_t l = 0; l < H.leaf_keys.size(); l++) {
+            H.leaf_src[l] = (int)ia;
+            while (ia < H.sk.size() && H.sk[ia].first == H.leaf_keys[l]) ia++;
+            H.leaf_tgt[l] = (int)ib;
+            while (ib < H.tk.size() && H.tk[ib].first == H.leaf_keys[l]) ib++;
+        }
+        H.leaf_src.back() = (int)ia;
+        H.leaf_tgt.back() = (int)ib;
+        H.keys.assign(L + 1, {});
+        H.keys[L] = H.leaf_keys;
+        for (int l = L - 1; l >= 2; l--)
+            for (uint64_t k : H.keys[l + 1])
+                if (H.keys[l].empty() || H.keys[l].back() != (k >> 3)) H.keys[l].push_back(k >> 3);
     }
-    const int nleaf = (int)lk.size();
-    t->nleaf = nleaf;
-    std::vector<int> leaf_src(nleaf + 1, 0), leaf_tgt(nleaf + 1, 0), leaf_ijk(3 * (size_t)nleaf);
-    {
-        size_t a = 0, b = 0;
-        for (int l = 0; l < nleaf; l++) {
-            leaf_src[l] = (int)a;
-            while (a < sk.size() && sk[a].first == lk[l]) a++;
-            leaf_tgt[l] = (int)b;
-            while (b < tk.size() && tk[b].first == lk[l]) b++;
-            decode(lk[l], &leaf_ijk[3 * (size_t)l]);
-        }
-        leaf_src[nleaf] = (int)a;
-        leaf_tgt[nleaf] = (int)b;
-    }
-    // leaf-local coordinates in leaf units
-    const double w = t->s0 / nside;
-    auto local = [&](const double *p, const int *lijk, double *o) {
-        for (int d = 0; d < 3; d++) {
-            const double cc = t->c0[d] - 0.5 * t->s0 + (lijk[d] + 0.5) * w;
-            o[d] = (p[d] - cc) / w;
-        }
-    };
-    std::vector<int> src_dst(ns), tgt_node(nt);
-    std::vector<double> sloc(4 * (size_t)ns, 0.0), tloc(4 * (size_t)nt, 0.0);
-    for (int l = 0; l < nleaf; l++) {
-        for (int k = leaf_src[l]; k < leaf_src[l + 1]; k++) {
-            src_dst[sk[k].second] = k;
-            local(&c.h_src_xyz[3 * (size_t)sk[k].second], &leaf_ijk[3 * (size_t)l], &sloc[4 * (size_t)k]);
-        }
-        for (int k = leaf_tgt[l]; k < leaf_tgt[l + 1]; k++) {
-            tgt_node[k] = tk[k].second;
-            local(&c.h_xyz[3 * (size_t)tk[k].second], &leaf_ijk[3 * (size_t)l], &tloc[4 * (size_t)k]);
-        }
-    }
-    // levels 2..L
-    std::vector<std::vector<uint64_t>> keys(L + 1);
-    keys[L] = lk;
-    for (int l = L - 1; l >= 2; l--)
-        for (uint64_t k : keys[l + 1]) {
-            const uint64_t pk = k >> 3;
-            if (keys[l].empty() || keys[l].back() != pk) keys[l].push_back(pk);
-        }
+    // global numbering: level-major, then sample, then Morton order
     t->lev_begin.assign(L + 2, 0);
-    for (int l = 2; l <= L; l++) t->lev_begin[l + 1] = t->lev_begin[l] + (int)keys[l].size();
-    const int ncell = t->lev_begin[L + 1];
+    std::vector<std::vector<int>> base(L + 1, std::vector<int>(nseg, 0));  // first global id of (level, sample)
+    int next = 0;
+    for (int l = 2; l <= L; l++) {
+        t->lev_begin[l] = next;
+        for (int g = 0; g < nseg; g++) {
+            base[l][g] = next;
+            next += (int)T[g].keys[l].size();
+        }
+    }
+    t->lev_begin[L + 1] = next;
+    const int ncell = next;
     t->ncell = ncell;
     t->leaf0 = t->lev_begin[L];
-    std::vector<std::unordered_map<uint64_t, int>> where(L + 1);
-    for (int l = 2; l <= L; l++) {
-        where[l].reserve(keys[l].size() * 2);
-        for (size_t i = 0; i < keys[l].size(); i++) where[l][keys[l][i]] = t->lev_begin[l] + (int)i;
-    }
+    int nleaf = ncell - t->leaf0;
+    t->nleaf = nleaf;
+    std::vector<int> leaf_src(nleaf + 1, 0), leaf_tgt(nleaf + 1, 0), leaf_ijk(3 * (size_t)nleaf, 0);
+    std::vector<double> leaf_scale(nleaf, 0.0);
+    std::vector<int> src_dst(c.nsrc, 0), tgt_node;
+    std::vector<double> sloc(4 * (size_t)c.nsrc, 0.0), tloc;
     std::vector<int> nsub_src(ncell, 0), nsub_tgt(ncell, 0);
-    for (int l = 0; l < nleaf; l++) {
-        nsub_src[t->leaf0 + l] = leaf_src[l + 1] - leaf_src[l];
-        nsub_tgt[t->leaf0 + l] = leaf_tgt[l + 1] - leaf_tgt[l];
-    }
     std::vector<int> m2m_tab((size_t)ncell * 8, -1), l2l_tab((size_t)ncell * 8, -1);
-    for (int l = L; l >= 3; l--)
-        for (size_t i = 0; i < keys[l].size(); i++) {
-            const int g = t->lev_begin[l] + (int)i;
-            const int p = where[l - 1][keys[l][i] >> 3];
-            const int oc = (int)(keys[l][i] & 7);
-            nsub_src[p] += nsub_src[g];
-            nsub_tgt[p] += nsub_tgt[g];
-            if (nsub_src[g] > 0) m2m_tab[(size_t)p * 8 + oc] = g;
-            l2l_tab[(size_t)g * 8 + oc] = p;
-        }
-    // M2L table: offset = target - source (cell units), code = (dx+3)*49 + (dy+3)*7 + (dz+3)
     std::vector<int> m2l_tab((size_t)ncell * NCODE_M2L, -1);
-    size_t nm2l = 0;
-    for (int l = 2; l <= L; l++) {
-        const int n = 1 << l;
-        for (size_t i = 0; i < keys[l].size(); i++) {
-            const int g = t->lev_begin[l] + (int)i;
-            if (nsub_tgt[g] == 0) continue;
-            decode(keys[l][i], ijk);
-            const int px = ijk[0] >> 1, py = ijk[1] >> 1, pz = ijk[2] >> 1;
-            for (int ax = 2 * (px - 1); ax <= 2 * (px + 1) + 1; ax++)
-                for (int ay = 2 * (py - 1); ay <= 2 * (py + 1) + 1; ay++)
-                    for (int az = 2 * (pz - 1); az <= 2 * (pz + 1) + 1; az++) {
-                        if (ax < 0 || ay < 0 || az < 0 || ax >= n || ay >= n || az >= n) continue;
-                        const int dx = ijk[0] - ax, dy = ijk[1] - ay, dz = ijk[2] - az;
-                        if (std::abs(dx) <= 1 && std::abs(dy) <= 1 && std::abs(dz) <= 1) continue;
-                        auto it = where[l].find(morton(ax, ay, az));
-                        if (it == where[l].end() || nsub_src[it->second] == 0) continue;
-                        m2l_tab[(size_t)g * NCODE_M2L + (dx + 3) * 49 + (dy + 3) * 7 + (dz + 3)] = it->second;
-                        nm2l++;
-                    }
-        }
-    }
-    t->n_m2l = nm2l;
     std::vector<int> near_ptr(nleaf + 1, 0), near_leaf;
-    t->n_p2p_pairs = 0;
-    for (int lf = 0; lf < nleaf; lf++) {
-        if (leaf_tgt[lf + 1] > leaf_tgt[lf]) {
-            const int *q = &leaf_ijk[3 * (size_t)lf];
-            for (int dx = -1; dx <= 1; dx++)
-                for (int dy = -1; dy <= 1; dy++)
-                    for (int dz = -1; dz <= 1; dz++) {
-                        const int ax = q[0] + dx, ay = q[1] + dy, az = q[2] + dz;
-                        if (ax < 0 || ay < 0 || az < 0 || ax >= nside || ay >= nside || az >= nside) continue;
-                        auto it = where[L].find(morton(ax, ay, az));
-                        if (it == where[L].end()) continue;
-                        const int nl = it->second - t->leaf0;
-                        if (leaf_src[nl + 1] == leaf_src[nl]) continue;
-                        near_leaf.push_back(nl);
-                        t->n_p2p_pairs += (size_t)(leaf_src[nl + 1] - leaf_src[nl]) * (leaf_tgt[lf + 1] - leaf_tgt[lf]);
-                    }
+    size_t src_off = 0, tgt_off = 0, nm2l = 0, np2p = 0;
+    int ijk[3];
+    for (int g = 0; g < nseg; g++) {
+        TreeH &H = T[g];
+        const SamplePts &P = SP[g];
+        const double w = P.side / nside;
+        std::vector<std::unordered_map<uint64_t, int>> where(L + 1);
+        for (int l = 2; l <= L; l++) {
+            where[l].reserve(H.keys[l].size() * 2);
+            for (size_t i = 0; i < H.keys[l].size(); i++) where[l][H.keys[l][i]] = base[l][g] + (int)i;
         }
-        near_ptr[lf + 1] = (int)near_leaf.size();
+        const int lf0 = base[L][g] - t->leaf0;  // first global leaf index of the sample
+        for (size_t l = 0; l < H.leaf_keys.size(); l++) {
+            const int gl = lf0 + (int)l;
+            leaf_src[gl] = (int)src_off + H.leaf_src[l];
+            leaf_tgt[gl] = (int)tgt_off + H.leaf_tgt[l];
+            decode(H.leaf_keys[l], &leaf_ijk[3 * (size_t)gl]);
+            leaf_scale[gl] = 1.0 / w;
+            const int *q = &leaf_ijk[3 * (size_t)gl];
+            double cc[3];
+            for (int d = 0; d < 3; d++) cc[d] = P.c0[d] - 0.5 * P.side + (q[d] + 0.5) * w;
+            for (int k = H.leaf_src[l]; k < H.leaf_src[l + 1]; k++) {
+                const size_t gk = src_off + k;
+                const int s = H.sk[k].second;
+                src_dst[s] = (int)gk;
+                for (int d = 0; d < 3; d++) sloc[4 * gk + d] = (c.h_src_xyz[3 * (size_t)s + d] - cc[d]) / w;
+            }
+            for (int k = H.leaf_tgt[l]; k < H.leaf_tgt[l + 1]; k++) {
+                const int i = H.tk[k].second;
+                tgt_node.push_back(i);
+                for (int d = 0; d < 3; d++) tloc.push_back((c.h_xyz[3 * (size_t)i + d] - cc[d]) / w);
+                tloc.push_back(0.0);
+            }
+            nsub_src[base[L][g] + (int)l] = H.leaf_src[l + 1] - H.leaf_src[l];
+            nsub_tgt[base[L][g] + (int)l] = H.leaf_tgt[l + 1] - H.leaf_tgt[l];
+        }
+        for (int l = L; l >= 3; l--)
+            for (size_t i = 0; i < H.keys[l].size(); i++) {
+                const int gc = base[l][g] + (int)i;
+                const int p = where[l - 1][H.keys[l][i] >> 3];
+                const int oc = (int)(H.keys[l][i] & 7);
+                nsub_src[p] += nsub_src[gc];
+                nsub_tgt[p] += nsub_tgt[gc];
+                if (nsub_src[gc] > 0) m2m_tab[(size_t)p * 8 + oc] = gc;
+                l2l_tab[(size_t)gc * 8 + oc] = p;
+            }
+        for (int l = 2; l <= L; l++) {
+            const int n = 1 << l;
+            for (size_t i = 0; i < H.keys[l].size(); i++) {
+                const int gc = base[l][g] + (int)i;
+                if (nsub_tgt[gc] == 0) continue;
+                decode(H.keys[l][i], ijk);
+                const int px = ijk[0] >> 1, py = ijk[1] >> 1, pz = ijk[2] >> 1;
+                for (int ax = 2 * (px - 1); ax <= 2 * (px + 1) + 1; ax++)
+                    for (int ay = 2 * (py - 1); ay <= 2 * (py + 1) + 1; ay++)
+                        for (int az = 2 * (pz - 1); az <= 2 * (pz + 1) + 1; az++) {
+                            if (ax < 0 || ay < 0 || az < 0 || ax >= n || ay >= n || az >= n) continue;
+                            const int dx = ijk[0] - ax, dy = ijk[1] - ay, dz = ijk[2] - az;
+                            if (std::abs(dx) <= 1 && std::abs(dy) <= 1 && std::abs(dz) <= 1) continue;
+                            auto it = where[l].find(morton(ax, ay, az));
+                            if (it == where[l].end() || nsub_src[it->second] == 0) continue;
+                            m2l_tab[(size_t)gc * NCODE_M2L + (dx + 3) * 49 + (dy + 3) * 7 + (dz + 3)] = it->second;
+                            nm2l++;
+                        }
+            }
+        }
+        for (size_t l = 0; l < H.leaf_keys.size(); l++) {
+            const int gl = lf0 + (int)l;
+            std::vector<int> nb;
+            if (H.leaf_tgt[l + 1] > H.leaf_tgt[l]) {
+                const int *q = &leaf_ijk[3 * (size_t)gl];
+                for (int dx = -1; dx <= 1; dx++)
+                    for (int dy = -1; dy <= 1; dy++)
+                        for (int dz = -1; dz <= 1; dz++) {
+                            const int ax = q[0] + dx, ay = q[1] + dy, az = q[2] + dz;
+                            if (ax < 0 || ay < 0 || az < 0 || ax >= nside || ay >= nside || az >= nside) continue;
+                            auto it = where[L].find(morton(ax, ay, az));
+                            if (it == where[L].end()) continue;
+                            const int nl = it->second - t->leaf0;
+                            const int ls = nl - lf0;
+                            if (H.leaf_src[ls + 1] == H.leaf_src[ls]) continue;
+                            nb.push_back(nl);
+                            np2p += (size_t)(H.leaf_src[ls + 1] - H.leaf_src[ls]) * (H.leaf_tgt[l + 1] - H.leaf_tgt[l]);
+                        }
+            }
+            near_leaf.insert(near_leaf.end(), nb.begin(), nb.end());
+            near_ptr[gl + 1] = (int)near_leaf.size();
+        }
+        src_off += H.sk.size();
+        tgt_off += H.tk.size();
     }
+    leaf_src[nleaf] = (int)src_off;
+    leaf_tgt[nleaf] = (int)tgt_off;
+    t->n_m2l = nm2l;
+    t->n_p2p_pairs = np2p;
     const FmmOps &ops = fmm_ops();
     FCK(up(&t->leaf_src, leaf_src));
     FCK(up(&t->leaf_tgt, leaf_tgt));
     FCK(up(&t->tgt_node, tgt_node));
     FCK(up(&t->leaf_ijk, leaf_ijk));
+    FCK(up(&t->leaf_scale, leaf_scale));
     FCK(up(&t->m2l_tab, m2l_tab));
     FCK(up(&t->m2m_tab, m2m_tab));
     FCK(up(&t->l2l_tab, l2l_tab));
@@ -735,15 +782,15 @@ static int fmm_build_level(Ctx &c, int L) {
     if (c.opts.profile)
         for (auto &e : t->ev) FCK(cudaEventCreate(&e));
     if (c.opts.verbose)
-        fprintf(stderr, "fmm: L=%d leaves=%d cells=%d m2l=%zu p2p_pairs=%zu (%s)\n", L, nleaf, ncell, t->n_m2l,
-                t->n_p2p_pairs, fp32 ? "fp32" : "fp64");
+        fprintf(stderr, "fmm: L=%d trees=%d leaves=%d cells=%d m2l=%zu p2p_pairs=%zu (%s)\n", L, nseg, nleaf, ncell,
+                t->n_m2l, t->n_p2p_pairs, fp32 ? "fp32" : "fp64");
     return FG_OK;
 }
 
 void fmm_free(Ctx &c) {
     FmmTree *t = static_cast<FmmTree *>(c.fmm);
     if (!t) return;
-    void *ptrs[] = {t->leaf_src, t->leaf_tgt, t->tgt_node, t->sloc, t->tloc, t->leaf_ijk, t->m2l_tab, t->m2m_tab,
+    void *ptrs[] = {t->leaf_scale, t->leaf_src, t->leaf_tgt, t->tgt_node, t->sloc, t->tloc, t->leaf_ijk, t->m2l_tab, t->m2m_tab,
                     t->l2l_tab, t->near_ptr, t->near_leaf, t->M, t->F, t->op_m2l, t->op_m2m, t->op_l2l};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -780,10 +827,9 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
                                                                             (const T *)t.op_l2l, F, F, 1);
     }
     if (prof) cudaEventRecord(t.ev[4], c.stream);
-    const double scale = 1.0 / (t.s0 / (double)(1 << L));
     k_l2p_p2p<T><<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node,
                                                            (const T *)t.tloc, (const T *)t.sloc, t.leaf_ijk, t.leaf0,
-                                                           scale, t.near_ptr, t.near_leaf, F, c.pot);
+                                                           t.leaf_scale, t.near_ptr, t.near_leaf, F, c.pot);
     if (prof) {
         cudaEventRecord(t.ev[5], c.stream);
         cudaEventSynchronize(t.ev[5]);

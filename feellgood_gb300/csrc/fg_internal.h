@@ -44,6 +44,26 @@ struct SolveResult {
     int pad;
 };
 
+// Per-sample parameters of one step of a batch of independent samples (device copy).
+struct SegPar {
+    double dt, prefactor;
+    double H[3];    // applied field, A/m
+    double cr, sr;  // cos / sin of the basis rotation angle of Node::setBasis
+    double c0;      // prefactor * theta * dt * gamma0
+};
+
+// Per-sample results accumulated over a multi-step batch run.
+struct SegAcc {
+    int fails;       // failed solves
+    int first_fail;  // step index of the first failure (valid if fails > 0)
+    int nit_max;
+    int nref_max;
+    int worst;       // worst step status: 0 ok, 1 iteration overflow, 2 cannot converge, 3 timed out
+    int pad;
+    long long nit_sum, nref_sum;
+    double v2max;    // max over steps of max |v|^2 / gamma0^2 (bit pattern compared as unsigned)
+};
+
 // Grid-wide barrier state of the persistent kernels (bounded wait, no hang).
 struct GridBar {
     unsigned int count;
@@ -93,6 +113,14 @@ struct MixedArgs {
     const double *u0;
     double *u1, *v1;
     double scale;  // 1/mean(A): the FP32 system is scale*K, entries O(1)
+    // batch of independent samples: sample g owns nodes [seg_node[g], seg_node[g+1]) and
+    // blocks [seg_blk[g], seg_blk[g+1]); each sample runs its own Krylov scalars and stops
+    // on its own residual (nseg == 1: one system over all nodes and blocks)
+    int nseg;
+    const int *seg_node, *seg_blk;
+    const SegPar *seg;    // per-sample dt and c0 (nullptr: the scalars above)
+    SegAcc *acc;          // per-sample accumulation over a run (nullable)
+    const int *step_ctr;  // step index of the run (with acc)
 };
 
 struct Ctx {
@@ -159,6 +187,8 @@ struct Ctx {
 
     // device: demag
     std::vector<double> h_src_xyz;  // source points (original order), host copy for the FMM tree
+    int nseg = 1;                   // independent samples packed in this context
+    std::vector<int> h_src_seg, h_node_seg;  // sample of every source / node (empty: one sample)
     int *src_dst = nullptr;      // original source index -> storage position (FMM order)
     void *fmm = nullptr;         // FMM tree and buffers (fg_fmm.cu)
     double *src_q = nullptr;
@@ -178,6 +208,30 @@ struct Ctx {
     long long launches = 0;  // kernels launched by this context
     void *mlp = nullptr;     // learned initial guess (fg_mlp.cu)
     double *heff = nullptr;  // per-node BE/A (effective field), written when the learned guess is on
+
+    // batch of independent samples packed as one block-diagonal system (fg_batch_*)
+    bool batch = false;
+    std::vector<int> h_seg_node, h_seg_tet, h_seg_tri;  // nseg+1 offsets (nodes, magnetic tets / tris)
+    std::vector<int> h_seg_blk;                         // nseg+1 block offsets of the persistent solver
+    int seg_grid = 0;                                   // blocks of the segmented persistent solver
+    int *tet_seg = nullptr, *node_seg = nullptr;        // sample of every magnetic tet / node
+    int *d_seg_node = nullptr, *d_seg_blk = nullptr;
+    SegPar *seg_par = nullptr;                          // current step's per-sample parameters
+    SegPar *hseg_par = nullptr;                         // pinned staging
+    SegPar *seg_sched = nullptr;                        // schedule of a multi-step run
+    long long seg_sched_len = 0;
+    int *step_ctr = nullptr;
+    SegAcc *seg_acc = nullptr, *hseg_acc = nullptr;
+    SegAcc *acc_active = nullptr;                       // set while a run is launched
+    int4 *eblk_rng = nullptr;                           // energy blocks: tet and tri ranges
+    int *eblk_seg = nullptr, *d_seg_eblk = nullptr;
+    int eblk_n = 0;
+    double *seg_H = nullptr, *hseg_H = nullptr;         // per-sample field of the energy
+    double *seg_epart = nullptr, *seg_energy = nullptr, *hseg_energy = nullptr;
+    cudaGraphExec_t graph = nullptr;                    // captured step + compute_all of a run
+    int graph_state = 0;                                // 0 not tried, 1 captured, -1 capture refused
+    bool run_graph = false;                             // the last run replayed the graph
+    float run_ms = 0.f;                                 // device time of the last run
 };
 
 // kernels (fg_kernels.cu)
@@ -193,6 +247,7 @@ cudaError_t launch_energy(Ctx &c, const double Hext[3]);
 cudaError_t launch_energy_into(Ctx &c, const double Hext[3], double *partial);
 int bicg_grid_size(Ctx &c, bool mixed);
 int mixed_grid_size(Ctx &c);
+int mixed_max_blocks(Ctx &c);
 int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p);
 int fmm_stage_ms(const Ctx &c, double ms[5]);
 int mlp_create(Ctx &c);
@@ -205,6 +260,11 @@ cudaError_t mlp_before_evolution(Ctx &c);
 double mlp_loss(const Ctx &c);
 int mlp_debug_grad(Ctx &c, int nsamples, const float *hx, const float *hy, float *w_out, float *g_out, float *loss);
 int mlp_nparam();
+int batch_setup(Ctx &c, const std::vector<int4> &htet, const std::vector<int4> &htri);
+void batch_free(Ctx &c);
+cudaError_t launch_select_params(Ctx &c);
+cudaError_t launch_advance(Ctx &c);
+cudaError_t launch_energy_seg(Ctx &c);
 
 }  // namespace fg
 

@@ -42,9 +42,14 @@ __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__
                                                const DevRegion *__restrict__ regs, const double *__restrict__ u0,
                                                const double *__restrict__ v0, const double *__restrict__ phi0,
                                                const double *__restrict__ phiv0, double dt, double Hx, double Hy,
-                                               double Hz, double4 *__restrict__ slot) {
+                                               double Hz, double4 *__restrict__ slot,
+                                               const int *__restrict__ tet_seg, const SegPar *__restrict__ seg) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nmt) return;
+    if (seg) {  // batch: the tet's sample carries dt and the applied field
+        const SegPar &P = seg[tet_seg[t]];
+        dt = P.dt; Hx = P.H[0]; Hy = P.H[1]; Hz = P.H[2];
+    }
     const int4 I = tet[t];
     const int ind[4] = {I.x, I.y, I.z, I.w};
     double d[4][3];
@@ -188,9 +193,14 @@ __global__ void __launch_bounds__(128) k_tet64_iso(int nmt, const int4 *__restri
                                                    const DevRegion *__restrict__ regs, const double *__restrict__ u0,
                                                    const double *__restrict__ phi0, const double *__restrict__ phiv0,
                                                    double dt, double Hx, double Hy, double Hz,
-                                                   double4 *__restrict__ slot) {
+                                                   double4 *__restrict__ slot, const int *__restrict__ tet_seg,
+                                                   const SegPar *__restrict__ seg) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nmt) return;
+    if (seg) {
+        const SegPar &P = seg[tet_seg[t]];
+        dt = P.dt; Hx = P.H[0]; Hy = P.H[1]; Hz = P.H[2];
+    }
     const int4 I = tet[t];
     const int ind[4] = {I.x, I.y, I.z, I.w};
     double d[4][3];
@@ -272,9 +282,14 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
                          const double *__restrict__ A, const double *__restrict__ u0, const double *__restrict__ v1,
                          double cr, double sr, double *__restrict__ ep, double *__restrict__ eq,
                          double *__restrict__ Dl, double *__restrict__ rhs, double *__restrict__ x,
-                         double *__restrict__ Minv, double *__restrict__ W, double *__restrict__ heff) {
+                         double *__restrict__ Minv, double *__restrict__ W, double *__restrict__ heff,
+                         const int *__restrict__ node_seg, const SegPar *__restrict__ seg) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
+    if (seg) {  // batch: the angle of the node's sample
+        cr = seg[node_seg[i]].cr;
+        sr = seg[node_seg[i]].sr;
+    }
     const double u[3] = {u0[3 * i], u0[3 * i + 1], u0[3 * i + 2]};
     double e[3], q[3];
     if (mag[i]) {
@@ -685,10 +700,22 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
                                                 const int *__restrict__ treg, const DevRegion *__restrict__ regs,
                                                 const int4 *__restrict__ tri, const DevTri *__restrict__ tc,
                                                 const double *__restrict__ u, const double *__restrict__ phi,
-                                                double Hx, double Hy, double Hz, double *__restrict__ partial) {
+                                                double Hx, double Hy, double Hz, double *__restrict__ partial,
+                                                const int4 *__restrict__ blk_rng, const int *__restrict__ blk_seg,
+                                                const double *__restrict__ segH) {
     double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-    const int stride = gridDim.x * blockDim.x;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nmt; k += stride) {
+    // default: grid-stride over all elements; batch: this block's ranges of one sample
+    int stride = gridDim.x * blockDim.x, t0 = blockIdx.x * blockDim.x + threadIdx.x, t1 = nmt;
+    int f0 = t0, f1 = nft;
+    if (blk_rng) {
+        const int4 r = blk_rng[blockIdx.x];
+        stride = blockDim.x;
+        t0 = r.x + threadIdx.x; t1 = r.y;
+        f0 = r.z + threadIdx.x; f1 = r.w;
+        const double *h = segH + 3 * blk_seg[blockIdx.x];
+        Hx = h[0]; Hy = h[1]; Hz = h[2];
+    }
+    for (int k = t0; k < t1; k += stride) {
         const int4 I = tet[k];
         const int ind[4] = {I.x, I.y, I.z, I.w};
         const DevRegion &R = regs[treg[k]];
@@ -756,7 +783,7 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
         acc[5] += my;
         acc[6] += mz;
     }
-    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nft; f += stride) {
+    for (int f = f0; f < f1; f += stride) {
         const int4 I = tri[f];
         const int ind[3] = {I.x, I.y, I.z};
         const DevTri &T = tc[f];
@@ -783,6 +810,28 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
         acc[2] += 0.5 * FG_MU0 * T.dMs * dm;
     }
     block_store<7>(acc, partial, gridDim.x);
+}
+
+// Per-sample sums of the energy partials: one block per sample adds its blocks' partials.
+__global__ void k_seg_energy_sum(int G, const int *__restrict__ seg_blk, const double *__restrict__ partial,
+                                 double *__restrict__ out) {
+    const int g = blockIdx.x;
+    if (threadIdx.x < 7) {
+        double s = 0.0;
+        for (int b = seg_blk[g]; b < seg_blk[g + 1]; b++) s += partial[threadIdx.x * G + b];
+        out[7 * g + threadIdx.x] = s;
+    }
+}
+
+// Step parameters of a run: copy step *ctr of the schedule to the current parameters.
+__global__ void k_select_params(int nseg, const SegPar *__restrict__ sched, const int *__restrict__ ctr,
+                                SegPar *__restrict__ cur) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < nseg) cur[g] = sched[(size_t)(*ctr) * nseg + g];
+}
+
+__global__ void k_advance(int *ctr) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *ctr += 1;
 }
 
 // ---------------------------------------------------------------------------------
@@ -829,18 +878,22 @@ cudaError_t launch_tet(Ctx &c, double dt, const double H[3]) {
     if (!c.aniso) {
         if (c.npi_t == 5)
             k_tet64_iso<5><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0],
-                                                                   c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot);
+                                                                   c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
+                                                                   c.tet_seg, c.batch ? c.seg_par : nullptr);
         else
             k_tet64_iso<1><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0],
-                                                                   c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot);
+                                                                   c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
+                                                                   c.tet_seg, c.batch ? c.seg_par : nullptr);
         return cudaGetLastError();
     }
     if (c.npi_t == 5)
         k_tet64<5><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0], c.v[0],
-                                                          c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot);
+                                                          c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
+                                                          c.tet_seg, c.batch ? c.seg_par : nullptr);
     else
         k_tet64<1><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0], c.v[0],
-                                                          c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot);
+                                                          c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
+                                                          c.tet_seg, c.batch ? c.seg_par : nullptr);
     return cudaGetLastError();
 }
 
@@ -851,7 +904,8 @@ cudaError_t launch_node(Ctx &c, double angle) {
     double *Minv = bv + 8 * n2;
     k_node64<<<nblocks(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.inc_ptr, c.inc, c.slot, c.mag, c.A, c.u[0], c.v[1],
                                                         cr, sr, c.ep, c.eq, c.Dl, c.rhs, c.x, Minv, c.W,
-                                                        c.mlp ? c.heff : nullptr);
+                                                        c.mlp ? c.heff : nullptr, c.node_seg,
+                                                        c.batch ? c.seg_par : nullptr);
     return cudaGetLastError();
 }
 
@@ -926,10 +980,12 @@ cudaError_t launch_energy(Ctx &c, const double H[3]) {
     const int G = c.epart_blocks;
     if (c.npi_t == 5)
         k_energy<5, 4><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
-                                                 c.u[1], c.phi[1], H[0], H[1], H[2], c.epart);
+                                                 c.u[1], c.phi[1], H[0], H[1], H[2], c.epart, nullptr, nullptr,
+                                                 nullptr);
     else
         k_energy<1, 1><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
-                                                 c.u[1], c.phi[1], H[0], H[1], H[2], c.epart);
+                                                 c.u[1], c.phi[1], H[0], H[1], H[2], c.epart, nullptr, nullptr,
+                                                 nullptr);
     return cudaGetLastError();
 }
 
@@ -939,10 +995,38 @@ cudaError_t launch_energy_into(Ctx &c, const double H[3], double *partial) {
     const int G = c.epart_blocks;
     if (c.npi_t == 5)
         k_energy<5, 4><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
-                                                 c.u[1], c.phi[1], H[0], H[1], H[2], partial);
+                                                 c.u[1], c.phi[1], H[0], H[1], H[2], partial, nullptr, nullptr,
+                                                 nullptr);
     else
         k_energy<1, 1><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
-                                                 c.u[1], c.phi[1], H[0], H[1], H[2], partial);
+                                                 c.u[1], c.phi[1], H[0], H[1], H[2], partial, nullptr, nullptr,
+                                                 nullptr);
+    return cudaGetLastError();
+}
+
+// Per-sample energies of a batch: blocks aligned to samples, then one sum per sample.
+cudaError_t launch_energy_seg(Ctx &c) {
+    const int G = c.eblk_n;
+    const double H0[3] = {0, 0, 0};
+    if (c.npi_t == 5)
+        k_energy<5, 4><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
+                                                 c.u[1], c.phi[1], H0[0], H0[1], H0[2], c.seg_epart, c.eblk_rng,
+                                                 c.eblk_seg, c.seg_H);
+    else
+        k_energy<1, 1><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
+                                                 c.u[1], c.phi[1], H0[0], H0[1], H0[2], c.seg_epart, c.eblk_rng,
+                                                 c.eblk_seg, c.seg_H);
+    k_seg_energy_sum<<<c.nseg, 32, 0, c.stream>>>(G, c.d_seg_eblk, c.seg_epart, c.seg_energy);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_select_params(Ctx &c) {
+    k_select_params<<<nblocks(c.nseg, 128), 128, 0, c.stream>>>(c.nseg, c.seg_sched, c.step_ctr, c.seg_par);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advance(Ctx &c) {
+    k_advance<<<1, 32, 0, c.stream>>>(c.step_ctr);
     return cudaGetLastError();
 }
 

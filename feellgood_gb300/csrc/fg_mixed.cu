@@ -9,6 +9,7 @@
 //                       keeps every FP32 quantity O(1) (raw entries are ~1e-27);
 //   x += scale |r| d in FP64.
 // One cooperative launch per solve; the node update (Node::make_evol) is fused at the end.
+#include <algorithm>
 #include <cmath>
 
 #include "fg_device.cuh"
@@ -16,16 +17,52 @@
 
 namespace fg {
 
+// Rows and blocks of this block's sample. One system: all nodes, all blocks.
+struct SegView {
+    int g, lo, hi, b0, b1;
+};
+
+__device__ __forceinline__ SegView seg_view(const MixedArgs &a) {
+    SegView v{0, 0, a.nn, 0, (int)gridDim.x};
+    if (a.nseg > 1) {
+        int lo = 0, hi = a.nseg - 1;
+        const int b = blockIdx.x;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a.seg_blk[mid] <= b) lo = mid;
+            else hi = mid - 1;
+        }
+        v.g = lo;
+        v.lo = a.seg_node[lo];
+        v.hi = a.seg_node[lo + 1];
+        v.b0 = a.seg_blk[lo];
+        v.b1 = a.seg_blk[lo + 1];
+    }
+    return v;
+}
+
+// Batched form (nseg > 1): every sample of a block-diagonal system runs the same
+// iteration with its own scalars (rho, alpha, omega), its own |b| and its own stopping
+// tests, exactly as if it were solved alone; a sample that has stopped idles through the
+// remaining grid barriers. The loops end when no sample is active: an activity flag rides
+// along the first reduction of each loop pass (slot 1, summed over the whole grid).
+#define SAMPLE_ROWS(i) for (int i = sv.lo + (blockIdx.x - sv.b0) * (int)blockDim.x + (int)threadIdx.x; i < sv.hi; i += rstride)
+
 __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
     const int G = gridDim.x;
-    const int nn = a.nn;
-    const int stride = G * blockDim.x;
-    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
-    const float c32 = (float)(a.c0 * a.scale);
+    const SegView sv = seg_view(a);
+    const int rstride = (sv.b1 - sv.b0) * blockDim.x;
+    const bool multi = a.nseg > 1;
+    double c0 = a.c0, dt = a.dt;
+    if (a.seg) {
+        c0 = a.seg[sv.g].c0;
+        dt = a.seg[sv.g].dt;
+    }
+    const float c32 = (float)(c0 * a.scale);
     // phase 0: FP32 copies of the per-step operator, FP64 tangent vectors of x, |b|^2
     {
         double bb = 0.0;
-        for (int i = i0; i < nn; i += stride) {
+        SAMPLE_ROWS(i) {
             for (int c = 0; c < 3; c++) {
                 a.ep32[3 * i + c] = (float)a.ep[3 * i + c];
                 a.eq32[3 * i + c] = (float)a.eq[3 * i + c];
@@ -43,117 +80,144 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
     if (!grid_sync(a.bar)) goto timeout;
     {
         double s1[1];
-        grid_sum<1>(a.partial, G, s1);
+        range_sum<1>(a.partial, G, sv.b0, sv.b1, s1);
         const double rhsn = sqrt(fabs(s1[0]));
         int status = -1, nit = 0, nref = 0;
         double res = 0.0, res0 = 0.0;
+        bool done = false;  // this sample's solve has ended (status set)
         for (;;) {
             // refinement residual r64 = b - K x (FP64, masked)
             {
                 double rr = 0.0;
-                for (int i = i0; i < nn; i += stride) {
-                    double y0, y1;
-                    apply_row<double>(i, a.Sptr, a.Scol, a.Sval, a.W64, a.ep, a.eq, a.A, a.Dl, a.c0, a.x[2 * i],
-                                      a.x[2 * i + 1], y0, y1);
-                    const bool m = a.mag[i];
-                    const double r0 = m ? a.b[2 * i] - y0 : 0.0, r1 = m ? a.b[2 * i + 1] - y1 : 0.0;
-                    a.r64[2 * i] = r0;
-                    a.r64[2 * i + 1] = r1;
-                    rr += r0 * r0 + r1 * r1;
-                }
+                if (!done)
+                    SAMPLE_ROWS(i) {
+                        double y0, y1;
+                        apply_row<double>(i, a.Sptr, a.Scol, a.Sval, a.W64, a.ep, a.eq, a.A, a.Dl, c0, a.x[2 * i],
+                                          a.x[2 * i + 1], y0, y1);
+                        const bool m = a.mag[i];
+                        const double r0 = m ? a.b[2 * i] - y0 : 0.0, r1 = m ? a.b[2 * i + 1] - y1 : 0.0;
+                        a.r64[2 * i] = r0;
+                        a.r64[2 * i + 1] = r1;
+                        rr += r0 * r0 + r1 * r1;
+                    }
                 double v1[1] = {rr};
                 block_store<1>(v1, a.partial, G);
             }
             if (!grid_sync(a.bar)) goto timeout;
             {
                 double s2[1];
-                grid_sum<1>(a.partial, G, s2);
-                res = sqrt(fabs(s2[0]));
+                range_sum<1>(a.partial, G, sv.b0, sv.b1, s2);
+                if (!done) res = sqrt(fabs(s2[0]));
             }
-            if (nref == 0) res0 = res;
-            if (isnan(res)) { status = 2; break; }
-            if (res <= rhsn * a.tol) { status = 0; break; }
-            if (nref >= a.refine_max || nit >= a.maxiter) { status = 1; break; }
+            if (!done) {
+                if (nref == 0) res0 = res;
+                if (isnan(res)) { status = 2; done = true; }
+                else if (res <= rhsn * a.tol) { status = 0; done = true; }
+                else if (nref >= a.refine_max || nit >= a.maxiter) { status = 1; done = true; }
+            }
+            if (!multi && done) break;
             // inner FP32 BiCGSTAB on (scale K) d = r64/res, relative target
             const double rho = res;
-            const double target = fmax(a.inner_tol, 0.3 * a.tol * rhsn / res);
+            const double target = done ? 0.0 : fmax(a.inner_tol, 0.3 * a.tol * rhsn / res);
             {
-                const float inv = (float)(1.0 / rho);
                 double rr = 0.0;
-                for (int i = i0; i < nn; i += stride) {
-                    for (int c = 0; c < 2; c++) {
-                        const int k = 2 * i + c;
-                        const float rv = (float)a.r64[k] * inv;
-                        a.r[k] = rv;
-                        a.rt[k] = rv;
-                        a.p[k] = rv;
-                        a.d[k] = 0.0f;
-                        rr += (double)rv * rv;
+                if (!done) {
+                    const float inv = (float)(1.0 / rho);
+                    SAMPLE_ROWS(i) {
+                        for (int c = 0; c < 2; c++) {
+                            const int k = 2 * i + c;
+                            const float rv = (float)a.r64[k] * inv;
+                            a.r[k] = rv;
+                            a.rt[k] = rv;
+                            a.p[k] = rv;
+                            a.d[k] = 0.0f;
+                            rr += (double)rv * rv;
+                        }
                     }
                 }
-                double v1[1] = {rr};
-                block_store<1>(v1, a.partial, G);
+                double v2[2] = {rr, (threadIdx.x == 0 && !done) ? 1.0 : 0.0};
+                block_store<2>(v2, a.partial, G);
             }
             if (!grid_sync(a.bar)) goto timeout;
             {
                 double s2[1];
-                grid_sum<1>(a.partial, G, s2);
+                range_sum<1>(a.partial, G, sv.b0, sv.b1, s2);
+                if (multi) {
+                    double f[1];
+                    grid_sum<1>(a.partial + G, G, f);
+                    if (f[0] == 0.0) break;  // every sample has ended
+                }
                 double rr = s2[0], rtr = s2[0];
                 double rho1 = 0.0, rho2 = 0.0, alpha = 0.0, beta = 0.0, omega = 0.0;
                 int it = 0;
-                while (sqrt(rr) > target && nit < a.maxiter) {
-                    rho1 = rtr;
-                    if (it > 0) {
-                        if (rho2 == 0.0 || omega == 0.0) break;
-                        beta = (rho1 / rho2) * (alpha / omega);
-                    }
-                    const float fb = (float)beta, fo = (float)omega;
-                    for (int i = i0; i < nn; i += stride) {
-                        float p0 = a.p[2 * i], p1 = a.p[2 * i + 1];
+                bool act = !done;
+                for (;;) {
+                    if (act && !(sqrt(rr) > target && nit < a.maxiter)) act = false;
+                    if (act) {
+                        rho1 = rtr;
                         if (it > 0) {
-                            p0 = a.r[2 * i] + fb * (p0 - fo * a.v[2 * i]);
-                            p1 = a.r[2 * i + 1] + fb * (p1 - fo * a.v[2 * i + 1]);
-                            a.p[2 * i] = p0;
-                            a.p[2 * i + 1] = p1;
+                            if (rho2 == 0.0 || omega == 0.0) act = false;
+                            else beta = (rho1 / rho2) * (alpha / omega);
                         }
-                        const float h0 = a.Minv32[2 * i] * p0, h1 = a.Minv32[2 * i + 1] * p1;
-                        a.phat[2 * i] = h0;
-                        a.phat[2 * i + 1] = h1;
-                        tangent<float>(i, a.ep32, a.eq32, h0, h1, a.W32);
+                    }
+                    if (!multi && !act) break;
+                    if (act) {
+                        const float fb = (float)beta, fo = (float)omega;
+                        SAMPLE_ROWS(i) {
+                            float p0 = a.p[2 * i], p1 = a.p[2 * i + 1];
+                            if (it > 0) {
+                                p0 = a.r[2 * i] + fb * (p0 - fo * a.v[2 * i]);
+                                p1 = a.r[2 * i + 1] + fb * (p1 - fo * a.v[2 * i + 1]);
+                                a.p[2 * i] = p0;
+                                a.p[2 * i + 1] = p1;
+                            }
+                            const float h0 = a.Minv32[2 * i] * p0, h1 = a.Minv32[2 * i + 1] * p1;
+                            a.phat[2 * i] = h0;
+                            a.phat[2 * i + 1] = h1;
+                            tangent<float>(i, a.ep32, a.eq32, h0, h1, a.W32);
+                        }
                     }
                     if (!grid_sync(a.bar)) goto timeout;
                     {
                         double vr = 0.0;
-                        for (int i = i0; i < nn; i += stride) {
-                            float y0, y1;
-                            apply_row<float>(i, a.Sptr, a.Scol, a.Sval32, a.W32, a.ep32, a.eq32, a.A32, a.Dl32, c32,
-                                             a.phat[2 * i], a.phat[2 * i + 1], y0, y1);
-                            if (!a.mag[i]) y0 = y1 = 0.0f;
-                            a.v[2 * i] = y0;
-                            a.v[2 * i + 1] = y1;
-                            vr += (double)y0 * a.rt[2 * i] + (double)y1 * a.rt[2 * i + 1];
-                        }
-                        double v1[1] = {vr};
-                        block_store<1>(v1, a.partial, G);
+                        if (act)
+                            SAMPLE_ROWS(i) {
+                                float y0, y1;
+                                apply_row<float>(i, a.Sptr, a.Scol, a.Sval32, a.W32, a.ep32, a.eq32, a.A32, a.Dl32,
+                                                 c32, a.phat[2 * i], a.phat[2 * i + 1], y0, y1);
+                                if (!a.mag[i]) y0 = y1 = 0.0f;
+                                a.v[2 * i] = y0;
+                                a.v[2 * i + 1] = y1;
+                                vr += (double)y0 * a.rt[2 * i] + (double)y1 * a.rt[2 * i + 1];
+                            }
+                        double v2[2] = {vr, (threadIdx.x == 0 && act) ? 1.0 : 0.0};
+                        block_store<2>(v2, a.partial, G);
                     }
                     if (!grid_sync(a.bar)) goto timeout;
                     {
                         double s1b[1];
-                        grid_sum<1>(a.partial, G, s1b);
-                        alpha = rho1 / s1b[0];
+                        range_sum<1>(a.partial, G, sv.b0, sv.b1, s1b);
+                        if (multi) {
+                            double f[1];
+                            grid_sum<1>(a.partial + G, G, f);
+                            if (f[0] == 0.0) break;
+                        }
+                        if (act) alpha = rho1 / s1b[0];
                     }
                     {
-                        const float fa = (float)alpha;
                         double ss = 0.0;
-                        for (int i = i0; i < nn; i += stride) {
-                            const float s0 = a.r[2 * i] - fa * a.v[2 * i], s1 = a.r[2 * i + 1] - fa * a.v[2 * i + 1];
-                            a.s[2 * i] = s0;
-                            a.s[2 * i + 1] = s1;
-                            const float h0 = a.Minv32[2 * i] * s0, h1 = a.Minv32[2 * i + 1] * s1;
-                            a.shat[2 * i] = h0;
-                            a.shat[2 * i + 1] = h1;
-                            tangent<float>(i, a.ep32, a.eq32, h0, h1, a.W32);
-                            ss += (double)s0 * s0 + (double)s1 * s1;
+                        if (act) {
+                            const float fa = (float)alpha;
+                            SAMPLE_ROWS(i) {
+                                const float s0 = a.r[2 * i] - fa * a.v[2 * i], s1 = a.r[2 * i + 1] - fa * a.v[2 * i + 1];
+                                a.s[2 * i] = s0;
+                                a.s[2 * i + 1] = s1;
+                                const float h0 = a.Minv32[2 * i] * s0, h1 = a.Minv32[2 * i + 1] * s1;
+                                a.shat[2 * i] = h0;
+                                a.shat[2 * i + 1] = h1;
+                                tangent<float>(i, a.ep32, a.eq32, h0, h1, a.W32);
+                                ss += (double)s0 * s0 + (double)s1 * s1;
+                            }
                         }
                         double v1[1] = {ss};
                         block_store<1>(v1, a.partial, G);
@@ -161,50 +225,54 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
                     if (!grid_sync(a.bar)) goto timeout;
                     {
                         double s1c[1];
-                        grid_sum<1>(a.partial, G, s1c);
-                        if (sqrt(s1c[0]) <= target) {
+                        range_sum<1>(a.partial, G, sv.b0, sv.b1, s1c);
+                        if (act && sqrt(s1c[0]) <= target) {
                             const float fa = (float)alpha;
-                            for (int i = i0; i < nn; i += stride) {
+                            SAMPLE_ROWS(i) {
                                 a.d[2 * i] += fa * a.phat[2 * i];
                                 a.d[2 * i + 1] += fa * a.phat[2 * i + 1];
                             }
                             nit++;
-                            break;
+                            act = false;
                         }
                     }
+                    if (!multi && !act) break;
                     {
                         double ts = 0.0, tt = 0.0;
-                        for (int i = i0; i < nn; i += stride) {
-                            float y0, y1;
-                            apply_row<float>(i, a.Sptr, a.Scol, a.Sval32, a.W32, a.ep32, a.eq32, a.A32, a.Dl32, c32,
-                                             a.shat[2 * i], a.shat[2 * i + 1], y0, y1);
-                            if (!a.mag[i]) y0 = y1 = 0.0f;
-                            a.t[2 * i] = y0;
-                            a.t[2 * i + 1] = y1;
-                            ts += (double)y0 * a.s[2 * i] + (double)y1 * a.s[2 * i + 1];
-                            tt += (double)y0 * y0 + (double)y1 * y1;
-                        }
+                        if (act)
+                            SAMPLE_ROWS(i) {
+                                float y0, y1;
+                                apply_row<float>(i, a.Sptr, a.Scol, a.Sval32, a.W32, a.ep32, a.eq32, a.A32, a.Dl32,
+                                                 c32, a.shat[2 * i], a.shat[2 * i + 1], y0, y1);
+                                if (!a.mag[i]) y0 = y1 = 0.0f;
+                                a.t[2 * i] = y0;
+                                a.t[2 * i + 1] = y1;
+                                ts += (double)y0 * a.s[2 * i] + (double)y1 * a.s[2 * i + 1];
+                                tt += (double)y0 * y0 + (double)y1 * y1;
+                            }
                         double v2[2] = {ts, tt};
                         block_store<2>(v2, a.partial, G);
                     }
                     if (!grid_sync(a.bar)) goto timeout;
                     {
                         double s2b[2];
-                        grid_sum<2>(a.partial, G, s2b);
-                        omega = s2b[0] / s2b[1];
+                        range_sum<2>(a.partial, G, sv.b0, sv.b1, s2b);
+                        if (act) omega = s2b[0] / s2b[1];
                     }
                     {
-                        const float fa = (float)alpha, fo = (float)omega;
                         double r2 = 0.0, rtr2 = 0.0;
-                        for (int i = i0; i < nn; i += stride) {
+                        if (act) {
+                            const float fa = (float)alpha, fo = (float)omega;
+                            SAMPLE_ROWS(i) {
 #pragma unroll
-                            for (int c = 0; c < 2; c++) {
-                                const int k = 2 * i + c;
-                                a.d[k] += fa * a.phat[k] + fo * a.shat[k];
-                                const float rv = a.s[k] - fo * a.t[k];
-                                a.r[k] = rv;
-                                r2 += (double)rv * rv;
-                                rtr2 += (double)a.rt[k] * rv;
+                                for (int c = 0; c < 2; c++) {
+                                    const int k = 2 * i + c;
+                                    a.d[k] += fa * a.phat[k] + fo * a.shat[k];
+                                    const float rv = a.s[k] - fo * a.t[k];
+                                    a.r[k] = rv;
+                                    r2 += (double)rv * rv;
+                                    rtr2 += (double)a.rt[k] * rv;
+                                }
                             }
                         }
                         double v2[2] = {r2, rtr2};
@@ -213,34 +281,36 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
                     if (!grid_sync(a.bar)) goto timeout;
                     {
                         double s2c[2];
-                        grid_sum<2>(a.partial, G, s2c);
-                        rr = s2c[0];
-                        rtr = s2c[1];
+                        range_sum<2>(a.partial, G, sv.b0, sv.b1, s2c);
+                        if (act) {
+                            rr = s2c[0];
+                            rtr = s2c[1];
+                            rho2 = rho1;
+                            it++;
+                            nit++;
+                        }
                     }
-                    rho2 = rho1;
-                    it++;
-                    nit++;
                 }
             }
             // x += scale * rho * d (FP64) and the tangent vectors of the new x
-            {
+            if (!done) {
                 const double f = a.scale * rho;
-                for (int i = i0; i < nn; i += stride) {
+                SAMPLE_ROWS(i) {
                     const double x0 = a.x[2 * i] + f * (double)a.d[2 * i];
                     const double x1 = a.x[2 * i + 1] + f * (double)a.d[2 * i + 1];
                     a.x[2 * i] = x0;
                     a.x[2 * i + 1] = x1;
                     tangent<double>(i, a.ep, a.eq, x0, x1, a.W64);
                 }
+                nref++;
             }
-            nref++;
             if (!grid_sync(a.bar)) goto timeout;
         }
         const bool fail = (status != 0);
         if (!grid_sync(a.bar)) goto timeout;
         double v2max = 0.0;
         if (!fail) {
-            for (int i = i0; i < nn; i += stride) {
+            SAMPLE_ROWS(i) {
                 if (!a.mag[i]) continue;
                 const double vp = a.x[2 * i], vq = a.x[2 * i + 1];
                 v2max = fmax(v2max, vp * vp + vq * vq);
@@ -249,7 +319,7 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
                     nv[c] = pa * a.ep[3 * i + c] + qb * a.eq[3 * i + c];
-                    nu[c] = a.u0[3 * i + c] + a.dt * nv[c];
+                    nu[c] = a.u0[3 * i + c] + dt * nv[c];
                 }
                 const double n = sqrt(nu[0] * nu[0] + nu[1] * nu[1] + nu[2] * nu[2]);
 #pragma unroll
@@ -261,24 +331,53 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
         }
         v2max = dmax_reduce_block(v2max);
         if (threadIdx.x == 0) {
-            atomicMax((unsigned long long *)&a.res->v2max, (unsigned long long)__double_as_longlong(v2max));
-            if (blockIdx.x == 0) {
-                a.res->status = status;
-                a.res->nit = nit;
-                a.res->nref = nref;
-                a.res->fail = fail ? 1 : 0;
-                a.res->res = res;
-                a.res->rhsn = rhsn;
-                a.res->res0 = res0;
+            SolveResult *R = a.res + sv.g;
+            atomicMax((unsigned long long *)&R->v2max, (unsigned long long)__double_as_longlong(v2max));
+            if (blockIdx.x == sv.b0) {
+                R->status = status;
+                R->nit = nit;
+                R->nref = nref;
+                R->fail = fail ? 1 : 0;
+                R->res = res;
+                R->rhsn = rhsn;
+                R->res0 = res0;
+            }
+            if (a.acc) {
+                SegAcc *S = a.acc + sv.g;
+                atomicMax((unsigned long long *)&S->v2max, (unsigned long long)__double_as_longlong(v2max));
+                if (blockIdx.x == sv.b0) {
+                    S->nit_sum += nit;
+                    S->nref_sum += nref;
+                    S->nit_max = max(S->nit_max, nit);
+                    S->nref_max = max(S->nref_max, nref);
+                    if (fail) {
+                        if (S->fails == 0) S->first_fail = a.step_ctr ? *a.step_ctr : 0;
+                        S->fails++;
+                        S->worst = max(S->worst, status == 1 ? 1 : 2);
+                    }
+                }
             }
         }
         return;
     }
 timeout:
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.res->timeout = 1;
-        a.res->fail = 1;
+    if (blockIdx.x == sv.b0 && threadIdx.x == 0) {
+        a.res[sv.g].timeout = 1;
+        a.res[sv.g].fail = 1;
+        if (a.acc) {
+            if (a.acc[sv.g].fails == 0) a.acc[sv.g].first_fail = a.step_ctr ? *a.step_ctr : 0;
+            a.acc[sv.g].fails++;
+            a.acc[sv.g].worst = 3;
+        }
     }
+}
+
+#undef SAMPLE_ROWS
+
+int mixed_max_blocks(Ctx &c) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed, 256, 0);
+    return std::max(1, per_sm) * c.nsm;
 }
 
 int mixed_grid_size(Ctx &c) {
@@ -310,12 +409,36 @@ cudaError_t launch_mixed(Ctx &c, double dt, double prefactor) {
     a.maxiter = c.opts.max_iter; a.refine_max = c.opts.refine_max;
     a.dt = dt; a.u0 = c.u[0]; a.u1 = c.u[1]; a.v1 = c.v[1];
     a.scale = 1.0 / c.mean_A;
+    a.nseg = 1;
+    a.seg_node = a.seg_blk = nullptr;
+    a.seg = nullptr;
+    a.acc = nullptr;
+    a.step_ctr = nullptr;
+    int grid = c.mixed_grid, nres = 1;
+    if (c.batch) {
+        a.nseg = c.nseg;
+        a.seg_node = c.d_seg_node;
+        a.seg_blk = c.d_seg_blk;
+        a.seg = c.seg_par;
+        a.acc = c.acc_active;
+        a.step_ctr = c.step_ctr;
+        grid = c.seg_grid;
+        nres = c.nseg;
+    }
     cudaError_t e = cudaMemsetAsync(c.bar, 0, sizeof(GridBar), c.stream);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(c.dres, 0, sizeof(SolveResult), c.stream);
+    e = cudaMemsetAsync(c.dres, 0, sizeof(SolveResult) * nres, c.stream);
     if (e != cudaSuccess) return e;
-    void *args[] = {&a};
-    return cudaLaunchCooperativeKernel((void *)k_mixed, dim3(c.mixed_grid), dim3(256), args, 0, c.stream);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(256);
+    cfg.stream = c.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_mixed, a);
 }
 
 }  // namespace fg

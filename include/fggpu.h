@@ -17,6 +17,9 @@
  *   fg_get_state     the node data read by mesh::savesol / Fem::saver: src/save.cpp:164-186
  *   fg_demag         scal_fmm::fmm::demag for one field: src/fmm_demag.h:184-224
  *   fg_energy        Fem::energy: src/energy.cpp:5-68
+ *   fg_batch_*       no counterpart: the reference runs one mesh per process. A batch is
+ *                    many independent meshes stepped together, each sample following the
+ *                    per-step sequence above (src/time_integration.cpp:193-231) on its own.
  */
 #ifndef FGGPU_H
 #define FGGPU_H
@@ -79,7 +82,7 @@ typedef struct {
     int learned_guess;    /* 1: online-trained per-node MLP proposes the initial guess */
     int demag;            /* FG_DEMAG_* */
     int fmm_order;        /* expansion order P of the FMM (0: default) */
-    int fmm_leaf;         /* target number of sources per leaf (0: autotuned) */
+    int fmm_leaf;         /* target number of sources per leaf (0: autotuned; -L: octree depth L) */
     int one_gauss_point;  /* 1: single Gauss point rules (reference ONE_GAUSS_POINT build) */
     int first_order;      /* 1: skip the demag of v (reference FIRST_ORDER build) */
     int refine_max;       /* FP64 refinement sweeps in FG_PREC_FP32_REFINE */
@@ -169,6 +172,51 @@ int fg_mlp_info(const fg_ctx *ctx, long long *train_steps, double *last_loss);
 int fg_mlp_debug_grad(fg_ctx *ctx, int nsamples, const float *feat, const float *target, float *weights,
                       float *grad, float *loss);
 int fg_mlp_nparam(void);
+
+/* ---- batches of independent samples ----------------------------------------------
+ * n_samples meshes (all sharing the region tables) packed into one context: their node
+ * arrays are concatenated in sample order (fg_set_state / fg_get_state / fg_demag use
+ * that order; fg_batch_info gives the offsets), the per-step system is block diagonal
+ * and one persistent launch solves every block with its own Krylov scalars and its own
+ * stopping test, so each sample follows the iteration it would follow alone. The demag
+ * field is a forest FMM (one octree per sample): samples do not interact. A batch needs
+ * opts.precision = FG_PREC_FP32_REFINE and no learned guess. fg_step does not apply to a
+ * batch context; fg_compute_all and fg_energy sum over all samples with one field. */
+
+/* Per-sample parameters of one step (the arguments of fg_step). */
+typedef struct {
+    double dt, prefactor, Hext[3], basis_angle;
+} fg_sample_step;
+
+/* Per-sample summary of fg_batch_run. */
+typedef struct {
+    int fails;           /* steps whose solve failed (the sample kept its state on those) */
+    int first_fail;      /* index of the first failed step, if any */
+    int iters_max;       /* largest per-step iteration count */
+    int refinements_max;
+    long long iters;     /* summed over the run */
+    long long refinements;
+    double vmax;         /* largest per-step vmax */
+} fg_batch_report;
+
+int fg_batch_create(const fg_mesh *meshes, int n_samples, const fg_region *regions, int n_regions,
+                    const fg_tri_region *tri_regions, int n_tri_regions, const fg_opts *opts, fg_ctx **out);
+/* n_samples and, if node_offsets is not NULL, the n_samples + 1 node offsets. */
+int fg_batch_info(const fg_ctx *ctx, int *n_samples, int *node_offsets);
+/* fg_step for every sample at once: steps[n_samples] in, reports[n_samples] out (may be
+ * NULL). Returns FG_OK when every sample succeeded, else the worst sample status. */
+int fg_batch_step(fg_ctx *ctx, const fg_sample_step *steps, fg_step_report *reports);
+/* fg_compute_all for every sample; Hext[3*n_samples] (NULL: zero field) is used for the
+ * per-sample energies[4*n_samples] (may be NULL: energies skipped). */
+int fg_batch_compute_all(fg_ctx *ctx, const double *Hext, double *energies);
+/* n_steps of fg_batch_step + fg_batch_compute_all with no host round trip in between:
+ * steps[n_steps * n_samples] (step-major) are uploaded once and the whole step is
+ * replayed as one CUDA graph (or launched stream-ordered where the graph cannot be
+ * captured). reports[n_samples] may be NULL. Returns FG_OK or the worst status seen. */
+int fg_batch_run(fg_ctx *ctx, int n_steps, const fg_sample_step *steps, fg_batch_report *reports);
+/* Of the last fg_batch_run: graph_used 1 if it replayed a CUDA graph (0: stream-ordered
+ * launches) and its device time in ms (CUDA events around the steps). Either may be NULL. */
+int fg_batch_run_info(const fg_ctx *ctx, int *graph_used, double *device_ms);
 
 /* Device ms of the stages of the last FMM evaluation when opts.profile is set:
  * [0] P2M, [1] M2M, [2] M2L, [3] L2L, [4] L2P + P2P. */

@@ -1,0 +1,133 @@
+"""Batches of independent samples (fg_batch_*): the block-diagonal system, the forest FMM
+and the graph-replayed run against the same samples stepped one context at a time.
+
+A batch sample must follow the iteration it would follow alone: its Krylov scalars, its
+|b| and its stopping test are its own. What may differ is the order of the per-block
+partial sums (a sample gets a different number of solver blocks in a batch), so the
+per-sample solutions agree to the solver tolerance, not bit for bit; the demag potential
+(a forest of the same octrees) and a graph replay of the stream-ordered step agree exactly.
+"""
+import numpy as np
+import pytest
+
+import feellgood_gb300 as fg
+from oracle import fgo
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(4, 4, 4), (7, 5, 4), (5, 6, 8)]
+H = np.array([[0.0, 0.0, 3e4], [2e4, 0.0, 0.0], [1e4, -1e4, 5e3]])
+OPTS = dict(precision=fg.FG_PREC_FP32_REFINE, demag=fg.FG_DEMAG_FMM, fmm_leaf=-3, tol=1e-9, refine_max=12)
+
+
+def _samples():
+    ms = [cases.cuboid(*s) for s in SHAPES]
+    us = [cases.perturbed_state(m["xyz"], seed=10 + g, sigma=0.2) for g, m in enumerate(ms)]
+    return ms, us
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def _singles(ms, us):
+    cs = []
+    for m, u in zip(ms, us):
+        c = fg.Context(m, cases.regions(alpha=0.1), **OPTS)
+        c.set_state(u)
+        c.compute_all([0, 0, 0])
+        cs.append(c)
+    return cs
+
+
+def _batch(ms, us):
+    b = fg.Context(ms, cases.regions(alpha=0.1), **OPTS)
+    b.set_state(np.concatenate(us))
+    b.batch_compute_all(None, energies=False)
+    return b
+
+
+def test_batch_layout_and_forest_demag():
+    ms, us = _samples()
+    b = _batch(ms, us)
+    off = b.node_offsets
+    assert list(np.diff(off)) == [len(m["xyz"]) for m in ms]
+    singles = _singles(ms, us)
+    phi_b = b.get_state(0)["phi"]
+    for g, c in enumerate(singles):
+        phi = c.get_state(0)["phi"]
+        assert _rel(phi_b[off[g]:off[g + 1]], phi) < 1e-12
+    # the forest potential is each sample's own: it matches the oracle's exact sum per sample
+    for g, m in enumerate(ms):
+        o = fgo.Oracle(m, cases.oracle_regions(alpha=0.1))
+        o.set_state(us[g])
+        assert _rel(phi_b[off[g]:off[g + 1]], o.demag(0)) < 1e-4
+
+
+def test_batch_step_matches_single_contexts():
+    ms, us = _samples()
+    b = _batch(ms, us)
+    singles = _singles(ms, us)
+    off = b.node_offsets
+    dt, pref = 1e-14, 1.0
+    angles = np.array([0.3, 1.1, 2.0])
+    for it in range(3):
+        s, reps = b.batch_step(dt, pref, H, angles + it)
+        assert s == fg.FG_OK
+        vb = b.get_state(1)["v"]
+        for g, c in enumerate(singles):
+            r = c.step(dt, pref, H[g], angles[g] + it)
+            assert r["status"] == fg.FG_OK
+            v = c.get_state(1)["v"]
+            assert _rel(vb[off[g]:off[g + 1]], v) < 1e-7
+            assert abs(reps[g]["vmax"] - r["vmax"]) <= 1e-7 * r["vmax"]
+            assert reps[g]["res"] <= 1e-9 * reps[g]["rhsn"]
+        E = b.batch_compute_all(H)
+        for g, c in enumerate(singles):
+            e = c.compute_all(H[g])
+            np.testing.assert_allclose(E[g], e, rtol=1e-6, atol=1e-30)
+
+
+def test_batch_of_one_is_the_single_path():
+    ms, us = _samples()
+    b = fg.Context([ms[2]], cases.regions(alpha=0.1), **OPTS)
+    b.set_state(us[2])
+    b.batch_compute_all(None, energies=False)
+    c = _singles(ms[2:], us[2:])[0]
+    s, reps = b.batch_step(1e-14, 1.0, H[2:], [0.7])
+    r = c.step(1e-14, 1.0, H[2], 0.7)
+    assert s == fg.FG_OK and r["status"] == fg.FG_OK
+    assert reps[0]["iters"] == r["iters"]
+    np.testing.assert_array_equal(b.get_state(1)["v"], c.get_state(1)["v"])
+
+
+def test_batch_run_graph_equals_stepwise():
+    ms, us = _samples()
+    nsteps = 5
+    rng = np.random.default_rng(3)
+    angles = rng.uniform(0, 2 * np.pi, (nsteps, len(ms)))
+    a = _batch(ms, us)
+    s, reps = a.batch_run(1e-14, 1.0, H, angles)
+    assert s == fg.FG_OK
+    graph, ms_dev = a.batch_run_info()
+    print(f"batch run: graph replay {graph}, {ms_dev:.3f} ms for {nsteps} steps")
+    assert ms_dev > 0
+    b = _batch(ms, us)
+    iters = np.zeros(len(ms), dtype=int)
+    for k in range(nsteps):
+        s, rr = b.batch_step(1e-14, 1.0, H, angles[k])
+        assert s == fg.FG_OK
+        iters += [r["iters"] for r in rr]
+        b.batch_compute_all(None, energies=False)
+    sa, sb = a.get_state(0), b.get_state(0)
+    for k in ("u", "v", "phi", "phiv"):
+        np.testing.assert_array_equal(sa[k], sb[k])
+    assert [r["iters"] for r in reps] == list(iters)
+    assert all(r["fails"] == 0 for r in reps)
+    # a second run continues from the committed state and reuses the captured graph
+    s, _ = a.batch_run(1e-14, 1.0, H, angles)
+    assert s == fg.FG_OK
+    assert a.batch_run_info()[0] == graph
+    u = a.get_state(0)["u"]
+    assert np.allclose(np.linalg.norm(u, axis=1), 1.0, atol=1e-12)
