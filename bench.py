@@ -1,5 +1,6 @@
 #!/usr/bin/env python3
-"""Benchmark: LLG steps/s at 1.2M tets, FP32-body + FP64-refinement path vs plain FP64 GPU path.
+"""Benchmark: LLG steps/s at 1.2M tets, learned-guess FP32-body + FP64-refinement path vs the
+plain FP64 GPU path at the same BiCG tolerance.
 
 Workload (the film configuration): permalloy film 400 x 400 x 10 nm on a 2 nm grid
 (200 x 200 x 5 cells x 6 tetrahedra = 1,200,000 tets, 242,406 nodes, 168,000 boundary
@@ -8,9 +9,12 @@ uniform random unit vectors smoothed by 3 Jacobi passes over the node graph; zer
 field; fixed dt = 5e-14 s; BiCG tolerance 1e-6 (max 700 iterations); FMM demag (P = 9).
 A step is one accepted time step of the reference loop: base_projection, element
 integrals, solve, node update, demag of m and of v, energies, evolution
-(src/time_integration.cpp:193-231). Synthetic data; no files are read.
+(src/time_integration.cpp:193-231). The learned initial guess is trained online on the
+solver's own solutions for --train-steps untimed solves first and keeps training (timed)
+afterwards. Synthetic data; no files are read.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py --workload batch64     # 64 independent cubes, batched (its own line)
 
 One JSON line on stdout (rank 0). For N > 1 every rank runs an independent replica on its
 own GPU (the path does not shard); value is the sum over ranks of steps/s (max-over-ranks
@@ -138,17 +142,18 @@ def max_over_ranks(dist, x):
 
 
 def run_steps(ctx, n, H, dtmax, angles):
-    """n accepted steps; returns (device ms per step list, reports)."""
+    """n accepted steps (angles: a callable or a sequence); returns (per-step device ms of the
+    phases [elements, solve, demag x2, energy + evolution, whole step], reports)."""
     ms, reps = [], []
     for k in range(n):
-        rep = ctx.step(DT, prefactor(DT, dtmax), H, angles())
+        ang = angles() if callable(angles) else angles[k]
+        rep = ctx.step(DT, prefactor(DT, dtmax), H, ang)
         if rep["status"] != 0:
             raise RuntimeError(f"solver failed: {rep}")
         ctx.compute_all(H)
-        t = ctx.timings()
-        ms.append(float(np.sum(t)))
+        ms.append([float(x) for x in ctx.timings()])
         reps.append(rep)
-    return ms, reps
+    return np.array(ms).reshape(-1, 5), reps
 
 
 def cpu_leg(mesh, u0, steps, warmup, budget_s=25.0, levels=5):
@@ -205,19 +210,48 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+P2P_FLOPS_PER_PAIR = 9  # 3 sub, 3 fma (r^2), rsqrt, fma (q/r): FP32 + SFU
+
+
+def roofline_of(kernel, ms, units, peaks):
+    """Roofline entry of one kernel from its live per-launch device time (CUDA events)."""
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    tc = peaks.get("bf16_tflops", 1900.0)
+    src = "measured" if peaks else "fallback"
+    if kernel == "k_m2l_tc (M2L, tcgen05 3xTF32)":
+        fl = 2.0 * 100 * 100 * units["m2l_pairs"]
+        ach = fl / (ms * 1e-3) / 1e12
+        return {"kernel": kernel, "bound": "tensor", "achieved": ach, "peak": tc, "unit": "TFLOP/s",
+                "frac": ach / tc, "traffic": None, "algorithmic_per_launch": fl, "peak_source": src}
+    by = units["bytes"]
+    ach = by / (ms * 1e-3) / 1e9
+    e = {"kernel": kernel, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+         "traffic": units.get("traffic"), "algorithmic_per_launch": by, "peak_source": src}
+    return e
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="film", choices=["film", "batch64"])
     ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--train-steps", type=int, default=40, help="untimed solves that train the learned guess")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--quick", action="store_true",
+                    help="timed steps only (no training, comparisons, end-to-end or CPU legs): for profiling")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.quick:
+        args.train_steps, args.plain_steps, args.e2e_steps, args.no_cpu = 0, 0, 0, True
     if args.impl == "reference":
         reference_arm(args)
+        return
+    if args.workload == "batch64":
+        bench_batch(args)
         return
     rank, world, dist = dist_setup(args.gpus)
     import __graft_entry__
@@ -229,37 +263,39 @@ def main():
     H = np.zeros(3)
     fg.rng_seed(SEED)
     angles = fg.rng_angle
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
 
-    # FP32 body + FP64 refinement (headline)
+    # learned guess + FP32 body + FP64 refinement (headline). The guess is trained online
+    # on the solver's own solutions; those solves are not timed.
     ctx = fg.Context(mesh, regions(), tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP32_REFINE,
-                     demag=fg.FG_DEMAG_FMM, profile=0)
+                     demag=fg.FG_DEMAG_FMM, learned_guess=1, profile=1)
     ctx.set_state(u0)
     ctx.compute_all(H)  # initial compute_all of the reference loop (time_integration.cpp:140)
+    train_ms, _ = run_steps(ctx, args.train_steps, H, DT, angles)
     run_steps(ctx, args.warmup, H, DT, angles)
+    start = ctx.get_state(0)
+    ctx.fmm_timings()  # resets the stage accumulators: the stage times below are the timed region's
+    step_angles = [angles() for _ in range(args.steps)]
     launches0 = ctx.counters()[0]
     clk = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")) if world > 1 else 0)
     clk.start()
     t_wall0 = time.perf_counter()
-    ms, reps = run_steps(ctx, args.steps, H, DT, angles)
+    ms, reps = run_steps(ctx, args.steps, H, DT, step_angles)
     t_wall = time.perf_counter() - t_wall0
     clocks = clk.stop()
-    launches = (ctx.counters()[0] - launches0) // args.steps
-    dev_s = max_over_ranks(dist, float(np.sum(ms)) / 1e3)
+    fmm_stage = ctx.fmm_timings()
+    cnt = ctx.counters()
+    launches = (cnt[0] - launches0) // args.steps
+    dev_s = max_over_ranks(dist, float(ms[:, 4].sum()) / 1e3)
     value = world * args.steps / dev_s
     iters = [r["iters"] for r in reps]
     refs = [r["refinements"] for r in reps]
-
-    # stage breakdown (separate, profiled evaluations; not part of the timed region)
-    prof = fg.Context(mesh, regions(), tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP32_REFINE,
-                      demag=fg.FG_DEMAG_FMM, profile=1)
-    st = ctx.get_state(0)
-    prof.set_state(st["u"], st["v"], st["phi"], st["phiv"])
-    prof.demag(0)
-    fmm_stage = prof.fmm_timings()
-    cnt = prof.counters()
-    prof.step(DT, prefactor(DT, DT), H, 0.3)
-    phase = prof.timings()
-    prof.close()
+    acc = [r["guess_accepted"] for r in reps]
+    r0_ratio = [r["res0"] / r["res0_fallback"] for r in reps if r["res0_fallback"] > 0]
 
     # end to end through the C ABI with host buffers: state in, step, compute_all, state out
     nn = len(mesh["xyz"])
@@ -275,51 +311,57 @@ def main():
         h_u, h_v, h_phi, h_phiv = out["u"], out["v"], out["phi"], out["phiv"]
         if k:
             e2e_t.append(time.perf_counter() - t0)
-    e2e_s = max_over_ranks(dist, float(np.sum(e2e_t)))
-    e2e_value = world * len(e2e_t) / e2e_s
+    e2e_s = max_over_ranks(dist, float(np.sum(e2e_t))) if e2e_t else None
+    e2e_value = world * len(e2e_t) / e2e_s if e2e_t else None
     state_bytes = nn * 8 * 8
+    ctx.close()
 
-    # plain FP64 GPU path, same workload and tolerance
-    plain_value = None
-    plain_iters = None
-    if args.plain_steps > 0:
-        cp = fg.Context(mesh, regions(), tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP64, demag=fg.FG_DEMAG_FMM)
-        cp.set_state(u0)
-        cp.compute_all(H)
-        fg.rng_seed(SEED)
-        run_steps(cp, 1, H, DT, angles)
-        pms, preps = run_steps(cp, args.plain_steps, H, DT, angles)
-        plain_value = args.plain_steps / (float(np.sum(pms)) / 1e3)
-        plain_iters = float(np.mean([r["iters"] for r in preps]))
-        pu = cp.get_state(0)["u"]
+    # the same steps (state and angles) with the previous-step guess: what the learned guess gains
+    prev_value = prev_iters = None
+    cp = None if args.quick else fg.Context(mesh, regions(), tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP32_REFINE,
+                    demag=fg.FG_DEMAG_FMM)
+    if cp is not None:
+        cp.set_state(start["u"], start["v"], start["phi"], start["phiv"])
+        pms, preps = run_steps(cp, args.steps, H, DT, step_angles)
+        prev_value = args.steps / (float(pms[:, 4].sum()) / 1e3)
+        prev_iters = float(np.mean([r["iters"] for r in preps]))
         cp.close()
 
-    # roofline of the dominant kernel of the step
-    ms_step = float(np.mean(ms))
-    L, n_m2l, n_p2p = cnt[1], cnt[2], cnt[3]
+    # plain FP64 GPU path, same state, angles and tolerance
+    plain_value = plain_iters = None
+    if args.plain_steps > 0:
+        cp = fg.Context(mesh, regions(), tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP64, demag=fg.FG_DEMAG_FMM)
+        cp.set_state(start["u"], start["v"], start["phi"], start["phiv"])
+        n = min(args.plain_steps, args.steps)
+        pms, preps = run_steps(cp, n, H, DT, step_angles)
+        plain_value = n / (float(pms[:, 4].sum()) / 1e3)
+        plain_iters = float(np.mean([r["iters"] for r in preps]))
+        cp.close()
+
+    # roofline of the dominant kernel: per-launch device times from CUDA events in the timed region
+    ph = ms.mean(axis=0)
+    L, n_m2l, n_p2p = int(cnt[1]), float(cnt[2]), float(cnt[3])
     stage_names = ["p2m", "m2m", "m2l", "l2l", "l2p_p2p"]
-    dom = int(np.argmax(fmm_stage))
-    share = 2 * fmm_stage[dom] / ms_step
-    roof = None
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    if stage_names[dom] == "m2l":
-        flops = 2.0 * 100 * 100 * n_m2l
-        ach = flops / (fmm_stage[dom] * 1e-3) / 1e12
-        pk = peaks.get("bf16_tflops", 1900.0)
-        roof = {"kernel": "k_translate (M2L, FP32 CUDA cores)", "bound": "tensor", "achieved": ach, "peak": pk,
-                "unit": "TFLOP/s", "frac": ach / pk, "traffic": None,
-                "note": "M2L is a batched 100x100 GEMM run on FP32 CUDA cores; peak is the measured bf16 tensor peak"}
-    else:
-        # near field: pairs; bytes = leaf-local source reads (16 B per source per target leaf)
-        ach_pairs = n_p2p / (fmm_stage[dom] * 1e-3)
-        roof = {"kernel": f"{stage_names[dom]}", "bound": "hbm", "achieved": None, "peak": peaks.get("hbm_gbs"),
-                "unit": "GB/s", "frac": None, "traffic": None, "pairs_per_s": ach_pairs}
-    roof["share_of_step"] = share
-    roof["peak_source"] = "measured" if peaks else "fallback"
+    nsrc = 5 * 1200000 + 4 * 168000
+    kernels = {
+        # per step: (device ms per launch, launches per step, algorithmic units)
+        "k_l2p_p2p (near field + L2P)": (fmm_stage[4], 2, {"bytes": 16.0 * nsrc + 28.0 * nn}),
+        "k_m2l_tc (M2L, tcgen05 3xTF32)": (fmm_stage[2], 2, {"m2l_pairs": n_m2l}),
+        "k_tet64_iso + k_node64 (elements)": (ph[0], 1, {"bytes": 1200000 * (4 * 4 + 12 * 8 + 8 + 4 + 4 * 32) +
+                                                          nn * (3 * 8 + 2 * 8 + 8 * 8)}),
+    }
+    dom = max(kernels, key=lambda k: kernels[k][0] * kernels[k][1])
+    roof = roofline_of(dom, kernels[dom][0], kernels[dom][2], peaks)
+    roof["share_of_step"] = kernels[dom][0] * kernels[dom][1] / float(ms[:, 4].mean())
+    if dom.startswith("k_l2p_p2p"):
+        # the near field does one reciprocal square root per (target, source) pair: its real
+        # limit is the SFU issue rate, reported beside the HBM roof
+        sm = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+        pairs_s = n_p2p / (fmm_stage[4] * 1e-3)
+        sfu_peak = 152 * 16 * sm * 1e6
+        roof["pairs_per_s"] = pairs_s
+        roof["sfu_rsqrt_limit_pairs_per_s"] = sfu_peak
+        roof["sfu_frac"] = pairs_s / sfu_peak
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -332,15 +374,20 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded smoothed random film state)",
             "config": {"workload": "film 400x400x10 nm, 2 nm grid: 1,200,000 tets, 242,406 nodes; alpha 0.02; "
-                                   "dt 5e-14; BiCG tol 1e-6; FMM P=9",
+                                   "dt 5e-14; BiCG tol 1e-6; FMM P=9; learned guess trained online for "
+                                   f"{args.train_steps} untimed solves",
                        "global_batch": 1, "seq_len": 0, "parallelism": "replicas" if world > 1 else "single",
-                       "guess": "previous-step v (learned guess not in this line)",
-                       "l2": "working set per step > L2 (tets 163 MB + sources 107 MB + FMM operators 15 MB)"},
+                       "l2": "inputs larger than L2 (tets 163 MB + sources 107 MB + FMM operators 15 MB per step)"},
             "plain_fp64_steps_per_s": plain_value,
             "speedup_vs_plain_fp64": (value / world) / plain_value if plain_value else None,
+            "prev_guess_fp32_refine_steps_per_s": prev_value,
             "iters_per_step": float(np.mean(iters)), "refinements_per_step": float(np.mean(refs)),
-            "plain_iters_per_step": plain_iters,
-            "phase_ms": {"elements": phase[0], "solve": phase[1], "demag_x2": float(2 * np.sum(fmm_stage))},
+            "prev_guess_iters_per_step": prev_iters, "plain_iters_per_step": plain_iters,
+            "learned_guess": {"accepted_frac": float(np.mean(acc)),
+                              "res0_over_fallback_median": float(np.median(r0_ratio)) if r0_ratio else None,
+                              "train_solves": args.train_steps},
+            "phase_ms": dict(zip(["elements", "solve", "demag_x2", "energy_evolution", "step"],
+                                 [float(x) for x in ph])),
             "fmm": {"L": L, "m2l_pairs": n_m2l, "p2p_pairs": n_p2p,
                     "stage_ms": dict(zip(stage_names, [float(x) for x in fmm_stage]))},
             "roofline": roof,
@@ -354,6 +401,93 @@ def main():
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
+
+
+BATCH_N, BATCH_H = 64, 2.5
+
+
+def batch_workload(fg, seed=SEED):
+    """64 cubes, edges uniform(20, 80) nm rounded to the 2.5 nm grid, seeded applied fields of
+    magnitude uniform(0, 100) mT in random directions, uniform random initial m."""
+    rng = np.random.default_rng(seed)
+    n = np.clip(np.rint(rng.uniform(20, 80, BATCH_N) / BATCH_H), 1, None).astype(int)
+    meshes = [fg.cuboid(int(k), int(k), int(k), k * BATCH_H, k * BATCH_H, k * BATCH_H, 1e-9, MS) for k in n]
+    dirs = rng.normal(size=(BATCH_N, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    Hext = dirs * (rng.uniform(0, 0.1, BATCH_N) / fg.MU0)[:, None]
+    us = []
+    for m in meshes:
+        u = rng.normal(size=(len(m["xyz"]), 3))
+        us.append(u / np.linalg.norm(u, axis=1, keepdims=True))
+    return n, meshes, Hext, us
+
+
+def bench_batch(args):
+    """Batched samples: steps*samples/s of one batch context (one persistent solve per step,
+    graph-replayed) against looping single contexts over the samples."""
+    rank, world, dist = dist_setup(args.gpus)
+    import __graft_entry__
+    __graft_entry__.build_product()
+    import feellgood_gb300 as fg
+    dt, alpha = 1e-14, 0.1
+    regs = [dict(Ae=1e-11, Ms=795774.7, alpha=0.5), dict(Ae=AE, Ms=MS, alpha=alpha)]
+    n, meshes, Hext, us = batch_workload(fg)
+    ntets = int(sum(6 * k ** 3 for k in n))
+    b = fg.Context(meshes, regs, tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP32_REFINE,
+                   demag=fg.FG_DEMAG_FMM)
+    b.set_state(np.concatenate(us))
+    b.batch_compute_all(Hext, energies=False)
+    fg.rng_seed(SEED)
+    ang = np.array([[fg.rng_angle() for _ in range(BATCH_N)] for _ in range(args.warmup + args.steps)])
+    s, _ = b.batch_run(dt, prefactor(dt, dt), Hext, ang[:args.warmup])
+    launches0 = b.counters()[0]
+    clk = ClockSampler(0)
+    clk.start()
+    s, reps = b.batch_run(dt, prefactor(dt, dt), Hext, ang[args.warmup:])
+    clocks = clk.stop()
+    graph, dev_ms = b.batch_run_info()
+    launches = (b.counters()[0] - launches0) // args.steps
+    value = args.steps * BATCH_N / (dev_ms * 1e-3)
+    fails = int(sum(r["fails"] for r in reps))
+    iters = float(np.mean([r["iters"] / args.steps for r in reps]))
+    E = b.batch_compute_all(Hext)
+    b.close()
+
+    # looping single contexts over the samples, the same steps: plain FP64 and FP32 + refinement
+    loops = {}
+    for name, prec in (("plain_fp64", fg.FG_PREC_FP64), ("fp32_refine", fg.FG_PREC_FP32_REFINE)):
+        tot = 0.0
+        for g, m in enumerate(meshes):
+            c = fg.Context(m, regs, tol=TOL, max_iter=MAXITER, precision=prec, demag=fg.FG_DEMAG_FMM)
+            c.set_state(us[g])
+            c.compute_all(Hext[g])
+            c.step(dt, prefactor(dt, dt), Hext[g], ang[0, g])
+            c.compute_all(Hext[g])
+            k = min(2, args.steps)
+            for j in range(k):
+                r = c.step(dt, prefactor(dt, dt), Hext[g], ang[args.warmup + j, g])
+                c.compute_all(Hext[g])
+                tot += float(c.timings()[4]) / k
+            c.close()
+        loops[name] = BATCH_N / (tot * 1e-3)
+    if rank == 0:
+        line = {
+            "metric": "LLG steps*samples/s, 64 independent cubes (batched, one persistent solve per step)",
+            "value": value, "unit": "steps*samples/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"64 cubes, edges uniform(20,80) nm on a 2.5 nm grid ({n.min()}..{n.max()} "
+                                   f"cells per edge, {ntets} tets), alpha 0.1, dt 1e-14, random fields "
+                                   "0-100 mT, FP32 + FP64 refinement, forest FMM",
+                       "global_batch": BATCH_N, "seq_len": 0, "parallelism": "single"},
+            "graph_replay": bool(graph), "failed_solves": fails, "iters_per_step_mean": iters,
+            "loop_single_contexts_steps_samples_per_s": loops,
+            "speedup_vs_loop_plain_fp64": value / loops["plain_fp64"],
+            "speedup_vs_loop_fp32_refine": value / loops["fp32_refine"],
+            "gpu_launches": int(launches), "clocks": clocks,
+            "energy_sample0": [float(x) for x in E[0]],
+        }
+        print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -55,7 +55,7 @@ class fg_opts(C.Structure):
                 ("demag", C.c_int), ("fmm_order", C.c_int), ("fmm_leaf", C.c_int), ("one_gauss_point", C.c_int),
                 ("first_order", C.c_int), ("refine_max", C.c_int), ("inner_tol", C.c_double),
                 ("verbose", C.c_int), ("profile", C.c_int), ("mlp_train_steps", C.c_int), ("mlp_batch", C.c_int),
-                ("mlp_lr", C.c_double)]
+                ("mlp_lr", C.c_double), ("fmm_tensor", C.c_int)]
 
 
 class fg_step_report(C.Structure):
@@ -112,6 +112,8 @@ SIGNATURES = {
     "fg_mlp_debug_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p]),
     "fg_mlp_nparam": (C.c_int, []),
+    "fg_debug_translate_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_int]),
     "fg_batch_create": (C.c_int, [C.POINTER(fg_mesh), C.c_int, C.POINTER(fg_region), C.c_int,
                                   C.POINTER(fg_tri_region), C.c_int, C.POINTER(fg_opts), C.POINTER(C.c_void_p)]),
     "fg_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
@@ -459,6 +461,21 @@ class Context:
         return ms
 
     def timings(self):
-        ms = np.zeros(4)
+        """[elements, solve, demag, energy + evolution, whole step] device ms of the last step."""
+        ms = np.zeros(5)
         self._check(self.L.fg_timings(self.h, _dptr(ms)))
         return ms
+
+
+def debug_translate_tc(ops, tab, x, terms=7):
+    """fg_debug_translate_tc: tensor-core translation of x[n_in, 100] by ops[ncode, 100, 100]
+    through tab[n_out, ncode] (-1 = none); returns out[n_out, 100] (float32)."""
+    L = fg_lib()
+    ops = np.ascontiguousarray(ops, dtype=np.float32)
+    tab = np.ascontiguousarray(tab, dtype=np.int32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.zeros((tab.shape[0], 100), dtype=np.float32)
+    s = L.fg_debug_translate_tc(x.shape[0], tab.shape[0], tab.shape[1], _ptr(ops), _ptr(tab), _ptr(x), _ptr(out), terms)
+    if s != FG_OK:
+        raise FgError(s, "fg_debug_translate_tc")
+    return out

@@ -134,6 +134,7 @@ void fg_opts_default(fg_opts *o) {
     o->mlp_train_steps = 20;
     o->mlp_batch = 16384;
     o->mlp_lr = 1e-3;
+    o->fmm_tensor = 1;
 }
 
 const char *fg_strerror(int s) {
@@ -471,6 +472,8 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     CK(cudaMemset(c.bar, 0, sizeof(GridBar)));
     CK(dalloc(&c.dres, 1));
     CK(cudaMallocHost((void **)&c.hres, sizeof(SolveResult)));
+    CK(cudaMallocHost((void **)&c.hflag, sizeof(int)));
+    *c.hflag = 0;
     CK(dalloc(&c.src_q, c.nsrc));
     CK(dalloc(&c.tri_slot, 3 * (size_t)c.nft));
     CK(dalloc(&c.pot, nn));
@@ -617,6 +620,7 @@ void fg_destroy(fg_ctx *h) {
     batch_free(c);
     if (c.heff) cudaFree(c.heff);
     if (c.hres) cudaFreeHost(c.hres);
+    if (c.hflag) cudaFreeHost(c.hflag);
     if (c.hepart) cudaFreeHost(c.hepart);
     for (int k = 0; k < 8; k++)
         if (c.ev[k]) cudaEventDestroy(c.ev[k]);
@@ -662,9 +666,10 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
         return FG_EINVAL;
     }
     CK(cudaEventRecord(c.ev[0], c.stream));
+    c.step_open = true;
     CK(launch_tet(c, dt, Hext));
     CK(launch_node(c, basis_angle));
-    c.launches += 3;
+    c.launches += 2;
     h->last_c0 = prefactor * FG_THETA * dt * FG_GAMMA0;
     const bool use_mlp = c.mlp && mlp_steps(c) >= c.opts.mlp_train_steps;
     if (c.mlp) CK(mlp_before_solve(c, h->last_c0, use_mlp));
@@ -767,9 +772,21 @@ int fg_compute_all(fg_ctx *h, const double Hext[3], double energies[4]) {
     CK(cudaMemcpyAsync(c.phi[0], c.phi[1], n1, cudaMemcpyDeviceToDevice, c.stream));
     CK(cudaMemcpyAsync(c.phiv[0], c.phiv[1], n1, cudaMemcpyDeviceToDevice, c.stream));
     CK(cudaEventRecord(c.ev[5], c.stream));
+    if (int *fl = fmm_error_flag(c)) CK(cudaMemcpyAsync(c.hflag, fl, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
+    if (*c.hflag) {
+        c.err = "fmm: a tensor-core pipeline wait timed out";
+        *c.hflag = 0;
+        cudaMemsetAsync(fmm_error_flag(c), 0, sizeof(int), c.stream);
+        return FG_ETIMEDOUT;
+    }
     cudaEventElapsedTime(&c.ms[2], c.ev[3], c.ev[4]);
     cudaEventElapsedTime(&c.ms[3], c.ev[4], c.ev[5]);
+    // whole step on the stream's timeline: fg_step's first event to this call's last one
+    // (includes the learned guess's training kernels and the host gap between the calls)
+    c.ms[4] = c.ms[2] + c.ms[3];
+    if (c.step_open) cudaEventElapsedTime(&c.ms[4], c.ev[0], c.ev[5]);
+    c.step_open = false;
     return FG_OK;
 }
 
@@ -779,9 +796,15 @@ int fg_demag(fg_ctx *h, int which, double *out) {
     int s = demag_into(h, which ? c.v[1] : c.u[1], c.bv + 9 * 2 * (size_t)c.nn);
     if (s) return s;
     // non-magnetic nodes keep 0 in the scratch vector
-    std::vector<double> tmp(c.nn);
     CK(cudaMemcpyAsync(out, c.bv + 9 * 2 * (size_t)c.nn, sizeof(double) * c.nn, cudaMemcpyDeviceToHost, c.stream));
+    if (int *fl = fmm_error_flag(c)) CK(cudaMemcpyAsync(c.hflag, fl, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
+    if (*c.hflag) {
+        c.err = "fmm: a tensor-core pipeline wait timed out";
+        *c.hflag = 0;
+        cudaMemsetAsync(fmm_error_flag(c), 0, sizeof(int), c.stream);
+        return FG_ETIMEDOUT;
+    }
     for (int i = 0; i < c.nn; i++)
         if (!c.h_mag[i]) out[i] = 0.0;
     return FG_OK;
@@ -862,9 +885,9 @@ int fg_fmm_timings(const fg_ctx *h, double ms[5]) {
     return fmm_stage_ms(h->c, ms);
 }
 
-int fg_timings(const fg_ctx *h, double ms[4]) {
+int fg_timings(const fg_ctx *h, double ms[5]) {
     if (!h || !ms) return FG_EINVAL;
-    for (int k = 0; k < 4; k++) ms[k] = h->c.ms[k];
+    for (int k = 0; k < 5; k++) ms[k] = h->c.ms[k];
     return FG_OK;
 }
 

@@ -311,13 +311,15 @@ int fg_batch_step(fg_ctx *h, const fg_sample_step *steps, fg_step_report *reps) 
     const double H0[3] = {0, 0, 0};
     CK(cudaMemcpyAsync(c.seg_par, c.hseg_par, sizeof(SegPar) * ns, cudaMemcpyHostToDevice, c.stream));
     CK(cudaEventRecord(c.ev[0], c.stream));
+    c.step_open = true;
     CK(launch_tet(c, 1.0, H0));
     CK(launch_node(c, 0.0));
     CK(cudaEventRecord(c.ev[1], c.stream));
+    c.launches += 2;
     c.acc_active = nullptr;
     CK(launch_mixed(c, 1.0, 1.0));
     CK(cudaEventRecord(c.ev[2], c.stream));
-    c.launches += 3;
+    c.launches += 1;
     CK(cudaMemcpyAsync(c.hres, c.dres, sizeof(SolveResult) * ns, cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
     cudaEventElapsedTime(&c.ms[0], c.ev[0], c.ev[1]);
@@ -370,9 +372,19 @@ int fg_batch_compute_all(fg_ctx *h, const double *Hext, double *energies) {
     CK(cudaMemcpyAsync(c.phi[0], c.phi[1], n1, cudaMemcpyDeviceToDevice, c.stream));
     CK(cudaMemcpyAsync(c.phiv[0], c.phiv[1], n1, cudaMemcpyDeviceToDevice, c.stream));
     CK(cudaEventRecord(c.ev[5], c.stream));
+    if (int *fl = fmm_error_flag(c)) CK(cudaMemcpyAsync(c.hflag, fl, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
+    if (*c.hflag) {
+        c.err = "fmm: a tensor-core pipeline wait timed out";
+        *c.hflag = 0;
+        cudaMemsetAsync(fmm_error_flag(c), 0, sizeof(int), c.stream);
+        return FG_ETIMEDOUT;
+    }
     cudaEventElapsedTime(&c.ms[2], c.ev[3], c.ev[4]);
     cudaEventElapsedTime(&c.ms[3], c.ev[4], c.ev[5]);
+    c.ms[4] = c.ms[2] + c.ms[3];
+    if (c.step_open) cudaEventElapsedTime(&c.ms[4], c.ev[0], c.ev[5]);
+    c.step_open = false;
     if (energies)
         for (int g = 0; g < ns; g++)
             for (int k = 0; k < 4; k++) energies[4 * g + k] = c.hseg_energy[7 * g + k];
@@ -421,7 +433,15 @@ int fg_batch_run(fg_ctx *h, int n_steps, const fg_sample_step *steps, fg_batch_r
     c.launches += (long long)n_steps * body_launches(c);
     c.run_graph = (c.graph_state == 1);
     CK(cudaMemcpyAsync(c.hseg_acc, c.seg_acc, sizeof(SegAcc) * ns, cudaMemcpyDeviceToHost, c.stream));
+    if (int *fl = fmm_error_flag(c)) CK(cudaMemcpyAsync(c.hflag, fl, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
+    if (*c.hflag) {
+        c.err = "fmm: a tensor-core pipeline wait timed out";
+        *c.hflag = 0;
+        cudaMemsetAsync(fmm_error_flag(c), 0, sizeof(int), c.stream);
+        c.acc_active = nullptr;
+        return FG_ETIMEDOUT;
+    }
     c.acc_active = nullptr;
     cudaEventElapsedTime(&c.run_ms, c.ev[6], c.ev[7]);
     int worst = FG_OK;

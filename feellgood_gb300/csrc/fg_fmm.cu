@@ -53,8 +53,13 @@ struct FmmTree {
     size_t n_m2l = 0, n_p2p_pairs = 0;
     bool fp32 = false;
     double eval_ms = 0;
-    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    float stage_ms[5] = {0, 0, 0, 0, 0};
+    // profiling: two sets of stage events used in turn (recorded without synchronising); a
+    // set is read back when it is about to be reused or when the timings are requested
+    cudaEvent_t ev[2][6] = {};
+    bool ev_pending[2] = {false, false};
+    int ev_next = 0;
+    double stage_sum[5] = {0, 0, 0, 0, 0};
+    long long stage_n = 0;
     // device
     int *leaf_src = nullptr, *leaf_tgt = nullptr, *tgt_node = nullptr;
     void *sloc = nullptr;  // 4 x nsrc: leaf-local source coordinates (T), w unused
@@ -67,6 +72,13 @@ struct FmmTree {
     int *near_ptr = nullptr, *near_leaf = nullptr;
     void *M = nullptr, *F = nullptr;
     void *op_m2l = nullptr, *op_m2m = nullptr, *op_l2l = nullptr;  // [code][NR][NR] (out x in)
+    // tensor-core translations (FP32 path): per launch, for each tile of 64 output cells,
+    // the list of operator codes that bring any input to the tile
+    bool tc = false;
+    int *tc_ptr = nullptr, *tc_code = nullptr;  // tile offsets (absolute in tc_code), codes
+    std::vector<int> tc_off_m2m, tc_off_l2l;     // per level: offset of the level's tile_ptr in tc_ptr
+    int tc_off_m2l = 0;
+    int *tc_err = nullptr;                       // FG_ETIMEDOUT when a pipeline wait expired
     int *dst_keep = nullptr;
 };
 
@@ -748,6 +760,37 @@ static int fmm_build_forest(Ctx &c, int L) {
     t->n_m2l = nm2l;
     t->n_p2p_pairs = np2p;
     const FmmOps &ops = fmm_ops();
+    t->tc = fp32 && c.opts.fmm_tensor != 0;
+    if (t->tc) {
+        std::vector<int> ptr, codes;
+        auto tiles = [&](int n_out, int out0, int ncode, const std::vector<int> &tab) {
+            const int off = (int)ptr.size();
+            const int ntile = (n_out + 63) / 64;
+            for (int b = 0; b < ntile; b++) {
+                ptr.push_back((int)codes.size());
+                const int c0_ = b * 64, c1_ = std::min(n_out, c0_ + 64);
+                for (int code = 0; code < ncode; code++) {
+                    bool any = false;
+                    for (int cc = c0_; cc < c1_ && !any; cc++) any = tab[(size_t)(out0 + cc) * ncode + code] >= 0;
+                    if (any) codes.push_back(code);
+                }
+            }
+            ptr.push_back((int)codes.size());
+            return off;
+        };
+        t->tc_off_m2m.assign(L + 1, 0);
+        t->tc_off_l2l.assign(L + 1, 0);
+        for (int l = L - 1; l >= 2; l--)
+            t->tc_off_m2m[l] = tiles(t->lev_begin[l + 1] - t->lev_begin[l], t->lev_begin[l], 8, m2m_tab);
+        t->tc_off_m2l = tiles(ncell, 0, NCODE_M2L, m2l_tab);
+        for (int l = 3; l <= L; l++)
+            t->tc_off_l2l[l] = tiles(t->lev_begin[l + 1] - t->lev_begin[l], t->lev_begin[l], 8, l2l_tab);
+        FCK(up(&t->tc_ptr, ptr));
+        FCK(up(&t->tc_code, codes));
+        FCK(cudaMalloc(&t->tc_err, sizeof(int)));
+        FCK(cudaMemset(t->tc_err, 0, sizeof(int)));
+        FCK(translate_tc_setup());
+    }
     FCK(up(&t->leaf_src, leaf_src));
     FCK(up(&t->leaf_tgt, leaf_tgt));
     FCK(up(&t->tgt_node, tgt_node));
@@ -780,7 +823,8 @@ static int fmm_build_forest(Ctx &c, int L) {
         FCK(cudaFuncSetAttribute(k_translate<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_tr));
     }
     if (c.opts.profile)
-        for (auto &e : t->ev) FCK(cudaEventCreate(&e));
+        for (auto &set : t->ev)
+            for (auto &e : set) FCK(cudaEventCreate(&e));
     if (c.opts.verbose)
         fprintf(stderr, "fmm: L=%d trees=%d leaves=%d cells=%d m2l=%zu p2p_pairs=%zu (%s)\n", L, nseg, nleaf, ncell,
                 t->n_m2l, t->n_p2p_pairs, fp32 ? "fp32" : "fp64");
@@ -791,13 +835,32 @@ void fmm_free(Ctx &c) {
     FmmTree *t = static_cast<FmmTree *>(c.fmm);
     if (!t) return;
     void *ptrs[] = {t->leaf_scale, t->leaf_src, t->leaf_tgt, t->tgt_node, t->sloc, t->tloc, t->leaf_ijk, t->m2l_tab, t->m2m_tab,
-                    t->l2l_tab, t->near_ptr, t->near_leaf, t->M, t->F, t->op_m2l, t->op_m2m, t->op_l2l};
+                    t->l2l_tab, t->near_ptr, t->near_leaf, t->M, t->F, t->op_m2l, t->op_m2m, t->op_l2l,
+                    t->tc_ptr, t->tc_code, t->tc_err};
     for (void *p : ptrs)
         if (p) cudaFree(p);
-    for (auto &e : t->ev)
-        if (e) cudaEventDestroy(e);
+    for (auto &set : t->ev)
+        for (auto &e : set)
+            if (e) cudaEventDestroy(e);
     delete t;
     c.fmm = nullptr;
+}
+
+template <typename T> static bool tc_path(const FmmTree &t);
+template <> bool tc_path<float>(const FmmTree &t) { return t.tc; }
+template <> bool tc_path<double>(const FmmTree &) { return false; }
+
+// Adds the stage times of a recorded event set to the running sums (waits for its last event).
+static void harvest_set(FmmTree &t, int k) {
+    if (!t.ev_pending[k]) return;
+    cudaEventSynchronize(t.ev[k][5]);
+    for (int s = 0; s < 5; s++) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, t.ev[k][s], t.ev[k][s + 1]);
+        t.stage_sum[s] += ms;
+    }
+    t.stage_n++;
+    t.ev_pending[k] = false;
 }
 
 template <typename T>
@@ -806,38 +869,42 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
     T *M = (T *)t.M, *F = (T *)t.F;
     const size_t esz = sizeof(T);
     const int smem_p2m = (int)(NR * 65 * esz), smem_tr = (int)((NR * NR + NR * (TB + 4)) * esz);
-    const bool prof = c.opts.profile && t.ev[0];
-    if (prof) cudaEventRecord(t.ev[0], c.stream);
+    const bool prof = c.opts.profile && t.ev[0][0];
+    cudaEvent_t *ev = t.ev[t.ev_next];
+    if (prof) {
+        harvest_set(t, t.ev_next);
+        cudaEventRecord(ev[0], c.stream);
+    }
     k_p2m<T><<<t.nleaf, 64, smem_p2m, c.stream>>>(t.nleaf, t.leaf_src, (T *)t.sloc, c.src_q, t.leaf0, M);
-    if (prof) cudaEventRecord(t.ev[1], c.stream);
-    for (int l = L - 1; l >= 2; l--) {
-        const int n = t.lev_begin[l + 1] - t.lev_begin[l];
-        if (n)
-            k_translate<T><<<(n + TB - 1) / TB, 160, smem_tr, c.stream>>>(n, t.lev_begin[l], 8, t.m2m_tab,
-                                                                            (const T *)t.op_m2m, M, M, 0);
-    }
-    if (prof) cudaEventRecord(t.ev[2], c.stream);
-    k_translate<T><<<(t.ncell + TB - 1) / TB, 160, smem_tr, c.stream>>>(t.ncell, 0, NCODE_M2L, t.m2l_tab,
-                                                                          (const T *)t.op_m2l, M, F, 0);
-    if (prof) cudaEventRecord(t.ev[3], c.stream);
-    for (int l = 3; l <= L; l++) {
-        const int n = t.lev_begin[l + 1] - t.lev_begin[l];
-        if (n)
-            k_translate<T><<<(n + TB - 1) / TB, 160, smem_tr, c.stream>>>(n, t.lev_begin[l], 8, t.l2l_tab,
-                                                                            (const T *)t.op_l2l, F, F, 1);
-    }
-    if (prof) cudaEventRecord(t.ev[4], c.stream);
+    if (prof) cudaEventRecord(ev[1], c.stream);
+    // out (+)= sum_code Op[code] in[tab[cell][code]] over n output cells from out0
+    auto translate = [&](int n, int out0, int ncode, const int *tab, const void *ops, T *in, T *out, int acc,
+                         int tc_off) {
+        if (!n) return;
+        if (tc_path<T>(t))
+            launch_translate_tc(c.stream, n, out0, ncode, tab, (const float *)ops, (const float *)in, (float *)out,
+                                acc, t.tc_ptr + tc_off, t.tc_code, t.tc_err);
+        else
+            k_translate<T><<<(n + TB - 1) / TB, 160, smem_tr, c.stream>>>(n, out0, ncode, tab, (const T *)ops, in,
+                                                                            out, acc);
+    };
+    for (int l = L - 1; l >= 2; l--)
+        translate(t.lev_begin[l + 1] - t.lev_begin[l], t.lev_begin[l], 8, t.m2m_tab, t.op_m2m, M, M, 0,
+                  t.tc ? t.tc_off_m2m[l] : 0);
+    if (prof) cudaEventRecord(ev[2], c.stream);
+    translate(t.ncell, 0, NCODE_M2L, t.m2l_tab, t.op_m2l, M, F, 0, t.tc_off_m2l);
+    if (prof) cudaEventRecord(ev[3], c.stream);
+    for (int l = 3; l <= L; l++)
+        translate(t.lev_begin[l + 1] - t.lev_begin[l], t.lev_begin[l], 8, t.l2l_tab, t.op_l2l, F, F, 1,
+                  t.tc ? t.tc_off_l2l[l] : 0);
+    if (prof) cudaEventRecord(ev[4], c.stream);
     k_l2p_p2p<T><<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node,
                                                            (const T *)t.tloc, (const T *)t.sloc, t.leaf_ijk, t.leaf0,
                                                            t.leaf_scale, t.near_ptr, t.near_leaf, F, c.pot);
     if (prof) {
-        cudaEventRecord(t.ev[5], c.stream);
-        cudaEventSynchronize(t.ev[5]);
-        cudaEventElapsedTime(&t.stage_ms[0], t.ev[0], t.ev[1]);
-        cudaEventElapsedTime(&t.stage_ms[1], t.ev[1], t.ev[2]);
-        cudaEventElapsedTime(&t.stage_ms[2], t.ev[2], t.ev[3]);
-        cudaEventElapsedTime(&t.stage_ms[3], t.ev[3], t.ev[4]);
-        cudaEventElapsedTime(&t.stage_ms[4], t.ev[4], t.ev[5]);
+        cudaEventRecord(ev[5], c.stream);
+        t.ev_pending[t.ev_next] = true;
+        t.ev_next ^= 1;
     }
     return cudaGetLastError();
 }
@@ -849,10 +916,19 @@ cudaError_t fmm_eval(Ctx &c) {
 }
 
 int fmm_stage_ms(const Ctx &c, double ms[5]) {
-    const FmmTree *t = static_cast<const FmmTree *>(c.fmm);
+    FmmTree *t = static_cast<FmmTree *>(c.fmm);
     if (!t) return FG_EINVAL;
-    for (int k = 0; k < 5; k++) ms[k] = t->stage_ms[k];
+    harvest_set(*t, t->ev_next ^ 1);
+    harvest_set(*t, t->ev_next);
+    for (int k = 0; k < 5; k++) ms[k] = t->stage_n ? t->stage_sum[k] / t->stage_n : 0.0;
+    for (double &x : t->stage_sum) x = 0.0;
+    t->stage_n = 0;
     return FG_OK;
+}
+
+int *fmm_error_flag(const Ctx &c) {
+    const FmmTree *t = static_cast<const FmmTree *>(c.fmm);
+    return t ? t->tc_err : nullptr;
 }
 
 int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p) {

@@ -184,6 +184,7 @@ struct Ctx {
     GridBar *bar = nullptr;
     SolveResult *dres = nullptr;
     SolveResult *hres = nullptr;  // pinned
+    int *hflag = nullptr;         // pinned copy of the FMM error flag
 
     // device: demag
     std::vector<double> h_src_xyz;  // source points (original order), host copy for the FMM tree
@@ -204,7 +205,8 @@ struct Ctx {
 
     // timings
     cudaEvent_t ev[8];
-    float ms[4] = {0, 0, 0, 0};
+    float ms[5] = {0, 0, 0, 0, 0};
+    bool step_open = false;  // ev[0] recorded by a step not yet closed by compute_all
     long long launches = 0;  // kernels launched by this context
     void *mlp = nullptr;     // learned initial guess (fg_mlp.cu)
     double *heff = nullptr;  // per-node BE/A (effective field), written when the learned guess is on
@@ -249,6 +251,13 @@ int bicg_grid_size(Ctx &c, bool mixed);
 int mixed_grid_size(Ctx &c);
 int mixed_max_blocks(Ctx &c);
 int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p);
+int *fmm_error_flag(const Ctx &c);  // device int: FG_ETIMEDOUT after an expired wait (or nullptr)
+// tensor-core translations (fg_fmm_tc.cu)
+int translate_tc_smem();
+cudaError_t translate_tc_setup();
+cudaError_t launch_translate_tc(cudaStream_t st, int n_out, int out0, int ncode, const int *tab, const float *ops,
+                                const float *in, float *out, int accumulate, const int *tile_ptr,
+                                const int *tile_code, int *err, int terms = 7);
 int fmm_stage_ms(const Ctx &c, double ms[5]);
 int mlp_create(Ctx &c);
 void mlp_free(Ctx &c);

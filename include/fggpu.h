@@ -92,6 +92,8 @@ typedef struct {
     int mlp_train_steps;  /* learned guess: solves that only train before the guess is proposed */
     int mlp_batch;        /* learned guess: nodes per training minibatch */
     double mlp_lr;        /* learned guess: Adam learning rate */
+    int fmm_tensor;       /* FP32 FMM: 1 (default) translations on the tensor cores (3 x TF32 MMAs),
+                             0 on the CUDA cores */
 } fg_opts;
 
 typedef struct {
@@ -155,8 +157,10 @@ int fg_debug_system(fg_ctx *ctx, double *rhs, double *ep, double *eq);
 int fg_debug_apply(fg_ctx *ctx, const double *x, double *y);
 
 /* Device time of the last fg_step / fg_compute_all phases, in ms:
- * [0] elements, [1] solve, [2] demag, [3] energy+evolution. */
-int fg_timings(const fg_ctx *ctx, double ms[4]);
+ * [0] elements, [1] solve, [2] demag, [3] energy+evolution, [4] the whole step on the
+ * stream's timeline from fg_step's start to fg_compute_all's end (adds the learned guess's
+ * training kernels and any host gap between the two calls). */
+int fg_timings(const fg_ctx *ctx, double ms[5]);
 
 /* Counters: [0] kernels launched by the context so far, [1] FMM tree depth (0 without FMM),
  * [2] M2L (cell, cell) pairs, [3] P2P (target, source) pairs per evaluation. */
@@ -218,8 +222,17 @@ int fg_batch_run(fg_ctx *ctx, int n_steps, const fg_sample_step *steps, fg_batch
  * launches) and its device time in ms (CUDA events around the steps). Either may be NULL. */
 int fg_batch_run_info(const fg_ctx *ctx, int *graph_used, double *device_ms);
 
-/* Device ms of the stages of the last FMM evaluation when opts.profile is set:
- * [0] P2M, [1] M2M, [2] M2L, [3] L2L, [4] L2P + P2P. */
+/* Precision check of the tensor-core FMM translation (no reference counterpart): runs the
+ * kernel once on host data, out[c*100 + i] = sum_code sum_j ops[code][i][j] in[tab[c][code]][j]
+ * (tab entries -1 = no input; 100 coefficients per expansion), with the product terms of
+ * the TF32 hi/lo split selected by terms (bit 0 hi*hi, bit 1 hi*lo, bit 2 lo*hi; 7 is what
+ * the FMM uses). Allocates and frees its own device buffers. */
+int fg_debug_translate_tc(int n_in, int n_out, int ncode, const float *ops, const int *tab, const float *in,
+                          float *out, int terms);
+
+/* Device ms of the FMM stages when opts.profile is set, averaged over the evaluations
+ * since the previous call (CUDA events around each stage, recorded without any extra
+ * synchronisation): [0] P2M, [1] M2M, [2] M2L, [3] L2L, [4] L2P + P2P. */
 int fg_fmm_timings(const fg_ctx *ctx, double ms[5]);
 
 /* ---- host-side mesh set-up (no GPU work) ----------------------------------------

@@ -46,3 +46,47 @@ def test_direct_matches_oracle():
     cf = fg.Context(m, cases.regions(), demag=fg.FG_DEMAG_FMM, fmm_leaf=50)
     cf.set_state(u)
     assert _rel(cf.demag(0), o.demag(0)) < 1e-5
+
+
+@pytest.mark.parametrize("shape,leaf", [((12, 12, 12), -3), ((40, 40, 3), -4), ((24, 20, 6), 60)])
+def test_tensor_core_translations(shape, leaf):
+    """FP32 FMM with the tcgen05 translations (3 x TF32) against the CUDA-core FP32
+    translations and the exact sum: the same accuracy, agreement to FP32 rounding."""
+    m = cases.cuboid(*shape)
+    u = cases.perturbed_state(m["xyz"], seed=7, sigma=0.3)
+    v = cases.tangent_field(u, seed=8)
+    cd = fg.Context(m, cases.regions(), demag=fg.FG_DEMAG_DIRECT)
+    cd.set_state(u, v)
+    ct = fg.Context(m, cases.regions(), demag=fg.FG_DEMAG_FMM, precision=fg.FG_PREC_FP32_REFINE, fmm_leaf=leaf)
+    ct.set_state(u, v)
+    cc = fg.Context(m, cases.regions(), demag=fg.FG_DEMAG_FMM, precision=fg.FG_PREC_FP32_REFINE, fmm_leaf=leaf,
+                    fmm_tensor=0)
+    cc.set_state(u, v)
+    for which, bound in ((0, 1e-5), (1, 1e-4)):
+        pd, pt, pc = cd.demag(which), ct.demag(which), cc.demag(which)
+        assert _rel(pt, pd) < bound
+        assert _rel(pt, pc) < 3e-6
+
+
+def test_tensor_core_split_precision():
+    """The tcgen05 translation on random data against an FP64 product: the three-term TF32
+    split (hi*hi + hi*lo + lo*hi) must give FP32-level accuracy, far below one TF32 term."""
+    rng = np.random.default_rng(11)
+    ncode, n_in, n_out = 7, 300, 200
+    ops = rng.normal(size=(ncode, 100, 100)) * np.exp(rng.uniform(-3, 3, size=(ncode, 100, 1)))
+    x = rng.normal(size=(n_in, 100))
+    tab = rng.integers(-1, n_in, size=(n_out, ncode))
+    tab[5] = -1  # a cell with no input
+    ref = np.zeros((n_out, 100))
+    for c in range(n_out):
+        for k in range(ncode):
+            if tab[c, k] >= 0:
+                ref[c] += ops[k].astype(np.float32).astype(np.float64) @ x[tab[c, k]].astype(np.float32)
+    err = {}
+    for terms in (1, 7):
+        out = fg.api.debug_translate_tc(ops, tab, x, terms)
+        err[terms] = np.linalg.norm(out - ref) / np.linalg.norm(ref)
+        assert np.all(out[5] == 0)
+    print("tensor-core translation rel. error: 1 term %.2e, 3 terms %.2e" % (err[1], err[7]))
+    assert err[7] < 1.5e-6
+    assert err[7] < err[1] / 30
