@@ -719,10 +719,7 @@ static int demag_into(fg_ctx *h, const double *m, double *phi_out) {
     CK(launch_charges(c, m));
     if (c.opts.demag == FG_DEMAG_FMM) {
         CK(fmm_eval(c));
-        int L = 0, nl = 0;
-        double a, b;
-        fmm_info(c, &L, &nl, &a, &b);
-        c.launches += 3 + 2 * (L - 2);
+        c.launches += fmm_launches_per_eval(c);
     } else {
         CK(launch_p2p_direct(c));
         c.launches += 1;

@@ -203,12 +203,7 @@ static void fill_par(SegPar &P, const fg_sample_step &s) {
     P.c0 = s.prefactor * FG_THETA * s.dt * FG_GAMMA0;
 }
 
-static int fmm_launch_count(const Ctx &c) {
-    int L = 0, nl = 0;
-    double a = 0, b = 0;
-    fmm_info(c, &L, &nl, &a, &b);
-    return 3 + 2 * (L - 2);
-}
+static int fmm_launch_count(const Ctx &c) { return fmm_launches_per_eval(c); }
 
 static cudaError_t batch_demag(Ctx &c, const double *m, double *phi) {
     cudaError_t e = launch_charges(c, m);

@@ -75,10 +75,15 @@ struct FmmTree {
     // tensor-core translations (FP32 path): per launch, for each tile of 64 output cells,
     // the list of operator codes that bring any input to the tile
     bool tc = false;
-    int *tc_ptr = nullptr, *tc_code = nullptr;  // tile offsets (absolute in tc_code), codes
-    std::vector<int> tc_off_m2m, tc_off_l2l;     // per level: offset of the level's tile_ptr in tc_ptr
-    int tc_off_m2l = 0;
+    int *tc_code = nullptr;                      // codes per tile, all launches
+    int4 *tc_units = nullptr, *tc_comb = nullptr;
+    float *tc_scratch = nullptr;
+    struct TcLaunch { int unit0 = 0, nunit = 0, comb0 = 0, ncomb = 0; };
+    std::vector<TcLaunch> tc_m2m, tc_l2l;        // per level
+    TcLaunch tc_m2l;
     int *tc_err = nullptr;                       // FG_ETIMEDOUT when a pipeline wait expired
+    float *Mh = nullptr, *Ml = nullptr, *Fh = nullptr, *Fl = nullptr;  // hi/lo splits of M and F
+    unsigned char *img_m2l = nullptr, *img_m2m = nullptr, *img_l2l = nullptr;  // operator images
     int *dst_keep = nullptr;
 };
 
@@ -200,7 +205,8 @@ __device__ __forceinline__ void ups_cols(T x, T y, T z, Fn &&f) {
 // shared tile, each coefficient is summed over the tile in a fixed order.
 template <typename T>
 __global__ void __launch_bounds__(64) k_p2m(int nleaf, const int *__restrict__ leaf_src, T *__restrict__ sloc,
-                                            const double *__restrict__ q, int leaf0, T *__restrict__ M) {
+                                            const double *__restrict__ q, int leaf0, T *__restrict__ M,
+                                            float *__restrict__ Mh, float *__restrict__ Ml) {
     constexpr int LD = 65;
     extern __shared__ unsigned char smem_raw[];
     T *tile = reinterpret_cast<T *>(smem_raw);  // [NR][LD]
@@ -234,7 +240,16 @@ __global__ void __launch_bounds__(64) k_p2m(int nleaf, const int *__restrict__ l
 #pragma unroll
     for (int h = 0; h < 2; h++) {
         const int j = tid + 64 * h;
-        if (j < NR) M[(size_t)(leaf0 + leaf) * NR + j] = acc[h];
+        if (j < NR) {
+            const size_t o = (size_t)(leaf0 + leaf) * NR + j;
+            M[o] = acc[h];
+            if (Mh) {  // split for the tensor-core translations: hi = tf32(x), lo = x - hi
+                const float x = (float)acc[h];
+                const float hi = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+                Mh[o] = hi;
+                Ml[o] = x - hi;
+            }
+        }
     }
 }
 
@@ -296,9 +311,13 @@ __global__ void __launch_bounds__(160) k_translate(int n_out, int out0, int ncod
     }
 }
 
-// 1/sqrt in the precision of the path (CUDA's rsqrtf / rsqrt).
+// 1/sqrt in the precision of the path.
 template <typename T> __device__ __forceinline__ T rsqrt_p(T x);
-template <> __device__ __forceinline__ float rsqrt_p<float>(float x) { return rsqrtf(x); }
+template <> __device__ __forceinline__ float rsqrt_p<float>(float x) {
+    float r;  // the SFU reciprocal square root (relative error below 2^-22), denormals flushed
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 template <> __device__ __forceinline__ double rsqrt_p<double>(double x) { return rsqrt(x); }
 
 template <typename T> struct Vec4;
@@ -306,12 +325,12 @@ template <> struct Vec4<float> { using type = float4; };
 template <> struct Vec4<double> { using type = double4; };
 
 // L2P + P2P: one warp per leaf. Sources of the adjacent leaves are spread over the lanes
-// (x, y, z, q in one vector load), up to NT targets of the leaf are held in registers;
-// coordinates are leaf-local (leaf units), so FP32 keeps the relative precision of close
-// pairs. Per-lane partial sums of each adjacent leaf are added in FP64, reduced over the
-// warp in a fixed order.
+// (x, y, z, q in one vector load; each lane takes two sources per pass and already loads
+// the next two), up to NT targets of the leaf are held in registers; coordinates are
+// leaf-local (leaf units), so FP32 keeps the relative precision of close pairs. The
+// per-lane sums are reduced over the warp in FP64 in a fixed order.
 template <typename T>
-__global__ void __launch_bounds__(128) k_l2p_p2p(int nleaf, const int *__restrict__ leaf_src,
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1) k_l2p_p2p(int nleaf, const int *__restrict__ leaf_src,
                                                  const int *__restrict__ leaf_tgt, const int *__restrict__ tgt_node,
                                                  const T *__restrict__ tloc, const T *__restrict__ sloc,
                                                  const int *__restrict__ leaf_ijk, int leaf0,
@@ -330,15 +349,14 @@ __global__ void __launch_bounds__(128) k_l2p_p2p(int nleaf, const int *__restric
     const T *Fl = F + (size_t)(leaf0 + leaf) * NR;
     for (int tb = t0; tb < t1; tb += NT) {
         const int nt = min(NT, t1 - tb);
-        T tx[NT], ty[NT], tz[NT];
-        double near[NT];
+        T tx[NT], ty[NT], tz[NT], ns[NT];
 #pragma unroll
         for (int j = 0; j < NT; j++) {
             const int ti = tb + (j < nt ? j : 0);
             tx[j] = tloc[4 * (size_t)ti];
             ty[j] = tloc[4 * (size_t)ti + 1];
             tz[j] = tloc[4 * (size_t)ti + 2];
-            near[j] = 0.0;
+            ns[j] = 0;
         }
         for (int e = near_ptr[leaf]; e < near_ptr[leaf + 1]; e++) {
             const int nl = near_leaf[e];
@@ -348,21 +366,36 @@ __global__ void __launch_bounds__(128) k_l2p_p2p(int nleaf, const int *__restric
             T acc[NT];
 #pragma unroll
             for (int j = 0; j < NT; j++) acc[j] = 0;
-            for (int s = s0 + lane; s < s1; s += 32) {
-                const V4 sv = src4[s];
-                const T sx = sv.x + ox, sy = sv.y + oy, sz = sv.z + oz, qq = sv.w;
+            // two sources per lane and pass, the next two already in flight; a missing source
+            // is a zero charge far away
+            V4 far;
+            far.x = far.y = far.z = T(1e4);
+            far.w = T(0);
+            int s = s0 + lane;
+            V4 na = s < s1 ? src4[s] : far, nb = s + 32 < s1 ? src4[s + 32] : far;
+            for (; s < s1; s += 64) {
+                const V4 sa = na, sb = nb;
+                na = s + 64 < s1 ? src4[s + 64] : far;
+                nb = s + 96 < s1 ? src4[s + 96] : far;
+                const T ax = sa.x + ox, ay = sa.y + oy, az = sa.z + oz, aq = sa.w;
+                const T bx = sb.x + ox, by = sb.y + oy, bz = sb.z + oz, bq = sb.w;
 #pragma unroll
                 for (int j = 0; j < NT; j++) {
-                    const T dx = tx[j] - sx, dy = ty[j] - sy, dz = tz[j] - sz;
-                    acc[j] += qq * rsqrt_p<T>(dx * dx + dy * dy + dz * dz);
+                    const T dx = tx[j] - ax, dy = ty[j] - ay, dz = tz[j] - az;
+                    const T ex = tx[j] - bx, ey = ty[j] - by, ez = tz[j] - bz;
+                    acc[j] += aq * rsqrt_p<T>(dx * dx + dy * dy + dz * dz);
+                    acc[j] += bq * rsqrt_p<T>(ex * ex + ey * ey + ez * ez);
                 }
             }
 #pragma unroll
-            for (int j = 0; j < NT; j++) near[j] += double(acc[j]);
+            for (int j = 0; j < NT; j++) ns[j] += acc[j];
         }
+        double near[NT];
 #pragma unroll
-        for (int j = 0; j < NT; j++)
+        for (int j = 0; j < NT; j++) {
+            near[j] = double(ns[j]);
             for (int o = 16; o > 0; o >>= 1) near[j] += __shfl_xor_sync(0xffffffffu, near[j], o);
+        }
         // L2P: lane j evaluates target j
         if (lane < nt) {
             T x = 0, y = 0, z = 0;
@@ -762,34 +795,47 @@ static int fmm_build_forest(Ctx &c, int L) {
     const FmmOps &ops = fmm_ops();
     t->tc = fp32 && c.opts.fmm_tensor != 0;
     if (t->tc) {
-        std::vector<int> ptr, codes;
-        auto tiles = [&](int n_out, int out0, int ncode, const std::vector<int> &tab) {
-            const int off = (int)ptr.size();
-            const int ntile = (n_out + 63) / 64;
-            for (int b = 0; b < ntile; b++) {
-                ptr.push_back((int)codes.size());
-                const int c0_ = b * 64, c1_ = std::min(n_out, c0_ + 64);
-                for (int code = 0; code < ncode; code++) {
-                    bool any = false;
-                    for (int cc = c0_; cc < c1_ && !any; cc++) any = tab[(size_t)(out0 + cc) * ncode + code] >= 0;
-                    if (any) codes.push_back(code);
-                }
-            }
-            ptr.push_back((int)codes.size());
-            return off;
+        std::vector<int> codes;
+        std::vector<int4> units, comb;
+        int nslot = 0;
+        auto plan = [&](int n_out, int out0, int ncode, const std::vector<int> &tab, int max_codes) {
+            FmmTree::TcLaunch l;
+            l.unit0 = (int)units.size();
+            l.comb0 = (int)comb.size();
+            translate_tc_units(n_out, ncode, tab.data(), out0, max_codes, codes, units, comb, nslot);
+            l.nunit = (int)units.size() - l.unit0;
+            l.ncomb = (int)comb.size() - l.comb0;
+            return l;
         };
-        t->tc_off_m2m.assign(L + 1, 0);
-        t->tc_off_l2l.assign(L + 1, 0);
+        t->tc_m2m.assign(L + 1, FmmTree::TcLaunch());
+        t->tc_l2l.assign(L + 1, FmmTree::TcLaunch());
         for (int l = L - 1; l >= 2; l--)
-            t->tc_off_m2m[l] = tiles(t->lev_begin[l + 1] - t->lev_begin[l], t->lev_begin[l], 8, m2m_tab);
-        t->tc_off_m2l = tiles(ncell, 0, NCODE_M2L, m2l_tab);
+            t->tc_m2m[l] = plan(t->lev_begin[l + 1] - t->lev_begin[l], t->lev_begin[l], 8, m2m_tab, 8);
+        t->tc_m2l = plan(ncell, 0, NCODE_M2L, m2l_tab, 48);
         for (int l = 3; l <= L; l++)
-            t->tc_off_l2l[l] = tiles(t->lev_begin[l + 1] - t->lev_begin[l], t->lev_begin[l], 8, l2l_tab);
-        FCK(up(&t->tc_ptr, ptr));
+            t->tc_l2l[l] = plan(t->lev_begin[l + 1] - t->lev_begin[l], t->lev_begin[l], 8, l2l_tab, 8);
         FCK(up(&t->tc_code, codes));
+        FCK(up(&t->tc_units, units));
+        FCK(up(&t->tc_comb, comb));
+        FCK(cudaMalloc(&t->tc_scratch, sizeof(float) * (size_t)std::max(1, nslot) * 64 * NR));
         FCK(cudaMalloc(&t->tc_err, sizeof(int)));
         FCK(cudaMemset(t->tc_err, 0, sizeof(int)));
         FCK(translate_tc_setup());
+        const size_t nexp = (size_t)ncell * NR;
+        FCK(cudaMalloc(&t->Mh, nexp * sizeof(float)));
+        FCK(cudaMalloc(&t->Ml, nexp * sizeof(float)));
+        FCK(cudaMalloc(&t->Fh, nexp * sizeof(float)));
+        FCK(cudaMalloc(&t->Fl, nexp * sizeof(float)));
+        FCK(cudaMemset(t->Mh, 0, nexp * sizeof(float)));
+        FCK(cudaMemset(t->Ml, 0, nexp * sizeof(float)));
+        FCK(cudaMemset(t->Fh, 0, nexp * sizeof(float)));
+        FCK(cudaMemset(t->Fl, 0, nexp * sizeof(float)));
+        static const std::vector<float> im2l = translate_tc_images(ops.m2l, NCODE_M2L);
+        static const std::vector<float> im2m = translate_tc_images(ops.m2m, 8);
+        static const std::vector<float> il2l = translate_tc_images(ops.l2l, 8);
+        FCK(up((float **)&t->img_m2l, im2l));
+        FCK(up((float **)&t->img_m2m, im2m));
+        FCK(up((float **)&t->img_l2l, il2l));
     }
     FCK(up(&t->leaf_src, leaf_src));
     FCK(up(&t->leaf_tgt, leaf_tgt));
@@ -836,7 +882,8 @@ void fmm_free(Ctx &c) {
     if (!t) return;
     void *ptrs[] = {t->leaf_scale, t->leaf_src, t->leaf_tgt, t->tgt_node, t->sloc, t->tloc, t->leaf_ijk, t->m2l_tab, t->m2m_tab,
                     t->l2l_tab, t->near_ptr, t->near_leaf, t->M, t->F, t->op_m2l, t->op_m2m, t->op_l2l,
-                    t->tc_ptr, t->tc_code, t->tc_err};
+                    t->tc_code, t->tc_units, t->tc_comb, t->tc_scratch, t->tc_err, t->Mh, t->Ml, t->Fh, t->Fl,
+                    t->img_m2l, t->img_m2m, t->img_l2l};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &set : t->ev)
@@ -875,28 +922,47 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
         harvest_set(t, t.ev_next);
         cudaEventRecord(ev[0], c.stream);
     }
-    k_p2m<T><<<t.nleaf, 64, smem_p2m, c.stream>>>(t.nleaf, t.leaf_src, (T *)t.sloc, c.src_q, t.leaf0, M);
+    const bool tc = tc_path<T>(t);
+    k_p2m<T><<<t.nleaf, 64, smem_p2m, c.stream>>>(t.nleaf, t.leaf_src, (T *)t.sloc, c.src_q, t.leaf0, M,
+                                                    tc ? t.Mh : nullptr, tc ? t.Ml : nullptr);
     if (prof) cudaEventRecord(ev[1], c.stream);
     // out (+)= sum_code Op[code] in[tab[cell][code]] over n output cells from out0
-    auto translate = [&](int n, int out0, int ncode, const int *tab, const void *ops, T *in, T *out, int acc,
-                         int tc_off) {
+    // out (+)= sum_code Op[code] in[tab[cell][code]] over n output cells from out0; the
+    // tensor-core form reads the inputs' hi/lo split and writes the outputs' split
+    enum { M2M, M2L, L2L };
+    auto translate = [&](int kind, int n, int out0, const FmmTree::TcLaunch &tl) {
         if (!n) return;
-        if (tc_path<T>(t))
-            launch_translate_tc(c.stream, n, out0, ncode, tab, (const float *)ops, (const float *)in, (float *)out,
-                                acc, t.tc_ptr + tc_off, t.tc_code, t.tc_err);
-        else
+        const int ncode = kind == M2L ? NCODE_M2L : 8;
+        const int *tab = kind == M2M ? t.m2m_tab : kind == M2L ? t.m2l_tab : t.l2l_tab;
+        if (tc) {
+            TcArgs a{};
+            a.n_out = n; a.out0 = out0; a.ncode = ncode; a.tab = tab;
+            a.op_img = kind == M2M ? t.img_m2m : kind == M2L ? t.img_m2l : t.img_l2l;
+            a.in_hi = kind == L2L ? t.Fh : t.Mh;
+            a.in_lo = kind == L2L ? t.Fl : t.Ml;
+            a.out = (float *)(kind == M2M ? M : F);
+            a.out_hi = kind == M2M ? t.Mh : t.Fh;
+            a.out_lo = kind == M2M ? t.Ml : t.Fl;
+            a.accumulate = kind == L2L;
+            a.tile_code = t.tc_code; a.err = t.tc_err; a.terms = 7;
+            a.units = t.tc_units + tl.unit0; a.nunits = tl.nunit;
+            a.comb = t.tc_comb + tl.comb0; a.ncomb = tl.ncomb; a.scratch = t.tc_scratch;
+            launch_translate_tc(c.stream, a);
+        } else {
+            const void *ops = kind == M2M ? t.op_m2m : kind == M2L ? t.op_m2l : t.op_l2l;
+            T *in = kind == L2L ? F : M, *out = kind == M2M ? M : F;
             k_translate<T><<<(n + TB - 1) / TB, 160, smem_tr, c.stream>>>(n, out0, ncode, tab, (const T *)ops, in,
-                                                                            out, acc);
+                                                                            out, kind == L2L);
+        }
     };
+    const FmmTree::TcLaunch none;
     for (int l = L - 1; l >= 2; l--)
-        translate(t.lev_begin[l + 1] - t.lev_begin[l], t.lev_begin[l], 8, t.m2m_tab, t.op_m2m, M, M, 0,
-                  t.tc ? t.tc_off_m2m[l] : 0);
+        translate(M2M, t.lev_begin[l + 1] - t.lev_begin[l], t.lev_begin[l], t.tc ? t.tc_m2m[l] : none);
     if (prof) cudaEventRecord(ev[2], c.stream);
-    translate(t.ncell, 0, NCODE_M2L, t.m2l_tab, t.op_m2l, M, F, 0, t.tc_off_m2l);
+    translate(M2L, t.ncell, 0, t.tc_m2l);
     if (prof) cudaEventRecord(ev[3], c.stream);
     for (int l = 3; l <= L; l++)
-        translate(t.lev_begin[l + 1] - t.lev_begin[l], t.lev_begin[l], 8, t.l2l_tab, t.op_l2l, F, F, 1,
-                  t.tc ? t.tc_off_l2l[l] : 0);
+        translate(L2L, t.lev_begin[l + 1] - t.lev_begin[l], t.lev_begin[l], t.tc ? t.tc_l2l[l] : none);
     if (prof) cudaEventRecord(ev[4], c.stream);
     k_l2p_p2p<T><<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node,
                                                            (const T *)t.tloc, (const T *)t.sloc, t.leaf_ijk, t.leaf0,
@@ -924,6 +990,16 @@ int fmm_stage_ms(const Ctx &c, double ms[5]) {
     for (double &x : t->stage_sum) x = 0.0;
     t->stage_n = 0;
     return FG_OK;
+}
+
+int fmm_launches_per_eval(const Ctx &c) {
+    const FmmTree *t = static_cast<const FmmTree *>(c.fmm);
+    if (!t) return 0;
+    int n = 2;  // P2M, L2P + P2P
+    for (int l = 2; l <= t->L - 1; l++) n += 1 + (t->tc && t->tc_m2m[l].ncomb > 0);
+    n += 1 + (t->tc && t->tc_m2l.ncomb > 0);
+    for (int l = 3; l <= t->L; l++) n += 1 + (t->tc && t->tc_l2l[l].ncomb > 0);
+    return n;
 }
 
 int *fmm_error_flag(const Ctx &c) {

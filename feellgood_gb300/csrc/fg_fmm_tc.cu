@@ -14,16 +14,22 @@
 // accumulation) keeps about 21 bits of every product, the accuracy of the FP32 CUDA-core
 // translation.
 //
-// Pipeline (one CTA of 9 warps per tile, 4 shared-memory stages of K = 32):
-//   warps 0-3  load one K-chunk of the operator and of the 64 gathered inputs with vector
-//              loads, split hi/lo, store them in the no-swizzle K-major core-matrix layout
-//              (8 rows x 16 bytes per core matrix), fence the async proxy, arrive on full[s];
+// Pipeline (one CTA of 9 warps per tile, two CTAs per SM, 4 shared-memory stages of K = 16):
+//   warps 0-3  fill one stage per item: thread 0 starts two bulk copies
+//              (cp.async.bulk, completion counted in bytes on full[s]) of the operator
+//              item, stored pre-split (hi, lo) in global memory in exactly the shared-memory
+//              image the MMA reads (no-swizzle K-major core matrices, 8 rows x 16 bytes);
+//              all 128 threads gather the 64 input expansions' item with 16-byte cp.async
+//              from pre-split hi/lo arrays into the same layout (zero fill where a cell has
+//              no input). A thread arrives on full[s] once its copies for that item have
+//              landed, three items later, so four items per CTA are in flight;
 //   warp 4     one lane waits full[s], issues the MMAs of each K-step of 8 and
 //              tcgen05.commit arrives on empty[s] when they have read the stage; each code
 //              accumulates into its own TMEM buffer (two, used in turn), committed to tfull;
 //   warps 5-8  drain a finished code buffer with tcgen05.ld (warp w owns TMEM lanes
 //              32(w%4)..+31 = coefficient rows), add it to FP32 registers with round to
-//              nearest, release it (tfree), and finally store (or add to) the outputs.
+//              nearest, release it (tfree), and finally store (or add to) the outputs and
+//              their hi/lo split for the next translation.
 // The tensor core's FP32 accumulation rounds toward zero, so an accumulator summed over
 // all codes in place drifts by about 2.4e-7 per 13 K-steps (measured); one accumulator per
 // code and per term group keeps the translation at FP32 rounding level.
@@ -31,6 +37,7 @@
 // in *err, stops issuing work, frees its TMEM and returns.
 #include <algorithm>
 #include <cstdint>
+#include <cstring>
 #include <vector>
 
 #include "fg_internal.h"
@@ -42,15 +49,18 @@ namespace {
 constexpr int NRC = 100;  // reals per expansion (P = 9)
 constexpr int NC = 64;    // output cells per CTA = MMA N
 constexpr int MR = 128;   // MMA M
-constexpr int KC = 32;    // K per pipeline item
-constexpr int NCHUNK = 4; // K = 104 = 32 + 32 + 32 + 8
-constexpr int NSTAGE = 4;
-constexpr int A_BYTES = MR * KC * 4;                    // 16 KB per part (hi or lo)
-constexpr int B_BYTES = NC * KC * 4;                    // 8 KB per part
-constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // 48 KB
+constexpr int KI = 16;    // K per pipeline item (2 MMA K-steps of 8)
+constexpr int IPC = 7;    // items per code: K = 104 = 6 x 16 + 8
+constexpr int KQ = KI / 4;                              // 16-byte quads of K per row and item
+constexpr int NSTAGE = 4;                               // 96 KB of stages: two CTAs per SM
 constexpr uint32_t LBO = 128;                           // next core matrix along K
-constexpr uint32_t SBO = 1024;                          // next group of 8 rows
+constexpr uint32_t SBO = KQ * 128;                      // next group of 8 rows (512 B)
+constexpr int A_BYTES = 16 * SBO;                       // 8 KB per part (hi or lo), rows 0..127
+constexpr int B_BYTES = (NC / 8) * SBO;                 // 4 KB per part
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // 24 KB
 constexpr int TMEM_COLS = 256;  // 2 buffers x (main, corr) x 64 columns
+constexpr int IMG_BYTES = 13 * SBO;  // one operator image part: rows 0..103 (13 groups of 8)
+constexpr int LAG = NSTAGE - 1;      // items whose gathers may still be in flight
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -106,6 +116,25 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, int *err
     }
 }
 
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+// Bulk global -> shared copy whose completion is counted (in bytes) on an mbarrier.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// 16-byte global -> shared copy (L2 only); src_bytes = 0 fills the destination with zeros.
+__device__ __forceinline__ void cp16(void *dst, const void *src, uint32_t src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -155,58 +184,55 @@ __device__ __forceinline__ void store_split(unsigned char *hi, unsigned char *lo
     *reinterpret_cast<float4 *>(lo + off) = make_float4(v.x - h0, v.y - h1, v.z - h2, v.w - h3);
 }
 
-// One K-chunk (KQN quads of K) of the operator rows 0..103 and of the 64 gathered inputs.
-// Thread mapping: 8 consecutive threads take the 8 rows of one core matrix (conflict-free
-// 16-byte shared stores); 4 such groups of a warp read 64 contiguous bytes of each row.
-template <int KQN>
-__device__ __forceinline__ void load_chunk(unsigned char *st, int tid, const float *__restrict__ op, int k0,
-                                           const int *__restrict__ tab, int ncode, int code, int out0, int c_begin,
-                                           int n_out, const float *in) {
-    for (int e = tid; e < 104 * KQN; e += 128) {
-        const int il = e & 7, r = e >> 3, kq = r % KQN, ig = r / KQN, i = ig * 8 + il;
-        const int j = k0 + 4 * kq;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (i < NRC && j < NRC) v = __ldg(reinterpret_cast<const float4 *>(op + i * NRC + j));
-        store_split(st, st + A_BYTES, ig * 1024 + kq * 128 + il * 16, v);
-    }
-    unsigned char *bs = st + 2 * A_BYTES;
-    for (int e = tid; e < NC * KQN; e += 128) {
-        const int il = e & 7, r = e >> 3, kq = r % KQN, cg = r / KQN, n = cg * 8 + il;
-        const int j = k0 + 4 * kq;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        const int cell = c_begin + n;
-        if (cell < n_out && j < NRC) {
-            const int sc = __ldg(tab + (size_t)(out0 + cell) * ncode + code);
-            if (sc >= 0) v = *reinterpret_cast<const float4 *>(in + (size_t)sc * NRC + j);
-        }
-        store_split(bs, bs + B_BYTES, cg * 1024 + kq * 128 + il * 16, v);
+// Gather of one item (K = 16) of the 64 input expansions, hi and lo parts, with 16-byte
+// async copies into the core-matrix layout: thread t copies quads 2(t&1), 2(t&1)+1 of cell
+// t>>1 (zero fill beyond coefficient 99 or where the cell has no input, sc < 0).
+__device__ __forceinline__ void gather_item(unsigned char *bs, int tid, int k0, int sc, const float *in_hi,
+                                            const float *in_lo) {
+    const int n = tid >> 1;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int kq = 2 * (tid & 1) + h, j = k0 + 4 * kq;
+        const bool ok = sc >= 0 && j < NRC;
+        const size_t o = ok ? (size_t)sc * NRC + j : 0;
+        unsigned char *d = bs + (n >> 3) * SBO + kq * 128 + (n & 7) * 16;
+        cp16(d, in_hi + o, ok ? 16u : 0u);
+        cp16(d + B_BYTES, in_lo + o, ok ? 16u : 0u);
     }
 }
 
-__device__ __forceinline__ void translate_tc_body(int n_out, int out0, int ncode, const int *__restrict__ tab,
-                                                  const float *__restrict__ ops, const float *in, float *out,
-                                                  int accumulate, const int *__restrict__ tile_ptr,
-                                                  const int *__restrict__ tile_code, int *err, int terms) {
+__device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
+    const int n_out = a.n_out, out0 = a.out0, ncode = a.ncode, accumulate = a.accumulate, terms = a.terms;
+    const int *__restrict__ tab = a.tab;
+    const int *__restrict__ tile_code = a.tile_code;
+    float *out = a.out;
+    int *err = a.err;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     __shared__ __align__(8) uint64_t full[NSTAGE], empty[NSTAGE], tfull[2], tfree[2];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int bail;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int c_begin = blockIdx.x * NC;
-    const int q0 = tile_ptr[blockIdx.x], q1 = tile_ptr[blockIdx.x + 1];
-    const int ncodes = q1 - q0, nitems = ncodes * NCHUNK;
+    const int4 unit = a.units[blockIdx.x];
+    const int c_begin = unit.x * NC;
+    const int q0 = unit.y, q1 = unit.z, slot = unit.w;
+    const int ncodes = q1 - q0, nitems = ncodes * IPC;
     if (nitems == 0) {  // no input reaches these cells: a stored result is zero
         if (!accumulate)
             for (int e = tid; e < NC * NRC; e += blockDim.x) {
                 const int cell = c_begin + e / NRC;
-                if (cell < n_out) out[(size_t)(out0 + cell) * NRC + e % NRC] = 0.f;
+                if (cell < n_out) {
+                    const size_t o = (size_t)(out0 + cell) * NRC + e % NRC;
+                    out[o] = 0.f;
+                    a.out_hi[o] = 0.f;
+                    a.out_lo[o] = 0.f;
+                }
             }
         return;
     }
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; s++) {
-            mbar_init(&full[s], 128);
+            mbar_init(&full[s], 129);  // 128 gathering threads + the bulk copies' expect_tx
             mbar_init(&empty[s], 1);
         }
         for (int b = 0; b < 2; b++) {
@@ -217,9 +243,10 @@ __device__ __forceinline__ void translate_tc_body(int n_out, int out0, int ncode
         fence_mbar_init();
     }
     // rows 104..127 of the operator images are read by the M = 128 MMA: keep them zero
-    for (int e = tid; e < NSTAGE * 2 * 192; e += blockDim.x) {
-        const int s = e / 384, part = (e / 192) & 1, k = e % 192;
-        *reinterpret_cast<uint4 *>(sm + s * STAGE_BYTES + part * A_BYTES + 13 * 1024 + k * 16) = make_uint4(0, 0, 0, 0);
+    constexpr int ZQ = 3 * SBO / 16;  // 16-byte words of groups 13..15
+    for (int e = tid; e < NSTAGE * 2 * ZQ; e += blockDim.x) {
+        const int s = e / (2 * ZQ), part = (e / ZQ) & 1, k = e % ZQ;
+        *reinterpret_cast<uint4 *>(sm + s * STAGE_BYTES + part * A_BYTES + 13 * SBO + k * 16) = make_uint4(0, 0, 0, 0);
     }
     if (warp == 4) tmem_alloc(&tmem_base, TMEM_COLS);
     fence_proxy_async();
@@ -229,18 +256,40 @@ __device__ __forceinline__ void translate_tc_body(int n_out, int out0, int ncode
     const uint32_t tmem = tmem_base;
 
     if (warp < 4) {
-        // producers: operator and gathered inputs, one K-chunk per pipeline item
-        for (int it = 0; it < nitems; it++) {
-            const int s = it % NSTAGE;
-            if (it >= NSTAGE && !mbar_wait(&empty[s], ((it / NSTAGE) - 1) & 1, err, &bail)) break;
-            const int code = tile_code[q0 + it / NCHUNK], q = it % NCHUNK;
-            const float *op = ops + (size_t)code * NRC * NRC;
-            unsigned char *st = sm + s * STAGE_BYTES;
-            if (q < 3) load_chunk<8>(st, tid, op, 32 * q, tab, ncode, code, out0, c_begin, n_out, in);
-            else load_chunk<2>(st, tid, op, 96, tab, ncode, code, out0, c_begin, n_out, in);
-            fence_proxy_async();
-            mbar_arrive(&full[s]);
+        // producers: one item (K = 16) per pipeline step; a thread's gathers of item it are
+        // complete (cp.async.wait_group) when it arrives for that item, LAG items later.
+        // The source cell of this thread's output cell is read once per code.
+        bool live = true;
+        int sc = -1;
+        for (int it = 0; it < nitems + LAG; it++) {
+            if (it < nitems && live) {
+                const int s = it % NSTAGE;
+                if (it >= NSTAGE && !mbar_wait(&empty[s], ((it / NSTAGE) - 1) & 1, err, &bail)) live = false;
+                if (live) {
+                    const int ci = it / IPC, q = it % IPC;
+                    const int code = tile_code[q0 + ci];
+                    if (q == 0) {
+                        const int cell = c_begin + (tid >> 1);
+                        sc = cell < n_out ? __ldg(tab + (size_t)(out0 + cell) * ncode + code) : -1;
+                    }
+                    unsigned char *st = sm + s * STAGE_BYTES;
+                    if (tid == 0) {
+                        const unsigned char *img = a.op_img + ((size_t)code * IPC + q) * 2 * IMG_BYTES;
+                        mbar_arrive_expect_tx(&full[s], 2 * IMG_BYTES);
+                        bulk_g2s(st, img, IMG_BYTES, &full[s]);
+                        bulk_g2s(st + A_BYTES, img + IMG_BYTES, IMG_BYTES, &full[s]);
+                    }
+                    gather_item(st + 2 * A_BYTES, tid, KI * q, sc, a.in_hi, a.in_lo);
+                }
+            }
+            cp_commit();
+            if (it >= LAG) {
+                cp_wait<LAG>();
+                fence_proxy_async();
+                if (live) mbar_arrive(&full[(it - LAG) % NSTAGE]);
+            }
         }
+        cp_wait<0>();
     } else if (warp == 4) {
         if (lane == 0) {
             // MMA issuer. Each code accumulates into a fresh pair of TMEM accumulators
@@ -255,11 +304,11 @@ __device__ __forceinline__ void translate_tc_body(int n_out, int out0, int ncode
                 if (ci >= 2 && !mbar_wait(&tfree[b], ((ci >> 1) - 1) & 1, err, &bail)) break;
                 tc_fence_after();
                 const uint32_t dmain = tmem + b * 2 * NC, dcorr = dmain + NC;
-                for (int q = 0; q < NCHUNK; q++) {
-                    const int it = ci * NCHUNK + q, s = it % NSTAGE;
+                for (int q = 0; q < IPC; q++) {
+                    const int it = ci * IPC + q, s = it % NSTAGE;
                     if (!mbar_wait(&full[s], (it / NSTAGE) & 1, err, &bail)) { ok = false; break; }
                     tc_fence_after();
-                    const int ksteps = q < 3 ? 4 : 1;
+                    const int ksteps = q < IPC - 1 ? KI / 8 : 1;
                     const uint32_t base = smem_u32(sm + s * STAGE_BYTES);
                     for (int k = 0; k < ksteps; k++) {
                         const uint64_t ah = sdesc(base + k * 256), al = sdesc(base + A_BYTES + k * 256);
@@ -308,12 +357,22 @@ __device__ __forceinline__ void translate_tc_body(int n_out, int out0, int ncode
             drained++;
         }
         if (drained == ncodes && row < NRC) {
+            if (slot >= 0) {  // one of several units of this tile: partial result
+                float *p = a.scratch + (size_t)slot * NC * NRC + row;
 #pragma unroll
-            for (int j = 0; j < NC; j++) {
-                const int cell = c_begin + j;
-                if (cell < n_out) {
-                    float *o = out + (size_t)(out0 + cell) * NRC + row;
-                    *o = accumulate ? *o + acc[j] : acc[j];
+                for (int j = 0; j < NC; j++) p[j * NRC] = acc[j];
+            } else {
+#pragma unroll
+                for (int j = 0; j < NC; j++) {
+                    const int cell = c_begin + j;
+                    if (cell < n_out) {
+                        const size_t o = (size_t)(out0 + cell) * NRC + row;
+                        const float v = accumulate ? out[o] + acc[j] : acc[j];
+                        out[o] = v;
+                        const float h = tf32_rn(v);
+                        a.out_hi[o] = h;
+                        a.out_lo[o] = v - h;
+                    }
                 }
             }
         }
@@ -327,17 +386,29 @@ __device__ __forceinline__ void translate_tc_body(int n_out, int out0, int ncode
 }
 
 // One entry per translation kind, so that profiles tell them apart.
-#define FG_TC_KERNEL(name)                                                                                       \
-    __global__ void __launch_bounds__(288, 1)                                                                    \
-        name(int n_out, int out0, int ncode, const int *__restrict__ tab, const float *__restrict__ ops,          \
-             const float *in, float *out, int accumulate, const int *__restrict__ tile_ptr,                     \
-             const int *__restrict__ tile_code, int *err, int terms) {                                          \
-        translate_tc_body(n_out, out0, ncode, tab, ops, in, out, accumulate, tile_ptr, tile_code, err, terms); \
-    }
+#define FG_TC_KERNEL(name) \
+    __global__ void __launch_bounds__(288, 2) name(TcArgs a) { translate_tc_body(a); }
 FG_TC_KERNEL(k_m2m_tc)
 FG_TC_KERNEL(k_m2l_tc)
 FG_TC_KERNEL(k_l2l_tc)
 #undef FG_TC_KERNEL
+
+// Sum of the partial results of tiles split over several units, in slot order.
+__global__ void __launch_bounds__(256) k_tc_combine(TcArgs a) {
+    const int4 ct = a.comb[blockIdx.x];
+    for (int e = threadIdx.x; e < NC * NRC; e += blockDim.x) {
+        const int cell = ct.x * NC + e / NRC;
+        if (cell >= a.n_out) continue;
+        float v = 0.f;
+        for (int u = 0; u < ct.z; u++) v += a.scratch[(size_t)(ct.y + u) * NC * NRC + e];
+        const size_t o = (size_t)(a.out0 + cell) * NRC + e % NRC;
+        if (a.accumulate) v += a.out[o];
+        a.out[o] = v;
+        const float h = tf32_rn(v);
+        a.out_hi[o] = h;
+        a.out_lo[o] = v - h;
+    }
+}
 
 }  // namespace
 
@@ -352,15 +423,64 @@ cudaError_t translate_tc_setup() {
     return e;
 }
 
-cudaError_t launch_translate_tc(cudaStream_t st, int n_out, int out0, int ncode, const int *tab, const float *ops,
-                                const float *in, float *out, int accumulate, const int *tile_ptr,
-                                const int *tile_code, int *err, int terms) {
-    if (n_out <= 0) return cudaSuccess;
-    const int ntile = (n_out + NC - 1) / NC;
-    auto k = accumulate ? k_l2l_tc : (ncode == 8 ? k_m2m_tc : k_m2l_tc);
-    k<<<ntile, 288, translate_tc_smem(), st>>>(n_out, out0, ncode, tab, ops, in, out, accumulate, tile_ptr,
-                                               tile_code, err, terms);
+cudaError_t launch_translate_tc(cudaStream_t st, const TcArgs &a) {
+    if (a.n_out <= 0 || a.nunits <= 0) return cudaSuccess;
+    auto k = a.accumulate ? k_l2l_tc : (a.ncode == 8 ? k_m2m_tc : k_m2l_tc);
+    k<<<a.nunits, 288, translate_tc_smem(), st>>>(a);
+    if (a.ncomb > 0) k_tc_combine<<<a.ncomb, 256, 0, st>>>(a);
     return cudaGetLastError();
+}
+
+void translate_tc_units(int n_out, int ncode, const int *tab, int out0, int max_codes, std::vector<int> &codes,
+                        std::vector<int4> &units, std::vector<int4> &comb, int &nslot) {
+    const int ntile = (n_out + NC - 1) / NC;
+    for (int b = 0; b < ntile; b++) {
+        const int first = (int)codes.size();
+        const int c0 = b * NC, c1 = std::min(n_out, c0 + NC);
+        for (int code = 0; code < ncode; code++) {
+            bool any = false;
+            for (int cc = c0; cc < c1 && !any; cc++) any = tab[(size_t)(out0 + cc) * ncode + code] >= 0;
+            if (any) codes.push_back(code);
+        }
+        const int n = (int)codes.size() - first;
+        const int nu = std::max(1, (n + max_codes - 1) / max_codes);
+        if (nu == 1) {
+            units.push_back(make_int4(b, first, first + n, -1));
+        } else {
+            comb.push_back(make_int4(b, nslot, nu, 0));
+            for (int u = 0; u < nu; u++)
+                units.push_back(make_int4(b, first + (int)((long)n * u / nu), first + (int)((long)n * (u + 1) / nu),
+                                          nslot + u));
+            nslot += nu;
+        }
+    }
+}
+
+// Pre-split operator images: for each code and item (K = 16), the hi and lo parts of
+// operator rows 0..103 exactly as the MMA reads them from shared memory (core matrix
+// (g, kq) at g*SBO + kq*128, row r of the group at + 16 r, four K values per row).
+std::vector<float> translate_tc_images(const std::vector<double> &ops, int ncode) {
+    std::vector<float> img((size_t)ncode * IPC * 2 * (IMG_BYTES / 4), 0.f);
+    for (int code = 0; code < ncode; code++)
+        for (int q = 0; q < IPC; q++) {
+            float *hi = img.data() + ((size_t)code * IPC + q) * 2 * (IMG_BYTES / 4);
+            float *lo = hi + IMG_BYTES / 4;
+            for (int i = 0; i < NRC; i++)
+                for (int kk = 0; kk < KI; kk++) {
+                    const int j = KI * q + kk;
+                    if (j >= NRC) continue;
+                    const float v = (float)ops[((size_t)code * NRC + i) * NRC + j];
+                    uint32_t bits;
+                    std::memcpy(&bits, &v, 4);
+                    bits = (bits + 0x1000u) & 0xFFFFE000u;
+                    float h;
+                    std::memcpy(&h, &bits, 4);
+                    const size_t off = ((i >> 3) * SBO + (kk >> 2) * 128 + (i & 7) * 16 + (kk & 3) * 4) / 4;
+                    hi[off] = h;
+                    lo[off] = v - h;
+                }
+        }
+    return img;
 }
 
 }  // namespace fg
@@ -374,46 +494,58 @@ extern "C" int fg_debug_translate_tc(int n_in, int n_out, int ncode, const float
     if (n_in <= 0 || n_out <= 0 || ncode <= 0 || !ops || !tab || !in || !out) return FG_EINVAL;
     for (long k = 0; k < (long)n_out * ncode; k++)
         if (tab[k] < -1 || tab[k] >= n_in) return FG_EINVAL;
-    std::vector<int> ptr, codes;
-    const int ntile = (n_out + NC - 1) / NC;
-    for (int b = 0; b < ntile; b++) {
-        ptr.push_back((int)codes.size());
-        for (int code = 0; code < ncode; code++) {
-            bool any = false;
-            for (int cc = b * NC; cc < std::min(n_out, b * NC + NC) && !any; cc++) any = tab[(size_t)cc * ncode + code] >= 0;
-            if (any) codes.push_back(code);
-        }
+    std::vector<int> codes;
+    std::vector<int4> units, comb;
+    int nslot = 0;
+    translate_tc_units(n_out, ncode, tab, 0, 3, codes, units, comb, nslot);  // small units: exercise the combine
+    const std::vector<double> opd(ops, ops + (size_t)ncode * NRC * NRC);
+    const std::vector<float> img = translate_tc_images(opd, ncode);
+    std::vector<float> xh((size_t)n_in * NRC), xl((size_t)n_in * NRC);
+    for (size_t k = 0; k < xh.size(); k++) {
+        uint32_t bits;
+        std::memcpy(&bits, &in[k], 4);
+        bits = (bits + 0x1000u) & 0xFFFFE000u;
+        std::memcpy(&xh[k], &bits, 4);
+        xl[k] = in[k] - xh[k];
     }
-    ptr.push_back((int)codes.size());
-    float *d_ops = nullptr, *d_in = nullptr, *d_out = nullptr;
-    int *d_tab = nullptr, *d_ptr = nullptr, *d_code = nullptr, *d_err = nullptr;
+    float *d_img = nullptr, *d_xh = nullptr, *d_xl = nullptr, *d_out = nullptr, *d_oh = nullptr, *d_ol = nullptr;
+    int *d_tab = nullptr, *d_code = nullptr, *d_err = nullptr;
+    int4 *d_units = nullptr, *d_comb = nullptr;
+    float *d_scr = nullptr;
     int status = FG_OK, herr = 0;
     auto ok = [&](cudaError_t e) { if (e != cudaSuccess && status == FG_OK) status = FG_ECUDA; return e == cudaSuccess; };
-    if (ok(cudaMalloc(&d_ops, sizeof(float) * (size_t)ncode * NRC * NRC)) &&
-        ok(cudaMalloc(&d_in, sizeof(float) * (size_t)n_in * NRC)) &&
-        ok(cudaMalloc(&d_out, sizeof(float) * (size_t)n_out * NRC)) &&
+    const size_t nx = (size_t)n_in * NRC, no = (size_t)n_out * NRC;
+    if (ok(cudaMalloc(&d_img, sizeof(float) * img.size())) && ok(cudaMalloc(&d_xh, sizeof(float) * nx)) &&
+        ok(cudaMalloc(&d_xl, sizeof(float) * nx)) && ok(cudaMalloc(&d_out, sizeof(float) * no)) &&
+        ok(cudaMalloc(&d_oh, sizeof(float) * no)) && ok(cudaMalloc(&d_ol, sizeof(float) * no)) &&
         ok(cudaMalloc(&d_tab, sizeof(int) * (size_t)n_out * ncode)) &&
-        ok(cudaMalloc(&d_ptr, sizeof(int) * ptr.size())) &&
+        ok(cudaMalloc(&d_units, sizeof(int4) * units.size())) &&
+        ok(cudaMalloc(&d_comb, sizeof(int4) * std::max<size_t>(1, comb.size()))) &&
+        ok(cudaMalloc(&d_scr, sizeof(float) * std::max(1, nslot) * NC * NRC)) &&
         ok(cudaMalloc(&d_code, sizeof(int) * std::max<size_t>(1, codes.size()))) &&
         ok(cudaMalloc(&d_err, sizeof(int))) &&
-        ok(cudaMemcpy(d_ops, ops, sizeof(float) * (size_t)ncode * NRC * NRC, cudaMemcpyHostToDevice)) &&
-        ok(cudaMemcpy(d_in, in, sizeof(float) * (size_t)n_in * NRC, cudaMemcpyHostToDevice)) &&
+        ok(cudaMemcpy(d_img, img.data(), sizeof(float) * img.size(), cudaMemcpyHostToDevice)) &&
+        ok(cudaMemcpy(d_xh, xh.data(), sizeof(float) * nx, cudaMemcpyHostToDevice)) &&
+        ok(cudaMemcpy(d_xl, xl.data(), sizeof(float) * nx, cudaMemcpyHostToDevice)) &&
         ok(cudaMemcpy(d_tab, tab, sizeof(int) * (size_t)n_out * ncode, cudaMemcpyHostToDevice)) &&
-        ok(cudaMemcpy(d_ptr, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice)) &&
+        ok(cudaMemcpy(d_units, units.data(), sizeof(int4) * units.size(), cudaMemcpyHostToDevice)) &&
+        (comb.empty() || ok(cudaMemcpy(d_comb, comb.data(), sizeof(int4) * comb.size(), cudaMemcpyHostToDevice))) &&
         (codes.empty() || ok(cudaMemcpy(d_code, codes.data(), sizeof(int) * codes.size(), cudaMemcpyHostToDevice))) &&
-        ok(cudaMemset(d_err, 0, sizeof(int))) && ok(translate_tc_setup()) &&
-        ok(launch_translate_tc(0, n_out, 0, ncode, d_tab, d_ops, d_in, d_out, 0, d_ptr, d_code, d_err, terms)) &&
-        ok(cudaDeviceSynchronize()) &&
-        ok(cudaMemcpy(out, d_out, sizeof(float) * (size_t)n_out * NRC, cudaMemcpyDeviceToHost)) &&
-        ok(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost))) {
-        if (herr) status = FG_ETIMEDOUT;
+        ok(cudaMemset(d_err, 0, sizeof(int))) && ok(translate_tc_setup())) {
+        TcArgs a{};
+        a.n_out = n_out; a.out0 = 0; a.ncode = ncode; a.tab = d_tab;
+        a.op_img = reinterpret_cast<const unsigned char *>(d_img);
+        a.in_hi = d_xh; a.in_lo = d_xl; a.out = d_out; a.out_hi = d_oh; a.out_lo = d_ol;
+        a.accumulate = 0; a.tile_code = d_code; a.err = d_err; a.terms = terms;
+        a.units = d_units; a.nunits = (int)units.size(); a.scratch = d_scr;
+        a.comb = d_comb; a.ncomb = (int)comb.size();
+        if (ok(launch_translate_tc(0, a)) && ok(cudaDeviceSynchronize()) &&
+            ok(cudaMemcpy(out, d_out, sizeof(float) * no, cudaMemcpyDeviceToHost)) &&
+            ok(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost)) && herr)
+            status = FG_ETIMEDOUT;
     }
-    void *ptrs[] = {d_ops, d_in, d_out, d_tab, d_ptr, d_code, d_err};
+    void *ptrs[] = {d_img, d_xh, d_xl, d_out, d_oh, d_ol, d_tab, d_code, d_err, d_units, d_comb, d_scr};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     return status;
 }
-
-namespace fg {
-
-}  // namespace fg

@@ -251,13 +251,34 @@ int bicg_grid_size(Ctx &c, bool mixed);
 int mixed_grid_size(Ctx &c);
 int mixed_max_blocks(Ctx &c);
 int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p);
-int *fmm_error_flag(const Ctx &c);  // device int: FG_ETIMEDOUT after an expired wait (or nullptr)
+int *fmm_error_flag(const Ctx &c);
+int fmm_launches_per_eval(const Ctx &c);  // kernels one FMM evaluation launches  // device int: FG_ETIMEDOUT after an expired wait (or nullptr)
 // tensor-core translations (fg_fmm_tc.cu)
 int translate_tc_smem();
 cudaError_t translate_tc_setup();
-cudaError_t launch_translate_tc(cudaStream_t st, int n_out, int out0, int ncode, const int *tab, const float *ops,
-                                const float *in, float *out, int accumulate, const int *tile_ptr,
-                                const int *tile_code, int *err, int terms = 7);
+// out (+)= sum_code Op[code] in[tab[cell][code]] over n_out cells from out0 (FP32 path)
+struct TcArgs {
+    int n_out, out0, ncode;
+    const int *tab;                 // [cell][ncode] input cell or -1
+    const unsigned char *op_img;    // translate_tc_images of the operators
+    const float *in_hi, *in_lo;     // inputs split hi = tf32(x), lo = x - hi
+    float *out, *out_hi, *out_lo;   // outputs and their split
+    int accumulate;                 // 1: out += result
+    const int *tile_code;           // codes that reach each tile of 64 cells, tile after tile
+    const int4 *units;              // per CTA: tile, first and end index into tile_code, scratch slot
+    int nunits;                     //   (slot -1: the tile's only unit, which writes the output)
+    float *scratch;                 // [slot][64][100] partial results of tiles split over units
+    const int4 *comb;               // per split tile: tile, first slot, number of slots
+    int ncomb;
+    int *err;                       // FG_ETIMEDOUT after an expired wait
+    int terms;                      // product terms of the split (7 in production)
+};
+cudaError_t launch_translate_tc(cudaStream_t st, const TcArgs &a);
+std::vector<float> translate_tc_images(const std::vector<double> &ops, int ncode);
+// Work units of one translation launch: the codes reaching each tile of 64 output cells,
+// split into units of at most max_codes codes (appended to codes/units/comb; nslot grows).
+void translate_tc_units(int n_out, int ncode, const int *tab, int out0, int max_codes, std::vector<int> &codes,
+                        std::vector<int4> &units, std::vector<int4> &comb, int &nslot);
 int fmm_stage_ms(const Ctx &c, double ms[5]);
 int mlp_create(Ctx &c);
 void mlp_free(Ctx &c);
