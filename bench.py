@@ -328,14 +328,21 @@ def main():
         cp.close()
 
     # plain FP64 GPU path, same state, angles and tolerance
-    plain_value = plain_iters = None
+    plain_value = plain_iters = plain_detail = None
     if args.plain_steps > 0:
-        cp = fg.Context(mesh, regions(), tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP64, demag=fg.FG_DEMAG_FMM)
+        cp = fg.Context(mesh, regions(), tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP64, demag=fg.FG_DEMAG_FMM,
+                        profile=1)
         cp.set_state(start["u"], start["v"], start["phi"], start["phiv"])
         n = min(args.plain_steps, args.steps)
         pms, preps = run_steps(cp, n, H, DT, step_angles)
         plain_value = n / (float(pms[:, 4].sum()) / 1e3)
         plain_iters = float(np.mean([r["iters"] for r in preps]))
+        pc = cp.counters()
+        plain_detail = {"phase_ms": dict(zip(["elements", "solve", "demag_x2", "energy_evolution", "step"],
+                                             [float(x) for x in pms.mean(axis=0)])),
+                        "fmm": {"L": int(pc[1]), "m2l_pairs": float(pc[2]), "p2p_pairs": float(pc[3]),
+                                "stage_ms": dict(zip(["p2m", "m2m", "m2l", "l2l", "l2p_p2p"],
+                                                     [float(x) for x in cp.fmm_timings()]))}}
         cp.close()
 
     # roofline of the dominant kernel: per-launch device times from CUDA events in the timed region
@@ -383,6 +390,7 @@ def main():
             "prev_guess_fp32_refine_steps_per_s": prev_value,
             "iters_per_step": float(np.mean(iters)), "refinements_per_step": float(np.mean(refs)),
             "prev_guess_iters_per_step": prev_iters, "plain_iters_per_step": plain_iters,
+            "plain_fp64_detail": plain_detail,
             "learned_guess": {"accepted_frac": float(np.mean(acc)),
                               "res0_over_fallback_median": float(np.median(r0_ratio)) if r0_ratio else None,
                               "train_solves": args.train_steps},

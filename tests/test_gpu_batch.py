@@ -4,8 +4,11 @@ and the graph-replayed run against the same samples stepped one context at a tim
 A batch sample must follow the iteration it would follow alone: its Krylov scalars, its
 |b| and its stopping test are its own. What may differ is the order of the per-block
 partial sums (a sample gets a different number of solver blocks in a batch), so the
-per-sample solutions agree to the solver tolerance, not bit for bit; the demag potential
-(a forest of the same octrees) and a graph replay of the stream-ordered step agree exactly.
+per-sample solutions agree to the solver tolerance, not bit for bit. The demag potential is
+a forest of the same octrees, but the tensor-core translations group the interaction codes
+of a tile of 64 cells (which may hold cells of several samples) into work units, so sums
+are grouped differently: it agrees to FP32 rounding. A graph replay of the stream-ordered
+step agrees exactly.
 """
 import numpy as np
 import pytest
@@ -57,7 +60,7 @@ def test_batch_layout_and_forest_demag():
     phi_b = b.get_state(0)["phi"]
     for g, c in enumerate(singles):
         phi = c.get_state(0)["phi"]
-        assert _rel(phi_b[off[g]:off[g + 1]], phi) < 1e-12
+        assert _rel(phi_b[off[g]:off[g + 1]], phi) < 1e-6
     # the forest potential is each sample's own: it matches the oracle's exact sum per sample
     for g, m in enumerate(ms):
         o = fgo.Oracle(m, cases.oracle_regions(alpha=0.1))
