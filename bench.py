@@ -241,6 +241,9 @@ def main():
     ap.add_argument("--train-steps", type=int, default=40, help="untimed solves that train the learned guess")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--drift", type=int, default=0,
+                    help="accuracy study: N steps of the headline path and of the plain FP64 path from the same "
+                         "state and angles; prints max |dm|, rel-L2 of v and phi (its own JSON line)")
     ap.add_argument("--quick", action="store_true",
                     help="timed steps only (no training, comparisons, end-to-end or CPU legs): for profiling")
     args = ap.parse_args()
@@ -252,6 +255,9 @@ def main():
         return
     if args.workload == "batch64":
         bench_batch(args)
+        return
+    if args.drift > 0:
+        drift_study(args)
         return
     rank, world, dist = dist_setup(args.gpus)
     import __graft_entry__
@@ -409,6 +415,45 @@ def main():
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
+
+
+def drift_study(args):
+    """The headline path (learned guess, FP32 body + FP64 refinement, FP32 FMM) against the plain
+    FP64 path over N steps of the film workload, same initial state, angles and tolerance."""
+    import __graft_entry__
+    __graft_entry__.build_product()
+    import feellgood_gb300 as fg
+    mesh = film_mesh()
+    u0 = initial_state(mesh)
+    H = np.zeros(3)
+    fg.rng_seed(SEED)
+    angles = [fg.rng_angle() for _ in range(args.drift)]
+    out = {}
+    for name, opts in (("mixed", dict(precision=fg.FG_PREC_FP32_REFINE, learned_guess=1)),
+                       ("plain", dict(precision=fg.FG_PREC_FP64))):
+        c = fg.Context(mesh, regions(), tol=TOL, max_iter=MAXITER, demag=fg.FG_DEMAG_FMM, **opts)
+        c.set_state(u0)
+        c.compute_all(H)
+        t0 = time.perf_counter()
+        ms, reps = run_steps(c, args.drift, H, DT, angles)
+        out[name] = (c.get_state(0), float(ms[:, 4].sum()), time.perf_counter() - t0,
+                     float(np.mean([r["iters"] for r in reps])))
+        c.close()
+    (a, ta, wa, ia), (b, tb, wb, ib) = out["mixed"], out["plain"]
+    dm = np.linalg.norm(a["u"] - b["u"], axis=1)
+
+    def rel(x, y):
+        return float(np.linalg.norm(x - y) / np.linalg.norm(y))
+    line = {"metric": f"max |dm| after {args.drift} steps, learned-guess FP32+refine vs plain FP64 (film 1.2M tets)",
+            "value": float(dm.max()), "unit": "1", "higher_is_better": False, "steps": args.drift,
+            "rel_l2_u": rel(a["u"], b["u"]), "rel_l2_v": rel(a["v"], b["v"]), "rel_l2_phi": rel(a["phi"], b["phi"]),
+            "rel_l2_phiv": rel(a["phiv"], b["phiv"]),
+            "mean_m_mixed": [float(x) for x in a["u"].mean(axis=0)],
+            "mean_m_plain": [float(x) for x in b["u"].mean(axis=0)],
+            "device_s": {"mixed": ta / 1e3, "plain": tb / 1e3}, "iters_per_step": {"mixed": ia, "plain": ib},
+            "config": {"workload": "film 400x400x10 nm, 2 nm grid, 1.2M tets, alpha 0.02, dt 5e-14, tol 1e-6, "
+                                   "zero field, seeded smoothed random initial m"}}
+    print(json.dumps(line), flush=True)
 
 
 BATCH_N, BATCH_H = 64, 2.5

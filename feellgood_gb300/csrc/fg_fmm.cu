@@ -40,7 +40,13 @@ namespace fg {
 constexpr int FMM_P = 9;
 constexpr int NR = (FMM_P + 1) * (FMM_P + 1);  // reals per expansion (100)
 constexpr int NCODE_M2L = 343;                   // offsets in [-3,3]^3 (27 unused)
-constexpr int TB = 64;                           // output cells per translation block
+// CUDA-core translations: output cells per block and per thread. FP64 uses narrow blocks
+// of 16 cells (the FP64 pipe bounds them, so operator reuse matters less than spreading
+// the blocks evenly over the SMs, two per SM); FP32 blocks of 64 cells.
+template <typename T> struct TrShape;
+template <> struct TrShape<float> { static constexpr int TB = 64, CT = 4; };
+template <> struct TrShape<double> { static constexpr int TB = 16, CT = 1; };
+template <typename T> constexpr int tr_smem() { return (int)((100 * 100 + 100 * (TrShape<T>::TB + 4)) * sizeof(T)); }
 
 __host__ __device__ constexpr int cidx(int n, int m) { return n * (n + 1) / 2 + m; }
 // real layout: Re X_n^0 at n*n; Re/Im X_n^m (m>0) at n*n + 2m-1, n*n + 2m
@@ -253,14 +259,14 @@ __global__ void __launch_bounds__(64) k_p2m(int nleaf, const int *__restrict__ l
     }
 }
 
-// Batched translation out[c] (+)= sum_code Op[code] in[tab[c][code]] for TB=64 output cells
-// per block. 160 threads: 10 row groups (10 rows each) x 16 column groups (4 cells each).
+// Batched translation out[c] (+)= sum_code Op[code] in[tab[c][code]] for TB output cells
+// per block. 160 threads: 10 row groups (10 rows each) x 16 column groups (CT cells each).
 template <typename T>
 __global__ void __launch_bounds__(160) k_translate(int n_out, int out0, int ncode, const int *__restrict__ tab,
                                                    const T *__restrict__ ops, const T *in, T *out,
                                                    int accumulate) {
     // in and out may be the same array (M2M, L2L): the cells read and written are disjoint.
-    constexpr int RT = 10, CT = 4, BLD = TB + 4;
+    constexpr int TB = TrShape<T>::TB, CT = TrShape<T>::CT, RT = 10, BLD = TB + 4;
     extern __shared__ unsigned char smem_raw[];
     T *AT = reinterpret_cast<T *>(smem_raw);  // [NR][NR]: AT[k*NR + row] = Op[row][k]
     T *Bs = AT + NR * NR;                      // [NR][BLD]
@@ -318,6 +324,8 @@ template <> __device__ __forceinline__ float rsqrt_p<float>(float x) {
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
+// FP64: CUDA's rsqrt (a single-precision-seeded Newton step written out here measured
+// slower: the FP64 <-> FP32 conversions cost more than they save).
 template <> __device__ __forceinline__ double rsqrt_p<double>(double x) { return rsqrt(x); }
 
 template <typename T> struct Vec4;
@@ -330,14 +338,14 @@ template <> struct Vec4<double> { using type = double4; };
 // leaf-local (leaf units), so FP32 keeps the relative precision of close pairs. The
 // per-lane sums are reduced over the warp in FP64 in a fixed order.
 template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1) k_l2p_p2p(int nleaf, const int *__restrict__ leaf_src,
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_l2p_p2p(int nleaf, const int *__restrict__ leaf_src,
                                                  const int *__restrict__ leaf_tgt, const int *__restrict__ tgt_node,
                                                  const T *__restrict__ tloc, const T *__restrict__ sloc,
                                                  const int *__restrict__ leaf_ijk, int leaf0,
                                                  const double *__restrict__ leaf_scale,
                                                  const int *__restrict__ near_ptr, const int *__restrict__ near_leaf,
                                                  const T *__restrict__ F, double *__restrict__ pot) {
-    constexpr int NT = 16;
+    constexpr int NT = 16;  // targets per pass
     using V4 = typename Vec4<T>::type;
     const V4 *__restrict__ src4 = reinterpret_cast<const V4 *>(sloc);
     const int lane = threadIdx.x & 31;
@@ -860,13 +868,13 @@ static int fmm_build_forest(Ctx &c, int L) {
     FCK(cudaMalloc(&t->F, (size_t)ncell * NR * esz));
     FCK(cudaMemset(t->M, 0, (size_t)ncell * NR * esz));
     FCK(cudaMemset(t->F, 0, (size_t)ncell * NR * esz));
-    const int smem_p2m = (int)(NR * 65 * esz), smem_tr = (int)((NR * NR + NR * (TB + 4)) * esz);
+    const int smem_p2m = (int)(NR * 65 * esz);
     if (fp32) {
         FCK(cudaFuncSetAttribute(k_p2m<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_p2m));
-        FCK(cudaFuncSetAttribute(k_translate<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_tr));
+        FCK(cudaFuncSetAttribute(k_translate<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, tr_smem<float>()));
     } else {
         FCK(cudaFuncSetAttribute(k_p2m<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_p2m));
-        FCK(cudaFuncSetAttribute(k_translate<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_tr));
+        FCK(cudaFuncSetAttribute(k_translate<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, tr_smem<double>()));
     }
     if (c.opts.profile)
         for (auto &set : t->ev)
@@ -915,7 +923,8 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
     const int L = t.L;
     T *M = (T *)t.M, *F = (T *)t.F;
     const size_t esz = sizeof(T);
-    const int smem_p2m = (int)(NR * 65 * esz), smem_tr = (int)((NR * NR + NR * (TB + 4)) * esz);
+    const int smem_p2m = (int)(NR * 65 * esz);
+    constexpr int TB = TrShape<T>::TB;
     const bool prof = c.opts.profile && t.ev[0][0];
     cudaEvent_t *ev = t.ev[t.ev_next];
     if (prof) {
@@ -951,7 +960,7 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
         } else {
             const void *ops = kind == M2M ? t.op_m2m : kind == M2L ? t.op_m2l : t.op_l2l;
             T *in = kind == L2L ? F : M, *out = kind == M2M ? M : F;
-            k_translate<T><<<(n + TB - 1) / TB, 160, smem_tr, c.stream>>>(n, out0, ncode, tab, (const T *)ops, in,
+            k_translate<T><<<(n + TB - 1) / TB, 160, tr_smem<T>(), c.stream>>>(n, out0, ncode, tab, (const T *)ops, in,
                                                                             out, kind == L2L);
         }
     };
