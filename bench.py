@@ -239,11 +239,17 @@ def main():
     ap.add_argument("--workload", default="film", choices=["film", "batch64"])
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--train-steps", type=int, default=40, help="untimed solves that train the learned guess")
+    ap.add_argument("--train-every", type=int, default=4,
+                    help="after those, the guess keeps training (timed) on every n-th solve")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--drift", type=int, default=0,
                     help="accuracy study: N steps of the headline path and of the plain FP64 path from the same "
                          "state and angles; prints max |dm|, rel-L2 of v and phi (its own JSON line)")
+    ap.add_argument("--drift-pair", default="mixed-plain", choices=["mixed-plain", "plain-plainguess"],
+                    help="mixed-plain: headline path vs plain FP64; plain-plainguess: plain FP64 with the "
+                         "previous-step guess vs plain FP64 with the learned guess (same arithmetic, another "
+                         "valid initial guess: the spread the tolerance alone allows)")
     ap.add_argument("--quick", action="store_true",
                     help="timed steps only (no training, comparisons, end-to-end or CPU legs): for profiling")
     args = ap.parse_args()
@@ -278,7 +284,7 @@ def main():
     # learned guess + FP32 body + FP64 refinement (headline). The guess is trained online
     # on the solver's own solutions; those solves are not timed.
     ctx = fg.Context(mesh, regions(), tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP32_REFINE,
-                     demag=fg.FG_DEMAG_FMM, learned_guess=1, profile=1)
+                     demag=fg.FG_DEMAG_FMM, learned_guess=1, mlp_train_every=args.train_every, profile=1)
     ctx.set_state(u0)
     ctx.compute_all(H)  # initial compute_all of the reference loop (time_integration.cpp:140)
     train_ms, _ = run_steps(ctx, args.train_steps, H, DT, angles)
@@ -388,7 +394,7 @@ def main():
             "data": "synthetic (seeded smoothed random film state)",
             "config": {"workload": "film 400x400x10 nm, 2 nm grid: 1,200,000 tets, 242,406 nodes; alpha 0.02; "
                                    "dt 5e-14; BiCG tol 1e-6; FMM P=9; learned guess trained online for "
-                                   f"{args.train_steps} untimed solves",
+                                   f"{args.train_steps} untimed solves, then on every {args.train_every}th",
                        "global_batch": 1, "seq_len": 0, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (tets 163 MB + sources 107 MB + FMM operators 15 MB per step)"},
             "plain_fp64_steps_per_s": plain_value,
@@ -429,8 +435,13 @@ def drift_study(args):
     fg.rng_seed(SEED)
     angles = [fg.rng_angle() for _ in range(args.drift)]
     out = {}
-    for name, opts in (("mixed", dict(precision=fg.FG_PREC_FP32_REFINE, learned_guess=1)),
-                       ("plain", dict(precision=fg.FG_PREC_FP64))):
+    if args.drift_pair == "mixed-plain":
+        pair = (("mixed", dict(precision=fg.FG_PREC_FP32_REFINE, learned_guess=1, mlp_train_every=args.train_every)),
+                ("plain", dict(precision=fg.FG_PREC_FP64)))
+    else:
+        pair = (("mixed", dict(precision=fg.FG_PREC_FP64, learned_guess=1, mlp_train_every=args.train_every)),
+                ("plain", dict(precision=fg.FG_PREC_FP64)))
+    for name, opts in pair:
         c = fg.Context(mesh, regions(), tol=TOL, max_iter=MAXITER, demag=fg.FG_DEMAG_FMM, **opts)
         c.set_state(u0)
         c.compute_all(H)
@@ -444,7 +455,9 @@ def drift_study(args):
 
     def rel(x, y):
         return float(np.linalg.norm(x - y) / np.linalg.norm(y))
-    line = {"metric": f"max |dm| after {args.drift} steps, learned-guess FP32+refine vs plain FP64 (film 1.2M tets)",
+    what = ("learned-guess FP32+refine vs plain FP64" if args.drift_pair == "mixed-plain"
+            else "plain FP64 learned guess vs plain FP64 previous-step guess")
+    line = {"metric": f"max |dm| after {args.drift} steps, {what} (film 1.2M tets)",
             "value": float(dm.max()), "unit": "1", "higher_is_better": False, "steps": args.drift,
             "rel_l2_u": rel(a["u"], b["u"]), "rel_l2_v": rel(a["v"], b["v"]), "rel_l2_phi": rel(a["phi"], b["phi"]),
             "rel_l2_phiv": rel(a["phiv"], b["phiv"]),

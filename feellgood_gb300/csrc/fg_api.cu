@@ -135,6 +135,7 @@ void fg_opts_default(fg_opts *o) {
     o->mlp_batch = 16384;
     o->mlp_lr = 1e-3;
     o->fmm_tensor = 1;
+    o->mlp_train_every = 1;
 }
 
 const char *fg_strerror(int s) {
@@ -693,7 +694,13 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
         mlp_after_sync(c, use_mlp ? &accepted : nullptr, &r0m, &r0p, nullptr);
         if (!use_mlp) { r0m = r.res0; r0p = r.res0; }
         // train on this step's solution (asynchronous; its loss is read at the next sync)
-        if (status == FG_OK) CK(mlp_train(c));
+        if (status == FG_OK) {
+            const int every = std::max(1, c.opts.mlp_train_every);
+            if (!use_mlp || (++h->solves_since_train) >= every) {
+                h->solves_since_train = 0;
+                CK(mlp_train(c));
+            }
+        }
     }
     if (rep) {
         std::memset(rep, 0, sizeof(*rep));

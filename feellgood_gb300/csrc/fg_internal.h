@@ -302,4 +302,5 @@ cudaError_t launch_energy_seg(Ctx &c);
 struct fg_ctx {
     fg::Ctx c;
     double last_c0 = 0.0;
+    int solves_since_train = 0;  // learned guess: successful solves since the last training step
 };

@@ -94,6 +94,8 @@ typedef struct {
     double mlp_lr;        /* learned guess: Adam learning rate */
     int fmm_tensor;       /* FP32 FMM: 1 (default) translations on the tensor cores (3 x TF32 MMAs),
                              0 on the CUDA cores */
+    int mlp_train_every;  /* learned guess: after the first mlp_train_steps solves, train on every
+                             n-th successful solve only (1, the default: on every one) */
 } fg_opts;
 
 typedef struct {
