@@ -141,6 +141,12 @@ def max_over_ranks(dist, x):
     return float(t.item())
 
 
+def replicas_value(dist, world, steps, seconds):
+    """Whole-job throughput of N independent replicas: all ranks' steps over the slowest rank's time."""
+    slowest = max_over_ranks(dist, seconds)
+    return world * steps / slowest, slowest
+
+
 def run_steps(ctx, n, H, dtmax, angles):
     """n accepted steps (angles: a callable or a sequence); returns (per-step device ms of the
     phases [elements, solve, demag x2, energy + evolution, whole step], reports)."""
@@ -211,6 +217,24 @@ def reference_arm(args):
 
 
 P2P_FLOPS_PER_PAIR = 9  # 3 sub, 3 fma (r^2), rsqrt, fma (q/r): FP32 + SFU
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes (read + write) of one launch of `kernel` on the film workload, from the ncu
+    capture summarised in profiles/<kernel>_film_1.2M.md (None if there is no capture)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_film_1.2M.md")
+    scale = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
+    try:
+        tot, seen = 0.0, 0
+        for line in open(path):
+            for key in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+                if f"`{key}`" in line:
+                    val, unit = line.split("|")[2].split()
+                    tot += float(val.replace(",", "")) * scale[unit]
+                    seen += 1
+        return tot if seen == 2 else None
+    except (OSError, ValueError, KeyError):
+        return None
 
 
 def roofline_of(kernel, ms, units, peaks):
@@ -295,6 +319,8 @@ def main():
     launches0 = ctx.counters()[0]
     clk = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")) if world > 1 else 0)
     clk.start()
+    if dist is not None:
+        dist.barrier()
     t_wall0 = time.perf_counter()
     ms, reps = run_steps(ctx, args.steps, H, DT, step_angles)
     t_wall = time.perf_counter() - t_wall0
@@ -302,8 +328,7 @@ def main():
     fmm_stage = ctx.fmm_timings()
     cnt = ctx.counters()
     launches = (cnt[0] - launches0) // args.steps
-    dev_s = max_over_ranks(dist, float(ms[:, 4].sum()) / 1e3)
-    value = world * args.steps / dev_s
+    value, dev_s = replicas_value(dist, world, args.steps, float(ms[:, 4].sum()) / 1e3)
     iters = [r["iters"] for r in reps]
     refs = [r["refinements"] for r in reps]
     acc = [r["guess_accepted"] for r in reps]
@@ -370,7 +395,9 @@ def main():
                                                           nn * (3 * 8 + 2 * 8 + 8 * 8)}),
     }
     dom = max(kernels, key=lambda k: kernels[k][0] * kernels[k][1])
+    kernels[dom][2]["traffic"] = ncu_traffic(dom.split()[0])
     roof = roofline_of(dom, kernels[dom][0], kernels[dom][2], peaks)
+    roof["traffic_source"] = f"profiles/{dom.split()[0]}_film_1.2M.md (one ncu launch)"
     roof["share_of_step"] = kernels[dom][0] * kernels[dom][1] / float(ms[:, 4].mean())
     if dom.startswith("k_l2p_p2p"):
         # the near field does one reciprocal square root per (target, source) pair: its real
