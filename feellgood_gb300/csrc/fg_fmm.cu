@@ -178,82 +178,79 @@ static void l2l_c(const std::vector<cd> &F, const std::vector<cd> &U, int P, std
 // ---------------------------------------------------------------------------------
 // device
 
-template <typename T, typename Fn>
-__device__ __forceinline__ void ups_cols(T x, T y, T z, Fn &&f) {
-    constexpr int P = FMM_P;
-    const T r2 = x * x + y * y + z * z;
-    T dre = 1, dim = 0;
-#pragma unroll
-    for (int m = 0; m <= P; m++) {
-        if (m > 0) {
-            const T s = T(1) / T(2 * m);
-            const T nre = (x * dre - y * dim) * s, nim = (x * dim + y * dre) * s;
-            dre = nre;
-            dim = nim;
-        }
-        f(m, m, dre, dim);
+template <typename T, int M, typename Fn>
+__device__ __forceinline__ void ups_col(T x, T y, T z, T r2, T &dre, T &dim, Fn &f) {
+    if constexpr (M > 0) {
+        const T s = T(1) / T(2 * M);
+        const T nre = (x * dre - y * dim) * s, nim = (x * dim + y * dre) * s;
+        dre = nre;
+        dim = nim;
+    }
+    f(M, M, dre, dim);
+    if constexpr (M + 1 <= FMM_P) {
         T p2re = dre, p2im = dim;
         T p1re = z * dre, p1im = z * dim;
-        if (m + 1 <= P) f(m + 1, m, p1re, p1im);
+        f(M + 1, M, p1re, p1im);
 #pragma unroll
-        for (int n = m + 2; n <= P; n++) {
-            const T a = T(2 * n - 1), b = T(1) / T((n + m) * (n - m));
+        for (int n = M + 2; n <= FMM_P; n++) {
+            const T a = T(2 * n - 1), b = T(1) / T((n + M) * (n - M));
             const T cre = (a * z * p1re - r2 * p2re) * b, cim = (a * z * p1im - r2 * p2im) * b;
-            f(n, m, cre, cim);
+            f(n, M, cre, cim);
             p2re = p1re; p2im = p1im;
             p1re = cre; p1im = cim;
         }
     }
+    if constexpr (M < FMM_P) ups_col<T, M + 1>(x, y, z, r2, dre, dim, f);
+}
+
+// Every Ups_n^m(x, y, z), 0 <= m <= n <= P, passed to f(n, m, re, im) by the recurrences
+// in m (diagonal) and n (columns); the column index m is a template parameter so that
+// callers accumulating into register arrays see constant indices.
+template <typename T, typename Fn>
+__device__ __forceinline__ void ups_cols(T x, T y, T z, Fn &&f) {
+    const T r2 = x * x + y * y + z * z;
+    T dre = 1, dim = 0;
+    ups_col<T, 0>(x, y, z, r2, dre, dim, f);
 }
 
 
-// P2M: one block (64 threads) per leaf; each thread forms q*conj(Ups) of one source into a
-// shared tile, each coefficient is summed over the tile in a fixed order.
+// P2M: one warp per leaf; each lane forms q*conj(Ups) of every 32nd source of the leaf into
+// 100 register accumulators, which are then reduced over the warp in a fixed order (lane
+// k mod 32 stores coefficient k). The charge is also stored beside the source coordinates
+// for the near field, and with the tensor-core translations the hi/lo split of M.
 template <typename T>
-__global__ void __launch_bounds__(64) k_p2m(int nleaf, const int *__restrict__ leaf_src, T *__restrict__ sloc,
-                                            const double *__restrict__ q, int leaf0, T *__restrict__ M,
-                                            float *__restrict__ Mh, float *__restrict__ Ml) {
-    constexpr int LD = 65;
-    extern __shared__ unsigned char smem_raw[];
-    T *tile = reinterpret_cast<T *>(smem_raw);  // [NR][LD]
-    const int leaf = blockIdx.x, tid = threadIdx.x;
+__global__ void __launch_bounds__(128) k_p2m(int nleaf, const int *__restrict__ leaf_src, T *__restrict__ sloc,
+                                             const double *__restrict__ q, int leaf0, T *__restrict__ M,
+                                             float *__restrict__ Mh, float *__restrict__ Ml) {
+    const int lane = threadIdx.x & 31;
+    const int leaf = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (leaf >= nleaf) return;
     const int s0 = leaf_src[leaf], s1 = leaf_src[leaf + 1];
-    T acc[2] = {0, 0};
-    for (int base = s0; base < s1; base += 64) {
-        const int s = base + tid;
-        if (s < s1) {
-            const T x = sloc[4 * (size_t)s], y = sloc[4 * (size_t)s + 1], z = sloc[4 * (size_t)s + 2];
-            const T qq = T(q[s]);
-            sloc[4 * (size_t)s + 3] = qq;  // charge beside the coordinates for the near field
-            ups_cols<T>(x, y, z, [&](int n, int m, T re, T im) {
-                tile[ridx(n, m, 0) * LD + tid] = qq * re;
-                if (m) tile[ridx(n, m, 1) * LD + tid] = -qq * im;
-            });
-        } else {
+    T acc[NR];
 #pragma unroll
-            for (int j = 0; j < NR; j++) tile[j * LD + tid] = 0;
-        }
-        __syncthreads();
-        const int cnt = min(64, s1 - base);
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int j = tid + 64 * h;
-            if (j < NR)
-                for (int k = 0; k < cnt; k++) acc[h] += tile[j * LD + k];
-        }
-        __syncthreads();
+    for (int k = 0; k < NR; k++) acc[k] = 0;
+    for (int s = s0 + lane; s < s1; s += 32) {
+        const T x = sloc[4 * (size_t)s], y = sloc[4 * (size_t)s + 1], z = sloc[4 * (size_t)s + 2];
+        const T qq = T(q[s]);
+        sloc[4 * (size_t)s + 3] = qq;  // charge beside the coordinates for the near field
+        ups_cols<T>(x, y, z, [&](int n, int m, T re, T im) {
+            acc[ridx(n, m, 0)] += qq * re;
+            if (m) acc[ridx(n, m, 1)] -= qq * im;
+        });
     }
+    const size_t base = (size_t)(leaf0 + leaf) * NR;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int j = tid + 64 * h;
-        if (j < NR) {
-            const size_t o = (size_t)(leaf0 + leaf) * NR + j;
-            M[o] = acc[h];
+    for (int k = 0; k < NR; k++) {
+        T v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((k & 31) == lane) {
+            M[base + k] = v;
             if (Mh) {  // split for the tensor-core translations: hi = tf32(x), lo = x - hi
-                const float x = (float)acc[h];
-                const float hi = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
-                Mh[o] = hi;
-                Ml[o] = x - hi;
+                const float xf = (float)v;
+                const float hi = __uint_as_float((__float_as_uint(xf) + 0x1000u) & 0xFFFFE000u);
+                Mh[base + k] = hi;
+                Ml[base + k] = xf - hi;
             }
         }
     }
@@ -398,11 +395,14 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_l2p_p2p(int nle
 #pragma unroll
             for (int j = 0; j < NT; j++) ns[j] += acc[j];
         }
+        // warp sums in the path's precision (fixed butterfly order), then FP64
         double near[NT];
 #pragma unroll
         for (int j = 0; j < NT; j++) {
-            near[j] = double(ns[j]);
-            for (int o = 16; o > 0; o >>= 1) near[j] += __shfl_xor_sync(0xffffffffu, near[j], o);
+            T v = ns[j];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            near[j] = double(v);
         }
         // L2P: lane j evaluates target j
         if (lane < nt) {
@@ -817,15 +817,17 @@ static int fmm_build_forest(Ctx &c, int L) {
         };
         t->tc_m2m.assign(L + 1, FmmTree::TcLaunch());
         t->tc_l2l.assign(L + 1, FmmTree::TcLaunch());
+        // M2M and L2L run level by level, each level a short launch: units of 2 codes keep
+        // its critical path short; M2L has the whole tree in one launch: units of 48 codes
         for (int l = L - 1; l >= 2; l--)
-            t->tc_m2m[l] = plan(t->lev_begin[l + 1] - t->lev_begin[l], t->lev_begin[l], 8, m2m_tab, 8);
+            t->tc_m2m[l] = plan(t->lev_begin[l + 1] - t->lev_begin[l], t->lev_begin[l], 8, m2m_tab, 2);
         t->tc_m2l = plan(ncell, 0, NCODE_M2L, m2l_tab, 48);
         for (int l = 3; l <= L; l++)
-            t->tc_l2l[l] = plan(t->lev_begin[l + 1] - t->lev_begin[l], t->lev_begin[l], 8, l2l_tab, 8);
+            t->tc_l2l[l] = plan(t->lev_begin[l + 1] - t->lev_begin[l], t->lev_begin[l], 8, l2l_tab, 2);
         FCK(up(&t->tc_code, codes));
         FCK(up(&t->tc_units, units));
         FCK(up(&t->tc_comb, comb));
-        FCK(cudaMalloc(&t->tc_scratch, sizeof(float) * (size_t)std::max(1, nslot) * 64 * NR));
+        FCK(cudaMalloc(&t->tc_scratch, sizeof(float) * (size_t)std::max(1, nslot) * translate_tc_tile() * NR));
         FCK(cudaMalloc(&t->tc_err, sizeof(int)));
         FCK(cudaMemset(t->tc_err, 0, sizeof(int)));
         FCK(translate_tc_setup());
@@ -868,12 +870,9 @@ static int fmm_build_forest(Ctx &c, int L) {
     FCK(cudaMalloc(&t->F, (size_t)ncell * NR * esz));
     FCK(cudaMemset(t->M, 0, (size_t)ncell * NR * esz));
     FCK(cudaMemset(t->F, 0, (size_t)ncell * NR * esz));
-    const int smem_p2m = (int)(NR * 65 * esz);
     if (fp32) {
-        FCK(cudaFuncSetAttribute(k_p2m<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_p2m));
         FCK(cudaFuncSetAttribute(k_translate<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, tr_smem<float>()));
     } else {
-        FCK(cudaFuncSetAttribute(k_p2m<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_p2m));
         FCK(cudaFuncSetAttribute(k_translate<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, tr_smem<double>()));
     }
     if (c.opts.profile)
@@ -923,7 +922,6 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
     const int L = t.L;
     T *M = (T *)t.M, *F = (T *)t.F;
     const size_t esz = sizeof(T);
-    const int smem_p2m = (int)(NR * 65 * esz);
     constexpr int TB = TrShape<T>::TB;
     const bool prof = c.opts.profile && t.ev[0][0];
     cudaEvent_t *ev = t.ev[t.ev_next];
@@ -932,8 +930,8 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
         cudaEventRecord(ev[0], c.stream);
     }
     const bool tc = tc_path<T>(t);
-    k_p2m<T><<<t.nleaf, 64, smem_p2m, c.stream>>>(t.nleaf, t.leaf_src, (T *)t.sloc, c.src_q, t.leaf0, M,
-                                                    tc ? t.Mh : nullptr, tc ? t.Ml : nullptr);
+    k_p2m<T><<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, (T *)t.sloc, c.src_q, t.leaf0, M,
+                                                       tc ? t.Mh : nullptr, tc ? t.Ml : nullptr);
     if (prof) cudaEventRecord(ev[1], c.stream);
     // out (+)= sum_code Op[code] in[tab[cell][code]] over n output cells from out0
     // out (+)= sum_code Op[code] in[tab[cell][code]] over n output cells from out0; the

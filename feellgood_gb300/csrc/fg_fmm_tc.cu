@@ -413,6 +413,7 @@ __global__ void __launch_bounds__(256) k_tc_combine(TcArgs a) {
 }  // namespace
 
 int translate_tc_smem() { return NSTAGE * STAGE_BYTES + 1024; }
+int translate_tc_tile() { return NC; }
 
 cudaError_t translate_tc_setup() {
     cudaError_t e = cudaFuncSetAttribute(k_m2m_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, translate_tc_smem());

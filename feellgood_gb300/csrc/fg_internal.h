@@ -255,6 +255,7 @@ int *fmm_error_flag(const Ctx &c);
 int fmm_launches_per_eval(const Ctx &c);  // kernels one FMM evaluation launches  // device int: FG_ETIMEDOUT after an expired wait (or nullptr)
 // tensor-core translations (fg_fmm_tc.cu)
 int translate_tc_smem();
+int translate_tc_tile();  // output cells per tile of the tensor-core translations
 cudaError_t translate_tc_setup();
 // out (+)= sum_code Op[code] in[tab[cell][code]] over n_out cells from out0 (FP32 path)
 struct TcArgs {
