@@ -56,7 +56,7 @@ class fg_opts(C.Structure):
                 ("first_order", C.c_int), ("refine_max", C.c_int), ("inner_tol", C.c_double),
                 ("verbose", C.c_int), ("profile", C.c_int), ("mlp_train_steps", C.c_int), ("mlp_batch", C.c_int),
                 ("mlp_lr", C.c_double), ("fmm_tensor", C.c_int),
-                ("mlp_train_every", C.c_int)]
+                ("mlp_train_every", C.c_int), ("fmm_native_fp64", C.c_int)]
 
 
 class fg_step_report(C.Structure):

@@ -70,6 +70,10 @@ struct FmmTree {
     int *leaf_src = nullptr, *leaf_tgt = nullptr, *tgt_node = nullptr;
     void *sloc = nullptr;  // 4 x nsrc: leaf-local source coordinates (T), w unused
     void *tloc = nullptr;  // 4 x ntgt: leaf-local target coordinates (T)
+    // FP64 path, near field in double-single arithmetic: every coordinate split as
+    // hi (on a 2^-20 grid of leaf units) + lo, the charge as hi + lo; (x, y, z, q) per part
+    bool ds = false;
+    float4 *ds_src_hi = nullptr, *ds_src_lo = nullptr, *ds_tgt_hi = nullptr, *ds_tgt_lo = nullptr;
     int *leaf_ijk = nullptr;  // 3 x nleaf integer leaf coordinates (within the leaf's own tree)
     double *leaf_scale = nullptr;  // 1 / physical leaf width of the leaf's tree
     int *m2l_tab = nullptr;   // [ncell][343] source cell or -1
@@ -221,7 +225,8 @@ __device__ __forceinline__ void ups_cols(T x, T y, T z, Fn &&f) {
 template <typename T>
 __global__ void __launch_bounds__(128) k_p2m(int nleaf, const int *__restrict__ leaf_src, T *__restrict__ sloc,
                                              const double *__restrict__ q, int leaf0, T *__restrict__ M,
-                                             float *__restrict__ Mh, float *__restrict__ Ml) {
+                                             float *__restrict__ Mh, float *__restrict__ Ml,
+                                             float4 *__restrict__ ds_hi, float4 *__restrict__ ds_lo) {
     const int lane = threadIdx.x & 31;
     const int leaf = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (leaf >= nleaf) return;
@@ -233,6 +238,11 @@ __global__ void __launch_bounds__(128) k_p2m(int nleaf, const int *__restrict__ 
         const T x = sloc[4 * (size_t)s], y = sloc[4 * (size_t)s + 1], z = sloc[4 * (size_t)s + 2];
         const T qq = T(q[s]);
         sloc[4 * (size_t)s + 3] = qq;  // charge beside the coordinates for the near field
+        if (ds_hi) {  // charge as hi + lo for the double-single near field
+            const float qh = (float)q[s];
+            ds_hi[s].w = qh;
+            ds_lo[s].w = (float)(q[s] - (double)qh);
+        }
         ups_cols<T>(x, y, z, [&](int n, int m, T re, T im) {
             acc[ridx(n, m, 0)] += qq * re;
             if (m) acc[ridx(n, m, 1)] -= qq * im;
@@ -417,6 +427,121 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_l2p_p2p(int nle
                 else far += T(2) * (Fl[ridx(n, m, 0)] * re + Fl[ridx(n, m, 1)] * im);
             });
             pot[tgt_node[tb + lane]] = (double(far) + nr) * leaf_scale[leaf];
+        }
+    }
+}
+
+// Double-single arithmetic on the FP32 pipes: an FP64-accurate near field for the FP64
+// path, whose FP64 pipe (2 DFMA per clock and SM on this GPU) would otherwise bound it.
+// A value is hi + lo with |lo| <= ulp(hi)/2 (Dekker, "A floating-point technique for
+// extending the available precision", 1971; Knuth's two-sum).
+__device__ __forceinline__ void ds_two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// L2P + P2P of the FP64 path in double-single arithmetic. Coordinates are leaf-local with
+// hi parts on a 2^-20 grid (|x| < 4, so hi - hi' is exact in FP32) and lo = x - hi
+// (|lo| <= 2^-21, held to 2^-45); per pair: dx = (hi - hi') + (lo - lo'), r^2 as a
+// double-single sum of the squares (the leading products exact through fma), 1/r from the
+// SFU estimate and one Newton step evaluated in double-single (error ~1e-13), q/r as a
+// double-single product, summed with two-sum. One warp per target leaf, 8 targets per
+// lane pass, sources spread over the lanes; per-lane sums reduced over the warp in FP64.
+__global__ void __launch_bounds__(128) k_l2p_p2p_ds(int nleaf, const int *__restrict__ leaf_src,
+                                                    const int *__restrict__ leaf_tgt,
+                                                    const int *__restrict__ tgt_node,
+                                                    const double *__restrict__ tloc,
+                                                    const float4 *__restrict__ th4, const float4 *__restrict__ tl4,
+                                                    const float4 *__restrict__ sh4, const float4 *__restrict__ sl4,
+                                                    const int *__restrict__ leaf_ijk, int leaf0,
+                                                    const double *__restrict__ leaf_scale,
+                                                    const int *__restrict__ near_ptr,
+                                                    const int *__restrict__ near_leaf, const double *__restrict__ F,
+                                                    double *__restrict__ pot) {
+    constexpr int NT = 8;
+    const int lane = threadIdx.x & 31;
+    const int leaf = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (leaf >= nleaf) return;
+    const int t0 = leaf_tgt[leaf], t1 = leaf_tgt[leaf + 1];
+    if (t0 == t1) return;
+    const int li = leaf_ijk[3 * leaf], lj = leaf_ijk[3 * leaf + 1], lk = leaf_ijk[3 * leaf + 2];
+    const double *Fl = F + (size_t)(leaf0 + leaf) * NR;
+    for (int tb = t0; tb < t1; tb += NT) {
+        const int nt = min(NT, t1 - tb);
+        float thx[NT], thy[NT], thz[NT], tlx[NT], tly[NT], tlz[NT], ah[NT], al[NT];
+#pragma unroll
+        for (int j = 0; j < NT; j++) {
+            const int ti = tb + (j < nt ? j : 0);
+            const float4 h = th4[ti], l = tl4[ti];
+            thx[j] = h.x; thy[j] = h.y; thz[j] = h.z;
+            tlx[j] = l.x; tly[j] = l.y; tlz[j] = l.z;
+            ah[j] = 0.f;
+            al[j] = 0.f;
+        }
+        for (int e = near_ptr[leaf]; e < near_ptr[leaf + 1]; e++) {
+            const int nl = near_leaf[e];
+            // integer offset of the adjacent leaf, added exactly to the hi parts
+            const float ox = float(leaf_ijk[3 * nl] - li), oy = float(leaf_ijk[3 * nl + 1] - lj),
+                        oz = float(leaf_ijk[3 * nl + 2] - lk);
+            const int s0 = leaf_src[nl], s1 = leaf_src[nl + 1];
+            for (int s = s0 + lane; s < s1; s += 32) {
+                const float4 h = sh4[s], l = sl4[s];
+                const float sx = h.x + ox, sy = h.y + oy, sz = h.z + oz, qh = h.w, ql = l.w;
+#pragma unroll
+                for (int j = 0; j < NT; j++) {
+                    const float d1x = thx[j] - sx, d1y = thy[j] - sy, d1z = thz[j] - sz;  // exact
+                    const float d2x = tlx[j] - l.x, d2y = tly[j] - l.y, d2z = tlz[j] - l.z;
+                    // squares: d^2 = d1^2 + d2 (2 d1 + d2), leading products exact
+                    const float px = d1x * d1x, py = d1y * d1y, pz = d1z * d1z;
+                    float ex = fmaf(d1x, d1x, -px), ey = fmaf(d1y, d1y, -py), ez = fmaf(d1z, d1z, -pz);
+                    ex = fmaf(d2x, 2.f * d1x + d2x, ex);
+                    ey = fmaf(d2y, 2.f * d1y + d2y, ey);
+                    ez = fmaf(d2z, 2.f * d1z + d2z, ez);
+                    float s1_, e1, s2_, e2;
+                    ds_two_sum(px, py, s1_, e1);
+                    ds_two_sum(s1_, pz, s2_, e2);
+                    const float el = (e1 + e2) + (ex + ey + ez);
+                    const float Sh = s2_ + el, Sl = el - (Sh - s2_);
+                    // 1/sqrt(S): SFU estimate y, then y (1 + (1 - S y^2) / 2) with S y^2 in
+                    // double-single (1 - S y^2 is small and exact to ~2^-46)
+                    float y;
+                    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(Sh));
+                    const float t1_ = y * y, t2_ = fmaf(y, y, -t1_);
+                    const float u1 = Sh * t1_;
+                    const float u2 = fmaf(Sh, t1_, -u1) + fmaf(Sh, t2_, Sl * t1_);
+                    const float delta = (1.f - u1) - u2;
+                    const float yl = 0.5f * y * delta;
+                    // q / r = (qh + ql)(y + yl), accumulated with two-sum
+                    const float c1 = qh * y;
+                    const float c2 = fmaf(qh, y, -c1) + fmaf(qh, yl, ql * y);
+                    float sn, en;
+                    ds_two_sum(ah[j], c1, sn, en);
+                    ah[j] = sn;
+                    al[j] += en + c2;
+                }
+            }
+        }
+        double near[NT];
+#pragma unroll
+        for (int j = 0; j < NT; j++) {
+            near[j] = double(ah[j]) + double(al[j]);
+            for (int o = 16; o > 0; o >>= 1) near[j] += __shfl_xor_sync(0xffffffffu, near[j], o);
+        }
+        // L2P in FP64: lane j evaluates target j
+        if (lane < nt) {
+            double nr = 0;
+#pragma unroll
+            for (int j = 0; j < NT; j++)
+                if (j == lane) nr = near[j];
+            const int ti = tb + lane;
+            const double x = tloc[4 * (size_t)ti], y = tloc[4 * (size_t)ti + 1], z = tloc[4 * (size_t)ti + 2];
+            double far = 0;
+            ups_cols<double>(x, y, z, [&](int n, int m, double re, double im) {
+                if (m == 0) far += Fl[ridx(n, 0, 0)] * re;
+                else far += 2.0 * (Fl[ridx(n, m, 0)] * re + Fl[ridx(n, m, 1)] * im);
+            });
+            pot[tgt_node[ti]] = (far + nr) * leaf_scale[leaf];
         }
     }
 }
@@ -859,6 +984,33 @@ static int fmm_build_forest(Ctx &c, int L) {
     FCK(up(&t->near_leaf, near_leaf));
     FCK(up_as<double>(&t->sloc, sloc, fp32));
     FCK(up_as<double>(&t->tloc, tloc, fp32));
+    t->ds = !fp32 && c.opts.fmm_native_fp64 == 0;
+    if (t->ds) {
+        // x = hi + lo, hi on the 2^-20 grid (|x| < 4 leaf units: exact in FP32)
+        auto split = [](const std::vector<double> &v, std::vector<float4> &hi, std::vector<float4> &lo) {
+            const size_t n = v.size() / 4;
+            hi.resize(n);
+            lo.resize(n);
+            for (size_t k = 0; k < n; k++) {
+                float h[3], l[3];
+                for (int d = 0; d < 3; d++) {
+                    const double x = v[4 * k + d];
+                    const double xh = std::nearbyint(x * 1048576.0) / 1048576.0;
+                    h[d] = (float)xh;
+                    l[d] = (float)(x - xh);
+                }
+                hi[k] = make_float4(h[0], h[1], h[2], 0.f);
+                lo[k] = make_float4(l[0], l[1], l[2], 0.f);
+            }
+        };
+        std::vector<float4> sh, sl, th, tl;
+        split(sloc, sh, sl);
+        split(tloc, th, tl);
+        FCK(up(&t->ds_src_hi, sh));
+        FCK(up(&t->ds_src_lo, sl));
+        FCK(up(&t->ds_tgt_hi, th));
+        FCK(up(&t->ds_tgt_lo, tl));
+    }
     FCK(up_as<double>(&t->op_m2l, ops.m2l, fp32));
     FCK(up_as<double>(&t->op_m2m, ops.m2m, fp32));
     FCK(up_as<double>(&t->op_l2l, ops.l2l, fp32));
@@ -890,7 +1042,7 @@ void fmm_free(Ctx &c) {
     void *ptrs[] = {t->leaf_scale, t->leaf_src, t->leaf_tgt, t->tgt_node, t->sloc, t->tloc, t->leaf_ijk, t->m2l_tab, t->m2m_tab,
                     t->l2l_tab, t->near_ptr, t->near_leaf, t->M, t->F, t->op_m2l, t->op_m2m, t->op_l2l,
                     t->tc_code, t->tc_units, t->tc_comb, t->tc_scratch, t->tc_err, t->Mh, t->Ml, t->Fh, t->Fl,
-                    t->img_m2l, t->img_m2m, t->img_l2l};
+                    t->img_m2l, t->img_m2m, t->img_l2l, t->ds_src_hi, t->ds_src_lo, t->ds_tgt_hi, t->ds_tgt_lo};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &set : t->ev)
@@ -931,7 +1083,8 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
     }
     const bool tc = tc_path<T>(t);
     k_p2m<T><<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, (T *)t.sloc, c.src_q, t.leaf0, M,
-                                                       tc ? t.Mh : nullptr, tc ? t.Ml : nullptr);
+                                                       tc ? t.Mh : nullptr, tc ? t.Ml : nullptr,
+                                                       t.ds ? t.ds_src_hi : nullptr, t.ds ? t.ds_src_lo : nullptr);
     if (prof) cudaEventRecord(ev[1], c.stream);
     // out (+)= sum_code Op[code] in[tab[cell][code]] over n output cells from out0
     // out (+)= sum_code Op[code] in[tab[cell][code]] over n output cells from out0; the
@@ -971,7 +1124,14 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
     for (int l = 3; l <= L; l++)
         translate(L2L, t.lev_begin[l + 1] - t.lev_begin[l], t.lev_begin[l], t.tc ? t.tc_l2l[l] : none);
     if (prof) cudaEventRecord(ev[4], c.stream);
-    k_l2p_p2p<T><<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node,
+    if (t.ds)
+        k_l2p_p2p_ds<<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node,
+                                                              (const double *)t.tloc, t.ds_tgt_hi, t.ds_tgt_lo,
+                                                              t.ds_src_hi, t.ds_src_lo, t.leaf_ijk, t.leaf0,
+                                                              t.leaf_scale, t.near_ptr, t.near_leaf,
+                                                              (const double *)F, c.pot);
+    else
+        k_l2p_p2p<T><<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node,
                                                            (const T *)t.tloc, (const T *)t.sloc, t.leaf_ijk, t.leaf0,
                                                            t.leaf_scale, t.near_ptr, t.near_leaf, F, c.pot);
     if (prof) {

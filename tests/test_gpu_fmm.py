@@ -90,3 +90,21 @@ def test_tensor_core_split_precision():
     print("tensor-core translation rel. error: 1 term %.2e, 3 terms %.2e" % (err[1], err[7]))
     assert err[7] < 1.5e-6
     assert err[7] < err[1] / 30
+
+
+@pytest.mark.parametrize("shape,leaf", [((12, 12, 12), -3), ((40, 40, 3), -4)])
+def test_double_single_near_field(shape, leaf):
+    """The FP64 path's near field in double-single arithmetic on the FP32 pipes against the
+    same near field on the FP64 pipe (same tree, same far field): FP64-level agreement."""
+    m = cases.cuboid(*shape)
+    u = cases.perturbed_state(m["xyz"], seed=9, sigma=0.3)
+    v = cases.tangent_field(u, seed=10)
+    cs = fg.Context(m, cases.regions(), demag=fg.FG_DEMAG_FMM, precision=fg.FG_PREC_FP64, fmm_leaf=leaf)
+    cs.set_state(u, v)
+    cn = fg.Context(m, cases.regions(), demag=fg.FG_DEMAG_FMM, precision=fg.FG_PREC_FP64, fmm_leaf=leaf,
+                    fmm_native_fp64=1)
+    cn.set_state(u, v)
+    for which in (0, 1):
+        ps, pn = cs.demag(which), cn.demag(which)
+        print("double-single vs FP64 near field, rel. difference %.2e" % _rel(ps, pn))
+        assert _rel(ps, pn) < 1e-12
