@@ -56,7 +56,8 @@ class fg_opts(C.Structure):
                 ("first_order", C.c_int), ("refine_max", C.c_int), ("inner_tol", C.c_double),
                 ("verbose", C.c_int), ("profile", C.c_int), ("mlp_train_steps", C.c_int), ("mlp_batch", C.c_int),
                 ("mlp_lr", C.c_double), ("fmm_tensor", C.c_int),
-                ("mlp_train_every", C.c_int), ("fmm_native_fp64", C.c_int)]
+                ("mlp_train_every", C.c_int), ("fmm_native_fp64", C.c_int),
+                ("solver_lpr", C.c_int)]
 
 
 class fg_step_report(C.Structure):
@@ -113,6 +114,7 @@ SIGNATURES = {
     "fg_mlp_debug_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p]),
     "fg_mlp_nparam": (C.c_int, []),
+    "fg_solver_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "fg_debug_translate_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_int]),
     "fg_batch_create": (C.c_int, [C.POINTER(fg_mesh), C.c_int, C.POINTER(fg_region), C.c_int,
@@ -376,6 +378,11 @@ class Context:
         if s == FG_ETIMEDOUT or s > FG_ETIMEDOUT:
             self._check(s)
         return s, [{k: getattr(r, k) for k, _ in fg_batch_report._fields_} for r in reps]
+
+    def solver_lanes_per_row(self):
+        v = C.c_int()
+        self._check(self.L.fg_solver_info(self.h, C.byref(v)))
+        return v.value
 
     def batch_run_info(self):
         g = C.c_int()

@@ -666,6 +666,10 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
         c.err = "fg_step: a batch context steps with fg_batch_step";
         return FG_EINVAL;
     }
+    if (c.opts.precision == FG_PREC_FP32_REFINE && c.lpr == 0) {
+        CK(launch_tet(c, dt, Hext));
+        CK(mixed_autotune(c, dt, prefactor, basis_angle));
+    }
     CK(cudaEventRecord(c.ev[0], c.stream));
     c.step_open = true;
     CK(launch_tet(c, dt, Hext));
@@ -883,6 +887,12 @@ int fg_mlp_debug_grad(fg_ctx *h, int nsamples, const float *feat, const float *t
 }
 
 int fg_mlp_nparam(void) { return mlp_nparam(); }
+
+int fg_solver_info(const fg_ctx *h, int *lanes_per_row) {
+    if (!h || !lanes_per_row) return FG_EINVAL;
+    *lanes_per_row = h->c.lpr;
+    return FG_OK;
+}
 
 int fg_fmm_timings(const fg_ctx *h, double ms[5]) {
     if (!h || !ms) return FG_EINVAL;

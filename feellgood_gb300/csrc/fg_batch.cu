@@ -305,6 +305,10 @@ int fg_batch_step(fg_ctx *h, const fg_sample_step *steps, fg_step_report *reps) 
     for (int g = 0; g < ns; g++) fill_par(c.hseg_par[g], steps[g]);
     const double H0[3] = {0, 0, 0};
     CK(cudaMemcpyAsync(c.seg_par, c.hseg_par, sizeof(SegPar) * ns, cudaMemcpyHostToDevice, c.stream));
+    if (c.lpr == 0) {
+        CK(launch_tet(c, 1.0, H0));
+        CK(mixed_autotune(c, 1.0, 1.0, 0.0));
+    }
     CK(cudaEventRecord(c.ev[0], c.stream));
     c.step_open = true;
     CK(launch_tet(c, 1.0, H0));
@@ -417,6 +421,13 @@ int fg_batch_run(fg_ctx *h, int n_steps, const fg_sample_step *steps, fg_batch_r
     CK(cudaMemsetAsync(c.step_ctr, 0, sizeof(int), c.stream));
     CK(cudaMemsetAsync(c.seg_acc, 0, sizeof(SegAcc) * ns, c.stream));
     CK(cudaStreamSynchronize(c.stream));  // the host schedule buffer is released below
+    if (c.lpr == 0) {  // choose the solver variant on the run's first step, before the capture
+        const double H0[3] = {0, 0, 0};
+        c.acc_active = nullptr;
+        CK(cudaMemcpyAsync(c.seg_par, c.seg_sched, sizeof(SegPar) * ns, cudaMemcpyDeviceToDevice, c.stream));
+        CK(launch_tet(c, 1.0, H0));
+        CK(mixed_autotune(c, 1.0, 1.0, 0.0));
+    }
     c.acc_active = c.seg_acc;
     if (c.graph_state == 0) try_capture(c);
     CK(cudaEventRecord(c.ev[6], c.stream));

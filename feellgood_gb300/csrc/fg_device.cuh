@@ -157,4 +157,43 @@ __device__ __forceinline__ void apply_row(int i, const int *__restrict__ Sptr, c
     y1 = c0 * (e0 * a0 + e1 * a1 + e2 * a2) + di * xp - ai * xq;
 }
 
+// apply_row for a group of LPR consecutive lanes sharing row i (LPR = 1: thread per row):
+// the lanes split the row's neighbour list and add their partial sums with shuffles, so a
+// row's column indices and values are read by adjacent lanes. Every lane of the warp must
+// call it (valid = false for lanes without a row); all lanes of the group get y0, y1.
+template <typename T, int LPR>
+__device__ __forceinline__ void apply_row_g(bool valid, int i, int sub, const int *__restrict__ Sptr,
+                                            const int *__restrict__ Scol, const T *__restrict__ Sval, const T *W,
+                                            const T *ep, const T *eq, const T *A, const T *Dl, T c0, T xp, T xq,
+                                            T &y0, T &y1) {
+    if constexpr (LPR == 1) {
+        if (valid) apply_row<T>(i, Sptr, Scol, Sval, W, ep, eq, A, Dl, c0, xp, xq, y0, y1);
+        return;
+    }
+    T a0 = 0, a1 = 0, a2 = 0;
+    if (valid) {
+        const int k1 = Sptr[i + 1];
+        for (int k = Sptr[i] + sub; k < k1; k += LPR) {
+            const int j = Scol[k];
+            const T s = Sval[k];
+            a0 += s * __ldcg(W + 3 * j);
+            a1 += s * __ldcg(W + 3 * j + 1);
+            a2 += s * __ldcg(W + 3 * j + 2);
+        }
+    }
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (valid) {
+        const T q0 = eq[3 * i], q1 = eq[3 * i + 1], q2 = eq[3 * i + 2];
+        const T e0 = ep[3 * i], e1 = ep[3 * i + 1], e2 = ep[3 * i + 2];
+        const T ai = A[i], di = Dl[i];
+        y0 = c0 * (q0 * a0 + q1 * a1 + q2 * a2) + ai * xp + di * xq;
+        y1 = c0 * (e0 * a0 + e1 * a1 + e2 * a2) + di * xp - ai * xq;
+    }
+}
+
 }  // namespace fg

@@ -202,6 +202,7 @@ struct Ctx {
     // persistent-kernel launch shapes
     int bicg_grid = 0, bicg_block = 256;
     int mixed_grid = 0;
+    int lpr = 0;  // lanes per row of the mixed solver's operator applications (0: not chosen yet)
 
     // timings
     cudaEvent_t ev[8];
@@ -250,6 +251,9 @@ cudaError_t launch_energy_into(Ctx &c, const double Hext[3], double *partial);
 int bicg_grid_size(Ctx &c, bool mixed);
 int mixed_grid_size(Ctx &c);
 int mixed_max_blocks(Ctx &c);
+// Chooses the lanes per row of the mixed solver (opts.solver_lpr, or the fastest of 1, 4, 8
+// timed on the current step's system); the node kernel is rerun before each timing.
+cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle);
 int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p);
 int *fmm_error_flag(const Ctx &c);
 int fmm_launches_per_eval(const Ctx &c);  // kernels one FMM evaluation launches  // device int: FG_ETIMEDOUT after an expired wait (or nullptr)

@@ -11,6 +11,8 @@
 // One cooperative launch per solve; the node update (Node::make_evol) is fused at the end.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <vector>
 
 #include "fg_device.cuh"
 #include "fg_internal.h"
@@ -48,10 +50,21 @@ __device__ __forceinline__ SegView seg_view(const MixedArgs &a) {
 // along the first reduction of each loop pass (slot 1, summed over the whole grid).
 #define SAMPLE_ROWS(i) for (int i = sv.lo + (blockIdx.x - sv.b0) * (int)blockDim.x + (int)threadIdx.x; i < sv.hi; i += rstride)
 
+// Rows of the operator applications: LPR lanes per row (LPR = 1: thread per row), the loop
+// warp-uniform so that the group shuffles see every lane; body(i, valid, sub).
+#define GROUP_ROWS(body)                                                                                \
+    for (int gbase = sv.lo + ((blockIdx.x - sv.b0) * (int)blockDim.x + (int)(threadIdx.x & ~31)) / LPR; \
+         gbase < sv.hi; gbase += gstride) {                                                             \
+        const int i_ = gbase + (int)(threadIdx.x & 31) / LPR;                                           \
+        body(i_, i_ < sv.hi, (int)threadIdx.x % LPR);                                                   \
+    }
+
+template <int LPR>
 __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
     const int G = gridDim.x;
     const SegView sv = seg_view(a);
     const int rstride = (sv.b1 - sv.b0) * blockDim.x;
+    const int gstride = (sv.b1 - sv.b0) * (int)blockDim.x / LPR;
     const bool multi = a.nseg > 1;
     double c0 = a.c0, dt = a.dt;
     if (a.seg) {
@@ -89,17 +102,21 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
             // refinement residual r64 = b - K x (FP64, masked)
             {
                 double rr = 0.0;
-                if (!done)
-                    SAMPLE_ROWS(i) {
-                        double y0, y1;
-                        apply_row<double>(i, a.Sptr, a.Scol, a.Sval, a.W64, a.ep, a.eq, a.A, a.Dl, c0, a.x[2 * i],
-                                          a.x[2 * i + 1], y0, y1);
-                        const bool m = a.mag[i];
-                        const double r0 = m ? a.b[2 * i] - y0 : 0.0, r1 = m ? a.b[2 * i + 1] - y1 : 0.0;
-                        a.r64[2 * i] = r0;
-                        a.r64[2 * i + 1] = r1;
-                        rr += r0 * r0 + r1 * r1;
-                    }
+                if (!done) {
+                    auto row = [&](int i, bool valid, int sub) {
+                        double y0 = 0, y1 = 0;
+                        apply_row_g<double, LPR>(valid, i, sub, a.Sptr, a.Scol, a.Sval, a.W64, a.ep, a.eq, a.A, a.Dl,
+                                                 c0, valid ? a.x[2 * i] : 0.0, valid ? a.x[2 * i + 1] : 0.0, y0, y1);
+                        if (valid && sub == 0) {
+                            const bool m = a.mag[i];
+                            const double r0 = m ? a.b[2 * i] - y0 : 0.0, r1 = m ? a.b[2 * i + 1] - y1 : 0.0;
+                            a.r64[2 * i] = r0;
+                            a.r64[2 * i + 1] = r1;
+                            rr += r0 * r0 + r1 * r1;
+                        }
+                    };
+                    GROUP_ROWS(row)
+                }
                 double v1[1] = {rr};
                 block_store<1>(v1, a.partial, G);
             }
@@ -180,16 +197,21 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
                     if (!grid_sync(a.bar)) goto timeout;
                     {
                         double vr = 0.0;
-                        if (act)
-                            SAMPLE_ROWS(i) {
-                                float y0, y1;
-                                apply_row<float>(i, a.Sptr, a.Scol, a.Sval32, a.W32, a.ep32, a.eq32, a.A32, a.Dl32,
-                                                 c32, a.phat[2 * i], a.phat[2 * i + 1], y0, y1);
-                                if (!a.mag[i]) y0 = y1 = 0.0f;
-                                a.v[2 * i] = y0;
-                                a.v[2 * i + 1] = y1;
-                                vr += (double)y0 * a.rt[2 * i] + (double)y1 * a.rt[2 * i + 1];
-                            }
+                        if (act) {
+                            auto row = [&](int i, bool valid, int sub) {
+                                float y0 = 0, y1 = 0;
+                                apply_row_g<float, LPR>(valid, i, sub, a.Sptr, a.Scol, a.Sval32, a.W32, a.ep32, a.eq32,
+                                                        a.A32, a.Dl32, c32, valid ? a.phat[2 * i] : 0.f,
+                                                        valid ? a.phat[2 * i + 1] : 0.f, y0, y1);
+                                if (valid && sub == 0) {
+                                    if (!a.mag[i]) y0 = y1 = 0.0f;
+                                    a.v[2 * i] = y0;
+                                    a.v[2 * i + 1] = y1;
+                                    vr += (double)y0 * a.rt[2 * i] + (double)y1 * a.rt[2 * i + 1];
+                                }
+                            };
+                            GROUP_ROWS(row)
+                        }
                         double v2[2] = {vr, (threadIdx.x == 0 && act) ? 1.0 : 0.0};
                         block_store<2>(v2, a.partial, G);
                     }
@@ -239,17 +261,22 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
                     if (!multi && !act) break;
                     {
                         double ts = 0.0, tt = 0.0;
-                        if (act)
-                            SAMPLE_ROWS(i) {
-                                float y0, y1;
-                                apply_row<float>(i, a.Sptr, a.Scol, a.Sval32, a.W32, a.ep32, a.eq32, a.A32, a.Dl32,
-                                                 c32, a.shat[2 * i], a.shat[2 * i + 1], y0, y1);
-                                if (!a.mag[i]) y0 = y1 = 0.0f;
-                                a.t[2 * i] = y0;
-                                a.t[2 * i + 1] = y1;
-                                ts += (double)y0 * a.s[2 * i] + (double)y1 * a.s[2 * i + 1];
-                                tt += (double)y0 * y0 + (double)y1 * y1;
-                            }
+                        if (act) {
+                            auto row = [&](int i, bool valid, int sub) {
+                                float y0 = 0, y1 = 0;
+                                apply_row_g<float, LPR>(valid, i, sub, a.Sptr, a.Scol, a.Sval32, a.W32, a.ep32, a.eq32,
+                                                        a.A32, a.Dl32, c32, valid ? a.shat[2 * i] : 0.f,
+                                                        valid ? a.shat[2 * i + 1] : 0.f, y0, y1);
+                                if (valid && sub == 0) {
+                                    if (!a.mag[i]) y0 = y1 = 0.0f;
+                                    a.t[2 * i] = y0;
+                                    a.t[2 * i + 1] = y1;
+                                    ts += (double)y0 * a.s[2 * i] + (double)y1 * a.s[2 * i + 1];
+                                    tt += (double)y0 * y0 + (double)y1 * y1;
+                                }
+                            };
+                            GROUP_ROWS(row)
+                        }
                         double v2[2] = {ts, tt};
                         block_store<2>(v2, a.partial, G);
                     }
@@ -373,16 +400,27 @@ timeout:
 }
 
 #undef SAMPLE_ROWS
+#undef GROUP_ROWS
 
 int mixed_max_blocks(Ctx &c) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed, 256, 0);
+    int per_sm2 = 0, per_sm3 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed<1>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_mixed<4>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm3, k_mixed<8>, 256, 0);
+    per_sm = std::min(per_sm, std::min(per_sm2, per_sm3));
     return std::max(1, per_sm) * c.nsm;
 }
 
 int mixed_grid_size(Ctx &c) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed, 256, 0);
+    {
+        int p1 = 0, p4 = 0, p8 = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p1, k_mixed<1>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p4, k_mixed<4>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p8, k_mixed<8>, 256, 0);
+        per_sm = std::min(p1, std::min(p4, p8));
+    }
     if (per_sm < 1) per_sm = 1;
     int g = per_sm * c.nsm;
     const int need = (c.nn + 255) / 256;
@@ -438,7 +476,64 @@ cudaError_t launch_mixed(Ctx &c, double dt, double prefactor) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_mixed, a);
+    const int lpr = c.lpr > 0 ? c.lpr : 1;
+    if (lpr == 8) return cudaLaunchKernelEx(&cfg, k_mixed<8>, a);
+    if (lpr == 4) return cudaLaunchKernelEx(&cfg, k_mixed<4>, a);
+    return cudaLaunchKernelEx(&cfg, k_mixed<1>, a);
+}
+
+cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle) {
+    if (c.lpr > 0) return cudaSuccess;
+    if (c.opts.solver_lpr == 1 || c.opts.solver_lpr == 4 || c.opts.solver_lpr == 8) {
+        c.lpr = c.opts.solver_lpr;
+        return cudaSuccess;
+    }
+    const int cand[3] = {1, 4, 8};
+    cudaEvent_t e0, e1;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e != cudaSuccess) return e;
+    e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) return e;
+    SegAcc *acc = c.acc_active;
+    c.acc_active = nullptr;
+    // the timed solves write NEXT (u1, v1) and the next initial guess is read from v1: keep
+    // both in spare FP64 vectors and put them back afterwards
+    const size_t n3 = 3 * sizeof(double) * c.nn;
+    double *keep_v = c.bv + 4 * (size_t)c.nn, *keep_u = keep_v + 3 * (size_t)c.nn;
+    if ((e = cudaMemcpyAsync(keep_v, c.v[1], n3, cudaMemcpyDeviceToDevice, c.stream)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(keep_u, c.u[1], n3, cudaMemcpyDeviceToDevice, c.stream)) != cudaSuccess) return e;
+    double best = 1e300;
+    int bestv = 1;
+    std::vector<SolveResult> res(c.batch ? c.nseg : 1);
+    for (int v : cand) {
+        c.lpr = v;
+        for (int rep = 0; rep < 2; rep++) {  // the first run of each variant warms it up
+            if ((e = launch_node(c, angle)) != cudaSuccess) break;
+            cudaEventRecord(e0, c.stream);
+            if ((e = launch_mixed(c, dt, prefactor)) != cudaSuccess) break;
+            cudaEventRecord(e1, c.stream);
+            cudaMemcpyAsync(res.data(), c.dres, sizeof(SolveResult) * res.size(), cudaMemcpyDeviceToHost, c.stream);
+            if ((e = cudaStreamSynchronize(c.stream)) != cudaSuccess) break;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            int it = 1;
+            for (const SolveResult &r : res) it = std::max(it, r.nit + r.nref);
+            if (rep == 1 && !res[0].timeout && ms / it < best) {
+                best = ms / it;
+                bestv = v;
+            }
+        }
+        if (e != cudaSuccess) break;
+        cudaMemsetAsync(c.bar, 0, sizeof(GridBar), c.stream);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaMemcpyAsync(c.v[1], keep_v, n3, cudaMemcpyDeviceToDevice, c.stream);
+    cudaMemcpyAsync(c.u[1], keep_u, n3, cudaMemcpyDeviceToDevice, c.stream);
+    c.acc_active = acc;
+    c.lpr = bestv;
+    if (c.opts.verbose) fprintf(stderr, "mixed solver: %d lane(s) per row\n", bestv);
+    return e;
 }
 
 }  // namespace fg

@@ -98,6 +98,9 @@ typedef struct {
                              n-th successful solve only (1, the default: on every one) */
     int fmm_native_fp64;  /* FP64 FMM: 0 (default) near field in double-single arithmetic on the
                              FP32 pipes (relative error ~1e-13); 1 on the FP64 pipe */
+    int solver_lpr;       /* FP32 + refinement solver: lanes sharing one row of the operator
+                             (1 thread per row, 4, 8); 0 (default): the fastest, timed on the
+                             first step */
 } fg_opts;
 
 typedef struct {
@@ -169,6 +172,10 @@ int fg_timings(const fg_ctx *ctx, double ms[5]);
 /* Counters: [0] kernels launched by the context so far, [1] FMM tree depth (0 without FMM),
  * [2] M2L (cell, cell) pairs, [3] P2P (target, source) pairs per evaluation. */
 int fg_counters(const fg_ctx *ctx, long long out[4]);
+
+/* Lanes per row the FP32 + refinement solver uses (1, 4 or 8; 0 before the first step when
+ * it is chosen by timing). */
+int fg_solver_info(const fg_ctx *ctx, int *lanes_per_row);
 
 /* Learned guess: training steps done and the last minibatch MSE (scaled units). */
 int fg_mlp_info(const fg_ctx *ctx, long long *train_steps, double *last_loss);

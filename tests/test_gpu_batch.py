@@ -21,7 +21,9 @@ pytestmark = pytest.mark.gpu
 
 SHAPES = [(4, 4, 4), (7, 5, 4), (5, 6, 8)]
 H = np.array([[0.0, 0.0, 3e4], [2e4, 0.0, 0.0], [1e4, -1e4, 5e3]])
-OPTS = dict(precision=fg.FG_PREC_FP32_REFINE, demag=fg.FG_DEMAG_FMM, fmm_leaf=-3, tol=1e-9, refine_max=12)
+# fixed solver variant and tree depth: bitwise comparisons across contexts need the same kernels
+OPTS = dict(precision=fg.FG_PREC_FP32_REFINE, demag=fg.FG_DEMAG_FMM, fmm_leaf=-3, tol=1e-9, refine_max=12,
+            solver_lpr=1)
 
 
 def _samples():
@@ -134,3 +136,24 @@ def test_batch_run_graph_equals_stepwise():
     assert a.batch_run_info()[0] == graph
     u = a.get_state(0)["u"]
     assert np.allclose(np.linalg.norm(u, axis=1), 1.0, atol=1e-12)
+
+
+@pytest.mark.parametrize("lpr", [4, 8])
+def test_batch_solver_lanes_per_row(lpr):
+    """The group-per-row operator applications give the thread-per-row solution to the
+    solver tolerance (only the order of the row sums differs)."""
+    ms, us = _samples()
+    ref = _batch(ms, us)
+    opts = dict(OPTS, solver_lpr=lpr)
+    b = fg.Context(ms, cases.regions(alpha=0.1), **opts)
+    b.set_state(np.concatenate(us))
+    b.batch_compute_all(None, energies=False)
+    for k in range(2):
+        s1, _ = ref.batch_step(1e-14, 1.0, H, [0.4 + k, 1.2, 2.3])
+        s2, reps = b.batch_step(1e-14, 1.0, H, [0.4 + k, 1.2, 2.3])
+        assert s1 == fg.FG_OK and s2 == fg.FG_OK
+        assert _rel(b.get_state(1)["v"], ref.get_state(1)["v"]) < 1e-7
+        assert b.solver_lanes_per_row() == lpr
+        ref.batch_compute_all(None, energies=False)
+        b.batch_compute_all(None, energies=False)
+
