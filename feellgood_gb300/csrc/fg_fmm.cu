@@ -339,11 +339,88 @@ template <typename T> struct Vec4;
 template <> struct Vec4<float> { using type = float4; };
 template <> struct Vec4<double> { using type = double4; };
 
-// L2P + P2P: one warp per leaf. Sources of the adjacent leaves are spread over the lanes
-// (x, y, z, q in one vector load; each lane takes two sources per pass and already loads
-// the next two), up to NT targets of the leaf are held in registers; coordinates are
-// leaf-local (leaf units), so FP32 keeps the relative precision of close pairs. The
-// per-lane sums are reduced over the warp in FP64 in a fixed order.
+// One pass of the near field and L2P over up to NT targets tb.. of a leaf (nt of them real,
+// the rest padding): one warp; sources of the adjacent leaves spread over the lanes (x, y,
+// z, q in one vector load; each lane takes two sources per step and already loads the next
+// two); targets in registers; coordinates leaf-local (leaf units), so FP32 keeps the
+// relative precision of close pairs. The per-lane sums are reduced over the warp in a
+// fixed order, lane j then evaluates the local expansion at target j.
+template <typename T, int NT>
+__device__ __forceinline__ void l2p_p2p_pass(int leaf, int tb, int nt, int lane, int li, int lj, int lk,
+                                             const int *__restrict__ leaf_src, const int *__restrict__ tgt_node,
+                                             const T *__restrict__ tloc, const T *__restrict__ sloc,
+                                             const int *__restrict__ leaf_ijk, const double *__restrict__ leaf_scale,
+                                             const int *__restrict__ near_ptr, const int *__restrict__ near_leaf,
+                                             const T *__restrict__ Fl, double *__restrict__ pot) {
+    using V4 = typename Vec4<T>::type;
+    const V4 *__restrict__ src4 = reinterpret_cast<const V4 *>(sloc);
+    T tx[NT], ty[NT], tz[NT], ns[NT];
+#pragma unroll
+    for (int j = 0; j < NT; j++) {
+        const int ti = tb + (j < nt ? j : 0);
+        tx[j] = tloc[4 * (size_t)ti];
+        ty[j] = tloc[4 * (size_t)ti + 1];
+        tz[j] = tloc[4 * (size_t)ti + 2];
+        ns[j] = 0;
+    }
+    for (int e = near_ptr[leaf]; e < near_ptr[leaf + 1]; e++) {
+        const int nl = near_leaf[e];
+        // source coordinates relative to this leaf: own leaf-local + integer leaf offset
+        const T ox = T(leaf_ijk[3 * nl] - li), oy = T(leaf_ijk[3 * nl + 1] - lj), oz = T(leaf_ijk[3 * nl + 2] - lk);
+        const int s0 = leaf_src[nl], s1 = leaf_src[nl + 1];
+        T acc[NT];
+#pragma unroll
+        for (int j = 0; j < NT; j++) acc[j] = 0;
+        // a missing source is a zero charge far away
+        V4 far;
+        far.x = far.y = far.z = T(1e4);
+        far.w = T(0);
+        int s = s0 + lane;
+        V4 na = s < s1 ? src4[s] : far, nb = s + 32 < s1 ? src4[s + 32] : far;
+        for (; s < s1; s += 64) {
+            const V4 sa = na, sb = nb;
+            na = s + 64 < s1 ? src4[s + 64] : far;
+            nb = s + 96 < s1 ? src4[s + 96] : far;
+            const T ax = sa.x + ox, ay = sa.y + oy, az = sa.z + oz, aq = sa.w;
+            const T bx = sb.x + ox, by = sb.y + oy, bz = sb.z + oz, bq = sb.w;
+#pragma unroll
+            for (int j = 0; j < NT; j++) {
+                const T dx = tx[j] - ax, dy = ty[j] - ay, dz = tz[j] - az;
+                const T ex = tx[j] - bx, ey = ty[j] - by, ez = tz[j] - bz;
+                acc[j] += aq * rsqrt_p<T>(dx * dx + dy * dy + dz * dz);
+                acc[j] += bq * rsqrt_p<T>(ex * ex + ey * ey + ez * ez);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NT; j++) ns[j] += acc[j];
+    }
+    // warp sums in the path's precision (fixed butterfly order), then FP64
+    double near[NT];
+#pragma unroll
+    for (int j = 0; j < NT; j++) {
+        T v = ns[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        near[j] = double(v);
+    }
+    if (lane < nt) {
+        T x = 0, y = 0, z = 0;
+        double nr = 0;
+#pragma unroll
+        for (int j = 0; j < NT; j++)
+            if (j == lane) { x = tx[j]; y = ty[j]; z = tz[j]; nr = near[j]; }
+        T far = 0;
+        ups_cols<T>(x, y, z, [&](int n, int m, T re, T im) {
+            if (m == 0) far += Fl[ridx(n, 0, 0)] * re;
+            else far += T(2) * (Fl[ridx(n, m, 0)] * re + Fl[ridx(n, m, 1)] * im);
+        });
+        pot[tgt_node[tb + lane]] = (double(far) + nr) * leaf_scale[leaf];
+    }
+}
+
+// L2P + P2P: one warp per target leaf, its targets in passes of 16 and a tail pass of 8
+// or 4 (a leaf of the film holds 18 to 64 nodes: fixed passes of 16 would spend about a
+// fifth of the pair work on padding).
 template <typename T>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_l2p_p2p(int nleaf, const int *__restrict__ leaf_src,
                                                  const int *__restrict__ leaf_tgt, const int *__restrict__ tgt_node,
@@ -352,9 +429,6 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_l2p_p2p(int nle
                                                  const double *__restrict__ leaf_scale,
                                                  const int *__restrict__ near_ptr, const int *__restrict__ near_leaf,
                                                  const T *__restrict__ F, double *__restrict__ pot) {
-    constexpr int NT = 16;  // targets per pass
-    using V4 = typename Vec4<T>::type;
-    const V4 *__restrict__ src4 = reinterpret_cast<const V4 *>(sloc);
     const int lane = threadIdx.x & 31;
     const int leaf = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (leaf >= nleaf) return;
@@ -362,71 +436,20 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_l2p_p2p(int nle
     if (t0 == t1) return;
     const int li = leaf_ijk[3 * leaf], lj = leaf_ijk[3 * leaf + 1], lk = leaf_ijk[3 * leaf + 2];
     const T *Fl = F + (size_t)(leaf0 + leaf) * NR;
-    for (int tb = t0; tb < t1; tb += NT) {
-        const int nt = min(NT, t1 - tb);
-        T tx[NT], ty[NT], tz[NT], ns[NT];
-#pragma unroll
-        for (int j = 0; j < NT; j++) {
-            const int ti = tb + (j < nt ? j : 0);
-            tx[j] = tloc[4 * (size_t)ti];
-            ty[j] = tloc[4 * (size_t)ti + 1];
-            tz[j] = tloc[4 * (size_t)ti + 2];
-            ns[j] = 0;
-        }
-        for (int e = near_ptr[leaf]; e < near_ptr[leaf + 1]; e++) {
-            const int nl = near_leaf[e];
-            // source coordinates relative to this leaf: own leaf-local + integer leaf offset
-            const T ox = T(leaf_ijk[3 * nl] - li), oy = T(leaf_ijk[3 * nl + 1] - lj), oz = T(leaf_ijk[3 * nl + 2] - lk);
-            const int s0 = leaf_src[nl], s1 = leaf_src[nl + 1];
-            T acc[NT];
-#pragma unroll
-            for (int j = 0; j < NT; j++) acc[j] = 0;
-            // two sources per lane and pass, the next two already in flight; a missing source
-            // is a zero charge far away
-            V4 far;
-            far.x = far.y = far.z = T(1e4);
-            far.w = T(0);
-            int s = s0 + lane;
-            V4 na = s < s1 ? src4[s] : far, nb = s + 32 < s1 ? src4[s + 32] : far;
-            for (; s < s1; s += 64) {
-                const V4 sa = na, sb = nb;
-                na = s + 64 < s1 ? src4[s + 64] : far;
-                nb = s + 96 < s1 ? src4[s + 96] : far;
-                const T ax = sa.x + ox, ay = sa.y + oy, az = sa.z + oz, aq = sa.w;
-                const T bx = sb.x + ox, by = sb.y + oy, bz = sb.z + oz, bq = sb.w;
-#pragma unroll
-                for (int j = 0; j < NT; j++) {
-                    const T dx = tx[j] - ax, dy = ty[j] - ay, dz = tz[j] - az;
-                    const T ex = tx[j] - bx, ey = ty[j] - by, ez = tz[j] - bz;
-                    acc[j] += aq * rsqrt_p<T>(dx * dx + dy * dy + dz * dz);
-                    acc[j] += bq * rsqrt_p<T>(ex * ex + ey * ey + ez * ez);
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < NT; j++) ns[j] += acc[j];
-        }
-        // warp sums in the path's precision (fixed butterfly order), then FP64
-        double near[NT];
-#pragma unroll
-        for (int j = 0; j < NT; j++) {
-            T v = ns[j];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            near[j] = double(v);
-        }
-        // L2P: lane j evaluates target j
-        if (lane < nt) {
-            T x = 0, y = 0, z = 0;
-            double nr = 0;
-#pragma unroll
-            for (int j = 0; j < NT; j++)
-                if (j == lane) { x = tx[j]; y = ty[j]; z = tz[j]; nr = near[j]; }
-            T far = 0;
-            ups_cols<T>(x, y, z, [&](int n, int m, T re, T im) {
-                if (m == 0) far += Fl[ridx(n, 0, 0)] * re;
-                else far += T(2) * (Fl[ridx(n, m, 0)] * re + Fl[ridx(n, m, 1)] * im);
-            });
-            pot[tgt_node[tb + lane]] = (double(far) + nr) * leaf_scale[leaf];
+    for (int tb = t0; tb < t1;) {
+        const int r = t1 - tb;
+        if (r > 8) {
+            l2p_p2p_pass<T, 16>(leaf, tb, min(16, r), lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk,
+                                leaf_scale, near_ptr, near_leaf, Fl, pot);
+            tb += 16;
+        } else if (r > 4) {
+            l2p_p2p_pass<T, 8>(leaf, tb, r, lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk, leaf_scale,
+                               near_ptr, near_leaf, Fl, pot);
+            tb += 8;
+        } else {
+            l2p_p2p_pass<T, 4>(leaf, tb, r, lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk, leaf_scale,
+                               near_ptr, near_leaf, Fl, pot);
+            tb += 4;
         }
     }
 }
