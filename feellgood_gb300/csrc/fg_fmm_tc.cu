@@ -260,7 +260,14 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
         // complete (cp.async.wait_group) when it arrives for that item, LAG items later.
         // The source cell of this thread's output cell is read once per code.
         bool live = true;
-        int sc = -1;
+        // source cell of this thread's output cell for the current code; the next code's is
+        // loaded one code ahead so that its latency is hidden behind the current code's items
+        const int mycell = c_begin + (tid >> 1);
+        auto src_of = [&](int ci) {
+            return (ci < ncodes && mycell < n_out) ? __ldg(tab + (size_t)(out0 + mycell) * ncode + tile_code[q0 + ci])
+                                                   : -1;
+        };
+        int sc = src_of(0), sc_next = src_of(1);
         for (int it = 0; it < nitems + LAG; it++) {
             if (it < nitems && live) {
                 const int s = it % NSTAGE;
@@ -268,9 +275,9 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
                 if (live) {
                     const int ci = it / IPC, q = it % IPC;
                     const int code = tile_code[q0 + ci];
-                    if (q == 0) {
-                        const int cell = c_begin + (tid >> 1);
-                        sc = cell < n_out ? __ldg(tab + (size_t)(out0 + cell) * ncode + code) : -1;
+                    if (q == 0 && ci > 0) {
+                        sc = sc_next;
+                        sc_next = src_of(ci + 1);
                     }
                     unsigned char *st = sm + s * STAGE_BYTES;
                     if (tid == 0) {
