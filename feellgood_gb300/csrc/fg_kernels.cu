@@ -694,7 +694,7 @@ __global__ void k_phi_final(int nt, const int *__restrict__ tnode, const int *__
 // Energies of the NEXT state and <m> (Fem::energy, src/energy.cpp:5-68; mesh::avg,
 // src/mesh.cpp:89-106). partial layout: [7][G]: E_ex, E_aniso, E_demag, E_zeeman, <m>*V.
 
-template <int NPI, int NPF>
+template <int NPI, int NPF, bool ISO>
 __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__restrict__ tet,
                                                 const double *__restrict__ da, const double *__restrict__ detJ,
                                                 const int *__restrict__ treg, const DevRegion *__restrict__ regs,
@@ -744,6 +744,34 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
                             dU[2][1] * dU[2][1] + dU[2][2] * dU[2][2];
         const double div = dU[0][0] + dU[1][1] + dU[2][2];
         const double J = detJ[k];
+        if constexpr (ISO) {
+            // no anisotropy: every Gauss-point sum is a fixed combination of nodal values,
+            // sum_g w_g a_i(g) = J sum_g pds_g a_i(g) (the same sums, reassociated)
+            double aw[4], vol = 0.0;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                double c = 0.0;
+#pragma unroll
+                for (int g = 0; g < NPI; g++) c += c_tpds[g] * c_ta[i][g];
+                aw[i] = J * c;
+            }
+#pragma unroll
+            for (int g = 0; g < NPI; g++) vol += J * c_tpds[g];
+            double su[3] = {0, 0, 0}, sp = 0.0;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+#pragma unroll
+                for (int c = 0; c < 3; c++) su[c] += aw[i] * un[i][c];
+                sp += aw[i] * ph[i];
+            }
+            acc[0] += R.A * vol * dens;
+            acc[2] += -0.5 * FG_MU0 * R.Ms * div * sp;
+            acc[3] += -FG_MU0 * R.Ms * (su[0] * Hx + su[1] * Hy + su[2] * Hz);
+            acc[4] += su[0];
+            acc[5] += su[1];
+            acc[6] += su[2];
+            continue;
+        }
         double ex = 0.0, dm = 0.0, an = 0.0, ze = 0.0, cub = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
 #pragma unroll
         for (int g = 0; g < NPI; g++) {
@@ -979,11 +1007,13 @@ cudaError_t launch_phi_final(Ctx &c, double *phi_out) {
 cudaError_t launch_energy(Ctx &c, const double H[3]) {
     const int G = c.epart_blocks;
     if (c.npi_t == 5)
-        k_energy<5, 4><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
+        (c.aniso ? k_energy<5, 4, false> : k_energy<5, 4, true>)<<<G, 256, 0, c.stream>>>(
+            c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
                                                  c.u[1], c.phi[1], H[0], H[1], H[2], c.epart, nullptr, nullptr,
                                                  nullptr);
     else
-        k_energy<1, 1><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
+        (c.aniso ? k_energy<1, 1, false> : k_energy<1, 1, true>)<<<G, 256, 0, c.stream>>>(
+            c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
                                                  c.u[1], c.phi[1], H[0], H[1], H[2], c.epart, nullptr, nullptr,
                                                  nullptr);
     return cudaGetLastError();
@@ -994,11 +1024,13 @@ cudaError_t launch_energy(Ctx &c, const double H[3]) {
 cudaError_t launch_energy_into(Ctx &c, const double H[3], double *partial) {
     const int G = c.epart_blocks;
     if (c.npi_t == 5)
-        k_energy<5, 4><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
+        (c.aniso ? k_energy<5, 4, false> : k_energy<5, 4, true>)<<<G, 256, 0, c.stream>>>(
+            c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
                                                  c.u[1], c.phi[1], H[0], H[1], H[2], partial, nullptr, nullptr,
                                                  nullptr);
     else
-        k_energy<1, 1><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
+        (c.aniso ? k_energy<1, 1, false> : k_energy<1, 1, true>)<<<G, 256, 0, c.stream>>>(
+            c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
                                                  c.u[1], c.phi[1], H[0], H[1], H[2], partial, nullptr, nullptr,
                                                  nullptr);
     return cudaGetLastError();
@@ -1009,11 +1041,13 @@ cudaError_t launch_energy_seg(Ctx &c) {
     const int G = c.eblk_n;
     const double H0[3] = {0, 0, 0};
     if (c.npi_t == 5)
-        k_energy<5, 4><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
+        (c.aniso ? k_energy<5, 4, false> : k_energy<5, 4, true>)<<<G, 256, 0, c.stream>>>(
+            c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
                                                  c.u[1], c.phi[1], H0[0], H0[1], H0[2], c.seg_epart, c.eblk_rng,
                                                  c.eblk_seg, c.seg_H);
     else
-        k_energy<1, 1><<<G, 256, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
+        (c.aniso ? k_energy<1, 1, false> : k_energy<1, 1, true>)<<<G, 256, 0, c.stream>>>(
+            c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
                                                  c.u[1], c.phi[1], H0[0], H0[1], H0[2], c.seg_epart, c.eblk_rng,
                                                  c.eblk_seg, c.seg_H);
     k_seg_energy_sum<<<c.nseg, 32, 0, c.stream>>>(G, c.d_seg_eblk, c.seg_epart, c.seg_energy);
