@@ -115,6 +115,7 @@ SIGNATURES = {
                                     C.c_void_p]),
     "fg_mlp_nparam": (C.c_int, []),
     "fg_solver_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "fg_debug_wait_timeout": (C.c_int, [C.c_void_p, C.c_int]),
     "fg_debug_translate_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_int]),
     "fg_batch_create": (C.c_int, [C.POINTER(fg_mesh), C.c_int, C.POINTER(fg_region), C.c_int,
@@ -378,6 +379,10 @@ class Context:
         if s == FG_ETIMEDOUT or s > FG_ETIMEDOUT:
             self._check(s)
         return s, [{k: getattr(r, k) for k, _ in fg_batch_report._fields_} for r in reps]
+
+    def debug_wait_timeout(self, which):
+        """fg_debug_wait_timeout: the status a deliberately unended bounded device wait reports."""
+        return self.L.fg_debug_wait_timeout(self.h, which)
 
     def solver_lanes_per_row(self):
         v = C.c_int()

@@ -888,6 +888,30 @@ int fg_mlp_debug_grad(fg_ctx *h, int nsamples, const float *feat, const float *t
 
 int fg_mlp_nparam(void) { return mlp_nparam(); }
 
+int fg_debug_wait_timeout(fg_ctx *h, int which) {
+    if (!h || which < 0 || which > 1) return FG_EINVAL;
+    Ctx &c = h->c;
+    int *flag = nullptr;
+    CK(cudaMalloc(&flag, sizeof(int)));
+    int hv = 0;
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), c.stream);
+    if (e == cudaSuccess)
+        e = which == 0 ? launch_barrier_timeout_probe(c, flag) : launch_mbar_timeout_probe(c.stream, flag);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hv, flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    cudaFree(flag);
+    cudaMemsetAsync(c.bar, 0, sizeof(GridBar), c.stream);  // the context's barrier is reusable
+    if (e != cudaSuccess) {
+        c.err = std::string("fg_debug_wait_timeout: ") + cudaGetErrorString(e);
+        return FG_ECUDA;
+    }
+    if (hv) {
+        c.err = which == 0 ? "grid barrier: bounded wait expired" : "mbarrier: bounded wait expired";
+        return FG_ETIMEDOUT;
+    }
+    return FG_OK;
+}
+
 int fg_solver_info(const fg_ctx *h, int *lanes_per_row) {
     if (!h || !lanes_per_row) return FG_EINVAL;
     *lanes_per_row = h->c.lpr;

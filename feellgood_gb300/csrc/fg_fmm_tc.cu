@@ -417,7 +417,26 @@ __global__ void __launch_bounds__(256) k_tc_combine(TcArgs a) {
     }
 }
 
+// Failure-path probe: an mbarrier on which nothing ever arrives. The bounded wait must
+// expire (about 1 s), record FG_ETIMEDOUT in *err and return.
+__global__ void k_mbar_timeout_probe(int *err) {
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ volatile int bail;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        bail = 0;
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_wait(&bar, 0, err, &bail);
+}
+
 }  // namespace
+
+cudaError_t launch_mbar_timeout_probe(cudaStream_t st, int *err) {
+    k_mbar_timeout_probe<<<1, 32, 0, st>>>(err);
+    return cudaGetLastError();
+}
 
 int translate_tc_smem() { return NSTAGE * STAGE_BYTES + 1024; }
 int translate_tc_tile() { return NC; }

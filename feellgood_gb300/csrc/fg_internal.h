@@ -254,6 +254,9 @@ int mixed_max_blocks(Ctx &c);
 // Chooses the lanes per row of the mixed solver (opts.solver_lpr, or the fastest of 1, 4, 8
 // timed on the current step's system); the node kernel is rerun before each timing.
 cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle);
+// failure-path probes: a bounded device wait that nothing ends (*out / *err set on expiry)
+cudaError_t launch_barrier_timeout_probe(Ctx &c, int *out);
+cudaError_t launch_mbar_timeout_probe(cudaStream_t st, int *err);
 int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p);
 int *fmm_error_flag(const Ctx &c);
 int fmm_launches_per_eval(const Ctx &c);  // kernels one FMM evaluation launches  // device int: FG_ETIMEDOUT after an expired wait (or nullptr)

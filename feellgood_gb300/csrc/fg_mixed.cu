@@ -482,6 +482,29 @@ cudaError_t launch_mixed(Ctx &c, double dt, double prefactor) {
     return cudaLaunchKernelEx(&cfg, k_mixed<1>, a);
 }
 
+// Failure-path probe: block 0 leaves without arriving at the grid barrier, so block 1's
+// bounded wait must expire (about 2 s), set the barrier's error and return false.
+__global__ void k_barrier_timeout_probe(GridBar *bar, int *out) {
+    if (blockIdx.x == 0) return;
+    const bool ok = grid_sync(bar);
+    if (threadIdx.x == 0 && !ok) atomicExch(out, 1);
+}
+
+cudaError_t launch_barrier_timeout_probe(Ctx &c, int *out) {
+    cudaError_t e = cudaMemsetAsync(c.bar, 0, sizeof(GridBar), c.stream);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2);
+    cfg.blockDim = dim3(32);
+    cfg.stream = c.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_barrier_timeout_probe, c.bar, out);
+}
+
 cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle) {
     if (c.lpr > 0) return cudaSuccess;
     if (c.opts.solver_lpr == 1 || c.opts.solver_lpr == 4 || c.opts.solver_lpr == 8) {

@@ -173,6 +173,12 @@ int fg_timings(const fg_ctx *ctx, double ms[5]);
  * [2] M2L (cell, cell) pairs, [3] P2P (target, source) pairs per evaluation. */
 int fg_counters(const fg_ctx *ctx, long long out[4]);
 
+/* Failure-path check (no reference counterpart): runs a device wait that nothing ends —
+ * which 0: the persistent solvers' grid barrier with one block that never arrives (about
+ * 2 s); 1: an mbarrier wait of the tensor-core pipeline with no arrival (about 1 s) — and
+ * returns FG_ETIMEDOUT when the bounded wait expired as designed. The context stays usable. */
+int fg_debug_wait_timeout(fg_ctx *ctx, int which);
+
 /* Lanes per row the FP32 + refinement solver uses (1, 4 or 8; 0 before the first step when
  * it is chosen by timing). */
 int fg_solver_info(const fg_ctx *ctx, int *lanes_per_row);
