@@ -9,7 +9,7 @@
 // v_e = 2 v_prev - v_prev2 (in units of the RMS of that correction over the last solve),
 // so the candidate is v_e + scale * MLP(features), projected on the new tangent basis and
 // divided by gamma0. The reference's guess (previous v on the new basis,
-// src/linear_algebra.cpp:13-24) is the fallback and the judge: the candidate is used only
+// src/linear_algebra.cpp:13-24) is the fallback and the referee: the candidate is used only
 // when its FP64 initial residual |b - K x| is smaller than the fallback's. The network is
 // trained online on (features, solved v) pairs with hand-written kernels: BF16 weights
 // (FP32 master copy, Adam), FP32 accumulation, deterministic fixed-order reductions.
