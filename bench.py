@@ -327,7 +327,7 @@ def main():
     clocks = clk.stop()
     fmm_stage = ctx.fmm_timings()
     cnt = ctx.counters()
-    lanes_per_row = ctx.solver_lanes_per_row()
+    lanes_per_row, solver_blocks = ctx.solver_lanes_per_row(), ctx.solver_blocks()
     launches = (cnt[0] - launches0) // args.steps
     value, dev_s = replicas_value(dist, world, args.steps, float(ms[:, 4].sum()) / 1e3)
     iters = [r["iters"] for r in reps]
@@ -429,7 +429,7 @@ def main():
             "speedup_vs_plain_fp64": (value / world) / plain_value if plain_value else None,
             "prev_guess_fp32_refine_steps_per_s": prev_value,
             "iters_per_step": float(np.mean(iters)), "refinements_per_step": float(np.mean(refs)),
-            "solver_lanes_per_row": lanes_per_row,
+            "solver_lanes_per_row": lanes_per_row, "solver_blocks": solver_blocks,
             "prev_guess_iters_per_step": prev_iters, "plain_iters_per_step": plain_iters,
             "plain_fp64_detail": plain_detail,
             "learned_guess": {"accepted_frac": float(np.mean(acc)),

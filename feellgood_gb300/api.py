@@ -114,7 +114,7 @@ SIGNATURES = {
     "fg_mlp_debug_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p]),
     "fg_mlp_nparam": (C.c_int, []),
-    "fg_solver_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "fg_solver_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "fg_debug_wait_timeout": (C.c_int, [C.c_void_p, C.c_int]),
     "fg_debug_translate_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_int]),
@@ -386,7 +386,12 @@ class Context:
 
     def solver_lanes_per_row(self):
         v = C.c_int()
-        self._check(self.L.fg_solver_info(self.h, C.byref(v)))
+        self._check(self.L.fg_solver_info(self.h, C.byref(v), None))
+        return v.value
+
+    def solver_blocks(self):
+        v = C.c_int()
+        self._check(self.L.fg_solver_info(self.h, None, C.byref(v)))
         return v.value
 
     def batch_run_info(self):

@@ -912,9 +912,10 @@ int fg_debug_wait_timeout(fg_ctx *h, int which) {
     return FG_OK;
 }
 
-int fg_solver_info(const fg_ctx *h, int *lanes_per_row) {
-    if (!h || !lanes_per_row) return FG_EINVAL;
-    *lanes_per_row = h->c.lpr;
+int fg_solver_info(const fg_ctx *h, int *lanes_per_row, int *blocks) {
+    if (!h) return FG_EINVAL;
+    if (lanes_per_row) *lanes_per_row = h->c.lpr;
+    if (blocks) *blocks = h->c.batch ? h->c.seg_grid : h->c.mixed_grid;
     return FG_OK;
 }
 

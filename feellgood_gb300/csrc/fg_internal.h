@@ -252,7 +252,8 @@ int bicg_grid_size(Ctx &c, bool mixed);
 int mixed_grid_size(Ctx &c);
 int mixed_max_blocks(Ctx &c);
 // Chooses the lanes per row of the mixed solver (opts.solver_lpr, or the fastest of 1, 4, 8
-// timed on the current step's system); the node kernel is rerun before each timing.
+// timed on the current step's system) and, for a single system, its grid size (all
+// co-resident blocks, 2 or 1 per SM); the node kernel is rerun before each timing.
 cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle);
 // failure-path probes: a bounded device wait that nothing ends (*out / *err set on expiry)
 cudaError_t launch_barrier_timeout_probe(Ctx &c, int *out);

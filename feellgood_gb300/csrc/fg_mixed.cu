@@ -526,10 +526,19 @@ cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle) {
     if ((e = cudaMemcpyAsync(keep_v, c.v[1], n3, cudaMemcpyDeviceToDevice, c.stream)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(keep_u, c.u[1], n3, cudaMemcpyDeviceToDevice, c.stream)) != cudaSuccess) return e;
     double best = 1e300;
-    int bestv = 1;
+    int bestv = 1, bestg = c.mixed_grid;
     std::vector<SolveResult> res(c.batch ? c.nseg : 1);
-    for (int v : cand) {
+    // grid sizes of the single-system solver: all co-resident blocks, or 2 or 1 per SM (fewer
+    // blocks make each grid barrier cheaper; a batch keeps its per-sample block ranges)
+    std::vector<int> grids{c.mixed_grid};
+    if (!c.batch)
+        for (int g : {2 * c.nsm, c.nsm})
+            if (g < c.mixed_grid) grids.push_back(g);
+    const int gmax = c.mixed_grid;
+    for (int vi = 0; vi < 3 * (int)grids.size(); vi++) {
+        const int v = cand[vi % 3];
         c.lpr = v;
+        c.mixed_grid = grids[vi / 3];
         for (int rep = 0; rep < 2; rep++) {  // the first run of each variant warms it up
             if ((e = launch_node(c, angle)) != cudaSuccess) break;
             cudaEventRecord(e0, c.stream);
@@ -544,6 +553,7 @@ cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle) {
             if (rep == 1 && !res[0].timeout && ms / it < best) {
                 best = ms / it;
                 bestv = v;
+                bestg = c.mixed_grid;
             }
         }
         if (e != cudaSuccess) break;
@@ -555,7 +565,8 @@ cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle) {
     cudaMemcpyAsync(c.u[1], keep_u, n3, cudaMemcpyDeviceToDevice, c.stream);
     c.acc_active = acc;
     c.lpr = bestv;
-    if (c.opts.verbose) fprintf(stderr, "mixed solver: %d lane(s) per row\n", bestv);
+    c.mixed_grid = e == cudaSuccess ? bestg : gmax;
+    if (c.opts.verbose) fprintf(stderr, "mixed solver: %d lane(s) per row, %d blocks\n", bestv, c.mixed_grid);
     return e;
 }
 

@@ -180,8 +180,8 @@ int fg_counters(const fg_ctx *ctx, long long out[4]);
 int fg_debug_wait_timeout(fg_ctx *ctx, int which);
 
 /* Lanes per row the FP32 + refinement solver uses (1, 4 or 8; 0 before the first step when
- * it is chosen by timing). */
-int fg_solver_info(const fg_ctx *ctx, int *lanes_per_row);
+ * it is chosen by timing) and its number of blocks (either may be NULL). */
+int fg_solver_info(const fg_ctx *ctx, int *lanes_per_row, int *blocks);
 
 /* Learned guess: training steps done and the last minibatch MSE (scaled units). */
 int fg_mlp_info(const fg_ctx *ctx, long long *train_steps, double *last_loss);
