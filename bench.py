@@ -15,6 +15,8 @@ afterwards. Synthetic data; no files are read.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
   python bench.py --workload batch64     # 64 independent cubes, batched (its own line)
+  python bench.py --workload wire        # nanowire domain wall, learned guess (its own line)
+  python bench.py --workload platelet    # 3.84M-tet vortex platelet, learned guess at scale
 
 One JSON line on stdout (rank 0). For N > 1 every rank runs an independent replica on its
 own GPU (the path does not shard); value is the sum over ranks of steps/s (max-over-ranks
@@ -260,7 +262,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="film", choices=["film", "batch64"])
+    ap.add_argument("--workload", default="film", choices=["film", "batch64", "wire", "platelet"])
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--train-steps", type=int, default=40, help="untimed solves that train the learned guess")
     ap.add_argument("--train-every", type=int, default=4,
@@ -285,6 +287,9 @@ def main():
         return
     if args.workload == "batch64":
         bench_batch(args)
+        return
+    if args.workload in ("wire", "platelet"):
+        bench_learned_workload(args)
         return
     if args.drift > 0:
         drift_study(args)
@@ -495,6 +500,100 @@ def drift_study(args):
             "device_s": {"mixed": ta / 1e3, "plain": tb / 1e3}, "iters_per_step": {"mixed": ia, "plain": ib},
             "config": {"workload": "film 400x400x10 nm, 2 nm grid, 1.2M tets, alpha 0.02, dt 5e-14, tol 1e-6, "
                                    "zero field, seeded smoothed random initial m"}}
+    print(json.dumps(line), flush=True)
+
+
+def wire_workload(fg, seed=SEED):
+    """Nanowire 40 x 40 x 1000 nm on a 2.5 nm grid (16 x 16 x 400 cells x 6 = 614,400 tets),
+    head-to-head domain wall at z = 500 nm (m_z = tanh((500 - z) / 20 nm), transverse
+    component through the wall) with a seeded +-0.02 transverse perturbation; 5 mT along +z;
+    alpha 0.05."""
+    mesh = fg.cuboid(16, 16, 400, 40.0, 40.0, 1000.0, 1e-9, MS)
+    rng = np.random.default_rng(seed)
+    z = mesh["xyz"][:, 2] / 1e-9
+    mz = np.tanh((500.0 - z) / 20.0)
+    u = np.stack([np.sqrt(np.clip(1 - mz * mz, 0, 1)), np.zeros_like(mz), mz], axis=1)
+    u[:, :2] += rng.uniform(-0.02, 0.02, size=(len(z), 2))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    return mesh, u, np.array([0.0, 0.0, 0.005 / fg.MU0]), 0.05, 200
+
+
+def platelet_workload(fg, seed=SEED):
+    """Platelet 1000 x 1000 x 10 nm on a 2.5 nm grid (400 x 400 x 4 cells x 6 = 3,840,000 tets),
+    in-plane vortex m = (-y, x, 0) / r about the centre with m_z = 1 within r < 10 nm, seeded
+    Gaussian noise sigma 0.02; zero field; alpha 0.01."""
+    mesh = fg.cuboid(400, 400, 4, 1000.0, 1000.0, 10.0, 1e-9, MS)
+    rng = np.random.default_rng(seed)
+    xy = mesh["xyz"][:, :2] / 1e-9 - 500.0
+    r = np.hypot(xy[:, 0], xy[:, 1])
+    u = np.zeros((len(r), 3))
+    core = r < 10.0
+    u[~core, 0] = -xy[~core, 1] / r[~core]
+    u[~core, 1] = xy[~core, 0] / r[~core]
+    u[core, 2] = 1.0
+    u += rng.normal(0, 0.02, size=u.shape)
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    return mesh, u, np.zeros(3), 0.01, 300
+
+
+def bench_learned_workload(args):
+    """The learned guess where it is meant to be used: trained online on the first steps of the
+    run (200 for the wire, 300 for the platelet; not timed), then the timed steps, compared on
+    the same state and angles with the previous-step guess (same precision) and with the plain
+    FP64 path; for the platelet also max |dm| against the plain FP64 path after the timed steps."""
+    import __graft_entry__
+    __graft_entry__.build_product()
+    import feellgood_gb300 as fg
+    mesh, u0, H, alpha, ntrain = (wire_workload if args.workload == "wire" else platelet_workload)(fg)
+    regs = [dict(Ae=1e-11, Ms=795774.7, alpha=0.5), dict(Ae=AE, Ms=MS, alpha=alpha)]
+    fg.rng_seed(SEED)
+    angles = fg.rng_angle
+    ctx = fg.Context(mesh, regs, tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP32_REFINE, demag=fg.FG_DEMAG_FMM,
+                     learned_guess=1, mlp_train_steps=ntrain, mlp_train_every=args.train_every, profile=1)
+    ctx.set_state(u0)
+    ctx.compute_all(H)
+    run_steps(ctx, ntrain + args.warmup, H, DT, angles)
+    start = ctx.get_state(0)
+    ctx.fmm_timings()
+    step_angles = [angles() for _ in range(args.steps)]
+    clk = ClockSampler(0)
+    clk.start()
+    ms, reps = run_steps(ctx, args.steps, H, DT, step_angles)
+    clocks = clk.stop()
+    fmm_stage = ctx.fmm_timings()
+    cnt = ctx.counters()
+    learned = ctx.get_state(0)
+    ctx.close()
+    out = {"learned": (args.steps / (ms[:, 4].sum() / 1e3), float(np.mean([r["iters"] for r in reps])))}
+    acc = float(np.mean([r["guess_accepted"] for r in reps]))
+    r0 = float(np.median([r["res0"] / r["res0_fallback"] for r in reps if r["res0_fallback"] > 0]))
+    finals = {}
+    for name, opts, n in (("previous_step_guess", dict(precision=fg.FG_PREC_FP32_REFINE), args.steps),
+                          ("plain_fp64", dict(precision=fg.FG_PREC_FP64), args.steps)):
+        c = fg.Context(mesh, regs, tol=TOL, max_iter=MAXITER, demag=fg.FG_DEMAG_FMM, **opts)
+        c.set_state(start["u"], start["v"], start["phi"], start["phiv"])
+        pms, preps = run_steps(c, n, H, DT, step_angles)
+        out[name] = (n / (pms[:, 4].sum() / 1e3), float(np.mean([r["iters"] for r in preps])))
+        finals[name] = c.get_state(0)
+        c.close()
+    dm = np.linalg.norm(learned["u"] - finals["plain_fp64"]["u"], axis=1).max()
+    ntets = len(mesh["tets"])
+    line = {
+        "metric": f"LLG steps/s, {args.workload} ({ntets} tets), learned guess + FP32 body + FP64 refinement",
+        "value": out["learned"][0], "unit": "steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 / out["learned"][0], "higher_is_better": True, "dtype": "f32+f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": " ".join((wire_workload if args.workload == "wire" else platelet_workload).__doc__.split()),
+                   "train_solves_untimed": ntrain, "dt": DT, "tol": TOL},
+        "iters_per_step": {k: v[1] for k, v in out.items()},
+        "steps_per_s": {k: v[0] for k, v in out.items()},
+        "learned_guess": {"accepted_frac": acc, "res0_over_fallback_median": r0},
+        "speedup_vs_plain_fp64": out["learned"][0] / out["plain_fp64"][0],
+        "max_abs_dm_vs_plain_fp64_after_timed_steps": float(dm),
+        "fmm": {"L": int(cnt[1]), "m2l_pairs": float(cnt[2]), "p2p_pairs": float(cnt[3]),
+                "stage_ms": dict(zip(["p2m", "m2m", "m2l", "l2l", "l2p_p2p"], [float(x) for x in fmm_stage]))},
+        "clocks": clocks,
+    }
     print(json.dumps(line), flush=True)
 
 

@@ -16,7 +16,6 @@ namespace fg {
 void upload_rules(bool one_point);
 int fmm_build(Ctx &c);
 void fmm_free(Ctx &c);
-cudaError_t fmm_eval(Ctx &c);
 }  // namespace fg
 
 using namespace fg;
@@ -479,6 +478,12 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     CK(dalloc(&c.tri_slot, 3 * (size_t)c.nft));
     CK(dalloc(&c.pot, nn));
     CK(cudaMemset(c.pot, 0, sizeof(double) * nn));
+    if (!c.opts.first_order) {  // the demag of v is evaluated beside that of m
+        CK(dalloc(&c.src_q2, c.nsrc));
+        CK(dalloc(&c.tri_slot2, 3 * (size_t)c.nft));
+        CK(dalloc(&c.pot2, nn));
+        CK(cudaMemset(c.pot2, 0, sizeof(double) * nn));
+    }
     c.epart_blocks = std::max(1, std::min(4 * c.nsm, (nmt + 255) / 256));
     CK(dalloc(&c.epart, 7 * (size_t)c.epart_blocks));
     CK(cudaMallocHost((void **)&c.hepart, 7 * sizeof(double) * c.epart_blocks));
@@ -613,7 +618,7 @@ void fg_destroy(fg_ctx *h) {
                     c.Sval32, c.A, c.A32, c.tri, c.tri_c, c.tinc_ptr, c.tinc, c.src_xyz, c.mag_nodes, c.u[0], c.u[1],
                     c.v[0], c.v[1], c.phi[0], c.phi[1], c.phiv[0], c.phiv[1], c.ep, c.eq, c.ep32, c.eq32, c.Dl32,
                     c.slot, c.Dl, c.rhs, c.x, c.bv, c.W, c.fv, c.partial, c.bar, c.dres, c.src_q, c.tri_slot,
-                    c.pot, c.epart, c.src_dst};
+                    c.pot, c.epart, c.src_dst, c.src_q2, c.tri_slot2, c.pot2};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     fmm_free(c);
@@ -756,16 +761,30 @@ static int energy_impl(fg_ctx *h, const double Hext[3], double E[4], double avg[
     return FG_OK;
 }
 
+// Demag of m and of v (Fem::compute_all, src/fem.h): with the FMM one evaluation of both
+// charge sets (shared tree passes, one near-field pass), else one after the other.
+static int demag_pair(fg_ctx *h) {
+    Ctx &c = h->c;
+    if (c.opts.demag != FG_DEMAG_FMM || !c.src_q2) {
+        int s = demag_into(h, c.u[1], c.phi[1]);
+        if (s == FG_OK) s = demag_into(h, c.v[1], c.phiv[1]);
+        return s;
+    }
+    CK(launch_charges(c, c.u[1], 0));
+    CK(launch_charges(c, c.v[1], 1));
+    CK(fmm_eval(c, 2));
+    CK(launch_phi_final(c, c.phi[1], 0));
+    CK(launch_phi_final(c, c.phiv[1], 1));
+    c.launches += 4 + fmm_launches_per_eval(c, 2);
+    return FG_OK;
+}
+
 int fg_compute_all(fg_ctx *h, const double Hext[3], double energies[4]) {
     if (!h || !Hext) return FG_EINVAL;
     Ctx &c = h->c;
     CK(cudaEventRecord(c.ev[3], c.stream));
-    int s = demag_into(h, c.u[1], c.phi[1]);
+    int s = c.opts.first_order ? demag_into(h, c.u[1], c.phi[1]) : demag_pair(h);
     if (s) return s;
-    if (!c.opts.first_order) {
-        s = demag_into(h, c.v[1], c.phiv[1]);
-        if (s) return s;
-    }
     CK(cudaEventRecord(c.ev[4], c.stream));
     double E[4];
     s = energy_impl(h, Hext, E, nullptr);

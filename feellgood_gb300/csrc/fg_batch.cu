@@ -21,7 +21,6 @@
 
 namespace fg {
 
-cudaError_t fmm_eval(Ctx &c);
 
 #define BCK(call)                                                                     \
     do {                                                                              \
@@ -203,14 +202,21 @@ static void fill_par(SegPar &P, const fg_sample_step &s) {
     P.c0 = s.prefactor * FG_THETA * s.dt * FG_GAMMA0;
 }
 
-static int fmm_launch_count(const Ctx &c) { return fmm_launches_per_eval(c); }
 
-static cudaError_t batch_demag(Ctx &c, const double *m, double *phi) {
-    cudaError_t e = launch_charges(c, m);
-    if (e != cudaSuccess) return e;
-    e = fmm_eval(c);
-    if (e != cudaSuccess) return e;
-    return launch_phi_final(c, phi);
+// Demag of m (and of v beside it, one FMM evaluation of both charge sets).
+static cudaError_t batch_demag_all(Ctx &c) {
+    const int nq = c.opts.first_order ? 1 : 2;
+    cudaError_t e = launch_charges(c, c.u[1], 0);
+    if (e == cudaSuccess && nq == 2) e = launch_charges(c, c.v[1], 1);
+    if (e == cudaSuccess) e = fmm_eval(c, nq);
+    if (e == cudaSuccess) e = launch_phi_final(c, c.phi[1], 0);
+    if (e == cudaSuccess && nq == 2) e = launch_phi_final(c, c.phiv[1], 1);
+    return e;
+}
+
+static int demag_launches(const Ctx &c) {
+    const int nq = c.opts.first_order ? 1 : 2;
+    return 2 * nq + fmm_launches_per_eval(c, nq);
 }
 
 // Stream-ordered body of one step of a run (the graph is a capture of exactly this).
@@ -221,8 +227,7 @@ static cudaError_t run_body(Ctx &c) {
     if ((e = launch_tet(c, 1.0, H0)) != cudaSuccess) return e;
     if ((e = launch_node(c, 0.0)) != cudaSuccess) return e;
     if ((e = launch_mixed(c, 1.0, 1.0)) != cudaSuccess) return e;
-    if ((e = batch_demag(c, c.u[1], c.phi[1])) != cudaSuccess) return e;
-    if (!c.opts.first_order && (e = batch_demag(c, c.v[1], c.phiv[1])) != cudaSuccess) return e;
+    if ((e = batch_demag_all(c)) != cudaSuccess) return e;
     const size_t n3 = 3 * sizeof(double) * c.nn, n1 = sizeof(double) * c.nn;
     if ((e = cudaMemcpyAsync(c.u[0], c.u[1], n3, cudaMemcpyDeviceToDevice, c.stream)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(c.v[0], c.v[1], n3, cudaMemcpyDeviceToDevice, c.stream)) != cudaSuccess) return e;
@@ -233,7 +238,7 @@ static cudaError_t run_body(Ctx &c) {
 }
 
 static int body_launches(const Ctx &c) {
-    return 5 + (c.opts.first_order ? 1 : 2) * (2 + fmm_launch_count(c));
+    return 5 + demag_launches(c);
 }
 
 static void try_capture(Ctx &c) {
@@ -354,9 +359,8 @@ int fg_batch_compute_all(fg_ctx *h, const double *Hext, double *energies) {
     }
     const int ns = c.nseg;
     CK(cudaEventRecord(c.ev[3], c.stream));
-    CK(batch_demag(c, c.u[1], c.phi[1]));
-    if (!c.opts.first_order) CK(batch_demag(c, c.v[1], c.phiv[1]));
-    c.launches += (c.opts.first_order ? 1 : 2) * (2 + fmm_launch_count(c));
+    CK(batch_demag_all(c));
+    c.launches += demag_launches(c);
     CK(cudaEventRecord(c.ev[4], c.stream));
     if (energies) {
         for (int k = 0; k < 3 * ns; k++) c.hseg_H[k] = Hext ? Hext[k] : 0.0;

@@ -53,7 +53,7 @@ __host__ __device__ constexpr int cidx(int n, int m) { return n * (n + 1) / 2 + 
 __host__ __device__ constexpr int ridx(int n, int m, int part) { return m == 0 ? n * n : n * n + 2 * m - 1 + part; }
 
 struct FmmTree {
-    int L = 0, nleaf = 0, ncell = 0, leaf0 = 0;
+    int L = 0, nleaf = 0, ncell = 0, leaf0 = 0, nsrc = 0;
     double s0 = 1, c0[3] = {0, 0, 0};
     std::vector<int> lev_begin;
     size_t n_m2l = 0, n_p2p_pairs = 0;
@@ -68,7 +68,7 @@ struct FmmTree {
     long long stage_n = 0;
     // device
     int *leaf_src = nullptr, *leaf_tgt = nullptr, *tgt_node = nullptr;
-    void *sloc = nullptr;  // 4 x nsrc: leaf-local source coordinates (T), w unused
+    void *sloc = nullptr;  // 4 x nsrc: leaf-local source coordinates (T), w: charge of set 0
     void *tloc = nullptr;  // 4 x ntgt: leaf-local target coordinates (T)
     // FP64 path, near field in double-single arithmetic: every coordinate split as
     // hi (on a 2^-20 grid of leaf units) + lo, the charge as hi + lo; (x, y, z, q) per part
@@ -95,6 +95,13 @@ struct FmmTree {
     float *Mh = nullptr, *Ml = nullptr, *Fh = nullptr, *Fl = nullptr;  // hi/lo splits of M and F
     unsigned char *img_m2l = nullptr, *img_m2m = nullptr, *img_l2l = nullptr;  // operator images
     int *dst_keep = nullptr;
+    // charge sets evaluated together (2: demag of m and of v in one pass): M, F, Mh, Ml, Fh,
+    // Fl and tc_scratch hold nq sets one after the other; the second set's charges for the
+    // near field are in sq2 (T) and, double-single, in ds_q2 (hi [nsrc] then lo [nsrc])
+    int nq = 1;
+    void *sq2 = nullptr;
+    float *ds_q2 = nullptr;
+    size_t nslot_floats = 0;  // floats of tc_scratch per set
 };
 
 // ---------------------------------------------------------------------------------
@@ -220,28 +227,40 @@ __device__ __forceinline__ void ups_cols(T x, T y, T z, Fn &&f) {
 
 // P2M: one warp per leaf; each lane forms q*conj(Ups) of every 32nd source of the leaf into
 // 100 register accumulators, which are then reduced over the warp in a fixed order (lane
-// k mod 32 stores coefficient k). The charge is also stored beside the source coordinates
-// for the near field, and with the tensor-core translations the hi/lo split of M.
+// k mod 32 stores coefficient k). The charge is also stored for the near field (beside the
+// source coordinates for the first set), and with the tensor-core translations the hi/lo
+// split of M. Grid y selects the charge set.
 template <typename T>
-__global__ void __launch_bounds__(128) k_p2m(int nleaf, const int *__restrict__ leaf_src, T *__restrict__ sloc,
-                                             const double *__restrict__ q, int leaf0, T *__restrict__ M,
-                                             float *__restrict__ Mh, float *__restrict__ Ml,
-                                             float4 *__restrict__ ds_hi, float4 *__restrict__ ds_lo) {
+struct P2mSet {
+    const double *q;        // charges (storage order)
+    T *M;                   // expansions of this set
+    float *Mh, *Ml;         // their split (tensor-core translations) or nullptr
+    T *qn;                  // charge for the near field, element s at qn[s * qn_stride]
+    int qn_stride;
+    float *qh, *ql;         // double-single charge for the FP64 near field (or nullptr)
+    int qd_stride;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_p2m(int nleaf, const int *__restrict__ leaf_src, const T *__restrict__ sloc,
+                                             int leaf0, P2mSet<T> set0, P2mSet<T> set1) {
+    const P2mSet<T> st = blockIdx.y ? set1 : set0;
     const int lane = threadIdx.x & 31;
     const int leaf = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (leaf >= nleaf) return;
     const int s0 = leaf_src[leaf], s1 = leaf_src[leaf + 1];
+    const double *__restrict__ q = st.q;
     T acc[NR];
 #pragma unroll
     for (int k = 0; k < NR; k++) acc[k] = 0;
     for (int s = s0 + lane; s < s1; s += 32) {
         const T x = sloc[4 * (size_t)s], y = sloc[4 * (size_t)s + 1], z = sloc[4 * (size_t)s + 2];
         const T qq = T(q[s]);
-        sloc[4 * (size_t)s + 3] = qq;  // charge beside the coordinates for the near field
-        if (ds_hi) {  // charge as hi + lo for the double-single near field
+        st.qn[(size_t)s * st.qn_stride] = qq;
+        if (st.qh) {  // charge as hi + lo for the double-single near field
             const float qh = (float)q[s];
-            ds_hi[s].w = qh;
-            ds_lo[s].w = (float)(q[s] - (double)qh);
+            st.qh[(size_t)s * st.qd_stride] = qh;
+            st.ql[(size_t)s * st.qd_stride] = (float)(q[s] - (double)qh);
         }
         ups_cols<T>(x, y, z, [&](int n, int m, T re, T im) {
             acc[ridx(n, m, 0)] += qq * re;
@@ -255,12 +274,12 @@ __global__ void __launch_bounds__(128) k_p2m(int nleaf, const int *__restrict__ 
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if ((k & 31) == lane) {
-            M[base + k] = v;
-            if (Mh) {  // split for the tensor-core translations: hi = tf32(x), lo = x - hi
+            st.M[base + k] = v;
+            if (st.Mh) {  // split for the tensor-core translations: hi = tf32(x), lo = x - hi
                 const float xf = (float)v;
                 const float hi = __uint_as_float((__float_as_uint(xf) + 0x1000u) & 0xFFFFE000u);
-                Mh[base + k] = hi;
-                Ml[base + k] = xf - hi;
+                st.Mh[base + k] = hi;
+                st.Ml[base + k] = xf - hi;
             }
         }
     }
@@ -339,116 +358,166 @@ template <typename T> struct Vec4;
 template <> struct Vec4<float> { using type = float4; };
 template <> struct Vec4<double> { using type = double4; };
 
+// Charge sets of one near-field launch: the first set's charge rides in the w of the source
+// coordinates, the second (demag of v beside that of m) in its own array; the local
+// expansions and potentials of each set.
+template <typename T>
+struct NearSets {
+    const T *q2;            // second set's charges (NQ = 2)
+    const T *F[2];          // local expansions per set
+    double *pot[2];         // potentials per set
+};
+
 // One pass of the near field and L2P over up to NT targets tb.. of a leaf (nt of them real,
-// the rest padding): one warp; sources of the adjacent leaves spread over the lanes (x, y,
-// z, q in one vector load; each lane takes two sources per step and already loads the next
-// two); targets in registers; coordinates leaf-local (leaf units), so FP32 keeps the
-// relative precision of close pairs. The per-lane sums are reduced over the warp in a
-// fixed order, lane j then evaluates the local expansion at target j.
-template <typename T, int NT>
+// the rest padding), for NQ charge sets at once (the pair geometry and the reciprocal
+// distance are shared; each set keeps its own sums in the same order as alone): one warp;
+// sources of the adjacent leaves spread over the lanes (x, y, z, q in one vector load; each
+// lane takes two sources per step and already loads the next two); targets in registers;
+// coordinates leaf-local (leaf units), so FP32 keeps the relative precision of close
+// pairs. The per-lane sums are reduced over the warp in a fixed order, lane j then
+// evaluates the local expansion(s) at target j.
+template <typename T, int NT, int NQ>
 __device__ __forceinline__ void l2p_p2p_pass(int leaf, int tb, int nt, int lane, int li, int lj, int lk,
                                              const int *__restrict__ leaf_src, const int *__restrict__ tgt_node,
                                              const T *__restrict__ tloc, const T *__restrict__ sloc,
                                              const int *__restrict__ leaf_ijk, const double *__restrict__ leaf_scale,
                                              const int *__restrict__ near_ptr, const int *__restrict__ near_leaf,
-                                             const T *__restrict__ Fl, double *__restrict__ pot) {
+                                             size_t fbase, const NearSets<T> &sets) {
     using V4 = typename Vec4<T>::type;
     const V4 *__restrict__ src4 = reinterpret_cast<const V4 *>(sloc);
-    T tx[NT], ty[NT], tz[NT], ns[NT];
+    const T *__restrict__ q2 = sets.q2;
+    T tx[NT], ty[NT], tz[NT], ns[NQ][NT];
 #pragma unroll
     for (int j = 0; j < NT; j++) {
         const int ti = tb + (j < nt ? j : 0);
         tx[j] = tloc[4 * (size_t)ti];
         ty[j] = tloc[4 * (size_t)ti + 1];
         tz[j] = tloc[4 * (size_t)ti + 2];
-        ns[j] = 0;
+#pragma unroll
+        for (int k = 0; k < NQ; k++) ns[k][j] = 0;
     }
     for (int e = near_ptr[leaf]; e < near_ptr[leaf + 1]; e++) {
         const int nl = near_leaf[e];
         // source coordinates relative to this leaf: own leaf-local + integer leaf offset
         const T ox = T(leaf_ijk[3 * nl] - li), oy = T(leaf_ijk[3 * nl + 1] - lj), oz = T(leaf_ijk[3 * nl + 2] - lk);
         const int s0 = leaf_src[nl], s1 = leaf_src[nl + 1];
-        T acc[NT];
+        T acc[NQ][NT];
 #pragma unroll
-        for (int j = 0; j < NT; j++) acc[j] = 0;
+        for (int j = 0; j < NT; j++)
+#pragma unroll
+            for (int k = 0; k < NQ; k++) acc[k][j] = 0;
         // a missing source is a zero charge far away
         V4 far;
         far.x = far.y = far.z = T(1e4);
         far.w = T(0);
         int s = s0 + lane;
         V4 na = s < s1 ? src4[s] : far, nb = s + 32 < s1 ? src4[s + 32] : far;
+        T na2 = 0, nb2 = 0;
+        if constexpr (NQ == 2) {
+            na2 = s < s1 ? q2[s] : T(0);
+            nb2 = s + 32 < s1 ? q2[s + 32] : T(0);
+        }
         for (; s < s1; s += 64) {
             const V4 sa = na, sb = nb;
+            const T aq2 = na2, bq2 = nb2;
             na = s + 64 < s1 ? src4[s + 64] : far;
             nb = s + 96 < s1 ? src4[s + 96] : far;
+            if constexpr (NQ == 2) {
+                na2 = s + 64 < s1 ? q2[s + 64] : T(0);
+                nb2 = s + 96 < s1 ? q2[s + 96] : T(0);
+            }
             const T ax = sa.x + ox, ay = sa.y + oy, az = sa.z + oz, aq = sa.w;
             const T bx = sb.x + ox, by = sb.y + oy, bz = sb.z + oz, bq = sb.w;
 #pragma unroll
             for (int j = 0; j < NT; j++) {
                 const T dx = tx[j] - ax, dy = ty[j] - ay, dz = tz[j] - az;
                 const T ex = tx[j] - bx, ey = ty[j] - by, ez = tz[j] - bz;
-                acc[j] += aq * rsqrt_p<T>(dx * dx + dy * dy + dz * dz);
-                acc[j] += bq * rsqrt_p<T>(ex * ex + ey * ey + ez * ez);
+                const T ra = rsqrt_p<T>(dx * dx + dy * dy + dz * dz);
+                const T rb = rsqrt_p<T>(ex * ex + ey * ey + ez * ez);
+                acc[0][j] += aq * ra;
+                acc[0][j] += bq * rb;
+                if constexpr (NQ == 2) {
+                    acc[1][j] += aq2 * ra;
+                    acc[1][j] += bq2 * rb;
+                }
             }
         }
 #pragma unroll
-        for (int j = 0; j < NT; j++) ns[j] += acc[j];
+        for (int j = 0; j < NT; j++)
+#pragma unroll
+            for (int k = 0; k < NQ; k++) ns[k][j] += acc[k][j];
     }
     // warp sums in the path's precision (fixed butterfly order), then FP64
-    double near[NT];
+    double near[NQ][NT];
 #pragma unroll
-    for (int j = 0; j < NT; j++) {
-        T v = ns[j];
+    for (int k = 0; k < NQ; k++)
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        near[j] = double(v);
-    }
+        for (int j = 0; j < NT; j++) {
+            T v = ns[k][j];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            near[k][j] = double(v);
+        }
     if (lane < nt) {
         T x = 0, y = 0, z = 0;
-        double nr = 0;
+        double nr[NQ];
+#pragma unroll
+        for (int k = 0; k < NQ; k++) nr[k] = 0;
 #pragma unroll
         for (int j = 0; j < NT; j++)
-            if (j == lane) { x = tx[j]; y = ty[j]; z = tz[j]; nr = near[j]; }
-        T far = 0;
+            if (j == lane) {
+                x = tx[j]; y = ty[j]; z = tz[j];
+#pragma unroll
+                for (int k = 0; k < NQ; k++) nr[k] = near[k][j];
+            }
+        const T *__restrict__ Fa = sets.F[0] + fbase;
+        const T *__restrict__ Fb = sets.F[NQ - 1] + fbase;
+        T fa = 0, fb = 0;
         ups_cols<T>(x, y, z, [&](int n, int m, T re, T im) {
-            if (m == 0) far += Fl[ridx(n, 0, 0)] * re;
-            else far += T(2) * (Fl[ridx(n, m, 0)] * re + Fl[ridx(n, m, 1)] * im);
+            if (m == 0) {
+                fa += Fa[ridx(n, 0, 0)] * re;
+                if constexpr (NQ == 2) fb += Fb[ridx(n, 0, 0)] * re;
+            } else {
+                fa += T(2) * (Fa[ridx(n, m, 0)] * re + Fa[ridx(n, m, 1)] * im);
+                if constexpr (NQ == 2) fb += T(2) * (Fb[ridx(n, m, 0)] * re + Fb[ridx(n, m, 1)] * im);
+            }
         });
-        pot[tgt_node[tb + lane]] = (double(far) + nr) * leaf_scale[leaf];
+        const double sc = leaf_scale[leaf];
+        const int node = tgt_node[tb + lane];
+        sets.pot[0][node] = (double(fa) + nr[0]) * sc;
+        if constexpr (NQ == 2) sets.pot[1][node] = (double(fb) + nr[NQ - 1]) * sc;
     }
 }
 
 // L2P + P2P: one warp per target leaf, its targets in passes of 16 and a tail pass of 8
 // or 4 (a leaf of the film holds 18 to 64 nodes: fixed passes of 16 would spend about a
 // fifth of the pair work on padding).
-template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_l2p_p2p(int nleaf, const int *__restrict__ leaf_src,
-                                                 const int *__restrict__ leaf_tgt, const int *__restrict__ tgt_node,
-                                                 const T *__restrict__ tloc, const T *__restrict__ sloc,
-                                                 const int *__restrict__ leaf_ijk, int leaf0,
-                                                 const double *__restrict__ leaf_scale,
-                                                 const int *__restrict__ near_ptr, const int *__restrict__ near_leaf,
-                                                 const T *__restrict__ F, double *__restrict__ pot) {
+template <typename T, int NQ>
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? (NQ == 1 ? 4 : 3) : 2)
+    k_l2p_p2p(int nleaf, const int *__restrict__ leaf_src, const int *__restrict__ leaf_tgt,
+              const int *__restrict__ tgt_node, const T *__restrict__ tloc, const T *__restrict__ sloc,
+              const int *__restrict__ leaf_ijk, int leaf0, const double *__restrict__ leaf_scale,
+              const int *__restrict__ near_ptr, const int *__restrict__ near_leaf, NearSets<T> sets) {
     const int lane = threadIdx.x & 31;
     const int leaf = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (leaf >= nleaf) return;
     const int t0 = leaf_tgt[leaf], t1 = leaf_tgt[leaf + 1];
     if (t0 == t1) return;
     const int li = leaf_ijk[3 * leaf], lj = leaf_ijk[3 * leaf + 1], lk = leaf_ijk[3 * leaf + 2];
-    const T *Fl = F + (size_t)(leaf0 + leaf) * NR;
+    const size_t fbase = (size_t)(leaf0 + leaf) * NR;
     for (int tb = t0; tb < t1;) {
         const int r = t1 - tb;
         if (r > 8) {
-            l2p_p2p_pass<T, 16>(leaf, tb, min(16, r), lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk,
-                                leaf_scale, near_ptr, near_leaf, Fl, pot);
+            l2p_p2p_pass<T, 16, NQ>(leaf, tb, min(16, r), lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk,
+                                    leaf_scale, near_ptr, near_leaf, fbase, sets);
             tb += 16;
         } else if (r > 4) {
-            l2p_p2p_pass<T, 8>(leaf, tb, r, lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk, leaf_scale,
-                               near_ptr, near_leaf, Fl, pot);
+            l2p_p2p_pass<T, 8, NQ>(leaf, tb, r, lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk, leaf_scale,
+                                   near_ptr, near_leaf, fbase, sets);
             tb += 8;
         } else {
-            l2p_p2p_pass<T, 4>(leaf, tb, r, lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk, leaf_scale,
-                               near_ptr, near_leaf, Fl, pot);
+            l2p_p2p_pass<T, 4, NQ>(leaf, tb, r, lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk, leaf_scale,
+                                   near_ptr, near_leaf, fbase, sets);
             tb += 4;
         }
     }
@@ -471,17 +540,19 @@ __device__ __forceinline__ void ds_two_sum(float a, float b, float &s, float &e)
 // SFU estimate and one Newton step evaluated in double-single (error ~1e-13), q/r as a
 // double-single product, summed with two-sum. One warp per target leaf, 8 targets per
 // lane pass, sources spread over the lanes; per-lane sums reduced over the warp in FP64.
+// NQ charge sets share the pair geometry and 1/r (the second set's charge hi/lo in q2h/q2l).
+template <int NQ>
 __global__ void __launch_bounds__(128) k_l2p_p2p_ds(int nleaf, const int *__restrict__ leaf_src,
                                                     const int *__restrict__ leaf_tgt,
                                                     const int *__restrict__ tgt_node,
                                                     const double *__restrict__ tloc,
                                                     const float4 *__restrict__ th4, const float4 *__restrict__ tl4,
                                                     const float4 *__restrict__ sh4, const float4 *__restrict__ sl4,
+                                                    const float *__restrict__ q2h, const float *__restrict__ q2l,
                                                     const int *__restrict__ leaf_ijk, int leaf0,
                                                     const double *__restrict__ leaf_scale,
                                                     const int *__restrict__ near_ptr,
-                                                    const int *__restrict__ near_leaf, const double *__restrict__ F,
-                                                    double *__restrict__ pot) {
+                                                    const int *__restrict__ near_leaf, NearSets<double> sets) {
     constexpr int NT = 8;
     const int lane = threadIdx.x & 31;
     const int leaf = blockIdx.x * 4 + (threadIdx.x >> 5);
@@ -489,18 +560,18 @@ __global__ void __launch_bounds__(128) k_l2p_p2p_ds(int nleaf, const int *__rest
     const int t0 = leaf_tgt[leaf], t1 = leaf_tgt[leaf + 1];
     if (t0 == t1) return;
     const int li = leaf_ijk[3 * leaf], lj = leaf_ijk[3 * leaf + 1], lk = leaf_ijk[3 * leaf + 2];
-    const double *Fl = F + (size_t)(leaf0 + leaf) * NR;
+    const size_t fbase = (size_t)(leaf0 + leaf) * NR;
     for (int tb = t0; tb < t1; tb += NT) {
         const int nt = min(NT, t1 - tb);
-        float thx[NT], thy[NT], thz[NT], tlx[NT], tly[NT], tlz[NT], ah[NT], al[NT];
+        float thx[NT], thy[NT], thz[NT], tlx[NT], tly[NT], tlz[NT], ah[NQ][NT], al[NQ][NT];
 #pragma unroll
         for (int j = 0; j < NT; j++) {
             const int ti = tb + (j < nt ? j : 0);
             const float4 h = th4[ti], l = tl4[ti];
             thx[j] = h.x; thy[j] = h.y; thz[j] = h.z;
             tlx[j] = l.x; tly[j] = l.y; tlz[j] = l.z;
-            ah[j] = 0.f;
-            al[j] = 0.f;
+#pragma unroll
+            for (int k = 0; k < NQ; k++) ah[k][j] = al[k][j] = 0.f;
         }
         for (int e = near_ptr[leaf]; e < near_ptr[leaf + 1]; e++) {
             const int nl = near_leaf[e];
@@ -510,7 +581,14 @@ __global__ void __launch_bounds__(128) k_l2p_p2p_ds(int nleaf, const int *__rest
             const int s0 = leaf_src[nl], s1 = leaf_src[nl + 1];
             for (int s = s0 + lane; s < s1; s += 32) {
                 const float4 h = sh4[s], l = sl4[s];
-                const float sx = h.x + ox, sy = h.y + oy, sz = h.z + oz, qh = h.w, ql = l.w;
+                const float sx = h.x + ox, sy = h.y + oy, sz = h.z + oz;
+                float qh[NQ], ql[NQ];
+                qh[0] = h.w;
+                ql[0] = l.w;
+                if constexpr (NQ == 2) {
+                    qh[1] = q2h[s];
+                    ql[1] = q2l[s];
+                }
 #pragma unroll
                 for (int j = 0; j < NT; j++) {
                     const float d1x = thx[j] - sx, d1y = thy[j] - sy, d1z = thz[j] - sz;  // exact
@@ -536,35 +614,53 @@ __global__ void __launch_bounds__(128) k_l2p_p2p_ds(int nleaf, const int *__rest
                     const float delta = (1.f - u1) - u2;
                     const float yl = 0.5f * y * delta;
                     // q / r = (qh + ql)(y + yl), accumulated with two-sum
-                    const float c1 = qh * y;
-                    const float c2 = fmaf(qh, y, -c1) + fmaf(qh, yl, ql * y);
-                    float sn, en;
-                    ds_two_sum(ah[j], c1, sn, en);
-                    ah[j] = sn;
-                    al[j] += en + c2;
+#pragma unroll
+                    for (int k = 0; k < NQ; k++) {
+                        const float c1 = qh[k] * y;
+                        const float c2 = fmaf(qh[k], y, -c1) + fmaf(qh[k], yl, ql[k] * y);
+                        float sn, en;
+                        ds_two_sum(ah[k][j], c1, sn, en);
+                        ah[k][j] = sn;
+                        al[k][j] += en + c2;
+                    }
                 }
             }
         }
-        double near[NT];
+        double near[NQ][NT];
 #pragma unroll
-        for (int j = 0; j < NT; j++) {
-            near[j] = double(ah[j]) + double(al[j]);
-            for (int o = 16; o > 0; o >>= 1) near[j] += __shfl_xor_sync(0xffffffffu, near[j], o);
-        }
+        for (int k = 0; k < NQ; k++)
+#pragma unroll
+            for (int j = 0; j < NT; j++) {
+                near[k][j] = double(ah[k][j]) + double(al[k][j]);
+                for (int o = 16; o > 0; o >>= 1) near[k][j] += __shfl_xor_sync(0xffffffffu, near[k][j], o);
+            }
         // L2P in FP64: lane j evaluates target j
         if (lane < nt) {
-            double nr = 0;
+            double nr[NQ];
+#pragma unroll
+            for (int k = 0; k < NQ; k++) nr[k] = 0;
 #pragma unroll
             for (int j = 0; j < NT; j++)
-                if (j == lane) nr = near[j];
+                if (j == lane)
+#pragma unroll
+                    for (int k = 0; k < NQ; k++) nr[k] = near[k][j];
             const int ti = tb + lane;
             const double x = tloc[4 * (size_t)ti], y = tloc[4 * (size_t)ti + 1], z = tloc[4 * (size_t)ti + 2];
-            double far = 0;
+            const double *__restrict__ Fa = sets.F[0] + fbase;
+            const double *__restrict__ Fb = sets.F[NQ - 1] + fbase;
+            double fa = 0, fb = 0;
             ups_cols<double>(x, y, z, [&](int n, int m, double re, double im) {
-                if (m == 0) far += Fl[ridx(n, 0, 0)] * re;
-                else far += 2.0 * (Fl[ridx(n, m, 0)] * re + Fl[ridx(n, m, 1)] * im);
+                if (m == 0) {
+                    fa += Fa[ridx(n, 0, 0)] * re;
+                    if constexpr (NQ == 2) fb += Fb[ridx(n, 0, 0)] * re;
+                } else {
+                    fa += 2.0 * (Fa[ridx(n, m, 0)] * re + Fa[ridx(n, m, 1)] * im);
+                    if constexpr (NQ == 2) fb += 2.0 * (Fb[ridx(n, m, 0)] * re + Fb[ridx(n, m, 1)] * im);
+                }
             });
-            pot[tgt_node[ti]] = (far + nr) * leaf_scale[leaf];
+            const double sc = leaf_scale[leaf];
+            sets.pot[0][tgt_node[ti]] = (fa + nr[0]) * sc;
+            if constexpr (NQ == 2) sets.pot[1][tgt_node[ti]] = (fb + nr[NQ - 1]) * sc;
         }
     }
 }
@@ -664,7 +760,7 @@ static const FmmOps &fmm_ops() {
 void fmm_free(Ctx &c);
 static int fmm_build_forest(Ctx &c, int L);
 template <typename T>
-static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t);
+static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq);
 
 // Points of each sample (sources and target nodes) and the sample's root cube. A batch of
 // independent meshes gets one octree per sample (a forest); a single mesh is one tree.
@@ -744,6 +840,7 @@ int fmm_build(Ctx &c) {
         for (int l = std::max(2, l0 - 1); l <= std::min(10, l0 + 1); l++) cands.push_back(l);
     }
     cudaMemsetAsync(c.src_q, 0, sizeof(double) * std::max(1, c.nsrc), c.stream);
+    if (c.src_q2) cudaMemsetAsync(c.src_q2, 0, sizeof(double) * std::max(1, c.nsrc), c.stream);
     int bestL = cands[0];
     double bestms = 1e300;
     for (size_t k = 0; k < cands.size(); k++) {
@@ -754,13 +851,15 @@ int fmm_build(Ctx &c) {
         int s = fmm_build_forest(c, cands[k]);
         if (s != FG_OK) return s;
         if (cands.size() == 1) return FG_OK;
-        // autotune: time two evaluations with the current charges (values do not matter)
+        // autotune: time two evaluations (of all charge sets, as the steps run them) with
+        // the current charges (values do not matter)
         cudaEvent_t a, b;
         FCK(cudaEventCreate(&a));
         FCK(cudaEventCreate(&b));
-        FCK(fp32 ? fmm_eval_t<float>(c, *t) : fmm_eval_t<double>(c, *t));
+        FCK(fp32 ? fmm_eval_t<float>(c, *t, t->nq) : fmm_eval_t<double>(c, *t, t->nq));
         FCK(cudaEventRecord(a, c.stream));
-        for (int r = 0; r < 2; r++) FCK(fp32 ? fmm_eval_t<float>(c, *t) : fmm_eval_t<double>(c, *t));
+        for (int r = 0; r < 2; r++)
+            FCK(fp32 ? fmm_eval_t<float>(c, *t, t->nq) : fmm_eval_t<double>(c, *t, t->nq));
         FCK(cudaEventRecord(b, c.stream));
         FCK(cudaEventSynchronize(b));
         float ms = 0;
@@ -789,6 +888,8 @@ static int fmm_build_forest(Ctx &c, int L) {
     FmmTree *t = static_cast<FmmTree *>(c.fmm);
     const bool fp32 = t->fp32;
     t->L = L;
+    t->nsrc = c.nsrc;
+    t->nq = (c.opts.first_order || !c.src_q2 || !c.pot2) ? 1 : 2;  // m, and v beside it
     const int nside = 1 << L;
     const std::vector<SamplePts> SP = split_samples(c);
     const int nseg = (int)SP.size();
@@ -975,11 +1076,12 @@ static int fmm_build_forest(Ctx &c, int L) {
         FCK(up(&t->tc_code, codes));
         FCK(up(&t->tc_units, units));
         FCK(up(&t->tc_comb, comb));
-        FCK(cudaMalloc(&t->tc_scratch, sizeof(float) * (size_t)std::max(1, nslot) * translate_tc_tile() * NR));
+        t->nslot_floats = (size_t)std::max(1, nslot) * translate_tc_tile() * NR;
+        FCK(cudaMalloc(&t->tc_scratch, sizeof(float) * t->nslot_floats * t->nq));
         FCK(cudaMalloc(&t->tc_err, sizeof(int)));
         FCK(cudaMemset(t->tc_err, 0, sizeof(int)));
         FCK(translate_tc_setup());
-        const size_t nexp = (size_t)ncell * NR;
+        const size_t nexp = (size_t)ncell * NR * t->nq;
         FCK(cudaMalloc(&t->Mh, nexp * sizeof(float)));
         FCK(cudaMalloc(&t->Ml, nexp * sizeof(float)));
         FCK(cudaMalloc(&t->Fh, nexp * sizeof(float)));
@@ -1041,10 +1143,19 @@ static int fmm_build_forest(Ctx &c, int L) {
     c.src_dst = nullptr;
     FCK(up(&c.src_dst, src_dst));
     const size_t esz = fp32 ? sizeof(float) : sizeof(double);
-    FCK(cudaMalloc(&t->M, (size_t)ncell * NR * esz));
-    FCK(cudaMalloc(&t->F, (size_t)ncell * NR * esz));
-    FCK(cudaMemset(t->M, 0, (size_t)ncell * NR * esz));
-    FCK(cudaMemset(t->F, 0, (size_t)ncell * NR * esz));
+    const size_t nexp_all = (size_t)ncell * NR * t->nq;
+    FCK(cudaMalloc(&t->M, nexp_all * esz));
+    FCK(cudaMalloc(&t->F, nexp_all * esz));
+    FCK(cudaMemset(t->M, 0, nexp_all * esz));
+    FCK(cudaMemset(t->F, 0, nexp_all * esz));
+    if (t->nq == 2) {
+        FCK(cudaMalloc(&t->sq2, std::max(1, c.nsrc) * esz));
+        FCK(cudaMemset(t->sq2, 0, std::max(1, c.nsrc) * esz));
+        if (t->ds) {
+            FCK(cudaMalloc(&t->ds_q2, 2 * sizeof(float) * std::max(1, c.nsrc)));
+            FCK(cudaMemset(t->ds_q2, 0, 2 * sizeof(float) * std::max(1, c.nsrc)));
+        }
+    }
     if (fp32) {
         FCK(cudaFuncSetAttribute(k_translate<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, tr_smem<float>()));
     } else {
@@ -1065,7 +1176,8 @@ void fmm_free(Ctx &c) {
     void *ptrs[] = {t->leaf_scale, t->leaf_src, t->leaf_tgt, t->tgt_node, t->sloc, t->tloc, t->leaf_ijk, t->m2l_tab, t->m2m_tab,
                     t->l2l_tab, t->near_ptr, t->near_leaf, t->M, t->F, t->op_m2l, t->op_m2m, t->op_l2l,
                     t->tc_code, t->tc_units, t->tc_comb, t->tc_scratch, t->tc_err, t->Mh, t->Ml, t->Fh, t->Fl,
-                    t->img_m2l, t->img_m2m, t->img_l2l, t->ds_src_hi, t->ds_src_lo, t->ds_tgt_hi, t->ds_tgt_lo};
+                    t->img_m2l, t->img_m2m, t->img_l2l, t->ds_src_hi, t->ds_src_lo, t->ds_tgt_hi, t->ds_tgt_lo,
+                    t->sq2, t->ds_q2};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &set : t->ev)
@@ -1092,12 +1204,16 @@ static void harvest_set(FmmTree &t, int k) {
     t.ev_pending[k] = false;
 }
 
+// One FMM evaluation of nq charge sets: set 0 from c.src_q into c.pot, set 1 (nq = 2) from
+// c.src_q2 into c.pot2. The sets share every table, operator image and launch (grid y of
+// P2M and of the tensor-core translations; one near-field pass computes both).
 template <typename T>
-static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
+static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq) {
+    if (nq < 1 || nq > t.nq || (nq == 2 && (!c.src_q2 || !c.pot2))) return cudaErrorInvalidValue;
     const int L = t.L;
     T *M = (T *)t.M, *F = (T *)t.F;
-    const size_t esz = sizeof(T);
     constexpr int TB = TrShape<T>::TB;
+    const size_t sstride = (size_t)t.ncell * NR;  // elements between the sets' expansions
     const bool prof = c.opts.profile && t.ev[0][0];
     cudaEvent_t *ev = t.ev[t.ev_next];
     if (prof) {
@@ -1105,11 +1221,26 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
         cudaEventRecord(ev[0], c.stream);
     }
     const bool tc = tc_path<T>(t);
-    k_p2m<T><<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, (T *)t.sloc, c.src_q, t.leaf0, M,
-                                                       tc ? t.Mh : nullptr, tc ? t.Ml : nullptr,
-                                                       t.ds ? t.ds_src_hi : nullptr, t.ds ? t.ds_src_lo : nullptr);
+    P2mSet<T> ps[2];
+    for (int k = 0; k < 2; k++) {
+        const int q = k < nq ? k : 0;
+        P2mSet<T> &p = ps[k];
+        p.q = q ? c.src_q2 : c.src_q;
+        p.M = M + q * sstride;
+        p.Mh = tc ? t.Mh + q * sstride : nullptr;
+        p.Ml = tc ? t.Ml + q * sstride : nullptr;
+        p.qn = q ? (T *)t.sq2 : (T *)t.sloc + 3;
+        p.qn_stride = q ? 1 : 4;
+        p.qh = p.ql = nullptr;
+        p.qd_stride = q ? 1 : 4;
+        if (t.ds) {
+            p.qh = q ? t.ds_q2 : (float *)t.ds_src_hi + 3;
+            p.ql = q ? t.ds_q2 + t.nsrc : (float *)t.ds_src_lo + 3;
+        }
+    }
+    k_p2m<T><<<dim3((t.nleaf + 3) / 4, nq), 128, 0, c.stream>>>(t.nleaf, t.leaf_src, (const T *)t.sloc, t.leaf0,
+                                                                 ps[0], ps[1]);
     if (prof) cudaEventRecord(ev[1], c.stream);
-    // out (+)= sum_code Op[code] in[tab[cell][code]] over n output cells from out0
     // out (+)= sum_code Op[code] in[tab[cell][code]] over n output cells from out0; the
     // tensor-core form reads the inputs' hi/lo split and writes the outputs' split
     enum { M2M, M2L, L2L };
@@ -1130,12 +1261,15 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
             a.tile_code = t.tc_code; a.err = t.tc_err; a.terms = 7;
             a.units = t.tc_units + tl.unit0; a.nunits = tl.nunit;
             a.comb = t.tc_comb + tl.comb0; a.ncomb = tl.ncomb; a.scratch = t.tc_scratch;
+            a.nset = nq; a.set_io = sstride; a.set_scratch = t.nslot_floats;
             launch_translate_tc(c.stream, a);
         } else {
             const void *ops = kind == M2M ? t.op_m2m : kind == M2L ? t.op_m2l : t.op_l2l;
-            T *in = kind == L2L ? F : M, *out = kind == M2M ? M : F;
-            k_translate<T><<<(n + TB - 1) / TB, 160, tr_smem<T>(), c.stream>>>(n, out0, ncode, tab, (const T *)ops, in,
-                                                                            out, kind == L2L);
+            for (int q = 0; q < nq; q++) {
+                T *in = (kind == L2L ? F : M) + q * sstride, *out = (kind == M2M ? M : F) + q * sstride;
+                k_translate<T><<<(n + TB - 1) / TB, 160, tr_smem<T>(), c.stream>>>(n, out0, ncode, tab,
+                                                                                (const T *)ops, in, out, kind == L2L);
+            }
         }
     };
     const FmmTree::TcLaunch none;
@@ -1147,16 +1281,28 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
     for (int l = 3; l <= L; l++)
         translate(L2L, t.lev_begin[l + 1] - t.lev_begin[l], t.lev_begin[l], t.tc ? t.tc_l2l[l] : none);
     if (prof) cudaEventRecord(ev[4], c.stream);
-    if (t.ds)
-        k_l2p_p2p_ds<<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node,
-                                                              (const double *)t.tloc, t.ds_tgt_hi, t.ds_tgt_lo,
-                                                              t.ds_src_hi, t.ds_src_lo, t.leaf_ijk, t.leaf0,
-                                                              t.leaf_scale, t.near_ptr, t.near_leaf,
-                                                              (const double *)F, c.pot);
-    else
-        k_l2p_p2p<T><<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node,
-                                                           (const T *)t.tloc, (const T *)t.sloc, t.leaf_ijk, t.leaf0,
-                                                           t.leaf_scale, t.near_ptr, t.near_leaf, F, c.pot);
+    NearSets<T> ns;
+    ns.q2 = nq == 2 ? (const T *)t.sq2 : nullptr;
+    ns.F[0] = F;
+    ns.F[1] = F + (nq == 2 ? sstride : 0);
+    ns.pot[0] = c.pot;
+    ns.pot[1] = nq == 2 ? c.pot2 : c.pot;
+    const int nb = (t.nleaf + 3) / 4;
+    if constexpr (sizeof(T) == 8) {
+        if (t.ds) {
+            auto k = nq == 2 ? k_l2p_p2p_ds<2> : k_l2p_p2p_ds<1>;
+            k<<<nb, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node, (const double *)t.tloc,
+                                        t.ds_tgt_hi, t.ds_tgt_lo, t.ds_src_hi, t.ds_src_lo, t.ds_q2,
+                                        t.ds_q2 ? t.ds_q2 + t.nsrc : nullptr, t.leaf_ijk, t.leaf0, t.leaf_scale,
+                                        t.near_ptr, t.near_leaf, ns);
+        }
+    }
+    if (!t.ds) {
+        auto k = nq == 2 ? k_l2p_p2p<T, 2> : k_l2p_p2p<T, 1>;
+        k<<<nb, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node, (const T *)t.tloc,
+                                    (const T *)t.sloc, t.leaf_ijk, t.leaf0, t.leaf_scale, t.near_ptr, t.near_leaf,
+                                    ns);
+    }
     if (prof) {
         cudaEventRecord(ev[5], c.stream);
         t.ev_pending[t.ev_next] = true;
@@ -1165,10 +1311,10 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t) {
     return cudaGetLastError();
 }
 
-cudaError_t fmm_eval(Ctx &c) {
+cudaError_t fmm_eval(Ctx &c, int nq) {
     FmmTree *t = static_cast<FmmTree *>(c.fmm);
     if (!t) return cudaErrorNotSupported;
-    return t->fp32 ? fmm_eval_t<float>(c, *t) : fmm_eval_t<double>(c, *t);
+    return t->fp32 ? fmm_eval_t<float>(c, *t, nq) : fmm_eval_t<double>(c, *t, nq);
 }
 
 int fmm_stage_ms(const Ctx &c, double ms[5]) {
@@ -1182,13 +1328,16 @@ int fmm_stage_ms(const Ctx &c, double ms[5]) {
     return FG_OK;
 }
 
-int fmm_launches_per_eval(const Ctx &c) {
+int fmm_launches_per_eval(const Ctx &c, int nq) {
     const FmmTree *t = static_cast<const FmmTree *>(c.fmm);
     if (!t) return 0;
-    int n = 2;  // P2M, L2P + P2P
-    for (int l = 2; l <= t->L - 1; l++) n += 1 + (t->tc && t->tc_m2m[l].ncomb > 0);
-    n += 1 + (t->tc && t->tc_m2l.ncomb > 0);
-    for (int l = 3; l <= t->L; l++) n += 1 + (t->tc && t->tc_l2l[l].ncomb > 0);
+    int n = 2;  // P2M, L2P + P2P (both sets in one launch each)
+    // tensor-core translations: both sets in one launch (and one combine launch); the
+    // k_translate form launches once per set
+    const int per = t->tc ? 1 : nq;
+    for (int l = 2; l <= t->L - 1; l++) n += per + (t->tc && t->tc_m2m[l].ncomb > 0);
+    n += per + (t->tc && t->tc_m2l.ncomb > 0);
+    for (int l = 3; l <= t->L; l++) n += per + (t->tc && t->tc_l2l[l].ncomb > 0);
     return n;
 }
 

@@ -205,7 +205,11 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
     const int n_out = a.n_out, out0 = a.out0, ncode = a.ncode, accumulate = a.accumulate, terms = a.terms;
     const int *__restrict__ tab = a.tab;
     const int *__restrict__ tile_code = a.tile_code;
-    float *out = a.out;
+    // set of expansions (grid y): the same tables and operators on another set of inputs
+    const size_t io = blockIdx.y * a.set_io;
+    float *out = a.out + io, *out_hi = a.out_hi + io, *out_lo = a.out_lo + io;
+    const float *in_hi = a.in_hi + io, *in_lo = a.in_lo + io;
+    float *scratch = a.scratch + blockIdx.y * a.set_scratch;
     int *err = a.err;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -224,8 +228,8 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
                 if (cell < n_out) {
                     const size_t o = (size_t)(out0 + cell) * NRC + e % NRC;
                     out[o] = 0.f;
-                    a.out_hi[o] = 0.f;
-                    a.out_lo[o] = 0.f;
+                    out_hi[o] = 0.f;
+                    out_lo[o] = 0.f;
                 }
             }
         return;
@@ -286,7 +290,7 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
                         bulk_g2s(st, img, IMG_BYTES, &full[s]);
                         bulk_g2s(st + A_BYTES, img + IMG_BYTES, IMG_BYTES, &full[s]);
                     }
-                    gather_item(st + 2 * A_BYTES, tid, KI * q, sc, a.in_hi, a.in_lo);
+                    gather_item(st + 2 * A_BYTES, tid, KI * q, sc, in_hi, in_lo);
                 }
             }
             cp_commit();
@@ -365,7 +369,7 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
         }
         if (drained == ncodes && row < NRC) {
             if (slot >= 0) {  // one of several units of this tile: partial result
-                float *p = a.scratch + (size_t)slot * NC * NRC + row;
+                float *p = scratch + (size_t)slot * NC * NRC + row;
 #pragma unroll
                 for (int j = 0; j < NC; j++) p[j * NRC] = acc[j];
             } else {
@@ -377,8 +381,8 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
                         const float v = accumulate ? out[o] + acc[j] : acc[j];
                         out[o] = v;
                         const float h = tf32_rn(v);
-                        a.out_hi[o] = h;
-                        a.out_lo[o] = v - h;
+                        out_hi[o] = h;
+                        out_lo[o] = v - h;
                     }
                 }
             }
@@ -403,17 +407,20 @@ FG_TC_KERNEL(k_l2l_tc)
 // Sum of the partial results of tiles split over several units, in slot order.
 __global__ void __launch_bounds__(256) k_tc_combine(TcArgs a) {
     const int4 ct = a.comb[blockIdx.x];
+    const size_t io = blockIdx.y * a.set_io;
+    const float *scratch = a.scratch + blockIdx.y * a.set_scratch;
+    float *out = a.out + io, *out_hi = a.out_hi + io, *out_lo = a.out_lo + io;
     for (int e = threadIdx.x; e < NC * NRC; e += blockDim.x) {
         const int cell = ct.x * NC + e / NRC;
         if (cell >= a.n_out) continue;
         float v = 0.f;
-        for (int u = 0; u < ct.z; u++) v += a.scratch[(size_t)(ct.y + u) * NC * NRC + e];
+        for (int u = 0; u < ct.z; u++) v += scratch[(size_t)(ct.y + u) * NC * NRC + e];
         const size_t o = (size_t)(a.out0 + cell) * NRC + e % NRC;
-        if (a.accumulate) v += a.out[o];
-        a.out[o] = v;
+        if (a.accumulate) v += out[o];
+        out[o] = v;
         const float h = tf32_rn(v);
-        a.out_hi[o] = h;
-        a.out_lo[o] = v - h;
+        out_hi[o] = h;
+        out_lo[o] = v - h;
     }
 }
 
@@ -453,8 +460,9 @@ cudaError_t translate_tc_setup() {
 cudaError_t launch_translate_tc(cudaStream_t st, const TcArgs &a) {
     if (a.n_out <= 0 || a.nunits <= 0) return cudaSuccess;
     auto k = a.accumulate ? k_l2l_tc : (a.ncode == 8 ? k_m2m_tc : k_m2l_tc);
-    k<<<a.nunits, 288, translate_tc_smem(), st>>>(a);
-    if (a.ncomb > 0) k_tc_combine<<<a.ncomb, 256, 0, st>>>(a);
+    const unsigned nset = a.nset > 1 ? (unsigned)a.nset : 1u;
+    k<<<dim3(a.nunits, nset), 288, translate_tc_smem(), st>>>(a);
+    if (a.ncomb > 0) k_tc_combine<<<dim3(a.ncomb, nset), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

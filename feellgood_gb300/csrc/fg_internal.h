@@ -193,8 +193,11 @@ struct Ctx {
     int *src_dst = nullptr;      // original source index -> storage position (FMM order)
     void *fmm = nullptr;         // FMM tree and buffers (fg_fmm.cu)
     double *src_q = nullptr;
+    double *src_q2 = nullptr;    // charges of v (demag of m and v evaluated together), or nullptr
     double *tri_slot = nullptr;  // 3 x nft corrections
+    double *tri_slot2 = nullptr; // 3 x nft corrections of src_q2
     double *pot = nullptr;       // nn
+    double *pot2 = nullptr;      // nn, potential of src_q2
     double *epart = nullptr;     // energy partials
     double *hepart = nullptr;    // pinned
     int epart_blocks = 0;
@@ -243,9 +246,10 @@ cudaError_t launch_node(Ctx &c, double angle);
 cudaError_t launch_bicg64(Ctx &c, double dt, double prefactor);
 cudaError_t launch_mixed(Ctx &c, double dt, double prefactor);
 cudaError_t launch_apply(Ctx &c, double c0, const double *x, double *y);
-cudaError_t launch_charges(Ctx &c, const double *m);
+// set 0: charges into src_q / tri_slot, potential from pot; set 1: src_q2 / tri_slot2 / pot2
+cudaError_t launch_charges(Ctx &c, const double *m, int set = 0);
 cudaError_t launch_p2p_direct(Ctx &c);
-cudaError_t launch_phi_final(Ctx &c, double *phi_out);
+cudaError_t launch_phi_final(Ctx &c, double *phi_out, int set = 0);
 cudaError_t launch_energy(Ctx &c, const double Hext[3]);
 cudaError_t launch_energy_into(Ctx &c, const double Hext[3], double *partial);
 int bicg_grid_size(Ctx &c, bool mixed);
@@ -260,7 +264,8 @@ cudaError_t launch_barrier_timeout_probe(Ctx &c, int *out);
 cudaError_t launch_mbar_timeout_probe(cudaStream_t st, int *err);
 int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p);
 int *fmm_error_flag(const Ctx &c);
-int fmm_launches_per_eval(const Ctx &c);  // kernels one FMM evaluation launches  // device int: FG_ETIMEDOUT after an expired wait (or nullptr)
+cudaError_t fmm_eval(Ctx &c, int nq = 1);  // nq 2: c.src_q2 -> c.pot2 beside c.src_q -> c.pot
+int fmm_launches_per_eval(const Ctx &c, int nq = 1);  // kernels one FMM evaluation launches  // device int: FG_ETIMEDOUT after an expired wait (or nullptr)
 // tensor-core translations (fg_fmm_tc.cu)
 int translate_tc_smem();
 int translate_tc_tile();  // output cells per tile of the tensor-core translations
@@ -281,6 +286,8 @@ struct TcArgs {
     int ncomb;
     int *err;                       // FG_ETIMEDOUT after an expired wait
     int terms;                      // product terms of the split (7 in production)
+    int nset;                       // independent sets of expansions (grid y; 0 or 1: one set)
+    size_t set_io, set_scratch;     // floats between sets in in/out arrays and in scratch
 };
 cudaError_t launch_translate_tc(cudaStream_t st, const TcArgs &a);
 std::vector<float> translate_tc_images(const std::vector<double> &ops, int ncode);

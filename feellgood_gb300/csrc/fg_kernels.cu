@@ -978,15 +978,17 @@ cudaError_t launch_apply(Ctx &c, double c0, const double *x, double *y) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_charges(Ctx &c, const double *m) {
+cudaError_t launch_charges(Ctx &c, const double *m, int set) {
     const int n = c.nmt + c.nft;
     if (n == 0) return cudaSuccess;
+    double *q = set ? c.src_q2 : c.src_q, *ts = set ? c.tri_slot2 : c.tri_slot;
+    if (!q || !ts) return cudaErrorInvalidValue;
     if (c.npi_t == 5)
         k_charges<5, 4><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs,
-                                                                c.tri, c.tri_c, m, c.src_dst, c.src_q, c.tri_slot);
+                                                                c.tri, c.tri_c, m, c.src_dst, q, ts);
     else
         k_charges<1, 1><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs,
-                                                                c.tri, c.tri_c, m, c.src_dst, c.src_q, c.tri_slot);
+                                                                c.tri, c.tri_c, m, c.src_dst, q, ts);
     return cudaGetLastError();
 }
 
@@ -997,10 +999,12 @@ cudaError_t launch_p2p_direct(Ctx &c) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_phi_final(Ctx &c, double *phi_out) {
+cudaError_t launch_phi_final(Ctx &c, double *phi_out, int set) {
     if (c.n_mag_nodes == 0) return cudaSuccess;
+    const double *ts = set ? c.tri_slot2 : c.tri_slot, *pot = set ? c.pot2 : c.pot;
+    if (!ts || !pot) return cudaErrorInvalidValue;
     k_phi_final<<<nblocks(c.n_mag_nodes, 256), 256, 0, c.stream>>>(c.n_mag_nodes, c.mag_nodes, c.tinc_ptr, c.tinc,
-                                                                     c.tri_slot, c.pot, phi_out);
+                                                                     ts, pot, phi_out);
     return cudaGetLastError();
 }
 

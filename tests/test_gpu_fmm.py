@@ -108,3 +108,25 @@ def test_double_single_near_field(shape, leaf):
         ps, pn = cs.demag(which), cn.demag(which)
         print("double-single vs FP64 near field, rel. difference %.2e" % _rel(ps, pn))
         assert _rel(ps, pn) < 1e-12
+
+
+@pytest.mark.parametrize("precision,native", [(fg.FG_PREC_FP32_REFINE, 0), (fg.FG_PREC_FP64, 0),
+                                              (fg.FG_PREC_FP64, 1)])
+@pytest.mark.parametrize("shape,leaf", [((12, 12, 12), -3), ((40, 40, 3), 60)])
+def test_pair_evaluation_matches_single(precision, native, shape, leaf):
+    """compute_all evaluates the demag of m and of v in one FMM pass (both charge sets
+    through the same launches, one near-field pass with shared pair geometry); each set
+    follows the arithmetic of its own single evaluation, so the potentials agree with
+    fg_demag(0) and fg_demag(1) to the last bits."""
+    m = cases.cuboid(*shape)
+    u = cases.perturbed_state(m["xyz"], seed=11, sigma=0.3)
+    v = cases.tangent_field(u, seed=12)
+    c = fg.Context(m, cases.regions(), demag=fg.FG_DEMAG_FMM, precision=precision, fmm_leaf=leaf,
+                   fmm_native_fp64=native)
+    c.set_state(u, v)
+    c.compute_all(np.zeros(3))
+    st = c.get_state(0)
+    for got, which in ((st["phi"], 0), (st["phiv"], 1)):
+        single = c.demag(which)
+        scale = np.abs(single).max()
+        assert np.abs(got - single).max() <= 1e-13 * scale, (which, np.abs(got - single).max() / scale)
