@@ -264,7 +264,8 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="film", choices=["film", "batch64", "wire", "platelet"])
     ap.add_argument("--plain-steps", type=int, default=3)
-    ap.add_argument("--train-steps", type=int, default=40, help="untimed solves that train the learned guess")
+    ap.add_argument("--train-steps", type=int, default=None,
+                    help="untimed solves that train the learned guess (default 40; 0 with --quick)")
     ap.add_argument("--train-every", type=int, default=4,
                     help="after those, the guess keeps training (timed) on every n-th solve")
     ap.add_argument("--no-cpu", action="store_true")
@@ -281,7 +282,9 @@ def main():
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.quick:
-        args.train_steps, args.plain_steps, args.e2e_steps, args.no_cpu = 0, 0, 0, True
+        args.plain_steps, args.e2e_steps, args.no_cpu = 0, 0, True
+    if args.train_steps is None:
+        args.train_steps = 0 if args.quick else 40
     if args.impl == "reference":
         reference_arm(args)
         return
@@ -360,7 +363,7 @@ def main():
     ctx.close()
 
     # the same steps (state and angles) with the previous-step guess: what the learned guess gains
-    prev_value = prev_iters = None
+    prev_value = prev_iters = prev_phase = None
     cp = None if args.quick else fg.Context(mesh, regions(), tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP32_REFINE,
                     demag=fg.FG_DEMAG_FMM)
     if cp is not None:
@@ -368,6 +371,8 @@ def main():
         pms, preps = run_steps(cp, args.steps, H, DT, step_angles)
         prev_value = args.steps / (float(pms[:, 4].sum()) / 1e3)
         prev_iters = float(np.mean([r["iters"] for r in preps]))
+        prev_phase = dict(zip(["elements", "solve", "demag_x2", "energy_evolution", "step"],
+                              [float(x) for x in pms.mean(axis=0)]))
         cp.close()
 
     # plain FP64 GPU path, same state, angles and tolerance
@@ -435,7 +440,7 @@ def main():
             "prev_guess_fp32_refine_steps_per_s": prev_value,
             "iters_per_step": float(np.mean(iters)), "refinements_per_step": float(np.mean(refs)),
             "solver_lanes_per_row": lanes_per_row, "solver_blocks": solver_blocks,
-            "prev_guess_iters_per_step": prev_iters, "plain_iters_per_step": plain_iters,
+            "prev_guess_iters_per_step": prev_iters, "prev_guess_phase_ms": prev_phase, "plain_iters_per_step": plain_iters,
             "plain_fp64_detail": plain_detail,
             "learned_guess": {"accepted_frac": float(np.mean(acc)),
                               "res0_over_fallback_median": float(np.median(r0_ratio)) if r0_ratio else None,

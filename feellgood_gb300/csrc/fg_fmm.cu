@@ -489,6 +489,177 @@ __device__ __forceinline__ void l2p_p2p_pass(int leaf, int tb, int nt, int lane,
     }
 }
 
+// Packed FP32 pairs (Blackwell f32x2 instructions): two lanes of a 64-bit register hold
+// the same quantity for two targets, so one instruction serves two pairs.
+using u64 = unsigned long long;
+__device__ __forceinline__ u64 pk2(float lo, float hi) {
+    u64 d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+__device__ __forceinline__ void upk2(u64 v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ u64 sub2(u64 a, u64 b) {
+    u64 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 add2(u64 a, u64 b) {
+    u64 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 mul2(u64 a, u64 b) {
+    u64 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 fma2(u64 a, u64 b, u64 c) {
+    u64 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// The FP32 pass of l2p_p2p_pass with the pair arithmetic on packed target pairs: per two
+// pairs 3 subtractions, 3 for r^2 (d_x^2, then + d_y^2, + d_z^2 as fused multiply-adds),
+// two SFU reciprocal square roots and one fused multiply-add per charge set; every
+// operation and its order per pair are those of the scalar pass.
+template <int NT, int NQ>
+__device__ __forceinline__ void l2p_p2p_pass_x2(int leaf, int tb, int nt, int lane, int li, int lj, int lk,
+                                                const int *__restrict__ leaf_src, const int *__restrict__ tgt_node,
+                                                const float *__restrict__ tloc, const float *__restrict__ sloc,
+                                                const int *__restrict__ leaf_ijk,
+                                                const double *__restrict__ leaf_scale,
+                                                const int *__restrict__ near_ptr, const int *__restrict__ near_leaf,
+                                                size_t fbase, const NearSets<float> &sets) {
+    static_assert(NT % 2 == 0, "targets come in pairs");
+    constexpr int NP = NT / 2;
+    const float4 *__restrict__ src4 = reinterpret_cast<const float4 *>(sloc);
+    const float *__restrict__ q2 = sets.q2;
+    u64 TX[NP], TY[NP], TZ[NP], NS[NQ][NP];
+#pragma unroll
+    for (int p = 0; p < NP; p++) {
+        const int t0 = tb + (2 * p < nt ? 2 * p : 0), t1 = tb + (2 * p + 1 < nt ? 2 * p + 1 : 0);
+        TX[p] = pk2(tloc[4 * (size_t)t0], tloc[4 * (size_t)t1]);
+        TY[p] = pk2(tloc[4 * (size_t)t0 + 1], tloc[4 * (size_t)t1 + 1]);
+        TZ[p] = pk2(tloc[4 * (size_t)t0 + 2], tloc[4 * (size_t)t1 + 2]);
+#pragma unroll
+        for (int k = 0; k < NQ; k++) NS[k][p] = 0ull;
+    }
+    for (int e = near_ptr[leaf]; e < near_ptr[leaf + 1]; e++) {
+        const int nl = near_leaf[e];
+        const float ox = float(leaf_ijk[3 * nl] - li), oy = float(leaf_ijk[3 * nl + 1] - lj),
+                    oz = float(leaf_ijk[3 * nl + 2] - lk);
+        const int s0 = leaf_src[nl], s1 = leaf_src[nl + 1];
+        u64 ACC[NQ][NP];
+#pragma unroll
+        for (int p = 0; p < NP; p++)
+#pragma unroll
+            for (int k = 0; k < NQ; k++) ACC[k][p] = 0ull;
+        const float4 far = make_float4(1e4f, 1e4f, 1e4f, 0.f);  // a missing source: zero charge far away
+        int s = s0 + lane;
+        float4 na = s < s1 ? src4[s] : far, nb = s + 32 < s1 ? src4[s + 32] : far;
+        float na2 = 0.f, nb2 = 0.f;
+        if constexpr (NQ == 2) {
+            na2 = s < s1 ? q2[s] : 0.f;
+            nb2 = s + 32 < s1 ? q2[s + 32] : 0.f;
+        }
+        for (; s < s1; s += 64) {
+            const float4 sa = na, sb = nb;
+            const float aq2 = na2, bq2 = nb2;
+            na = s + 64 < s1 ? src4[s + 64] : far;
+            nb = s + 96 < s1 ? src4[s + 96] : far;
+            if constexpr (NQ == 2) {
+                na2 = s + 64 < s1 ? q2[s + 64] : 0.f;
+                nb2 = s + 96 < s1 ? q2[s + 96] : 0.f;
+            }
+            const float ax = sa.x + ox, ay = sa.y + oy, az = sa.z + oz;
+            const float bx = sb.x + ox, by = sb.y + oy, bz = sb.z + oz;
+            const u64 AX = pk2(ax, ax), AY = pk2(ay, ay), AZ = pk2(az, az), AQ = pk2(sa.w, sa.w);
+            const u64 BX = pk2(bx, bx), BY = pk2(by, by), BZ = pk2(bz, bz), BQ = pk2(sb.w, sb.w);
+            const u64 AQ2 = pk2(aq2, aq2), BQ2 = pk2(bq2, bq2);
+#pragma unroll
+            for (int p = 0; p < NP; p++) {
+                const u64 dx = sub2(TX[p], AX), dy = sub2(TY[p], AY), dz = sub2(TZ[p], AZ);
+                const u64 ex = sub2(TX[p], BX), ey = sub2(TY[p], BY), ez = sub2(TZ[p], BZ);
+                const u64 da = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+                const u64 db = fma2(ez, ez, fma2(ey, ey, mul2(ex, ex)));
+                float a0, a1, b0, b1;
+                upk2(da, a0, a1);
+                upk2(db, b0, b1);
+                const u64 RA = pk2(rsqrt_p<float>(a0), rsqrt_p<float>(a1));
+                const u64 RB = pk2(rsqrt_p<float>(b0), rsqrt_p<float>(b1));
+                ACC[0][p] = fma2(AQ, RA, ACC[0][p]);
+                ACC[0][p] = fma2(BQ, RB, ACC[0][p]);
+                if constexpr (NQ == 2) {
+                    ACC[1][p] = fma2(AQ2, RA, ACC[1][p]);
+                    ACC[1][p] = fma2(BQ2, RB, ACC[1][p]);
+                }
+            }
+        }
+#pragma unroll
+        for (int p = 0; p < NP; p++)
+#pragma unroll
+            for (int k = 0; k < NQ; k++) NS[k][p] = add2(NS[k][p], ACC[k][p]);
+    }
+    // warp sums (fixed butterfly order), then FP64
+    double near[NQ][NT];
+#pragma unroll
+    for (int k = 0; k < NQ; k++)
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            float v0, v1;
+            upk2(NS[k][p], v0, v1);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                v0 += __shfl_xor_sync(0xffffffffu, v0, o);
+                v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+            }
+            near[k][2 * p] = double(v0);
+            near[k][2 * p + 1] = double(v1);
+        }
+    if (lane < nt) {
+        float x = 0, y = 0, z = 0;
+        double nr[NQ];
+#pragma unroll
+        for (int k = 0; k < NQ; k++) nr[k] = 0;
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            float x0, x1, y0, y1, z0, z1;
+            upk2(TX[p], x0, x1);
+            upk2(TY[p], y0, y1);
+            upk2(TZ[p], z0, z1);
+            if (2 * p == lane) {
+                x = x0; y = y0; z = z0;
+#pragma unroll
+                for (int k = 0; k < NQ; k++) nr[k] = near[k][2 * p];
+            }
+            if (2 * p + 1 == lane) {
+                x = x1; y = y1; z = z1;
+#pragma unroll
+                for (int k = 0; k < NQ; k++) nr[k] = near[k][2 * p + 1];
+            }
+        }
+        const float *__restrict__ Fa = sets.F[0] + fbase;
+        const float *__restrict__ Fb = sets.F[NQ - 1] + fbase;
+        float fa = 0, fb = 0;
+        ups_cols<float>(x, y, z, [&](int n, int m, float re, float im) {
+            if (m == 0) {
+                fa += Fa[ridx(n, 0, 0)] * re;
+                if constexpr (NQ == 2) fb += Fb[ridx(n, 0, 0)] * re;
+            } else {
+                fa += 2.f * (Fa[ridx(n, m, 0)] * re + Fa[ridx(n, m, 1)] * im);
+                if constexpr (NQ == 2) fb += 2.f * (Fb[ridx(n, m, 0)] * re + Fb[ridx(n, m, 1)] * im);
+            }
+        });
+        const double sc = leaf_scale[leaf];
+        const int node = tgt_node[tb + lane];
+        sets.pot[0][node] = (double(fa) + nr[0]) * sc;
+        if constexpr (NQ == 2) sets.pot[1][node] = (double(fb) + nr[NQ - 1]) * sc;
+    }
+}
+
 // L2P + P2P: one warp per target leaf, its targets in passes of 16 and a tail pass of 8
 // or 4 (a leaf of the film holds 18 to 64 nodes: fixed passes of 16 would spend about a
 // fifth of the pair work on padding).
@@ -507,19 +678,29 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? (NQ == 1 ? 4 : 3) : 2)
     const size_t fbase = (size_t)(leaf0 + leaf) * NR;
     for (int tb = t0; tb < t1;) {
         const int r = t1 - tb;
-        if (r > 8) {
-            l2p_p2p_pass<T, 16, NQ>(leaf, tb, min(16, r), lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk,
-                                    leaf_scale, near_ptr, near_leaf, fbase, sets);
-            tb += 16;
-        } else if (r > 4) {
-            l2p_p2p_pass<T, 8, NQ>(leaf, tb, r, lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk, leaf_scale,
-                                   near_ptr, near_leaf, fbase, sets);
-            tb += 8;
+        const int nt = r > 8 ? 16 : r > 4 ? 8 : 4;
+        if constexpr (sizeof(T) == 4) {
+            if (nt == 16)
+                l2p_p2p_pass_x2<16, NQ>(leaf, tb, min(16, r), lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc,
+                                        leaf_ijk, leaf_scale, near_ptr, near_leaf, fbase, sets);
+            else if (nt == 8)
+                l2p_p2p_pass_x2<8, NQ>(leaf, tb, r, lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk,
+                                       leaf_scale, near_ptr, near_leaf, fbase, sets);
+            else
+                l2p_p2p_pass_x2<4, NQ>(leaf, tb, r, lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk,
+                                       leaf_scale, near_ptr, near_leaf, fbase, sets);
         } else {
-            l2p_p2p_pass<T, 4, NQ>(leaf, tb, r, lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk, leaf_scale,
-                                   near_ptr, near_leaf, fbase, sets);
-            tb += 4;
+            if (nt == 16)
+                l2p_p2p_pass<T, 16, NQ>(leaf, tb, min(16, r), lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc,
+                                        leaf_ijk, leaf_scale, near_ptr, near_leaf, fbase, sets);
+            else if (nt == 8)
+                l2p_p2p_pass<T, 8, NQ>(leaf, tb, r, lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk,
+                                       leaf_scale, near_ptr, near_leaf, fbase, sets);
+            else
+                l2p_p2p_pass<T, 4, NQ>(leaf, tb, r, lane, li, lj, lk, leaf_src, tgt_node, tloc, sloc, leaf_ijk,
+                                       leaf_scale, near_ptr, near_leaf, fbase, sets);
         }
+        tb += nt;
     }
 }
 
