@@ -682,7 +682,10 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
     c.launches += 2;
     h->last_c0 = prefactor * FG_THETA * dt * FG_GAMMA0;
     const bool use_mlp = c.mlp && mlp_steps(c) >= c.opts.mlp_train_steps;
-    if (c.mlp) CK(mlp_before_solve(c, h->last_c0, use_mlp));
+    const int train_every = std::max(1, c.opts.mlp_train_every);
+    // a successful solve of this step trains the guess (features kept from before the solve)
+    const bool will_train = !use_mlp || h->solves_since_train + 1 >= train_every;
+    if (c.mlp) CK(mlp_before_solve(c, h->last_c0, use_mlp, will_train));
     CK(cudaEventRecord(c.ev[1], c.stream));
     if (c.opts.precision == FG_PREC_FP32_REFINE) CK(launch_mixed(c, dt, prefactor));
     else CK(launch_bicg64(c, dt, prefactor));
@@ -704,8 +707,8 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
         if (!use_mlp) { r0m = r.res0; r0p = r.res0; }
         // train on this step's solution (asynchronous; its loss is read at the next sync)
         if (status == FG_OK) {
-            const int every = std::max(1, c.opts.mlp_train_every);
-            if (!use_mlp || (++h->solves_since_train) >= every) {
+            ++h->solves_since_train;
+            if (will_train) {
                 h->solves_since_train = 0;
                 CK(mlp_train(c));
             }

@@ -298,7 +298,7 @@ void translate_tc_units(int n_out, int ncode, const int *tab, int out0, int max_
 int fmm_stage_ms(const Ctx &c, double ms[5]);
 int mlp_create(Ctx &c);
 void mlp_free(Ctx &c);
-cudaError_t mlp_before_solve(Ctx &c, double c0, bool use);
+cudaError_t mlp_before_solve(Ctx &c, double c0, bool use, bool train);
 cudaError_t mlp_train(Ctx &c);
 void mlp_after_sync(Ctx &c, int *accepted, double *res0_mlp, double *res0_prev, double *loss);
 long long mlp_steps(const Ctx &c);

@@ -28,6 +28,9 @@ namespace fg {
 
 __constant__ double c_ta[4][5];   // tet shape functions at Gauss points (src/tetra.h:50-80)
 __constant__ double c_tpds[5];
+__constant__ double c_cw[4][5];   // c_ta[i][g] * c_tpds[g]: weight of vertex i at Gauss point g per unit detJ
+__constant__ double c_cws[4];     // sum_g c_cw[i][g]
+__constant__ double c_tps;        // sum_g c_tpds[g]
 __constant__ double c_fa[3][4];   // triangle rule (src/triangle.h:42-64)
 __constant__ double c_fpds[4];
 
@@ -241,33 +244,32 @@ __global__ void __launch_bounds__(128) k_tet64_iso(int nmt, const int4 *__restri
     const double reduced_dt = FG_GAMMA0 * dt;
     const double M = 2. * alpha * 0.1 / reduced_dt;
     const double kv = FG_THETA * dt;  // s_dt / gamma0
-    double w[NPI], aw[4] = {0, 0, 0, 0}, contrib[4] = {0, 0, 0, 0}, vol = 0.0;
+    // calc_alpha_eff (src/tetra.cpp:47-75): alpha + (reduced_dt / 2) min(h, M) for h > 0,
+    // alpha / (1 - reduced_dt / (2 alpha) max(h, -M)) otherwise
+    const double half_rdt = reduced_dt / 2., k2 = reduced_dt / (2. * alpha);
+    const double hx = -Abis * gradsq;
+    // sum_g w_g a_i(g) aeff(g) with w_g = J tpds_g: the vertex weights c_cw = a_i(g) tpds_g
+    // are constants, so J multiplies once
+    double contrib[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int g = 0; g < NPI; g++) {
-        w[g] = J * c_tpds[g];
-        vol += w[g];
-        const double h = -Abis * gradsq + c_ta[0][g] * uh[0] + c_ta[1][g] * uh[1] + c_ta[2][g] * uh[2] + c_ta[3][g] * uh[3];
-        double a;
-        if (h > 0.0)
-            a = (h > M) ? alpha + reduced_dt / 2. * M : alpha + reduced_dt / 2. * h;
-        else
-            a = (h < -M) ? alpha / (1. + reduced_dt / (2. * alpha) * M) : alpha / (1. - reduced_dt / (2. * alpha) * h);
+        const double h = hx + c_ta[0][g] * uh[0] + c_ta[1][g] * uh[1] + c_ta[2][g] * uh[2] + c_ta[3][g] * uh[3];
+        const double a = (h > 0.0) ? alpha + half_rdt * fmin(h, M) : alpha / (1. - k2 * fmax(h, -M));
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            aw[i] += c_ta[i][g] * w[g];
-            contrib[i] += c_ta[i][g] * w[g] * a;
-        }
+        for (int i = 0; i < 4; i++) contrib[i] += c_cw[i][g] * a;
     }
+    const double vol = J * c_tps, nva = -vol * Abis;
     const double H[3] = {He[0] + kv * Hv[0], He[1] + kv * Hv[1], He[2] + kv * Hv[2]};
 #pragma unroll
     for (int i = 0; i < 4; i++) {
+        const double aw = J * c_cws[i];
         double BE[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             const double ex = d[i][0] * dU[0][c] + d[i][1] * dU[1][c] + d[i][2] * dU[2][c];
-            BE[c] = -vol * Abis * ex + aw[i] * H[c];
+            BE[c] = nva * ex + aw * H[c];
         }
-        slot[4 * (size_t)t + i] = make_double4(contrib[i], BE[0], BE[1], BE[2]);
+        slot[4 * (size_t)t + i] = make_double4(J * contrib[i], BE[0], BE[1], BE[2]);
     }
 }
 
@@ -896,6 +898,16 @@ void upload_rules(bool one_point) {
     }
     cudaMemcpyToSymbol(c_ta, ta, sizeof(ta));
     cudaMemcpyToSymbol(c_tpds, tp, sizeof(tp));
+    double cw[4][5] = {}, cws[4] = {}, tps = 0.0;
+    for (int j = 0; j < 5; j++) tps += tp[j];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 5; j++) {
+            cw[i][j] = ta[i][j] * tp[j];
+            cws[i] += cw[i][j];
+        }
+    cudaMemcpyToSymbol(c_cw, cw, sizeof(cw));
+    cudaMemcpyToSymbol(c_cws, cws, sizeof(cws));
+    cudaMemcpyToSymbol(c_tps, &tps, sizeof(tps));
     cudaMemcpyToSymbol(c_fa, fa, sizeof(fa));
     cudaMemcpyToSymbol(c_fpds, fp, sizeof(fp));
 }

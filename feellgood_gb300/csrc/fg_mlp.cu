@@ -52,7 +52,34 @@ struct MlpState {
 
 __device__ __forceinline__ float bf(const __nv_bfloat16 *w, int k) { return __bfloat162float(w[k]); }
 
-// Features of every node (magnetic nodes; others get zeros).
+// Features of node i (magnetic nodes; others get zeros).
+__device__ __forceinline__ void node_features(int i, const unsigned char *__restrict__ mag,
+                                              const double *__restrict__ u0, const double *__restrict__ heff,
+                                              const double *__restrict__ vprev, const int *__restrict__ Sptr,
+                                              const int *__restrict__ Scol, double inv_ms, double inv_v0,
+                                              float (&f)[NF]) {
+#pragma unroll
+    for (int k = 0; k < NF; k++) f[k] = 0.0f;
+    if (!mag[i]) return;
+    double mb[3] = {0, 0, 0};
+    int deg = 0;
+    for (int k = Sptr[i]; k < Sptr[i + 1]; k++) {
+        const int j = Scol[k];
+        if (j == i) continue;
+        mb[0] += u0[3 * j]; mb[1] += u0[3 * j + 1]; mb[2] += u0[3 * j + 2];
+        deg++;
+    }
+    const double id = deg ? 1.0 / deg : 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        f[c] = (float)u0[3 * i + c];
+        f[3 + c] = (float)(heff[3 * i + c] * inv_ms);
+        f[6 + c] = (float)(vprev[3 * i + c] * inv_v0);
+        f[9 + c] = (float)(mb[c] * id);
+    }
+}
+
+// Features of every node, for the training of a step that runs no inference.
 __global__ void k_features(int nn, const unsigned char *__restrict__ mag, const double *__restrict__ u0,
                            const double *__restrict__ heff, const double *__restrict__ vprev,
                            const int *__restrict__ Sptr, const int *__restrict__ Scol, double inv_ms,
@@ -60,64 +87,59 @@ __global__ void k_features(int nn, const unsigned char *__restrict__ mag, const 
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
     float f[NF];
-#pragma unroll
-    for (int k = 0; k < NF; k++) f[k] = 0.0f;
-    if (mag[i]) {
-        double mb[3] = {0, 0, 0};
-        int deg = 0;
-        for (int k = Sptr[i]; k < Sptr[i + 1]; k++) {
-            const int j = Scol[k];
-            if (j == i) continue;
-            mb[0] += u0[3 * j]; mb[1] += u0[3 * j + 1]; mb[2] += u0[3 * j + 2];
-            deg++;
-        }
-        const double id = deg ? 1.0 / deg : 0.0;
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            f[c] = (float)u0[3 * i + c];
-            f[3 + c] = (float)(heff[3 * i + c] * inv_ms);
-            f[6 + c] = (float)(vprev[3 * i + c] * inv_v0);
-            f[9 + c] = (float)(mb[c] * id);
-        }
-    }
+    node_features(i, mag, u0, heff, vprev, Sptr, Scol, inv_ms, inv_v0, f);
 #pragma unroll
     for (int k = 0; k < NF; k++) feat[(size_t)i * NF + k] = f[k];
 }
 
-// Inference: one thread per node, weights staged in shared memory as FP32 (from BF16).
-// Writes the candidate x (2 per node) and its tangent vectors W.
+// tanh on the SFU (tanh.approx.f32, relative error about 2^-11): the guess only has to be
+// good, the referee below decides on its FP64 residual.
+__device__ __forceinline__ float tanh_sfu(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Inference: one thread per node, features formed in place (and stored for the training
+// when feat is given), weights staged in shared memory as FP32 (from BF16). Writes the
+// candidate x (2 per node) and its tangent vectors W.
 __global__ void __launch_bounds__(256) k_mlp_infer(int nn, const unsigned char *__restrict__ mag,
-                                                   const float *__restrict__ feat,
+                                                   const double *__restrict__ u0, const double *__restrict__ heff,
+                                                   const int *__restrict__ Sptr, const int *__restrict__ Scol,
+                                                   double inv_ms, double inv_v0, float *__restrict__ feat,
                                                    const __nv_bfloat16 *__restrict__ w, const double *__restrict__ ep,
                                                    const double *__restrict__ eq, const double *__restrict__ vprev,
                                                    const double *__restrict__ vprev2, const double *__restrict__ scale,
                                                    double *__restrict__ xm, double *__restrict__ Wm) {
-    __shared__ float sw[NPARAM];
+    __shared__ __align__(16) float sw[NPARAM];
     for (int k = threadIdx.x; k < NPARAM; k += blockDim.x) sw[k] = bf(w, k);
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
+    float x[NF];
+    node_features(i, mag, u0, heff, vprev, Sptr, Scol, inv_ms, inv_v0, x);
+    if (feat)
+#pragma unroll
+        for (int k = 0; k < NF; k++) feat[(size_t)i * NF + k] = x[k];
     if (!mag[i]) {
         xm[2 * i] = xm[2 * i + 1] = 0.0;
         Wm[3 * i] = Wm[3 * i + 1] = Wm[3 * i + 2] = 0.0;
         return;
     }
-    float x[NF], h1[NH];
-#pragma unroll
-    for (int k = 0; k < NF; k++) x[k] = feat[(size_t)i * NF + k];
+    float h1[NH];
 #pragma unroll
     for (int j = 0; j < NH; j++) {
         float z = sw[OFF_B1 + j];
 #pragma unroll
         for (int k = 0; k < NF; k++) z += sw[OFF_W1 + j * NF + k] * x[k];
-        h1[j] = tanhf(z);
+        h1[j] = tanh_sfu(z);
     }
     float o0 = sw[OFF_B3], o1 = sw[OFF_B3 + 1], o2 = sw[OFF_B3 + 2];
     for (int j = 0; j < NH; j++) {
         float z = sw[OFF_B2 + j];
 #pragma unroll
         for (int k = 0; k < NH; k++) z += sw[OFF_W2 + j * NH + k] * h1[k];
-        const float h2 = tanhf(z);
+        const float h2 = tanh_sfu(z);
         o0 += sw[OFF_W3 + j] * h2;
         o1 += sw[OFF_W3 + NH + j] * h2;
         o2 += sw[OFF_W3 + 2 * NH + j] * h2;
@@ -444,20 +466,26 @@ void mlp_free(Ctx &c) {
 
 static double v0_scale(const Ctx &c) { return FG_GAMMA0 * c.ms_ref; }
 
-// Features of the current state; with use != 0 also the candidate guess and the decision
-// against the fallback guess already in c.x (writes c.x / c.W when the candidate wins).
-cudaError_t mlp_before_solve(Ctx &c, double c0, bool use) {
+// With use != 0 the candidate guess and the decision against the fallback guess already in
+// c.x (writes c.x / c.W when the candidate wins); the features of the current state are
+// stored for the training when train is set (formed inside the inference when it runs).
+cudaError_t mlp_before_solve(Ctx &c, double c0, bool use, bool train) {
     MlpState *s = static_cast<MlpState *>(c.mlp);
-    k_features<<<nb(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.mag, c.u[0], c.heff, c.v[1], c.Sptr, c.Scol,
-                                                      1.0 / c.ms_ref, 1.0 / v0_scale(c), s->feat);
-    c.launches += 1;
-    if (!use) return cudaGetLastError();
+    if (!use) {
+        if (train) {
+            k_features<<<nb(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.mag, c.u[0], c.heff, c.v[1], c.Sptr, c.Scol,
+                                                              1.0 / c.ms_ref, 1.0 / v0_scale(c), s->feat);
+            c.launches += 1;
+        }
+        return cudaGetLastError();
+    }
     if (!s->primed) {  // no history yet: the extrapolation degenerates to v_prev
         cudaMemcpyAsync(s->vprev2, c.v[0], 3 * (size_t)c.nn * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
         s->primed = true;
     }
-    k_mlp_infer<<<nb(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.mag, s->feat, s->w, c.ep, c.eq, c.v[0], s->vprev2,
-                                                      s->scale, s->xm, s->Wm);
+    k_mlp_infer<<<nb(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.mag, c.u[0], c.heff, c.Sptr, c.Scol, 1.0 / c.ms_ref,
+                                                      1.0 / v0_scale(c), train ? s->feat : nullptr, s->w, c.ep, c.eq,
+                                                      c.v[0], s->vprev2, s->scale, s->xm, s->Wm);
     k_resid2<<<s->nblk_res, 256, 0, c.stream>>>(c.nn, c.Sptr, c.Scol, c.Sval, c.ep, c.eq, c.A, c.Dl, c.mag, c0,
                                                 c.rhs, s->xm, s->Wm, c.x, c.W, s->rpart);
     k_choose<<<1, 32, 0, c.stream>>>(s->nblk_res, s->rpart, s->flag, s->res2);
