@@ -116,6 +116,9 @@ SIGNATURES = {
     "fg_mlp_nparam": (C.c_int, []),
     "fg_solver_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "fg_debug_wait_timeout": (C.c_int, [C.c_void_p, C.c_int]),
+    "fg_gauss_points": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
+    "fg_set_space_field": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fg_set_field_amplitude": (C.c_int, [C.c_void_p, C.c_double]),
     "fg_debug_translate_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_int]),
     "fg_batch_create": (C.c_int, [C.POINTER(fg_mesh), C.c_int, C.POINTER(fg_region), C.c_int,
@@ -388,6 +391,26 @@ class Context:
         v = C.c_int()
         self._check(self.L.fg_solver_info(self.h, C.byref(v), None))
         return v.value
+
+    def gauss_points(self):
+        """fg_gauss_points: coordinates of the magnetic tets' Gauss points, (n_mag_tets * npi, 3)."""
+        n = C.c_int()
+        self._check(self.L.fg_gauss_points(self.h, C.byref(n), None))
+        pts = np.zeros((n.value, 3))
+        self._check(self.L.fg_gauss_points(self.h, C.byref(n), _ptr(pts)))
+        return pts
+
+    def set_space_field(self, field):
+        """fg_set_space_field: f at the Gauss points (same rows as gauss_points()), or None."""
+        if field is None:
+            self._check(self.L.fg_set_space_field(self.h, None))
+            return
+        f = np.ascontiguousarray(field, dtype=np.float64)
+        self._check(self.L.fg_set_space_field(self.h, _ptr(f)))
+
+    def set_field_amplitude(self, a):
+        """fg_set_field_amplitude: A(t) of the space field for the next steps."""
+        self._check(self.L.fg_set_field_amplitude(self.h, float(a)))
 
     def solver_blocks(self):
         v = C.c_int()

@@ -439,6 +439,12 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     CK(upload(&c.tri_c, htc));
     CK(upload(&c.tinc_ptr, tinc_ptr));
     CK(upload(&c.tinc, tinc));
+    bool surf_aniso = false;
+    for (const DevTri &T : htc) surf_aniso = surf_aniso || T.Ks != 0.0;
+    if (surf_aniso && c.nft > 0) {
+        CK(dalloc(&c.tri_be, 9 * (size_t)c.nft));
+        CK(cudaMemset(c.tri_be, 0, 9 * sizeof(double) * c.nft));
+    }
     CK(upload(&c.src_xyz, sxyz));
     c.h_src_xyz = std::move(sxyz);
     CK(upload(&c.mag_nodes, mnodes));
@@ -618,7 +624,7 @@ void fg_destroy(fg_ctx *h) {
                     c.Sval32, c.A, c.A32, c.tri, c.tri_c, c.tinc_ptr, c.tinc, c.src_xyz, c.mag_nodes, c.u[0], c.u[1],
                     c.v[0], c.v[1], c.phi[0], c.phi[1], c.phiv[0], c.phiv[1], c.ep, c.eq, c.ep32, c.eq32, c.Dl32,
                     c.slot, c.Dl, c.rhs, c.x, c.bv, c.W, c.fv, c.partial, c.bar, c.dres, c.src_q, c.tri_slot,
-                    c.pot, c.epart, c.src_dst, c.src_q2, c.tri_slot2, c.pot2};
+                    c.pot, c.epart, c.src_dst, c.src_q2, c.tri_slot2, c.pot2, c.tri_be, c.hsp};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     fmm_free(c);
@@ -773,12 +779,11 @@ static int demag_pair(fg_ctx *h) {
         if (s == FG_OK) s = demag_into(h, c.v[1], c.phiv[1]);
         return s;
     }
-    CK(launch_charges(c, c.u[1], 0));
-    CK(launch_charges(c, c.v[1], 1));
+    CK(launch_charges_pair(c, c.u[1], c.v[1]));
     CK(fmm_eval(c, 2));
     CK(launch_phi_final(c, c.phi[1], 0));
     CK(launch_phi_final(c, c.phiv[1], 1));
-    c.launches += 4 + fmm_launches_per_eval(c, 2);
+    c.launches += 3 + fmm_launches_per_eval(c, 2);
     return FG_OK;
 }
 
@@ -931,6 +936,40 @@ int fg_debug_wait_timeout(fg_ctx *h, int which) {
         c.err = which == 0 ? "grid barrier: bounded wait expired" : "mbarrier: bounded wait expired";
         return FG_ETIMEDOUT;
     }
+    return FG_OK;
+}
+
+int fg_gauss_points(const fg_ctx *h, int *n_points, double *pts) {
+    if (!h || !n_points) return FG_EINVAL;
+    const Ctx &c = h->c;
+    const size_t n = (size_t)c.nmt * c.npi_t;
+    *n_points = (int)n;
+    // the tet sources are the magnetic tets' Gauss points, in magnetic-tet order
+    if (pts) std::memcpy(pts, c.h_src_xyz.data(), 3 * n * sizeof(double));
+    return FG_OK;
+}
+
+int fg_set_space_field(fg_ctx *h, const double *field) {
+    if (!h) return FG_EINVAL;
+    Ctx &c = h->c;
+    if (c.batch) {
+        c.err = "fg_set_space_field: not available for batch contexts";
+        return FG_EINVAL;
+    }
+    if (!field) {
+        if (c.hsp) cudaFree(c.hsp);
+        c.hsp = nullptr;
+        return FG_OK;
+    }
+    const size_t n = 3 * (size_t)c.nmt * c.npi_t;
+    if (!c.hsp) CK(dalloc(&c.hsp, std::max<size_t>(n, 1)));
+    CK(cudaMemcpy(c.hsp, field, n * sizeof(double), cudaMemcpyHostToDevice));
+    return FG_OK;
+}
+
+int fg_set_field_amplitude(fg_ctx *h, double amplitude) {
+    if (!h || !std::isfinite(amplitude)) return FG_EINVAL;
+    h->c.field_amp = amplitude;
     return FG_OK;
 }
 

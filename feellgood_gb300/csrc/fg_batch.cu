@@ -206,8 +206,7 @@ static void fill_par(SegPar &P, const fg_sample_step &s) {
 // Demag of m (and of v beside it, one FMM evaluation of both charge sets).
 static cudaError_t batch_demag_all(Ctx &c) {
     const int nq = c.opts.first_order ? 1 : 2;
-    cudaError_t e = launch_charges(c, c.u[1], 0);
-    if (e == cudaSuccess && nq == 2) e = launch_charges(c, c.v[1], 1);
+    cudaError_t e = nq == 2 ? launch_charges_pair(c, c.u[1], c.v[1]) : launch_charges(c, c.u[1], 0);
     if (e == cudaSuccess) e = fmm_eval(c, nq);
     if (e == cudaSuccess) e = launch_phi_final(c, c.phi[1], 0);
     if (e == cudaSuccess && nq == 2) e = launch_phi_final(c, c.phiv[1], 1);
@@ -216,7 +215,7 @@ static cudaError_t batch_demag_all(Ctx &c) {
 
 static int demag_launches(const Ctx &c) {
     const int nq = c.opts.first_order ? 1 : 2;
-    return 2 * nq + fmm_launches_per_eval(c, nq);
+    return 1 + nq + fmm_launches_per_eval(c, nq);
 }
 
 // Stream-ordered body of one step of a run (the graph is a capture of exactly this).

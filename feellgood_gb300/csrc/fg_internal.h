@@ -196,6 +196,11 @@ struct Ctx {
     double *src_q2 = nullptr;    // charges of v (demag of m and v evaluated together), or nullptr
     double *tri_slot = nullptr;  // 3 x nft corrections
     double *tri_slot2 = nullptr; // 3 x nft corrections of src_q2
+    double *tri_be = nullptr;    // 9 x nft surface-anisotropy BE per (triangle, vertex), or nullptr (all Ks = 0)
+    // space-dependent applied field (the reference's R4toR3 field type): H(g) = Hext + amp F(g)
+    // at every Gauss point g of every magnetic tet; F is [nmt][npi_t][3] or nullptr
+    double *hsp = nullptr;
+    double field_amp = 1.0;
     double *pot = nullptr;       // nn
     double *pot2 = nullptr;      // nn, potential of src_q2
     double *epart = nullptr;     // energy partials
@@ -248,6 +253,7 @@ cudaError_t launch_mixed(Ctx &c, double dt, double prefactor);
 cudaError_t launch_apply(Ctx &c, double c0, const double *x, double *y);
 // set 0: charges into src_q / tri_slot, potential from pot; set 1: src_q2 / tri_slot2 / pot2
 cudaError_t launch_charges(Ctx &c, const double *m, int set = 0);
+cudaError_t launch_charges_pair(Ctx &c, const double *m, const double *v);  // sets 0 and 1 in one pass
 cudaError_t launch_p2p_direct(Ctx &c);
 cudaError_t launch_phi_final(Ctx &c, double *phi_out, int set = 0);
 cudaError_t launch_energy(Ctx &c, const double Hext[3]);

@@ -46,7 +46,8 @@ __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__
                                                const double *__restrict__ v0, const double *__restrict__ phi0,
                                                const double *__restrict__ phiv0, double dt, double Hx, double Hy,
                                                double Hz, double4 *__restrict__ slot,
-                                               const int *__restrict__ tet_seg, const SegPar *__restrict__ seg) {
+                                               const int *__restrict__ tet_seg, const SegPar *__restrict__ seg,
+                                               const double *__restrict__ hsp, double amp) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nmt) return;
     if (seg) {  // batch: the tet's sample carries dt and the applied field
@@ -149,7 +150,12 @@ __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__
             }
             uHeff += -R.K3bis * (ku[0] * uuu[0] + ku[1] * uuu[1] + ku[2] * uuu[2]);
         }
-        uHeff += U[0] * He[0] + U[1] * He[1] + U[2] * He[2];
+        double Hg[3] = {He[0], He[1], He[2]};
+        if (hsp) {  // space-dependent applied field at this Gauss point (R4toR3)
+            const double *F = hsp + 3 * ((size_t)t * NPI + g);
+            Hg[0] += amp * F[0]; Hg[1] += amp * F[1]; Hg[2] += amp * F[2];
+        }
+        uHeff += U[0] * Hg[0] + U[1] * Hg[1] + U[2] * Hg[2];
         // calc_alpha_eff (src/tetra.cpp:47-75)
         double a;
         if (uHeff > 0.0)
@@ -160,7 +166,7 @@ __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__
         aeff[g] = a;
         const double kv = s_dt / FG_GAMMA0;
 #pragma unroll
-        for (int c = 0; c < 3; c++) H[g][c] = He[c] + Han[c] + kv * Hv[c];
+        for (int c = 0; c < 3; c++) H[g][c] = Hg[c] + Han[c] + kv * Hv[c];
     }
 #pragma unroll
     for (int i = 0; i < 4; i++) {
@@ -197,7 +203,8 @@ __global__ void __launch_bounds__(128) k_tet64_iso(int nmt, const int4 *__restri
                                                    const double *__restrict__ phi0, const double *__restrict__ phiv0,
                                                    double dt, double Hx, double Hy, double Hz,
                                                    double4 *__restrict__ slot, const int *__restrict__ tet_seg,
-                                                   const SegPar *__restrict__ seg) {
+                                                   const SegPar *__restrict__ seg, const double *__restrict__ hsp,
+                                                   double amp) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nmt) return;
     if (seg) {
@@ -251,9 +258,24 @@ __global__ void __launch_bounds__(128) k_tet64_iso(int nmt, const int4 *__restri
     // sum_g w_g a_i(g) aeff(g) with w_g = J tpds_g: the vertex weights c_cw = a_i(g) tpds_g
     // are constants, so J multiplies once
     double contrib[4] = {0, 0, 0, 0};
+    // space-dependent applied field (R4toR3): amp F(g) adds U(g) . amp F(g) to uHeff(g) and
+    // sum_g w_g a_i(g) amp F(g) to BE_i
+    double fw[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
 #pragma unroll
     for (int g = 0; g < NPI; g++) {
-        const double h = hx + c_ta[0][g] * uh[0] + c_ta[1][g] * uh[1] + c_ta[2][g] * uh[2] + c_ta[3][g] * uh[3];
+        double h = hx + c_ta[0][g] * uh[0] + c_ta[1][g] * uh[1] + c_ta[2][g] * uh[2] + c_ta[3][g] * uh[3];
+        if (hsp) {
+            const double *F = hsp + 3 * ((size_t)t * NPI + g);
+            double U[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+                U[c] = c_ta[0][g] * un[0][c] + c_ta[1][g] * un[1][c] + c_ta[2][g] * un[2][c] + c_ta[3][g] * un[3][c];
+            h += amp * (U[0] * F[0] + U[1] * F[1] + U[2] * F[2]);
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) fw[i][c] += c_cw[i][g] * F[c];
+        }
         const double a = (h > 0.0) ? alpha + half_rdt * fmin(h, M) : alpha / (1. - k2 * fmax(h, -M));
 #pragma unroll
         for (int i = 0; i < 4; i++) contrib[i] += c_cw[i][g] * a;
@@ -268,9 +290,48 @@ __global__ void __launch_bounds__(128) k_tet64_iso(int nmt, const int4 *__restri
         for (int c = 0; c < 3; c++) {
             const double ex = d[i][0] * dU[0][c] + d[i][1] * dU[1][c] + d[i][2] * dU[2][c];
             BE[c] = nva * ex + aw * H[c];
+            if (hsp) BE[c] += (amp * J) * fw[i][c];
         }
         slot[4 * (size_t)t + i] = make_double4(J * contrib[i], BE[0], BE[1], BE[2]);
     }
+}
+
+// Surface anisotropy of the magnetic triangles, Tri::integrales (src/triangle.cpp:6-36):
+// BE(k, i) = sum_g w_g Kbis (uk . u(g)) a_i(g) uk_k with Kbis = 2 Ks / dMs, u of CURRENT;
+// written per (triangle, vertex) beside the tet slots and gathered by the node kernel
+// (zero for triangles of regions with Ks = 0, which the reference skips).
+template <int NPF>
+__global__ void k_tri_aniso(int nft, const int4 *__restrict__ tri, const DevTri *__restrict__ tc,
+                            const double *__restrict__ u0, double *__restrict__ tri_be) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nft) return;
+    const DevTri &T = tc[f];
+    double BE[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    if (T.Ks != 0.0) {
+        const int4 I = tri[f];
+        const int ind[3] = {I.x, I.y, I.z};
+        const double Kbis = 2.0 * T.Ks / T.dMs;
+#pragma unroll
+        for (int g = 0; g < NPF; g++) {
+            double U[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                double s = 0.0;
+#pragma unroll
+                for (int i = 0; i < 3; i++) s += c_fa[i][g] * u0[3 * (size_t)ind[i] + c];
+                U[c] = s;
+            }
+            const double pre = T.w[g] * Kbis * (T.uk[0] * U[0] + T.uk[1] * U[1] + T.uk[2] * U[2]);
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int k = 0; k < 3; k++) BE[i][k] += pre * c_fa[i][g] * T.uk[k];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) tri_be[9 * (size_t)f + 3 * i + k] = BE[i][k];
 }
 
 // ---------------------------------------------------------------------------------
@@ -280,7 +341,9 @@ __global__ void __launch_bounds__(128) k_tet64_iso(int nmt, const int4 *__restri
 // (src/linear_algebra.cpp:13-24: previous v on the new basis / gamma0).
 
 __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
-                         const double4 *__restrict__ slot, const unsigned char *__restrict__ mag,
+                         const double4 *__restrict__ slot, const int *__restrict__ tinc_ptr,
+                         const int *__restrict__ tinc, const double *__restrict__ tri_be,
+                         const unsigned char *__restrict__ mag,
                          const double *__restrict__ A, const double *__restrict__ u0, const double *__restrict__ v1,
                          double cr, double sr, double *__restrict__ ep, double *__restrict__ eq,
                          double *__restrict__ Dl, double *__restrict__ rhs, double *__restrict__ x,
@@ -324,6 +387,11 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
         const double4 s = slot[inc[k]];
         dl += s.x; be0 += s.y; be1 += s.z; be2 += s.w;
     }
+    if (tri_be)  // surface anisotropy of the adjacent magnetic triangles (Tri::integrales)
+        for (int k = tinc_ptr[i]; k < tinc_ptr[i + 1]; k++) {
+            const double *b = tri_be + 3 * (size_t)tinc[k];
+            be0 += b[0]; be1 += b[1]; be2 += b[2];
+        }
     Dl[i] = dl;
     if (heff) {  // effective field BE_i / A_i, a feature of the learned guess
         const double ia = mag[i] ? 1.0 / A[i] : 0.0;
@@ -600,50 +668,64 @@ __global__ void k_apply64(int nn, const int *Sptr, const int *Scol, const double
 // self-corrections of Tri::correctionCharges + Tri::potential (src/triangle.cpp:45-125),
 // in the source order of fmm::calc_charges (src/fmm_demag.h:155-179).
 
-template <int NPI, int NPF>
+template <int NPI, int NPF, int NQ>
 __global__ void k_charges(int nmt, int nft, const int4 *__restrict__ tet, const double *__restrict__ da,
                           const double *__restrict__ detJ, const int *__restrict__ treg,
                           const DevRegion *__restrict__ regs, const int4 *__restrict__ tri,
-                          const DevTri *__restrict__ tc, const double *__restrict__ m,
-                          const int *__restrict__ dst, double *__restrict__ q, double *__restrict__ tri_slot) {
+                          const DevTri *__restrict__ tc, const double *__restrict__ m0, const double *__restrict__ m1,
+                          const int *__restrict__ dst, double *__restrict__ q0, double *__restrict__ q1,
+                          double *__restrict__ ts0, double *__restrict__ ts1) {
+    // NQ = 2: the charges of two fields (m and v) from one pass over the geometry
+    const double *mm[2] = {m0, m1};
+    double *qq[2] = {q0, q1}, *ts[2] = {ts0, ts1};
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < nmt) {
         const int4 I = tet[k];
         const int ind[4] = {I.x, I.y, I.z, I.w};
-        double dud = 0.0;
+        double d[4][3];
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const double *pm = m + 3 * (size_t)ind[i];
-            dud += pm[0] * da[(3 * i) * (size_t)nmt + k] + pm[1] * da[(3 * i + 1) * (size_t)nmt + k] +
-                   pm[2] * da[(3 * i + 2) * (size_t)nmt + k];
-        }
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) d[i][c] = da[(3 * i + c) * (size_t)nmt + k];
         const double Ms = regs[treg[k]].Ms, J = detJ[k];
 #pragma unroll
-        for (int g = 0; g < NPI; g++) {
-            const size_t s = (size_t)k * NPI + g;
-            q[dst ? dst[s] : s] = -Ms * (J * c_tpds[g]) * dud;
+        for (int f = 0; f < NQ; f++) {
+            double dud = 0.0;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const double *pm = mm[f] + 3 * (size_t)ind[i];
+                dud += pm[0] * d[i][0] + pm[1] * d[i][1] + pm[2] * d[i][2];
+            }
+#pragma unroll
+            for (int g = 0; g < NPI; g++) {
+                const size_t s = (size_t)k * NPI + g;
+                qq[f][dst ? dst[s] : s] = -Ms * (J * c_tpds[g]) * dud;
+            }
         }
     } else if (k < nmt + nft) {
         const int f = k - nmt;
         const int4 I = tri[f];
         const int ind[3] = {I.x, I.y, I.z};
         const DevTri &T = tc[f];
-        double s[3];
 #pragma unroll
-        for (int i = 0; i < 3; i++) {
-            const double *pm = m + 3 * (size_t)ind[i];
-            s[i] = pm[0] * T.n[0] + pm[1] * T.n[1] + pm[2] * T.n[2];
+        for (int h = 0; h < NQ; h++) {
+            double s[3];
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                const double *pm = mm[h] + 3 * (size_t)ind[i];
+                s[i] = pm[0] * T.n[0] + pm[1] * T.n[1] + pm[2] * T.n[2];
+            }
+#pragma unroll
+            for (int g = 0; g < NPF; g++) {
+                double un = c_fa[0][g] * s[0] + c_fa[1][g] * s[1] + c_fa[2][g] * s[2];
+                const size_t sidx = (size_t)nmt * NPI + (size_t)f * NPF + g;
+                qq[h][dst ? dst[sidx] : sidx] = (T.dMs != 0.0) ? T.dMs * T.w[g] * un : 0.0;
+            }
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+                ts[h][3 * (size_t)f + i] =
+                    T.dMs * (T.beta[3 * i] * s[0] + T.beta[3 * i + 1] * s[1] + T.beta[3 * i + 2] * s[2]);
         }
-#pragma unroll
-        for (int g = 0; g < NPF; g++) {
-            double un = c_fa[0][g] * s[0] + c_fa[1][g] * s[1] + c_fa[2][g] * s[2];
-            const size_t sidx = (size_t)nmt * NPI + (size_t)f * NPF + g;
-            q[dst ? dst[sidx] : sidx] = (T.dMs != 0.0) ? T.dMs * T.w[g] * un : 0.0;
-        }
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-            tri_slot[3 * (size_t)f + i] =
-                T.dMs * (T.beta[3 * i] * s[0] + T.beta[3 * i + 1] * s[1] + T.beta[3 * i + 2] * s[2]);
     }
 }
 
@@ -704,7 +786,8 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
                                                 const double *__restrict__ u, const double *__restrict__ phi,
                                                 double Hx, double Hy, double Hz, double *__restrict__ partial,
                                                 const int4 *__restrict__ blk_rng, const int *__restrict__ blk_seg,
-                                                const double *__restrict__ segH) {
+                                                const double *__restrict__ segH, const double *__restrict__ hsp,
+                                                double amp) {
     double acc[7] = {0, 0, 0, 0, 0, 0, 0};
     // default: grid-stride over all elements; batch: this block's ranges of one sample
     int stride = gridDim.x * blockDim.x, t0 = blockIdx.x * blockDim.x + threadIdx.x, t1 = nmt;
@@ -800,7 +883,12 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
                 const double a2 = U[0] * R.ez[0] + U[1] * R.ez[1] + U[2] * R.ez[2];
                 cub += w * ((a0 * a1) * (a0 * a1) + (a1 * a2) * (a1 * a2) + (a2 * a0) * (a2 * a0));
             }
-            ze += w * (U[0] * Hx + U[1] * Hy + U[2] * Hz);
+            if (hsp) {  // Tet::zeemanEnergy with the space field (src/tetra.cpp:381-390)
+                const double *F = hsp + 3 * ((size_t)k * NPI + g);
+                ze += w * (U[0] * (Hx + amp * F[0]) + U[1] * (Hy + amp * F[1]) + U[2] * (Hz + amp * F[2]));
+            } else {
+                ze += w * (U[0] * Hx + U[1] * Hy + U[2] * Hz);
+            }
             mx += w * U[0];
             my += w * U[1];
             mz += w * U[2];
@@ -913,27 +1001,33 @@ void upload_rules(bool one_point) {
 }
 
 cudaError_t launch_tet(Ctx &c, double dt, const double H[3]) {
-    if (c.nmt == 0) return cudaSuccess;
+    if (c.tri_be && c.nft > 0) {  // surface anisotropy (only when some region has Ks != 0)
+        if (c.npi_f == 4) k_tri_aniso<4><<<nblocks(c.nft, 128), 128, 0, c.stream>>>(c.nft, c.tri, c.tri_c, c.u[0], c.tri_be);
+        else k_tri_aniso<1><<<nblocks(c.nft, 128), 128, 0, c.stream>>>(c.nft, c.tri, c.tri_c, c.u[0], c.tri_be);
+    }
+    if (c.nmt == 0) return cudaGetLastError();
     const int b = 128;
     if (!c.aniso) {
         if (c.npi_t == 5)
             k_tet64_iso<5><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0],
                                                                    c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
-                                                                   c.tet_seg, c.batch ? c.seg_par : nullptr);
+                                                                   c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp,
+                                                                   c.field_amp);
         else
             k_tet64_iso<1><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0],
                                                                    c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
-                                                                   c.tet_seg, c.batch ? c.seg_par : nullptr);
+                                                                   c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp,
+                                                                   c.field_amp);
         return cudaGetLastError();
     }
     if (c.npi_t == 5)
         k_tet64<5><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0], c.v[0],
                                                           c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
-                                                          c.tet_seg, c.batch ? c.seg_par : nullptr);
+                                                          c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp, c.field_amp);
     else
         k_tet64<1><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0], c.v[0],
                                                           c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
-                                                          c.tet_seg, c.batch ? c.seg_par : nullptr);
+                                                          c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp, c.field_amp);
     return cudaGetLastError();
 }
 
@@ -942,7 +1036,8 @@ cudaError_t launch_node(Ctx &c, double angle) {
     double *bv = c.bv;
     const long n2 = 2L * c.nn;
     double *Minv = bv + 8 * n2;
-    k_node64<<<nblocks(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.inc_ptr, c.inc, c.slot, c.mag, c.A, c.u[0], c.v[1],
+    k_node64<<<nblocks(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.inc_ptr, c.inc, c.slot, c.tinc_ptr, c.tinc, c.tri_be,
+                                                        c.mag, c.A, c.u[0], c.v[1],
                                                         cr, sr, c.ep, c.eq, c.Dl, c.rhs, c.x, Minv, c.W,
                                                         c.mlp ? c.heff : nullptr, c.node_seg,
                                                         c.batch ? c.seg_par : nullptr);
@@ -996,11 +1091,26 @@ cudaError_t launch_charges(Ctx &c, const double *m, int set) {
     double *q = set ? c.src_q2 : c.src_q, *ts = set ? c.tri_slot2 : c.tri_slot;
     if (!q || !ts) return cudaErrorInvalidValue;
     if (c.npi_t == 5)
-        k_charges<5, 4><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs,
-                                                                c.tri, c.tri_c, m, c.src_dst, q, ts);
+        k_charges<5, 4, 1><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs,
+                                                                   c.tri, c.tri_c, m, m, c.src_dst, q, q, ts, ts);
     else
-        k_charges<1, 1><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs,
-                                                                c.tri, c.tri_c, m, c.src_dst, q, ts);
+        k_charges<1, 1, 1><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs,
+                                                                   c.tri, c.tri_c, m, m, c.src_dst, q, q, ts, ts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_charges_pair(Ctx &c, const double *m, const double *v) {
+    const int n = c.nmt + c.nft;
+    if (n == 0) return cudaSuccess;
+    if (!c.src_q2 || !c.tri_slot2) return cudaErrorInvalidValue;
+    if (c.npi_t == 5)
+        k_charges<5, 4, 2><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs,
+                                                                   c.tri, c.tri_c, m, v, c.src_dst, c.src_q, c.src_q2,
+                                                                   c.tri_slot, c.tri_slot2);
+    else
+        k_charges<1, 1, 2><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs,
+                                                                   c.tri, c.tri_c, m, v, c.src_dst, c.src_q, c.src_q2,
+                                                                   c.tri_slot, c.tri_slot2);
     return cudaGetLastError();
 }
 
@@ -1020,35 +1130,24 @@ cudaError_t launch_phi_final(Ctx &c, double *phi_out, int set) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_energy(Ctx &c, const double H[3]) {
-    const int G = c.epart_blocks;
-    if (c.npi_t == 5)
-        (c.aniso ? k_energy<5, 4, false> : k_energy<5, 4, true>)<<<G, 256, 0, c.stream>>>(
-            c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
-                                                 c.u[1], c.phi[1], H[0], H[1], H[2], c.epart, nullptr, nullptr,
-                                                 nullptr);
-    else
-        (c.aniso ? k_energy<1, 1, false> : k_energy<1, 1, true>)<<<G, 256, 0, c.stream>>>(
-            c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
-                                                 c.u[1], c.phi[1], H[0], H[1], H[2], c.epart, nullptr, nullptr,
-                                                 nullptr);
-    return cudaGetLastError();
-}
+// The closed isotropic form needs a uniform applied field: a space field takes the
+// Gauss-point form.
+static bool energy_iso(const Ctx &c) { return !c.aniso && !c.hsp; }
+
+cudaError_t launch_energy(Ctx &c, const double H[3]) { return launch_energy_into(c, H, c.epart); }
 
 // Same reduction as launch_energy with the per-block partial sums written to a caller-given
 // device buffer of at least 7 * c.epart_blocks doubles (used by fg_energy_noalloc).
 cudaError_t launch_energy_into(Ctx &c, const double H[3], double *partial) {
     const int G = c.epart_blocks;
     if (c.npi_t == 5)
-        (c.aniso ? k_energy<5, 4, false> : k_energy<5, 4, true>)<<<G, 256, 0, c.stream>>>(
-            c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
-                                                 c.u[1], c.phi[1], H[0], H[1], H[2], partial, nullptr, nullptr,
-                                                 nullptr);
+        (energy_iso(c) ? k_energy<5, 4, true> : k_energy<5, 4, false>)<<<G, 256, 0, c.stream>>>(
+            c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c, c.u[1], c.phi[1], H[0], H[1], H[2],
+            partial, nullptr, nullptr, nullptr, c.hsp, c.field_amp);
     else
-        (c.aniso ? k_energy<1, 1, false> : k_energy<1, 1, true>)<<<G, 256, 0, c.stream>>>(
-            c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
-                                                 c.u[1], c.phi[1], H[0], H[1], H[2], partial, nullptr, nullptr,
-                                                 nullptr);
+        (energy_iso(c) ? k_energy<1, 1, true> : k_energy<1, 1, false>)<<<G, 256, 0, c.stream>>>(
+            c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c, c.u[1], c.phi[1], H[0], H[1], H[2],
+            partial, nullptr, nullptr, nullptr, c.hsp, c.field_amp);
     return cudaGetLastError();
 }
 
@@ -1060,12 +1159,12 @@ cudaError_t launch_energy_seg(Ctx &c) {
         (c.aniso ? k_energy<5, 4, false> : k_energy<5, 4, true>)<<<G, 256, 0, c.stream>>>(
             c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
                                                  c.u[1], c.phi[1], H0[0], H0[1], H0[2], c.seg_epart, c.eblk_rng,
-                                                 c.eblk_seg, c.seg_H);
+                                                 c.eblk_seg, c.seg_H, nullptr, 0.0);
     else
         (c.aniso ? k_energy<1, 1, false> : k_energy<1, 1, true>)<<<G, 256, 0, c.stream>>>(
             c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
                                                  c.u[1], c.phi[1], H0[0], H0[1], H0[2], c.seg_epart, c.eblk_rng,
-                                                 c.eblk_seg, c.seg_H);
+                                                 c.eblk_seg, c.seg_H, nullptr, 0.0);
     k_seg_energy_sum<<<c.nseg, 32, 0, c.stream>>>(G, c.d_seg_eblk, c.seg_epart, c.seg_energy);
     return cudaGetLastError();
 }

@@ -155,6 +155,22 @@ int fg_energy(fg_ctx *ctx, const double Hext[3], double energies[4]);
  * overlaps race on the array. Same results as fg_energy. */
 int fg_energy_noalloc(fg_ctx *ctx, const double Hext[3], double energies[4]);
 
+/* Space-dependent applied field, the reference's R4toR3 field type B(x, t) = A(t) f(x)
+ * (src/settings.h:33-43; mesh::setExtSpaceField src/mesh.cpp:377-389 evaluates f at the
+ * Gauss points of the magnetic tets, LinAlgebra::prepareElements src/linear_algebra.cpp:54-81
+ * and Tet::zeemanEnergy src/tetra.cpp:381-390 use A(t) f). The caller evaluates f (A/m)
+ * itself:
+ *   fg_gauss_points: *n_points = magnetic tets x Gauss points; pts (may be NULL) gets their
+ *     coordinates [n_mag_tets][npi][3], magnetic tets in mesh order (the order of magTet);
+ *   fg_set_space_field: field [n_mag_tets][npi][3] at those points, copied to the device
+ *     (NULL removes it);
+ *   fg_set_field_amplitude: A of the next fg_step / fg_compute_all calls (default 1).
+ * With a space field set, the applied field at Gauss point g is Hext + A f(g), Hext being the
+ * uniform field those calls take (pass zeros for a pure R4toR3 run). Not for batches. */
+int fg_gauss_points(const fg_ctx *ctx, int *n_points, double *pts);
+int fg_set_space_field(fg_ctx *ctx, const double *field);
+int fg_set_field_amplitude(fg_ctx *ctx, double amplitude);
+
 /* <u_d> (which 0) or <v_d> (which 1) of NEXT over the magnetic volume, src/mesh.cpp:89-106. */
 int fg_average(fg_ctx *ctx, int which, double avg[3]);
 

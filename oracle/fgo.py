@@ -62,6 +62,7 @@ def lib():
         L.fgo_set_threads.argtypes = [C.c_void_p, C.c_int]
         L.fgo_max_threads.restype = C.c_int
         L.fgo_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_int]
+        L.fgo_set_space_field.argtypes = [C.c_void_p, C.c_void_p, C.c_double]
         L.fgo_set_state.argtypes = [C.c_void_p, _dp, C.c_void_p, C.c_void_p, C.c_void_p]
         L.fgo_get_state.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]
         L.fgo_get_basis.argtypes = [C.c_void_p, _dp, _dp]
@@ -134,6 +135,15 @@ class Oracle:
 
     def set_solver(self, tol=1e-6, maxiter=700):
         self.L.fgo_set_solver(self.h, tol, maxiter)
+
+    def set_space_field(self, field, amp=1.0):
+        """R4toR3 applied field: f at the magnetic tets' Gauss points ([n_mag_tets * npi, 3],
+        magTet order) or None, and its amplitude; the applied field is Hext + amp f(g)."""
+        if field is None:
+            self.L.fgo_set_space_field(self.h, None, float(amp))
+            return
+        f = np.ascontiguousarray(field, dtype=np.float64)
+        self.L.fgo_set_space_field(self.h, f.ctypes.data_as(C.c_void_p), float(amp))
 
     def set_state(self, u, v=None, phi=None, phiv=None):
         u = np.ascontiguousarray(u, dtype=np.float64).ravel()

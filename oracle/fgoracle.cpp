@@ -134,6 +134,10 @@ struct Oracle {
     std::vector<double> da, wt, tri_n, tri_surf, tri_w;
     std::vector<char> magNode;
     std::vector<int> magTet, magTri, lvd;
+    // R4toR3 applied field (mesh::setExtSpaceField, src/mesh.cpp:377-389): f at the Gauss points
+    // of every tet [nt][npi][3] (zero for non-magnetic tets), used as Hext + amp f(g)
+    std::vector<double> hsp;
+    double amp = 1.0;
     double totalMagVol = 0;
     // scalar CSR with 2x2 blocks per node and per edge (src/solver.h:75-104)
     std::vector<int> rowptr, col;
@@ -379,6 +383,8 @@ void integrales(Oracle &o, int t, double dt, double prefactor, const double Hext
     V3 He = v3(Hext);
     for (int g = 0; g < npi; g++) {
         V3 Heff = Hd + He;
+        if (!o.hsp.empty())  // calc_Hext of the R4toR3 prepareElements (src/linear_algebra.cpp:54-72)
+            Heff = Heff + o.amp * v3(&o.hsp[3 * ((size_t)t * npi + g)]);
         H[g] = Heff;
         uHeff[g] += dot(U[g], Heff);
     }
@@ -858,7 +864,9 @@ void energy(Oracle &o, const double Hext[3]) {
             ex += w[g] * dens;
             dm += w[g] * (dUd[0].x + dUd[1].y + dUd[2].z) * phg;
             if (p.K != 0.0) an += w[g] * sq(dot(v3(p.uk), U));
-            ze += w[g] * dot(U, He);
+            V3 Hg = He;
+            if (!o.hsp.empty()) Hg = Hg + o.amp * v3(&o.hsp[3 * ((size_t)t * R.npi + g)]);
+            ze += w[g] * dot(U, Hg);
             if (p.K3 != 0.0) {
                 double a0 = dot(U, v3(p.ex)), a1 = dot(U, v3(p.ey)), a2 = dot(U, v3(p.ez));
                 E[1] += p.K3 * w[g] * (sq(a0 * a1) + sq(a1 * a2) + sq(a2 * a0));
@@ -1040,6 +1048,21 @@ int fgo_max_threads() {
 #else
     return 1;
 #endif
+}
+
+// R4toR3 field: f at the Gauss points of the magnetic tets, [n_mag_tets][npi][3] in magTet
+// order (NULL removes it), and its amplitude A(t).
+void fgo_set_space_field(void *h, const double *field, double amp) {
+    Oracle *o = static_cast<Oracle *>(h);
+    o->amp = amp;
+    if (!field) {
+        o->hsp.clear();
+        return;
+    }
+    const int npi = o->tr.npi;
+    o->hsp.assign(3 * (size_t)o->nt * npi, 0.0);
+    for (size_t k = 0; k < o->magTet.size(); k++)
+        for (int q = 0; q < 3 * npi; q++) o->hsp[3 * (size_t)o->magTet[k] * npi + q] = field[3 * k * npi + q];
 }
 
 void fgo_set_solver(void *h, double tol, int maxiter) {

@@ -156,3 +156,88 @@ def test_mixed_precision_solve(tol):
     so, sg = o.get_state(1), cm.get_state(1)
     assert _rel(sg["v"], so["v"]) <= 50 * tol
     assert np.max(np.abs(np.linalg.norm(sg["u"], axis=1) - 1.0)) < 1e-14
+
+
+@pytest.mark.parametrize("one_point", [False, True])
+def test_surface_anisotropy(one_point):
+    """Tri::integrales (src/triangle.cpp:6-36): the surface anisotropy of the magnetic
+    triangles enters the RHS of their nodes; RHS within 1e-12 of the oracle's explicit
+    assembly, the solution within 1e-9. Kbis = 2 Ks / dMs carries the sign of the
+    triangle's dMs (+-Ms by orientation, src/mesh.cpp:239); the structured test mesh
+    alternates orientations, which would cancel the term at shared nodes, so the test
+    gives every triangle dMs = +Ms (both sides get the same mesh)."""
+    m = cases.cuboid(6, 5, 4)
+    m["dMs"] = np.abs(m["dMs"])
+    u = cases.perturbed_state(m["xyz"], seed=21)
+    v = cases.tangent_field(u, seed=22)
+    ks, uks = 500.0, (0.2, -0.4, 1.0)
+    # the cuboid's boundary triangles are in surface region 1
+    o = fgo.Oracle(m, cases.oracle_regions(alpha=0.5), [fgo.make_tri_region(), fgo.make_tri_region(Ks=ks, uk=uks)],
+                   one_gauss_point=one_point)
+    o.set_solver(1e-12, 5000)
+    o.set_state(u, v)
+    H = np.array([2e4, -1e4, 3e4])
+    o.compute_all(H)
+    st = o.get_state(0)
+    c = fg.Context(m, cases.regions(alpha=0.5), [dict(), dict(Ks=ks, uk=uks)], tol=1e-12, max_iter=5000,
+                   one_gauss_point=int(one_point))
+    c.set_state(st["u"], st["v"], st["phi"], st["phiv"])
+    angle, pref = 0.73, fgo.prefactor(DT, DTMAX)
+    o.base_projection(angle)
+    ro = o.step(DT, pref, H)
+    rowptr, col, val, rhs_o = o.export_system()
+    rg = c.step(DT, pref, H, angle)
+    assert not ro["fail"] and rg["status"] == fg.FG_OK
+    rhs_g, _, _ = c.debug_system()
+    assert _rel(rhs_g, rhs_o) <= 1e-12
+    # the surface term is a visible part of the RHS
+    o2 = fgo.Oracle(m, cases.oracle_regions(alpha=0.5), one_gauss_point=one_point)
+    o2.set_solver(1e-12, 5000)
+    o2.set_state(st["u"], st["v"], st["phi"], st["phiv"])
+    o2.base_projection(angle)
+    o2.step(DT, pref, H)
+    assert _rel(o2.export_system()[3], rhs_o) > 1e-2
+    assert _rel(c.get_state(1)["v"], o.get_state(1)["v"]) <= 1e-9
+
+
+@pytest.mark.parametrize("K", [0.0, 4e4])
+def test_space_field(K):
+    """R4toR3 applied field B(x, t) = A(t) f(x): f at the magnetic tets' Gauss points
+    (mesh::setExtSpaceField, src/mesh.cpp:377-389), A per step; the applied field is
+    Hext + A f(g). RHS within 1e-12 of the oracle, v within 1e-9, energies within 1e-10
+    (both the isotropic element kernel and the general one with anisotropy)."""
+    m = cases.cuboid(6, 5, 4)
+    u = cases.perturbed_state(m["xyz"], seed=31)
+    v = cases.tangent_field(u, seed=32)
+    regs_o, regs_g = cases.oracle_regions(alpha=0.5, K=K, uk=UK), cases.regions(alpha=0.5, K=K, uk=UK)
+    c = fg.Context(m, regs_g, tol=1e-12, max_iter=5000)
+    pts = c.gauss_points()
+    assert pts.shape == (len(m["tets"]) * 5, 3)
+    s = pts / 3e-9
+    f = 4e4 * np.stack([np.sin(s[:, 0]), np.cos(s[:, 1]), np.sin(s[:, 2] + s[:, 0])], axis=1)
+    amp, H = 0.7, np.array([1e4, 0.0, -2e4])
+    o = fgo.Oracle(m, regs_o)
+    o.set_solver(1e-12, 5000)
+    o.set_space_field(f, amp)
+    o.set_state(u, v)
+    o.compute_all(H)
+    st = o.get_state(0)
+    c.set_space_field(f)
+    c.set_field_amplitude(amp)
+    c.set_state(st["u"], st["v"], st["phi"], st["phiv"])
+    angle, pref = 0.37, fgo.prefactor(DT, DTMAX)
+    o.base_projection(angle)
+    ro = o.step(DT, pref, H)
+    rowptr, col, val, rhs_o = o.export_system()
+    rg = c.step(DT, pref, H, angle)
+    assert not ro["fail"] and rg["status"] == fg.FG_OK
+    assert _rel(c.debug_system()[0], rhs_o) <= 1e-12
+    assert _rel(c.get_state(1)["v"], o.get_state(1)["v"]) <= 1e-9
+    Eo, Eg = o.compute_all(H), c.compute_all(H)
+    for k in range(4):
+        assert abs(Eg[k] - Eo[k]) <= 1e-10 * np.max(np.abs(Eo)), (k, Eg, Eo)
+    # the space field is a visible part of the RHS and of the Zeeman energy
+    c.set_space_field(None)
+    c.set_state(st["u"], st["v"], st["phi"], st["phiv"])
+    c.step(DT, pref, H, angle)
+    assert _rel(c.debug_system()[0], rhs_o) > 1e-3
