@@ -57,7 +57,7 @@ class fg_opts(C.Structure):
                 ("verbose", C.c_int), ("profile", C.c_int), ("mlp_train_steps", C.c_int), ("mlp_batch", C.c_int),
                 ("mlp_lr", C.c_double), ("fmm_tensor", C.c_int),
                 ("mlp_train_every", C.c_int), ("fmm_native_fp64", C.c_int),
-                ("solver_lpr", C.c_int)]
+                ("solver_lpr", C.c_int), ("solver_blocks", C.c_int)]
 
 
 class fg_step_report(C.Structure):
@@ -119,6 +119,7 @@ SIGNATURES = {
     "fg_gauss_points": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
     "fg_set_space_field": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fg_set_field_amplitude": (C.c_int, [C.c_void_p, C.c_double]),
+    "fg_checkpoint_peek": (C.c_int, [C.c_char_p, C.c_void_p, C.c_void_p]),
     "fg_debug_translate_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_int]),
     "fg_batch_create": (C.c_int, [C.POINTER(fg_mesh), C.c_int, C.POINTER(fg_region), C.c_int,
@@ -188,6 +189,29 @@ def settings_dump(settings_path):
 
 def rng_seed(seed):
     fg_lib().fg_rng_seed(seed)
+
+
+class fg_checkpoint_shape(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("n_mag_tets", C.c_int), ("precision", C.c_int), ("solver_lpr", C.c_int),
+                ("solver_blocks", C.c_int), ("fmm_depth", C.c_int)]
+
+
+class fg_checkpoint_meta(C.Structure):
+    _fields_ = [("t0", C.c_double), ("t", C.c_double), ("dt", C.c_double), ("dt_soft_max", C.c_double),
+                ("steps", C.c_longlong), ("output_index", C.c_longlong), ("rng_seed", C.c_uint),
+                ("rng_draws", C.c_longlong), ("E", C.c_double * 4)]
+
+
+def checkpoint_peek(path):
+    """fg_checkpoint_peek: header of a checkpoint file (shape and run metadata) as a dict."""
+    sh, me = fg_checkpoint_shape(), fg_checkpoint_meta()
+    s = fg_lib().fg_checkpoint_peek(str(path).encode(), C.byref(sh), C.byref(me))
+    if s != FG_OK:
+        raise FgError(s, f"cannot read checkpoint {path}")
+    out = {k: getattr(sh, k) for k, _ in fg_checkpoint_shape._fields_}
+    out.update({k: getattr(me, k) for k, _ in fg_checkpoint_meta._fields_ if k != "E"})
+    out["E"] = list(me.E)
+    return out
 
 
 def rng_angle():

@@ -509,6 +509,7 @@ cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle) {
     if (c.lpr > 0) return cudaSuccess;
     if (c.opts.solver_lpr == 1 || c.opts.solver_lpr == 4 || c.opts.solver_lpr == 8) {
         c.lpr = c.opts.solver_lpr;
+        if (c.opts.solver_blocks > 0 && !c.batch) c.mixed_grid = std::min(c.opts.solver_blocks, c.mixed_grid);
         return cudaSuccess;
     }
     const int cand[3] = {1, 4, 8};

@@ -75,6 +75,7 @@ struct Run {
     double E[4] = {0, 0, 0, 0};
     double vmax = 0, t = 0, dt = 0;
     long long nsteps = 0;
+    long long rng_draws = 0;  // basis angles drawn since fg_rng_seed (for checkpoints)
     std::vector<std::pair<int, int>> edges;
     ~Run() {
         if (ctx) fg_destroy(ctx);
@@ -224,8 +225,23 @@ int run_impl(Run &R, const char *settings_path, unsigned int seed, int verbose, 
         if (k >= 1 && k <= (int)S.surf.size()) set_surf(tregs[k], S.surf[k - 1]);
         else set_surf(tregs[k], S.surf_default);
     }
+    // resume: the checkpoint fixes the solver's and the FMM's choices of the original run, so
+    // that the continuation repeats it bit for bit
+    fg_checkpoint_shape ck{};
+    fg_checkpoint_meta cm{};
+    const bool resume = !S.resume_file.empty();
+    if (resume && fg_checkpoint_peek(S.resume_file.c_str(), &ck, &cm) != FG_OK)
+        return fail(FG_EIO, "cannot read checkpoint " + S.resume_file);
     fg_opts o;
     fg_opts_default(&o);
+    o.solver_lpr = S.solver_lpr;
+    o.solver_blocks = S.solver_blocks;
+    if (S.fmm_depth > 0) o.fmm_leaf = -S.fmm_depth;
+    if (resume) {
+        o.solver_lpr = ck.solver_lpr;
+        o.solver_blocks = ck.solver_blocks;
+        if (ck.fmm_depth > 0) o.fmm_leaf = -ck.fmm_depth;
+    }
     o.tol = S.tol;
     o.max_iter = S.max_iter;
     o.precision = S.gpu_precision;
@@ -255,27 +271,41 @@ int run_impl(Run &R, const char *settings_path, unsigned int seed, int verbose, 
     R.phi.assign(nn, 0.0);
     R.phiv.assign(nn, 0.0);
     double t0 = 0.0;
-    if (S.init_from_file) {
-        s = read_sol(R, S.restore_file, &t0);
-        if (s != FG_OK) return s;
-    } else {
-        for (int i = 0; i < nn; i++)
-            if (R.mag[i])
-                for (int k = 0; k < 3; k++) R.u[3 * i + k] = S.m0[k];
-    }
-    if (!std::isnan(S.initial_time)) t0 = S.initial_time;
-    s = fg_set_state(R.ctx, R.u.data(), R.v.data(), R.phi.data(), R.phiv.data());
-    if (s != FG_OK) return fail(s, fg_last_error(R.ctx));
     const double H[3] = {S.Bext[0] / MU0, S.Bext[1] / MU0, S.Bext[2] / MU0};
-    // main(): srand(seed); the LinAlgebra constructor draws one basis angle
-    fg_rng_seed(seed);
-    fg_rng_angle();
-    s = fg_compute_all(R.ctx, H, R.E);
-    if (s != FG_OK) return fail(s, fg_last_error(R.ctx));
+    if (resume) {
+        // full-precision state of the checkpoint; its energies stand for the initial compute_all
+        s = fg_checkpoint_load(R.ctx, S.resume_file.c_str(), &cm);
+        if (s != FG_OK) return fail(s, fg_last_error(R.ctx));
+        t0 = cm.t0;
+        for (int k = 0; k < 4; k++) R.E[k] = cm.E[k];
+        seed = cm.rng_seed;
+        fg_rng_seed(seed);
+        for (long long k = 0; k < cm.rng_draws; k++) fg_rng_angle();
+        R.rng_draws = cm.rng_draws;
+    } else {
+        if (S.init_from_file) {
+            s = read_sol(R, S.restore_file, &t0);
+            if (s != FG_OK) return s;
+        } else {
+            for (int i = 0; i < nn; i++)
+                if (R.mag[i])
+                    for (int k = 0; k < 3; k++) R.u[3 * i + k] = S.m0[k];
+        }
+        if (!std::isnan(S.initial_time)) t0 = S.initial_time;
+        s = fg_set_state(R.ctx, R.u.data(), R.v.data(), R.phi.data(), R.phiv.data());
+        if (s != FG_OK) return fail(s, fg_last_error(R.ctx));
+        // main(): srand(seed); the LinAlgebra constructor draws one basis angle
+        fg_rng_seed(seed);
+        fg_rng_angle();
+        R.rng_draws = 1;
+        s = fg_compute_all(R.ctx, H, R.E);
+        if (s != FG_OK) return fail(s, fg_last_error(R.ctx));
+    }
     const std::string base = S.out_dir + "/" + S.sim_name;
-    std::FILE *fe = std::fopen((base + ".evol").c_str(), "w");
+    // a resumed run appends its rows to the .evol of the original run
+    std::FILE *fe = std::fopen((base + ".evol").c_str(), resume ? "a" : "w");
     if (!fe) return fail(FG_EIO, "cannot open file " + base + ".evol");
-    {
+    if (!resume) {
         std::string meta = common_metadata(S, R.settings_name);
         std::fprintf(fe, "%s## columns:", meta.c_str());
         for (size_t k = 0; k < S.evol_columns.size(); k++)
@@ -287,8 +317,15 @@ int run_impl(Run &R, const char *settings_path, unsigned int seed, int verbose, 
     Stepper st{S.dt_min, S.dt_max * (1 + FLT_EPSILON), R.dt};
     const int step_count = (int)std::lround((S.final_time - t0) / S.evol_time_step);
     int status = FG_OK, nt_output = 0;
+    if (resume) {
+        R.t = cm.t;
+        R.dt = cm.dt;
+        st.soft_max = cm.dt_soft_max;
+        R.nsteps = cm.steps;
+        nt_output = (int)cm.output_index;
+    }
     const auto wall0 = std::chrono::steady_clock::now();
-    for (int step_nb = 0; step_nb <= step_count && status == FG_OK; step_nb++) {
+    for (int step_nb = nt_output; step_nb <= step_count && status == FG_OK; step_nb++) {
         const double target = t0 + step_nb * S.evol_time_step;
         while (R.t < target) {
             if (g_stop.load()) {
@@ -306,6 +343,7 @@ int run_impl(Run &R, const char *settings_path, unsigned int seed, int verbose, 
                 break;
             }
             fg_step_report rp;
+            R.rng_draws++;
             s = fg_step(R.ctx, R.dt, prefactor_of(R.dt, S.dt_max), H, fg_rng_angle(), &rp);
             if (s != FG_OK && s != FG_SOLVER_ITER_OVERFLOW && s != FG_SOLVER_CANNOT_CONVERGE) {
                 status = s;
@@ -339,6 +377,24 @@ int run_impl(Run &R, const char *settings_path, unsigned int seed, int verbose, 
             if (s != FG_OK) { status = s; break; }
         }
         nt_output++;
+        if (S.checkpoint_every > 0 && nt_output % S.checkpoint_every == 0) {
+            fg_checkpoint_meta m{};
+            m.t0 = t0;
+            m.t = R.t;
+            m.dt = R.dt;
+            m.dt_soft_max = st.soft_max;
+            m.steps = R.nsteps;
+            m.output_index = nt_output;
+            m.rng_seed = seed;
+            m.rng_draws = R.rng_draws;
+            for (int k = 0; k < 4; k++) m.E[k] = R.E[k];
+            s = fg_checkpoint_save(R.ctx, (base + ".ckpt").c_str(), &m);
+            if (s != FG_OK) {
+                status = s;
+                g_run_error = fg_last_error(R.ctx);
+                break;
+            }
+        }
     }
     std::fclose(fe);
     if (rep) {

@@ -418,6 +418,22 @@ void apply_yaml(Settings &S, const std::shared_ptr<YNode> &y) {
         if (auto d = g->get("learned_guess"); !is_null(d)) S.gpu_learned = to_bool(d, "gpu.learned_guess");
         if (auto d = g->get("demag"); !is_null(d)) S.gpu_demag = d->scalar == "direct" ? 1 : (d->scalar == "fmm" ? 2 : 0);
         if (auto d = g->get("one_gauss_point"); !is_null(d)) S.one_gauss_point = to_bool(d, "gpu.one_gauss_point");
+        if (auto d = g->get("checkpoint_every"); !is_null(d)) {
+            const double n = to_num(d, "gpu.checkpoint_every");
+            if (!(n >= 0) || n != std::floor(n)) throw SettingsError("gpu.checkpoint_every must be a count >= 0");
+            S.checkpoint_every = (int)n;
+        }
+        if (auto d = g->get("resume"); !is_null(d)) S.resume_file = d->scalar;
+        auto count = [&](const char *key, int &out) {
+            if (auto d = g->get(key); !is_null(d)) {
+                const double n = to_num(d, std::string("gpu.") + key);
+                if (!(n >= 0) || n != std::floor(n)) throw SettingsError(std::string("gpu.") + key + " must be a count >= 0");
+                out = (int)n;
+            }
+        };
+        count("solver_lanes_per_row", S.solver_lpr);
+        count("solver_blocks", S.solver_blocks);
+        count("fmm_depth", S.fmm_depth);
     }
 }
 

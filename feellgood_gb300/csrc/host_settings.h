@@ -63,6 +63,9 @@ struct Settings {
     // options of this build, read from an optional "gpu:" section
     int gpu_precision = 0, gpu_demag = 0;
     bool gpu_learned = false, one_gauss_point = false;
+    int checkpoint_every = 0;    // write <out_dir>/<sim_name>.ckpt after every n-th output row
+    int solver_lpr = 0, solver_blocks = 0, fmm_depth = 0;  // fixed solver / FMM choices (0: timed)
+    std::string resume_file;     // continue the run of this checkpoint
     void finish();
 };
 

@@ -101,6 +101,10 @@ typedef struct {
     int solver_lpr;       /* FP32 + refinement solver: lanes sharing one row of the operator
                              (1 thread per row, 4, 8); 0 (default): the fastest, timed on the
                              first step */
+    int solver_blocks;    /* FP32 + refinement solver with solver_lpr set: persistent blocks
+                             (0: all co-resident blocks). Fixing both (and fmm_leaf = -depth)
+                             makes runs repeat bit for bit: the timed choices decide the
+                             order of the solver's reductions */
 } fg_opts;
 
 typedef struct {
@@ -170,6 +174,32 @@ int fg_energy_noalloc(fg_ctx *ctx, const double Hext[3], double energies[4]);
 int fg_gauss_points(const fg_ctx *ctx, int *n_points, double *pts);
 int fg_set_space_field(fg_ctx *ctx, const double *field);
 int fg_set_field_amplitude(fg_ctx *ctx, double amplitude);
+
+/* Full-precision checkpoint of a context (no reference counterpart: the reference's .sol
+ * keeps u and phi to 7 digits and loses v and phiv, src/save.cpp:164-186). The file holds the
+ * CURRENT state (u, v, phi, phiv in FP64), the caller's run metadata below, and the choices
+ * that fix the order of the solver's and the FMM's arithmetic (solver lanes per row and
+ * blocks, FMM depth), so that a run resumed from it with those choices (fg_opts.solver_lpr,
+ * solver_blocks, fmm_leaf = -depth) repeats the uninterrupted run bit for bit (the learned
+ * guess's network is not saved: with it the resumed run agrees to the solver tolerance).
+ * Binary, little-endian, with an FNV-1a checksum; fg_checkpoint_peek reads the header
+ * without a context. Call fg_checkpoint_save after fg_compute_all. */
+typedef struct {
+    double t0;                 /* start time of the run */
+    double t, dt, dt_soft_max; /* time, last dt, the step controller's soft limit */
+    long long steps;           /* accepted steps */
+    long long output_index;    /* next output row */
+    unsigned int rng_seed;     /* fg_rng_seed of the run */
+    long long rng_draws;       /* fg_rng_angle draws since then */
+    double E[4];               /* energies of the state */
+} fg_checkpoint_meta;
+typedef struct {
+    int n_nodes, n_mag_tets, precision;
+    int solver_lpr, solver_blocks, fmm_depth; /* 0 where not used */
+} fg_checkpoint_shape;
+int fg_checkpoint_save(fg_ctx *ctx, const char *path, const fg_checkpoint_meta *meta);
+int fg_checkpoint_peek(const char *path, fg_checkpoint_shape *shape, fg_checkpoint_meta *meta);
+int fg_checkpoint_load(fg_ctx *ctx, const char *path, fg_checkpoint_meta *meta);
 
 /* <u_d> (which 0) or <v_d> (which 1) of NEXT over the magnetic volume, src/mesh.cpp:89-106. */
 int fg_average(fg_ctx *ctx, int which, double avg[3]);

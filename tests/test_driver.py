@@ -138,3 +138,39 @@ def test_sol_written_and_restarted(tmp_path, golden_dir):
     assert abs(rep["t"] - 6e-12) < 1e-20
     first = [l for l in open(tmp_path / "restart.evol") if not l.startswith("#")][0].split()
     assert abs(float(first[0]) - 5e-12) < 1e-20
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("gpu", [{}, {"precision": "fp32_refine", "demag": "fmm"}])
+def test_checkpoint_resume_is_bitwise(tmp_path, golden_dir, gpu):
+    """A run stopped at a full-precision checkpoint (gpu.checkpoint_every) and resumed from
+    it (gpu.resume) writes the same .evol rows, to the last printed digit (%.16g), as the
+    uninterrupted run: the checkpoint keeps u, v, phi, phiv in FP64, the step controller, the
+    basis-angle stream position and the solver / FMM choices that fix the arithmetic order
+    (the uninterrupted run is given the choices the first half timed)."""
+    g, st = _full_test_settings(golden_dir, tmp_path)
+    total = 12 * g["evol_time_step"]
+    cols = ["t", "<Mx>", "<My>", "<Mz>", "E_ex", "E_demag", "E_zeeman", "E_tot"]
+    # first half, checkpoint after row 6 (rows 0..6 = 7 rows)
+    half = dict(st, gpu=dict(gpu, checkpoint_every=7),
+                outputs=dict(st["outputs"], file_basename="split", final_time=6 * g["evol_time_step"],
+                             evol_columns=cols))
+    (tmp_path / "half.json").write_text(json.dumps(half))
+    fg.run(tmp_path / "half.json", seed=3)
+    ck = tmp_path / "split.ckpt"
+    head = fg.checkpoint_peek(ck)
+    assert head["output_index"] == 7 and head["rng_seed"] == 3 and head["steps"] > 0
+    rest = dict(half, gpu=dict(gpu, resume=str(ck)), outputs=dict(half["outputs"], final_time=total))
+    (tmp_path / "rest.json").write_text(json.dumps(rest))
+    rep = fg.run(tmp_path / "rest.json", seed=12345)  # the checkpoint's seed and stream position win
+    assert abs(rep["t"] - total) < 1e-20
+    fixed = dict(solver_lanes_per_row=head["solver_lpr"], solver_blocks=head["solver_blocks"],
+                 fmm_depth=head["fmm_depth"])
+    full = dict(st, gpu=dict(gpu, **fixed), outputs=dict(st["outputs"], file_basename="full", final_time=total,
+                                                        evol_columns=cols))
+    (tmp_path / "full.json").write_text(json.dumps(full))
+    fg.run(tmp_path / "full.json", seed=3)
+    a = [l for l in open(tmp_path / "full.evol") if not l.startswith("#")]
+    b = [l for l in open(tmp_path / "split.evol") if not l.startswith("#")]
+    assert len(a) == len(b) == 13
+    assert a == b

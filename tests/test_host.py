@@ -78,3 +78,40 @@ def test_missing_mesh_file():
     with pytest.raises(fg.FgError) as e:
         fg.load_msh("/nonexistent/file.msh", ["v"], [1.0])
     assert e.value.status == fg.api.FG_EIO
+
+
+def _checkpoint_bytes(n=4, nmt=2, meta=None):
+    """A checkpoint in the documented layout (fg_checkpoint.cu): header, meta, state, FNV-1a."""
+    import struct
+    m = dict(t0=0.0, t=1.5e-12, dt=2e-14, dt_soft_max=3e-14, steps=75, output_index=4, rng_seed=9, rng_draws=80,
+             E=[1.0, 2.0, -3.0, 4.0])
+    m.update(meta or {})
+    b = b"FGGPUCK1" + struct.pack("<I6i", 1, n, nmt, 1, 4, 304, 6)
+    b += struct.pack("<4d", m["t0"], m["t"], m["dt"], m["dt_soft_max"])
+    b += struct.pack("<qqIq", m["steps"], m["output_index"], m["rng_seed"], m["rng_draws"])
+    b += struct.pack("<4d", *m["E"])
+    b += np.arange(8 * n, dtype="<f8").tobytes()
+    h = 1469598103934665603
+    for x in b:
+        h = ((h ^ x) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    return b + struct.pack("<Q", h), m
+
+
+def test_checkpoint_header_and_checksum(tmp_path):
+    """fg_checkpoint_peek reads the documented layout and rejects a corrupted file."""
+    raw, m = _checkpoint_bytes()
+    p = tmp_path / "a.ckpt"
+    p.write_bytes(raw)
+    h = fg.checkpoint_peek(p)
+    assert (h["n_nodes"], h["n_mag_tets"], h["precision"], h["solver_lpr"], h["solver_blocks"], h["fmm_depth"]) == \
+        (4, 2, 1, 4, 304, 6)
+    for k in ("t0", "t", "dt", "dt_soft_max", "steps", "output_index", "rng_seed", "rng_draws", "E"):
+        assert h[k] == m[k], k
+    bad = bytearray(raw)
+    bad[100] ^= 1
+    p.write_bytes(bytes(bad))
+    with pytest.raises(fg.FgError):
+        fg.checkpoint_peek(p)
+    p.write_bytes(raw[:-9])
+    with pytest.raises(fg.FgError):
+        fg.checkpoint_peek(p)
