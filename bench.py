@@ -399,9 +399,12 @@ def main():
     stage_names = ["p2m", "m2m", "m2l", "l2l", "l2p_p2p"]
     nsrc = 5 * 1200000 + 4 * 168000
     kernels = {
-        # per step: (device ms per launch, launches per step, algorithmic units)
-        "k_l2p_p2p (near field + L2P)": (fmm_stage[4], 2, {"bytes": 16.0 * nsrc + 28.0 * nn}),
-        "k_m2l_tc (M2L, tcgen05 3xTF32)": (fmm_stage[2], 2, {"m2l_pairs": n_m2l}),
+        # per step: (device ms per launch, launches per step, algorithmic units). One FMM
+        # evaluation per step covers both charge sets (m and v): the near field reads each
+        # source's (x, y, z, q_m) and q_v once (20 B) and each target's coordinates and node
+        # index once and writes two potentials (36 B); M2L does both sets' products.
+        "k_l2p_p2p (near field + L2P)": (fmm_stage[4], 1, {"bytes": 20.0 * nsrc + 36.0 * nn}),
+        "k_m2l_tc (M2L, tcgen05 3xTF32)": (fmm_stage[2], 1, {"m2l_pairs": 2 * n_m2l}),
         "k_tet64_iso + k_node64 (elements)": (ph[0], 1, {"bytes": 1200000 * (4 * 4 + 12 * 8 + 8 + 4 + 4 * 32) +
                                                           nn * (3 * 8 + 2 * 8 + 8 * 8)}),
     }
