@@ -43,11 +43,13 @@ class fg_mesh(C.Structure):
 class fg_region(C.Structure):
     _fields_ = [("Ae", C.c_double), ("Ms", C.c_double), ("K", C.c_double), ("uk", C.c_double * 3),
                 ("K3", C.c_double), ("ex", C.c_double * 3), ("ey", C.c_double * 3), ("ez", C.c_double * 3),
-                ("alpha", C.c_double)]
+                ("alpha", C.c_double), ("sigma", C.c_double), ("dens_state", C.c_double), ("P", C.c_double),
+                ("lsd", C.c_double), ("lsf", C.c_double)]
 
 
 class fg_tri_region(C.Structure):
-    _fields_ = [("Ks", C.c_double), ("uk", C.c_double * 3), ("suppress_charges", C.c_int)]
+    _fields_ = [("Ks", C.c_double), ("uk", C.c_double * 3), ("suppress_charges", C.c_int), ("jn", C.c_double),
+                ("V", C.c_double), ("uP", C.c_double * 3), ("s", C.c_double * 3)]
 
 
 class fg_opts(C.Structure):
@@ -57,7 +59,8 @@ class fg_opts(C.Structure):
                 ("verbose", C.c_int), ("profile", C.c_int), ("mlp_train_steps", C.c_int), ("mlp_batch", C.c_int),
                 ("mlp_lr", C.c_double), ("fmm_tensor", C.c_int),
                 ("mlp_train_every", C.c_int), ("fmm_native_fp64", C.c_int),
-                ("solver_lpr", C.c_int), ("solver_blocks", C.c_int)]
+                ("solver_lpr", C.c_int), ("solver_blocks", C.c_int), ("spin_acc", C.c_int), ("spin_tol", C.c_double),
+                ("spin_max_iter", C.c_int)]
 
 
 class fg_step_report(C.Structure):
@@ -117,6 +120,8 @@ SIGNATURES = {
     "fg_solver_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "fg_debug_wait_timeout": (C.c_int, [C.c_void_p, C.c_int]),
     "fg_gauss_points": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
+    "fg_spin_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.POINTER(C.c_int)]),
+    "fg_get_spin": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fg_set_space_field": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fg_set_field_amplitude": (C.c_int, [C.c_void_p, C.c_double]),
     "fg_checkpoint_peek": (C.c_int, [C.c_char_p, C.c_void_p, C.c_void_p]),
@@ -271,21 +276,28 @@ def _dptr(a):
 
 
 def make_region(Ae=1e-11, Ms=795774.7, K=0.0, uk=(0, 0, 1), K3=0.0, ex=(1, 0, 0), ey=(0, 1, 0), ez=(0, 0, 1),
-                alpha=0.5, **_):
+                alpha=0.5, sigma=0.0, dens_state=0.0, P=0.0, lsd=0.0, lsf=0.0, **_):
     r = fg_region()
     r.Ae, r.Ms, r.K, r.K3, r.alpha = Ae, Ms, K, K3, alpha
+    r.sigma, r.dens_state, r.P, r.lsd, r.lsf = sigma, dens_state, P, lsd, lsf
     for name, v in (("uk", uk), ("ex", ex), ("ey", ey), ("ez", ez)):
         v = np.asarray(v, float)
         getattr(r, name)[:] = list(v / np.linalg.norm(v))
     return r
 
 
-def make_tri_region(Ks=0.0, uk=(0, 0, 1), suppress_charges=False, **_):
+def make_tri_region(Ks=0.0, uk=(0, 0, 1), suppress_charges=False, jn=None, V=None, uP=(0, 0, 1), s=None, **_):
+    """jn, V, s: None where not given (NaN in the C struct)."""
     r = fg_tri_region()
     r.Ks = Ks
     v = np.asarray(uk, float)
     r.uk[:] = list(v / np.linalg.norm(v))
     r.suppress_charges = int(bool(suppress_charges))
+    r.jn = float("nan") if jn is None else jn
+    r.V = float("nan") if V is None else V
+    p = np.asarray(uP, float)
+    r.uP[:] = list(p / np.linalg.norm(p))
+    r.s[:] = [float("nan")] * 3 if s is None else list(np.asarray(s, float))
     return r
 
 
@@ -415,6 +427,19 @@ class Context:
         v = C.c_int()
         self._check(self.L.fg_solver_info(self.h, C.byref(v), None))
         return v.value
+
+    def spin_info(self):
+        """fg_spin_info: last spin solve (status, iterations), the potential V and its CG iterations."""
+        st, it, vit = C.c_int(), C.c_int(), C.c_int()
+        V = np.zeros(self.nn)
+        self._check(self.L.fg_spin_info(self.h, C.byref(st), C.byref(it), _ptr(V), C.byref(vit)))
+        return {"status": st.value, "iters": it.value, "V": V, "V_iters": vit.value}
+
+    def get_spin(self):
+        """fg_get_spin: the spin accumulation s, (n_nodes, 3)."""
+        s = np.zeros((self.nn, 3))
+        self._check(self.L.fg_get_spin(self.h, _ptr(s)))
+        return s
 
     def gauss_points(self):
         """fg_gauss_points: coordinates of the magnetic tets' Gauss points, (n_mag_tets * npi, 3)."""

@@ -44,13 +44,7 @@ static cudaError_t upload(T **p, const std::vector<T> &h) {
     return e;
 }
 
-namespace {
-
-struct Rules {
-    int npi_t, npi_f;
-    double ta[4][5], tp[5], fa[3][4], fp[4];
-};
-
+namespace fg {
 Rules make_rules(bool one) {
     Rules r{};
     if (one) {
@@ -84,6 +78,9 @@ Rules make_rules(bool one) {
     }
     return r;
 }
+}  // namespace fg
+
+namespace {
 
 struct P3 {
     double x, y, z;
@@ -135,6 +132,8 @@ void fg_opts_default(fg_opts *o) {
     o->mlp_lr = 1e-3;
     o->fmm_tensor = 1;
     o->mlp_train_every = 1;
+    o->spin_tol = 1e-8;        // spinAcc and electrostatSolver tolerance (src/main.cpp:252)
+    o->spin_max_iter = 1000;
 }
 
 const char *fg_strerror(int s) {
@@ -163,6 +162,10 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
         if (c.opts.precision != FG_PREC_FP32_REFINE || c.opts.learned_guess ||
             c.opts.demag == FG_DEMAG_DIRECT) {
             c.err = "fg_batch_create: a batch needs precision FG_PREC_FP32_REFINE, demag FMM and no learned guess";
+            return FG_EINVAL;
+        }
+        if (c.opts.spin_acc) {
+            c.err = "fg_batch_create: spin accumulation is not available for batches";
             return FG_EINVAL;
         }
         c.opts.demag = FG_DEMAG_FMM;
@@ -419,6 +422,10 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     CK(upload(&c.da, da));
     CK(upload(&c.detJ, detJ));
     CK(upload(&c.treg, htreg));
+    if (c.opts.spin_acc) {  // before the region table goes to the device: it adds the Hst prefactors
+        const int s = spin_setup(c, m, regs, nreg, tregs, ntreg, hreg);
+        if (s != FG_OK) return s;
+    }
     CK(upload(&c.regs, hreg));
     c.nreg = nreg;
     CK(upload(&c.mag, mag));
@@ -629,6 +636,7 @@ void fg_destroy(fg_ctx *h) {
         if (p) cudaFree(p);
     fmm_free(c);
     mlp_free(c);
+    spin_free(c);
     batch_free(c);
     if (c.heff) cudaFree(c.heff);
     if (c.hres) cudaFreeHost(c.hres);
@@ -793,6 +801,10 @@ int fg_compute_all(fg_ctx *h, const double Hext[3], double energies[4]) {
     CK(cudaEventRecord(c.ev[3], c.stream));
     int s = c.opts.first_order ? demag_into(h, c.u[1], c.phi[1]) : demag_pair(h);
     if (s) return s;
+    if (c.spin) {  // spinAcc::compute after the demag (src/fem.h:203-224)
+        CK(launch_spin(c));
+        c.launches += 1;
+    }
     CK(cudaEventRecord(c.ev[4], c.stream));
     double E[4];
     s = energy_impl(h, Hext, E, nullptr);
@@ -936,6 +948,19 @@ int fg_debug_wait_timeout(fg_ctx *h, int which) {
         c.err = which == 0 ? "grid barrier: bounded wait expired" : "mbarrier: bounded wait expired";
         return FG_ETIMEDOUT;
     }
+    return FG_OK;
+}
+
+int fg_spin_info(const fg_ctx *h, int *status, int *iters, double *V, int *v_iters) {
+    if (!h || !h->c.spin) return FG_EINVAL;
+    return spin_info(h->c, status, iters, V, v_iters);
+}
+
+int fg_get_spin(const fg_ctx *hc, double *s) {
+    if (!hc || !s || !hc->c.spin_s) return FG_EINVAL;
+    Ctx &c = const_cast<fg_ctx *>(hc)->c;
+    CK(cudaMemcpyAsync(s, c.spin_s, 3 * sizeof(double) * c.nn, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
     return FG_OK;
 }
 

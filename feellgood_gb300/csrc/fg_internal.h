@@ -21,7 +21,16 @@ namespace fg {
 struct DevRegion {
     double A, Ms, alpha, Abis, K, Kbis, K3, K3bis;
     double uk[3], ex[3], ey[3], ez[3];
+    double hst;  // spin accumulation: Hst = hst * s at the Gauss points (0 without the coupling)
 };
+
+// Gauss rules of the tets (5 points, or 1) and triangles (4 points, or 1): shape functions
+// a_i(g) and weights per unit Jacobian (src/tetra.h:27-81, src/triangle.h:43-66).
+struct Rules {
+    int npi_t, npi_f;
+    double ta[4][5], tp[5], fa[3][4], fp[4];
+};
+Rules make_rules(bool one_point);
 
 // Per-magnetic-triangle constants for charges, self-corrections and energies.
 struct DevTri {
@@ -201,6 +210,9 @@ struct Ctx {
     // at every Gauss point g of every magnetic tet; F is [nmt][npi_t][3] or nullptr
     double *hsp = nullptr;
     double field_amp = 1.0;
+    // spin accumulation (fg_spin.cu): solver state and the last solution s [3 nn]
+    void *spin = nullptr;
+    double *spin_s = nullptr;
     double *pot = nullptr;       // nn
     double *pot2 = nullptr;      // nn, potential of src_q2
     double *epart = nullptr;     // energy partials
@@ -314,6 +326,11 @@ int mlp_debug_grad(Ctx &c, int nsamples, const float *hx, const float *hy, float
 int mlp_nparam();
 int batch_setup(Ctx &c, const std::vector<int4> &htet, const std::vector<int4> &htri);
 void batch_free(Ctx &c);
+int spin_setup(Ctx &c, const fg_mesh *m, const fg_region *regs, int nreg, const fg_tri_region *tregs, int ntreg,
+               std::vector<DevRegion> &hreg);
+void spin_free(Ctx &c);
+cudaError_t launch_spin(Ctx &c);
+int spin_info(const Ctx &c, int *status, int *iters, double *V, int *v_iters);
 cudaError_t launch_select_params(Ctx &c);
 cudaError_t launch_advance(Ctx &c);
 cudaError_t launch_energy_seg(Ctx &c);

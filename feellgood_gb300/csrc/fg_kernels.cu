@@ -47,7 +47,8 @@ __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__
                                                const double *__restrict__ phiv0, double dt, double Hx, double Hy,
                                                double Hz, double4 *__restrict__ slot,
                                                const int *__restrict__ tet_seg, const SegPar *__restrict__ seg,
-                                               const double *__restrict__ hsp, double amp) {
+                                               const double *__restrict__ hsp, double amp,
+                                               const double *__restrict__ s_node) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nmt) return;
     if (seg) {  // batch: the tet's sample carries dt and the applied field
@@ -102,6 +103,10 @@ __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__
                           dU[2][0] * dU[2][0] + dU[2][1] * dU[2][1] + dU[2][2] * dU[2][2];
     const double He[3] = {Hd[0] + Hx, Hd[1] + Hy, Hd[2] + Hz};
     double w[NPI], aeff[NPI], H[NPI][3];
+    // spin accumulation field Hst = hst s at the Gauss points (spinAcc::prepareExtraField,
+    // Tetra::calc_Hst src/tetra.cpp:93-106), and the second-order term's (Hst . U) and V
+    const bool spin = s_node && R.hst != 0.0;
+    double Hst[NPI][3], sHu[NPI], Vg[NPI][3];
     const double reduced_dt = FG_GAMMA0 * dt;
     const double M = 2. * alpha * 0.1 / reduced_dt;
 #pragma unroll
@@ -155,7 +160,20 @@ __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__
             const double *F = hsp + 3 * ((size_t)t * NPI + g);
             Hg[0] += amp * F[0]; Hg[1] += amp * F[1]; Hg[2] += amp * F[2];
         }
-        uHeff += U[0] * Hg[0] + U[1] * Hg[1] + U[2] * Hg[2];
+        if (spin) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                double h = 0.0;
+#pragma unroll
+                for (int i = 0; i < 4; i++) h += (R.hst * s_node[3 * (size_t)ind[i] + c]) * c_ta[i][g];
+                Hst[g][c] = h;
+                Vg[g][c] = V[c];
+            }
+            sHu[g] = Hst[g][0] * U[0] + Hst[g][1] * U[1] + Hst[g][2] * U[2];
+            uHeff += U[0] * (Hg[0] + Hst[g][0]) + U[1] * (Hg[1] + Hst[g][1]) + U[2] * (Hg[2] + Hst[g][2]);
+        } else {
+            uHeff += U[0] * Hg[0] + U[1] * Hg[1] + U[2] * Hg[2];
+        }
         // calc_alpha_eff (src/tetra.cpp:47-75)
         double a;
         if (uHeff > 0.0)
@@ -183,7 +201,12 @@ __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 BE[c] -= w[g] * Abis * ex[c];
-                BE[c] += ai_w * H[g][c];
+                if (spin) {  // Hst and the spin accumulation's second-order term (src/tetra.cpp:296-303)
+                    BE[c] += ai_w * (H[g][c] + Hst[g][c]);
+                    BE[c] -= ai_w * sHu[g] * (FG_THETA * dt * FG_GAMMA0) * Vg[g][c];
+                } else {
+                    BE[c] += ai_w * H[g][c];
+                }
             }
         }
         slot[4 * (size_t)t + i] = make_double4(contrib, BE[0], BE[1], BE[2]);
@@ -1007,7 +1030,7 @@ cudaError_t launch_tet(Ctx &c, double dt, const double H[3]) {
     }
     if (c.nmt == 0) return cudaGetLastError();
     const int b = 128;
-    if (!c.aniso) {
+    if (!c.aniso && !c.spin_s) {
         if (c.npi_t == 5)
             k_tet64_iso<5><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0],
                                                                    c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
@@ -1023,11 +1046,13 @@ cudaError_t launch_tet(Ctx &c, double dt, const double H[3]) {
     if (c.npi_t == 5)
         k_tet64<5><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0], c.v[0],
                                                           c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
-                                                          c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp, c.field_amp);
+                                                          c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp, c.field_amp,
+                                                          c.spin_s);
     else
         k_tet64<1><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0], c.v[0],
                                                           c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
-                                                          c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp, c.field_amp);
+                                                          c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp, c.field_amp,
+                                                          c.spin_s);
     return cudaGetLastError();
 }
 

@@ -124,16 +124,27 @@ int write_sol(Run &R, const std::string &file, double t) {
     if (!f) return fail(FG_EIO, "cannot open file " + file);
     std::string meta = common_metadata(R.S, R.settings_name);
     std::fprintf(f, "%s", meta.c_str());
-    std::fprintf(f, "## time: %e\n## columns: idx\tmx\tmy\tmz\tphi\n", t);
+    const bool spin = R.S.spin_acc;
+    std::fprintf(f, "## time: %e\n## columns: idx\tmx\tmy\tmz\tphi%s\n", t, spin ? "\tsx\tsy\tsz" : "");
     const int p = R.S.precision;
     const int nn = R.md->n_nodes;
+    std::vector<double> s;
+    if (spin) {  // mesh::savesol with the spin accumulation (src/save.cpp:164-186)
+        s.assign(3 * (size_t)nn, 0.0);
+        if (fg_get_spin(R.ctx, s.data()) != FG_OK) {
+            std::fclose(f);
+            return fail(FG_EIO, "cannot read the spin accumulation");
+        }
+    }
     for (int i = 0; i < nn; i++) {
         const int k = R.md->node_index[i];
         if (R.mag[k])
-            std::fprintf(f, "%d\t%.*e\t%.*e\t%.*e\t%.*e\n", i, p, R.u[3 * k], p, R.u[3 * k + 1], p, R.u[3 * k + 2], p,
+            std::fprintf(f, "%d\t%.*e\t%.*e\t%.*e\t%.*e", i, p, R.u[3 * k], p, R.u[3 * k + 1], p, R.u[3 * k + 2], p,
                          R.phi[k]);
         else
-            std::fprintf(f, "%d\tnan\tnan\tnan\t%.*e\n", i, p, R.phi[k]);
+            std::fprintf(f, "%d\tnan\tnan\tnan\t%.*e", i, p, R.phi[k]);
+        if (spin) std::fprintf(f, "\t%.*e\t%.*e\t%.*e", p, s[3 * k], p, s[3 * k + 1], p, s[3 * k + 2]);
+        std::fputc('\n', f);
     }
     std::fclose(f);
     return FG_OK;
@@ -212,6 +223,7 @@ int run_impl(Run &R, const char *settings_path, unsigned int seed, int verbose, 
     std::vector<fg_region> regs(1 + S.vol.size());
     auto set_vol = [](fg_region &g, const fgh::VolRegion &r) {
         g.Ae = r.Ae; g.Ms = r.Ms; g.K = r.K; g.K3 = r.K3; g.alpha = r.alpha;
+        g.sigma = r.sigma; g.dens_state = r.dens_state; g.P = r.P; g.lsd = r.lsd; g.lsf = r.lsf;
         for (int k = 0; k < 3; k++) { g.uk[k] = r.uk[k]; g.ex[k] = r.ex[k]; g.ey[k] = r.ey[k]; g.ez[k] = r.ez[k]; }
     };
     set_vol(regs[0], S.vol_default);
@@ -219,7 +231,8 @@ int run_impl(Run &R, const char *settings_path, unsigned int seed, int verbose, 
     std::vector<fg_tri_region> tregs(std::max(1, R.md->n_surf_regions));
     auto set_surf = [](fg_tri_region &g, const fgh::SurfRegion &r) {
         g.Ks = r.Ks; g.suppress_charges = r.suppress_charges ? 1 : 0;
-        for (int k = 0; k < 3; k++) g.uk[k] = r.uk[k];
+        g.jn = r.jn; g.V = r.V;
+        for (int k = 0; k < 3; k++) { g.uk[k] = r.uk[k]; g.uP[k] = r.uP[k]; g.s[k] = r.s[k]; }
     };
     for (int k = 0; k < R.md->n_surf_regions; k++) {
         if (k >= 1 && k <= (int)S.surf.size()) set_surf(tregs[k], S.surf[k - 1]);
@@ -248,12 +261,23 @@ int run_impl(Run &R, const char *settings_path, unsigned int seed, int verbose, 
     o.learned_guess = S.gpu_learned ? 1 : 0;
     o.demag = S.gpu_demag;
     o.one_gauss_point = S.one_gauss_point ? 1 : 0;
+    o.spin_acc = S.spin_acc ? 1 : 0;
     o.verbose = verbose;
     fg_mesh m;
     fg_mesh_view(R.md, &m);
     s = fg_create(&m, regs.data(), (int)regs.size(), tregs.data(), R.md->n_surf_regions, &o, &R.ctx);
     if (s != FG_OK) return fail(s, fg_last_error(nullptr));
     const int nn = R.md->n_nodes;
+    if (S.spin_acc && S.V_file) {  // electrostatSolver::save (src/electrostatSolver.cpp:133-152)
+        std::vector<double> V(nn);
+        if (fg_spin_info(R.ctx, nullptr, nullptr, V.data(), nullptr) != FG_OK) return fail(FG_EINVAL, "no potential");
+        const std::string vf = S.out_dir + "/" + S.sim_name + "_V.sol";
+        std::FILE *f = std::fopen(vf.c_str(), "w");
+        if (!f) return fail(FG_EIO, "cannot open file " + vf);
+        std::fprintf(f, "## real-world time: %s\n## columns: index\tV\n", now_string().c_str());
+        for (int i = 0; i < nn; i++) std::fprintf(f, "%d\t%.8e\n", i, V[R.md->node_index[i]]);
+        std::fclose(f);
+    }
     R.mag.assign(nn, 0);
     for (int t = 0; t < R.md->n_tets; t++)
         if (regs[R.md->tet_region[t]].Ms > 0)
@@ -457,7 +481,30 @@ int fg_settings_dump(const char *settings_path, char *out, int len) {
         for (size_t k = 0; k < S.surf.size(); k++)
             j << (k ? ", " : "") << "{\"name\": \"" << S.surf[k].name << "\", \"Ks\": " << S.surf[k].Ks
               << ", \"suppress_charges\": " << (S.surf[k].suppress_charges ? "true" : "false") << "}";
-        j << "]}";
+        auto num = [&](double x) {  // NaN (not given) as null
+            if (std::isnan(x)) j << "null";
+            else j << x;
+        };
+        j << "], \"spin_accumulation\": {\"enable\": " << (S.spin_acc ? "true" : "false")
+          << ", \"V_file\": " << (S.V_file ? "true" : "false") << ", \"volume\": [";
+        for (size_t k = 0; k < S.vol.size(); k++) {
+            const auto &r = S.vol[k];
+            j << (k ? ", " : "") << "{\"name\": \"" << r.name << "\", \"sigma\": " << r.sigma
+              << ", \"dens_state\": " << r.dens_state << ", \"P\": " << r.P << ", \"l_sd\": " << r.lsd
+              << ", \"l_sf\": " << r.lsf << "}";
+        }
+        j << "], \"surface\": [";
+        for (size_t k = 0; k < S.surf.size(); k++) {
+            const auto &r = S.surf[k];
+            j << (k ? ", " : "") << "{\"name\": \"" << r.name << "\", \"jn\": ";
+            num(r.jn);
+            j << ", \"V\": ";
+            num(r.V);
+            j << ", \"uP\": [" << r.uP[0] << ", " << r.uP[1] << ", " << r.uP[2] << "], \"s\": [";
+            num(r.s[0]); j << ", "; num(r.s[1]); j << ", "; num(r.s[2]);
+            j << "]}";
+        }
+        j << "]}}";
         const std::string s = j.str();
         if ((int)s.size() + 1 > len) return FG_EINVAL;
         std::memcpy(out, s.c_str(), s.size() + 1);

@@ -361,6 +361,11 @@ void apply_yaml(Settings &S, const std::shared_ptr<YNode> &y) {
                     if (auto d = R->get("ey"); !is_null(d)) to_vec(d, r.ey, true, kv.first + ".ey");
                     if (auto d = R->get("ez"); !is_null(d)) to_vec(d, r.ez, true, kv.first + ".ez");
                     if (auto d = R->get("alpha_LLG"); !is_null(d)) r.alpha = to_num(d, kv.first + ".alpha_LLG");
+                    if (auto d = R->get("sigma"); !is_null(d)) r.sigma = to_num(d, kv.first + ".sigma");
+                    if (auto d = R->get("dens_state"); !is_null(d)) r.dens_state = to_num(d, kv.first + ".dens_state");
+                    if (auto d = R->get("P"); !is_null(d)) r.P = to_num(d, kv.first + ".P");
+                    if (auto d = R->get("l_sd"); !is_null(d)) r.lsd = to_num(d, kv.first + ".l_sd");
+                    if (auto d = R->get("l_sf"); !is_null(d)) r.lsf = to_num(d, kv.first + ".l_sf");
                 }
                 if (kv.first == "__default__") S.vol_default = r;
                 else S.vol.push_back(r);
@@ -376,6 +381,10 @@ void apply_yaml(Settings &S, const std::shared_ptr<YNode> &y) {
                     if (auto d = R->get("suppress_charges"); !is_null(d)) r.suppress_charges = to_bool(d, kv.first + ".suppress_charges");
                     if (auto d = R->get("Ks"); !is_null(d)) r.Ks = to_num(d, kv.first + ".Ks");
                     if (auto d = R->get("uk"); !is_null(d)) to_vec(d, r.uk, true, kv.first + ".uk");
+                    if (auto d = R->get("jn"); !is_null(d)) r.jn = to_num(d, kv.first + ".jn");
+                    if (auto d = R->get("V"); !is_null(d)) r.V = to_num(d, kv.first + ".V");
+                    if (auto d = R->get("uP"); !is_null(d)) to_vec(d, r.uP, true, kv.first + ".uP");
+                    if (auto d = R->get("s"); !is_null(d)) to_vec(d, r.s, false, kv.first + ".s");
                 }
                 if (kv.first == "__default__") S.surf_default = r;
                 else S.surf.push_back(r);
@@ -401,8 +410,8 @@ void apply_yaml(Settings &S, const std::shared_ptr<YNode> &y) {
         to_vec(d, S.Bext, false, "Bext");
     }
     if (auto d = y->get("spin_accumulation"); !is_null(d)) {
-        if (auto e = d->get("enable"); !is_null(e) && to_bool(e, "spin_accumulation.enable"))
-            throw SettingsError("spin accumulation is not supported by this build");
+        if (auto e = d->get("enable"); !is_null(e)) S.spin_acc = to_bool(e, "spin_accumulation.enable");
+        if (auto e = d->get("V_file"); !is_null(e)) S.V_file = to_bool(e, "spin_accumulation.V_file");
     }
     if (auto s = y->get("finite_element_solver"); !is_null(s)) {
         if (auto d = s->get("max(iter)"); !is_null(d)) S.max_iter = (int)to_num(d, "max(iter)");

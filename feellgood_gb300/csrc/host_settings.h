@@ -4,6 +4,7 @@
 #include <iostream>
 #include <memory>
 #include <stdexcept>
+#include <cmath>
 #include <string>
 #include <utility>
 #include <vector>
@@ -33,11 +34,15 @@ struct VolRegion {
     std::string name;
     double Ae = 1e-11, Ms = 795774.7, K = 0.0, uk[3] = {0, 0, 1}, K3 = 0.0;
     double ex[3] = {1, 0, 0}, ey[3] = {0, 1, 0}, ez[3] = {0, 0, 1}, alpha = 0.5;
+    double sigma = 0.0, dens_state = 0.0, P = 0.0, lsd = 0.0, lsf = 0.0;  // spin accumulation
 };
 struct SurfRegion {
     std::string name;
     bool suppress_charges = false;
     double Ks = 0.0, uk[3] = {0, 0, 1};
+    // boundary conditions of the electrostatic and spin-diffusion problems (NaN: not given)
+    double jn = std::nan(""), V = std::nan(""), uP[3] = {0, 0, 1};
+    double s[3] = {std::nan(""), std::nan(""), std::nan("")};
 };
 
 struct Settings {
@@ -63,6 +68,7 @@ struct Settings {
     // options of this build, read from an optional "gpu:" section
     int gpu_precision = 0, gpu_demag = 0;
     bool gpu_learned = false, one_gauss_point = false;
+    bool spin_acc = false, V_file = false;  // spin_accumulation.enable, .V_file
     int checkpoint_every = 0;    // write <out_dir>/<sim_name>.ckpt after every n-th output row
     int solver_lpr = 0, solver_blocks = 0, fmm_depth = 0;  // fixed solver / FMM choices (0: timed)
     std::string resume_file;     // continue the run of this checkpoint

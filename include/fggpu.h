@@ -64,15 +64,20 @@ typedef struct {
     const double *tri_dMs;     /* n_tris */
 } fg_mesh;
 
-/* Tetra::prm subset (src/tetra.h:86-112); Ms <= 0 marks a non-magnetic region. */
+/* Tetra::prm subset (src/tetra.h:86-112); Ms <= 0 marks a non-magnetic region. The last
+ * five are the spin-accumulation parameters (used only with fg_opts.spin_acc): conductivity
+ * sigma, density of states N0 (dens_state), polarization rate P, s-d and spin-flip lengths. */
 typedef struct {
     double Ae, Ms, K, uk[3], K3, ex[3], ey[3], ez[3], alpha;
+    double sigma, dens_state, P, lsd, lsf;
 } fg_region;
 
-/* Triangle::prm subset (src/triangle.h:69-101) */
+/* Triangle::prm subset (src/triangle.h:69-101). jn, V and s are NaN where not given (the
+ * boundary conditions of the electrostatic and spin-diffusion problems, fg_opts.spin_acc). */
 typedef struct {
     double Ks, uk[3];
     int suppress_charges;
+    double jn, V, uP[3], s[3];
 } fg_tri_region;
 
 typedef struct {
@@ -105,6 +110,12 @@ typedef struct {
                              (0: all co-resident blocks). Fixing both (and fmm_leaf = -depth)
                              makes runs repeat bit for bit: the timed choices decide the
                              order of the solver's reductions */
+    int spin_acc;         /* 1: spin accumulation coupling (spin_accumulation.enable): the
+                             electrostatic potential is solved once, the spin accumulation s
+                             in every fg_compute_all, and its field Hst enters the next
+                             step's element integrals */
+    double spin_tol;      /* relative tolerance of the spin and potential solves (1e-8) */
+    int spin_max_iter;    /* their iteration limit (1000) */
 } fg_opts;
 
 typedef struct {
@@ -172,6 +183,13 @@ int fg_energy_noalloc(fg_ctx *ctx, const double Hext[3], double energies[4]);
  * With a space field set, the applied field at Gauss point g is Hext + A f(g), Hext being the
  * uniform field those calls take (pass zeros for a pure R4toR3 run). Not for batches. */
 int fg_gauss_points(const fg_ctx *ctx, int *n_points, double *pts);
+
+/* Spin accumulation (fg_opts.spin_acc): the last spin solve's status (FG_OK when converged;
+ * on failure s is zero, as spinAcc::compute leaves it) and iterations, the electrostatic
+ * potential V[n_nodes] (host copy, may be NULL) and its CG iterations; fg_get_spin copies s
+ * [n_nodes][3] (the field of the next step's Hst). */
+int fg_spin_info(const fg_ctx *ctx, int *status, int *iters, double *V, int *v_iters);
+int fg_get_spin(const fg_ctx *ctx, double *s);
 int fg_set_space_field(fg_ctx *ctx, const double *field);
 int fg_set_field_amplitude(fg_ctx *ctx, double amplitude);
 

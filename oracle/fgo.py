@@ -18,31 +18,39 @@ _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 class Region(C.Structure):
     _fields_ = [("A", C.c_double), ("Ms", C.c_double), ("K", C.c_double), ("uk", C.c_double * 3),
                 ("K3", C.c_double), ("ex", C.c_double * 3), ("ey", C.c_double * 3), ("ez", C.c_double * 3),
-                ("alpha", C.c_double)]
+                ("alpha", C.c_double), ("sigma", C.c_double), ("N0", C.c_double), ("P", C.c_double),
+                ("lsd", C.c_double), ("lsf", C.c_double)]
 
 
 class TriRegion(C.Structure):
-    _fields_ = [("Ks", C.c_double), ("uk", C.c_double * 3), ("suppress_charges", C.c_int)]
+    _fields_ = [("Ks", C.c_double), ("uk", C.c_double * 3), ("suppress_charges", C.c_int), ("jn", C.c_double),
+                ("V", C.c_double), ("uP", C.c_double * 3), ("s", C.c_double * 3)]
 
 
 def make_region(A=1e-11, Ms=795774.7, K=0.0, uk=(0, 0, 1), K3=0.0, ex=(1, 0, 0), ey=(0, 1, 0), ez=(0, 0, 1),
-                alpha=0.5):
+                alpha=0.5, sigma=0.0, N0=0.0, P=0.0, lsd=0.0, lsf=0.0):
     def unit(v):
         v = np.asarray(v, float)
         return v / np.linalg.norm(v)
     r = Region()
     r.A, r.Ms, r.K, r.K3, r.alpha = A, Ms, K, K3, alpha
+    r.sigma, r.N0, r.P, r.lsd, r.lsf = sigma, N0, P, lsd, lsf
     for name, v in (("uk", uk), ("ex", ex), ("ey", ey), ("ez", ez)):
         getattr(r, name)[:] = list(unit(v))
     return r
 
 
-def make_tri_region(Ks=0.0, uk=(0, 0, 1), suppress_charges=False):
+def make_tri_region(Ks=0.0, uk=(0, 0, 1), suppress_charges=False, jn=None, V=None, uP=(0, 0, 1), s=None):
     r = TriRegion()
     r.Ks = Ks
     u = np.asarray(uk, float)
     r.uk[:] = list(u / np.linalg.norm(u))
     r.suppress_charges = int(bool(suppress_charges))
+    r.jn = float("nan") if jn is None else jn
+    r.V = float("nan") if V is None else V
+    p = np.asarray(uP, float)
+    r.uP[:] = list(p / np.linalg.norm(p))
+    r.s[:] = [float("nan")] * 3 if s is None else list(np.asarray(s, float))
     return r
 
 
@@ -63,6 +71,9 @@ def lib():
         L.fgo_max_threads.restype = C.c_int
         L.fgo_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_int]
         L.fgo_set_space_field.argtypes = [C.c_void_p, C.c_void_p, C.c_double]
+        L.fgo_set_spin.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int)]
+        L.fgo_get_spin.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.fgo_set_state.argtypes = [C.c_void_p, _dp, C.c_void_p, C.c_void_p, C.c_void_p]
         L.fgo_get_state.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]
         L.fgo_get_basis.argtypes = [C.c_void_p, _dp, _dp]
@@ -135,6 +146,20 @@ class Oracle:
 
     def set_solver(self, tol=1e-6, maxiter=700):
         self.L.fgo_set_solver(self.h, tol, maxiter)
+
+    def set_spin(self, enable=True, tol=1e-8, maxiter=1000):
+        """Spin accumulation on: solves the electrostatic potential now; returns its (status, iters)."""
+        st, it = C.c_int(), C.c_int()
+        self.L.fgo_set_spin(self.h, int(enable), tol, maxiter, C.byref(st), C.byref(it))
+        return st.value, it.value
+
+    def spin(self):
+        """(V [nn], s [nn, 3], last spin solve status, iterations)."""
+        V, s = np.zeros(self.nn), np.zeros((self.nn, 3))
+        st, it = C.c_int(), C.c_int()
+        self.L.fgo_get_spin(self.h, V.ctypes.data_as(C.c_void_p), s.ctypes.data_as(C.c_void_p), C.byref(st),
+                            C.byref(it))
+        return V, s, st.value, it.value
 
     def set_space_field(self, field, amp=1.0):
         """R4toR3 applied field: f at the magnetic tets' Gauss points ([n_mag_tets * npi, 3],

@@ -34,6 +34,8 @@ namespace {
 constexpr double MU0 = 1.25663706127e-6;
 constexpr double GAMMA0 = 1.76085962784e11 * MU0;
 constexpr double THETA = 0.5;
+constexpr double QE = 1.602176634e-19;  // src/config.h.in:31-37
+constexpr double MUB = QE * (6.62607015e-34 / (2 * M_PI)) / (2. * 9.1093837139e-31);
 
 inline double sq(double x) { return x * x; }
 
@@ -108,10 +110,12 @@ TriRule make_tri_rule(bool one_point) {
 // Tetra::prm subset (src/tetra.h:86-112) and Triangle::prm subset (src/triangle.h:69-101).
 struct Region {
     double A, Ms, K, uk[3], K3, ex[3], ey[3], ez[3], alpha;
+    double sigma, N0, P, lsd, lsf;  // spin accumulation (src/tetra.h:86-112)
 };
 struct TriRegion {
     double Ks, uk[3];
     int suppress_charges;
+    double jn, V, uP[3], s[3];  // NaN where not given (src/triangle.h:69-101)
 };
 
 struct Node {
@@ -138,6 +142,12 @@ struct Oracle {
     // of every tet [nt][npi][3] (zero for non-magnetic tets), used as Hext + amp f(g)
     std::vector<double> hsp;
     double amp = 1.0;
+    // spin accumulation (spinAcc, electrostatSolver): potential V, spin accumulation s
+    bool spin = false;
+    double spin_tol = 1e-8;
+    int spin_maxiter = 1000, spin_status = -1, spin_nit = 0, V_status = -1, V_nit = 0;
+    std::vector<double> Vpot;
+    std::vector<V3> sacc;
     double totalMagVol = 0;
     // scalar CSR with 2x2 blocks per node and per edge (src/solver.h:75-104)
     std::vector<int> rowptr, col;
@@ -381,11 +391,23 @@ void integrales(Oracle &o, int t, double dt, double prefactor, const double Hext
     }
     V3 H[5];
     V3 He = v3(Hext);
+    // spin accumulation field (spinAcc::prepareExtraField, Tetra::calc_Hst src/tetra.cpp:93-106)
+    V3 Hst[5];
+    const bool spin = o.spin && !o.sacc.empty();
+    if (spin) {
+        const double D0 = 2.0 * p.sigma / (QE * QE * p.N0);
+        const double pref = D0 / (sq(p.lsd) * GAMMA0 * Ms);
+        for (int g = 0; g < npi; g++) {
+            Hst[g] = {0, 0, 0};
+            for (int i = 0; i < 4; i++) Hst[g] = Hst[g] + R.a[i][g] * (pref * o.sacc[ind[i]]);
+        }
+    }
     for (int g = 0; g < npi; g++) {
         V3 Heff = Hd + He;
         if (!o.hsp.empty())  // calc_Hext of the R4toR3 prepareElements (src/linear_algebra.cpp:54-72)
             Heff = Heff + o.amp * v3(&o.hsp[3 * ((size_t)t * npi + g)]);
         H[g] = Heff;
+        if (spin) Heff = Heff + Hst[g];
         uHeff[g] += dot(U[g], Heff);
     }
     double a_eff[5];
@@ -464,7 +486,12 @@ void integrales(Oracle &o, int t, double dt, double prefactor, const double Hext
             V3 ex = da[3 * i] * dUd[0] + da[3 * i + 1] * dUd[1] + da[3 * i + 2] * dUd[2];
             for (int d = 0; d < 3; d++) {
                 BE[d][i] -= wg * Abis * comp(ex, d);
-                BE[d][i] += ai_w * comp(H[g], d);
+                if (spin) {  // Hst and its second-order term (src/tetra.cpp:296-303)
+                    BE[d][i] += ai_w * (comp(H[g], d) + comp(Hst[g], d));
+                    BE[d][i] -= ai_w * dot(Hst[g], U[g]) * s_dt * comp(V[g], d);
+                } else {
+                    BE[d][i] += ai_w * comp(H[g], d);
+                }
             }
         }
     }
@@ -900,10 +927,307 @@ void energy(Oracle &o, const double Hext[3]) {
     for (int k = 0; k < 4; k++) o.E[k] = E[k];
 }
 
-// Fem::compute_all (src/fem.h:203-224) without spin accumulation.
+// ----- spin accumulation: electrostatSolver and spinAcc with explicit CSR assembly -----
+
+// Sparse matrix with the reference's shape over all tets (solver::build_shape): rows of
+// dim * node + component, every component pair of every node pair of a tet.
+struct Csr {
+    std::vector<int> ptr, col;
+    std::vector<double> val;
+    void add(int i, int j, double v) {
+        auto b = col.begin() + ptr[i], e = col.begin() + ptr[i + 1];
+        val[std::lower_bound(b, e, j) - col.begin()] += v;
+    }
+    double diag(int i) const {
+        auto b = col.begin() + ptr[i], e = col.begin() + ptr[i + 1];
+        auto q = std::lower_bound(b, e, i);
+        return (q != e && *q == i) ? val[q - col.begin()] : 0.0;
+    }
+    void mult(const std::vector<double> &x, std::vector<double> &y) const {
+        for (size_t r = 0; r + 1 < ptr.size(); r++) {
+            double s = 0;
+            for (int k = ptr[r]; k < ptr[r + 1]; k++) s += val[k] * x[col[k]];
+            y[r] = s;
+        }
+    }
+};
+
+Csr shape(const Oracle &o, int dim) {
+    std::vector<std::vector<int>> nb((size_t)o.nn * dim);
+    for (int t = 0; t < o.nt; t++)
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++)
+                for (int a = 0; a < dim; a++)
+                    for (int b = 0; b < dim; b++) nb[dim * o.tet[4 * t + i] + a].push_back(dim * o.tet[4 * t + j] + b);
+    Csr M;
+    M.ptr.assign(nb.size() + 1, 0);
+    for (size_t r = 0; r < nb.size(); r++) {
+        auto &v = nb[r];
+        v.push_back((int)r);
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        M.ptr[r + 1] = M.ptr[r] + (int)v.size();
+    }
+    for (auto &v : nb) M.col.insert(M.col.end(), v.begin(), v.end());
+    M.val.assign(M.col.size(), 0.0);
+    return M;
+}
+
+// algebra::cg_dir (src/algebra/cg.h:67-121)
+void cg_dir(const Csr &A, std::vector<double> &x, const std::vector<double> &rhs, const std::vector<double> &xd,
+            const std::vector<int> &ld, Iter &it) {
+    const size_t n = x.size();
+    std::vector<double> p(n), q(n), r(n), z(n), diag(n), b(rhs), tmp(n);
+    for (size_t i = 0; i < n; i++) diag[i] = 1.0 / A.diag((int)i);
+    A.mult(xd, z);
+    for (size_t i = 0; i < n; i++) b[i] -= z[i];
+    mask(ld, b);
+    mask(ld, diag);
+    it.rhsn = vnorm(b);
+    r = b;
+    A.mult(x, tmp);
+    for (size_t i = 0; i < n; i++) r[i] -= tmp[i];
+    mask(ld, r);
+    for (size_t i = 0; i < n; i++) z[i] = diag[i] * r[i];
+    double rho = vdot(z, r), rho_1 = 0.0;
+    p = z;
+    while (!it.finished(vnorm(r)) && it.status != 1 && it.status != 2) {
+        if (it.nit > 0) {
+            for (size_t i = 0; i < n; i++) z[i] = diag[i] * r[i];
+            rho = vdot(z, r);
+            for (size_t i = 0; i < n; i++) p[i] *= rho / rho_1;
+            for (size_t i = 0; i < n; i++) p[i] += z[i];
+        }
+        A.mult(p, q);
+        mask(ld, q);
+        const double qp = vdot(q, p);
+        if (qp == 0.0) {
+            it.status = 2;
+            break;
+        }
+        const double a = rho / qp;
+        for (size_t i = 0; i < n; i++) x[i] += a * p[i];
+        for (size_t i = 0; i < n; i++) r[i] += (-a) * q[i];
+        rho_1 = rho;
+        it.inc();
+    }
+    for (size_t i = 0; i < n; i++) x[i] += xd[i];
+}
+
+// algebra::bicg_dir with Dirichlet values (src/algebra/bicg.h:82-153)
+void bicg_dir_values(const Csr &A, std::vector<double> &x, const std::vector<double> &rhs,
+                     const std::vector<double> &xd, const std::vector<int> &ld, Iter &it) {
+    const size_t n = x.size();
+    double rho_1 = 0, rho_2 = 0, alpha = 0, beta = 0, omega = 0;
+    std::vector<double> p(n), phat(n), shat(n), r(n), rt(n), s(n), t(n), v(n), diag(n), b(rhs);
+    for (size_t i = 0; i < n; i++) diag[i] = 1.0 / A.diag((int)i);
+    A.mult(xd, v);
+    for (size_t i = 0; i < n; i++) b[i] -= v[i];
+    mask(ld, b);
+    mask(ld, diag);
+    it.rhsn = vnorm(b);
+    r = b;
+    A.mult(x, v);
+    for (size_t i = 0; i < n; i++) r[i] -= v[i];
+    mask(ld, r);
+    rt = r;
+    p = r;
+    while (!it.finished(vnorm(r))) {
+        rho_1 = vdot(rt, r);
+        if (it.nit > 0) {
+            if (rho_2 == 0 || omega == 0) {
+                it.status = 2;
+                break;
+            }
+            beta = (rho_1 / rho_2) * (alpha / omega);
+            for (size_t i = 0; i < n; i++) p[i] = (p[i] - omega * v[i]) * beta + r[i];
+        }
+        for (size_t i = 0; i < n; i++) phat[i] = diag[i] * p[i];
+        A.mult(phat, v);
+        mask(ld, v);
+        alpha = rho_1 / vdot(v, rt);
+        for (size_t i = 0; i < n; i++) s[i] = r[i] + (-alpha) * v[i];
+        if (it.finished(vnorm(s))) {
+            for (size_t i = 0; i < n; i++) x[i] += alpha * phat[i];
+            break;
+        } else if (it.status == 1 || it.status == 2) {
+            break;
+        }
+        for (size_t i = 0; i < n; i++) shat[i] = diag[i] * s[i];
+        A.mult(shat, t);
+        mask(ld, t);
+        omega = vdot(t, s) / vdot(t, t);
+        for (size_t i = 0; i < n; i++) {
+            x[i] += alpha * phat[i];
+            x[i] += omega * shat[i];
+        }
+        for (size_t i = 0; i < n; i++) r[i] = s[i] - omega * t[i];
+        rho_2 = rho_1;
+        it.inc();
+    }
+    for (size_t i = 0; i < n; i++) x[i] += xd[i];
+}
+
+inline bool finite3(const double *v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+// electrostatSolver::solve (src/electrostatSolver.cpp:94-131), all tets and triangles
+void electrostat(Oracle &o) {
+    const TetRule &R = o.tr;
+    Csr K = shape(o, 1);
+    std::vector<double> L(o.nn, 0.0), Vd(o.nn, 0.0);
+    for (int t = 0; t < o.nt; t++) {
+        const double sigma = o.reg[o.tet_reg[t]].sigma;
+        const double *da = &o.da[12 * t];
+        const int *ind = &o.tet[4 * t];
+        double AE[4][4] = {};
+        for (int g = 0; g < R.npi; g++) {
+            const double sw = sigma * o.wt[(size_t)t * R.npi + g];
+            for (int i = 0; i < 4; i++)
+                for (int j = 0; j < 4; j++)
+                    AE[i][j] += sw * (da[3 * i] * da[3 * j] + da[3 * i + 1] * da[3 * j + 1] + da[3 * i + 2] * da[3 * j + 2]);
+        }
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) K.add(ind[i], ind[j], AE[i][j]);
+    }
+    for (int f = 0; f < o.nf; f++) {
+        const TriRegion &g = o.treg[o.tri_reg[f]];
+        const double J = std::isfinite(g.jn) ? g.jn : 0.0;
+        double BE[3] = {0, 0, 0};
+        for (int q = 0; q < o.fr.npi; q++) {
+            const double Jw = J * o.tri_w[(size_t)f * o.fr.npi + q];
+            for (int i = 0; i < 3; i++) BE[i] -= o.fr.a[i][q] * Jw;
+        }
+        for (int i = 0; i < 3; i++) L[o.tri[3 * f + i]] += BE[i];
+    }
+    std::vector<int> ld;
+    for (int f = 0; f < o.nf; f++) {
+        const double V = o.treg[o.tri_reg[f]].V;
+        if (std::isnan(V)) continue;
+        for (int i = 0; i < 3; i++) {
+            Vd[o.tri[3 * f + i]] = V;
+            ld.push_back(o.tri[3 * f + i]);
+        }
+    }
+    std::sort(ld.begin(), ld.end());
+    ld.erase(std::unique(ld.begin(), ld.end()), ld.end());
+    o.Vpot.assign(o.nn, 0.0);
+    Iter it;
+    it.resmax = o.spin_tol;
+    it.maxiter = o.spin_maxiter;
+    cg_dir(K, o.Vpot, L, Vd, ld, it);
+    o.V_status = it.status;
+    o.V_nit = it.nit;
+}
+
+// spinAcc::solve / compute (src/spinAccumulationSolver.cpp:130-287): operator with m of
+// CURRENT (calcOffDiagBlock), RHS with m of NEXT (getNode_u); s = 0 when it fails.
+void spin_solve(Oracle &o) {
+    const TetRule &R = o.tr;
+    const int N = 4;
+    Csr K = shape(o, 3);
+    std::vector<double> L(3 * (size_t)o.nn, 0.0), xd(3 * (size_t)o.nn, 0.0);
+    for (int t = 0; t < o.nt; t++) {
+        const Region &p = o.reg[o.tet_reg[t]];
+        const double *da = &o.da[12 * t];
+        const double *w = &o.wt[(size_t)t * R.npi];
+        const int *ind = &o.tet[4 * t];
+        const double D0 = 2.0 * p.sigma / (sq(QE) * p.N0);
+        double aw[4] = {0, 0, 0, 0}, wsum = 0;
+        for (int i = 0; i < 4; i++)
+            for (int g = 0; g < R.npi; g++) aw[i] += R.a[i][g] * w[g];
+        for (int g = 0; g < R.npi; g++) wsum += w[g];
+        double AE[12][12] = {};
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) {
+                double v = (da[3 * i] * da[3 * j] + da[3 * i + 1] * da[3 * j + 1] + da[3 * i + 2] * da[3 * j + 2]) *
+                           (D0 * wsum);
+                if (i == j) v += (D0 / sq(p.lsf)) * aw[i];
+                for (int d = 0; d < 3; d++) AE[d * N + i][d * N + j] += v;
+            }
+        double BE[12] = {};
+        if (p.Ms > 0) {
+            const double itsd = D0 / sq(p.lsd);
+            for (int i = 0; i < 4; i++) {
+                const V3 m = o.node[ind[i]].u[CUR];
+                const double dx = itsd * aw[i] * m.x, dy = itsd * aw[i] * m.y, dz = itsd * aw[i] * m.z;
+                AE[N + i][2 * N + i] += dx;
+                AE[2 * N + i][N + i] -= dx;
+                AE[i][2 * N + i] -= dy;
+                AE[2 * N + i][i] += dy;
+                AE[i][N + i] += dz;
+                AE[N + i][i] -= dz;
+            }
+            const double cst0 = MUB * p.P * p.sigma / QE;
+            V3 gV = {0, 0, 0};
+            for (int i = 0; i < 4; i++) gV = gV + o.Vpot[ind[i]] * v3(&da[3 * i]);
+            for (int g = 0; g < R.npi; g++) {
+                const V3 c = (cst0 * w[g]) * gV;
+                for (int i = 0; i < 4; i++) {
+                    const V3 m = o.node[ind[i]].u[NXT];
+                    const double tmp = dot(c, v3(&da[3 * i]));
+                    BE[i] += tmp * m.x;
+                    BE[N + i] += tmp * m.y;
+                    BE[2 * N + i] += tmp * m.z;
+                }
+            }
+        }
+        for (int a = 0; a < 12; a++) {
+            for (int b = 0; b < 12; b++)
+                if (AE[a][b] != 0.0) K.add(3 * ind[a % N] + a / N, 3 * ind[b % N] + b / N, AE[a][b]);
+            L[3 * (size_t)ind[a % N] + a / N] += BE[a];
+        }
+    }
+    for (int f = 0; f < o.nf; f++) {
+        const TriRegion &g = o.treg[o.tri_reg[f]];
+        double sv[3] = {g.s[0], g.s[1], g.s[2]};
+        if (std::isfinite(g.jn) && finite3(g.uP))
+            for (int d = 0; d < 3; d++) sv[d] = -g.jn * (MUB / QE) * g.uP[d];
+        if (!finite3(sv)) continue;
+        for (int q = 0; q < o.fr.npi; q++) {
+            const double wq = o.tri_w[(size_t)f * o.fr.npi + q];
+            for (int i = 0; i < 3; i++) {
+                const double aiw = wq * o.fr.a[i][q];
+                for (int d = 0; d < 3; d++) L[3 * (size_t)o.tri[3 * f + i] + d] -= sv[d] * aiw;
+            }
+        }
+    }
+    std::vector<int> ld;
+    for (int f = 0; f < o.nf; f++) {
+        const TriRegion &g = o.treg[o.tri_reg[f]];
+        double sv[3];
+        if (!finite3(g.s) && std::isfinite(g.jn)) {
+            for (int d = 0; d < 3; d++) sv[d] = -g.jn * (MUB / QE) * g.uP[d];
+        } else if (finite3(g.s) && std::isnan(g.jn)) {
+            for (int d = 0; d < 3; d++) sv[d] = g.s[d];
+        } else {
+            continue;
+        }
+        for (int i = 0; i < 3; i++)
+            for (int d = 0; d < 3; d++) {
+                xd[3 * (size_t)o.tri[3 * f + i] + d] = sv[d];
+                ld.push_back(3 * o.tri[3 * f + i] + d);
+            }
+    }
+    std::sort(ld.begin(), ld.end());
+    ld.erase(std::unique(ld.begin(), ld.end()), ld.end());
+    std::vector<double> X(3 * (size_t)o.nn, 0.0);
+    Iter it;
+    it.resmax = o.spin_tol;
+    it.maxiter = o.spin_maxiter;
+    bicg_dir_values(K, X, L, xd, ld, it);
+    o.spin_status = it.status;
+    o.spin_nit = it.nit;
+    o.sacc.assign(o.nn, {0, 0, 0});
+    if (it.status == 0)
+        for (int i = 0; i < o.nn; i++) o.sacc[i] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
+}
+
+// Fem::compute_all (src/fem.h:203-224): demag of m and v, the spin accumulation when
+// enabled, energies, CURRENT <- NEXT.
 void compute_all(Oracle &o, const double Hext[3], bool first_order) {
     demag_direct(o, 0);
     if (!first_order) demag_direct(o, 1);
+    if (o.spin) spin_solve(o);
     energy(o, Hext);
     for (auto &nd : o.node) {
         nd.u[CUR] = nd.u[NXT];
@@ -974,10 +1298,12 @@ extern "C" {
 
 struct fgo_region {
     double A, Ms, K, uk[3], K3, ex[3], ey[3], ez[3], alpha;
+    double sigma, N0, P, lsd, lsf;
 };
 struct fgo_tri_region {
     double Ks, uk[3];
     int suppress_charges;
+    double jn, V, uP[3], s[3];
 };
 
 void *fgo_create(int nn, const double *xyz, int nt, const int *tet, const int *tet_reg, int nf, const int *tri,
@@ -1014,6 +1340,12 @@ void *fgo_create(int nn, const double *xyz, int nt, const int *tet, const int *t
         g.Ks = tregs[r].Ks;
         for (int k = 0; k < 3; k++) g.uk[k] = tregs[r].uk[k];
         g.suppress_charges = tregs[r].suppress_charges;
+        g.jn = tregs[r].jn;
+        g.V = tregs[r].V;
+        for (int k = 0; k < 3; k++) {
+            g.uP[k] = tregs[r].uP[k];
+            g.s[k] = tregs[r].s[k];
+        }
         o->treg.push_back(g);
     }
     build_geometry(*o);
@@ -1048,6 +1380,34 @@ int fgo_max_threads() {
 #else
     return 1;
 #endif
+}
+
+// Spin accumulation on (the potential is solved here, once) or off; status and iterations of
+// the potential solve are returned.
+void fgo_set_spin(void *h, int enable, double tol, int maxiter, int *v_status, int *v_iters) {
+    Oracle *o = static_cast<Oracle *>(h);
+    o->spin = enable != 0;
+    o->spin_tol = tol;
+    o->spin_maxiter = maxiter;
+    o->sacc.clear();
+    if (o->spin) electrostat(*o);
+    if (v_status) *v_status = o->V_status;
+    if (v_iters) *v_iters = o->V_nit;
+}
+
+// V[nn], s[3 nn] (either may be NULL), last spin solve status and iterations.
+void fgo_get_spin(void *h, double *V, double *s, int *status, int *iters) {
+    Oracle *o = static_cast<Oracle *>(h);
+    if (V && !o->Vpot.empty()) std::memcpy(V, o->Vpot.data(), sizeof(double) * o->nn);
+    if (s)
+        for (int i = 0; i < o->nn; i++) {
+            const V3 v = o->sacc.empty() ? V3{0, 0, 0} : o->sacc[i];
+            s[3 * i] = v.x;
+            s[3 * i + 1] = v.y;
+            s[3 * i + 2] = v.z;
+        }
+    if (status) *status = o->spin_status;
+    if (iters) *iters = o->spin_nit;
 }
 
 // R4toR3 field: f at the Gauss points of the magnetic tets, [n_mag_tets][npi][3] in magTet

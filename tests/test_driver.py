@@ -174,3 +174,32 @@ def test_checkpoint_resume_is_bitwise(tmp_path, golden_dir, gpu):
     b = [l for l in open(tmp_path / "split.evol") if not l.startswith("#")]
     assert len(a) == len(b) == 13
     assert a == b
+
+
+SPIN_YAML = """
+outputs: {directory: out, final_time: 1e-12}
+mesh:
+  filename: wire.msh
+  volume_regions:
+    cu: {Ms: 0, sigma: 5.8e7, dens_state: 1e47, P: 0, l_sf: 300e-9}
+    py: {sigma: 5e6, dens_state: 1e47, P: 0.5, l_sd: 1e-9, l_sf: 5e-9}
+  surface_regions:
+    ground: {V: 0, s: [0, 0, 0]}
+    contact: {jn: 1e11, uP: [0, 2, 0]}
+spin_accumulation: {enable: true, V_file: true}
+"""
+
+
+def test_settings_spin_accumulation(tmp_path):
+    """spin_accumulation and the regions' spin parameters and boundary conditions are read
+    with the reference's keys (src/default-settings.yml)."""
+    p = tmp_path / "spin.yml"
+    p.write_text(SPIN_YAML)
+    s = fg.settings_dump(p)["spin_accumulation"]
+    assert s["enable"] and s["V_file"]
+    vol = {r["name"]: r for r in s["volume"]}
+    assert vol["cu"]["sigma"] == 5.8e7 and vol["cu"]["l_sf"] == 300e-9 and vol["py"]["l_sd"] == 1e-9
+    assert vol["py"]["P"] == 0.5 and vol["py"]["dens_state"] == 1e47
+    surf = {r["name"]: r for r in s["surface"]}
+    assert surf["ground"]["V"] == 0 and surf["ground"]["s"] == [0, 0, 0] and surf["ground"]["jn"] is None
+    assert surf["contact"]["jn"] == 1e11 and surf["contact"]["uP"] == [0, 1, 0] and surf["contact"]["V"] is None

@@ -241,3 +241,75 @@ def test_space_field(K):
     c.set_state(st["u"], st["v"], st["phi"], st["phiv"])
     c.step(DT, pref, H, angle)
     assert _rel(c.debug_system()[0], rhs_o) > 1e-3
+
+
+def _spin_case():
+    """Cuboid with the bottom face (V = 0, s = 0) and the top face (jn, uP) as the two
+    boundary surfaces of the electrostatic and spin-diffusion problems."""
+    m = cases.cuboid(6, 5, 4)
+    z = m["xyz"][:, 2]
+    reg = np.ones(len(m["tris"]), np.int32)
+    for f, t in enumerate(m["tris"]):
+        if np.all(np.abs(z[t] - z.min()) < 1e-15):
+            reg[f] = 2
+        if np.all(np.abs(z[t] - z.max()) < 1e-15):
+            reg[f] = 3
+    m["tri_reg"] = reg
+    sp = dict(sigma=5e6, P=0.5, lsd=1e-9, lsf=5e-9)
+    regs_o = [fgo.make_region(N0=1e47, **sp), fgo.make_region(A=cases.AE, Ms=cases.MS, alpha=0.5, N0=1e47, **sp)]
+    regs_g = [dict(Ae=1e-11, Ms=795774.7, alpha=0.5, dens_state=1e47, **sp),
+              dict(Ae=cases.AE, Ms=cases.MS, alpha=0.5, dens_state=1e47, **sp)]
+    bc = [dict(), dict(), dict(V=0.0, s=(0, 0, 0)), dict(jn=1e6, uP=(0, 1, 0))]
+    tregs_o = [fgo.make_tri_region(**b) for b in bc]
+    return m, regs_o, regs_g, tregs_o, bc
+
+
+def test_spin_accumulation():
+    """Spin accumulation coupling (spinAcc, electrostatSolver): the potential V (CG, once),
+    the spin accumulation s (BiCGSTAB with Dirichlet values, every compute_all, operator with
+    the CURRENT and RHS with the NEXT magnetisation) and its field Hst in the next step's
+    element integrals, against the oracle's explicit assembly: V within 1e-10, s within
+    1e-8 (both solved to 1e-12), the step's RHS within 1e-9 and v within 1e-8."""
+    m, regs_o, regs_g, tregs_o, bc = _spin_case()
+    u = cases.perturbed_state(m["xyz"], seed=41)
+    v = cases.tangent_field(u, seed=42)
+    H = np.array([2e4, -1e4, 3e4])
+    o = fgo.Oracle(m, regs_o, tregs_o)
+    assert o.set_spin(True, 1e-12, 5000)[0] == 0
+    o.set_solver(1e-12, 5000)
+    o.set_state(u, v)
+    o.compute_all(H)
+    st = o.get_state(0)
+    Vo, so, sst, _ = o.spin()
+    assert sst == 0 and np.abs(so).max() > 0
+    c = fg.Context(m, regs_g, bc, tol=1e-12, max_iter=5000, spin_acc=1, spin_tol=1e-12, spin_max_iter=5000)
+    c.set_state(st["u"], st["v"], st["phi"], st["phiv"])
+    c.compute_all(H)
+    info = c.spin_info()
+    assert info["status"] == fg.FG_OK
+    assert _rel(info["V"], Vo) <= 1e-10
+    assert _rel(c.get_spin(), so) <= 1e-8
+    angle, pref = 0.5, fgo.prefactor(DT, DTMAX)
+    o.base_projection(angle)
+    ro = o.step(DT, pref, H)
+    rhs_o = o.export_system()[3]
+    rg = c.step(DT, pref, H, angle)
+    assert not ro["fail"] and rg["status"] == fg.FG_OK
+    assert _rel(c.debug_system()[0], rhs_o) <= 1e-9
+    assert _rel(c.get_state(1)["v"], o.get_state(1)["v"]) <= 1e-8
+    # Hst is a visible part of the RHS
+    o2 = fgo.Oracle(m, regs_o, tregs_o)
+    o2.set_solver(1e-12, 5000)
+    o2.set_state(st["u"], st["v"], st["phi"], st["phiv"])
+    o2.base_projection(angle)
+    o2.step(DT, pref, H)
+    assert _rel(o2.export_system()[3], rhs_o) > 1e-2
+
+
+def test_spin_boundary_conditions_checked():
+    """A spin-accumulation context without exactly one jn surface, one V surface and one s
+    surface is refused (the reference's checkBoundaryConditions exit)."""
+    m, regs_o, regs_g, tregs_o, bc = _spin_case()
+    bad = [dict(), dict(), dict(V=0.0), dict(jn=1e6)]
+    with pytest.raises(fg.FgError):
+        fg.Context(m, regs_g, bad, spin_acc=1)
