@@ -17,6 +17,7 @@ afterwards. Synthetic data; no files are read.
   python bench.py --workload batch64     # 64 independent cubes, batched (its own line)
   python bench.py --workload wire        # nanowire domain wall, learned guess (its own line)
   python bench.py --workload platelet    # 3.84M-tet vortex platelet, learned guess at scale
+  python bench.py --workload spin        # the film with the spin-accumulation coupling
 
 One JSON line on stdout (rank 0). For N > 1 every rank runs an independent replica on its
 own GPU (the path does not shard); value is the sum over ranks of steps/s (max-over-ranks
@@ -262,7 +263,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="film", choices=["film", "batch64", "wire", "platelet"])
+    ap.add_argument("--workload", default="film", choices=["film", "batch64", "wire", "platelet", "spin"])
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--train-steps", type=int, default=None,
                     help="untimed solves that train the learned guess (default 40; 0 with --quick)")
@@ -293,6 +294,9 @@ def main():
         return
     if args.workload in ("wire", "platelet"):
         bench_learned_workload(args)
+        return
+    if args.workload == "spin":
+        bench_spin(args)
         return
     if args.drift > 0:
         drift_study(args)
@@ -602,6 +606,75 @@ def bench_learned_workload(args):
                 "stage_ms": dict(zip(["p2m", "m2m", "m2l", "l2l", "l2p_p2p"], [float(x) for x in fmm_stage]))},
         "clocks": clocks,
     }
+    print(json.dumps(line), flush=True)
+
+
+def bench_spin(args):
+    """The film with the spin-accumulation coupling: current injected through the x = 400 nm
+    face (jn = 1e5 A/m^2, polarisation along y: Hst of the order of Ms, so that the fixed
+    dt = 5e-14 s stays stable), the x = 0 face grounded (V = 0, s = 0);
+    permalloy-like transport parameters (sigma 5e6 S/m, N0 1e47, P 0.5, l_sd 1 nm, l_sf 5 nm).
+    FP32 body + FP64 refinement with the previous-step guess, with and without the coupling,
+    same state and angles; the spin solve (FP64 BiCGSTAB over 3 x 242k unknowns) runs in
+    every compute_all."""
+    import __graft_entry__
+    __graft_entry__.build_product()
+    import feellgood_gb300 as fg
+    mesh = film_mesh()
+    x = mesh["xyz"][:, 0]
+    reg = np.ones(len(mesh["tris"]), np.int32)
+    tx = x[mesh["tris"]]
+    reg[np.all(np.abs(tx - x.min()) < 1e-15, axis=1)] = 2
+    reg[np.all(np.abs(tx - x.max()) < 1e-15, axis=1)] = 3
+    mesh = dict(mesh, tri_reg=reg)
+    sp = dict(sigma=5e6, dens_state=1e47, P=0.5, lsd=1e-9, lsf=5e-9)
+    regs = [dict(Ae=1e-11, Ms=795774.7, alpha=0.5, **sp), dict(Ae=AE, Ms=MS, alpha=ALPHA, **sp)]
+    bc = [dict(), dict(), dict(V=0.0, s=(0, 0, 0)), dict(jn=1e5, uP=(0, 1, 0))]
+    u0 = initial_state(mesh)
+    H = np.zeros(3)
+    fg.rng_seed(SEED)
+    angles = [fg.rng_angle() for _ in range(args.warmup + args.steps)]
+    out = {}
+    for name, spin in (("spin", 1), ("no_spin", 0)):
+        c = fg.Context(mesh, regs, bc, tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP32_REFINE,
+                       demag=fg.FG_DEMAG_FMM, spin_acc=spin)
+        c.set_state(u0)
+        c.compute_all(H)
+        run_steps(c, args.warmup, H, DT, angles[:args.warmup])
+        clk = ClockSampler(0)
+        clk.start()
+        if spin:  # the spin solve's own device time and iterations, step by step
+            ms_l, reps = [], []
+            spin_ms, spin_it = [], []
+            for k in range(args.steps):
+                m1, r1 = run_steps(c, 1, H, DT, angles[args.warmup + k:args.warmup + k + 1])
+                ms_l.append(m1[0])
+                reps += r1
+                inf = c.spin_info()
+                spin_ms.append(inf["ms"])
+                spin_it.append(inf["iters"])
+            ms = np.array(ms_l)
+        else:
+            ms, reps = run_steps(c, args.steps, H, DT, angles[args.warmup:])
+        clocks = clk.stop()
+        info = c.spin_info() if spin else {}
+        out[name] = {"steps_per_s": args.steps / (ms[:, 4].sum() / 1e3), "ms_per_step": float(ms[:, 4].mean()),
+                     "phase_ms": dict(zip(["elements", "solve", "demag_x2_and_spin", "energy_evolution", "step"],
+                                          [float(v) for v in ms.mean(axis=0)])),
+                     "iters_per_step": float(np.mean([r["iters"] for r in reps])), "clocks": clocks}
+        if spin:
+            out[name]["spin_solve"] = {"status": info["status"], "iters_per_solve": float(np.mean(spin_it)),
+                                       "ms_per_solve": float(np.mean(spin_ms)),
+                                       "us_per_iteration": 1e3 * float(np.sum(spin_ms)) / max(1, int(np.sum(spin_it))),
+                                       "potential_cg_iters": info["V_iters"]}
+            out[name]["max_abs_s"] = float(np.abs(c.get_spin()).max())
+        c.close()
+    line = {"metric": "LLG steps/s, film 1.2M tets with spin accumulation (FP32 body + FP64 refinement)",
+            "value": out["spin"]["steps_per_s"], "unit": "steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": out["spin"]["ms_per_step"], "higher_is_better": True,
+            "dtype": "f32+f64", "data": "synthetic (seeded smoothed random film state)",
+            "config": {"workload": " ".join(bench_spin.__doc__.split())}, "detail": out,
+            "spin_cost_ms_per_step": out["spin"]["ms_per_step"] - out["no_spin"]["ms_per_step"]}
     print(json.dumps(line), flush=True)
 
 

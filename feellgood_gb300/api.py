@@ -120,7 +120,8 @@ SIGNATURES = {
     "fg_solver_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "fg_debug_wait_timeout": (C.c_int, [C.c_void_p, C.c_int]),
     "fg_gauss_points": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
-    "fg_spin_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.POINTER(C.c_int)]),
+    "fg_spin_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.POINTER(C.c_int),
+                               C.POINTER(C.c_double)]),
     "fg_get_spin": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fg_set_space_field": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fg_set_field_amplitude": (C.c_int, [C.c_void_p, C.c_double]),
@@ -430,10 +431,10 @@ class Context:
 
     def spin_info(self):
         """fg_spin_info: last spin solve (status, iterations), the potential V and its CG iterations."""
-        st, it, vit = C.c_int(), C.c_int(), C.c_int()
+        st, it, vit, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
         V = np.zeros(self.nn)
-        self._check(self.L.fg_spin_info(self.h, C.byref(st), C.byref(it), _ptr(V), C.byref(vit)))
-        return {"status": st.value, "iters": it.value, "V": V, "V_iters": vit.value}
+        self._check(self.L.fg_spin_info(self.h, C.byref(st), C.byref(it), _ptr(V), C.byref(vit), C.byref(ms)))
+        return {"status": st.value, "iters": it.value, "V": V, "V_iters": vit.value, "ms": ms.value}
 
     def get_spin(self):
         """fg_get_spin: the spin accumulation s, (n_nodes, 3)."""

@@ -802,7 +802,10 @@ int fg_compute_all(fg_ctx *h, const double Hext[3], double energies[4]) {
     int s = c.opts.first_order ? demag_into(h, c.u[1], c.phi[1]) : demag_pair(h);
     if (s) return s;
     if (c.spin) {  // spinAcc::compute after the demag (src/fem.h:203-224)
+        CK(cudaEventRecord(c.ev[6], c.stream));
         CK(launch_spin(c));
+        CK(cudaEventRecord(c.ev[7], c.stream));
+        c.spin_timed = true;
         c.launches += 1;
     }
     CK(cudaEventRecord(c.ev[4], c.stream));
@@ -951,8 +954,14 @@ int fg_debug_wait_timeout(fg_ctx *h, int which) {
     return FG_OK;
 }
 
-int fg_spin_info(const fg_ctx *h, int *status, int *iters, double *V, int *v_iters) {
+int fg_spin_info(const fg_ctx *h, int *status, int *iters, double *V, int *v_iters, double *ms) {
     if (!h || !h->c.spin) return FG_EINVAL;
+    if (ms) {
+        float f = 0.f;
+        if (h->c.spin_timed && cudaEventSynchronize(h->c.ev[7]) == cudaSuccess)
+            cudaEventElapsedTime(&f, h->c.ev[6], h->c.ev[7]);
+        *ms = f;
+    }
     return spin_info(h->c, status, iters, V, v_iters);
 }
 

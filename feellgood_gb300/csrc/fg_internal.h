@@ -213,6 +213,7 @@ struct Ctx {
     // spin accumulation (fg_spin.cu): solver state and the last solution s [3 nn]
     void *spin = nullptr;
     double *spin_s = nullptr;
+    bool spin_timed = false;  // ev[6] / ev[7] bracket the last spin solve
     double *pot = nullptr;       // nn
     double *pot2 = nullptr;      // nn, potential of src_q2
     double *epart = nullptr;     // energy partials

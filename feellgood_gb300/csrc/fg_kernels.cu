@@ -227,7 +227,8 @@ __global__ void __launch_bounds__(128) k_tet64_iso(int nmt, const int4 *__restri
                                                    double dt, double Hx, double Hy, double Hz,
                                                    double4 *__restrict__ slot, const int *__restrict__ tet_seg,
                                                    const SegPar *__restrict__ seg, const double *__restrict__ hsp,
-                                                   double amp) {
+                                                   double amp, const double *__restrict__ s_node,
+                                                   const double *__restrict__ v0) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nmt) return;
     if (seg) {
@@ -284,15 +285,46 @@ __global__ void __launch_bounds__(128) k_tet64_iso(int nmt, const int4 *__restri
     // space-dependent applied field (R4toR3): amp F(g) adds U(g) . amp F(g) to uHeff(g) and
     // sum_g w_g a_i(g) amp F(g) to BE_i
     double fw[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    // spin accumulation (src/tetra.cpp:248-303): Hst(g) = hst sum_i a_i(g) s_i adds U(g).Hst(g)
+    // to uHeff(g) and sum_g w_g a_i(g) (Hst(g) - (Hst(g).U(g)) s_dt V(g)) to BE_i
+    const bool spin = s_node && R.hst != 0.0;
+    double sw[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double sn[4][3], vn[4][3];
+    if (spin) {
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                sn[i][c] = R.hst * s_node[3 * (size_t)ind[i] + c];
+                vn[i][c] = v0[3 * (size_t)ind[i] + c];
+            }
+    }
+    const double sdt = FG_THETA * dt * FG_GAMMA0;
 #pragma unroll
     for (int g = 0; g < NPI; g++) {
         double h = hx + c_ta[0][g] * uh[0] + c_ta[1][g] * uh[1] + c_ta[2][g] * uh[2] + c_ta[3][g] * uh[3];
-        if (hsp) {
-            const double *F = hsp + 3 * ((size_t)t * NPI + g);
-            double U[3];
+        double U[3] = {0, 0, 0};
+        if (hsp || spin) {
 #pragma unroll
             for (int c = 0; c < 3; c++)
                 U[c] = c_ta[0][g] * un[0][c] + c_ta[1][g] * un[1][c] + c_ta[2][g] * un[2][c] + c_ta[3][g] * un[3][c];
+        }
+        if (spin) {
+            double Hs[3], Vg[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                Hs[c] = sn[0][c] * c_ta[0][g] + sn[1][c] * c_ta[1][g] + sn[2][c] * c_ta[2][g] + sn[3][c] * c_ta[3][g];
+                Vg[c] = c_ta[0][g] * vn[0][c] + c_ta[1][g] * vn[1][c] + c_ta[2][g] * vn[2][c] + c_ta[3][g] * vn[3][c];
+            }
+            const double hu = Hs[0] * U[0] + Hs[1] * U[1] + Hs[2] * U[2];
+            h += U[0] * Hs[0] + U[1] * Hs[1] + U[2] * Hs[2];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) sw[i][c] += c_cw[i][g] * (Hs[c] - hu * sdt * Vg[c]);
+        }
+        if (hsp) {
+            const double *F = hsp + 3 * ((size_t)t * NPI + g);
             h += amp * (U[0] * F[0] + U[1] * F[1] + U[2] * F[2]);
 #pragma unroll
             for (int i = 0; i < 4; i++)
@@ -314,6 +346,7 @@ __global__ void __launch_bounds__(128) k_tet64_iso(int nmt, const int4 *__restri
             const double ex = d[i][0] * dU[0][c] + d[i][1] * dU[1][c] + d[i][2] * dU[2][c];
             BE[c] = nva * ex + aw * H[c];
             if (hsp) BE[c] += (amp * J) * fw[i][c];
+            if (spin) BE[c] += J * sw[i][c];
         }
         slot[4 * (size_t)t + i] = make_double4(J * contrib[i], BE[0], BE[1], BE[2]);
     }
@@ -1030,17 +1063,17 @@ cudaError_t launch_tet(Ctx &c, double dt, const double H[3]) {
     }
     if (c.nmt == 0) return cudaGetLastError();
     const int b = 128;
-    if (!c.aniso && !c.spin_s) {
+    if (!c.aniso) {
         if (c.npi_t == 5)
             k_tet64_iso<5><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0],
                                                                    c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
                                                                    c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp,
-                                                                   c.field_amp);
+                                                                   c.field_amp, c.spin_s, c.v[0]);
         else
             k_tet64_iso<1><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0],
                                                                    c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
                                                                    c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp,
-                                                                   c.field_amp);
+                                                                   c.field_amp, c.spin_s, c.v[0]);
         return cudaGetLastError();
     }
     if (c.npi_t == 5)

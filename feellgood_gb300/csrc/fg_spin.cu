@@ -71,6 +71,9 @@ __device__ __forceinline__ void spin_apply(const SpinArgs &a, const double *__re
     y[2] = d ? 0.0 : s2;
 }
 
+// bicg_dir with Dirichlet values (src/algebra/bicg.h:82-153), every dot product formed as in
+// the reference (five grid barriers per iteration: forming rho and |r| from the iteration's
+// other sums instead stalled at tight tolerances).
 __global__ void __launch_bounds__(256) k_spin_bicg(SpinArgs a) {
     const int G = gridDim.x, nn = a.nn;
     const int stride = G * blockDim.x, i0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -124,13 +127,18 @@ __global__ void __launch_bounds__(256) k_spin_bicg(SpinArgs a) {
                 }
                 beta = (rho1 / rho2) * (alpha / omega);
             }
-            for (int k = i0; k < 3 * nn; k += stride) {
-                double pv = a.p[k];
-                if (nit > 0) {
-                    pv = (pv - omega * a.v[k]) * beta + a.r[k];
-                    a.p[k] = pv;
+            for (int i = i0; i < nn; i += stride) {
+                const double di = a.dinv[i];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const int k = 3 * i + c;
+                    double pv = a.p[k];
+                    if (nit > 0) {
+                        pv = (pv - omega * a.v[k]) * beta + a.r[k];
+                        a.p[k] = pv;
+                    }
+                    a.phat[k] = di * pv;
                 }
-                a.phat[k] = a.dinv[k / 3] * pv;
             }
             if (!grid_sync(a.bar)) goto timeout;
             {
@@ -155,11 +163,16 @@ __global__ void __launch_bounds__(256) k_spin_bicg(SpinArgs a) {
             }
             {
                 double ss = 0.0;
-                for (int k = i0; k < 3 * nn; k += stride) {
-                    const double sv = a.r[k] + (-alpha) * a.v[k];
-                    a.s[k] = sv;
-                    a.shat[k] = a.dinv[k / 3] * sv;
-                    ss += sv * sv;
+                for (int i = i0; i < nn; i += stride) {
+                    const double di = a.dinv[i];
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const int k = 3 * i + c;
+                        const double sv = a.r[k] + (-alpha) * a.v[k];
+                        a.s[k] = sv;
+                        a.shat[k] = di * sv;
+                        ss += sv * sv;
+                    }
                 }
                 double v1[1] = {ss};
                 block_store<1>(v1, a.partial, G);
@@ -169,7 +182,9 @@ __global__ void __launch_bounds__(256) k_spin_bicg(SpinArgs a) {
                 double s1c[1];
                 grid_sum<1>(a.partial, G, s1c);
                 if (finished(sqrt(fabs(s1c[0])))) {
-                    for (int k = i0; k < 3 * nn; k += stride) a.x[k] += alpha * a.phat[k];
+                    for (int i = i0; i < nn; i += stride)
+#pragma unroll
+                        for (int c = 0; c < 3; c++) a.x[3 * i + c] += alpha * a.phat[3 * i + c];
                     break;
                 } else if (status == 1 || status == 2) {
                     break;
@@ -198,15 +213,18 @@ __global__ void __launch_bounds__(256) k_spin_bicg(SpinArgs a) {
             }
             {
                 double r2 = 0.0, rtr2 = 0.0;
-                for (int k = i0; k < 3 * nn; k += stride) {
-                    double xv = a.x[k] + alpha * a.phat[k];
-                    xv += omega * a.shat[k];
-                    a.x[k] = xv;
-                    const double rv = a.s[k] - omega * a.t[k];
-                    a.r[k] = rv;
-                    r2 += rv * rv;
-                    rtr2 += a.rt[k] * rv;
-                }
+                for (int i = i0; i < nn; i += stride)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const int k = 3 * i + c;
+                        double xv = a.x[k] + alpha * a.phat[k];
+                        xv += omega * a.shat[k];
+                        a.x[k] = xv;
+                        const double rv = a.s[k] - omega * a.t[k];
+                        a.r[k] = rv;
+                        r2 += rv * rv;
+                        rtr2 += a.rt[k] * rv;
+                    }
                 double v2[2] = {r2, rtr2};
                 block_store<2>(v2, a.partial, G);
             }
@@ -576,8 +594,9 @@ int spin_setup(Ctx &c, const fg_mesh *m, const fg_region *regs, int nreg, const 
     }
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spin_bicg, 256, 0);
-    S->grid = std::max(1, std::min(std::max(1, per_sm) * c.nsm, (nn + 255) / 256));
-    if (cudaMalloc(&S->partial, 2 * sizeof(double) * std::max(1024, S->grid)) != cudaSuccess) return FG_ECUDA;
+    // two blocks per SM: fewer blocks make each of the solve's grid barriers cheaper
+    S->grid = std::max(1, std::min(std::min(std::max(1, per_sm), 2) * c.nsm, (nn + 255) / 256));
+    if (cudaMalloc(&S->partial, 3 * sizeof(double) * std::max(1024, S->grid)) != cudaSuccess) return FG_ECUDA;
     c.spin_s = S->out;
     return FG_OK;
 }

@@ -270,7 +270,8 @@ int run_impl(Run &R, const char *settings_path, unsigned int seed, int verbose, 
     const int nn = R.md->n_nodes;
     if (S.spin_acc && S.V_file) {  // electrostatSolver::save (src/electrostatSolver.cpp:133-152)
         std::vector<double> V(nn);
-        if (fg_spin_info(R.ctx, nullptr, nullptr, V.data(), nullptr) != FG_OK) return fail(FG_EINVAL, "no potential");
+        if (fg_spin_info(R.ctx, nullptr, nullptr, V.data(), nullptr, nullptr) != FG_OK)
+            return fail(FG_EINVAL, "no potential");
         const std::string vf = S.out_dir + "/" + S.sim_name + "_V.sol";
         std::FILE *f = std::fopen(vf.c_str(), "w");
         if (!f) return fail(FG_EIO, "cannot open file " + vf);

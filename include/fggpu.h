@@ -185,10 +185,10 @@ int fg_energy_noalloc(fg_ctx *ctx, const double Hext[3], double energies[4]);
 int fg_gauss_points(const fg_ctx *ctx, int *n_points, double *pts);
 
 /* Spin accumulation (fg_opts.spin_acc): the last spin solve's status (FG_OK when converged;
- * on failure s is zero, as spinAcc::compute leaves it) and iterations, the electrostatic
- * potential V[n_nodes] (host copy, may be NULL) and its CG iterations; fg_get_spin copies s
- * [n_nodes][3] (the field of the next step's Hst). */
-int fg_spin_info(const fg_ctx *ctx, int *status, int *iters, double *V, int *v_iters);
+ * on failure s is zero, as spinAcc::compute leaves it), iterations and device time in ms,
+ * the electrostatic potential V[n_nodes] (host copy) and its CG iterations (any pointer may
+ * be NULL); fg_get_spin copies s [n_nodes][3] (the field of the next step's Hst). */
+int fg_spin_info(const fg_ctx *ctx, int *status, int *iters, double *V, int *v_iters, double *ms);
 int fg_get_spin(const fg_ctx *ctx, double *s);
 int fg_set_space_field(fg_ctx *ctx, const double *field);
 int fg_set_field_amplitude(fg_ctx *ctx, double amplitude);
