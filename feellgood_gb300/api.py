@@ -123,6 +123,7 @@ SIGNATURES = {
     "fg_spin_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.POINTER(C.c_int),
                                C.POINTER(C.c_double)]),
     "fg_get_spin": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fg_recenter": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_int)]),
     "fg_set_space_field": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fg_set_field_amplitude": (C.c_int, [C.c_void_p, C.c_double]),
     "fg_checkpoint_peek": (C.c_int, [C.c_char_p, C.c_void_p, C.c_void_p]),
@@ -435,6 +436,13 @@ class Context:
         V = np.zeros(self.nn)
         self._check(self.L.fg_spin_info(self.h, C.byref(st), C.byref(it), _ptr(V), C.byref(vit), C.byref(ms)))
         return {"status": st.value, "iters": it.value, "V": V, "V_iters": vit.value, "ms": ms.value}
+
+    def recenter(self, direction, threshold):
+        """fg_recenter: direction 0/1/2 (x/y/z) or 'X'/'Y'/'Z'; returns True when it translated."""
+        d = {"X": 0, "Y": 1, "Z": 2}.get(direction, direction)
+        sh = C.c_int()
+        self._check(self.L.fg_recenter(self.h, int(d), float(threshold), C.byref(sh)))
+        return bool(sh.value)
 
     def get_spin(self):
         """fg_get_spin: the spin accumulation s, (n_nodes, 3)."""

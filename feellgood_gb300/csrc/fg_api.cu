@@ -637,6 +637,7 @@ void fg_destroy(fg_ctx *h) {
     fmm_free(c);
     mlp_free(c);
     spin_free(c);
+    recenter_free(c);
     batch_free(c);
     if (c.heff) cudaFree(c.heff);
     if (c.hres) cudaFreeHost(c.hres);
@@ -952,6 +953,19 @@ int fg_debug_wait_timeout(fg_ctx *h, int which) {
         return FG_ETIMEDOUT;
     }
     return FG_OK;
+}
+
+int fg_recenter(fg_ctx *h, int direction, double threshold, int *shifted) {
+    if (!h || !shifted || direction < 0 || direction > 2) return FG_EINVAL;
+    Ctx &c = h->c;
+    if (c.batch) {
+        c.err = "fg_recenter: not available for batch contexts";
+        return FG_EINVAL;
+    }
+    double avg[3];
+    int s = fg_average(h, 0, avg);
+    if (s != FG_OK) return s;
+    return recenter_apply(c, direction, threshold, avg[direction], shifted);
 }
 
 int fg_spin_info(const fg_ctx *h, int *status, int *iters, double *V, int *v_iters, double *ms) {

@@ -214,6 +214,7 @@ struct Ctx {
     void *spin = nullptr;
     double *spin_s = nullptr;
     bool spin_timed = false;  // ev[6] / ev[7] bracket the last spin solve
+    void *recenter = nullptr;  // nearest-node grid for recentering (fg_recenter.cu), built on first use
     double *pot = nullptr;       // nn
     double *pot2 = nullptr;      // nn, potential of src_q2
     double *epart = nullptr;     // energy partials
@@ -332,6 +333,8 @@ int spin_setup(Ctx &c, const fg_mesh *m, const fg_region *regs, int nreg, const 
 void spin_free(Ctx &c);
 cudaError_t launch_spin(Ctx &c);
 int spin_info(const Ctx &c, int *status, int *iters, double *V, int *v_iters);
+int recenter_apply(Ctx &c, int dir, double threshold, double avg_dir, int *shifted);
+void recenter_free(Ctx &c);
 cudaError_t launch_select_params(Ctx &c);
 cudaError_t launch_advance(Ctx &c);
 cudaError_t launch_energy_seg(Ctx &c);

@@ -392,6 +392,15 @@ int run_impl(Run &R, const char *settings_path, unsigned int seed, int verbose, 
             }
             R.nsteps++;
             R.t = last ? target : R.t + R.dt;
+            if (S.recenter) {  // src/time_integration.cpp:241
+                int shifted = 0;
+                s = fg_recenter(R.ctx, S.recenter_dir, S.recenter_threshold, &shifted);
+                if (s != FG_OK) {
+                    status = s;
+                    g_run_error = std::string("Error No Domain Wall: ") + fg_last_error(R.ctx);
+                    break;
+                }
+            }
         }
         if (status != FG_OK) break;
         s = evol_row(R, fe, nt_output, H);
@@ -505,7 +514,8 @@ int fg_settings_dump(const char *settings_path, char *out, int len) {
             num(r.s[0]); j << ", "; num(r.s[1]); j << ", "; num(r.s[2]);
             j << "]}";
         }
-        j << "]}}";
+        j << "]}, \"recentering\": {\"enable\": " << (S.recenter ? "true" : "false") << ", \"direction\": "
+          << S.recenter_dir << ", \"threshold\": " << S.recenter_threshold << "}}";
         const std::string s = j.str();
         if ((int)s.size() + 1 > len) return FG_EINVAL;
         std::memcpy(out, s.c_str(), s.size() + 1);

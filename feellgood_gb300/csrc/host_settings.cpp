@@ -402,8 +402,15 @@ void apply_yaml(Settings &S, const std::shared_ptr<YNode> &y) {
     }
     if (auto d = y->get("initial_time"); !is_null(d)) S.initial_time = to_num(d, "initial_time");
     if (auto d = y->get("recentering"); !is_null(d)) {
-        if (auto e = d->get("enable"); !is_null(e) && to_bool(e, "recentering.enable"))
-            throw SettingsError("recentering is not supported by this build");
+        if (auto e = d->get("enable"); !is_null(e)) S.recenter = to_bool(e, "recentering.enable");
+        if (auto e = d->get("direction"); !is_null(e)) {
+            const std::string v = e->scalar;
+            if (v == "X" || v == "x") S.recenter_dir = 0;
+            else if (v == "Y" || v == "y") S.recenter_dir = 1;
+            else if (v == "Z" || v == "z") S.recenter_dir = 2;
+            else throw SettingsError("recentering.direction should be X, Y or Z");
+        }
+        if (auto e = d->get("threshold"); !is_null(e)) S.recenter_threshold = to_num(e, "recentering.threshold");
     }
     if (auto d = y->get("Bext"); !is_null(d)) {
         if (d->kind != YNode::SEQ) throw SettingsError("Bext should be a vector of numbers (expressions of t are not supported)");

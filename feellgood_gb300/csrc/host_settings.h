@@ -69,6 +69,9 @@ struct Settings {
     int gpu_precision = 0, gpu_demag = 0;
     bool gpu_learned = false, one_gauss_point = false;
     bool spin_acc = false, V_file = false;  // spin_accumulation.enable, .V_file
+    bool recenter = false;                  // recentering.enable
+    int recenter_dir = 2;                   // recentering.direction X/Y/Z -> 0/1/2
+    double recenter_threshold = 0.1;
     int checkpoint_every = 0;    // write <out_dir>/<sim_name>.ckpt after every n-th output row
     int solver_lpr = 0, solver_blocks = 0, fmm_depth = 0;  // fixed solver / FMM choices (0: timed)
     std::string resume_file;     // continue the run of this checkpoint

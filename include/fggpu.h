@@ -219,6 +219,16 @@ int fg_checkpoint_save(fg_ctx *ctx, const char *path, const fg_checkpoint_meta *
 int fg_checkpoint_peek(const char *path, fg_checkpoint_shape *shape, fg_checkpoint_meta *meta);
 int fg_checkpoint_load(fg_ctx *ctx, const char *path, fg_checkpoint_meta *meta);
 
+/* Recentering (Fem::recenter, src/recentering.cpp:47-131; call after fg_compute_all): when
+ * |<u_dir>| (NEXT, magnetic volume) reaches threshold, translates the magnetisation pattern by
+ * D = <u_dir> (l_dir / 2) u_dir(left end) along direction (0 x, 1 y, 2 z; l = the mesh's
+ * bounding box): CURRENT u of every node becomes NEXT u of the node nearest to its shifted
+ * position (clamped to the box as the reference does) and NEXT v becomes zero. *shifted tells
+ * whether it moved. FG_EINVAL when both ends have the same sign along the direction (the
+ * reference's "No Domain Wall" exit). The nearest node is exact, equal distances going to
+ * the lower node index (the reference's kd-tree may pick another of equally near nodes). */
+int fg_recenter(fg_ctx *ctx, int direction, double threshold, int *shifted);
+
 /* <u_d> (which 0) or <v_d> (which 1) of NEXT over the magnetic volume, src/mesh.cpp:89-106. */
 int fg_average(fg_ctx *ctx, int which, double avg[3]);
 

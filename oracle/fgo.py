@@ -71,6 +71,8 @@ def lib():
         L.fgo_max_threads.restype = C.c_int
         L.fgo_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_int]
         L.fgo_set_space_field.argtypes = [C.c_void_p, C.c_void_p, C.c_double]
+        L.fgo_recenter.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        L.fgo_recenter.restype = C.c_int
         L.fgo_set_spin.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int),
                                    C.POINTER(C.c_int)]
         L.fgo_get_spin.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -146,6 +148,10 @@ class Oracle:
 
     def set_solver(self, tol=1e-6, maxiter=700):
         self.L.fgo_set_solver(self.h, tol, maxiter)
+
+    def recenter(self, direction, threshold):
+        """Fem::recenter: 1 translated, 0 below the threshold, -1 no domain wall."""
+        return self.L.fgo_recenter(self.h, int(direction), float(threshold))
 
     def set_spin(self, enable=True, tol=1e-8, maxiter=1000):
         """Spin accumulation on: solves the electrostatic potential now; returns its (status, iters)."""

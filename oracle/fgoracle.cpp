@@ -1254,6 +1254,60 @@ double avg(const Oracle &o, int which, int d) {
     return sum / o.totalMagVol;
 }
 
+// Fem::recenter (src/recentering.cpp:47-131) with a brute-force nearest node (the
+// reference's ANN kd-tree; equal distances go to the lower node index). Returns 1 when the
+// pattern was translated, 0 when |<u_dir>| < threshold, -1 when there is no domain wall.
+int recenter(Oracle &o, int dir, double thres) {
+    thres = std::fabs(thres);
+    const double m_i = avg(o, 0, dir);
+    if (std::fabs(m_i) < thres) return 0;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (const Node &nd : o.node)
+        for (int a = 0; a < 3; a++) {
+            lo[a] = std::min(lo[a], comp(nd.p, a));
+            hi[a] = std::max(hi[a], comp(nd.p, a));
+        }
+    double c[3], l[3];
+    for (int a = 0; a < 3; a++) {
+        l[a] = hi[a] - lo[a];
+        c[a] = 0.5 * (hi[a] + lo[a]);
+    }
+    auto nearest = [&](const double q[3]) {
+        int best = -1;
+        double bd = 1e300;
+        for (int j = 0; j < o.nn; j++) {
+            const double dx = q[0] - o.node[j].p.x, dy = q[1] - o.node[j].p.y, dz = q[2] - o.node[j].p.z;
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 < bd) {
+                bd = d2;
+                best = j;
+            }
+        }
+        return best;
+    };
+    double qL[3] = {c[0], c[1], c[2]}, qR[3] = {c[0], c[1], c[2]};
+    qL[dir] -= 0.5 * l[dir];
+    qR[dir] += 0.5 * l[dir];
+    const double u2L = comp(o.node[nearest(qL)].u[NXT], dir), u2R = comp(o.node[nearest(qR)].u[NXT], dir);
+    if (u2L * u2R > 0) return -1;
+    const double D = m_i * 0.5 * l[dir] * u2L;
+    for (int i = 0; i < o.nn; i++) {
+        double p[3] = {o.node[i].p.x, o.node[i].p.y, o.node[i].p.z};
+        p[dir] += D;
+        if (p[dir] - c[dir] > +0.5 * l[dir]) {
+            for (int a = 0; a < 3; a++) p[a] = c[a];
+            p[dir] += 0.5 * l[dir];
+        }
+        if (p[dir] - c[dir] < -0.5 * l[dir]) {
+            for (int a = 0; a < 3; a++) p[a] = c[a];
+            p[dir] -= 0.5 * l[dir];
+        }
+        o.node[i].u[CUR] = o.node[nearest(p)].u[NXT];
+        o.node[i].v[NXT] = {0, 0, 0};
+    }
+    return 1;
+}
+
 // timing (src/time_integration.h:10-42)
 struct Timing {
     double tf, DTMIN, DTMAX, TAUR, t = 0, dt = 0, prefactor = 1;
@@ -1381,6 +1435,8 @@ int fgo_max_threads() {
     return 1;
 #endif
 }
+
+int fgo_recenter(void *h, int dir, double threshold) { return recenter(*static_cast<Oracle *>(h), dir, threshold); }
 
 // Spin accumulation on (the potential is solved here, once) or off; status and iterations of
 // the potential solve are returned.

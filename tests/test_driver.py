@@ -187,6 +187,7 @@ mesh:
     ground: {V: 0, s: [0, 0, 0]}
     contact: {jn: 1e11, uP: [0, 2, 0]}
 spin_accumulation: {enable: true, V_file: true}
+recentering: {enable: true, direction: Y, threshold: 0.2}
 """
 
 
@@ -203,3 +204,4 @@ def test_settings_spin_accumulation(tmp_path):
     surf = {r["name"]: r for r in s["surface"]}
     assert surf["ground"]["V"] == 0 and surf["ground"]["s"] == [0, 0, 0] and surf["ground"]["jn"] is None
     assert surf["contact"]["jn"] == 1e11 and surf["contact"]["uP"] == [0, 1, 0] and surf["contact"]["V"] is None
+    assert fg.settings_dump(p)["recentering"] == {"enable": True, "direction": 1, "threshold": 0.2}

@@ -313,3 +313,43 @@ def test_spin_boundary_conditions_checked():
     bad = [dict(), dict(), dict(V=0.0), dict(jn=1e6)]
     with pytest.raises(fg.FgError):
         fg.Context(m, regs_g, bad, spin_acc=1)
+
+
+def _wall(m, z0, width=5.0, seed=51):
+    z = m["xyz"][:, 2] / 1e-9
+    mz = np.tanh((z0 - z) / width)
+    u = np.stack([np.sqrt(np.clip(1 - mz * mz, 0, 1)), np.zeros_like(mz), mz], axis=1)
+    u[:, :2] += np.random.default_rng(seed).uniform(-0.02, 0.02, (len(z), 2))
+    return u / np.linalg.norm(u, axis=1, keepdims=True)
+
+
+@pytest.mark.parametrize("z0,expect", [(30.0, 1), (50.0, 0), (-1e3, -1)])
+def test_recentering(z0, expect):
+    """Fem::recenter (src/recentering.cpp:47-131): a head-to-head wall at z0 in a 10 x 10 x 100 nm
+    wire. Off centre the pattern is translated: CURRENT u of every node is NEXT u of the node
+    nearest to its shifted position (the oracle searches all nodes, the GPU a grid of cells;
+    both exact, so the result is bitwise equal) and NEXT v is zero; at the centre |<m_z>| is
+    below the threshold; without a wall (uniform m_z) both report the reference's error."""
+    m = cases.cuboid(4, 4, 40)
+    u = _wall(m, z0)
+    v = cases.tangent_field(u, seed=52)
+    H = np.zeros(3)
+    o = fgo.Oracle(m, cases.oracle_regions(alpha=0.5))
+    o.set_state(u, v)
+    o.compute_all(H)
+    c = fg.Context(m, cases.regions(alpha=0.5))
+    c.set_state(u, v)
+    c.compute_all(H)
+    r = o.recenter(2, 0.1)
+    assert r == expect
+    if expect < 0:
+        with pytest.raises(fg.FgError):
+            c.recenter("Z", 0.1)
+        return
+    assert c.recenter("Z", 0.1) == bool(expect)
+    so, sg = o.get_state(0), c.get_state(0)
+    assert np.array_equal(sg["u"], so["u"])
+    if expect:
+        assert not np.array_equal(sg["u"], u)
+        assert np.array_equal(c.get_state(1)["v"], np.zeros_like(v))
+        assert np.array_equal(o.get_state(1)["v"], np.zeros_like(v))
