@@ -575,6 +575,19 @@ def bench_learned_workload(args):
     fmm_stage = ctx.fmm_timings()
     cnt = ctx.counters()
     learned = ctx.get_state(0)
+    recenter_ms = None
+    if args.workload == "wire":
+        # Fem::recenter on the wire's state (threshold 0: it always translates), wall clock of
+        # the call (average, nearest-node search and copy, synchronised); on a copy of the state
+        rc = fg.Context(mesh, regs, tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP32_REFINE,
+                        demag=fg.FG_DEMAG_FMM)
+        rc.set_state(learned["u"], learned["v"], learned["phi"], learned["phiv"])
+        rc.recenter("Z", 0.0)  # first call builds the nearest-node grid
+        t0 = time.perf_counter()
+        for _ in range(5):
+            rc.recenter("Z", 0.0)
+        recenter_ms = (time.perf_counter() - t0) / 5 * 1e3
+        rc.close()
     ctx.close()
     out = {"learned": (args.steps / (ms[:, 4].sum() / 1e3), float(np.mean([r["iters"] for r in reps])))}
     acc = float(np.mean([r["guess_accepted"] for r in reps]))
@@ -606,6 +619,8 @@ def bench_learned_workload(args):
                 "stage_ms": dict(zip(["p2m", "m2m", "m2l", "l2l", "l2p_p2p"], [float(x) for x in fmm_stage]))},
         "clocks": clocks,
     }
+    if recenter_ms is not None:
+        line["recenter_ms_per_call"] = recenter_ms
     print(json.dumps(line), flush=True)
 
 
