@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <numeric>
@@ -204,6 +205,9 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
             if (g.K != 0.0 || g.K3 != 0.0) c.aniso = true;
             c.ms_ref = std::max(c.ms_ref == 1.0 ? 0.0 : c.ms_ref, g.Ms);
             d.Abis = 2.0 * g.Ae / (FG_MU0 * g.Ms);
+            const float ah = (float)d.Abis, lh = (float)g.alpha;
+            d.Abis_ds = make_float2(ah, (float)(d.Abis - (double)ah));
+            d.alpha_ds = make_float2(lh, (float)(g.alpha - (double)lh));
             d.Kbis = 2.0 * g.K / (FG_MU0 * g.Ms);
             d.K3bis = 2.0 * g.K3 / (FG_MU0 * g.Ms);
         }
@@ -421,6 +425,17 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     CK(upload(&c.tet, htet));
     CK(upload(&c.da, da));
     CK(upload(&c.detJ, detJ));
+    // double-single element integrals for the FP32 + refinement path without anisotropy
+    // (FG_DS_ELEMENTS=0 in the environment keeps the FP64 kernel, for comparisons)
+    {
+        const char *env = std::getenv("FG_DS_ELEMENTS");
+        c.elem_ds = c.opts.precision == FG_PREC_FP32_REFINE && !c.aniso && !c.opts.spin_acc &&
+                    !(env && env[0] == '0');
+    }
+    if (c.elem_ds) {
+        const int s = elem_ds_setup(c, da, detJ);
+        if (s != FG_OK) return s;
+    }
     CK(upload(&c.treg, htreg));
     if (c.opts.spin_acc) {  // before the region table goes to the device: it adds the Hst prefactors
         const int s = spin_setup(c, m, regs, nreg, tregs, ntreg, hreg);
@@ -631,7 +646,7 @@ void fg_destroy(fg_ctx *h) {
                     c.Sval32, c.A, c.A32, c.tri, c.tri_c, c.tinc_ptr, c.tinc, c.src_xyz, c.mag_nodes, c.u[0], c.u[1],
                     c.v[0], c.v[1], c.phi[0], c.phi[1], c.phiv[0], c.phiv[1], c.ep, c.eq, c.ep32, c.eq32, c.Dl32,
                     c.slot, c.Dl, c.rhs, c.x, c.bv, c.W, c.fv, c.partial, c.bar, c.dres, c.src_q, c.tri_slot,
-                    c.pot, c.epart, c.src_dst, c.src_q2, c.tri_slot2, c.pot2, c.tri_be, c.hsp};
+                    c.pot, c.epart, c.src_dst, c.src_q2, c.tri_slot2, c.pot2, c.tri_be, c.hsp, c.da_ds, c.J_ds, c.state_ds};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     fmm_free(c);

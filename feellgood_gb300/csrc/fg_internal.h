@@ -22,7 +22,12 @@ struct DevRegion {
     double A, Ms, alpha, Abis, K, Kbis, K3, K3bis;
     double uk[3], ex[3], ey[3], ez[3];
     double hst;  // spin accumulation: Hst = hst * s at the Gauss points (0 without the coupling)
+    float2 Abis_ds, alpha_ds;  // double-single copies for the double-single element kernel
 };
+
+// The double-single element slots are scaled by 2^DS_SLOT_SCALE (the Jacobian is scaled on
+// the host) so that their low words stay normal FP32 numbers.
+constexpr int DS_SLOT_SCALE = 70;
 
 // Gauss rules of the tets (5 points, or 1) and triangles (4 points, or 1): shape functions
 // a_i(g) and weights per unit Jacobian (src/tetra.h:27-81, src/triangle.h:43-66).
@@ -215,6 +220,10 @@ struct Ctx {
     double *spin_s = nullptr;
     bool spin_timed = false;  // ev[6] / ev[7] bracket the last spin solve
     void *recenter = nullptr;  // nearest-node grid for recentering (fg_recenter.cu), built on first use
+    // double-single element integrals (fg_elem_ds.cu): da [12][nmt], detJ * 2^DS_SLOT_SCALE,
+    // per-step double-single copies of u, phi, phiv of CURRENT
+    bool elem_ds = false;
+    float2 *da_ds = nullptr, *J_ds = nullptr, *state_ds = nullptr;
     double *pot = nullptr;       // nn
     double *pot2 = nullptr;      // nn, potential of src_q2
     double *epart = nullptr;     // energy partials
@@ -334,6 +343,10 @@ void spin_free(Ctx &c);
 cudaError_t launch_spin(Ctx &c);
 int spin_info(const Ctx &c, int *status, int *iters, double *V, int *v_iters);
 int recenter_apply(Ctx &c, int dir, double threshold, double avg_dir, int *shifted);
+int elem_ds_setup(Ctx &c, const std::vector<double> &da, const std::vector<double> &detJ);
+void upload_rules_ds(const double ta[4][5], const double tp[5]);
+cudaError_t launch_tet_ds(Ctx &c, double dt, const double H[3]);
+inline bool use_elem_ds(const Ctx &c) { return c.elem_ds && !c.hsp && !c.spin_s; }
 void recenter_free(Ctx &c);
 cudaError_t launch_select_params(Ctx &c);
 cudaError_t launch_advance(Ctx &c);

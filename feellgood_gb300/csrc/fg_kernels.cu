@@ -23,6 +23,7 @@
 
 #include "fg_internal.h"
 #include "fg_device.cuh"
+#include "fg_ds.cuh"
 
 namespace fg {
 
@@ -397,7 +398,7 @@ __global__ void k_tri_aniso(int nft, const int4 *__restrict__ tri, const DevTri 
 // (src/linear_algebra.cpp:13-24: previous v on the new basis / gamma0).
 
 __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
-                         const double4 *__restrict__ slot, const int *__restrict__ tinc_ptr,
+                         const double4 *__restrict__ slot, int slot_ds, const int *__restrict__ tinc_ptr,
                          const int *__restrict__ tinc, const double *__restrict__ tri_be,
                          const unsigned char *__restrict__ mag,
                          const double *__restrict__ A, const double *__restrict__ u0, const double *__restrict__ v1,
@@ -439,9 +440,25 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
     ep[3 * i] = e[0]; ep[3 * i + 1] = e[1]; ep[3 * i + 2] = e[2];
     eq[3 * i] = q[0]; eq[3 * i + 1] = q[1]; eq[3 * i + 2] = q[2];
     double dl = 0.0, be0 = 0.0, be1 = 0.0, be2 = 0.0;
-    for (int k = inc_ptr[i]; k < inc_ptr[i + 1]; k++) {
-        const double4 s = slot[inc[k]];
-        dl += s.x; be0 += s.y; be1 += s.z; be2 += s.w;
+    if (slot_ds) {  // double-single slots scaled by 2^DS_SLOT_SCALE: sum in double-single, convert once
+        const float4 *sf = reinterpret_cast<const float4 *>(slot);
+        dsf a0 = {0.f, 0.f}, a1 = a0, a2 = a0, a3 = a0;
+        for (int k = inc_ptr[i]; k < inc_ptr[i + 1]; k++) {
+            const float4 h = sf[2 * (size_t)inc[k]], l = sf[2 * (size_t)inc[k] + 1];
+            a0 = ds_add(a0, {h.x, l.x});
+            a1 = ds_add(a1, {h.y, l.y});
+            a2 = ds_add(a2, {h.z, l.z});
+            a3 = ds_add(a3, {h.w, l.w});
+        }
+        dl = std::ldexp(ds_to(a0), -DS_SLOT_SCALE);
+        be0 = std::ldexp(ds_to(a1), -DS_SLOT_SCALE);
+        be1 = std::ldexp(ds_to(a2), -DS_SLOT_SCALE);
+        be2 = std::ldexp(ds_to(a3), -DS_SLOT_SCALE);
+    } else {
+        for (int k = inc_ptr[i]; k < inc_ptr[i + 1]; k++) {
+            const double4 s = slot[inc[k]];
+            dl += s.x; be0 += s.y; be1 += s.z; be2 += s.w;
+        }
     }
     if (tri_be)  // surface anisotropy of the adjacent magnetic triangles (Tri::integrales)
         for (int k = tinc_ptr[i]; k < tinc_ptr[i + 1]; k++) {
@@ -1052,11 +1069,19 @@ void upload_rules(bool one_point) {
     cudaMemcpyToSymbol(c_cw, cw, sizeof(cw));
     cudaMemcpyToSymbol(c_cws, cws, sizeof(cws));
     cudaMemcpyToSymbol(c_tps, &tps, sizeof(tps));
+    upload_rules_ds(ta, tp);
     cudaMemcpyToSymbol(c_fa, fa, sizeof(fa));
     cudaMemcpyToSymbol(c_fpds, fp, sizeof(fp));
 }
 
 cudaError_t launch_tet(Ctx &c, double dt, const double H[3]) {
+    if (use_elem_ds(c)) {  // FP32 + refinement, isotropic, no space field / spin / batch
+        if (c.tri_be && c.nft > 0) {
+            if (c.npi_f == 4) k_tri_aniso<4><<<nblocks(c.nft, 128), 128, 0, c.stream>>>(c.nft, c.tri, c.tri_c, c.u[0], c.tri_be);
+            else k_tri_aniso<1><<<nblocks(c.nft, 128), 128, 0, c.stream>>>(c.nft, c.tri, c.tri_c, c.u[0], c.tri_be);
+        }
+        return launch_tet_ds(c, dt, H);
+    }
     if (c.tri_be && c.nft > 0) {  // surface anisotropy (only when some region has Ks != 0)
         if (c.npi_f == 4) k_tri_aniso<4><<<nblocks(c.nft, 128), 128, 0, c.stream>>>(c.nft, c.tri, c.tri_c, c.u[0], c.tri_be);
         else k_tri_aniso<1><<<nblocks(c.nft, 128), 128, 0, c.stream>>>(c.nft, c.tri, c.tri_c, c.u[0], c.tri_be);
@@ -1094,7 +1119,8 @@ cudaError_t launch_node(Ctx &c, double angle) {
     double *bv = c.bv;
     const long n2 = 2L * c.nn;
     double *Minv = bv + 8 * n2;
-    k_node64<<<nblocks(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.inc_ptr, c.inc, c.slot, c.tinc_ptr, c.tinc, c.tri_be,
+    k_node64<<<nblocks(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.inc_ptr, c.inc, c.slot, use_elem_ds(c) ? 1 : 0,
+                                                        c.tinc_ptr, c.tinc, c.tri_be,
                                                         c.mag, c.A, c.u[0], c.v[1],
                                                         cr, sr, c.ep, c.eq, c.Dl, c.rhs, c.x, Minv, c.W,
                                                         c.mlp ? c.heff : nullptr, c.node_seg,
