@@ -191,6 +191,11 @@ int elem_ds_setup(Ctx &c, const std::vector<double> &da, const std::vector<doubl
     return FG_OK;
 }
 
+void launch_state_ds(Ctx &c, const double *u, const double *phi, const double *phiv) {
+    float2 *uds = c.state_ds, *phids = uds + 3 * (size_t)c.nn, *phivds = phids + c.nn;
+    k_state_ds<<<(c.nn + 255) / 256, 256, 0, c.stream>>>(c.nn, u, phi, phiv, uds, phids, phivds);
+}
+
 cudaError_t launch_tet_ds(Ctx &c, double dt, const double H[3]) {
     if (c.nmt == 0) return cudaSuccess;
     float2 *uds = c.state_ds, *phids = uds + 3 * (size_t)c.nn, *phivds = phids + c.nn;

@@ -346,6 +346,7 @@ int recenter_apply(Ctx &c, int dir, double threshold, double avg_dir, int *shift
 int elem_ds_setup(Ctx &c, const std::vector<double> &da, const std::vector<double> &detJ);
 void upload_rules_ds(const double ta[4][5], const double tp[5]);
 cudaError_t launch_tet_ds(Ctx &c, double dt, const double H[3]);
+void launch_state_ds(Ctx &c, const double *u, const double *phi, const double *phiv);
 inline bool use_elem_ds(const Ctx &c) { return c.elem_ds && !c.hsp && !c.spin_s; }
 void recenter_free(Ctx &c);
 cudaError_t launch_select_params(Ctx &c);

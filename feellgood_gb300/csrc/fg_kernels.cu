@@ -860,8 +860,14 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
                                                 double Hx, double Hy, double Hz, double *__restrict__ partial,
                                                 const int4 *__restrict__ blk_rng, const int *__restrict__ blk_seg,
                                                 const double *__restrict__ segH, const double *__restrict__ hsp,
-                                                double amp) {
+                                                double amp, const float2 *__restrict__ da_ds,
+                                                const float2 *__restrict__ J_ds, const float2 *__restrict__ st_ds,
+                                                int nn_ds) {
     double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    // isotropic form in double-single (FP32 + refinement path): state of NEXT and geometry as
+    // double-single pairs, the Jacobian scaled by 2^DS_SLOT_SCALE; per-thread double-single sums
+    dsf dacc[7] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    const bool dsp = ISO && da_ds;
     // default: grid-stride over all elements; batch: this block's ranges of one sample
     int stride = gridDim.x * blockDim.x, t0 = blockIdx.x * blockDim.x + threadIdx.x, t1 = nmt;
     int f0 = t0, f1 = nft;
@@ -872,6 +878,63 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
         f0 = r.z + threadIdx.x; f1 = r.w;
         const double *h = segH + 3 * blk_seg[blockIdx.x];
         Hx = h[0]; Hy = h[1]; Hz = h[2];
+    }
+    if (dsp) {
+        const float2 *uds = st_ds, *pds = st_ds + 3 * (size_t)nn_ds;
+        dsf cw[4], tp = ds_from(c_tps);
+#pragma unroll
+        for (int i = 0; i < 4; i++) cw[i] = ds_from(c_cws[i]);
+        const dsf Hd[3] = {ds_from(Hx), ds_from(Hy), ds_from(Hz)};
+        for (int k = t0; k < t1; k += stride) {
+            const int4 I = tet[k];
+            const int ind[4] = {I.x, I.y, I.z, I.w};
+            const DevRegion &R = regs[treg[k]];
+            dsf un[4][3], ph[4], d[4][3];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const float2 a = uds[3 * (size_t)ind[i] + c], b = da_ds[(3 * i + c) * (size_t)nmt + k];
+                    un[i][c] = {a.x, a.y};
+                    d[i][c] = {b.x, b.y};
+                }
+                const float2 p = pds[ind[i]];
+                ph[i] = {p.x, p.y};
+            }
+            dsf dU[3][3];
+#pragma unroll
+            for (int kk = 0; kk < 3; kk++)
+#pragma unroll
+                for (int c = 0; c < 3; c++)
+                    dU[kk][c] = ds_fma(d[3][kk], un[3][c],
+                                       ds_fma(d[2][kk], un[2][c], ds_fma(d[1][kk], un[1][c], ds_mul(d[0][kk], un[0][c]))));
+            dsf dens = {0.f, 0.f};
+#pragma unroll
+            for (int kk = 0; kk < 3; kk++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) dens = ds_fma(dU[kk][c], dU[kk][c], dens);
+            const dsf div = ds_add(ds_add(dU[0][0], dU[1][1]), dU[2][2]);
+            const float2 Jf = J_ds[k];
+            const dsf J = {Jf.x, Jf.y};
+            dsf su[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, sp = {0.f, 0.f};
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const dsf aw = ds_mul(J, cw[i]);
+#pragma unroll
+                for (int c = 0; c < 3; c++) su[c] = ds_fma(aw, un[i][c], su[c]);
+                sp = ds_fma(aw, ph[i], sp);
+            }
+            dacc[0] = ds_fma(ds_mul(ds_from(R.A), ds_mul(J, tp)), dens, dacc[0]);
+            dacc[2] = ds_fma(ds_mul(ds_from(-0.5 * FG_MU0 * R.Ms), div), sp, dacc[2]);
+            dacc[3] = ds_fma(ds_from(-FG_MU0 * R.Ms),
+                             ds_fma(su[2], Hd[2], ds_fma(su[1], Hd[1], ds_mul(su[0], Hd[0]))), dacc[3]);
+            dacc[4] = ds_add(dacc[4], su[0]);
+            dacc[5] = ds_add(dacc[5], su[1]);
+            dacc[6] = ds_add(dacc[6], su[2]);
+        }
+#pragma unroll
+        for (int q = 0; q < 7; q++) acc[q] += std::ldexp(ds_to(dacc[q]), -DS_SLOT_SCALE);
+        t1 = t0;  // the FP64 tet loop below has nothing left to do
     }
     for (int k = t0; k < t1; k += stride) {
         const int4 I = tet[k];
@@ -1224,14 +1287,18 @@ cudaError_t launch_energy(Ctx &c, const double H[3]) { return launch_energy_into
 // device buffer of at least 7 * c.epart_blocks doubles (used by fg_energy_noalloc).
 cudaError_t launch_energy_into(Ctx &c, const double H[3], double *partial) {
     const int G = c.epart_blocks;
+    // the double-single form of the FP32 + refinement path reads NEXT as double-single pairs
+    const bool dsp = energy_iso(c) && use_elem_ds(c);
+    if (dsp) launch_state_ds(c, c.u[1], c.phi[1], c.phiv[1]);
+    const float2 *dda = dsp ? c.da_ds : nullptr;
     if (c.npi_t == 5)
         (energy_iso(c) ? k_energy<5, 4, true> : k_energy<5, 4, false>)<<<G, 256, 0, c.stream>>>(
             c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c, c.u[1], c.phi[1], H[0], H[1], H[2],
-            partial, nullptr, nullptr, nullptr, c.hsp, c.field_amp);
+            partial, nullptr, nullptr, nullptr, c.hsp, c.field_amp, dda, c.J_ds, c.state_ds, c.nn);
     else
         (energy_iso(c) ? k_energy<1, 1, true> : k_energy<1, 1, false>)<<<G, 256, 0, c.stream>>>(
             c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c, c.u[1], c.phi[1], H[0], H[1], H[2],
-            partial, nullptr, nullptr, nullptr, c.hsp, c.field_amp);
+            partial, nullptr, nullptr, nullptr, c.hsp, c.field_amp, dda, c.J_ds, c.state_ds, c.nn);
     return cudaGetLastError();
 }
 
@@ -1243,12 +1310,12 @@ cudaError_t launch_energy_seg(Ctx &c) {
         (c.aniso ? k_energy<5, 4, false> : k_energy<5, 4, true>)<<<G, 256, 0, c.stream>>>(
             c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
                                                  c.u[1], c.phi[1], H0[0], H0[1], H0[2], c.seg_epart, c.eblk_rng,
-                                                 c.eblk_seg, c.seg_H, nullptr, 0.0);
+                                                 c.eblk_seg, c.seg_H, nullptr, 0.0, nullptr, nullptr, nullptr, 0);
     else
         (c.aniso ? k_energy<1, 1, false> : k_energy<1, 1, true>)<<<G, 256, 0, c.stream>>>(
             c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
                                                  c.u[1], c.phi[1], H0[0], H0[1], H0[2], c.seg_epart, c.eblk_rng,
-                                                 c.eblk_seg, c.seg_H, nullptr, 0.0);
+                                                 c.eblk_seg, c.seg_H, nullptr, 0.0, nullptr, nullptr, nullptr, 0);
     k_seg_energy_sum<<<c.nseg, 32, 0, c.stream>>>(G, c.d_seg_eblk, c.seg_epart, c.seg_energy);
     return cudaGetLastError();
 }

@@ -374,3 +374,9 @@ def test_double_single_elements(one_point):
     for _ in range(3):
         x = rng.normal(size=2 * len(m["xyz"]))
         assert _rel(c.debug_apply(x), _csr_apply(rowptr, col, val, x)) <= 1e-12
+    # energies of the new state: the isotropic energy kernel of this path is double-single too
+    c.set_state(o.get_state(1)["u"], o.get_state(1)["v"])
+    Eg = c.compute_all(H)
+    Eo = o.compute_all(H)
+    for k in range(4):
+        assert abs(Eg[k] - Eo[k]) <= 1e-10 * np.max(np.abs(Eo)), (k, Eg, Eo)
