@@ -409,8 +409,8 @@ def main():
         # index once and writes two potentials (36 B); M2L does both sets' products.
         "k_l2p_p2p (near field + L2P)": (fmm_stage[4], 1, {"bytes": 20.0 * nsrc + 36.0 * nn}),
         "k_m2l_tc (M2L, tcgen05 3xTF32)": (fmm_stage[2], 1, {"m2l_pairs": 2 * n_m2l}),
-        "k_tet64_iso + k_node64 (elements)": (ph[0], 1, {"bytes": 1200000 * (4 * 4 + 12 * 8 + 8 + 4 + 4 * 32) +
-                                                          nn * (3 * 8 + 2 * 8 + 8 * 8)}),
+        "k_tet_ds + k_node64 (elements)": (ph[0], 1, {"bytes": 1200000 * (4 * 4 + 12 * 8 + 8 + 4 + 4 * 40 + 4 * 32) +
+                                                       nn * (3 * 8 + 2 * 8 + 8 * 8)}),
     }
     dom = max(kernels, key=lambda k: kernels[k][0] * kernels[k][1])
     kernels[dom][2]["traffic"] = ncu_traffic(dom.split()[0])
