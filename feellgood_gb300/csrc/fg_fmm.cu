@@ -33,6 +33,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "fg_f32x2.cuh"
 #include "fg_internal.h"
 
 namespace fg {
@@ -487,38 +488,6 @@ __device__ __forceinline__ void l2p_p2p_pass(int leaf, int tb, int nt, int lane,
         sets.pot[0][node] = (double(fa) + nr[0]) * sc;
         if constexpr (NQ == 2) sets.pot[1][node] = (double(fb) + nr[NQ - 1]) * sc;
     }
-}
-
-// Packed FP32 pairs (Blackwell f32x2 instructions): two lanes of a 64-bit register hold
-// the same quantity for two targets, so one instruction serves two pairs.
-using u64 = unsigned long long;
-__device__ __forceinline__ u64 pk2(float lo, float hi) {
-    u64 d;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
-    return d;
-}
-__device__ __forceinline__ void upk2(u64 v, float &lo, float &hi) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ u64 sub2(u64 a, u64 b) {
-    u64 d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ u64 add2(u64 a, u64 b) {
-    u64 d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ u64 mul2(u64 a, u64 b) {
-    u64 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ u64 fma2(u64 a, u64 b, u64 c) {
-    u64 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
 }
 
 // The FP32 pass of l2p_p2p_pass with the pair arithmetic on packed target pairs: per two
