@@ -71,6 +71,45 @@ __device__ __forceinline__ void block_store(double (&val)[NV], double *partial, 
     __syncthreads();
 }
 
+// The same from FP32 per-thread sums: the warp stage adds in FP32, the block and grid
+// stages in FP64. GB300's FP64 pipe runs at 1/64 of the FP32 rate, so converting and
+// accumulating every element in FP64 would bound an FP32 Krylov body on that pipe.
+template <int NV>
+__device__ __forceinline__ void block_store_f(float (&val)[NV], double *partial, int G) {
+    __shared__ double shf[NV][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++)
+        for (int o = 16; o > 0; o >>= 1) val[k] += __shfl_down_sync(0xffffffffu, val[k], o);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) shf[k][warp] = (double)val[k];
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double x = lane < nw ? shf[k][lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) partial[k * G + blockIdx.x] = x;
+        }
+    }
+    __syncthreads();
+}
+
+// Scalar FP64 work (divisions, square roots of the Krylov recurrences) evaluated once per
+// block by thread 0 and handed to every thread, instead of 256 copies on the 1/64-rate FP64
+// pipe. Every thread of the block must make the call.
+template <typename F>
+__device__ __forceinline__ double block_once(F f) {
+    __shared__ double v;
+    if (threadIdx.x == 0) v = f();
+    __syncthreads();
+    const double r = v;
+    __syncthreads();
+    return r;
+}
+
 // Every block sums the G partials of each of the NV slots in the same fixed order.
 template <int NV>
 __device__ __forceinline__ void grid_sum(const double *partial, int G, double (&out)[NV]) {

@@ -5,8 +5,11 @@
 //                       the reference's own test (src/algebra/iter.h:144-156) applied to
 //                       the true residual;
 //   inner loop (FP32):  BiCGSTAB on (scale K) d = r/|r| from d = 0 with FP32 vectors and
-//                       operator and FP64 dot-product accumulation; scale = 1/mean(A)
-//                       keeps every FP32 quantity O(1) (raw entries are ~1e-27);
+//                       operator; dot products summed in FP32 per warp and in FP64 across
+//                       warps and blocks, the recurrence scalars (alpha, beta, omega) in
+//                       FP64 once per block (GB300's FP64 pipe runs at 1/64 of the FP32
+//                       rate); scale = 1/mean(A) keeps every FP32 quantity O(1) (raw
+//                       entries are ~1e-27);
 //   x += scale |r| d in FP64.
 // One cooperative launch per solve; the node update (Node::make_evol) is fused at the end.
 #include <algorithm>
@@ -60,7 +63,7 @@ __device__ __forceinline__ SegView seg_view(const MixedArgs &a) {
     }
 
 template <int LPR>
-__global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
+__global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
     const int G = gridDim.x;
     const SegView sv = seg_view(a);
     const int rstride = (sv.b1 - sv.b0) * blockDim.x;
@@ -124,7 +127,7 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
             {
                 double s2[1];
                 range_sum<1>(a.partial, G, sv.b0, sv.b1, s2);
-                if (!done) res = sqrt(fabs(s2[0]));
+                if (!done) res = block_once([=] { return sqrt(fabs(s2[0])); });
             }
             if (!done) {
                 if (nref == 0) res0 = res;
@@ -135,11 +138,13 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
             if (!multi && done) break;
             // inner FP32 BiCGSTAB on (scale K) d = r64/res, relative target
             const double rho = res;
-            const double target = done ? 0.0 : fmax(a.inner_tol, 0.3 * a.tol * rhsn / res);
+            const double target =
+                done ? 0.0 : block_once([=] { return fmax(a.inner_tol, 0.3 * a.tol * rhsn / res); });
+            const double target2 = target * target;
             {
-                double rr = 0.0;
+                float rr = 0.0f;
                 if (!done) {
-                    const float inv = (float)(1.0 / rho);
+                    const float inv = (float)block_once([=] { return 1.0 / rho; });
                     SAMPLE_ROWS(i) {
                         for (int c = 0; c < 2; c++) {
                             const int k = 2 * i + c;
@@ -148,12 +153,12 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
                             a.rt[k] = rv;
                             a.p[k] = rv;
                             a.d[k] = 0.0f;
-                            rr += (double)rv * rv;
+                            rr += rv * rv;
                         }
                     }
                 }
-                double v2[2] = {rr, (threadIdx.x == 0 && !done) ? 1.0 : 0.0};
-                block_store<2>(v2, a.partial, G);
+                float v2[2] = {rr, (threadIdx.x == 0 && !done) ? 1.0f : 0.0f};
+                block_store_f<2>(v2, a.partial, G);
             }
             if (!grid_sync(a.bar)) goto timeout;
             {
@@ -169,12 +174,12 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
                 int it = 0;
                 bool act = !done;
                 for (;;) {
-                    if (act && !(sqrt(rr) > target && nit < a.maxiter)) act = false;
+                    if (act && !(rr > target2 && nit < a.maxiter)) act = false;
                     if (act) {
                         rho1 = rtr;
                         if (it > 0) {
                             if (rho2 == 0.0 || omega == 0.0) act = false;
-                            else beta = (rho1 / rho2) * (alpha / omega);
+                            else beta = block_once([=] { return (rho1 / rho2) * (alpha / omega); });
                         }
                     }
                     if (!multi && !act) break;
@@ -196,7 +201,7 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
                     }
                     if (!grid_sync(a.bar)) goto timeout;
                     {
-                        double vr = 0.0;
+                        float vr = 0.0f;
                         if (act) {
                             auto row = [&](int i, bool valid, int sub) {
                                 float y0 = 0, y1 = 0;
@@ -207,13 +212,13 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
                                     if (!a.mag[i]) y0 = y1 = 0.0f;
                                     a.v[2 * i] = y0;
                                     a.v[2 * i + 1] = y1;
-                                    vr += (double)y0 * a.rt[2 * i] + (double)y1 * a.rt[2 * i + 1];
+                                    vr += y0 * a.rt[2 * i] + y1 * a.rt[2 * i + 1];
                                 }
                             };
                             GROUP_ROWS(row)
                         }
-                        double v2[2] = {vr, (threadIdx.x == 0 && act) ? 1.0 : 0.0};
-                        block_store<2>(v2, a.partial, G);
+                        float v2[2] = {vr, (threadIdx.x == 0 && act) ? 1.0f : 0.0f};
+                        block_store_f<2>(v2, a.partial, G);
                     }
                     if (!grid_sync(a.bar)) goto timeout;
                     {
@@ -224,10 +229,10 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
                             grid_sum<1>(a.partial + G, G, f);
                             if (f[0] == 0.0) break;
                         }
-                        if (act) alpha = rho1 / s1b[0];
+                        if (act) alpha = block_once([=] { return rho1 / s1b[0]; });
                     }
                     {
-                        double ss = 0.0;
+                        float ss = 0.0f;
                         if (act) {
                             const float fa = (float)alpha;
                             SAMPLE_ROWS(i) {
@@ -238,17 +243,17 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
                                 a.shat[2 * i] = h0;
                                 a.shat[2 * i + 1] = h1;
                                 tangent<float>(i, a.ep32, a.eq32, h0, h1, a.W32);
-                                ss += (double)s0 * s0 + (double)s1 * s1;
+                                ss += s0 * s0 + s1 * s1;
                             }
                         }
-                        double v1[1] = {ss};
-                        block_store<1>(v1, a.partial, G);
+                        float v1[1] = {ss};
+                        block_store_f<1>(v1, a.partial, G);
                     }
                     if (!grid_sync(a.bar)) goto timeout;
                     {
                         double s1c[1];
                         range_sum<1>(a.partial, G, sv.b0, sv.b1, s1c);
-                        if (act && sqrt(s1c[0]) <= target) {
+                        if (act && s1c[0] <= target2) {
                             const float fa = (float)alpha;
                             SAMPLE_ROWS(i) {
                                 a.d[2 * i] += fa * a.phat[2 * i];
@@ -260,7 +265,7 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
                     }
                     if (!multi && !act) break;
                     {
-                        double ts = 0.0, tt = 0.0;
+                        float ts = 0.0f, tt = 0.0f;
                         if (act) {
                             auto row = [&](int i, bool valid, int sub) {
                                 float y0 = 0, y1 = 0;
@@ -271,23 +276,23 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
                                     if (!a.mag[i]) y0 = y1 = 0.0f;
                                     a.t[2 * i] = y0;
                                     a.t[2 * i + 1] = y1;
-                                    ts += (double)y0 * a.s[2 * i] + (double)y1 * a.s[2 * i + 1];
-                                    tt += (double)y0 * y0 + (double)y1 * y1;
+                                    ts += y0 * a.s[2 * i] + y1 * a.s[2 * i + 1];
+                                    tt += y0 * y0 + y1 * y1;
                                 }
                             };
                             GROUP_ROWS(row)
                         }
-                        double v2[2] = {ts, tt};
-                        block_store<2>(v2, a.partial, G);
+                        float v2[2] = {ts, tt};
+                        block_store_f<2>(v2, a.partial, G);
                     }
                     if (!grid_sync(a.bar)) goto timeout;
                     {
                         double s2b[2];
                         range_sum<2>(a.partial, G, sv.b0, sv.b1, s2b);
-                        if (act) omega = s2b[0] / s2b[1];
+                        if (act) omega = block_once([=] { return s2b[0] / s2b[1]; });
                     }
                     {
-                        double r2 = 0.0, rtr2 = 0.0;
+                        float r2 = 0.0f, rtr2 = 0.0f;
                         if (act) {
                             const float fa = (float)alpha, fo = (float)omega;
                             SAMPLE_ROWS(i) {
@@ -297,13 +302,13 @@ __global__ void __launch_bounds__(256) k_mixed(MixedArgs a) {
                                     a.d[k] += fa * a.phat[k] + fo * a.shat[k];
                                     const float rv = a.s[k] - fo * a.t[k];
                                     a.r[k] = rv;
-                                    r2 += (double)rv * rv;
-                                    rtr2 += (double)a.rt[k] * rv;
+                                    r2 += rv * rv;
+                                    rtr2 += a.rt[k] * rv;
                                 }
                             }
                         }
-                        double v2[2] = {r2, rtr2};
-                        block_store<2>(v2, a.partial, G);
+                        float v2[2] = {r2, rtr2};
+                        block_store_f<2>(v2, a.partial, G);
                     }
                     if (!grid_sync(a.bar)) goto timeout;
                     {

@@ -15,6 +15,7 @@
 // (src/algebra/bicg.h:82-153) as one persistent cooperative kernel, FP64.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -45,31 +46,67 @@ struct SpinArgs {
     SolveResult *res;
     double tol;
     int maxiter;
+    // FP32 body with FP64 refinement (FG_PREC_FP32_REFINE): the operator scaled by `scale`
+    // in FP32, CURRENT m in FP32, FP64 b and refinement residual, FP32 Krylov vectors
+    // (the FP32 vectors are padded to n4 float4 chunks; dinv3 is the Jacobi factor per
+    // component, zero at Dirichlet nodes and in the padding)
+    const float *A32, *cc32, *dinv3;
+    float *m32;
+    int n4;
+    double *b64, *r64;
+    float *fr, *frt, *fp, *fphat, *fv, *fs, *fshat, *ft, *fd;
+    double scale, inner_tol;
+    int refine_max;
 };
 
-// y_i = sum_j A_ij x_j + c_i (x_i x m_i), zero at Dirichlet nodes
-__device__ __forceinline__ void spin_apply(const SpinArgs &a, const double *__restrict__ x, int i, double y[3]) {
-    double s0 = 0, s1 = 0, s2 = 0;
-    for (int k = a.ptr[i]; k < a.ptr[i + 1]; k++) {
-        const int j = a.col[k];
-        const double w = a.A[k];
-        s0 += w * __ldcg(x + 3 * j);
-        s1 += w * __ldcg(x + 3 * j + 1);
-        s2 += w * __ldcg(x + 3 * j + 2);
+// One row of y = A x + c (x x m), zero at Dirichlet nodes, on LPR lanes (the group's lanes
+// split the row's entries and combine with shuffles; every lane of the warp takes part).
+template <typename T, int LPR>
+__device__ __forceinline__ void spin_row(bool valid, int i, int sub, const int *__restrict__ ptr,
+                                         const int *__restrict__ col, const T *__restrict__ A,
+                                         const T *__restrict__ cc, const T *m, const unsigned char *__restrict__ dir,
+                                         const T *x, T y[3]) {
+    T s0 = 0, s1 = 0, s2 = 0;
+    if (valid) {
+        const int k1 = ptr[i + 1];
+        for (int k = ptr[i] + sub; k < k1; k += LPR) {
+            const int j = col[k];
+            const T w = A[k];
+            s0 += w * __ldcg(x + 3 * j);
+            s1 += w * __ldcg(x + 3 * j + 1);
+            s2 += w * __ldcg(x + 3 * j + 2);
+        }
     }
-    const double c = a.cc[i];
-    if (c != 0.0) {
-        const double x0 = __ldcg(x + 3 * i), x1 = __ldcg(x + 3 * i + 1), x2 = __ldcg(x + 3 * i + 2);
-        const double m0 = a.m0[3 * i], m1 = a.m0[3 * i + 1], m2 = a.m0[3 * i + 2];
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    y[0] = y[1] = y[2] = T(0);
+    if (!valid || dir[i]) return;
+    const T c = cc[i];
+    if (c != T(0)) {
+        const T x0 = __ldcg(x + 3 * i), x1 = __ldcg(x + 3 * i + 1), x2 = __ldcg(x + 3 * i + 2);
+        const T m0 = __ldcg(m + 3 * i), m1 = __ldcg(m + 3 * i + 1), m2 = __ldcg(m + 3 * i + 2);
         s0 += c * (x1 * m2 - x2 * m1);
         s1 += c * (x2 * m0 - x0 * m2);
         s2 += c * (x0 * m1 - x1 * m0);
     }
-    const bool d = a.dir[i];
-    y[0] = d ? 0.0 : s0;
-    y[1] = d ? 0.0 : s1;
-    y[2] = d ? 0.0 : s2;
+    y[0] = s0;
+    y[1] = s1;
+    y[2] = s2;
 }
+
+constexpr int SPIN_LPR = 4;
+
+// Rows in groups of SPIN_LPR lanes, the loop warp-uniform: body(i, valid, sub).
+#define SPIN_ROWS(body)                                                                                 \
+    for (int gb_ = (blockIdx.x * (int)blockDim.x + (int)(threadIdx.x & ~31)) / SPIN_LPR; gb_ < nn;      \
+         gb_ += gstride) {                                                                              \
+        const int i_ = gb_ + (int)(threadIdx.x & 31) / SPIN_LPR;                                        \
+        body(i_, i_ < nn, (int)threadIdx.x % SPIN_LPR);                                                 \
+    }
 
 // bicg_dir with Dirichlet values (src/algebra/bicg.h:82-153), every dot product formed as in
 // the reference (five grid barriers per iteration: forming rho and |r| from the iteration's
@@ -77,12 +114,14 @@ __device__ __forceinline__ void spin_apply(const SpinArgs &a, const double *__re
 __global__ void __launch_bounds__(256) k_spin_bicg(SpinArgs a) {
     const int G = gridDim.x, nn = a.nn;
     const int stride = G * blockDim.x, i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gstride = G * (int)blockDim.x / SPIN_LPR;
     // b = rhs - K xd (masked); x = 0 (the reference starts from a zero vector), r = rt = p = b
     {
         double bb = 0.0;
-        for (int i = i0; i < nn; i += stride) {
+        auto row = [&](int i, bool valid, int sub) {
             double y[3];
-            spin_apply(a, a.xd, i, y);
+            spin_row<double, SPIN_LPR>(valid, i, sub, a.ptr, a.col, a.A, a.cc, a.m0, a.dir, a.xd, y);
+            if (!valid || sub != 0) return;
             const bool d = a.dir[i];
 #pragma unroll
             for (int c = 0; c < 3; c++) {
@@ -94,7 +133,8 @@ __global__ void __launch_bounds__(256) k_spin_bicg(SpinArgs a) {
                 a.p[k] = b;
                 bb += b * b;
             }
-        }
+        };
+        SPIN_ROWS(row)
         double v1[1] = {bb};
         block_store<1>(v1, a.partial, G);
     }
@@ -143,15 +183,17 @@ __global__ void __launch_bounds__(256) k_spin_bicg(SpinArgs a) {
             if (!grid_sync(a.bar)) goto timeout;
             {
                 double vr = 0.0;
-                for (int i = i0; i < nn; i += stride) {
+                auto row = [&](int i, bool valid, int sub) {
                     double y[3];
-                    spin_apply(a, a.phat, i, y);
+                    spin_row<double, SPIN_LPR>(valid, i, sub, a.ptr, a.col, a.A, a.cc, a.m0, a.dir, a.phat, y);
+                    if (!valid || sub != 0) return;
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
                         a.v[3 * i + c] = y[c];
                         vr += y[c] * a.rt[3 * i + c];
                     }
-                }
+                };
+                SPIN_ROWS(row)
                 double v1[1] = {vr};
                 block_store<1>(v1, a.partial, G);
             }
@@ -192,16 +234,18 @@ __global__ void __launch_bounds__(256) k_spin_bicg(SpinArgs a) {
             }
             {
                 double ts = 0.0, tt = 0.0;
-                for (int i = i0; i < nn; i += stride) {
+                auto row = [&](int i, bool valid, int sub) {
                     double y[3];
-                    spin_apply(a, a.shat, i, y);
+                    spin_row<double, SPIN_LPR>(valid, i, sub, a.ptr, a.col, a.A, a.cc, a.m0, a.dir, a.shat, y);
+                    if (!valid || sub != 0) return;
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
                         a.t[3 * i + c] = y[c];
                         ts += y[c] * a.s[3 * i + c];
                         tt += y[c] * y[c];
                     }
-                }
+                };
+                SPIN_ROWS(row)
                 double v2[2] = {ts, tt};
                 block_store<2>(v2, a.partial, G);
             }
@@ -240,6 +284,274 @@ __global__ void __launch_bounds__(256) k_spin_bicg(SpinArgs a) {
             if (nit >= a.maxiter) status = 1;
         }
         // spinAcc::solve / compute: s = x + xd when converged, zero otherwise
+        const bool ok = (status == 0);
+        for (int k = i0; k < 3 * nn; k += stride) a.out[k] = ok ? a.x[k] + a.xd[k] : 0.0;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            a.res->status = status;
+            a.res->nit = nit;
+            a.res->fail = ok ? 0 : 1;
+            a.res->res = res;
+            a.res->rhsn = rhsn;
+            a.res->res0 = res0;
+        }
+        return;
+    }
+timeout:
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.res->timeout = 1;
+        a.res->fail = 1;
+    }
+}
+
+// The same problem with an FP32 Krylov body and FP64 iterative refinement (the arithmetic
+// of the LLG solve in FG_PREC_FP32_REFINE):
+//   outer (FP64): r = b - K x; stop when |r| <= tol |b|, the reference's test on the true
+//                 residual; status 1 after refine_max sweeps or maxiter inner iterations;
+//   inner (FP32): Jacobi BiCGSTAB on (scale K) d = r / |r| from d = 0, dot products summed
+//                 in FP32 per warp and FP64 across warps and blocks, the recurrence scalars
+//                 in FP64 once per block, to the relative target max(inner_tol,
+//                 0.3 tol |b| / |r|);
+//   x += scale |r| d in FP64.
+__global__ void __launch_bounds__(256, 4) k_spin_mixed(SpinArgs a) {
+    const int G = gridDim.x, nn = a.nn;
+    const int stride = G * blockDim.x, i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gstride = G * (int)blockDim.x / SPIN_LPR;
+    // FP32 CURRENT m; b = rhs - K xd (FP64, masked) = the first refinement residual; x = 0
+    for (int k = i0; k < 3 * nn; k += stride) {
+        a.m32[k] = (float)a.m0[k];
+        a.x[k] = 0.0;
+    }
+    {
+        double bb = 0.0;
+        auto row = [&](int i, bool valid, int sub) {
+            double y[3];
+            spin_row<double, SPIN_LPR>(valid, i, sub, a.ptr, a.col, a.A, a.cc, a.m0, a.dir, a.xd, y);
+            if (!valid || sub != 0) return;
+            const bool d = a.dir[i];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const int k = 3 * i + c;
+                const double b = d ? 0.0 : a.G[i] * a.m1[k] + a.L[k] - y[c];
+                a.b64[k] = b;
+                a.r64[k] = b;
+                bb += b * b;
+            }
+        };
+        SPIN_ROWS(row)
+        double v1[1] = {bb};
+        block_store<1>(v1, a.partial, G);
+    }
+    if (!grid_sync(a.bar)) goto timeout;
+    {
+        double s1[1];
+        grid_sum<1>(a.partial, G, s1);
+        const double rhsn = sqrt(fabs(s1[0]));
+        double res = rhsn;
+        const double res0 = res;
+        int status = -1, nit = 0, nref = 0;
+        for (;;) {
+            if (nref > 0) {
+                // refinement residual r64 = b - K x (FP64)
+                double rr = 0.0;
+                auto row = [&](int i, bool valid, int sub) {
+                    double y[3];
+                    spin_row<double, SPIN_LPR>(valid, i, sub, a.ptr, a.col, a.A, a.cc, a.m0, a.dir, a.x, y);
+                    if (!valid || sub != 0) return;
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const double rv = a.b64[3 * i + c] - y[c];
+                        a.r64[3 * i + c] = rv;
+                        rr += rv * rv;
+                    }
+                };
+                SPIN_ROWS(row)
+                double v1[1] = {rr};
+                block_store<1>(v1, a.partial, G);
+                if (!grid_sync(a.bar)) goto timeout;
+                double s1r[1];
+                grid_sum<1>(a.partial, G, s1r);
+                res = block_once([=] { return sqrt(fabs(s1r[0])); });
+            }
+            if (isnan(res)) { status = 2; break; }
+            if (res <= rhsn * a.tol) { status = 0; break; }
+            if (nref >= a.refine_max || nit >= a.maxiter) { status = 1; break; }
+            const double target = block_once([=] { return fmax(a.inner_tol, 0.3 * a.tol * rhsn / res); });
+            const double target2 = target * target;
+            {
+                float rr = 0.0f;
+                const float inv = (float)block_once([=] { return 1.0 / res; });
+                for (int k = i0; k < 3 * nn; k += stride) {
+                    const float rv = (float)a.r64[k] * inv;
+                    a.fr[k] = rv;
+                    a.frt[k] = rv;
+                    a.fp[k] = rv;
+                    a.fd[k] = 0.0f;
+                    rr += rv * rv;
+                }
+                float v1[1] = {rr};
+                block_store_f<1>(v1, a.partial, G);
+            }
+            if (!grid_sync(a.bar)) goto timeout;
+            {
+                double s1i[1];
+                grid_sum<1>(a.partial, G, s1i);
+                double rr = s1i[0], rtr = s1i[0];
+                double rho1 = 0.0, rho2 = 0.0, alpha = 0.0, beta = 0.0, omega = 0.0;
+                for (int it = 0;; it++) {
+                    if (!(rr > target2 && nit < a.maxiter)) break;
+                    rho1 = rtr;
+                    if (it > 0) {
+                        if (rho2 == 0.0 || omega == 0.0) break;
+                        beta = block_once([=] { return (rho1 / rho2) * (alpha / omega); });
+                    }
+                    {
+                        const float fb = (float)beta, fo = (float)omega;
+                        float4 *__restrict__ P = reinterpret_cast<float4 *>(a.fp);
+                        float4 *__restrict__ PH = reinterpret_cast<float4 *>(a.fphat);
+                        const float4 *__restrict__ R = reinterpret_cast<const float4 *>(a.fr);
+                        const float4 *__restrict__ V = reinterpret_cast<const float4 *>(a.fv);
+                        const float4 *__restrict__ D = reinterpret_cast<const float4 *>(a.dinv3);
+                        for (int q = i0; q < a.n4; q += stride) {
+                            float4 pv = P[q];
+                            if (it > 0) {
+                                const float4 r = R[q], v = V[q];
+                                pv.x = r.x + fb * (pv.x - fo * v.x);
+                                pv.y = r.y + fb * (pv.y - fo * v.y);
+                                pv.z = r.z + fb * (pv.z - fo * v.z);
+                                pv.w = r.w + fb * (pv.w - fo * v.w);
+                                P[q] = pv;
+                            }
+                            const float4 d = D[q];
+                            PH[q] = make_float4(d.x * pv.x, d.y * pv.y, d.z * pv.z, d.w * pv.w);
+                        }
+                    }
+                    if (!grid_sync(a.bar)) goto timeout;
+                    {
+                        float vr = 0.0f;
+                        auto row = [&](int i, bool valid, int sub) {
+                            float y[3];
+                            spin_row<float, SPIN_LPR>(valid, i, sub, a.ptr, a.col, a.A32, a.cc32, a.m32, a.dir,
+                                                      a.fphat, y);
+                            if (!valid || sub != 0) return;
+#pragma unroll
+                            for (int c = 0; c < 3; c++) {
+                                a.fv[3 * i + c] = y[c];
+                                vr += y[c] * a.frt[3 * i + c];
+                            }
+                        };
+                        SPIN_ROWS(row)
+                        float v1[1] = {vr};
+                        block_store_f<1>(v1, a.partial, G);
+                    }
+                    if (!grid_sync(a.bar)) goto timeout;
+                    {
+                        double s1b[1];
+                        grid_sum<1>(a.partial, G, s1b);
+                        alpha = block_once([=] { return rho1 / s1b[0]; });
+                    }
+                    {
+                        float ss = 0.0f;
+                        const float fa = (float)alpha;
+                        float4 *__restrict__ S4 = reinterpret_cast<float4 *>(a.fs);
+                        float4 *__restrict__ SH = reinterpret_cast<float4 *>(a.fshat);
+                        const float4 *__restrict__ R = reinterpret_cast<const float4 *>(a.fr);
+                        const float4 *__restrict__ V = reinterpret_cast<const float4 *>(a.fv);
+                        const float4 *__restrict__ D = reinterpret_cast<const float4 *>(a.dinv3);
+                        for (int q = i0; q < a.n4; q += stride) {
+                            const float4 r = R[q], v = V[q], d = D[q];
+                            const float4 sv = make_float4(r.x - fa * v.x, r.y - fa * v.y, r.z - fa * v.z, r.w - fa * v.w);
+                            S4[q] = sv;
+                            SH[q] = make_float4(d.x * sv.x, d.y * sv.y, d.z * sv.z, d.w * sv.w);
+                            ss += sv.x * sv.x + sv.y * sv.y + sv.z * sv.z + sv.w * sv.w;
+                        }
+                        float v1[1] = {ss};
+                        block_store_f<1>(v1, a.partial, G);
+                    }
+                    if (!grid_sync(a.bar)) goto timeout;
+                    {
+                        double s1c[1];
+                        grid_sum<1>(a.partial, G, s1c);
+                        if (s1c[0] <= target2) {
+                            const float fa = (float)alpha;
+                            float4 *__restrict__ D4 = reinterpret_cast<float4 *>(a.fd);
+                            const float4 *__restrict__ PH = reinterpret_cast<const float4 *>(a.fphat);
+                            for (int q = i0; q < a.n4; q += stride) {
+                                float4 d = D4[q];
+                                const float4 h = PH[q];
+                                d.x += fa * h.x; d.y += fa * h.y; d.z += fa * h.z; d.w += fa * h.w;
+                                D4[q] = d;
+                            }
+                            nit++;
+                            break;
+                        }
+                    }
+                    {
+                        float ts = 0.0f, tt = 0.0f;
+                        auto row = [&](int i, bool valid, int sub) {
+                            float y[3];
+                            spin_row<float, SPIN_LPR>(valid, i, sub, a.ptr, a.col, a.A32, a.cc32, a.m32, a.dir,
+                                                      a.fshat, y);
+                            if (!valid || sub != 0) return;
+#pragma unroll
+                            for (int c = 0; c < 3; c++) {
+                                a.ft[3 * i + c] = y[c];
+                                ts += y[c] * a.fs[3 * i + c];
+                                tt += y[c] * y[c];
+                            }
+                        };
+                        SPIN_ROWS(row)
+                        float v2[2] = {ts, tt};
+                        block_store_f<2>(v2, a.partial, G);
+                    }
+                    if (!grid_sync(a.bar)) goto timeout;
+                    {
+                        double s2[2];
+                        grid_sum<2>(a.partial, G, s2);
+                        omega = block_once([=] { return s2[0] / s2[1]; });
+                    }
+                    {
+                        float r2 = 0.0f, rtr2 = 0.0f;
+                        const float fa = (float)alpha, fo = (float)omega;
+                        float4 *__restrict__ D4 = reinterpret_cast<float4 *>(a.fd);
+                        float4 *__restrict__ R4 = reinterpret_cast<float4 *>(a.fr);
+                        const float4 *__restrict__ PH = reinterpret_cast<const float4 *>(a.fphat);
+                        const float4 *__restrict__ SH = reinterpret_cast<const float4 *>(a.fshat);
+                        const float4 *__restrict__ S4 = reinterpret_cast<const float4 *>(a.fs);
+                        const float4 *__restrict__ T4 = reinterpret_cast<const float4 *>(a.ft);
+                        const float4 *__restrict__ RT = reinterpret_cast<const float4 *>(a.frt);
+                        for (int q = i0; q < a.n4; q += stride) {
+                            float4 d = D4[q];
+                            const float4 h = PH[q], g = SH[q], sv = S4[q], t = T4[q], rt = RT[q];
+                            d.x += fa * h.x + fo * g.x; d.y += fa * h.y + fo * g.y;
+                            d.z += fa * h.z + fo * g.z; d.w += fa * h.w + fo * g.w;
+                            D4[q] = d;
+                            const float4 rv = make_float4(sv.x - fo * t.x, sv.y - fo * t.y, sv.z - fo * t.z, sv.w - fo * t.w);
+                            R4[q] = rv;
+                            r2 += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+                            rtr2 += rt.x * rv.x + rt.y * rv.y + rt.z * rv.z + rt.w * rv.w;
+                        }
+                        float v2[2] = {r2, rtr2};
+                        block_store_f<2>(v2, a.partial, G);
+                    }
+                    if (!grid_sync(a.bar)) goto timeout;
+                    {
+                        double s2c[2];
+                        grid_sum<2>(a.partial, G, s2c);
+                        rr = s2c[0];
+                        rtr = s2c[1];
+                    }
+                    rho2 = rho1;
+                    nit++;
+                }
+            }
+            // x += scale |r| d (FP64); the next residual gathers x across the grid
+            {
+                const double f = a.scale * res;
+                for (int k = i0; k < 3 * nn; k += stride) a.x[k] += f * (double)a.fd[k];
+            }
+            nref++;
+            if (!grid_sync(a.bar)) goto timeout;
+        }
         const bool ok = (status == 0);
         for (int k = i0; k < 3 * nn; k += stride) a.out[k] = ok ? a.x[k] + a.xd[k] : 0.0;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -356,6 +668,13 @@ struct SpinState {
     double *partial = nullptr;
     GridBar *bar = nullptr;
     SolveResult *res = nullptr, *hres = nullptr;
+    // FG_PREC_FP32_REFINE: scaled FP32 operator, FP32 Krylov vectors and CURRENT m
+    // (10 x 3nn floats), FP64 b and refinement residual (2 x 3nn)
+    bool mixed = false;
+    double scale = 1.0;
+    float *A32 = nullptr, *cc32 = nullptr, *dinv3 = nullptr, *work32 = nullptr;
+    size_t n3p = 0;  // 3nn rounded up to whole float4 chunks
+    double *b64 = nullptr;
     std::vector<double> V;   // electrostatic potential (host, node order of the mesh)
     int v_iters = 0, v_status = 0;
 };
@@ -592,10 +911,43 @@ int spin_setup(Ctx &c, const fg_mesh *m, const fg_region *regs, int nreg, const 
         c.err = "fg_create: device allocation for the spin accumulation failed";
         return FG_ECUDA;
     }
-    int per_sm = 0;
+    if (c.opts.precision == FG_PREC_FP32_REFINE) {
+        // scale = 1 / mean diagonal of the free rows keeps the FP32 operator O(1)
+        double dsum = 0.0;
+        int nfree = 0;
+        for (int i = 0; i < nn; i++)
+            if (!sdir[i]) {
+                dsum += A[find_col(ptr, col, i, i)];
+                nfree++;
+            }
+        S->mixed = true;
+        S->scale = (nfree > 0 && dsum > 0.0) ? nfree / dsum : 1.0;
+        S->n3p = (n3 + 3) / 4 * 4;
+        std::vector<float> A32(nnz), cc32(nn), dinv3(S->n3p, 0.0f);
+        for (size_t k = 0; k < nnz; k++) A32[k] = (float)(S->scale * A[k]);
+        for (int i = 0; i < nn; i++) {
+            cc32[i] = (float)(S->scale * cc[i]);
+            for (int d = 0; d < 3; d++) dinv3[3 * (size_t)i + d] = sdir[i] ? 0.0f : (float)(dinv[i] / S->scale);
+        }
+        // the Krylov vectors start (and their padding stays) zero
+        if (up(&S->A32, A32) || up(&S->cc32, cc32) || up(&S->dinv3, dinv3) ||
+            cudaMalloc(&S->work32, 10 * S->n3p * sizeof(float)) ||
+            cudaMemset(S->work32, 0, 10 * S->n3p * sizeof(float)) || cudaMalloc(&S->b64, 2 * n3 * sizeof(double))) {
+            c.err = "fg_create: device allocation for the spin accumulation failed";
+            return FG_ECUDA;
+        }
+    }
+    int per_sm = 0, per_sm_mixed = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spin_bicg, 256, 0);
-    // two blocks per SM: fewer blocks make each of the solve's grid barriers cheaper
-    S->grid = std::max(1, std::min(std::min(std::max(1, per_sm), 2) * c.nsm, (nn + 255) / 256));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_mixed, k_spin_mixed, 256, 0);
+    if (S->mixed) per_sm = per_sm_mixed;
+    // blocks per SM: the FP64 kernel runs best with two (fewer blocks make each grid barrier
+    // cheaper), the FP32 body with four (its latency-bound sweeps want the warps; measured
+    // 77 against 93 us per iteration on the 1.2M-tet film); FG_SPIN_BLOCKS_PER_SM overrides
+    // it (up to the kernel's occupancy)
+    int bps = S->mixed ? 4 : 2;
+    if (const char *env = std::getenv("FG_SPIN_BLOCKS_PER_SM")) bps = std::max(1, std::atoi(env));
+    S->grid = std::max(1, std::min(std::min(std::max(1, per_sm), bps) * c.nsm, (nn + 255) / 256));
     if (cudaMalloc(&S->partial, 3 * sizeof(double) * std::max(1024, S->grid)) != cudaSuccess) return FG_ECUDA;
     c.spin_s = S->out;
     return FG_OK;
@@ -605,7 +957,7 @@ void spin_free(Ctx &c) {
     SpinState *S = static_cast<SpinState *>(c.spin);
     if (!S) return;
     void *p[] = {S->ptr, S->col, S->A, S->dinv, S->cc, S->G, S->L, S->xd, S->dir, S->work, S->out, S->partial,
-                 S->bar, S->res};
+                 S->bar, S->res, S->A32, S->cc32, S->dinv3, S->work32, S->b64};
     for (void *q : p)
         if (q) cudaFree(q);
     if (S->hres) cudaFreeHost(S->hres);
@@ -629,10 +981,22 @@ cudaError_t launch_spin(Ctx &c) {
     a.out = S->out;
     a.partial = S->partial; a.bar = S->bar; a.res = S->res;
     a.tol = c.opts.spin_tol; a.maxiter = c.opts.spin_max_iter;
+    a.A32 = S->A32; a.cc32 = S->cc32; a.dinv3 = S->dinv3; a.n4 = (int)(S->n3p / 4);
+    a.m32 = a.fr = a.frt = a.fp = a.fphat = a.fv = a.fs = a.fshat = a.ft = a.fd = nullptr;
+    a.b64 = a.r64 = nullptr;
+    if (S->mixed) {
+        float *w = S->work32;
+        const size_t q = S->n3p;
+        a.fr = w; a.frt = w + q; a.fp = w + 2 * q; a.fphat = w + 3 * q; a.fv = w + 4 * q; a.fs = w + 5 * q;
+        a.fshat = w + 6 * q; a.ft = w + 7 * q; a.fd = w + 8 * q; a.m32 = w + 9 * q;
+        a.b64 = S->b64; a.r64 = S->b64 + n3;
+    }
+    a.scale = S->scale; a.inner_tol = c.opts.inner_tol; a.refine_max = c.opts.refine_max;
     cudaError_t e = cudaMemsetAsync(S->res, 0, sizeof(SolveResult), c.stream);
     if (e != cudaSuccess) return e;
     void *args[] = {&a};
-    return cudaLaunchCooperativeKernel((void *)k_spin_bicg, dim3(S->grid), dim3(256), args, 0, c.stream);
+    return cudaLaunchCooperativeKernel(S->mixed ? (void *)k_spin_mixed : (void *)k_spin_bicg, dim3(S->grid),
+                                       dim3(256), args, 0, c.stream);
 }
 
 int spin_info(const Ctx &c, int *status, int *iters, double *V, int *v_iters) {

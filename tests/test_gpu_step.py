@@ -306,6 +306,39 @@ def test_spin_accumulation():
     assert _rel(o2.export_system()[3], rhs_o) > 1e-2
 
 
+@pytest.mark.parametrize("spin_tol", [1e-12, 1e-8])
+def test_spin_accumulation_fp32_refine(spin_tol):
+    """In FG_PREC_FP32_REFINE the spin problem is solved with an FP32 BiCGSTAB body and FP64
+    refinement: the same stopping test on the true FP64 residual, so s agrees with the
+    oracle's FP64 bicg_dir solution to the level the tolerance allows (1e-8 at a solve
+    tolerance of 1e-12, 1e-5 at 1e-8), and the step's RHS carries the same Hst."""
+    m, regs_o, regs_g, tregs_o, bc = _spin_case()
+    u = cases.perturbed_state(m["xyz"], seed=43)
+    v = cases.tangent_field(u, seed=44)
+    H = np.array([1e4, 2e4, -3e4])
+    o = fgo.Oracle(m, regs_o, tregs_o)
+    assert o.set_spin(True, 1e-12, 5000)[0] == 0
+    o.set_solver(1e-12, 5000)
+    o.set_state(u, v)
+    o.compute_all(H)
+    st = o.get_state(0)
+    _, so, sst, _ = o.spin()
+    assert sst == 0
+    c = fg.Context(m, regs_g, bc, tol=1e-12, max_iter=5000, spin_acc=1, spin_tol=spin_tol, spin_max_iter=5000,
+                   precision=fg.FG_PREC_FP32_REFINE)
+    c.set_state(st["u"], st["v"], st["phi"], st["phiv"])
+    c.compute_all(H)
+    info = c.spin_info()
+    assert info["status"] == fg.FG_OK and info["iters"] > 0
+    assert _rel(c.get_spin(), so) <= (1e-8 if spin_tol < 1e-10 else 1e-5)
+    if spin_tol < 1e-10:
+        angle, pref = 0.3, fgo.prefactor(DT, DTMAX)
+        o.base_projection(angle)
+        o.step(DT, pref, H)
+        c.step(DT, pref, H, angle)
+        assert _rel(c.debug_system()[0], o.export_system()[3]) <= 1e-9
+
+
 def test_spin_boundary_conditions_checked():
     """A spin-accumulation context without exactly one jn surface, one V surface and one s
     surface is refused (the reference's checkBoundaryConditions exit)."""
