@@ -347,18 +347,19 @@ def main():
     acc = [r["guess_accepted"] for r in reps]
     r0_ratio = [r["res0"] / r["res0_fallback"] for r in reps if r["res0_fallback"] > 0]
 
-    # end to end through the C ABI with host buffers: state in, step, compute_all, state out
+    # end to end through the C ABI with pinned host buffers: state in, step, compute_all,
+    # state out (into the same buffers)
     nn = len(mesh["xyz"])
-    st = ctx.get_state(0)
-    h_u, h_v, h_phi, h_phiv = st["u"].copy(), st["v"].copy(), st["phi"].copy(), st["phiv"].copy()
+    host = {"u": fg.pinned_empty((nn, 3)), "v": fg.pinned_empty((nn, 3)), "phi": fg.pinned_empty(nn),
+            "phiv": fg.pinned_empty(nn)}
+    ctx.get_state(0, out=host)
     e2e_t = []
     for k in range(args.e2e_steps + 1):
         t0 = time.perf_counter()
-        ctx.set_state(h_u, h_v, h_phi, h_phiv)
+        ctx.set_state(host["u"], host["v"], host["phi"], host["phiv"])
         ctx.step(DT, prefactor(DT, DT), H, angles())
         ctx.compute_all(H)
-        out = ctx.get_state(0)
-        h_u, h_v, h_phi, h_phiv = out["u"], out["v"], out["phi"], out["phiv"]
+        ctx.get_state(0, out=host)
         if k:
             e2e_t.append(time.perf_counter() - t0)
     e2e_s = max_over_ranks(dist, float(np.sum(e2e_t))) if e2e_t else None

@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -91,6 +92,8 @@ SIGNATURES = {
     "fg_step": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, C.c_double, C.POINTER(fg_step_report)]),
     "fg_compute_all": (C.c_int, [C.c_void_p, _dp, _dp]),
     "fg_get_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fg_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
+    "fg_host_free": (C.c_int, [C.c_void_p]),
     "fg_demag": (C.c_int, [C.c_void_p, C.c_int, _dp]),
     "fg_energy": (C.c_int, [C.c_void_p, _dp, _dp]),
     "fg_energy_noalloc": (C.c_int, [C.c_void_p, _dp, _dp]),
@@ -219,6 +222,21 @@ def checkpoint_peek(path):
     out.update({k: getattr(me, k) for k, _ in fg_checkpoint_meta._fields_ if k != "E"})
     out["E"] = list(me.E)
     return out
+
+
+def pinned_empty(shape, dtype=np.float64):
+    """numpy array in page-locked host memory (fg_host_alloc), freed with the array: state
+    buffers for Context.set_state / get_state(out=...) that cross the host link at full speed."""
+    dt = np.dtype(dtype)
+    n = int(np.prod(shape)) * dt.itemsize
+    L = fg_lib()
+    p = C.c_void_p()
+    st = L.fg_host_alloc(n, C.byref(p))
+    if st != FG_OK:
+        raise FgError(st, "fg_host_alloc: " + L.fg_strerror(st).decode())
+    buf = (C.c_char * max(n, 1)).from_address(p.value)
+    weakref.finalize(buf, L.fg_host_free, C.c_void_p(p.value))
+    return np.frombuffer(buf, dtype=dt, count=int(np.prod(shape))).reshape(shape)
 
 
 def rng_angle():
@@ -376,11 +394,20 @@ class Context:
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (u, v, phi, phiv)]
         self._check(self.L.fg_set_state(self.h, *[_ptr(a) for a in arrs]))
 
-    def get_state(self, which=1):
-        u, v = np.zeros((self.nn, 3)), np.zeros((self.nn, 3))
-        phi, phiv = np.zeros(self.nn), np.zeros(self.nn)
-        self._check(self.L.fg_get_state(self.h, which, _ptr(u), _ptr(v), _ptr(phi), _ptr(phiv)))
-        return {"u": u, "v": v, "phi": phi, "phiv": phiv}
+    def get_state(self, which=1, out=None):
+        """fg_get_state; `out` (a dict of C-contiguous float64 arrays u, v, phi, phiv of the
+        node count's shapes, e.g. from pinned_empty) is filled in place and returned."""
+        if out is None:
+            out = {"u": np.zeros((self.nn, 3)), "v": np.zeros((self.nn, 3)), "phi": np.zeros(self.nn),
+                   "phiv": np.zeros(self.nn)}
+        else:
+            for k, shape in (("u", (self.nn, 3)), ("v", (self.nn, 3)), ("phi", (self.nn,)), ("phiv", (self.nn,))):
+                a = out[k]
+                if a.dtype != np.float64 or a.shape != shape or not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError(f"get_state: out[{k!r}] must be a C-contiguous float64 array of shape {shape}")
+        self._check(self.L.fg_get_state(self.h, which, _ptr(out["u"]), _ptr(out["v"]), _ptr(out["phi"]),
+                                        _ptr(out["phiv"])))
+        return out
 
     @staticmethod
     def _sample_steps(dt, prefactor, Hext, angle, shape):

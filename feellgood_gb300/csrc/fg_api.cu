@@ -668,16 +668,38 @@ int fg_set_state(fg_ctx *h, const double *u, const double *v, const double *phi,
     if (!h || !u) return FG_EINVAL;
     Ctx &c = h->c;
     const size_t n3 = 3 * sizeof(double) * c.nn, n1 = sizeof(double) * c.nn;
-    for (int k = 0; k < 2; k++) {
-        CK(cudaMemcpyAsync(c.u[k], u, n3, cudaMemcpyHostToDevice, c.stream));
-        if (v) CK(cudaMemcpyAsync(c.v[k], v, n3, cudaMemcpyHostToDevice, c.stream));
-        else CK(cudaMemsetAsync(c.v[k], 0, n3, c.stream));
-        if (phi) CK(cudaMemcpyAsync(c.phi[k], phi, n1, cudaMemcpyHostToDevice, c.stream));
-        else CK(cudaMemsetAsync(c.phi[k], 0, n1, c.stream));
-        if (phiv) CK(cudaMemcpyAsync(c.phiv[k], phiv, n1, cudaMemcpyHostToDevice, c.stream));
-        else CK(cudaMemsetAsync(c.phiv[k], 0, n1, c.stream));
-    }
+    // the host data crosses the link once (into CURRENT); NEXT is a device-side copy
+    CK(cudaMemcpyAsync(c.u[0], u, n3, cudaMemcpyHostToDevice, c.stream));
+    if (v) CK(cudaMemcpyAsync(c.v[0], v, n3, cudaMemcpyHostToDevice, c.stream));
+    else CK(cudaMemsetAsync(c.v[0], 0, n3, c.stream));
+    if (phi) CK(cudaMemcpyAsync(c.phi[0], phi, n1, cudaMemcpyHostToDevice, c.stream));
+    else CK(cudaMemsetAsync(c.phi[0], 0, n1, c.stream));
+    if (phiv) CK(cudaMemcpyAsync(c.phiv[0], phiv, n1, cudaMemcpyHostToDevice, c.stream));
+    else CK(cudaMemsetAsync(c.phiv[0], 0, n1, c.stream));
+    CK(cudaMemcpyAsync(c.u[1], c.u[0], n3, cudaMemcpyDeviceToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.v[1], c.v[0], n3, cudaMemcpyDeviceToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.phi[1], c.phi[0], n1, cudaMemcpyDeviceToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.phiv[1], c.phiv[0], n1, cudaMemcpyDeviceToDevice, c.stream));
     CK(cudaStreamSynchronize(c.stream));
+    return FG_OK;
+}
+
+int fg_host_alloc(size_t bytes, void **ptr) {
+    if (!ptr) return FG_EINVAL;
+    *ptr = nullptr;
+    if (cudaMallocHost(ptr, bytes > 0 ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return FG_ECUDA;
+    }
+    return FG_OK;
+}
+
+int fg_host_free(void *ptr) {
+    if (ptr && cudaFreeHost(ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return FG_ECUDA;
+    }
     return FG_OK;
 }
 

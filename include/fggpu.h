@@ -154,6 +154,12 @@ int fg_compute_all(fg_ctx *ctx, const double Hext[3], double energies[4]);
 /* which: 0 = CURRENT, 1 = NEXT. Any output may be NULL. */
 int fg_get_state(const fg_ctx *ctx, int which, double *u, double *v, double *phi, double *phiv);
 
+/* Page-locked host memory for the state buffers of fg_set_state / fg_get_state: transfers
+ * from and to it run at the host link's full speed, pageable buffers are staged by the
+ * driver. No counterpart in the reference (its state never leaves the host). */
+int fg_host_alloc(size_t bytes, void **ptr);
+int fg_host_free(void *ptr);
+
 /* Demag potential of the NEXT field (which: 0 = u, 1 = v) into out[n_nodes], without
  * touching the state. */
 int fg_demag(fg_ctx *ctx, int which, double *out);

@@ -121,6 +121,30 @@ def test_compute_all(one_point):
         assert abs(avg[d] - o.avg(0, d)) <= 1e-12
 
 
+def test_state_round_trip_pinned():
+    """fg_set_state fills CURRENT and NEXT (one host upload, NEXT copied on the device);
+    fg_get_state writes into caller buffers, pinned (fg_host_alloc) or pageable, bit for bit;
+    malformed output buffers are refused before any copy."""
+    m, st, H, o, c = _setup()
+    nn = len(m["xyz"])
+    host = {"u": fg.pinned_empty((nn, 3)), "v": fg.pinned_empty((nn, 3)), "phi": fg.pinned_empty(nn),
+            "phiv": fg.pinned_empty(nn)}
+    for k in host:
+        host[k][...] = st[k]
+    c.set_state(host["u"], host["v"], host["phi"], host["phiv"])
+    for which in (0, 1):
+        out = {k: fg.pinned_empty(a.shape) for k, a in host.items()}
+        assert c.get_state(which, out=out) is out
+        for k in host:
+            assert np.array_equal(out[k], st[k])
+        pageable = c.get_state(which)
+        for k in host:
+            assert np.array_equal(pageable[k], st[k])
+    with pytest.raises(ValueError):
+        c.get_state(0, out={"u": np.zeros((nn, 3), np.float32), "v": host["v"], "phi": host["phi"],
+                            "phiv": host["phiv"]})
+
+
 def test_bad_mesh_is_rejected():
     m = cases.cuboid(2, 2, 2)
     bad = dict(m)
