@@ -423,8 +423,9 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
         e[0] = (m == 0) - u[m] * u[0];
         e[1] = (m == 1) - u[m] * u[1];
         e[2] = (m == 2) - u[m] * u[2];
-        const double n = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
-        e[0] /= n; e[1] /= n; e[2] /= n;
+        // one reciprocal instead of three divisions (GB300's FP64 pipe is 1/64 rate)
+        const double in = 1.0 / sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+        e[0] *= in; e[1] *= in; e[2] *= in;
         q[0] = u[1] * e[2] - u[2] * e[1];
         q[1] = u[2] * e[0] - u[0] * e[2];
         q[2] = u[0] * e[1] - u[1] * e[0];
@@ -466,8 +467,8 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
             be0 += b[0]; be1 += b[1]; be2 += b[2];
         }
     Dl[i] = dl;
+    const double ia = mag[i] ? 1.0 / A[i] : 0.0;
     if (heff) {  // effective field BE_i / A_i, a feature of the learned guess
-        const double ia = mag[i] ? 1.0 / A[i] : 0.0;
         heff[3 * i] = be0 * ia;
         heff[3 * i + 1] = be1 * ia;
         heff[3 * i + 2] = be2 * ia;
@@ -475,11 +476,14 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
     if (mag[i]) {
         rhs[2 * i] = q[0] * be0 + q[1] * be1 + q[2] * be2;
         rhs[2 * i + 1] = e[0] * be0 + e[1] * be1 + e[2] * be2;
-        Minv[2 * i] = 1.0 / A[i];
-        Minv[2 * i + 1] = -1.0 / A[i];
+        Minv[2 * i] = ia;
+        Minv[2 * i + 1] = -ia;
+        // initial guess v / gamma0 in the new basis (a start vector: the product with the
+        // reciprocal is as good as the quotient)
+        constexpr double inv_gamma0 = 1.0 / FG_GAMMA0;
         const double vv[3] = {v1[3 * i], v1[3 * i + 1], v1[3 * i + 2]};
-        const double xp = (vv[0] * e[0] + vv[1] * e[1] + vv[2] * e[2]) / FG_GAMMA0;
-        const double xq = (vv[0] * q[0] + vv[1] * q[1] + vv[2] * q[2]) / FG_GAMMA0;
+        const double xp = (vv[0] * e[0] + vv[1] * e[1] + vv[2] * e[2]) * inv_gamma0;
+        const double xq = (vv[0] * q[0] + vv[1] * q[1] + vv[2] * q[2]) * inv_gamma0;
         x[2 * i] = xp;
         x[2 * i + 1] = xq;
         W[3 * i] = xp * e[0] + xq * q[0];
