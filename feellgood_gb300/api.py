@@ -93,6 +93,7 @@ SIGNATURES = {
     "fg_compute_all": (C.c_int, [C.c_void_p, _dp, _dp]),
     "fg_get_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fg_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
+    "fg_set_drift": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "fg_host_free": (C.c_int, [C.c_void_p]),
     "fg_demag": (C.c_int, [C.c_void_p, C.c_int, _dp]),
     "fg_energy": (C.c_int, [C.c_void_p, _dp, _dp]),
@@ -463,6 +464,12 @@ class Context:
         V = np.zeros(self.nn)
         self._check(self.L.fg_spin_info(self.h, C.byref(st), C.byref(it), _ptr(V), C.byref(vit), C.byref(ms)))
         return {"status": st.value, "iters": it.value, "V": V, "V_iters": vit.value, "ms": ms.value}
+
+    def set_drift(self, direction, vdrift):
+        """fg_set_drift: recentering drift of the element integrals along direction 0/1/2
+        ('X'/'Y'/'Z', -1 or None for none) at vdrift m/s."""
+        d = {"X": 0, "Y": 1, "Z": 2, None: -1}.get(direction, direction)
+        self._check(self.L.fg_set_drift(self.h, int(d), float(vdrift)))
 
     def recenter(self, direction, threshold):
         """fg_recenter: direction 0/1/2 (x/y/z) or 'X'/'Y'/'Z'; returns True when it translated."""

@@ -1058,6 +1058,17 @@ int fg_set_field_amplitude(fg_ctx *h, double amplitude) {
     return FG_OK;
 }
 
+int fg_set_drift(fg_ctx *h, int direction, double vdrift) {
+    if (!h || direction < -1 || direction > 2 || !std::isfinite(vdrift)) return FG_EINVAL;
+    if (h->c.batch && direction >= 0 && vdrift != 0.0) {
+        h->c.err = "fg_set_drift: not available for batch contexts";
+        return FG_EINVAL;
+    }
+    h->c.drift_dir = direction;
+    h->c.drift_v = vdrift;
+    return FG_OK;
+}
+
 int fg_solver_info(const fg_ctx *h, int *lanes_per_row, int *blocks) {
     if (!h) return FG_EINVAL;
     if (lanes_per_row) *lanes_per_row = h->c.lpr;

@@ -215,6 +215,9 @@ struct Ctx {
     // at every Gauss point g of every magnetic tet; F is [nmt][npi_t][3] or nullptr
     double *hsp = nullptr;
     double field_amp = 1.0;
+    // recentering drift of the element integrals (fg_set_drift): direction 0/1/2 or -1, speed
+    int drift_dir = -1;
+    double drift_v = 0.0;
     // spin accumulation (fg_spin.cu): solver state and the last solution s [3 nn]
     void *spin = nullptr;
     double *spin_s = nullptr;
@@ -347,7 +350,8 @@ int elem_ds_setup(Ctx &c, const std::vector<double> &da, const std::vector<doubl
 void upload_rules_ds(const double ta[4][5], const double tp[5]);
 cudaError_t launch_tet_ds(Ctx &c, double dt, const double H[3]);
 void launch_state_ds(Ctx &c, const double *u, const double *phi, const double *phiv);
-inline bool use_elem_ds(const Ctx &c) { return c.elem_ds && !c.hsp && !c.spin_s; }
+inline bool drift_on(const Ctx &c) { return c.drift_dir >= 0 && c.drift_v != 0.0; }
+inline bool use_elem_ds(const Ctx &c) { return c.elem_ds && !c.hsp && !c.spin_s && !drift_on(c); }
 void recenter_free(Ctx &c);
 cudaError_t launch_select_params(Ctx &c);
 cudaError_t launch_advance(Ctx &c);

@@ -40,7 +40,7 @@ __constant__ double c_fpds[4];
 // calc_alpha_eff, anisotropy and BE parts of Tet::integrales (src/tetra.cpp:47-75,
 // 171-307) and writes per vertex (lumped alpha_eff weight, BE_i) to its slot.
 
-template <int NPI>
+template <int NPI, bool DRIFT>
 __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__ tet, const double *__restrict__ da,
                                                const double *__restrict__ detJ, const int *__restrict__ treg,
                                                const DevRegion *__restrict__ regs, const double *__restrict__ u0,
@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__
                                                double Hz, double4 *__restrict__ slot,
                                                const int *__restrict__ tet_seg, const SegPar *__restrict__ seg,
                                                const double *__restrict__ hsp, double amp,
-                                               const double *__restrict__ s_node) {
+                                               const double *__restrict__ s_node, int ddir, double vdrift) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nmt) return;
     if (seg) {  // batch: the tet's sample carries dt and the applied field
@@ -110,6 +110,22 @@ __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__
     double Hst[NPI][3], sHu[NPI], Vg[NPI][3];
     const double reduced_dt = FG_GAMMA0 * dt;
     const double M = 2. * alpha * 0.1 / reduced_dt;
+    // recentering drift (Tet::add_drift_BE, src/tetra.cpp:150-169, called at :277-288):
+    // Dr(g) = alpha dU + U x dU + s_dt (alpha dV + U x dV + V x dU) with dU, dV the constant
+    // derivatives of u and v along the direction; BE_i += vdrift w_g a_i(g) Dr(g)
+    double dUr[3] = {0.0, 0.0, 0.0}, dVr[3] = {0.0, 0.0, 0.0}, Dr[DRIFT ? NPI : 1][3];
+    if constexpr (DRIFT) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {  // selects the direction without indexing registers at run time
+            if (k != ddir) continue;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                dUr[c] = dU[k][c];
+#pragma unroll
+                for (int i = 0; i < 4; i++) dVr[c] += d[i][k] * vn[i][c];
+            }
+        }
+    }
 #pragma unroll
     for (int g = 0; g < NPI; g++) {
         w[g] = J * c_tpds[g];
@@ -124,6 +140,15 @@ __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__
             }
             U[c] = su;
             V[c] = sv;
+        }
+        if constexpr (DRIFT) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+                Dr[g][c] = alpha * dUr[c] + (U[c1] * dUr[c2] - U[c2] * dUr[c1]) +
+                           s_dt * (alpha * dVr[c] + (U[c1] * dVr[c2] - U[c2] * dVr[c1]) +
+                                   (V[c1] * dUr[c2] - V[c2] * dUr[c1]));
+            }
         }
         double uHeff = -Abis * gradsq;
         double Han[3] = {0.0, 0.0, 0.0};
@@ -208,6 +233,7 @@ __global__ void __launch_bounds__(128) k_tet64(int nmt, const int4 *__restrict__
                 } else {
                     BE[c] += ai_w * H[g][c];
                 }
+                if constexpr (DRIFT) BE[c] += vdrift * ai_w * Dr[g][c];
             }
         }
         slot[4 * (size_t)t + i] = make_double4(contrib, BE[0], BE[1], BE[2]);
@@ -1155,7 +1181,7 @@ cudaError_t launch_tet(Ctx &c, double dt, const double H[3]) {
     }
     if (c.nmt == 0) return cudaGetLastError();
     const int b = 128;
-    if (!c.aniso) {
+    if (!c.aniso && !drift_on(c)) {
         if (c.npi_t == 5)
             k_tet64_iso<5><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0],
                                                                    c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
@@ -1169,15 +1195,13 @@ cudaError_t launch_tet(Ctx &c, double dt, const double H[3]) {
         return cudaGetLastError();
     }
     if (c.npi_t == 5)
-        k_tet64<5><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0], c.v[0],
-                                                          c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
-                                                          c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp, c.field_amp,
-                                                          c.spin_s);
+        (drift_on(c) ? k_tet64<5, true> : k_tet64<5, false>)<<<nblocks(c.nmt, b), b, 0, c.stream>>>(
+            c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0], c.v[0], c.phi[0], c.phiv[0], dt, H[0], H[1], H[2],
+            c.slot, c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp, c.field_amp, c.spin_s, c.drift_dir, c.drift_v);
     else
-        k_tet64<1><<<nblocks(c.nmt, b), b, 0, c.stream>>>(c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0], c.v[0],
-                                                          c.phi[0], c.phiv[0], dt, H[0], H[1], H[2], c.slot,
-                                                          c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp, c.field_amp,
-                                                          c.spin_s);
+        (drift_on(c) ? k_tet64<1, true> : k_tet64<1, false>)<<<nblocks(c.nmt, b), b, 0, c.stream>>>(
+            c.nmt, c.tet, c.da, c.detJ, c.treg, c.regs, c.u[0], c.v[0], c.phi[0], c.phiv[0], dt, H[0], H[1], H[2],
+            c.slot, c.tet_seg, c.batch ? c.seg_par : nullptr, c.hsp, c.field_amp, c.spin_s, c.drift_dir, c.drift_v);
     return cudaGetLastError();
 }
 

@@ -199,6 +199,14 @@ int fg_get_spin(const fg_ctx *ctx, double *s);
 int fg_set_space_field(fg_ctx *ctx, const double *field);
 int fg_set_field_amplitude(fg_ctx *ctx, double amplitude);
 
+/* Recentering drift of the element integrals (Tet::add_drift_BE, src/tetra.cpp:150-169,
+ * applied at :277-288): direction 0/1/2 (x/y/z, the recentering direction; -1 none) and the
+ * drift speed in m/s (LinAlgebra::set_DW_vz, src/linear_algebra.h:97-98). With a speed other
+ * than 0, BE_i of every magnetic tet gains vdrift sum_g w_g a_i(g) (alpha dU + U x dU +
+ * s_dt (alpha dV + U x dV + V x dU)), dU and dV the derivatives of u and v along the
+ * direction. Not for batches. */
+int fg_set_drift(fg_ctx *ctx, int direction, double vdrift);
+
 /* Full-precision checkpoint of a context (no reference counterpart: the reference's .sol
  * keeps u and phi to 7 digits and loses v and phiv, src/save.cpp:164-186). The file holds the
  * CURRENT state (u, v, phi, phiv in FP64), the caller's run metadata below, and the choices

@@ -71,6 +71,7 @@ def lib():
         L.fgo_max_threads.restype = C.c_int
         L.fgo_set_solver.argtypes = [C.c_void_p, C.c_double, C.c_int]
         L.fgo_set_space_field.argtypes = [C.c_void_p, C.c_void_p, C.c_double]
+        L.fgo_set_drift.argtypes = [C.c_void_p, C.c_int, C.c_double]
         L.fgo_recenter.argtypes = [C.c_void_p, C.c_int, C.c_double]
         L.fgo_recenter.restype = C.c_int
         L.fgo_set_spin.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int),
@@ -175,6 +176,10 @@ class Oracle:
             return
         f = np.ascontiguousarray(field, dtype=np.float64)
         self.L.fgo_set_space_field(self.h, f.ctypes.data_as(C.c_void_p), float(amp))
+
+    def set_drift(self, direction, vdrift):
+        """Recentering drift of the element integrals: direction 0/1/2 (x/y/z) or -1, speed m/s."""
+        self.L.fgo_set_drift(self.h, int(direction), float(vdrift))
 
     def set_state(self, u, v=None, phi=None, phiv=None):
         u = np.ascontiguousarray(u, dtype=np.float64).ravel()

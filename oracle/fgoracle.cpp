@@ -142,6 +142,10 @@ struct Oracle {
     // of every tet [nt][npi][3] (zero for non-magnetic tets), used as Hext + amp f(g)
     std::vector<double> hsp;
     double amp = 1.0;
+    // recentering drift (LinAlgebra::idx_dir and DW_vz, src/linear_algebra.h:51-53,97-118):
+    // direction 0/1/2 or -1 (IDX_UNDEF), speed in m/s
+    int drift_dir = -1;
+    double drift_v = 0.0;
     // spin accumulation (spinAcc, electrostatSolver): potential V, spin accumulation s
     bool spin = false;
     double spin_tol = 1e-8;
@@ -318,7 +322,8 @@ void alpha_eff(double dt, double alpha, const double *uHeff, int npi, double *a_
 
 // Tet::integrales, src/tetra.cpp:210-307, with lumping :108-131, calcDiagBlock :133-140,
 // calc_aniso_uniax :171-181, calc_aniso_cub :183-208, buildMatP src/element.h:81-96.
-// Hext is the constant applied field (RtoR3 field type); Hst and the drift are zero.
+// Hext is the constant applied field plus the R4toR3 field at the Gauss points; Hst of the
+// spin accumulation; the recentering drift when a direction is set (Tet::add_drift_BE).
 void integrales(Oracle &o, int t, double dt, double prefactor, const double Hext[3]) {
     const TetRule &R = o.tr;
     const int npi = R.npi;
@@ -478,6 +483,22 @@ void integrales(Oracle &o, int t, double dt, double prefactor, const double Hext
     // BE (3x4) -> Lp
     double BE[3][4];
     std::memset(BE, 0, sizeof(BE));
+    // recentering drift (Tet::add_drift_BE, src/tetra.cpp:150-169, called at :277-288):
+    // BE_i += Vdrift w_g a_i(g) (alpha dU + U x dU + s_dt (alpha dV + U x dV + V x dU)),
+    // dU and dV the derivatives of u and v along the direction
+    if (o.drift_dir >= 0) {
+        const V3 dUdir = dUd[o.drift_dir];
+        V3 dVdir = {0, 0, 0};
+        for (int i = 0; i < 4; i++) dVdir = dVdir + da[3 * i + o.drift_dir] * vn[i];
+        for (int g = 0; g < npi; g++) {
+            const V3 D = alpha * dUdir + cross(U[g], dUdir) +
+                         s_dt * (alpha * dVdir + cross(U[g], dVdir) + cross(V[g], dUdir));
+            for (int i = 0; i < 4; i++) {
+                const double f = o.drift_v * w[g] * R.a[i][g];
+                for (int d = 0; d < 3; d++) BE[d][i] += f * comp(D, d);
+            }
+        }
+    }
     for (int g = 0; g < npi; g++) H[g] = H[g] + Han[g] + (s_dt / GAMMA0) * Hv;
     for (int g = 0; g < npi; g++) {
         const double wg = w[g];
@@ -1479,6 +1500,13 @@ void fgo_set_space_field(void *h, const double *field, double amp) {
     o->hsp.assign(3 * (size_t)o->nt * npi, 0.0);
     for (size_t k = 0; k < o->magTet.size(); k++)
         for (int q = 0; q < 3 * npi; q++) o->hsp[3 * (size_t)o->magTet[k] * npi + q] = field[3 * k * npi + q];
+}
+
+// LinAlgebra::set_DW_vz (src/linear_algebra.h:97-98) and the recentering direction
+void fgo_set_drift(void *h, int dir, double vdrift) {
+    Oracle *o = static_cast<Oracle *>(h);
+    o->drift_dir = (dir >= 0 && dir < 3) ? dir : -1;
+    o->drift_v = vdrift;
 }
 
 void fgo_set_solver(void *h, double tol, int maxiter) {

@@ -412,6 +412,45 @@ def test_recentering(z0, expect):
         assert np.array_equal(o.get_state(1)["v"], np.zeros_like(v))
 
 
+@pytest.mark.parametrize("direction,K,precision", [(0, 0.0, fg.FG_PREC_FP64), (2, 0.0, fg.FG_PREC_FP32_REFINE),
+                                                   (1, 3e4, fg.FG_PREC_FP64)])
+def test_recentering_drift(direction, K, precision):
+    """Tet::add_drift_BE (src/tetra.cpp:150-169): with a drift direction and speed the
+    element integrals gain vdrift w_g a_i(g) (alpha dU + U x dU + s_dt (alpha dV + U x dV +
+    V x dU)). The assembled RHS matches the oracle's to 1e-12 (the operator is unchanged),
+    the term is a visible part of the RHS, and a zero speed or no direction leaves the
+    step as it was."""
+    m, st, H, o, c = _setup(K=K, precision=precision)
+    angle, pref = 0.37, fgo.prefactor(DT, DTMAX)
+    vdrift = 5e-3
+    o.set_drift(direction, vdrift)
+    o.base_projection(angle)
+    o.step(DT, pref, H)
+    rowptr, col, val, rhs_o = o.export_system()
+    c.set_drift(direction, vdrift)
+    assert c.step(DT, pref, H, angle)["status"] == fg.FG_OK
+    rhs_g = c.debug_system()[0]
+    assert _rel(rhs_g, rhs_o) <= 1e-12
+    x = np.random.default_rng(3).normal(size=2 * len(m["xyz"]))
+    assert _rel(c.debug_apply(x), _csr_apply(rowptr, col, val, x)) <= 1e-12
+    # without the drift (speed 0, then no direction) the RHS differs visibly and matches the
+    # oracle's drift-free system
+    o2 = fgo.Oracle(m, cases.oracle_regions(alpha=0.5, K=K, uk=UK))
+    o2.set_solver(1e-12, 5000)
+    o2.set_state(st["u"], st["v"], st["phi"], st["phiv"])
+    o2.base_projection(angle)
+    o2.step(DT, pref, H)
+    rhs_0 = o2.export_system()[3]
+    assert _rel(rhs_0, rhs_o) > 1e-3
+    for d, vd in ((direction, 0.0), (-1, vdrift)):
+        c.set_state(st["u"], st["v"], st["phi"], st["phiv"])
+        c.set_drift(d, vd)
+        assert c.step(DT, pref, H, angle)["status"] == fg.FG_OK
+        assert _rel(c.debug_system()[0], rhs_0) <= 1e-12
+    with pytest.raises(fg.FgError):
+        c.set_drift(3, 1.0)
+
+
 @pytest.mark.parametrize("one_point", [False, True])
 def test_double_single_elements(one_point):
     """The FP32 + refinement path computes the isotropic element integrals in double-single

@@ -77,3 +77,27 @@ def test_oracle_cpu_fmm_matches_direct_sum():
     o.set_demag(3)
     f = o.demag(0)
     assert np.linalg.norm(f - d) / np.linalg.norm(d) < 1e-5
+
+
+def test_oracle_drift_term_properties():
+    """The oracle's recentering drift (Tet::add_drift_BE) is linear in the drift speed and
+    vanishes for a uniform state with v = 0 (no derivative along the direction)."""
+    from tests import cases
+    m = cases.cuboid(5, 4, 3)
+    H = np.array([1e4, 0.0, 2e4])
+
+    def rhs(u, v, direction, vdrift):
+        o = fgo.Oracle(m, cases.oracle_regions())
+        o.set_state(u, v)
+        o.set_drift(direction, vdrift)
+        o.base_projection(0.3)
+        o.step(1e-14, 1.0, H)
+        return o.export_system()[3]
+
+    u = cases.perturbed_state(m["xyz"], seed=5)
+    v = cases.tangent_field(u, seed=6)
+    r0, r1, r2 = (rhs(u, v, 1, s) for s in (0.0, 1e-3, 2e-3))
+    assert np.linalg.norm(r1 - r0) > 1e-6 * np.linalg.norm(r0)
+    assert np.linalg.norm((r2 - r0) - 2 * (r1 - r0)) <= 1e-9 * np.linalg.norm(r2 - r0)
+    uni = np.tile(np.array([0.6, 0.0, 0.8]), (len(m["xyz"]), 1))
+    assert np.array_equal(rhs(uni, None, 2, 1e-3), rhs(uni, None, -1, 0.0))
