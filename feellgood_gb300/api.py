@@ -131,6 +131,7 @@ SIGNATURES = {
     "fg_set_space_field": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fg_set_field_amplitude": (C.c_int, [C.c_void_p, C.c_double]),
     "fg_checkpoint_peek": (C.c_int, [C.c_char_p, C.c_void_p, C.c_void_p]),
+    "fg_debug_tc_resources": (C.c_int, [C.POINTER(C.c_int)]),
     "fg_debug_translate_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_int]),
     "fg_batch_create": (C.c_int, [C.POINTER(fg_mesh), C.c_int, C.POINTER(fg_region), C.c_int,

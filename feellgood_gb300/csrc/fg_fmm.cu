@@ -31,6 +31,7 @@
 #include <cstdint>
 #include <cstring>
 #include <unordered_map>
+#include <queue>
 #include <vector>
 
 #include "fg_f32x2.cuh"
@@ -1217,10 +1218,45 @@ static int fmm_build_forest(Ctx &c, int L) {
         t->tc_m2m.assign(L + 1, FmmTree::TcLaunch());
         t->tc_l2l.assign(L + 1, FmmTree::TcLaunch());
         // M2M and L2L run level by level, each level a short launch: units of 2 codes keep
-        // its critical path short; M2L has the whole tree in one launch: units of 48 codes
+        // its critical path short. M2L has the whole tree in one launch; its unit size is
+        // the one whose units, handed in launch order to the earliest free of the SMs' CTA
+        // slots (one per SM), finish first: a unit costs its codes plus about 3 codes of
+        // pipeline fill, drain and output, and a split tile adds a combine pass
+        int m2l_codes = 48;
+        {
+            std::vector<int> cs;  // codes per tile: one unit per tile
+            std::vector<int4> us, cb;
+            int ns = 0;
+            translate_tc_units(ncell, NCODE_M2L, m2l_tab.data(), 0, 1 << 30, cs, us, cb, ns);
+            double best = 1e300;
+            const int slots = std::max(1, c.nsm);
+            for (int mc : {64, 48, 32, 24, 16, 12, 8}) {
+                std::priority_queue<double, std::vector<double>, std::greater<double>> free_at;
+                for (int k = 0; k < slots; k++) free_at.push(0.0);
+                double span = 0.0;
+                bool split = false;
+                for (const int4 &u : us) {  // the split of translate_tc_units, unit by unit
+                    const int n = u.z - u.y, nu = std::max(1, (n + mc - 1) / mc);
+                    split = split || nu > 1;
+                    for (int k = 0; k < nu; k++) {
+                        const int cnt = (int)((long)n * (k + 1) / nu - (long)n * k / nu);
+                        const double t0 = free_at.top();
+                        free_at.pop();
+                        const double t1 = t0 + 3.0 + cnt;
+                        span = std::max(span, t1);
+                        free_at.push(t1);
+                    }
+                }
+                span += split ? 1.0 : 0.0;
+                if (span < best) {
+                    best = span;
+                    m2l_codes = mc;
+                }
+            }
+        }
         for (int l = L - 1; l >= 2; l--)
             t->tc_m2m[l] = plan(t->lev_begin[l + 1] - t->lev_begin[l], t->lev_begin[l], 8, m2m_tab, 2);
-        t->tc_m2l = plan(ncell, 0, NCODE_M2L, m2l_tab, 48);
+        t->tc_m2l = plan(ncell, 0, NCODE_M2L, m2l_tab, m2l_codes);
         for (int l = 3; l <= L; l++)
             t->tc_l2l[l] = plan(t->lev_begin[l + 1] - t->lev_begin[l], t->lev_begin[l], 8, l2l_tab, 2);
         FCK(up(&t->tc_code, codes));
@@ -1394,6 +1430,7 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq) {
     // out (+)= sum_code Op[code] in[tab[cell][code]] over n output cells from out0; the
     // tensor-core form reads the inputs' hi/lo split and writes the outputs' split
     enum { M2M, M2L, L2L };
+    cudaError_t terr = cudaSuccess;  // first failed translation launch
     auto translate = [&](int kind, int n, int out0, const FmmTree::TcLaunch &tl) {
         if (!n) return;
         const int ncode = kind == M2L ? NCODE_M2L : 8;
@@ -1412,7 +1449,8 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq) {
             a.units = t.tc_units + tl.unit0; a.nunits = tl.nunit;
             a.comb = t.tc_comb + tl.comb0; a.ncomb = tl.ncomb; a.scratch = t.tc_scratch;
             a.nset = nq; a.set_io = sstride; a.set_scratch = t.nslot_floats;
-            launch_translate_tc(c.stream, a);
+            const cudaError_t e = launch_translate_tc(c.stream, a);
+            if (e != cudaSuccess && terr == cudaSuccess) terr = e;
         } else {
             const void *ops = kind == M2M ? t.op_m2m : kind == M2L ? t.op_m2l : t.op_l2l;
             for (int q = 0; q < nq; q++) {
@@ -1458,7 +1496,8 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq) {
         t.ev_pending[t.ev_next] = true;
         t.ev_next ^= 1;
     }
-    return cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
+    return terr != cudaSuccess ? terr : e;
 }
 
 cudaError_t fmm_eval(Ctx &c, int nq) {

@@ -3,10 +3,12 @@
 // Every translation of the FMM (M2L for each cell offset, M2M and L2L for each child
 // octant) applies a fixed real 100x100 operator to 100-coefficient expansions. For a tile
 // of 64 output cells the work of one operator code is one GEMM
-//     D[128 x 64] += Op_code[128 x 104] * X_code[104 x 64],
-// rows = output coefficients (100 used), columns = the 64 cells, X_code = the input
-// expansions that this code brings to each of the 64 cells (zero where there is none),
-// K = input coefficients padded to 104. D lives in tensor memory (TMEM, 64 columns of
+//     D[128 x 64 ns] += Op_code[128 x 104] * X_code[104 x 64 ns],
+// rows = output coefficients (100 used), columns = the 64 cells of each of the ns sets of
+// expansions evaluated together (the FMM evaluates the charges of m and of v at once: set s
+// takes columns 64 s .. 64 s + 63, so the operator image is read once for both), X_code =
+// the input expansions that this code brings to each cell (zero where there is none),
+// K = input coefficients padded to 104. D lives in tensor memory (TMEM, 64 ns columns of
 // FP32) and accumulates over all the codes of the tile, so each output is written once.
 //
 // Precision: the FP32 expansions are split as x = hi + lo with hi = tf32(x) (round to
@@ -14,12 +16,12 @@
 // accumulation) keeps about 21 bits of every product, the accuracy of the FP32 CUDA-core
 // translation.
 //
-// Pipeline (one CTA of 9 warps per tile, two CTAs per SM, 4 shared-memory stages of K = 16):
+// Pipeline (one CTA of 9 warps per tile, one CTA per SM, 6 shared-memory stages of K = 16):
 //   warps 0-3  fill one stage per item: thread 0 starts two bulk copies
 //              (cp.async.bulk, completion counted in bytes on full[s]) of the operator
 //              item, stored pre-split (hi, lo) in global memory in exactly the shared-memory
 //              image the MMA reads (no-swizzle K-major core matrices, 8 rows x 16 bytes);
-//              all 128 threads gather the 64 input expansions' item with 16-byte cp.async
+//              all 128 threads gather the 64 ns input expansions' item with 16-byte cp.async
 //              from pre-split hi/lo arrays into the same layout (zero fill where a cell has
 //              no input). A thread arrives on full[s] once its copies for that item have
 //              landed, three items later, so four items per CTA are in flight;
@@ -47,18 +49,20 @@ namespace fg {
 namespace {
 
 constexpr int NRC = 100;  // reals per expansion (P = 9)
-constexpr int NC = 64;    // output cells per CTA = MMA N
+constexpr int NC = 64;    // output cells per CTA
+constexpr int NSET = 2;   // sets of expansions per CTA at most (MMA N = 64 sets)
+constexpr int NB = NC * NSET;
 constexpr int MR = 128;   // MMA M
 constexpr int KI = 16;    // K per pipeline item (2 MMA K-steps of 8)
 constexpr int IPC = 7;    // items per code: K = 104 = 6 x 16 + 8
 constexpr int KQ = KI / 4;                              // 16-byte quads of K per row and item
-constexpr int NSTAGE = 4;                               // 96 KB of stages: two CTAs per SM
+constexpr int NSTAGE = 6;                               // 192 KB of stages: one CTA per SM
 constexpr uint32_t LBO = 128;                           // next core matrix along K
 constexpr uint32_t SBO = KQ * 128;                      // next group of 8 rows (512 B)
 constexpr int A_BYTES = 16 * SBO;                       // 8 KB per part (hi or lo), rows 0..127
-constexpr int B_BYTES = (NC / 8) * SBO;                 // 4 KB per part
-constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // 24 KB
-constexpr int TMEM_COLS = 256;  // 2 buffers x (main, corr) x 64 columns
+constexpr int B_BYTES = (NB / 8) * SBO;                 // 8 KB per part
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // 32 KB
+constexpr int TMEM_COLS = 512;  // 2 buffers x (main, corr) x 128 columns: all of an SM's TMEM
 constexpr int IMG_BYTES = 13 * SBO;  // one operator image part: rows 0..103 (13 groups of 8)
 constexpr int LAG = NSTAGE - 1;      // items whose gathers may still be in flight
 
@@ -184,20 +188,26 @@ __device__ __forceinline__ void store_split(unsigned char *hi, unsigned char *lo
     *reinterpret_cast<float4 *>(lo + off) = make_float4(v.x - h0, v.y - h1, v.z - h2, v.w - h3);
 }
 
-// Gather of one item (K = 16) of the 64 input expansions, hi and lo parts, with 16-byte
-// async copies into the core-matrix layout: thread t copies quads 2(t&1), 2(t&1)+1 of cell
-// t>>1 (zero fill beyond coefficient 99 or where the cell has no input, sc < 0).
+// Gather of one item (K = 16) of the 64 input expansions of each set, hi and lo parts, with
+// 16-byte async copies into the core-matrix layout: thread t copies quads 2(t&1), 2(t&1)+1
+// of cell t>>1 of every set (column t>>1 + 64 set; zero fill beyond coefficient 99 or where
+// the cell has no input, sc < 0). The sets share the tables: one source cell for all.
 __device__ __forceinline__ void gather_item(unsigned char *bs, int tid, int k0, int sc, const float *in_hi,
-                                            const float *in_lo) {
+                                            const float *in_lo, int ns, size_t set_io) {
     const int n = tid >> 1;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int kq = 2 * (tid & 1) + h, j = k0 + 4 * kq;
-        const bool ok = sc >= 0 && j < NRC;
-        const size_t o = ok ? (size_t)sc * NRC + j : 0;
-        unsigned char *d = bs + (n >> 3) * SBO + kq * 128 + (n & 7) * 16;
-        cp16(d, in_hi + o, ok ? 16u : 0u);
-        cp16(d + B_BYTES, in_lo + o, ok ? 16u : 0u);
+    for (int y = 0; y < NSET; y++) {
+        if (y >= ns) break;
+        const int col = n + NC * y;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int kq = 2 * (tid & 1) + h, j = k0 + 4 * kq;
+            const bool ok = sc >= 0 && j < NRC;
+            const size_t o = ok ? y * set_io + (size_t)sc * NRC + j : 0;
+            unsigned char *d = bs + (col >> 3) * SBO + kq * 128 + (col & 7) * 16;
+            cp16(d, in_hi + o, ok ? 16u : 0u);
+            cp16(d + B_BYTES, in_lo + o, ok ? 16u : 0u);
+        }
     }
 }
 
@@ -205,11 +215,13 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
     const int n_out = a.n_out, out0 = a.out0, ncode = a.ncode, accumulate = a.accumulate, terms = a.terms;
     const int *__restrict__ tab = a.tab;
     const int *__restrict__ tile_code = a.tile_code;
-    // set of expansions (grid y): the same tables and operators on another set of inputs
-    const size_t io = blockIdx.y * a.set_io;
-    float *out = a.out + io, *out_hi = a.out_hi + io, *out_lo = a.out_lo + io;
-    const float *in_hi = a.in_hi + io, *in_lo = a.in_lo + io;
-    float *scratch = a.scratch + blockIdx.y * a.set_scratch;
+    // ns sets of expansions: the same tables and operators on ns sets of inputs and outputs,
+    // set_io floats apart (set_scratch in the scratch array)
+    const int ns = a.nset > 1 ? NSET : 1;
+    const size_t set_io = a.set_io;
+    float *out = a.out, *out_hi = a.out_hi, *out_lo = a.out_lo;
+    const float *in_hi = a.in_hi, *in_lo = a.in_lo;
+    float *scratch = a.scratch;
     int *err = a.err;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -223,10 +235,11 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
     const int ncodes = q1 - q0, nitems = ncodes * IPC;
     if (nitems == 0) {  // no input reaches these cells: a stored result is zero
         if (!accumulate)
-            for (int e = tid; e < NC * NRC; e += blockDim.x) {
-                const int cell = c_begin + e / NRC;
+            for (int e = tid; e < ns * NC * NRC; e += blockDim.x) {
+                const int y = e / (NC * NRC), r = e % (NC * NRC);
+                const int cell = c_begin + r / NRC;
                 if (cell < n_out) {
-                    const size_t o = (size_t)(out0 + cell) * NRC + e % NRC;
+                    const size_t o = y * set_io + (size_t)(out0 + cell) * NRC + r % NRC;
                     out[o] = 0.f;
                     out_hi[o] = 0.f;
                     out_lo[o] = 0.f;
@@ -290,7 +303,7 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
                         bulk_g2s(st, img, IMG_BYTES, &full[s]);
                         bulk_g2s(st + A_BYTES, img + IMG_BYTES, IMG_BYTES, &full[s]);
                     }
-                    gather_item(st + 2 * A_BYTES, tid, KI * q, sc, in_hi, in_lo);
+                    gather_item(st + 2 * A_BYTES, tid, KI * q, sc, in_hi, in_lo, ns, set_io);
                 }
             }
             cp_commit();
@@ -308,13 +321,13 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
             // accumulation truncates, so its error grows with the number of MMAs summed in
             // place; 13 K-steps per accumulator keep it at FP32 rounding level, and the drain
             // warps add the per-code results with round-to-nearest.
-            const uint32_t idesc = idesc_tf32(MR, NC);
+            const uint32_t idesc = idesc_tf32(MR, NC * ns);
             bool ok = true;
             for (int ci = 0; ci < ncodes && ok; ci++) {
                 const int b = ci & 1;
                 if (ci >= 2 && !mbar_wait(&tfree[b], ((ci >> 1) - 1) & 1, err, &bail)) break;
                 tc_fence_after();
-                const uint32_t dmain = tmem + b * 2 * NC, dcorr = dmain + NC;
+                const uint32_t dmain = tmem + b * 2 * NB, dcorr = dmain + NB;
                 for (int q = 0; q < IPC; q++) {
                     const int it = ci * IPC + q, s = it % NSTAGE;
                     if (!mbar_wait(&full[s], (it / NSTAGE) & 1, err, &bail)) { ok = false; break; }
@@ -340,18 +353,19 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
         const int quarter = warp & 3;
         const int row = 32 * quarter + lane;
         const uint32_t lane_off = (uint32_t)(32 * quarter) << 16;
-        float acc[NC];
+        float acc[NB];
 #pragma unroll
-        for (int j = 0; j < NC; j++) acc[j] = 0.f;
+        for (int j = 0; j < NB; j++) acc[j] = 0.f;
         int drained = 0;
         for (int ci = 0; ci < ncodes; ci++) {
             const int b = ci & 1;
             const bool mine = mbar_wait(&tfull[b], (ci >> 1) & 1, err, &bail);
             if (!__all_sync(0xffffffffu, mine && !bail)) break;
             tc_fence_after();
-            const uint32_t dmain = tmem + lane_off + b * 2 * NC, dcorr = dmain + NC;
+            const uint32_t dmain = tmem + lane_off + b * 2 * NB, dcorr = dmain + NB;
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
+            for (int j = 0; j < NB / 16; j++) {
+                if (j >= ns * (NC / 16)) break;
                 uint32_t rm[16], rc[16];
                 tmem_ld16(dmain + 16 * j, rm);
                 tmem_ld16(dcorr + 16 * j, rc);
@@ -368,21 +382,25 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
             drained++;
         }
         if (drained == ncodes && row < NRC) {
-            if (slot >= 0) {  // one of several units of this tile: partial result
-                float *p = scratch + (size_t)slot * NC * NRC + row;
 #pragma unroll
-                for (int j = 0; j < NC; j++) p[j * NRC] = acc[j];
-            } else {
+            for (int y = 0; y < NSET; y++) {
+                if (y >= ns) break;
+                if (slot >= 0) {  // one of several units of this tile: partial result
+                    float *p = scratch + y * a.set_scratch + (size_t)slot * NC * NRC + row;
 #pragma unroll
-                for (int j = 0; j < NC; j++) {
-                    const int cell = c_begin + j;
-                    if (cell < n_out) {
-                        const size_t o = (size_t)(out0 + cell) * NRC + row;
-                        const float v = accumulate ? out[o] + acc[j] : acc[j];
-                        out[o] = v;
-                        const float h = tf32_rn(v);
-                        out_hi[o] = h;
-                        out_lo[o] = v - h;
+                    for (int j = 0; j < NC; j++) p[j * NRC] = acc[NC * y + j];
+                } else {
+#pragma unroll
+                    for (int j = 0; j < NC; j++) {
+                        const int cell = c_begin + j;
+                        if (cell < n_out) {
+                            const size_t o = y * set_io + (size_t)(out0 + cell) * NRC + row;
+                            const float v = accumulate ? out[o] + acc[NC * y + j] : acc[NC * y + j];
+                            out[o] = v;
+                            const float h = tf32_rn(v);
+                            out_hi[o] = h;
+                            out_lo[o] = v - h;
+                        }
                     }
                 }
             }
@@ -398,7 +416,7 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
 
 // One entry per translation kind, so that profiles tell them apart.
 #define FG_TC_KERNEL(name) \
-    __global__ void __launch_bounds__(288, 2) name(TcArgs a) { translate_tc_body(a); }
+    __global__ void __launch_bounds__(288, 1) name(TcArgs a) { translate_tc_body(a); }
 FG_TC_KERNEL(k_m2m_tc)
 FG_TC_KERNEL(k_m2l_tc)
 FG_TC_KERNEL(k_l2l_tc)
@@ -460,8 +478,9 @@ cudaError_t translate_tc_setup() {
 cudaError_t launch_translate_tc(cudaStream_t st, const TcArgs &a) {
     if (a.n_out <= 0 || a.nunits <= 0) return cudaSuccess;
     auto k = a.accumulate ? k_l2l_tc : (a.ncode == 8 ? k_m2m_tc : k_m2l_tc);
+    if (a.nset > NSET) return cudaErrorInvalidValue;
     const unsigned nset = a.nset > 1 ? (unsigned)a.nset : 1u;
-    k<<<dim3(a.nunits, nset), 288, translate_tc_smem(), st>>>(a);
+    k<<<a.nunits, 288, translate_tc_smem(), st>>>(a);  // every CTA takes all sets of its tile
     if (a.ncomb > 0) k_tc_combine<<<dim3(a.ncomb, nset), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
@@ -519,6 +538,27 @@ std::vector<float> translate_tc_images(const std::vector<double> &ops, int ncode
 }
 
 }  // namespace fg
+
+extern "C" int fg_debug_tc_resources(int attrs[8]) {
+    using namespace fg;
+    if (!attrs) return FG_EINVAL;
+    if (translate_tc_setup() != cudaSuccess) return FG_ECUDA;
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, k_m2l_tc) != cudaSuccess) return FG_ECUDA;
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_m2l_tc, 288, translate_tc_smem()) != cudaSuccess)
+        blocks = -1;
+    attrs[0] = fa.numRegs;
+    attrs[1] = fa.maxThreadsPerBlock;
+    attrs[2] = (int)fa.sharedSizeBytes;
+    attrs[3] = fa.maxDynamicSharedSizeBytes;
+    attrs[4] = (int)fa.localSizeBytes;
+    attrs[5] = translate_tc_smem();
+    attrs[6] = 288;
+    attrs[7] = blocks;
+    cudaGetLastError();
+    return FG_OK;
+}
 
 // Diagnostic entry: one tensor-core translation launch on caller data (host arrays),
 // out[c] = sum_code ops[code] in[tab[c][code]] for n_out cells, with the chosen product

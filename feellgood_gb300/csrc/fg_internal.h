@@ -318,7 +318,7 @@ struct TcArgs {
     int ncomb;
     int *err;                       // FG_ETIMEDOUT after an expired wait
     int terms;                      // product terms of the split (7 in production)
-    int nset;                       // independent sets of expansions (grid y; 0 or 1: one set)
+    int nset;                       // sets of expansions (at most 2, columns of one MMA; 0 or 1: one)
     size_t set_io, set_scratch;     // floats between sets in in/out arrays and in scratch
 };
 cudaError_t launch_translate_tc(cudaStream_t st, const TcArgs &a);

@@ -335,6 +335,13 @@ int fg_batch_run_info(const fg_ctx *ctx, int *graph_used, double *device_ms);
 int fg_debug_translate_tc(int n_in, int n_out, int ncode, const float *ops, const int *tab, const float *in,
                           float *out, int terms);
 
+/* Launch resources of the tensor-core translation kernel as the CUDA runtime sees them:
+ * attrs[0] registers per thread, [1] max threads per block, [2] static shared bytes,
+ * [3] max dynamic shared bytes (attribute), [4] local bytes per thread, [5] dynamic shared
+ * bytes a launch asks for, [6] threads per block of a launch, [7] resident blocks per SM
+ * for that launch (0: it cannot launch). */
+int fg_debug_tc_resources(int attrs[8]);
+
 /* Device ms of the FMM stages when opts.profile is set, averaged over the evaluations
  * since the previous call (CUDA events around each stage, recorded without any extra
  * synchronisation): [0] P2M, [1] M2M, [2] M2L, [3] L2L, [4] L2P + P2P. */

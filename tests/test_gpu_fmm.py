@@ -130,3 +130,18 @@ def test_pair_evaluation_matches_single(precision, native, shape, leaf):
         single = c.demag(which)
         scale = np.abs(single).max()
         assert np.abs(got - single).max() <= 1e-13 * scale, (which, np.abs(got - single).max() / scale)
+
+
+def test_tc_translation_launch_resources():
+    """The tensor-core translation kernel fits its own launch: the runtime's register and
+    shared-memory view admits at least one resident block of 288 threads with the dynamic
+    shared memory a launch asks for (a launch that does not fit fails with 'too many
+    resources requested for launch')."""
+    import ctypes as C
+    L = fg.fg_lib()
+    a = (C.c_int * 8)()
+    assert L.fg_debug_tc_resources(a) == fg.FG_OK
+    regs, max_threads, static_smem, max_dyn, local, dyn_req, threads, blocks = list(a)
+    assert threads <= max_threads
+    assert dyn_req <= max_dyn
+    assert blocks >= 1, list(a)
