@@ -1,7 +1,7 @@
 // FP64 CPU oracle for the per-time-step LLG path of FeeLLGood.
 //
-// TEST INFRASTRUCTURE ONLY. This library is the checker for the GPU path: only the
-// tests, the smoke check and the CPU-baseline leg of bench.py may load it. The
+// TEST INFRASTRUCTURE ONLY. This library is the reference against which the GPU path is
+// tested: only the tests, the smoke check and the CPU-baseline leg of bench.py may load it. The
 // product library never links, loads or calls it.
 //
 // It restates, step by step and in plain C++17 + OpenMP (no Eigen), the reference

@@ -1,6 +1,6 @@
 """Mesh reading and set-up, restated in numpy. TEST INFRASTRUCTURE ONLY.
 
-This module is part of the oracle (the CPU checker). Only tests, the smoke check and
+This module is part of the oracle (the CPU restatement). Only tests, the smoke check and
 bench.py's CPU-baseline leg may import it; the product never does.
 
 It restates what FeeLLGood does between opening a gmsh file and the first time step
