@@ -428,17 +428,27 @@ __global__ void __launch_bounds__(256) k_tc_combine(TcArgs a) {
     const size_t io = blockIdx.y * a.set_io;
     const float *scratch = a.scratch + blockIdx.y * a.set_scratch;
     float *out = a.out + io, *out_hi = a.out_hi + io, *out_lo = a.out_lo + io;
-    for (int e = threadIdx.x; e < NC * NRC; e += blockDim.x) {
+    // four coefficients per thread and step: 100 per cell keeps every float4 inside one cell,
+    // and every base (slot, set, output cell) is a multiple of 4 floats
+    static_assert(NRC % 4 == 0, "float4 steps stay inside a cell");
+    for (int e4 = threadIdx.x; e4 < NC * NRC / 4; e4 += blockDim.x) {
+        const int e = 4 * e4;
         const int cell = ct.x * NC + e / NRC;
         if (cell >= a.n_out) continue;
-        float v = 0.f;
-        for (int u = 0; u < ct.z; u++) v += scratch[(size_t)(ct.y + u) * NC * NRC + e];
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int u = 0; u < ct.z; u++) {
+            const float4 w = __ldg(reinterpret_cast<const float4 *>(scratch + (size_t)(ct.y + u) * NC * NRC + e));
+            v.x += w.x; v.y += w.y; v.z += w.z; v.w += w.w;
+        }
         const size_t o = (size_t)(a.out0 + cell) * NRC + e % NRC;
-        if (a.accumulate) v += out[o];
-        out[o] = v;
-        const float h = tf32_rn(v);
-        out_hi[o] = h;
-        out_lo[o] = v - h;
+        if (a.accumulate) {
+            const float4 b = *reinterpret_cast<const float4 *>(out + o);
+            v.x += b.x; v.y += b.y; v.z += b.z; v.w += b.w;
+        }
+        *reinterpret_cast<float4 *>(out + o) = v;
+        const float4 h = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
+        *reinterpret_cast<float4 *>(out_hi + o) = h;
+        *reinterpret_cast<float4 *>(out_lo + o) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
     }
 }
 
