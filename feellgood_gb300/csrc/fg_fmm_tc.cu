@@ -181,13 +181,6 @@ __device__ __forceinline__ float tf32_rn(float x) {
     return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
-// hi/lo split of 4 consecutive K values, stored at the same offset of the hi and lo images.
-__device__ __forceinline__ void store_split(unsigned char *hi, unsigned char *lo, int off, float4 v) {
-    const float h0 = tf32_rn(v.x), h1 = tf32_rn(v.y), h2 = tf32_rn(v.z), h3 = tf32_rn(v.w);
-    *reinterpret_cast<float4 *>(hi + off) = make_float4(h0, h1, h2, h3);
-    *reinterpret_cast<float4 *>(lo + off) = make_float4(v.x - h0, v.y - h1, v.z - h2, v.w - h3);
-}
-
 // Gather of one item (K = 16) of the 64 input expansions of each set, hi and lo parts, with
 // 16-byte async copies into the core-matrix layout: thread t copies quads 2(t&1), 2(t&1)+1
 // of cell t>>1 of every set (column t>>1 + 64 set; zero fill beyond coefficient 99 or where
