@@ -61,7 +61,7 @@ class fg_opts(C.Structure):
                 ("mlp_lr", C.c_double), ("fmm_tensor", C.c_int),
                 ("mlp_train_every", C.c_int), ("fmm_native_fp64", C.c_int),
                 ("solver_lpr", C.c_int), ("solver_blocks", C.c_int), ("spin_acc", C.c_int), ("spin_tol", C.c_double),
-                ("spin_max_iter", C.c_int)]
+                ("spin_max_iter", C.c_int), ("demag_increment", C.c_int)]
 
 
 class fg_step_report(C.Structure):
@@ -132,6 +132,7 @@ SIGNATURES = {
     "fg_set_field_amplitude": (C.c_int, [C.c_void_p, C.c_double]),
     "fg_checkpoint_peek": (C.c_int, [C.c_char_p, C.c_void_p, C.c_void_p]),
     "fg_debug_tc_resources": (C.c_int, [C.POINTER(C.c_int)]),
+    "fg_measure_peaks": (C.c_int, [_dp]),
     "fg_debug_translate_tc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_int]),
     "fg_batch_create": (C.c_int, [C.POINTER(fg_mesh), C.c_int, C.POINTER(fg_region), C.c_int,
@@ -599,6 +600,18 @@ class Context:
         ms = np.zeros(5)
         self._check(self.L.fg_timings(self.h, _dptr(ms)))
         return ms
+
+
+def measure_peaks():
+    """fg_measure_peaks: per-SM, per-clock throughputs of the FP32 FMA (scalar and f32x2), the
+    SFU reciprocal square root and tcgen05 kind::tf32 (N = 128 and 256), and the SM clock."""
+    out = np.zeros(6)
+    s = fg_lib().fg_measure_peaks(_dptr(out))
+    if s != FG_OK:
+        raise FgError(s, "fg_measure_peaks")
+    keys = ["ffma_per_clk_sm", "ffma2_per_clk_sm", "rsqrt_per_clk_sm", "tf32_n128_flops_per_clk_sm",
+            "tf32_n256_flops_per_clk_sm", "sm_mhz"]
+    return dict(zip(keys, (float(x) for x in out)))
 
 
 def debug_translate_tc(ops, tab, x, terms=7):

@@ -126,7 +126,7 @@ void fg_opts_default(fg_opts *o) {
     o->one_gauss_point = 0;
     o->first_order = 0;
     o->refine_max = 20;
-    o->inner_tol = 1e-3;
+    o->inner_tol = 1e-5;
     o->verbose = 0;
     o->mlp_train_steps = 20;
     o->mlp_batch = 16384;
@@ -135,6 +135,7 @@ void fg_opts_default(fg_opts *o) {
     o->mlp_train_every = 1;
     o->spin_tol = 1e-8;        // spinAcc and electrostatSolver tolerance (src/main.cpp:252)
     o->spin_max_iter = 1000;
+    o->demag_increment = 1;
 }
 
 const char *fg_strerror(int s) {
@@ -534,6 +535,9 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
         int s = fmm_build(c);
         if (s != FG_OK) return s;
     }
+    c.dinc = demag == FG_DEMAG_FMM && c.opts.precision == FG_PREC_FP32_REFINE && c.opts.demag_increment != 0 &&
+            !c.batch;
+    if (c.dinc) CK(dalloc(&c.dstate, 6 * (size_t)c.nn));
     CK(cudaDeviceSynchronize());
     return FG_OK;
 }
@@ -646,9 +650,11 @@ void fg_destroy(fg_ctx *h) {
                     c.Sval32, c.A, c.A32, c.tri, c.tri_c, c.tinc_ptr, c.tinc, c.src_xyz, c.mag_nodes, c.u[0], c.u[1],
                     c.v[0], c.v[1], c.phi[0], c.phi[1], c.phiv[0], c.phiv[1], c.ep, c.eq, c.ep32, c.eq32, c.Dl32,
                     c.slot, c.Dl, c.rhs, c.x, c.bv, c.W, c.fv, c.partial, c.bar, c.dres, c.src_q, c.tri_slot,
-                    c.pot, c.epart, c.src_dst, c.src_q2, c.tri_slot2, c.pot2, c.tri_be, c.hsp, c.da_ds, c.J_ds, c.state_ds};
+                    c.pot, c.epart, c.src_dst, c.src_q2, c.tri_slot2, c.pot2, c.tri_be, c.hsp, c.da_ds, c.J_ds, c.state_ds,
+                    c.dstate};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    fmm64_free(c);
     fmm_free(c);
     mlp_free(c);
     spin_free(c);
@@ -681,6 +687,9 @@ int fg_set_state(fg_ctx *h, const double *u, const double *v, const double *phi,
     CK(cudaMemcpyAsync(c.phi[1], c.phi[0], n1, cudaMemcpyDeviceToDevice, c.stream));
     CK(cudaMemcpyAsync(c.phiv[1], c.phiv[0], n1, cudaMemcpyDeviceToDevice, c.stream));
     CK(cudaStreamSynchronize(c.stream));
+    // given potentials are those of the given fields (v = 0 has phiv = 0)
+    c.dinc_valid[0] = phi != nullptr;
+    c.dinc_valid[1] = phiv != nullptr || v == nullptr;
     return FG_OK;
 }
 
@@ -833,11 +842,40 @@ static int demag_pair(fg_ctx *h) {
     return FG_OK;
 }
 
+// Incremental demag (fg_opts.demag_increment): the potentials are linear in the field, so
+// NEXT's = CURRENT's + those of d = NEXT - CURRENT; the FP32 FMM evaluates d only and the sum
+// is formed in FP64, so the FP32 rounding scales with the step's change, not with the
+// potential. Where CURRENT's potentials are not valid the FP64 FMM evaluates NEXT in full.
+static int demag_increment(fg_ctx *h) {
+    Ctx &c = h->c;
+    const int nq = c.opts.first_order ? 1 : 2;
+    const bool valid = c.dinc_valid[0] && (nq == 1 || c.dinc_valid[1]) && c.opts.demag_increment != 2;
+    if (valid) {
+        CK(launch_state_diff(c));
+        const double *du = c.dstate, *dv = c.dstate + 3 * (size_t)c.nn;
+        if (nq == 2) CK(launch_charges_pair(c, du, dv));
+        else CK(launch_charges(c, du));
+        CK(fmm_eval(c, nq));
+        CK(launch_phi_final(c, c.phi[1], 0, c.phi[0]));
+        if (nq == 2) CK(launch_phi_final(c, c.phiv[1], 1, c.phiv[0]));
+        c.launches += 2 + nq + fmm_launches_per_eval(c, nq);
+        return FG_OK;
+    }
+    if (nq == 2) CK(launch_charges_pair(c, c.u[1], c.v[1]));
+    else CK(launch_charges(c, c.u[1]));
+    const int s = fmm_eval_fp64(c, nq);
+    if (s != FG_OK) return s;
+    CK(launch_phi_final(c, c.phi[1], 0));
+    if (nq == 2) CK(launch_phi_final(c, c.phiv[1], 1));
+    c.launches += 1 + nq;
+    return FG_OK;
+}
+
 int fg_compute_all(fg_ctx *h, const double Hext[3], double energies[4]) {
     if (!h || !Hext) return FG_EINVAL;
     Ctx &c = h->c;
     CK(cudaEventRecord(c.ev[3], c.stream));
-    int s = c.opts.first_order ? demag_into(h, c.u[1], c.phi[1]) : demag_pair(h);
+    int s = c.dinc ? demag_increment(h) : c.opts.first_order ? demag_into(h, c.u[1], c.phi[1]) : demag_pair(h);
     if (s) return s;
     if (c.spin) {  // spinAcc::compute after the demag (src/fem.h:203-224)
         CK(cudaEventRecord(c.ev[6], c.stream));
@@ -875,6 +913,7 @@ int fg_compute_all(fg_ctx *h, const double Hext[3], double energies[4]) {
     c.ms[4] = c.ms[2] + c.ms[3];
     if (c.step_open) cudaEventElapsedTime(&c.ms[4], c.ev[0], c.ev[5]);
     c.step_open = false;
+    c.dinc_valid[0] = c.dinc_valid[1] = true;  // CURRENT now holds NEXT and its potentials
     return FG_OK;
 }
 
@@ -1002,7 +1041,9 @@ int fg_recenter(fg_ctx *h, int direction, double threshold, int *shifted) {
     double avg[3];
     int s = fg_average(h, 0, avg);
     if (s != FG_OK) return s;
-    return recenter_apply(c, direction, threshold, avg[direction], shifted);
+    const int st = recenter_apply(c, direction, threshold, avg[direction], shifted);
+    if (st == FG_OK && *shifted) c.dinc_valid[0] = c.dinc_valid[1] = false;  // the potentials belong to the old field
+    return st;
 }
 
 int fg_spin_info(const fg_ctx *h, int *status, int *iters, double *V, int *v_iters, double *ms) {

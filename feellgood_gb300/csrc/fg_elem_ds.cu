@@ -191,15 +191,17 @@ int elem_ds_setup(Ctx &c, const std::vector<double> &da, const std::vector<doubl
     return FG_OK;
 }
 
-void launch_state_ds(Ctx &c, const double *u, const double *phi, const double *phiv) {
+cudaError_t launch_state_ds(Ctx &c, const double *u, const double *phi, const double *phiv) {
     float2 *uds = c.state_ds, *phids = uds + 3 * (size_t)c.nn, *phivds = phids + c.nn;
     k_state_ds<<<(c.nn + 255) / 256, 256, 0, c.stream>>>(c.nn, u, phi, phiv, uds, phids, phivds);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_tet_ds(Ctx &c, double dt, const double H[3]) {
     if (c.nmt == 0) return cudaSuccess;
     float2 *uds = c.state_ds, *phids = uds + 3 * (size_t)c.nn, *phivds = phids + c.nn;
-    k_state_ds<<<(c.nn + 255) / 256, 256, 0, c.stream>>>(c.nn, c.u[0], c.phi[0], c.phiv[0], uds, phids, phivds);
+    cudaError_t e = launch_state_ds(c, c.u[0], c.phi[0], c.phiv[0]);
+    if (e != cudaSuccess) return e;
     const float2 hx = split(H[0]), hy = split(H[1]), hz = split(H[2]);
     const float2 rdt = split(FG_GAMMA0 * dt), kv = split(FG_THETA * dt);
     float4 *slot = reinterpret_cast<float4 *>(c.slot);

@@ -939,7 +939,9 @@ static std::vector<SamplePts> split_samples(const Ctx &c) {
                 hi[d] = std::max(hi[d], c.h_xyz[3 * (size_t)i + d]);
             }
         if (P.src.empty() && P.tgt.empty()) continue;
-        P.side = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2])) * (1.0 + 1e-9);
+        // the root cube of the reference: the points scaled by 2 / max(l) about the centre
+        // into a box of width 2.01 (src/fmm_demag.h:52-53, 72), i.e. 1.005 max(l)
+        P.side = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2])) * (2.01 / 2.0);
         if (!(P.side > 0)) P.side = 1.0;
         for (int d = 0; d < 3; d++) P.c0[d] = 0.5 * (lo[d] + hi[d]);
     }
@@ -1504,6 +1506,43 @@ cudaError_t fmm_eval(Ctx &c, int nq) {
     FmmTree *t = static_cast<FmmTree *>(c.fmm);
     if (!t) return cudaErrorNotSupported;
     return t->fp32 ? fmm_eval_t<float>(c, *t, nq) : fmm_eval_t<double>(c, *t, nq);
+}
+
+int fmm_eval_fp64(Ctx &c, int nq) {
+    FmmTree *t32 = static_cast<FmmTree *>(c.fmm);
+    if (!t32) {
+        c.err = "fmm: no tree";
+        return FG_EINVAL;
+    }
+    if (!t32->fp32) {
+        FCK(fmm_eval_t<double>(c, *t32, nq));
+        return FG_OK;
+    }
+    if (!c.fmm64) {
+        // the same depth (and so the same source order, src_dst) as the FP32 tree
+        FmmTree *t = new FmmTree();
+        t->fp32 = false;
+        c.fmm = t;
+        const int s = fmm_build_forest(c, t32->L);
+        if (s != FG_OK) {
+            fmm_free(c);
+            c.fmm = t32;
+            return s;
+        }
+        c.fmm64 = t;
+        c.fmm = t32;
+    }
+    FCK(fmm_eval_t<double>(c, *static_cast<FmmTree *>(c.fmm64), nq));
+    return FG_OK;
+}
+
+void fmm64_free(Ctx &c) {
+    if (!c.fmm64) return;
+    void *keep = c.fmm;
+    c.fmm = c.fmm64;
+    fmm_free(c);
+    c.fmm = keep;
+    c.fmm64 = nullptr;
 }
 
 int fmm_stage_ms(const Ctx &c, double ms[5]) {

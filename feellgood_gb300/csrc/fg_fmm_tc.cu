@@ -18,14 +18,14 @@
 //
 // Pipeline (one CTA of 9 warps per tile, one CTA per SM, 6 shared-memory stages of K = 16):
 //   warps 0-3  fill one stage per item: thread 0 starts two bulk copies
-//              (cp.async.bulk, completion counted in bytes on full[s]) of the operator
+//              (cp.async.bulk, completion counted in bytes on bfull[s]) of the operator
 //              item, stored pre-split (hi, lo) in global memory in exactly the shared-memory
 //              image the MMA reads (no-swizzle K-major core matrices, 8 rows x 16 bytes);
 //              all 128 threads gather the 64 ns input expansions' item with 16-byte cp.async
 //              from pre-split hi/lo arrays into the same layout (zero fill where a cell has
 //              no input). A thread arrives on full[s] once its copies for that item have
 //              landed, three items later, so four items per CTA are in flight;
-//   warp 4     one lane waits full[s], issues the MMAs of each K-step of 8 and
+//   warp 4     one lane waits full[s] and bfull[s], issues the MMAs of each K-step of 8 and
 //              tcgen05.commit arrives on empty[s] when they have read the stage; each code
 //              accumulates into its own TMEM buffer (two, used in turn), committed to tfull;
 //   warps 5-8  drain a finished code buffer with tcgen05.ld (warp w owns TMEM lanes
@@ -36,13 +36,16 @@
 // all codes in place drifts by about 2.4e-7 per 13 K-steps (measured); one accumulator per
 // code and per term group keeps the translation at FP32 rounding level.
 // Every wait on an mbarrier is bounded (about 1 s): on expiry the CTA records FG_ETIMEDOUT
-// in *err, stops issuing work, frees its TMEM and returns.
+// in *err and stops issuing work; before it frees its TMEM and returns, the issuer waits
+// (bounded) for the MMAs it started (tcgen05.commit on tdone) and thread 0 for the bytes of
+// the bulk copies it started (bfull), so no asynchronous write is left in flight.
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <vector>
 
 #include "fg_internal.h"
+#include "fg_tcgen05.cuh"
 
 namespace fg {
 
@@ -66,114 +69,10 @@ constexpr int TMEM_COLS = 512;  // 2 buffers x (main, corr) x 128 columns: all o
 constexpr int IMG_BYTES = 13 * SBO;  // one operator image part: rows 0..103 (13 groups of 8)
 constexpr int LAG = NSTAGE - 1;      // items whose gathers may still be in flight
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+using namespace tc;
 
-__device__ __forceinline__ unsigned long long now_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Shared-memory matrix descriptor: no swizzle, K-major core matrices of 8 rows x 16 bytes.
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-    d |= (uint64_t)((LBO >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t)((SBO >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t)1 << 46;  // descriptor version of tcgen05
-    return d;                // base offset 0, absolute LBO mode, layout type 0 (no swizzle)
-}
-
-// Instruction descriptor of kind::tf32: D f32, A and B tf32, both K-major, shape M x N.
-__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t *b) {
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(b))
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_test(uint64_t *b, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(b)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait for the completion of the phase with the given parity.
-__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, int *err, volatile int *bail) {
-    if (mbar_test(b, parity)) return true;
-    const unsigned long long t0 = now_ns();
-    for (;;) {
-        if (mbar_test(b, parity)) return true;
-        if (*bail) return false;
-        if (now_ns() - t0 > 1000000000ull) {
-            *bail = 1;
-            atomicExch(err, FG_ETIMEDOUT);
-            return false;
-        }
-    }
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *b, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
-}
-// Bulk global -> shared copy whose completion is counted (in bytes) on an mbarrier.
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-// 16-byte global -> shared copy (L2 only); src_bytes = 0 fills the destination with zeros.
-__device__ __forceinline__ void cp16(void *dst, const void *src, uint32_t src_bytes) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-        "l"(a), "l"(b), "r"(idesc), "r"(acc)
-        : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint64_t *b) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(b))
-                 : "memory");
-}
-
-// 16 consecutive TMEM columns of this warp's 32 lanes: one register per column.
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// Shared-memory descriptor of this file's operand layout (LBO / SBO above).
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) { return sdesc_kmajor(saddr, LBO, SBO); }
 
 // x rounded to the 10 explicit mantissa bits of TF32 (nearest, ties away from zero), as an
 // FP32 bit pattern whose 13 low bits are zero; x - tf32_rn(x) is then exact in FP32.
@@ -218,7 +117,9 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
     int *err = a.err;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    __shared__ __align__(8) uint64_t full[NSTAGE], empty[NSTAGE], tfull[2], tfree[2];
+    // full: the 128 gathering threads of a stage; bfull: the operator's bulk copies (bytes);
+    // tdone: every MMA the issuer started has completed (checked before TMEM is freed)
+    __shared__ __align__(8) uint64_t full[NSTAGE], bfull[NSTAGE], empty[NSTAGE], tfull[2], tfree[2], tdone;
     __shared__ uint32_t tmem_base;
     __shared__ volatile int bail;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -242,9 +143,11 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
     }
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; s++) {
-            mbar_init(&full[s], 129);  // 128 gathering threads + the bulk copies' expect_tx
+            mbar_init(&full[s], 128);  // the 128 gathering threads
+            mbar_init(&bfull[s], 1);   // thread 0's expect_tx, completed by the bulk copies' bytes
             mbar_init(&empty[s], 1);
         }
+        mbar_init(&tdone, 1);
         for (int b = 0; b < 2; b++) {
             mbar_init(&tfull[b], 1);
             mbar_init(&tfree[b], 128);
@@ -278,6 +181,7 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
                                                    : -1;
         };
         int sc = src_of(0), sc_next = src_of(1);
+        int armed = 0;  // thread 0: items whose bulk copies were started (in order)
         for (int it = 0; it < nitems + LAG; it++) {
             if (it < nitems && live) {
                 const int s = it % NSTAGE;
@@ -292,9 +196,10 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
                     unsigned char *st = sm + s * STAGE_BYTES;
                     if (tid == 0) {
                         const unsigned char *img = a.op_img + ((size_t)code * IPC + q) * 2 * IMG_BYTES;
-                        mbar_arrive_expect_tx(&full[s], 2 * IMG_BYTES);
-                        bulk_g2s(st, img, IMG_BYTES, &full[s]);
-                        bulk_g2s(st + A_BYTES, img + IMG_BYTES, IMG_BYTES, &full[s]);
+                        mbar_arrive_expect_tx(&bfull[s], 2 * IMG_BYTES);
+                        bulk_g2s(st, img, IMG_BYTES, &bfull[s]);
+                        bulk_g2s(st + A_BYTES, img + IMG_BYTES, IMG_BYTES, &bfull[s]);
+                        armed = it + 1;
                     }
                     gather_item(st + 2 * A_BYTES, tid, KI * q, sc, in_hi, in_lo, ns, set_io);
                 }
@@ -307,6 +212,11 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
             }
         }
         cp_wait<0>();
+        // after a bail the issuer may not have consumed the last stages: wait (bounded) until
+        // the bytes of every bulk copy still owed to a stage have landed before the CTA exits
+        if (tid == 0 && bail)
+            for (int it = armed > NSTAGE ? armed - NSTAGE : 0; it < armed; it++)
+                mbar_drain(&bfull[it % NSTAGE], (it / NSTAGE) & 1);
     } else if (warp == 4) {
         if (lane == 0) {
             // MMA issuer. Each code accumulates into a fresh pair of TMEM accumulators
@@ -323,7 +233,11 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
                 const uint32_t dmain = tmem + b * 2 * NB, dcorr = dmain + NB;
                 for (int q = 0; q < IPC; q++) {
                     const int it = ci * IPC + q, s = it % NSTAGE;
-                    if (!mbar_wait(&full[s], (it / NSTAGE) & 1, err, &bail)) { ok = false; break; }
+                    if (!mbar_wait(&full[s], (it / NSTAGE) & 1, err, &bail) ||
+                        !mbar_wait(&bfull[s], (it / NSTAGE) & 1, err, &bail)) {
+                        ok = false;
+                        break;
+                    }
                     tc_fence_after();
                     const int ksteps = q < IPC - 1 ? KI / 8 : 1;
                     const uint32_t base = smem_u32(sm + s * STAGE_BYTES);
@@ -340,6 +254,10 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
                 }
                 mma_commit(&tfull[b]);
             }
+            // tdone arrives once every MMA started above has completed (also after a bail,
+            // when the drain warps no longer wait for them): TMEM is freed only after that
+            mma_commit(&tdone);
+            mbar_drain(&tdone, 0);
         }
     } else {
         // drain warps 5..8: warp w reads TMEM lanes 32 (w % 4) .. +31 (coefficient rows)
@@ -460,6 +378,62 @@ __global__ void k_mbar_timeout_probe(int *err) {
 }
 
 }  // namespace
+
+// Tensor-pipe throughput of kind::tf32, the instruction of the translations: one CTA per SM
+// issues `iters` MMAs of M = 128, N = n, K = 8 from fixed shared-memory operands (FP32 ones,
+// the no-swizzle K-major layout of the translations) into one TMEM accumulator and waits
+// (bounded) for their completion; cyc[block] = clock64 cycles from the first issue to the
+// completion (-1 when the wait expired).
+__global__ void __launch_bounds__(128, 1) k_peak_mma_tf32(int n, int iters, long long *cyc, int *err) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    __shared__ __align__(8) uint64_t done;
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int bail;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int a_bytes = 16 * (int)SBO, b_bytes = (n / 8) * (int)SBO;  // K = 16 of A (128 rows) and B (n rows)
+    for (int e = tid; e < (a_bytes + b_bytes) / 4; e += blockDim.x) reinterpret_cast<float *>(sm)[e] = 1.0f;
+    if (tid == 0) {
+        mbar_init(&done, 1);
+        bail = 0;
+        fence_mbar_init();
+    }
+    if (warp == 0) tmem_alloc(&tmem_base, 256);
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    if (tid == 0) {
+        const uint32_t idesc = idesc_tf32(MR, n);
+        const uint32_t base = smem_u32(sm);
+        const uint64_t a0 = sdesc(base), a1 = sdesc(base + 256);
+        const uint64_t b0 = sdesc(base + a_bytes), b1 = sdesc(base + a_bytes + 256);
+        const long long t0 = clock64();
+        for (int i = 0; i < iters; i++) mma_tf32(tmem, (i & 1) ? a1 : a0, (i & 1) ? b1 : b0, idesc, i > 0 ? 1u : 0u);
+        mma_commit(&done);
+        const bool ok = mbar_wait(&done, 0, err, &bail);
+        const long long t1 = clock64();
+        if (!ok) mbar_drain(&done, 0);  // the MMAs still own TMEM: wait again before freeing it
+        cyc[blockIdx.x] = ok ? t1 - t0 : -1;
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 256);
+    }
+}
+
+int peak_mma_smem() { return 120 * 1024; }  // one CTA per SM
+
+cudaError_t launch_peak_mma_tf32(cudaStream_t st, int grid, int n, int iters, long long *cyc, int *err) {
+    if (n % 16 != 0 || n < 16 || n > 256) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_peak_mma_tf32, cudaFuncAttributeMaxDynamicSharedMemorySize, peak_mma_smem());
+    if (e != cudaSuccess) return e;
+    k_peak_mma_tf32<<<grid, 128, peak_mma_smem(), st>>>(n, iters, cyc, err);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_mbar_timeout_probe(cudaStream_t st, int *err) {
     k_mbar_timeout_probe<<<1, 32, 0, st>>>(err);

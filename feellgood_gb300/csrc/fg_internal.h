@@ -229,6 +229,13 @@ struct Ctx {
     float2 *da_ds = nullptr, *J_ds = nullptr, *state_ds = nullptr;
     double *pot = nullptr;       // nn
     double *pot2 = nullptr;      // nn, potential of src_q2
+    // incremental demag of the FP32 + refinement path (fg_opts.demag_increment): NEXT's
+    // potentials = CURRENT's + the potentials of NEXT - CURRENT (the potential is linear in
+    // the field), the FP32 FMM acting on the change only, the sum kept in FP64
+    bool dinc = false;
+    bool dinc_valid[2] = {false, false};  // phi / phiv of CURRENT are the potentials of u / v
+    double *dstate = nullptr;            // NEXT - CURRENT: u [3 nn], then v [3 nn]
+    void *fmm64 = nullptr;               // FP64 tree at the FP32 tree's depth, built on first use
     double *epart = nullptr;     // energy partials
     double *hepart = nullptr;    // pinned
     int epart_blocks = 0;
@@ -281,7 +288,9 @@ cudaError_t launch_apply(Ctx &c, double c0, const double *x, double *y);
 cudaError_t launch_charges(Ctx &c, const double *m, int set = 0);
 cudaError_t launch_charges_pair(Ctx &c, const double *m, const double *v);  // sets 0 and 1 in one pass
 cudaError_t launch_p2p_direct(Ctx &c);
-cudaError_t launch_phi_final(Ctx &c, double *phi_out, int set = 0);
+// phi_out = base + (pot + corr) / (4 pi) (base nullptr: no base)
+cudaError_t launch_phi_final(Ctx &c, double *phi_out, int set = 0, const double *base = nullptr);
+cudaError_t launch_state_diff(Ctx &c);  // dstate = NEXT - CURRENT for u and v
 cudaError_t launch_energy(Ctx &c, const double Hext[3]);
 cudaError_t launch_energy_into(Ctx &c, const double Hext[3], double *partial);
 int bicg_grid_size(Ctx &c, bool mixed);
@@ -294,9 +303,15 @@ cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle);
 // failure-path probes: a bounded device wait that nothing ends (*out / *err set on expiry)
 cudaError_t launch_barrier_timeout_probe(Ctx &c, int *out);
 cudaError_t launch_mbar_timeout_probe(cudaStream_t st, int *err);
+// throughput probe of tcgen05.mma kind::tf32 (M = 128, N = n, K = 8), one CTA per SM
+cudaError_t launch_peak_mma_tf32(cudaStream_t st, int grid, int n, int iters, long long *cyc, int *err);
 int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p);
 int *fmm_error_flag(const Ctx &c);
 cudaError_t fmm_eval(Ctx &c, int nq = 1);  // nq 2: c.src_q2 -> c.pot2 beside c.src_q -> c.pot
+// The same evaluation with an FP64 tree of the FP32 tree's depth (built on first use; the
+// FP32 tree itself when the context is FP64); FG_* status
+int fmm_eval_fp64(Ctx &c, int nq);
+void fmm64_free(Ctx &c);
 int fmm_launches_per_eval(const Ctx &c, int nq = 1);  // kernels one FMM evaluation launches  // device int: FG_ETIMEDOUT after an expired wait (or nullptr)
 // tensor-core translations (fg_fmm_tc.cu)
 int translate_tc_smem();
@@ -349,7 +364,7 @@ int recenter_apply(Ctx &c, int dir, double threshold, double avg_dir, int *shift
 int elem_ds_setup(Ctx &c, const std::vector<double> &da, const std::vector<double> &detJ);
 void upload_rules_ds(const double ta[4][5], const double tp[5]);
 cudaError_t launch_tet_ds(Ctx &c, double dt, const double H[3]);
-void launch_state_ds(Ctx &c, const double *u, const double *phi, const double *phiv);
+cudaError_t launch_state_ds(Ctx &c, const double *u, const double *phi, const double *phiv);
 inline bool drift_on(const Ctx &c) { return c.drift_dir >= 0 && c.drift_v != 0.0; }
 inline bool use_elem_ds(const Ctx &c) { return c.elem_ds && !c.hsp && !c.spin_s && !drift_on(c); }
 void recenter_free(Ctx &c);

@@ -868,13 +868,24 @@ __global__ void __launch_bounds__(256) k_p2p_direct64(int nt, const int *__restr
 // phi_i = (pot_i + corr_i) / (4 pi), src/fmm_demag.h:211-223; corr gathered per node.
 __global__ void k_phi_final(int nt, const int *__restrict__ tnode, const int *__restrict__ tinc_ptr,
                             const int *__restrict__ tinc, const double *__restrict__ tri_slot,
-                            const double *__restrict__ pot, double *__restrict__ phi) {
+                            const double *__restrict__ pot, const double *__restrict__ base,
+                            double *__restrict__ phi) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nt) return;
     const int i = tnode[k];
     double corr = 0.0;
     for (int j = tinc_ptr[i]; j < tinc_ptr[i + 1]; j++) corr += tri_slot[tinc[j]];
-    phi[i] = (pot[i] + corr) / (4 * M_PI);
+    const double p = (pot[i] + corr) / (4 * M_PI);
+    phi[i] = base ? base[i] + p : p;
+}
+
+// d = NEXT - CURRENT of u (first 3 nn) and of v (next 3 nn).
+__global__ void k_state_diff(size_t n3, const double *__restrict__ u1, const double *__restrict__ u0,
+                             const double *__restrict__ v1, const double *__restrict__ v0, double *__restrict__ d) {
+    const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (k >= n3) return;
+    d[k] = u1[k] - u0[k];
+    d[n3 + k] = v1[k] - v0[k];
 }
 
 // ---------------------------------------------------------------------------------
@@ -1296,12 +1307,19 @@ cudaError_t launch_p2p_direct(Ctx &c) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_phi_final(Ctx &c, double *phi_out, int set) {
+cudaError_t launch_phi_final(Ctx &c, double *phi_out, int set, const double *base) {
     if (c.n_mag_nodes == 0) return cudaSuccess;
     const double *ts = set ? c.tri_slot2 : c.tri_slot, *pot = set ? c.pot2 : c.pot;
     if (!ts || !pot) return cudaErrorInvalidValue;
     k_phi_final<<<nblocks(c.n_mag_nodes, 256), 256, 0, c.stream>>>(c.n_mag_nodes, c.mag_nodes, c.tinc_ptr, c.tinc,
-                                                                     ts, pot, phi_out);
+                                                                     ts, pot, base, phi_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_state_diff(Ctx &c) {
+    if (!c.dstate) return cudaErrorInvalidValue;
+    const size_t n3 = 3 * (size_t)c.nn;
+    k_state_diff<<<(unsigned)((n3 + 255) / 256), 256, 0, c.stream>>>(n3, c.u[1], c.u[0], c.v[1], c.v[0], c.dstate);
     return cudaGetLastError();
 }
 
@@ -1317,7 +1335,10 @@ cudaError_t launch_energy_into(Ctx &c, const double H[3], double *partial) {
     const int G = c.epart_blocks;
     // the double-single form of the FP32 + refinement path reads NEXT as double-single pairs
     const bool dsp = energy_iso(c) && use_elem_ds(c);
-    if (dsp) launch_state_ds(c, c.u[1], c.phi[1], c.phiv[1]);
+    if (dsp) {
+        const cudaError_t e = launch_state_ds(c, c.u[1], c.phi[1], c.phiv[1]);
+        if (e != cudaSuccess) return e;
+    }
     const float2 *dda = dsp ? c.da_ds : nullptr;
     if (c.npi_t == 5)
         (energy_iso(c) ? k_energy<5, 4, true> : k_energy<5, 4, false>)<<<G, 256, 0, c.stream>>>(

@@ -20,7 +20,9 @@
 //
 // In host code the array's name is only a host-side stand-in, not a device address. Its
 // device address is looked up once per device with cudaGetSymbolAddress, by the first call
-// made while that device is current; make that first call before any stream capture.
+// for a context on that device (the call makes the context's device current while it runs
+// and restores the caller's current device afterwards); make that first call before any
+// stream capture.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -41,31 +43,40 @@ constexpr int kMaxDevices = 64;
 std::mutex g_lock;
 double *g_dev_ptr[kMaxDevices] = {nullptr};
 
-// Device address of the scratch array on the current device (looked up once per device).
+// Device address of the scratch array on the context's device (looked up once per device,
+// with that device current: the caller's current device may be another one).
 int scratch_address(fg::Ctx &c, double **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        c.err = std::string("fg_energy_noalloc: cudaGetDevice: ") + cudaGetErrorString(e);
-        return FG_ECUDA;
-    }
-    if (dev < 0 || dev >= kMaxDevices) {
+    if (c.device < 0 || c.device >= kMaxDevices) {
         c.err = "fg_energy_noalloc: device ordinal out of range";
         return FG_EINVAL;
     }
     std::lock_guard<std::mutex> lk(g_lock);
-    if (!g_dev_ptr[dev]) {
+    if (!g_dev_ptr[c.device]) {
         void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
         if (e != cudaSuccess || !p) {
             c.err = std::string("fg_energy_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e);
             return FG_ECUDA;
         }
-        g_dev_ptr[dev] = static_cast<double *>(p);
+        g_dev_ptr[c.device] = static_cast<double *>(p);
     }
-    *out = g_dev_ptr[dev];
+    *out = g_dev_ptr[c.device];
     return FG_OK;
 }
+
+// Makes the context's device current for the duration of a call and restores the caller's.
+struct DeviceScope {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceScope(int dev) {
+        err = cudaGetDevice(&prev);
+        if (err == cudaSuccess && prev != dev) err = cudaSetDevice(dev);
+        else if (err == cudaSuccess) prev = -1;  // already current: nothing to restore
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
 }  // namespace
 
 extern "C" int fg_energy_noalloc(fg_ctx *h, const double Hext[3], double energies[4]) {
@@ -76,6 +87,12 @@ extern "C" int fg_energy_noalloc(fg_ctx *h, const double Hext[3], double energie
         c.err = "fg_energy_noalloc: the reduction needs " + std::to_string(need) + " partial sums, more than the " +
                 std::to_string(FG_NOALLOC_PARTIALS) + " of the static scratch array";
         return FG_EINVAL;
+    }
+    DeviceScope scope(c.device);
+    if (scope.err != cudaSuccess) {
+        c.err = std::string("fg_energy_noalloc: cannot make the context's device current: ") +
+                cudaGetErrorString(scope.err);
+        return FG_ECUDA;
     }
     double *scratch = nullptr;
     int s = scratch_address(c, &scratch);

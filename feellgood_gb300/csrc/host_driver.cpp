@@ -317,7 +317,8 @@ int run_impl(Run &R, const char *settings_path, unsigned int seed, int verbose, 
                     for (int k = 0; k < 3; k++) R.u[3 * i + k] = S.m0[k];
         }
         if (!std::isnan(S.initial_time)) t0 = S.initial_time;
-        s = fg_set_state(R.ctx, R.u.data(), R.v.data(), R.phi.data(), R.phiv.data());
+        // the potentials of the initial state are not known: the first compute_all evaluates them
+        s = fg_set_state(R.ctx, R.u.data(), R.v.data(), nullptr, nullptr);
         if (s != FG_OK) return fail(s, fg_last_error(R.ctx));
         // main(): srand(seed); the LinAlgebra constructor draws one basis angle
         fg_rng_seed(seed);

@@ -91,7 +91,7 @@ typedef struct {
     int one_gauss_point;  /* 1: single Gauss point rules (reference ONE_GAUSS_POINT build) */
     int first_order;      /* 1: skip the demag of v (reference FIRST_ORDER build) */
     int refine_max;       /* FP64 refinement sweeps in FG_PREC_FP32_REFINE */
-    double inner_tol;     /* relative tolerance of each FP32 inner solve */
+    double inner_tol;     /* floor of the relative target of each FP32 inner solve (1e-5) */
     int verbose;
     int profile;          /* 1: record device events around every FMM stage (fg_fmm_timings) */
     int mlp_train_steps;  /* learned guess: solves that only train before the guess is proposed */
@@ -116,6 +116,15 @@ typedef struct {
                              step's element integrals */
     double spin_tol;      /* relative tolerance of the spin and potential solves (1e-8) */
     int spin_max_iter;    /* their iteration limit (1000) */
+    int demag_increment;  /* FP32 + refinement with the FMM (single contexts): 1 (default) every
+                             fg_compute_all forms the potentials of NEXT as those of CURRENT plus
+                             the FP32 FMM of the change of the field (the potential is linear in
+                             the field), accumulated in FP64, so the FP32 FMM's rounding acts
+                             on the step's change only; where CURRENT has no valid potentials
+                             (after fg_create, fg_set_state without them, fg_recenter) the
+                             potentials are evaluated in full by the FP64 FMM. 0: a full FP32
+                             FMM evaluation in every fg_compute_all; 2: a full FP64 FMM
+                             evaluation in every fg_compute_all (accuracy studies) */
 } fg_opts;
 
 typedef struct {
@@ -139,7 +148,9 @@ int fg_create(const fg_mesh *mesh, const fg_region *regions, int n_regions, cons
               int n_tri_regions, const fg_opts *opts, fg_ctx **out);
 void fg_destroy(fg_ctx *ctx);
 
-/* Sets CURRENT and NEXT node data. v, phi, phiv may be NULL (zero). */
+/* Sets CURRENT and NEXT node data. v, phi, phiv may be NULL (zero). phi and phiv, when
+ * given, are taken as the demag potentials of u and v (fg_opts.demag_increment continues
+ * from them); pass NULL where they are not (the next fg_compute_all then evaluates them). */
 int fg_set_state(fg_ctx *ctx, const double *u, const double *v, const double *phi, const double *phiv);
 
 /* One attempt of a time step: tangent basis rotated by basis_angle (radians), element
@@ -341,6 +352,18 @@ int fg_debug_translate_tc(int n_in, int n_out, int ncode, const float *ops, cons
  * bytes a launch asks for, [6] threads per block of a launch, [7] resident blocks per SM
  * for that launch (0: it cannot launch). */
 int fg_debug_tc_resources(int attrs[8]);
+
+/* Measured compute roofs of the current device (no reference counterpart), for the rooflines
+ * of the compute-bound kernels: throughput microbenchmarks of a few ms each, counted per SM
+ * and per clock cycle (clock64 over each run, so the figures hold at any clock):
+ *   out[0] FP32 fused multiply-add lane operations (fma.rn.f32)
+ *   out[1] the same through packed pairs (fma.rn.f32x2, two lane operations an instruction)
+ *   out[2] SFU reciprocal square roots (rsqrt.approx.ftz.f32)
+ *   out[3] tensor flops of tcgen05.mma kind::tf32, M = 128, N = 128, K = 8 (the FMM
+ *          translations' shape), out[4] the same with N = 256
+ *   out[5] the SM clock in MHz during the FP32 run (cycles over its event time)
+ * Allocates and frees its own device buffers and stream. */
+int fg_measure_peaks(double out[6]);
 
 /* Device ms of the FMM stages when opts.profile is set, averaged over the evaluations
  * since the previous call (CUDA events around each stage, recorded without any extra

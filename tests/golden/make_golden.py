@@ -1,8 +1,8 @@
 """Regenerate the golden fixtures in tests/golden/ from the FeeLLGood source tree.
 
-Run in a container where the reference tree is mounted (path given as argv[1], default
-/root/reference). Nothing at test time reads the reference tree; the tests read only
-the files this script writes:
+Usage: ``python tests/golden/make_golden.py <path of the FeeLLGood source tree>`` (the path
+is required). Nothing at test time reads the reference tree; the tests read only the files
+this script writes:
 
 * ``ellipsoid.msh``          the mesh of the reference's functional test (examples/ellipsoid.msh),
                              copied byte for byte.
@@ -83,4 +83,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2 or not os.path.isdir(sys.argv[1]):
+        sys.exit("usage: make_golden.py <path of the FeeLLGood source tree>")
+    main(sys.argv[1])

@@ -39,7 +39,8 @@ def _rel(a, b):
 def _singles(ms, us):
     cs = []
     for m, u in zip(ms, us):
-        c = fg.Context(m, cases.regions(alpha=0.1), **OPTS)
+        # a batch evaluates the full FP32 FMM every step: the single context does the same
+        c = fg.Context(m, cases.regions(alpha=0.1), demag_increment=0, **OPTS)
         c.set_state(u)
         c.compute_all([0, 0, 0])
         cs.append(c)
