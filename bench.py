@@ -219,7 +219,6 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
-P2P_FLOPS_PER_PAIR = 9  # 3 sub, 3 fma (r^2), rsqrt, fma (q/r): FP32 + SFU
 
 
 def ncu_traffic(kernel):
@@ -240,16 +239,44 @@ def ncu_traffic(kernel):
         return None
 
 
-def roofline_of(kernel, ms, units, peaks):
+# FP32 lane operations of the near field per (target, source) pair, both charge sets (count
+# of the f32x2 pass: 3 subtractions, 1 multiply and 2 fused multiply-adds for r^2, one fused
+# multiply-add per set; packed instructions do two of them), and SFU reciprocal square
+# roots per pair (shared by the sets)
+P2P_FMA_LANE_OPS_PER_PAIR = 8
+P2P_RSQRT_PER_PAIR = 1
+
+
+def compute_roofs(compute, sm_mhz):
+    """Measured compute roofs (fg_measure_peaks, per SM and clock) at the sampled SM clock."""
+    if not compute:
+        return None
+    hz = (sm_mhz or compute["sm_mhz"]) * 1e6
+    n = compute["n_sm"]
+    return {"fma_lane_ops_per_s": compute["ffma_per_clk_sm"] * n * hz,
+            "rsqrt_per_s": compute["rsqrt_per_clk_sm"] * n * hz,
+            "tf32_tflops": compute["tf32_n128_flops_per_clk_sm"] * n * hz / 1e12,
+            "sm_mhz": hz / 1e6, "per_clk_per_sm": {k: compute[k] for k in (
+                "ffma_per_clk_sm", "ffma2_per_clk_sm", "rsqrt_per_clk_sm", "tf32_n128_flops_per_clk_sm")}}
+
+
+def roofline_of(kernel, ms, units, peaks, roofs=None):
     """Roofline entry of one kernel from its live per-launch device time (CUDA events)."""
     hbm = peaks.get("hbm_gbs", 6800.0)
-    tc = peaks.get("bf16_tflops", 1900.0)
     src = "measured" if peaks else "fallback"
-    if kernel == "k_m2l_tc (M2L, tcgen05 3xTF32)":
+    if kernel.startswith("k_m2l_tc"):
+        # useful flops: 2 x 100 x 100 per (cell, source cell) pair and charge set; the roof is
+        # the measured tcgen05 kind::tf32 rate at the sampled clock (the kernel's instruction)
         fl = 2.0 * 100 * 100 * units["m2l_pairs"]
         ach = fl / (ms * 1e-3) / 1e12
-        return {"kernel": kernel, "bound": "tensor", "achieved": ach, "peak": tc, "unit": "TFLOP/s",
-                "frac": ach / tc, "traffic": None, "algorithmic_per_launch": fl, "peak_source": src}
+        peak = roofs["tf32_tflops"] if roofs else peaks.get("bf16_tflops", 1900.0) / 2
+        # issued: three TF32 products per useful one, M padded 100 -> 128 rows, K 100 -> 104
+        issued = ach * 3 * 1.28 * 1.04
+        return {"kernel": kernel, "bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                "frac": ach / peak, "issued_tflops": issued, "issued_frac": issued / peak, "traffic": None,
+                "algorithmic_per_launch": fl,
+                "peak_source": "measured tcgen05.mma kind::tf32 throughput (fg_measure_peaks) at the sampled SM clock"
+                if roofs else "fallback: half the measured BF16 rate"}
     by = units["bytes"]
     ach = by / (ms * 1e-3) / 1e9
     e = {"kernel": kernel, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
@@ -271,13 +298,16 @@ def main():
                     help="after those, the guess keeps training (timed) on every n-th solve")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--compare-steps", type=int, default=0,
+                    help="wire / platelet: steps of the plain FP64 comparison run (default: all timed steps)")
     ap.add_argument("--drift", type=int, default=0,
-                    help="accuracy study: N steps of the headline path and of the plain FP64 path from the same "
-                         "state and angles; prints max |dm|, rel-L2 of v and phi (its own JSON line)")
-    ap.add_argument("--drift-pair", default="mixed-plain", choices=["mixed-plain", "plain-plainguess"],
-                    help="mixed-plain: headline path vs plain FP64; plain-plainguess: plain FP64 with the "
-                         "previous-step guess vs plain FP64 with the learned guess (same arithmetic, another "
-                         "valid initial guess: the spread the tolerance alone allows)")
+                    help="accuracy study: N steps of the precision paths and of the plain FP64 path from the same "
+                         "state and angles on --workload film, wire or platelet (JSON lines of max |dm|)")
+    ap.add_argument("--drift-tol", default="1e-6",
+                    help="accuracy study: comma-separated BiCG tolerances, one JSON line each")
+    ap.add_argument("--drift-split", action="store_true",
+                    help="accuracy study: add the FP32 + refinement path with a full FP64 demag and with a full "
+                         "FP32 demag every step (what the solver and the demag each contribute)")
     ap.add_argument("--quick", action="store_true",
                     help="timed steps only (no training, comparisons, end-to-end or CPU legs): for profiling")
     args = ap.parse_args()
@@ -289,6 +319,9 @@ def main():
     if args.impl == "reference":
         reference_arm(args)
         return
+    if args.drift > 0:
+        drift_study(args)
+        return
     if args.workload == "batch64":
         bench_batch(args)
         return
@@ -297,9 +330,6 @@ def main():
         return
     if args.workload == "spin":
         bench_spin(args)
-        return
-    if args.drift > 0:
-        drift_study(args)
         return
     rank, world, dist = dist_setup(args.gpus)
     import __graft_entry__
@@ -316,6 +346,7 @@ def main():
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
+    compute = fg.measure_peaks()  # measured FP32 / SFU / TF32 roofs, per SM and clock
 
     # learned guess + FP32 body + FP64 refinement (headline). The guess is trained online
     # on the solver's own solutions; those solves are not timed.
@@ -415,18 +446,24 @@ def main():
     }
     dom = max(kernels, key=lambda k: kernels[k][0] * kernels[k][1])
     kernels[dom][2]["traffic"] = ncu_traffic(dom.split()[0])
-    roof = roofline_of(dom, kernels[dom][0], kernels[dom][2], peaks)
+    roofs = compute_roofs(compute, clocks.get("sm_mhz"))
+    roof = roofline_of(dom, kernels[dom][0], kernels[dom][2], peaks, roofs)
     roof["traffic_source"] = f"profiles/{dom.split()[0]}_film_1.2M.md (one ncu launch)"
     roof["share_of_step"] = kernels[dom][0] * kernels[dom][1] / float(ms[:, 4].mean())
     if dom.startswith("k_l2p_p2p"):
-        # the near field does one reciprocal square root per (target, source) pair: its real
-        # limit is the SFU issue rate, reported beside the HBM roof
-        sm = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+        # the near field's binding roofs are its compute pipes, measured by fg_measure_peaks:
+        # one SFU reciprocal square root and 8 FP32 lane operations per (target, source) pair
         pairs_s = n_p2p / (fmm_stage[4] * 1e-3)
-        sfu_peak = 152 * 16 * sm * 1e6
         roof["pairs_per_s"] = pairs_s
-        roof["sfu_rsqrt_limit_pairs_per_s"] = sfu_peak
-        roof["sfu_frac"] = pairs_s / sfu_peak
+        roof["compute"] = {
+            "sfu_rsqrt": {"achieved_per_s": pairs_s * P2P_RSQRT_PER_PAIR, "peak_per_s": roofs["rsqrt_per_s"],
+                          "frac": pairs_s * P2P_RSQRT_PER_PAIR / roofs["rsqrt_per_s"]},
+            "fp32_fma_pipe": {"achieved_lane_ops_per_s": pairs_s * P2P_FMA_LANE_OPS_PER_PAIR,
+                              "peak_lane_ops_per_s": roofs["fma_lane_ops_per_s"],
+                              "frac": pairs_s * P2P_FMA_LANE_OPS_PER_PAIR / roofs["fma_lane_ops_per_s"]},
+            "peak_source": "fg_measure_peaks microbenchmarks (per SM and clock) at the sampled SM clock",
+            "sm_mhz": roofs["sm_mhz"]}
+    m2l_roof = roofline_of("k_m2l_tc (M2L, tcgen05 3xTF32)", fmm_stage[2], {"m2l_pairs": 2 * n_m2l}, peaks, roofs)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -458,6 +495,8 @@ def main():
             "fmm": {"L": L, "m2l_pairs": n_m2l, "p2p_pairs": n_p2p,
                     "stage_ms": dict(zip(stage_names, [float(x) for x in fmm_stage]))},
             "roofline": roof,
+            "m2l_roofline": m2l_roof,
+            "measured_compute_roofs": roofs,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
                     "d2h_bytes_per_step": state_bytes},
@@ -471,49 +510,66 @@ def main():
 
 
 def drift_study(args):
-    """The headline path (learned guess, FP32 body + FP64 refinement, FP32 FMM) against the plain
-    FP64 path over N steps of the film workload, same initial state, angles and tolerance."""
+    """Trajectory accuracy: N steps of the FP32 + refinement path (with and without the learned
+    guess) and of a control (the plain FP64 path with the learned guess: the same arithmetic,
+    another valid initial guess) against the plain FP64 path, from the same state with the same
+    basis angles, at each BiCG tolerance of --drift-tol, all with the FMM at the same depth.
+    Prints one JSON line per tolerance: max |dm| per pair at the checkpoints, iterations and
+    refinements per step, device ms per step."""
     import __graft_entry__
     __graft_entry__.build_product()
     import feellgood_gb300 as fg
-    mesh = film_mesh()
-    u0 = initial_state(mesh)
-    H = np.zeros(3)
+    if args.workload in ("wire", "platelet"):
+        mesh, u0, H, alpha, _ = (wire_workload if args.workload == "wire" else platelet_workload)(fg)
+        regs = [dict(Ae=1e-11, Ms=795774.7, alpha=0.5), dict(Ae=AE, Ms=MS, alpha=alpha)]
+        desc = " ".join((wire_workload if args.workload == "wire" else platelet_workload).__doc__.split())
+    else:
+        mesh = film_mesh()
+        u0, H, regs = initial_state(mesh), np.zeros(3), regions()
+        desc = "film 400x400x10 nm, 2 nm grid, 1.2M tets, alpha 0.02, dt 5e-14, zero field, seeded smoothed random m"
     fg.rng_seed(SEED)
     angles = [fg.rng_angle() for _ in range(args.drift)]
-    out = {}
-    if args.drift_pair == "mixed-plain":
-        pair = (("mixed", dict(precision=fg.FG_PREC_FP32_REFINE, learned_guess=1, mlp_train_every=args.train_every)),
-                ("plain", dict(precision=fg.FG_PREC_FP64)))
-    else:
-        pair = (("mixed", dict(precision=fg.FG_PREC_FP64, learned_guess=1, mlp_train_every=args.train_every)),
-                ("plain", dict(precision=fg.FG_PREC_FP64)))
-    for name, opts in pair:
-        c = fg.Context(mesh, regions(), tol=TOL, max_iter=MAXITER, demag=fg.FG_DEMAG_FMM, **opts)
-        c.set_state(u0)
-        c.compute_all(H)
-        t0 = time.perf_counter()
-        ms, reps = run_steps(c, args.drift, H, DT, angles)
-        out[name] = (c.get_state(0), float(ms[:, 4].sum()), time.perf_counter() - t0,
-                     float(np.mean([r["iters"] for r in reps])))
-        c.close()
-    (a, ta, wa, ia), (b, tb, wb, ib) = out["mixed"], out["plain"]
-    dm = np.linalg.norm(a["u"] - b["u"], axis=1)
-
-    def rel(x, y):
-        return float(np.linalg.norm(x - y) / np.linalg.norm(y))
-    what = ("learned-guess FP32+refine vs plain FP64" if args.drift_pair == "mixed-plain"
-            else "plain FP64 learned guess vs plain FP64 previous-step guess")
-    line = {"metric": f"max |dm| after {args.drift} steps, {what} (film 1.2M tets)",
-            "value": float(dm.max()), "unit": "1", "higher_is_better": False, "steps": args.drift,
-            "rel_l2_u": rel(a["u"], b["u"]), "rel_l2_v": rel(a["v"], b["v"]), "rel_l2_phi": rel(a["phi"], b["phi"]),
-            "rel_l2_phiv": rel(a["phiv"], b["phiv"]),
-            "mean_m_mixed": [float(x) for x in a["u"].mean(axis=0)],
-            "mean_m_plain": [float(x) for x in b["u"].mean(axis=0)],
-            "device_s": {"mixed": ta / 1e3, "plain": tb / 1e3}, "iters_per_step": {"mixed": ia, "plain": ib},
-            "config": {"workload": "film 400x400x10 nm, 2 nm grid, 1.2M tets, alpha 0.02, dt 5e-14, tol 1e-6, "
-                                   "zero field, seeded smoothed random initial m"}}
-    print(json.dumps(line), flush=True)
+    marks = sorted({k for k in (10, 100, 300, 1000, 2000, 5000) if k < args.drift} | {args.drift})
+    variants = {"plain": dict(precision=fg.FG_PREC_FP64),
+                "control_plain_learned": dict(precision=fg.FG_PREC_FP64, learned_guess=1),
+                "fp32_refine": dict(precision=fg.FG_PREC_FP32_REFINE),
+                "fp32_refine_learned": dict(precision=fg.FG_PREC_FP32_REFINE, learned_guess=1)}
+    if args.drift_split:
+        variants["fp32_refine_fp64_demag"] = dict(precision=fg.FG_PREC_FP32_REFINE, demag_increment=2)
+        variants["fp32_refine_full_fp32_demag"] = dict(precision=fg.FG_PREC_FP32_REFINE, demag_increment=0)
+    depth = None
+    for tol in [float(t) for t in args.drift_tol.split(",")]:
+        snaps, info = {}, {}
+        for name, opts in variants.items():
+            c = fg.Context(mesh, regs, tol=tol, max_iter=MAXITER, demag=fg.FG_DEMAG_FMM,
+                           mlp_train_every=args.train_every, fmm_leaf=-depth if depth else 0, **opts)
+            depth = depth or int(c.counters()[1])  # every run at the first run's FMM depth
+            c.set_state(u0)
+            c.compute_all(H)
+            snaps[name], its, refs, ms = {}, [], [], []
+            for k in range(args.drift):
+                rep = c.step(DT, prefactor(DT, DT), H, angles[k])
+                if rep["status"] != 0:
+                    raise RuntimeError(f"{name}: solver failed at step {k}: {rep}")
+                its.append(rep["iters"])
+                refs.append(rep["refinements"])
+                c.compute_all(H)
+                ms.append(float(c.timings()[4]))
+                if k + 1 in marks:
+                    snaps[name][k + 1] = c.get_state(0)["u"].copy()
+            info[name] = {"iters_per_step": float(np.mean(its)), "refinements_per_step": float(np.mean(refs)),
+                          "device_ms_per_step_median": float(np.median(ms))}
+            c.close()
+        for name in variants:
+            if name != "plain":
+                info[name]["max_abs_dm_vs_plain"] = {
+                    str(k): float(np.linalg.norm(snaps[name][k] - snaps["plain"][k], axis=1).max()) for k in marks}
+        ctrl = info["control_plain_learned"]["max_abs_dm_vs_plain"][str(args.drift)]
+        line = {"metric": f"max |dm| after {args.drift} steps vs the plain FP64 path, tol {tol:g} ({args.workload})",
+                "value": info["fp32_refine_learned"]["max_abs_dm_vs_plain"][str(args.drift)], "unit": "1",
+                "higher_is_better": False, "steps": args.drift, "tol": tol, "fmm_depth": depth,
+                "control_spread": ctrl, "runs": info, "config": {"workload": desc}}
+        print(json.dumps(line), flush=True)
 
 
 def wire_workload(fg, seed=SEED):
@@ -551,18 +607,22 @@ def platelet_workload(fg, seed=SEED):
 
 def bench_learned_workload(args):
     """The learned guess where it is meant to be used: trained online on the first steps of the
-    run (200 for the wire, 300 for the platelet; not timed), then the timed steps, compared on
-    the same state and angles with the previous-step guess (same precision) and with the plain
-    FP64 path; for the platelet also max |dm| against the plain FP64 path after the timed steps."""
+    run (200 for the wire, 300 for the platelet; not timed), then the timed steps (--steps:
+    2000 and 5000 are the configurations' lengths), compared on the same state and angles with
+    the previous-step guess (same precision) and with the plain FP64 path (its first
+    --compare-steps steps, default all): steps/s, BiCG iterations per step and max |dm| of the
+    learned-guess path against the plain FP64 path after those steps."""
     import __graft_entry__
     __graft_entry__.build_product()
     import feellgood_gb300 as fg
     mesh, u0, H, alpha, ntrain = (wire_workload if args.workload == "wire" else platelet_workload)(fg)
     regs = [dict(Ae=1e-11, Ms=795774.7, alpha=0.5), dict(Ae=AE, Ms=MS, alpha=alpha)]
+    ncmp = min(args.steps, args.compare_steps or args.steps)
     fg.rng_seed(SEED)
     angles = fg.rng_angle
     ctx = fg.Context(mesh, regs, tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP32_REFINE, demag=fg.FG_DEMAG_FMM,
                      learned_guess=1, mlp_train_steps=ntrain, mlp_train_every=args.train_every, profile=1)
+    depth = int(ctx.counters()[1])
     ctx.set_state(u0)
     ctx.compute_all(H)
     run_steps(ctx, ntrain + args.warmup, H, DT, angles)
@@ -571,8 +631,12 @@ def bench_learned_workload(args):
     step_angles = [angles() for _ in range(args.steps)]
     clk = ClockSampler(0)
     clk.start()
-    ms, reps = run_steps(ctx, args.steps, H, DT, step_angles)
+    ms1, reps1 = run_steps(ctx, ncmp, H, DT, step_angles[:ncmp])
+    learned_cmp = ctx.get_state(0)
+    ms2, reps2 = run_steps(ctx, args.steps - ncmp, H, DT, step_angles[ncmp:])
     clocks = clk.stop()
+    ms = np.concatenate([ms1, ms2]) if len(ms2) else ms1
+    reps = reps1 + reps2
     fmm_stage = ctx.fmm_timings()
     cnt = ctx.counters()
     learned = ctx.get_state(0)
@@ -590,19 +654,21 @@ def bench_learned_workload(args):
         recenter_ms = (time.perf_counter() - t0) / 5 * 1e3
         rc.close()
     ctx.close()
-    out = {"learned": (args.steps / (ms[:, 4].sum() / 1e3), float(np.mean([r["iters"] for r in reps])))}
+    out = {"learned": (args.steps / (ms[:, 4].sum() / 1e3), float(np.mean([r["iters"] for r in reps])),
+                       float(np.mean([r["refinements"] for r in reps])))}
     acc = float(np.mean([r["guess_accepted"] for r in reps]))
     r0 = float(np.median([r["res0"] / r["res0_fallback"] for r in reps if r["res0_fallback"] > 0]))
     finals = {}
     for name, opts, n in (("previous_step_guess", dict(precision=fg.FG_PREC_FP32_REFINE), args.steps),
-                          ("plain_fp64", dict(precision=fg.FG_PREC_FP64), args.steps)):
-        c = fg.Context(mesh, regs, tol=TOL, max_iter=MAXITER, demag=fg.FG_DEMAG_FMM, **opts)
+                          ("plain_fp64", dict(precision=fg.FG_PREC_FP64), ncmp)):
+        c = fg.Context(mesh, regs, tol=TOL, max_iter=MAXITER, demag=fg.FG_DEMAG_FMM, fmm_leaf=-depth, **opts)
         c.set_state(start["u"], start["v"], start["phi"], start["phiv"])
-        pms, preps = run_steps(c, n, H, DT, step_angles)
-        out[name] = (n / (pms[:, 4].sum() / 1e3), float(np.mean([r["iters"] for r in preps])))
+        pms, preps = run_steps(c, n, H, DT, step_angles[:n])
+        out[name] = (n / (pms[:, 4].sum() / 1e3), float(np.mean([r["iters"] for r in preps])),
+                     float(np.mean([r["refinements"] for r in preps])))
         finals[name] = c.get_state(0)
         c.close()
-    dm = np.linalg.norm(learned["u"] - finals["plain_fp64"]["u"], axis=1).max()
+    dm = np.linalg.norm(learned_cmp["u"] - finals["plain_fp64"]["u"], axis=1).max()
     ntets = len(mesh["tets"])
     line = {
         "metric": f"LLG steps/s, {args.workload} ({ntets} tets), learned guess + FP32 body + FP64 refinement",
@@ -610,12 +676,14 @@ def bench_learned_workload(args):
         "ms_per_step": 1e3 / out["learned"][0], "higher_is_better": True, "dtype": "f32+f64",
         "data": "synthetic (seeded)",
         "config": {"workload": " ".join((wire_workload if args.workload == "wire" else platelet_workload).__doc__.split()),
-                   "train_solves_untimed": ntrain, "dt": DT, "tol": TOL},
+                   "train_solves_untimed": ntrain, "dt": DT, "tol": TOL, "fmm_depth": depth},
         "iters_per_step": {k: v[1] for k, v in out.items()},
+        "refinements_per_step": {k: v[2] for k, v in out.items()},
         "steps_per_s": {k: v[0] for k, v in out.items()},
         "learned_guess": {"accepted_frac": acc, "res0_over_fallback_median": r0},
         "speedup_vs_plain_fp64": out["learned"][0] / out["plain_fp64"][0],
-        "max_abs_dm_vs_plain_fp64_after_timed_steps": float(dm),
+        "speedup_vs_previous_step_guess": out["learned"][0] / out["previous_step_guess"][0],
+        "max_abs_dm_vs_plain_fp64": {"after_steps": ncmp, "value": float(dm)},
         "fmm": {"L": int(cnt[1]), "m2l_pairs": float(cnt[2]), "p2p_pairs": float(cnt[3]),
                 "stage_ms": dict(zip(["p2m", "m2m", "m2l", "l2l", "l2p_p2p"], [float(x) for x in fmm_stage]))},
         "clocks": clocks,

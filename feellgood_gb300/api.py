@@ -121,6 +121,7 @@ SIGNATURES = {
     "fg_mlp_debug_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p]),
     "fg_mlp_nparam": (C.c_int, []),
+    "fg_mlp_debug_infer": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "fg_solver_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "fg_debug_wait_timeout": (C.c_int, [C.c_void_p, C.c_int]),
     "fg_gauss_points": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
@@ -588,6 +589,13 @@ class Context:
                                              _ptr(loss)))
         return w, g, float(loss[0])
 
+    def mlp_debug_infer(self, feat):
+        """The GPU inference kernel's network outputs [n, 3] for given feature rows [n, 12]."""
+        feat = np.ascontiguousarray(feat, dtype=np.float32)
+        out = np.zeros((len(feat), 3), np.float32)
+        self._check(self.L.fg_mlp_debug_infer(self.h, len(feat), _ptr(feat), _ptr(out)))
+        return out
+
     def fmm_timings(self):
         """Device ms of the FMM stages of the last evaluation (needs profile=1):
         P2M, M2M, M2L, L2L, L2P+P2P."""
@@ -604,13 +612,14 @@ class Context:
 
 def measure_peaks():
     """fg_measure_peaks: per-SM, per-clock throughputs of the FP32 FMA (scalar and f32x2), the
-    SFU reciprocal square root and tcgen05 kind::tf32 (N = 128 and 256), and the SM clock."""
-    out = np.zeros(6)
+    SFU reciprocal square root and tcgen05 kind::tf32 (N = 128 and 256), the SM clock and
+    the number of SMs."""
+    out = np.zeros(7)
     s = fg_lib().fg_measure_peaks(_dptr(out))
     if s != FG_OK:
         raise FgError(s, "fg_measure_peaks")
     keys = ["ffma_per_clk_sm", "ffma2_per_clk_sm", "rsqrt_per_clk_sm", "tf32_n128_flops_per_clk_sm",
-            "tf32_n256_flops_per_clk_sm", "sm_mhz"]
+            "tf32_n256_flops_per_clk_sm", "sm_mhz", "n_sm"]
     return dict(zip(keys, (float(x) for x in out)))
 
 

@@ -748,8 +748,13 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
     const bool will_train = !use_mlp || h->solves_since_train + 1 >= train_every;
     if (c.mlp) CK(mlp_before_solve(c, h->last_c0, use_mlp, will_train));
     CK(cudaEventRecord(c.ev[1], c.stream));
-    if (c.opts.precision == FG_PREC_FP32_REFINE) CK(launch_mixed(c, dt, prefactor));
-    else CK(launch_bicg64(c, dt, prefactor));
+    if (c.opts.precision == FG_PREC_FP32_REFINE) {
+        const cudaError_t e = launch_mixed(c, dt, prefactor);
+        c.cand_x = c.cand_W = nullptr;  // a candidate is judged by one solve only
+        CK(e);
+    } else {
+        CK(launch_bicg64(c, dt, prefactor));
+    }
     c.launches += 1;
     CK(cudaEventRecord(c.ev[2], c.stream));
     CK(cudaMemcpyAsync(c.hres, c.dres, sizeof(SolveResult), cudaMemcpyDeviceToHost, c.stream));
@@ -765,6 +770,10 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
     double r0m = r.res0, r0p = r.res0;
     if (c.mlp) {
         mlp_after_sync(c, use_mlp ? &accepted : nullptr, &r0m, &r0p, nullptr);
+        if (mlp_take_timeout(c)) {
+            status = FG_ETIMEDOUT;
+            c.err = "learned guess: a tensor-core pipeline wait timed out";
+        }
         if (!use_mlp) { r0m = r.res0; r0p = r.res0; }
         // train on this step's solution (asynchronous; its loss is read at the next sync)
         if (status == FG_OK) {
@@ -1006,6 +1015,11 @@ int fg_mlp_debug_grad(fg_ctx *h, int nsamples, const float *feat, const float *t
 }
 
 int fg_mlp_nparam(void) { return mlp_nparam(); }
+
+int fg_mlp_debug_infer(fg_ctx *h, int n, const float *feat, float *out) {
+    if (!h || !h->c.mlp || !feat || !out || n <= 0) return FG_EINVAL;
+    return mlp_debug_infer(h->c, n, feat, out);
+}
 
 int fg_debug_wait_timeout(fg_ctx *h, int which) {
     if (!h || which < 0 || which > 1) return FG_EINVAL;

@@ -135,6 +135,13 @@ struct MixedArgs {
     const SegPar *seg;    // per-sample dt and c0 (nullptr: the scalars above)
     SegAcc *acc;          // per-sample accumulation over a run (nullable)
     const int *step_ctr;  // step index of the run (with acc)
+    // learned initial guess (single system): a candidate x and its tangent vectors beside
+    // the fallback in x; the first refinement residual is formed for both and the smaller
+    // one wins (cand_flag 1: the candidate), cand_res2 = {|r_cand|^2, |r_fallback|^2}
+    const double *cand_x, *cand_W;
+    double *cand_r;       // the candidate's residual [2 nn]
+    int *cand_flag;
+    double *cand_res2;
 };
 
 struct Ctx {
@@ -251,6 +258,10 @@ struct Ctx {
     bool step_open = false;  // ev[0] recorded by a step not yet closed by compute_all
     long long launches = 0;  // kernels launched by this context
     void *mlp = nullptr;     // learned initial guess (fg_mlp.cu)
+    // a candidate guess for the next FP32 + refinement solve to judge (set by the learned guess)
+    const double *cand_x = nullptr, *cand_W = nullptr;
+    double *cand_r = nullptr, *cand_res2 = nullptr;
+    int *cand_flag = nullptr;
     double *heff = nullptr;  // per-node BE/A (effective field), written when the learned guess is on
 
     // batch of independent samples packed as one block-diagonal system (fg_batch_*)
@@ -353,6 +364,8 @@ cudaError_t mlp_before_evolution(Ctx &c);
 double mlp_loss(const Ctx &c);
 int mlp_debug_grad(Ctx &c, int nsamples, const float *hx, const float *hy, float *w_out, float *g_out, float *loss);
 int mlp_nparam();
+int mlp_debug_infer(Ctx &c, int n, const float *hx, float *hy);
+bool mlp_take_timeout(Ctx &c);  // a tensor-core wait of the learned guess expired (then cleared)
 int batch_setup(Ctx &c, const std::vector<int4> &htet, const std::vector<int4> &htri);
 void batch_free(Ctx &c);
 int spin_setup(Ctx &c, const fg_mesh *m, const fg_region *regs, int nreg, const fg_tri_region *tregs, int ntreg,

@@ -102,9 +102,11 @@ __global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
         double res = 0.0, res0 = 0.0;
         bool done = false;  // this sample's solve has ended (status set)
         for (;;) {
-            // refinement residual r64 = b - K x (FP64, masked)
+            // refinement residual r64 = b - K x (FP64, masked); on the first pass with a
+            // candidate guess, also the candidate's residual (the referee of the learned guess)
+            const bool judge = nref == 0 && a.cand_x != nullptr && !multi;
             {
-                double rr = 0.0;
+                double rr = 0.0, rc = 0.0;
                 if (!done) {
                     auto row = [&](int i, bool valid, int sub) {
                         double y0 = 0, y1 = 0;
@@ -117,16 +119,49 @@ __global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
                             a.r64[2 * i + 1] = r1;
                             rr += r0 * r0 + r1 * r1;
                         }
+                        if (judge) {
+                            double z0 = 0, z1 = 0;
+                            apply_row_g<double, LPR>(valid, i, sub, a.Sptr, a.Scol, a.Sval, a.cand_W, a.ep, a.eq, a.A,
+                                                     a.Dl, c0, valid ? a.cand_x[2 * i] : 0.0,
+                                                     valid ? a.cand_x[2 * i + 1] : 0.0, z0, z1);
+                            if (valid && sub == 0) {
+                                const bool m = a.mag[i];
+                                const double r0 = m ? a.b[2 * i] - z0 : 0.0, r1 = m ? a.b[2 * i + 1] - z1 : 0.0;
+                                a.cand_r[2 * i] = r0;
+                                a.cand_r[2 * i + 1] = r1;
+                                rc += r0 * r0 + r1 * r1;
+                            }
+                        }
                     };
                     GROUP_ROWS(row)
                 }
-                double v1[1] = {rr};
-                block_store<1>(v1, a.partial, G);
+                double v2[2] = {rr, rc};
+                block_store<2>(v2, a.partial, G);
             }
             if (!grid_sync(a.bar)) goto timeout;
             {
-                double s2[1];
-                range_sum<1>(a.partial, G, sv.b0, sv.b1, s2);
+                double s2[2];
+                range_sum<2>(a.partial, G, sv.b0, sv.b1, s2);
+                if (judge && !done) {
+                    // the candidate replaces the fallback when its residual is smaller
+                    const bool take = s2[1] < s2[0];
+                    if (blockIdx.x == 0 && threadIdx.x == 0) {
+                        *a.cand_flag = take ? 1 : 0;
+                        a.cand_res2[0] = s2[1];
+                        a.cand_res2[1] = s2[0];
+                    }
+                    if (take) {
+                        SAMPLE_ROWS(i) {
+                            a.x[2 * i] = a.cand_x[2 * i];
+                            a.x[2 * i + 1] = a.cand_x[2 * i + 1];
+                            a.r64[2 * i] = a.cand_r[2 * i];
+                            a.r64[2 * i + 1] = a.cand_r[2 * i + 1];
+#pragma unroll
+                            for (int c = 0; c < 3; c++) a.W64[3 * i + c] = a.cand_W[3 * i + c];
+                        }
+                        s2[0] = s2[1];
+                    }
+                }
                 if (!done) res = block_once([=] { return sqrt(fabs(s2[0])); });
             }
             if (!done) {
@@ -456,6 +491,11 @@ cudaError_t launch_mixed(Ctx &c, double dt, double prefactor) {
     a.maxiter = c.opts.max_iter; a.refine_max = c.opts.refine_max;
     a.dt = dt; a.u0 = c.u[0]; a.u1 = c.u[1]; a.v1 = c.v[1];
     a.scale = 1.0 / c.mean_A;
+    a.cand_x = c.batch ? nullptr : c.cand_x;
+    a.cand_W = c.cand_W;
+    a.cand_r = c.cand_r;
+    a.cand_flag = c.cand_flag;
+    a.cand_res2 = c.cand_res2;
     a.nseg = 1;
     a.seg_node = a.seg_blk = nullptr;
     a.seg = nullptr;

@@ -10,17 +10,22 @@
 // so the candidate is v_e + scale * MLP(features), projected on the new tangent basis and
 // divided by gamma0. The reference's guess (previous v on the new basis,
 // src/linear_algebra.cpp:13-24) is the fallback and the referee: the candidate is used only
-// when its FP64 initial residual |b - K x| is smaller than the fallback's. The network is
-// trained online on (features, solved v) pairs with hand-written kernels: BF16 weights
-// (FP32 master copy, Adam), FP32 accumulation, deterministic fixed-order reductions.
+// when its FP64 initial residual |b - K x| is smaller than the fallback's (judged inside the
+// FP32 + refinement solver's first FP64 residual pass; by separate kernels on the FP64
+// path). Inference runs the network's three GEMMs on the tensor cores (BF16 operands, FP32
+// accumulation in tensor memory). The network is trained online on (features, solved v)
+// pairs with hand-written kernels: BF16 weights (FP32 master copy, Adam), FP32
+// accumulation, deterministic fixed-order reductions.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <vector>
 
 #include "fg_device.cuh"
 #include "fg_internal.h"
+#include "fg_tcgen05.cuh"
 
 namespace fg {
 
@@ -42,8 +47,11 @@ struct MlpState {
     double *vprev2 = nullptr;                               // v of the step before the previous one
     double *scale = nullptr;                                // RMS of the extrapolation correction
     double *spart = nullptr;                                // its block partials
+    int *tc_err = nullptr;                                  // FG_ETIMEDOUT from a tensor-core wait
+    double *rc = nullptr;                                   // the candidate's residual (judged in the solver)
     int nblk_train = 0, nblk_res = 0;
     bool primed = false;   // vprev2 holds a real previous velocity
+    bool timed_out = false;  // a tensor-core wait of the last inference expired
     long long t = 0;       // Adam steps
     long long steps = 0;   // training steps done
     double loss = 0.0;
@@ -100,65 +108,242 @@ __device__ __forceinline__ float tanh_sfu(float x) {
     return y;
 }
 
-// Inference: one thread per node, features formed in place (and stored for the training
-// when feat is given), weights staged in shared memory as FP32 (from BF16). Writes the
-// candidate x (2 per node) and its tangent vectors W.
-__global__ void __launch_bounds__(256) k_mlp_infer(int nn, const unsigned char *__restrict__ mag,
-                                                   const double *__restrict__ u0, const double *__restrict__ heff,
-                                                   const int *__restrict__ Sptr, const int *__restrict__ Scol,
-                                                   double inv_ms, double inv_v0, float *__restrict__ feat,
-                                                   const __nv_bfloat16 *__restrict__ w, const double *__restrict__ ep,
-                                                   const double *__restrict__ eq, const double *__restrict__ vprev,
-                                                   const double *__restrict__ vprev2, const double *__restrict__ scale,
-                                                   double *__restrict__ xm, double *__restrict__ Wm) {
-    __shared__ __align__(16) float sw[NPARAM];
-    for (int k = threadIdx.x; k < NPARAM; k += blockDim.x) sw[k] = bf(w, k);
+// ---- forward pass on the tensor cores --------------------------------------------
+// A tile of 128 nodes is the M = 128 side of three tcgen05.mma kind::f16 GEMMs with BF16
+// operands and FP32 accumulators in tensor memory:
+//   layer 1  D1[128 x 64] = X[128 x 16] W1^T      (12 features padded to K = 16), 1 MMA
+//   layer 2  D2[128 x 64] = H1[128 x 64] W2^T     4 MMAs of K = 16
+//   layer 3  D3[128 x 16] = H2[128 x 64] W3^T     (3 outputs padded to N = 16), 4 MMAs
+// Thread t of the CTA owns node t of the tile: it forms the node's features, writes its BF16
+// row of X, drains its row of D1 / D2 with tcgen05.ld (TMEM lane t), adds the bias, applies
+// tanh and writes its BF16 row of H for the next layer; one thread issues the MMAs.
+// Operands sit in shared memory in the no-swizzle K-major layout of 8-row x 16-byte core
+// matrices (LBO 128 bytes along K; SBO = bytes of one 8-row group). TMEM: D1 and D3 in
+// columns 0..63, D2 in 64..127.
+constexpr int TM = 128;        // nodes per tile
+constexpr int K1 = 16;         // layer-1 K (features padded)
+constexpr int NO3 = 16;        // layer-3 N (outputs padded)
+constexpr uint32_t TC_LBO = 128;
+constexpr uint32_t SBO_K16 = 2 * TC_LBO, SBO_K64 = 8 * TC_LBO;
+constexpr int A1_OFF = 0, A1_BYTES = TM * K1 * 2;                   // 4 KB
+constexpr int A2_OFF = A1_OFF + A1_BYTES, A2_BYTES = TM * NH * 2;   // 16 KB: H1, then H2
+constexpr int B1_OFF = A2_OFF + A2_BYTES, B1_BYTES = NH * K1 * 2;   // 2 KB
+constexpr int B2_OFF = B1_OFF + B1_BYTES, B2_BYTES = NH * NH * 2;   // 8 KB
+constexpr int B3_OFF = B2_OFF + B2_BYTES, B3_BYTES = NO3 * NH * 2;  // 2 KB
+constexpr int BIAS_OFF = B3_OFF + B3_BYTES;                         // b1, b2, b3 as FP32
+constexpr int TC_SMEM = BIAS_OFF + (NH + NH + NO3) * 4 + 1024;      // + alignment slack
+constexpr int TC_TMEM_COLS = 128;
+
+// Byte offset of element (row, k) in a K-major image whose 8-row groups are sbo bytes apart.
+__device__ __forceinline__ int kmaj(int row, int k, uint32_t sbo) {
+    return (row >> 3) * (int)sbo + (k >> 3) * (int)TC_LBO + (row & 7) * 16 + (k & 7) * 2;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+// Writes the 8 BF16 values v[0..7] (K = k0..k0+7 of one row) as one 16-byte store.
+__device__ __forceinline__ void store8(unsigned char *img, int row, int k0, uint32_t sbo, const float *v) {
+    uint4 q;
+    q.x = pack_bf16(v[0], v[1]);
+    q.y = pack_bf16(v[2], v[3]);
+    q.z = pack_bf16(v[4], v[5]);
+    q.w = pack_bf16(v[6], v[7]);
+    *reinterpret_cast<uint4 *>(img + kmaj(row, k0, sbo)) = q;
+}
+
+struct MlpTcArgs {
+    int nn;
+    const unsigned char *mag;
+    const double *u0, *heff;
+    const int *Sptr, *Scol;
+    double inv_ms, inv_v0;
+    float *feat;                 // features of every node for the training (nullable)
+    const __nv_bfloat16 *w;
+    const double *ep, *eq, *vprev, *vprev2, *scale;
+    double *xm, *Wm;             // candidate guess and its tangent vectors
+    const float *xin;            // caller-given feature rows instead of the state (checks)
+    float *yout;                 // with xin: the network's outputs [nn][3]
+    int *err;                    // FG_ETIMEDOUT after an expired wait
+};
+
+// Drains 16 TMEM columns of this thread's lane (row) into v[0..15].
+__device__ __forceinline__ void drain16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    tc::tmem_ld16(taddr, r);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int k = 0; k < 16; k++) v[k] = __uint_as_float(r[k]);
+}
+
+__global__ void __launch_bounds__(TM) k_mlp_infer_tc(MlpTcArgs a) {
+    using namespace tc;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char *A1 = sm + A1_OFF, *A2 = sm + A2_OFF, *B1 = sm + B1_OFF, *B2 = sm + B2_OFF, *B3 = sm + B3_OFF;
+    float *bias = reinterpret_cast<float *>(sm + BIAS_OFF);  // b1 [64], b2 [64], b3 [16]
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int bail;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // weights and biases (BF16 weights as they are, zero padding)
+    for (int e = tid; e < NH * K1; e += TM) {
+        const int j = e / K1, k = e % K1;
+        *reinterpret_cast<__nv_bfloat16 *>(B1 + kmaj(j, k, SBO_K16)) =
+            k < NF ? a.w[OFF_W1 + j * NF + k] : __float2bfloat16(0.f);
+    }
+    for (int e = tid; e < NH * NH; e += TM) {
+        const int j = e / NH, k = e % NH;
+        *reinterpret_cast<__nv_bfloat16 *>(B2 + kmaj(j, k, SBO_K64)) = a.w[OFF_W2 + j * NH + k];
+    }
+    for (int e = tid; e < NO3 * NH; e += TM) {
+        const int j = e / NH, k = e % NH;
+        *reinterpret_cast<__nv_bfloat16 *>(B3 + kmaj(j, k, SBO_K64)) =
+            j < NO ? a.w[OFF_W3 + j * NH + k] : __float2bfloat16(0.f);
+    }
+    for (int e = tid; e < NH + NH + NO3; e += TM)
+        bias[e] = e < NH ? bf(a.w, OFF_B1 + e) : e < 2 * NH ? bf(a.w, OFF_B2 + e - NH)
+                                                             : (e - 2 * NH < NO ? bf(a.w, OFF_B3 + e - 2 * NH) : 0.f);
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        bail = 0;
+        fence_mbar_init();
+    }
+    if (warp == 0) tmem_alloc(&tmem_base, TC_TMEM_COLS);
+    fence_proxy_async();
+    tc_fence_before();
     __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nn) return;
-    float x[NF];
-    node_features(i, mag, u0, heff, vprev, Sptr, Scol, inv_ms, inv_v0, x);
-    if (feat)
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
+    const uint32_t sA1 = smem_u32(A1), sA2 = smem_u32(A2), sB1 = smem_u32(B1), sB2 = smem_u32(B2),
+                   sB3 = smem_u32(B3);
+    uint32_t parity = 0;
+    // all threads reach this after their shared-memory writes: the issuer's MMAs see them
+    auto issue_and_wait = [&](int layer) -> bool {
+        fence_proxy_async();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            if (layer == 1) {
+                mma_bf16(tmem, sdesc_kmajor(sA1, TC_LBO, SBO_K16), sdesc_kmajor(sB1, TC_LBO, SBO_K16),
+                         idesc_bf16(TM, NH), 0u);
+            } else {
+                const uint32_t d = layer == 2 ? tmem + NH : tmem;
+                const uint32_t sB = layer == 2 ? sB2 : sB3;
+                const uint32_t id = idesc_bf16(TM, layer == 2 ? NH : NO3);
 #pragma unroll
-        for (int k = 0; k < NF; k++) feat[(size_t)i * NF + k] = x[k];
-    if (!mag[i]) {
-        xm[2 * i] = xm[2 * i + 1] = 0.0;
-        Wm[3 * i] = Wm[3 * i + 1] = Wm[3 * i + 2] = 0.0;
-        return;
+                for (int k = 0; k < NH / 16; k++)
+                    mma_bf16(d, sdesc_kmajor(sA2 + 256 * k, TC_LBO, SBO_K64), sdesc_kmajor(sB + 256 * k, TC_LBO, SBO_K64),
+                             id, k > 0 ? 1u : 0u);
+            }
+            mma_commit(&bar);
+        }
+        const bool ok = mbar_wait(&bar, parity, a.err, &bail);
+        if (!ok && tid == 0) mbar_drain(&bar, parity);  // the MMAs still own TMEM and the operands
+        parity ^= 1u;
+        const bool all = __syncthreads_and(ok) != 0;
+        tc_fence_after();
+        return all;
+    };
+    const int ntiles = (a.nn + TM - 1) / TM;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int i = tile * TM + tid;
+        const bool live = i < a.nn;
+        float x[NF];
+        if (a.xin) {
+#pragma unroll
+            for (int k = 0; k < NF; k++) x[k] = live ? a.xin[(size_t)i * NF + k] : 0.f;
+        } else if (live) {
+            node_features(i, a.mag, a.u0, a.heff, a.vprev, a.Sptr, a.Scol, a.inv_ms, a.inv_v0, x);
+            if (a.feat)
+#pragma unroll
+                for (int k = 0; k < NF; k++) a.feat[(size_t)i * NF + k] = x[k];
+        } else {
+#pragma unroll
+            for (int k = 0; k < NF; k++) x[k] = 0.f;
+        }
+        {
+            const float x2[8] = {x[8], x[9], x[10], x[11], 0.f, 0.f, 0.f, 0.f};
+            store8(A1, tid, 0, SBO_K16, x);
+            store8(A1, tid, 8, SBO_K16, x2);
+        }
+        if (!issue_and_wait(1)) break;
+        // H1 = tanh(D1 + b1) -> A2
+#pragma unroll
+        for (int c = 0; c < NH / 16; c++) {
+            float v[16];
+            drain16(lane_addr + 16 * c, v);
+#pragma unroll
+            for (int k = 0; k < 16; k++) v[k] = tanh_sfu(v[k] + bias[16 * c + k]);
+            store8(A2, tid, 16 * c, SBO_K64, v);
+            store8(A2, tid, 16 * c + 8, SBO_K64, v + 8);
+        }
+        if (!issue_and_wait(2)) break;
+        // H2 = tanh(D2 + b2) -> A2 (layer 2's MMAs have completed: A2 is free)
+#pragma unroll
+        for (int c = 0; c < NH / 16; c++) {
+            float v[16];
+            drain16(lane_addr + NH + 16 * c, v);
+#pragma unroll
+            for (int k = 0; k < 16; k++) v[k] = tanh_sfu(v[k] + bias[NH + 16 * c + k]);
+            store8(A2, tid, 16 * c, SBO_K64, v);
+            store8(A2, tid, 16 * c + 8, SBO_K64, v + 8);
+        }
+        if (!issue_and_wait(3)) break;
+        float o[16];
+        drain16(lane_addr, o);
+        const float o0 = o[0] + bias[2 * NH], o1 = o[1] + bias[2 * NH + 1], o2 = o[2] + bias[2 * NH + 2];
+        if (!live) continue;
+        if (a.xin) {
+            a.yout[3 * (size_t)i] = o0;
+            a.yout[3 * (size_t)i + 1] = o1;
+            a.yout[3 * (size_t)i + 2] = o2;
+            continue;
+        }
+        if (!a.mag[i]) {
+            a.xm[2 * i] = a.xm[2 * i + 1] = 0.0;
+            a.Wm[3 * i] = a.Wm[3 * i + 1] = a.Wm[3 * i + 2] = 0.0;
+            continue;
+        }
+        // v = 2 v_prev - v_prev2 + scale * o; x = (v . ep, v . eq) / gamma0
+        const double sc = a.scale[0];
+        const double oo[3] = {o0, o1, o2};
+        double v[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) v[c] = 2.0 * a.vprev[3 * i + c] - a.vprev2[3 * i + c] + sc * oo[c];
+        const double e0 = a.ep[3 * i], e1 = a.ep[3 * i + 1], e2 = a.ep[3 * i + 2];
+        const double q0 = a.eq[3 * i], q1 = a.eq[3 * i + 1], q2 = a.eq[3 * i + 2];
+        const double xp = (v[0] * e0 + v[1] * e1 + v[2] * e2) / FG_GAMMA0;
+        const double xq = (v[0] * q0 + v[1] * q1 + v[2] * q2) / FG_GAMMA0;
+        a.xm[2 * i] = xp;
+        a.xm[2 * i + 1] = xq;
+        a.Wm[3 * i] = xp * e0 + xq * q0;
+        a.Wm[3 * i + 1] = xp * e1 + xq * q1;
+        a.Wm[3 * i + 2] = xp * e2 + xq * q2;
     }
-    float h1[NH];
-#pragma unroll
-    for (int j = 0; j < NH; j++) {
-        float z = sw[OFF_B1 + j];
-#pragma unroll
-        for (int k = 0; k < NF; k++) z += sw[OFF_W1 + j * NF + k] * x[k];
-        h1[j] = tanh_sfu(z);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, TC_TMEM_COLS);
     }
-    float o0 = sw[OFF_B3], o1 = sw[OFF_B3 + 1], o2 = sw[OFF_B3 + 2];
-    for (int j = 0; j < NH; j++) {
-        float z = sw[OFF_B2 + j];
-#pragma unroll
-        for (int k = 0; k < NH; k++) z += sw[OFF_W2 + j * NH + k] * h1[k];
-        const float h2 = tanh_sfu(z);
-        o0 += sw[OFF_W3 + j] * h2;
-        o1 += sw[OFF_W3 + NH + j] * h2;
-        o2 += sw[OFF_W3 + 2 * NH + j] * h2;
+}
+
+static cudaError_t launch_mlp_infer_tc(Ctx &c, const MlpTcArgs &a) {
+    static bool attr_set = false;  // per process; the attribute is a property of the function
+    if (!attr_set) {
+        const cudaError_t e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
     }
-    // v = 2 v_prev - v_prev2 + scale * o; x = (v . ep, v . eq) / gamma0
-    const double sc = scale[0];
-    double v[3];
-    const double oo[3] = {o0, o1, o2};
-#pragma unroll
-    for (int c = 0; c < 3; c++) v[c] = 2.0 * vprev[3 * i + c] - vprev2[3 * i + c] + sc * oo[c];
-    const double e0 = ep[3 * i], e1 = ep[3 * i + 1], e2 = ep[3 * i + 2];
-    const double q0 = eq[3 * i], q1 = eq[3 * i + 1], q2 = eq[3 * i + 2];
-    const double xp = (v[0] * e0 + v[1] * e1 + v[2] * e2) / FG_GAMMA0;
-    const double xq = (v[0] * q0 + v[1] * q1 + v[2] * q2) / FG_GAMMA0;
-    xm[2 * i] = xp;
-    xm[2 * i + 1] = xq;
-    Wm[3 * i] = xp * e0 + xq * q0;
-    Wm[3 * i + 1] = xp * e1 + xq * q1;
-    Wm[3 * i + 2] = xp * e2 + xq * q2;
+    const int ntiles = (a.nn + TM - 1) / TM;
+    const int grid = std::max(1, std::min(ntiles, 4 * c.nsm));  // 4 CTAs of 128 TMEM columns per SM
+    k_mlp_infer_tc<<<grid, TM, TC_SMEM, c.stream>>>(a);
+    return cudaGetLastError();
 }
 
 // |b - K x|^2 for the candidate and for the fallback guess (FP64, masked), block partials.
@@ -210,138 +395,285 @@ __device__ __forceinline__ uint32_t hash32(uint64_t x) {
     return (uint32_t)(x ^ (x >> 31));
 }
 
-// One training minibatch: each block takes SB nodes drawn by a counter-based hash,
-// runs forward and backward with activations in shared memory and writes its summed
-// gradient (per parameter, summed over its samples in a fixed order) and loss.
-__global__ void __launch_bounds__(256) k_mlp_grad(int nmag, const int *__restrict__ mag_nodes,
-                                                  const float *__restrict__ feat, const double *__restrict__ vtrue,
-                                                  const double *__restrict__ vprev, const double *__restrict__ vprev2,
-                                                  const double *__restrict__ scale,
-                                                  const __nv_bfloat16 *__restrict__ w, uint64_t seed,
-                                                  float inv_batch, float *__restrict__ gpart,
-                                                  float *__restrict__ lpart, const float *__restrict__ xin,
-                                                  const float *__restrict__ yin) {
-    extern __shared__ float sm[];
-    float *sw = sm;                 // NPARAM
-    float *X = sw + NPARAM;         // SB x NF
-    float *H1 = X + SB * NF;        // SB x NH
-    float *H2 = H1 + SB * NH;       // SB x NH
-    float *D3 = H2 + SB * NH;       // SB x NO
-    float *Y = D3 + SB * NO;        // SB x NO
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int k = tid; k < NPARAM; k += nt) sw[k] = bf(w, k);
-    for (int s = tid; s < SB; s += nt) {
-        if (xin) {  // caller-given samples (gradient checks)
-            const size_t g = (size_t)blockIdx.x * SB + s;
+// One training minibatch tile on the tensor cores: each CTA takes SB = 128 nodes drawn by a
+// counter-based hash (thread s owns sample s), runs the forward pass of the inference
+// kernel (BF16 operand images X, H1, H2 kept in shared memory) and the backward pass, and
+// writes its summed gradient (per parameter, a fixed summation order) and loss:
+//   d3 = 2 (o - y) / (batch x 3)                                        FP32, per sample
+//   [gW3 | gb3] [3 x 65]  = d3^T [H2 | 1]         M = 128 (rows 0..2 used), N = 80, K = 128 samples
+//   delta2 = (d3 W3) (1 - h2^2)                                         CUDA cores (K = 3)
+//   [gW2 | gb2] [64 x 65] = delta2^T [H1 | 1]     M = 128 (rows 0..63 used), N = 80, K = 128
+//   delta1 = (delta2 W2) (1 - h1^2)               M = 128 samples, N = 64, K = 64
+//   [gW1 | gb1] [64 x 13] = delta1^T [X | 1]      M = 128 (rows 0..63 used), N = 16, K = 128
+// The transposed operands (delta^T with samples along K, and [H | 1]^T, [X | 1]^T) are
+// written column by column, each thread its own sample; the ones rows make the bias
+// gradients come out of the same MMAs. Rows of D that are not read never need clearing:
+// an output row depends on its own row of A only. BF16 operands, FP32 accumulation in TMEM.
+constexpr uint32_t SBO_K128 = 16 * TC_LBO;
+constexpr int NB80 = 80;  // N of the [H | 1] operands (65 used)
+constexpr int G_A1 = 0;                          // X [128 x 16]
+constexpr int G_H1 = G_A1 + TM * K1 * 2;         // H1 [128 x 64]
+constexpr int G_H2 = G_H1 + TM * NH * 2;         // H2 [128 x 64]
+constexpr int G_D2 = G_H2 + TM * NH * 2;         // delta2 [128 x 64]
+constexpr int G_B1 = G_D2 + TM * NH * 2;         // W1 [64 x 16]
+constexpr int G_B2 = G_B1 + NH * K1 * 2;         // W2 [64 x 64]
+constexpr int G_B3 = G_B2 + NH * NH * 2;         // W3 [16 x 64]
+constexpr int G_B2T = G_B3 + NO3 * NH * 2;       // W2^T [64 x 64]
+constexpr int G_AT = G_B2T + NH * NH * 2;        // delta^T [128 x 128 samples]
+constexpr int G_H1T = G_AT + 128 * SB * 2;       // [H1 | 1]^T [80 x 128 samples]
+constexpr int G_H2T = G_H1T + NB80 * SB * 2;     // [H2 | 1]^T [80 x 128 samples]
+constexpr int G_XT = G_H2T + NB80 * SB * 2;      // [X | 1]^T [16 x 128 samples]
+constexpr int G_F32 = G_XT + K1 * SB * 2;        // b1, b2, b3 (16), W3 [3][64] as FP32, loss [128]
+constexpr int GRAD_SMEM = G_F32 + (NH + NH + NO3 + NO * NH + SB) * 4 + 1024;
+constexpr int GRAD_TMEM_COLS = 256;
+
+__device__ __forceinline__ void store_bf16(unsigned char *img, int row, int k, uint32_t sbo, float v) {
+    *reinterpret_cast<__nv_bfloat16 *>(img + kmaj(row, k, sbo)) = __float2bfloat16(v);
+}
+__device__ __forceinline__ float load_bf16(const unsigned char *img, int row, int k, uint32_t sbo) {
+    return __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(img + kmaj(row, k, sbo)));
+}
+
+__global__ void __launch_bounds__(SB) k_mlp_grad_tc(int nmag, const int *__restrict__ mag_nodes,
+                                                    const float *__restrict__ feat, const double *__restrict__ vtrue,
+                                                    const double *__restrict__ vprev,
+                                                    const double *__restrict__ vprev2,
+                                                    const double *__restrict__ scale,
+                                                    const __nv_bfloat16 *__restrict__ w, uint64_t seed,
+                                                    float inv_batch, float *__restrict__ gpart,
+                                                    float *__restrict__ lpart, const float *__restrict__ xin,
+                                                    const float *__restrict__ yin, int *err) {
+    using namespace tc;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char *A1 = sm + G_A1, *H1 = sm + G_H1, *H2 = sm + G_H2, *D2 = sm + G_D2, *B1 = sm + G_B1,
+                  *B2 = sm + G_B2, *B3 = sm + G_B3, *B2T = sm + G_B2T, *AT = sm + G_AT, *H1T = sm + G_H1T,
+                  *H2T = sm + G_H2T, *XT = sm + G_XT;
+    float *bias = reinterpret_cast<float *>(sm + G_F32);  // b1 [64], b2 [64], b3 [16]
+    float *w3f = bias + NH + NH + NO3;                    // W3 [3][64]
+    float *red = w3f + NO * NH;                           // loss per sample
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int bail;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int e = tid; e < NH * K1; e += SB) {
+        const int j = e / K1, k = e % K1;
+        *reinterpret_cast<__nv_bfloat16 *>(B1 + kmaj(j, k, SBO_K16)) =
+            k < NF ? w[OFF_W1 + j * NF + k] : __float2bfloat16(0.f);
+    }
+    for (int e = tid; e < NH * NH; e += SB) {
+        const int j = e / NH, k = e % NH;
+        const __nv_bfloat16 v = w[OFF_W2 + j * NH + k];
+        *reinterpret_cast<__nv_bfloat16 *>(B2 + kmaj(j, k, SBO_K64)) = v;   // rows j (outputs), K = k
+        *reinterpret_cast<__nv_bfloat16 *>(B2T + kmaj(k, j, SBO_K64)) = v;  // rows k (inputs), K = j
+    }
+    for (int e = tid; e < NO3 * NH; e += SB) {
+        const int j = e / NH, k = e % NH;
+        *reinterpret_cast<__nv_bfloat16 *>(B3 + kmaj(j, k, SBO_K64)) =
+            j < NO ? w[OFF_W3 + j * NH + k] : __float2bfloat16(0.f);
+    }
+    for (int e = tid; e < NH + NH + NO3; e += SB)
+        bias[e] = e < NH ? bf(w, OFF_B1 + e) : e < 2 * NH ? bf(w, OFF_B2 + e - NH)
+                                                           : (e - 2 * NH < NO ? bf(w, OFF_B3 + e - 2 * NH) : 0.f);
+    for (int e = tid; e < NO * NH; e += SB) w3f[e] = bf(w, OFF_W3 + e);
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        bail = 0;
+        fence_mbar_init();
+    }
+    if (warp == 0) tmem_alloc(&tmem_base, GRAD_TMEM_COLS);
+    // this thread's sample: features and target
+    float x[NF], y[NO];
+    if (xin) {
+        const size_t g = (size_t)blockIdx.x * SB + tid;
 #pragma unroll
-            for (int k = 0; k < NF; k++) X[s * NF + k] = xin[g * NF + k];
+        for (int k = 0; k < NF; k++) x[k] = xin[g * NF + k];
 #pragma unroll
-            for (int c = 0; c < NO; c++) Y[s * NO + c] = yin[g * NO + c];
-            continue;
-        }
-        const int node = mag_nodes[hash32(seed * 1000003ull + (uint64_t)blockIdx.x * SB + s) % (uint32_t)nmag];
+        for (int c = 0; c < NO; c++) y[c] = yin[g * NO + c];
+    } else {
+        const int node = mag_nodes[hash32(seed * 1000003ull + (uint64_t)blockIdx.x * SB + tid) % (uint32_t)nmag];
 #pragma unroll
-        for (int k = 0; k < NF; k++) X[s * NF + k] = feat[(size_t)node * NF + k];
+        for (int k = 0; k < NF; k++) x[k] = feat[(size_t)node * NF + k];
         const double isc = 1.0 / scale[0];
 #pragma unroll
         for (int c = 0; c < NO; c++) {
             const size_t q = 3 * (size_t)node + c;
-            Y[s * NO + c] = (float)((vtrue[q] - (2.0 * vprev[q] - vprev2[q])) * isc);
+            y[c] = (float)((vtrue[q] - (2.0 * vprev[q] - vprev2[q])) * isc);
         }
     }
-    __syncthreads();
-    for (int e = tid; e < SB * NH; e += nt) {
-        const int s = e / NH, j = e % NH;
-        float z = sw[OFF_B1 + j];
+    {
+        const float x2[8] = {x[8], x[9], x[10], x[11], 0.f, 0.f, 0.f, 0.f};
+        store8(A1, tid, 0, SBO_K16, x);
+        store8(A1, tid, 8, SBO_K16, x2);
 #pragma unroll
-        for (int k = 0; k < NF; k++) z += sw[OFF_W1 + j * NF + k] * X[s * NF + k];
-        H1[e] = tanhf(z);
+        for (int k = 0; k < NF; k++) store_bf16(XT, k, tid, SBO_K128, x[k]);
+        store_bf16(XT, NF, tid, SBO_K128, 1.0f);  // ones row: the bias gradient gb1
+        store_bf16(H1T, NH, tid, SBO_K128, 1.0f);
+        store_bf16(H2T, NH, tid, SBO_K128, 1.0f);
     }
+    fence_proxy_async();
+    tc_fence_before();
     __syncthreads();
-    for (int e = tid; e < SB * NH; e += nt) {
-        const int s = e / NH, j = e % NH;
-        float z = sw[OFF_B2 + j];
-        for (int k = 0; k < NH; k++) z += sw[OFF_W2 + j * NH + k] * H1[s * NH + k];
-        H2[e] = tanhf(z);
-    }
-    __syncthreads();
-    float lsum = 0.0f;
-    for (int e = tid; e < SB * NO; e += nt) {
-        const int s = e / NO, c = e % NO;
-        float o = sw[OFF_B3 + c];
-        for (int k = 0; k < NH; k++) o += sw[OFF_W3 + c * NH + k] * H2[s * NH + k];
-        const float d = o - Y[e];
-        D3[e] = 2.0f * d * inv_batch;
-        lsum += d * d;
-    }
-    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
+    uint32_t parity = 0;
+    const uint32_t sA1 = smem_u32(A1), sH1 = smem_u32(H1), sH2 = smem_u32(H2), sD2 = smem_u32(D2),
+                   sB1 = smem_u32(B1), sB2 = smem_u32(B2), sB3 = smem_u32(B3), sB2T = smem_u32(B2T),
+                   sAT = smem_u32(AT), sH1T = smem_u32(H1T), sH2T = smem_u32(H2T), sXT = smem_u32(XT);
+    // D (+)= A B over K = 16 ksteps; A and B K-major images with 8-row groups sboA / sboB apart
+    auto gemm = [&](uint32_t d, uint32_t sa, uint32_t sboA, uint32_t sb, uint32_t sboB, int n, int ksteps) {
+        for (int k = 0; k < ksteps; k++)
+            mma_bf16(d, sdesc_kmajor(sa + 256 * k, TC_LBO, sboA), sdesc_kmajor(sb + 256 * k, TC_LBO, sboB),
+                     idesc_bf16(TM, n), k > 0 ? 1u : 0u);
+    };
+    // all threads: make the shared-memory writes visible, issue (thread 0), wait for the MMAs
+    auto sync_issue_wait = [&](int stage) -> bool {
+        fence_proxy_async();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            if (stage == 1) gemm(tmem, sA1, SBO_K16, sB1, SBO_K16, NH, 1);
+            else if (stage == 2) gemm(tmem + 64, sH1, SBO_K64, sB2, SBO_K64, NH, 4);
+            else if (stage == 3) gemm(tmem + 128, sH2, SBO_K64, sB3, SBO_K64, NO3, 4);
+            else if (stage == 4) gemm(tmem + 144, sAT, SBO_K128, sH2T, SBO_K128, NB80, 8);  // gW3 | gb3
+            else if (stage == 5) {
+                gemm(tmem, sAT, SBO_K128, sH1T, SBO_K128, NB80, 8);      // gW2 | gb2
+                gemm(tmem + 80, sD2, SBO_K64, sB2T, SBO_K64, NH, 4);     // delta2 W2
+            } else {
+                gemm(tmem + 144, sAT, SBO_K128, sXT, SBO_K128, K1, 8);   // gW1 | gb1
+            }
+            mma_commit(&bar);
+        }
+        const bool ok = mbar_wait(&bar, parity, err, &bail);
+        if (!ok && tid == 0) mbar_drain(&bar, parity);
+        parity ^= 1u;
+        const bool all = __syncthreads_and(ok) != 0;
+        tc_fence_after();
+        return all;
+    };
     float *G = gpart + (size_t)blockIdx.x * NPARAM;
-    // layer 3 gradients
-    for (int p = tid; p < NO * NH + NO; p += nt) {
-        float g = 0.0f;
-        if (p < NO * NH) {
-            const int c = p / NH, k = p % NH;
-            for (int s = 0; s < SB; s++) g += D3[s * NO + c] * H2[s * NH + k];
-            G[OFF_W3 + p] = g;
-        } else {
-            const int c = p - NO * NH;
-            for (int s = 0; s < SB; s++) g += D3[s * NO + c];
-            G[OFF_B3 + c] = g;
-        }
-    }
-    __syncthreads();
-    // delta2 = (W3^T d3) * (1 - h2^2), in place of H2
-    for (int e = tid; e < SB * NH; e += nt) {
-        const int s = e / NH, k = e % NH;
-        float d = 0.0f;
+    float lsum = 0.f;
+    do {
+        if (!sync_issue_wait(1)) break;
 #pragma unroll
-        for (int c = 0; c < NO; c++) d += sw[OFF_W3 + c * NH + k] * D3[s * NO + c];
-        const float h = H2[e];
-        H2[e] = d * (1.0f - h * h);
-    }
-    __syncthreads();
-    for (int p = tid; p < NH * NH + NH; p += nt) {
-        float g = 0.0f;
-        if (p < NH * NH) {
-            const int j = p / NH, k = p % NH;
-            for (int s = 0; s < SB; s++) g += H2[s * NH + j] * H1[s * NH + k];
-            G[OFF_W2 + p] = g;
-        } else {
-            const int j = p - NH * NH;
-            for (int s = 0; s < SB; s++) g += H2[s * NH + j];
-            G[OFF_B2 + j] = g;
+        for (int c = 0; c < NH / 16; c++) {  // H1 = tanh(D1 + b1)
+            float v[16];
+            drain16(lane_addr + 16 * c, v);
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                v[k] = tanh_sfu(v[k] + bias[16 * c + k]);
+                store_bf16(H1T, 16 * c + k, tid, SBO_K128, v[k]);
+            }
+            store8(H1, tid, 16 * c, SBO_K64, v);
+            store8(H1, tid, 16 * c + 8, SBO_K64, v + 8);
         }
-    }
-    __syncthreads();
-    // delta1 = (W2^T delta2) * (1 - h1^2), in place of H1
-    for (int e = tid; e < SB * NH; e += nt) {
-        const int s = e / NH, k = e % NH;
-        float d = 0.0f;
-        for (int j = 0; j < NH; j++) d += sw[OFF_W2 + j * NH + k] * H2[s * NH + j];
-        const float h = H1[e];
-        H1[e] = d * (1.0f - h * h);
-    }
-    __syncthreads();
-    for (int p = tid; p < NH * NF + NH; p += nt) {
-        float g = 0.0f;
-        if (p < NH * NF) {
-            const int j = p / NF, k = p % NF;
-            for (int s = 0; s < SB; s++) g += H1[s * NH + j] * X[s * NF + k];
-            G[OFF_W1 + p] = g;
-        } else {
-            const int j = p - NH * NF;
-            for (int s = 0; s < SB; s++) g += H1[s * NH + j];
-            G[OFF_B1 + j] = g;
+        if (!sync_issue_wait(2)) break;
+#pragma unroll
+        for (int c = 0; c < NH / 16; c++) {  // H2 = tanh(D2 + b2)
+            float v[16];
+            drain16(lane_addr + 64 + 16 * c, v);
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                v[k] = tanh_sfu(v[k] + bias[NH + 16 * c + k]);
+                store_bf16(H2T, 16 * c + k, tid, SBO_K128, v[k]);
+            }
+            store8(H2, tid, 16 * c, SBO_K64, v);
+            store8(H2, tid, 16 * c + 8, SBO_K64, v + 8);
         }
-    }
+        if (!sync_issue_wait(3)) break;
+        float d3[NO];
+        {
+            float o[16];
+            drain16(lane_addr + 128, o);
+#pragma unroll
+            for (int c = 0; c < NO; c++) {
+                const float d = o[c] + bias[2 * NH + c] - y[c];
+                lsum += d * d;
+                d3[c] = 2.0f * d * inv_batch;
+                store_bf16(AT, c, tid, SBO_K128, d3[c]);
+            }
+        }
+        // delta2 = (d3 W3) (1 - h2^2) with this sample's BF16 h2
+#pragma unroll 4
+        for (int k0 = 0; k0 < NH; k0 += 8) {
+            float v[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int k = k0 + q;
+                const float h = load_bf16(H2, tid, k, SBO_K64);
+                v[q] = (d3[0] * w3f[k] + d3[1] * w3f[NH + k] + d3[2] * w3f[2 * NH + k]) * (1.0f - h * h);
+            }
+            store8(D2, tid, k0, SBO_K64, v);
+        }
+        if (!sync_issue_wait(4)) break;
+        if (warp == 0) {  // rows 0..2 of [gW3 | gb3]
+            float g[16];
+#pragma unroll
+            for (int c = 0; c < 5; c++) {
+                drain16(lane_addr + 144 + 16 * c, g);
+                if (tid < NO)
+#pragma unroll
+                    for (int k = 0; k < 16; k++) {
+                        const int col = 16 * c + k;
+                        if (col < NH) G[OFF_W3 + tid * NH + col] = g[k];
+                        else if (col == NH) G[OFF_B3 + tid] = g[k];
+                    }
+            }
+        }
+        // delta2^T into AT (the gW3 MMAs have read it)
+#pragma unroll 4
+        for (int k = 0; k < NH; k++) store_bf16(AT, k, tid, SBO_K128, load_bf16(D2, tid, k, SBO_K64));
+        if (!sync_issue_wait(5)) break;
+        if (warp < 2) {  // rows 0..63 of [gW2 | gb2]
+            float g[16];
+#pragma unroll
+            for (int c = 0; c < 5; c++) {
+                drain16(lane_addr + 16 * c, g);
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                    const int col = 16 * c + k;
+                    if (col < NH) G[OFF_W2 + tid * NH + col] = g[k];
+                    else if (col == NH) G[OFF_B2 + tid] = g[k];
+                }
+            }
+        }
+        // delta1 = (delta2 W2) (1 - h1^2), transposed into AT (the gW2 MMAs have read it)
+#pragma unroll
+        for (int c = 0; c < NH / 16; c++) {
+            float v[16];
+            drain16(lane_addr + 80 + 16 * c, v);
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                const float h = load_bf16(H1, tid, 16 * c + k, SBO_K64);
+                store_bf16(AT, 16 * c + k, tid, SBO_K128, v[k] * (1.0f - h * h));
+            }
+        }
+        if (!sync_issue_wait(6)) break;
+        if (warp < 2) {  // rows 0..63 of [gW1 | gb1]
+            float g[16];
+            drain16(lane_addr + 144, g);
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                if (k < NF) G[OFF_W1 + tid * NF + k] = g[k];
+                else if (k == NF) G[OFF_B1 + tid] = g[k];
+            }
+        }
+    } while (false);
     // loss partial (fixed-order block reduction)
-    __shared__ float red[256];
     red[tid] = lsum;
     __syncthreads();
     if (tid == 0) {
         float t = 0.0f;
-        for (int k = 0; k < nt; k++) t += red[k];
+        for (int k = 0; k < SB; k++) t += red[k];
         lpart[blockIdx.x] = t;
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, GRAD_TMEM_COLS);
     }
 }
 
@@ -435,6 +767,9 @@ int mlp_create(Ctx &c) {
     if (cudaMalloc(&s->vprev2, 3 * (size_t)c.nn * sizeof(double)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->scale, sizeof(double)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->spart, (size_t)s->nblk_res * sizeof(double)) != cudaSuccess) return FG_ECUDA;
+    if (cudaMalloc(&s->tc_err, sizeof(int)) != cudaSuccess) return FG_ECUDA;
+    if (cudaMalloc(&s->rc, 2 * (size_t)c.nn * sizeof(double)) != cudaSuccess) return FG_ECUDA;
+    cudaMemset(s->tc_err, 0, sizeof(int));
     {
         const double one = FG_GAMMA0 * c.ms_ref * 1e-3;
         cudaMemcpy(s->scale, &one, sizeof(double), cudaMemcpyHostToDevice);
@@ -446,8 +781,7 @@ int mlp_create(Ctx &c) {
     cudaMemset(s->m1, 0, NPARAM * sizeof(float));
     cudaMemset(s->m2, 0, NPARAM * sizeof(float));
     cudaMemset(s->flag, 0, sizeof(int));
-    const int smem = (NPARAM + SB * NF + 2 * SB * NH + 2 * SB * NO) * (int)sizeof(float);
-    if (cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_mlp_grad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, GRAD_SMEM) != cudaSuccess)
         return FG_ECUDA;
     return cudaGetLastError() == cudaSuccess ? FG_OK : FG_ECUDA;
 }
@@ -456,7 +790,7 @@ void mlp_free(Ctx &c) {
     MlpState *s = static_cast<MlpState *>(c.mlp);
     if (!s) return;
     void *p[] = {s->master, s->m1, s->m2, s->w, s->feat, s->gpart, s->lpart, s->xm, s->Wm, s->rpart, s->flag,
-                 s->res2, s->vprev2, s->scale, s->spart};
+                 s->res2, s->vprev2, s->scale, s->spart, s->tc_err, s->rc};
     for (void *q : p)
         if (q) cudaFree(q);
     if (s->hloss) cudaFreeHost(s->hloss);
@@ -483,21 +817,34 @@ cudaError_t mlp_before_solve(Ctx &c, double c0, bool use, bool train) {
         cudaMemcpyAsync(s->vprev2, c.v[0], 3 * (size_t)c.nn * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
         s->primed = true;
     }
-    k_mlp_infer<<<nb(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.mag, c.u[0], c.heff, c.Sptr, c.Scol, 1.0 / c.ms_ref,
-                                                      1.0 / v0_scale(c), train ? s->feat : nullptr, s->w, c.ep, c.eq,
-                                                      c.v[0], s->vprev2, s->scale, s->xm, s->Wm);
+    MlpTcArgs a{};
+    a.nn = c.nn; a.mag = c.mag; a.u0 = c.u[0]; a.heff = c.heff; a.Sptr = c.Sptr; a.Scol = c.Scol;
+    a.inv_ms = 1.0 / c.ms_ref; a.inv_v0 = 1.0 / v0_scale(c); a.feat = train ? s->feat : nullptr;
+    a.w = s->w; a.ep = c.ep; a.eq = c.eq; a.vprev = c.v[0]; a.vprev2 = s->vprev2; a.scale = s->scale;
+    a.xm = s->xm; a.Wm = s->Wm; a.xin = nullptr; a.yout = nullptr; a.err = s->tc_err;
+    cudaError_t e = launch_mlp_infer_tc(c, a);
+    if (e != cudaSuccess) return e;
+    c.launches += 1;
+    if (c.opts.precision == FG_PREC_FP32_REFINE && !c.batch) {
+        // the FP32 + refinement solver judges the candidate on its first FP64 residual
+        c.cand_x = s->xm;
+        c.cand_W = s->Wm;
+        c.cand_r = s->rc;
+        c.cand_flag = s->flag;
+        c.cand_res2 = s->res2;
+        return cudaSuccess;
+    }
     k_resid2<<<s->nblk_res, 256, 0, c.stream>>>(c.nn, c.Sptr, c.Scol, c.Sval, c.ep, c.eq, c.A, c.Dl, c.mag, c0,
                                                 c.rhs, s->xm, s->Wm, c.x, c.W, s->rpart);
     k_choose<<<1, 32, 0, c.stream>>>(s->nblk_res, s->rpart, s->flag, s->res2);
     k_take<<<nb(c.nn, 256), 256, 0, c.stream>>>(c.nn, s->flag, s->xm, s->Wm, c.x, c.W);
-    c.launches += 4;
+    c.launches += 3;
     return cudaGetLastError();
 }
 
 // One Adam step on a minibatch of (features at the start of the step, solved v).
 cudaError_t mlp_train(Ctx &c) {
     MlpState *s = static_cast<MlpState *>(c.mlp);
-    const int smem = (NPARAM + SB * NF + 2 * SB * NH + 2 * SB * NO) * (int)sizeof(float);
     const float inv_batch = 1.0f / (float)(s->nblk_train * SB * NO);
     if (!s->primed) {
         cudaMemcpyAsync(s->vprev2, c.v[0], 3 * (size_t)c.nn * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
@@ -505,9 +852,10 @@ cudaError_t mlp_train(Ctx &c) {
     }
     k_corr2<<<s->nblk_res, 256, 0, c.stream>>>(c.nn, c.mag, c.v[1], c.v[0], s->vprev2, s->spart);
     k_scale<<<1, 32, 0, c.stream>>>(s->nblk_res, s->spart, c.n_mag_nodes, s->scale);
-    k_mlp_grad<<<s->nblk_train, 256, smem, c.stream>>>(c.n_mag_nodes, c.mag_nodes, s->feat, c.v[1], c.v[0],
-                                                        s->vprev2, s->scale, s->w, (uint64_t)s->steps + 1, inv_batch,
-                                                        s->gpart, s->lpart, nullptr, nullptr);
+    k_mlp_grad_tc<<<s->nblk_train, SB, GRAD_SMEM, c.stream>>>(c.n_mag_nodes, c.mag_nodes, s->feat, c.v[1], c.v[0],
+                                                                s->vprev2, s->scale, s->w, (uint64_t)s->steps + 1,
+                                                                inv_batch, s->gpart, s->lpart, nullptr, nullptr,
+                                                                s->tc_err);
     c.launches += 2;
     s->t++;
     const float b1 = 0.9f, b2 = 0.999f;
@@ -527,6 +875,12 @@ void mlp_after_sync(Ctx &c, int *accepted, double *res0_mlp, double *res0_prev, 
     for (int b = 0; b < s->nblk_train; b++) l += s->hloss[b];
     s->loss = l / (s->nblk_train * SB * NO);
     if (loss) *loss = s->loss;
+    int terr = 0;
+    cudaMemcpy(&terr, s->tc_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (terr) {
+        s->timed_out = true;
+        cudaMemset(s->tc_err, 0, sizeof(int));
+    }
     if (accepted) {
         int f = 0;
         double r2[2] = {0, 0};
@@ -551,9 +905,8 @@ int mlp_debug_grad(Ctx &c, int nsamples, const float *hx, const float *hy, float
     cudaMalloc(&dl, sizeof(float) * nblk);
     cudaMemcpy(dx, hx, sizeof(float) * nsamples * NF, cudaMemcpyHostToDevice);
     cudaMemcpy(dy, hy, sizeof(float) * nsamples * NO, cudaMemcpyHostToDevice);
-    const int smem = (NPARAM + SB * NF + 2 * SB * NH + 2 * SB * NO) * (int)sizeof(float);
-    k_mlp_grad<<<nblk, 256, smem, c.stream>>>(1, c.mag_nodes, s->feat, c.v[1], c.v[0], s->vprev2, s->scale, s->w, 1,
-                                              1.0f / (nsamples * NO), dg, dl, dx, dy);
+    k_mlp_grad_tc<<<nblk, SB, GRAD_SMEM, c.stream>>>(1, c.mag_nodes, s->feat, c.v[1], c.v[0], s->vprev2, s->scale,
+                                                      s->w, 1, 1.0f / (nsamples * NO), dg, dl, dx, dy, s->tc_err);
     std::vector<float> g((size_t)nblk * NPARAM), l(nblk);
     std::vector<__nv_bfloat16> wb(NPARAM);
     cudaStreamSynchronize(c.stream);
@@ -573,7 +926,11 @@ int mlp_debug_grad(Ctx &c, int nsamples, const float *hx, const float *hy, float
     float lt = 0.0f;
     for (int b = 0; b < nblk; b++) lt += l[b];
     *loss = lt / (nsamples * NO);
-    return cudaGetLastError() == cudaSuccess ? FG_OK : FG_ECUDA;
+    int terr = 0;
+    cudaMemcpy(&terr, s->tc_err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemset(s->tc_err, 0, sizeof(int));
+    if (cudaGetLastError() != cudaSuccess) return FG_ECUDA;
+    return terr ? FG_ETIMEDOUT : FG_OK;
 }
 
 int mlp_nparam() { return NPARAM; }
@@ -584,6 +941,39 @@ cudaError_t mlp_before_evolution(Ctx &c) {
     if (!s) return cudaSuccess;
     s->primed = true;
     return cudaMemcpyAsync(s->vprev2, c.v[0], 3 * (size_t)c.nn * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
+}
+
+bool mlp_take_timeout(Ctx &c) {
+    MlpState *s = static_cast<MlpState *>(c.mlp);
+    if (!s || !s->timed_out) return false;
+    s->timed_out = false;
+    return true;
+}
+
+// The tensor-core forward pass on caller-given feature rows: out [n][3] (scaled units, the
+// network's raw outputs).
+int mlp_debug_infer(Ctx &c, int n, const float *hx, float *hy) {
+    MlpState *s = static_cast<MlpState *>(c.mlp);
+    if (!s || n <= 0) return FG_EINVAL;
+    float *dx = nullptr, *dy = nullptr;
+    if (cudaMalloc(&dx, sizeof(float) * (size_t)n * NF) != cudaSuccess) return FG_ECUDA;
+    if (cudaMalloc(&dy, sizeof(float) * (size_t)n * NO) != cudaSuccess) {
+        cudaFree(dx);
+        return FG_ECUDA;
+    }
+    cudaMemcpy(dx, hx, sizeof(float) * (size_t)n * NF, cudaMemcpyHostToDevice);
+    MlpTcArgs a{};
+    a.nn = n; a.w = s->w; a.xin = dx; a.yout = dy; a.err = s->tc_err;
+    cudaError_t e = launch_mlp_infer_tc(c, a);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e == cudaSuccess) e = cudaMemcpy(hy, dy, sizeof(float) * (size_t)n * NO, cudaMemcpyDeviceToHost);
+    int terr = 0;
+    cudaMemcpy(&terr, s->tc_err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemset(s->tc_err, 0, sizeof(int));
+    cudaFree(dx);
+    cudaFree(dy);
+    if (e != cudaSuccess) return FG_ECUDA;
+    return terr ? FG_ETIMEDOUT : FG_OK;
 }
 
 long long mlp_steps(const Ctx &c) {

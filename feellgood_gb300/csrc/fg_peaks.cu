@@ -118,7 +118,7 @@ long long max_cycles(const Scratch &S, int nblk) {
 
 using namespace fg;
 
-extern "C" int fg_measure_peaks(double out[6]) {
+extern "C" int fg_measure_peaks(double out[7]) {
     if (!out) return FG_EINVAL;
     int dev = 0, nsm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -178,5 +178,6 @@ extern "C" int fg_measure_peaks(double out[6]) {
     out[3] = tc[0];
     out[4] = tc[1];
     out[5] = mhz;
+    out[6] = nsm;
     return FG_OK;
 }

@@ -292,6 +292,10 @@ int fg_mlp_info(const fg_ctx *ctx, long long *train_steps, double *last_loss);
 int fg_mlp_debug_grad(fg_ctx *ctx, int nsamples, const float *feat, const float *target, float *weights,
                       float *grad, float *loss);
 int fg_mlp_nparam(void);
+/* Learned guess, for forward checks: the inference kernel (tensor-core BF16 GEMMs with FP32
+ * accumulation) on n caller-given feature rows (12 floats each) with the context's current
+ * weights; out[n][3] gets the network's outputs (before the step's scale). */
+int fg_mlp_debug_infer(fg_ctx *ctx, int n, const float *feat, float *out);
 
 /* ---- batches of independent samples ----------------------------------------------
  * n_samples meshes (all sharing the region tables) packed into one context: their node
@@ -362,8 +366,9 @@ int fg_debug_tc_resources(int attrs[8]);
  *   out[3] tensor flops of tcgen05.mma kind::tf32, M = 128, N = 128, K = 8 (the FMM
  *          translations' shape), out[4] the same with N = 256
  *   out[5] the SM clock in MHz during the FP32 run (cycles over its event time)
+ *   out[6] the number of SMs
  * Allocates and frees its own device buffers and stream. */
-int fg_measure_peaks(double out[6]);
+int fg_measure_peaks(double out[7]);
 
 /* Device ms of the FMM stages when opts.profile is set, averaged over the evaluations
  * since the previous call (CUDA events around each stage, recorded without any extra
