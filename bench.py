@@ -792,8 +792,10 @@ def bench_batch(args):
     regs = [dict(Ae=1e-11, Ms=795774.7, alpha=0.5), dict(Ae=AE, Ms=MS, alpha=alpha)]
     n, meshes, Hext, us = batch_workload(fg)
     ntets = int(sum(6 * k ** 3 for k in n))
+    t_setup = time.perf_counter()
     b = fg.Context(meshes, regs, tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP32_REFINE,
                    demag=fg.FG_DEMAG_FMM)
+    setup_s = time.perf_counter() - t_setup  # fg_batch_create: packing, forest of octrees, autotuning
     b.set_state(np.concatenate(us))
     b.batch_compute_all(Hext, energies=False)
     fg.rng_seed(SEED)
@@ -844,6 +846,7 @@ def bench_batch(args):
             "speedup_vs_loop_plain_fp64": value / loops["plain_fp64"],
             "speedup_vs_loop_fp32_refine": value / loops["fp32_refine"],
             "gpu_launches": int(launches), "clocks": clocks,
+            "batch_create_wall_s": setup_s,
             "energy_sample0": [float(x) for x in E[0]],
         }
         print(json.dumps(line), flush=True)

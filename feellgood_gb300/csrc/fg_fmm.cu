@@ -345,6 +345,100 @@ __global__ void __launch_bounds__(160) k_translate(int n_out, int out0, int ncod
     }
 }
 
+// FP64-path translations in double-single arithmetic on the FP32 pipes (GB300's FP64 pipe
+// does 2 DFMA per clock and SM, 1/64 of its FP32 rate): the same batched GEMM as
+// k_translate, both charge sets of a block of DS_TB output cells as its 2 DS_TB columns, the
+// operator and the inputs split into FP32 pairs hi + lo on their way into shared memory,
+// every product exact through fma (Dekker's TwoProduct) and summed with Knuth's two-sum,
+// the running sum renormalised once per code (about 44 significant bits), the result
+// rounded to FP64 once.
+constexpr int DS_TB = 16, DS_COLS = 2 * DS_TB, DS_CT = 2, DS_BLD = DS_COLS + 1;
+constexpr int tr_ds_smem() { return (NR * NR + NR * DS_BLD) * (int)sizeof(float2); }
+
+__device__ __forceinline__ float2 ds_split(double x) {
+    const float h = (float)x;
+    return make_float2(h, (float)(x - (double)h));
+}
+
+__global__ void __launch_bounds__(160, 2) k_translate_ds(int n_out, int out0, int ncode, const int *__restrict__ tab,
+                                                         const double *__restrict__ ops, const double *in,
+                                                         double *out, int accumulate, int nset, size_t set_stride) {
+    // in and out may be the same array (M2M, L2L): the cells read and written are disjoint.
+    constexpr int RT = 10;
+    extern __shared__ unsigned char smem_raw[];
+    float2 *AT = reinterpret_cast<float2 *>(smem_raw);  // AT[k * NR + row] = Op[row][k]
+    float2 *Bs = AT + NR * NR;                           // [NR][DS_BLD]: column set * DS_TB + cell
+    __shared__ int srcs[DS_TB];
+    const int tid = threadIdx.x, rg = tid / 16, cg = tid % 16;
+    const int c_begin = blockIdx.x * DS_TB;
+    float ah[RT][DS_CT], al[RT][DS_CT];
+#pragma unroll
+    for (int i = 0; i < RT; i++)
+#pragma unroll
+        for (int j = 0; j < DS_CT; j++) ah[i][j] = al[i][j] = 0.f;
+    for (int code = 0; code < ncode; code++) {
+        int sc = -1;
+        if (tid < DS_TB && c_begin + tid < n_out) sc = tab[(size_t)(out0 + c_begin + tid) * ncode + code];
+        if (tid < DS_TB) srcs[tid] = sc;
+        if (!__syncthreads_or(sc >= 0)) continue;
+        for (int e = tid; e < NR * NR; e += blockDim.x) {
+            const int row = e / NR, k = e % NR;
+            AT[k * NR + row] = ds_split(ops[(size_t)code * NR * NR + e]);
+        }
+        for (int e = tid; e < NR * DS_COLS; e += blockDim.x) {
+            const int col = e / NR, k = e % NR, cell = col % DS_TB, set = col / DS_TB;
+            const int src = srcs[cell];
+            Bs[k * DS_BLD + col] = (src >= 0 && set < nset) ? ds_split(in[set * set_stride + (size_t)src * NR + k])
+                                                              : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+#pragma unroll 2
+        for (int k = 0; k < NR; k++) {
+            float2 a[RT], b[DS_CT];
+#pragma unroll
+            for (int i = 0; i < RT; i++) a[i] = AT[k * NR + rg * RT + i];
+#pragma unroll
+            for (int j = 0; j < DS_CT; j++) b[j] = Bs[k * DS_BLD + cg * DS_CT + j];
+#pragma unroll
+            for (int i = 0; i < RT; i++)
+#pragma unroll
+                for (int j = 0; j < DS_CT; j++) {
+                    // (ah, al) += a b: exact leading product and cross terms, two-sum into hi
+                    const float p = a[i].x * b[j].x;
+                    float e = fmaf(a[i].x, b[j].x, -p);
+                    e = fmaf(a[i].x, b[j].y, e);
+                    e = fmaf(a[i].y, b[j].x, e);
+                    const float s = ah[i][j] + p;
+                    const float bb = s - ah[i][j];
+                    const float err = (ah[i][j] - (s - bb)) + (p - bb);
+                    ah[i][j] = s;
+                    al[i][j] += e + err;
+                }
+        }
+#pragma unroll
+        for (int i = 0; i < RT; i++)
+#pragma unroll
+            for (int j = 0; j < DS_CT; j++) {  // renormalise: |lo| back to half an ulp of hi
+                const float s = ah[i][j] + al[i][j];
+                al[i][j] = al[i][j] - (s - ah[i][j]);
+                ah[i][j] = s;
+            }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < DS_CT; j++) {
+        const int col = cg * DS_CT + j, cell = col % DS_TB, set = col / DS_TB;
+        const int c = c_begin + cell;
+        if (c >= n_out || set >= nset) continue;
+        double *o = out + set * set_stride + (size_t)(out0 + c) * NR + rg * RT;
+#pragma unroll
+        for (int i = 0; i < RT; i++) {
+            const double v = (double)ah[i][j] + (double)al[i][j];
+            o[i] = accumulate ? o[i] + v : v;
+        }
+    }
+}
+
 // 1/sqrt in the precision of the path.
 template <typename T> __device__ __forceinline__ T rsqrt_p(T x);
 template <> __device__ __forceinline__ float rsqrt_p<float>(float x) {
@@ -1348,6 +1442,7 @@ static int fmm_build_forest(Ctx &c, int L) {
         FCK(cudaFuncSetAttribute(k_translate<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, tr_smem<float>()));
     } else {
         FCK(cudaFuncSetAttribute(k_translate<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, tr_smem<double>()));
+        FCK(cudaFuncSetAttribute(k_translate_ds, cudaFuncAttributeMaxDynamicSharedMemorySize, tr_ds_smem()));
     }
     if (c.opts.profile)
         for (auto &set : t->ev)
@@ -1453,6 +1548,11 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq) {
             a.nset = nq; a.set_io = sstride; a.set_scratch = t.nslot_floats;
             const cudaError_t e = launch_translate_tc(c.stream, a);
             if (e != cudaSuccess && terr == cudaSuccess) terr = e;
+        } else if (sizeof(T) == 8 && t.ds) {  // FP64 path: double-single, both sets per launch
+            const double *ops = (const double *)(kind == M2M ? t.op_m2m : kind == M2L ? t.op_m2l : t.op_l2l);
+            double *in = (double *)(kind == L2L ? F : M), *out = (double *)(kind == M2M ? M : F);
+            k_translate_ds<<<(n + DS_TB - 1) / DS_TB, 160, tr_ds_smem(), c.stream>>>(n, out0, ncode, tab, ops, in, out,
+                                                                                     kind == L2L, nq, sstride);
         } else {
             const void *ops = kind == M2M ? t.op_m2m : kind == M2L ? t.op_m2l : t.op_l2l;
             for (int q = 0; q < nq; q++) {
@@ -1560,9 +1660,9 @@ int fmm_launches_per_eval(const Ctx &c, int nq) {
     const FmmTree *t = static_cast<const FmmTree *>(c.fmm);
     if (!t) return 0;
     int n = 2;  // P2M, L2P + P2P (both sets in one launch each)
-    // tensor-core translations: both sets in one launch (and one combine launch); the
-    // k_translate form launches once per set
-    const int per = t->tc ? 1 : nq;
+    // tensor-core and double-single translations: both sets in one launch (the tensor-core
+    // form adds one combine launch); the k_translate form launches once per set
+    const int per = (t->tc || (!t->fp32 && t->ds)) ? 1 : nq;
     for (int l = 2; l <= t->L - 1; l++) n += per + (t->tc && t->tc_m2m[l].ncomb > 0);
     n += per + (t->tc && t->tc_m2l.ncomb > 0);
     for (int l = 3; l <= t->L; l++) n += per + (t->tc && t->tc_l2l[l].ncomb > 0);

@@ -24,7 +24,9 @@
 //              all 128 threads gather the 64 ns input expansions' item with 16-byte cp.async
 //              from pre-split hi/lo arrays into the same layout (zero fill where a cell has
 //              no input). A thread arrives on full[s] once its copies for that item have
-//              landed, three items later, so four items per CTA are in flight;
+//              landed, LAG items later and before it waits for the next free stage, so
+//              LAG items per CTA are in flight and the MMAs of an item never wait for those
+//              of the item before it to complete;
 //   warp 4     one lane waits full[s] and bfull[s], issues the MMAs of each K-step of 8 and
 //              tcgen05.commit arrives on empty[s] when they have read the stage; each code
 //              accumulates into its own TMEM buffer (two, used in turn), committed to tfull;
@@ -183,6 +185,15 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
         int sc = src_of(0), sc_next = src_of(1);
         int armed = 0;  // thread 0: items whose bulk copies were started (in order)
         for (int it = 0; it < nitems + LAG; it++) {
+            // arrive for item it - LAG first: its copies were issued LAG items ago, and the
+            // arrival must not wait behind this iteration's wait for a free stage (that wait
+            // follows the MMAs of item it - NSTAGE; arriving after it would hold the MMAs of
+            // item it - LAG until those of the item before it had completed)
+            if (it >= LAG) {
+                cp_wait<LAG - 1>();  // it groups committed: item it - LAG's has landed
+                fence_proxy_async();
+                if (live) mbar_arrive(&full[(it - LAG) % NSTAGE]);
+            }
             if (it < nitems && live) {
                 const int s = it % NSTAGE;
                 if (it >= NSTAGE && !mbar_wait(&empty[s], ((it / NSTAGE) - 1) & 1, err, &bail)) live = false;
@@ -205,11 +216,6 @@ __device__ __forceinline__ void translate_tc_body(const TcArgs &a) {
                 }
             }
             cp_commit();
-            if (it >= LAG) {
-                cp_wait<LAG>();
-                fence_proxy_async();
-                if (live) mbar_arrive(&full[(it - LAG) % NSTAGE]);
-            }
         }
         cp_wait<0>();
         // after a bail the issuer may not have consumed the last stages: wait (bounded) until

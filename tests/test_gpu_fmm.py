@@ -94,8 +94,8 @@ def test_tensor_core_split_precision():
 
 @pytest.mark.parametrize("shape,leaf", [((12, 12, 12), -3), ((40, 40, 3), -4)])
 def test_double_single_near_field(shape, leaf):
-    """The FP64 path's near field in double-single arithmetic on the FP32 pipes against the
-    same near field on the FP64 pipe (same tree, same far field): FP64-level agreement."""
+    """The FP64 path's near field and translations in double-single arithmetic on the FP32
+    pipes against the same FMM on the FP64 pipe (same tree): FP64-level agreement."""
     m = cases.cuboid(*shape)
     u = cases.perturbed_state(m["xyz"], seed=9, sigma=0.3)
     v = cases.tangent_field(u, seed=10)
@@ -106,7 +106,7 @@ def test_double_single_near_field(shape, leaf):
     cn.set_state(u, v)
     for which in (0, 1):
         ps, pn = cs.demag(which), cn.demag(which)
-        print("double-single vs FP64 near field, rel. difference %.2e" % _rel(ps, pn))
+        print("double-single vs FP64 FMM, rel. difference %.2e" % _rel(ps, pn))
         assert _rel(ps, pn) < 1e-12
 
 
@@ -117,12 +117,13 @@ def test_pair_evaluation_matches_single(precision, native, shape, leaf):
     """compute_all evaluates the demag of m and of v in one FMM pass (both charge sets
     through the same launches, one near-field pass with shared pair geometry); each set
     follows the arithmetic of its own single evaluation, so the potentials agree with
-    fg_demag(0) and fg_demag(1) to the last bits."""
+    fg_demag(0) and fg_demag(1) to the last bits (a full evaluation per compute_all:
+    demag_increment 0)."""
     m = cases.cuboid(*shape)
     u = cases.perturbed_state(m["xyz"], seed=11, sigma=0.3)
     v = cases.tangent_field(u, seed=12)
     c = fg.Context(m, cases.regions(), demag=fg.FG_DEMAG_FMM, precision=precision, fmm_leaf=leaf,
-                   fmm_native_fp64=native)
+                   fmm_native_fp64=native, demag_increment=0)
     c.set_state(u, v)
     c.compute_all(np.zeros(3))
     st = c.get_state(0)
