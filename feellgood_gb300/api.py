@@ -61,7 +61,7 @@ class fg_opts(C.Structure):
                 ("mlp_lr", C.c_double), ("fmm_tensor", C.c_int),
                 ("mlp_train_every", C.c_int), ("fmm_native_fp64", C.c_int),
                 ("solver_lpr", C.c_int), ("solver_blocks", C.c_int), ("spin_acc", C.c_int), ("spin_tol", C.c_double),
-                ("spin_max_iter", C.c_int), ("demag_increment", C.c_int)]
+                ("spin_max_iter", C.c_int), ("demag_increment", C.c_int), ("fmm_overlap", C.c_int)]
 
 
 class fg_step_report(C.Structure):

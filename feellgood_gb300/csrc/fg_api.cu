@@ -136,6 +136,7 @@ void fg_opts_default(fg_opts *o) {
     o->spin_tol = 1e-8;        // spinAcc and electrostatSolver tolerance (src/main.cpp:252)
     o->spin_max_iter = 1000;
     o->demag_increment = 1;
+    o->fmm_overlap = 1;
 }
 
 const char *fg_strerror(int s) {
@@ -191,7 +192,16 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     cudaDeviceProp prop;
     CK(cudaGetDeviceProperties(&prop, c.device));
     c.nsm = prop.multiProcessorCount;
-    CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    {
+        // the near field of the FMM runs on a second stream of lower priority, so that the
+        // far-field chain's blocks go first where both wait for an SM
+        int least = 0, greatest = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CK(cudaStreamCreateWithPriority(&c.stream, cudaStreamNonBlocking, greatest));
+        CK(cudaStreamCreateWithPriority(&c.stream2, cudaStreamNonBlocking, least));
+        CK(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming));
+    }
     for (int k = 0; k < 8; k++) CK(cudaEventCreate(&c.ev[k]));
     upload_rules(c.opts.one_gauss_point != 0);
 
@@ -666,6 +676,10 @@ void fg_destroy(fg_ctx *h) {
     if (c.hepart) cudaFreeHost(c.hepart);
     for (int k = 0; k < 8; k++)
         if (c.ev[k]) cudaEventDestroy(c.ev[k]);
+    if (c.stream2) cudaStreamSynchronize(c.stream2);
+    if (c.ev_fork) cudaEventDestroy(c.ev_fork);
+    if (c.ev_join) cudaEventDestroy(c.ev_join);
+    if (c.stream2) cudaStreamDestroy(c.stream2);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete h;
 }
@@ -894,11 +908,11 @@ int fg_compute_all(fg_ctx *h, const double Hext[3], double energies[4]) {
         c.launches += 1;
     }
     CK(cudaEventRecord(c.ev[4], c.stream));
-    double E[4];
-    s = energy_impl(h, Hext, E, nullptr);
-    if (s) return s;
-    if (energies)
-        for (int k = 0; k < 4; k++) energies[k] = E[k];
+    // energies of NEXT: the partial sums are read back with the evolution's copies queued
+    // behind them, so the step has one host round trip here, at its end
+    CK(launch_energy(c, Hext));
+    c.launches += 1;
+    CK(cudaMemcpyAsync(c.hepart, c.epart, 7 * sizeof(double) * c.epart_blocks, cudaMemcpyDeviceToHost, c.stream));
     // Fem::evolution: CURRENT <- NEXT
     if (c.mlp) CK(mlp_before_evolution(c));
     const size_t n3 = 3 * sizeof(double) * c.nn, n1 = sizeof(double) * c.nn;
@@ -909,6 +923,12 @@ int fg_compute_all(fg_ctx *h, const double Hext[3], double energies[4]) {
     CK(cudaEventRecord(c.ev[5], c.stream));
     if (int *fl = fmm_error_flag(c)) CK(cudaMemcpyAsync(c.hflag, fl, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
+    if (energies) {
+        double E[4] = {0, 0, 0, 0};
+        for (int k = 0; k < 4; k++)
+            for (int b = 0; b < c.epart_blocks; b++) E[k] += c.hepart[k * c.epart_blocks + b];
+        for (int k = 0; k < 4; k++) energies[k] = E[k];
+    }
     if (*c.hflag) {
         c.err = "fmm: a tensor-core pipeline wait timed out";
         *c.hflag = 0;

@@ -64,7 +64,9 @@ struct FmmTree {
     // profiling: two sets of stage events used in turn (recorded without synchronising); a
     // set is read back when it is about to be reused or when the timings are requested
     cudaEvent_t ev[2][6] = {};
+    cudaEvent_t evn[2][2] = {};          // the near field on the second stream (overlapped evaluation)
     bool ev_pending[2] = {false, false};
+    bool ev_split[2] = {false, false};  // the set timed an overlapped evaluation
     int ev_next = 0;
     double stage_sum[5] = {0, 0, 0, 0, 0};
     long long stage_n = 0;
@@ -258,7 +260,7 @@ __global__ void __launch_bounds__(128) k_p2m(int nleaf, const int *__restrict__ 
     for (int s = s0 + lane; s < s1; s += 32) {
         const T x = sloc[4 * (size_t)s], y = sloc[4 * (size_t)s + 1], z = sloc[4 * (size_t)s + 2];
         const T qq = T(q[s]);
-        st.qn[(size_t)s * st.qn_stride] = qq;
+        if (st.qn) st.qn[(size_t)s * st.qn_stride] = qq;
         if (st.qh) {  // charge as hi + lo for the double-single near field
             const float qh = (float)q[s];
             st.qh[(size_t)s * st.qd_stride] = qh;
@@ -284,6 +286,22 @@ __global__ void __launch_bounds__(128) k_p2m(int nleaf, const int *__restrict__ 
                 st.Ml[base + k] = xf - hi;
             }
         }
+    }
+}
+
+// The near field's charges alone (what P2M stores beside its expansions), so that the near
+// field can start before P2M: grid y selects the charge set.
+template <typename T>
+__global__ void __launch_bounds__(256) k_near_charges(int nsrc, P2mSet<T> set0, P2mSet<T> set1) {
+    const P2mSet<T> st = blockIdx.y ? set1 : set0;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsrc) return;
+    const double q = st.q[s];
+    st.qn[(size_t)s * st.qn_stride] = T(q);
+    if (st.qh) {
+        const float qh = (float)q;
+        st.qh[(size_t)s * st.qd_stride] = qh;
+        st.ql[(size_t)s * st.qd_stride] = (float)(q - (double)qh);
     }
 }
 
@@ -462,6 +480,7 @@ struct NearSets {
     const T *q2;            // second set's charges (NQ = 2)
     const T *F[2];          // local expansions per set
     double *pot[2];         // potentials per set
+    int near_only;          // 1: write the near-field sums only (k_l2p adds the far field later)
 };
 
 // One pass of the near field and L2P over up to NT targets tb.. of a leaf (nt of them real,
@@ -566,6 +585,12 @@ __device__ __forceinline__ void l2p_p2p_pass(int leaf, int tb, int nt, int lane,
 #pragma unroll
                 for (int k = 0; k < NQ; k++) nr[k] = near[k][j];
             }
+        if (sets.near_only) {
+            const int node = tgt_node[tb + lane];
+#pragma unroll
+            for (int k = 0; k < NQ; k++) sets.pot[k][node] = nr[k];
+            return;
+        }
         const T *__restrict__ Fa = sets.F[0] + fbase;
         const T *__restrict__ Fb = sets.F[NQ - 1] + fbase;
         T fa = 0, fb = 0;
@@ -704,6 +729,12 @@ __device__ __forceinline__ void l2p_p2p_pass_x2(int leaf, int tb, int nt, int la
 #pragma unroll
                 for (int k = 0; k < NQ; k++) nr[k] = near[k][2 * p + 1];
             }
+        }
+        if (sets.near_only) {
+            const int node = tgt_node[tb + lane];
+#pragma unroll
+            for (int k = 0; k < NQ; k++) sets.pot[k][node] = nr[k];
+            return;
         }
         const float *__restrict__ Fa = sets.F[0] + fbase;
         const float *__restrict__ Fb = sets.F[NQ - 1] + fbase;
@@ -890,6 +921,11 @@ __global__ void __launch_bounds__(128) k_l2p_p2p_ds(int nleaf, const int *__rest
 #pragma unroll
                     for (int k = 0; k < NQ; k++) nr[k] = near[k][j];
             const int ti = tb + lane;
+            if (sets.near_only) {
+#pragma unroll
+                for (int k = 0; k < NQ; k++) sets.pot[k][tgt_node[ti]] = nr[k];
+                continue;
+            }
             const double x = tloc[4 * (size_t)ti], y = tloc[4 * (size_t)ti + 1], z = tloc[4 * (size_t)ti + 2];
             const double *__restrict__ Fa = sets.F[0] + fbase;
             const double *__restrict__ Fb = sets.F[NQ - 1] + fbase;
@@ -907,6 +943,39 @@ __global__ void __launch_bounds__(128) k_l2p_p2p_ds(int nleaf, const int *__rest
             sets.pot[0][tgt_node[ti]] = (fa + nr[0]) * sc;
             if constexpr (NQ == 2) sets.pot[1][tgt_node[ti]] = (fb + nr[NQ - 1]) * sc;
         }
+    }
+}
+
+// L2P after a near-field-only pass: one warp per target leaf, lane j of a pass evaluates
+// the local expansion(s) at target j and forms the potential from the stored near sum with
+// the same operations as the fused pass, pot = (far + near) * scale.
+template <typename T, int NQ>
+__global__ void __launch_bounds__(128) k_l2p(int nleaf, const int *__restrict__ leaf_tgt,
+                                             const int *__restrict__ tgt_node, const T *__restrict__ tloc,
+                                             int leaf0, const double *__restrict__ leaf_scale, NearSets<T> sets) {
+    const int lane = threadIdx.x & 31;
+    const int leaf = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (leaf >= nleaf) return;
+    const int t0 = leaf_tgt[leaf], t1 = leaf_tgt[leaf + 1];
+    const size_t fbase = (size_t)(leaf0 + leaf) * NR;
+    const double sc = leaf_scale[leaf];
+    const T *__restrict__ Fa = sets.F[0] + fbase;
+    const T *__restrict__ Fb = sets.F[NQ - 1] + fbase;
+    for (int ti = t0 + lane; ti < t1; ti += 32) {
+        const T x = tloc[4 * (size_t)ti], y = tloc[4 * (size_t)ti + 1], z = tloc[4 * (size_t)ti + 2];
+        T fa = 0, fb = 0;
+        ups_cols<T>(x, y, z, [&](int n, int m, T re, T im) {
+            if (m == 0) {
+                fa += Fa[ridx(n, 0, 0)] * re;
+                if constexpr (NQ == 2) fb += Fb[ridx(n, 0, 0)] * re;
+            } else {
+                fa += T(2) * (Fa[ridx(n, m, 0)] * re + Fa[ridx(n, m, 1)] * im);
+                if constexpr (NQ == 2) fb += T(2) * (Fb[ridx(n, m, 0)] * re + Fb[ridx(n, m, 1)] * im);
+            }
+        });
+        const int node = tgt_node[ti];
+        sets.pot[0][node] = (double(fa) + sets.pot[0][node]) * sc;
+        if constexpr (NQ == 2) sets.pot[1][node] = (double(fb) + sets.pot[1][node]) * sc;
     }
 }
 
@@ -1447,6 +1516,9 @@ static int fmm_build_forest(Ctx &c, int L) {
     if (c.opts.profile)
         for (auto &set : t->ev)
             for (auto &e : set) FCK(cudaEventCreate(&e));
+    if (c.opts.profile)
+        for (auto &set : t->evn)
+            for (auto &e : set) FCK(cudaEventCreate(&e));
     if (c.opts.verbose)
         fprintf(stderr, "fmm: L=%d trees=%d leaves=%d cells=%d m2l=%zu p2p_pairs=%zu (%s)\n", L, nseg, nleaf, ncell,
                 t->n_m2l, t->n_p2p_pairs, fp32 ? "fp32" : "fp64");
@@ -1466,6 +1538,9 @@ void fmm_free(Ctx &c) {
     for (auto &set : t->ev)
         for (auto &e : set)
             if (e) cudaEventDestroy(e);
+    for (auto &set : t->evn)
+        for (auto &e : set)
+            if (e) cudaEventDestroy(e);
     delete t;
     c.fmm = nullptr;
 }
@@ -1480,7 +1555,8 @@ static void harvest_set(FmmTree &t, int k) {
     cudaEventSynchronize(t.ev[k][5]);
     for (int s = 0; s < 5; s++) {
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, t.ev[k][s], t.ev[k][s + 1]);
+        if (s == 4 && t.ev_split[k]) cudaEventElapsedTime(&ms, t.evn[k][0], t.evn[k][1]);  // near field, own stream
+        else cudaEventElapsedTime(&ms, t.ev[k][s], t.ev[k][s + 1]);
         t.stage_sum[s] += ms;
     }
     t.stage_n++;
@@ -1520,6 +1596,49 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq) {
             p.qh = q ? t.ds_q2 : (float *)t.ds_src_hi + 3;
             p.ql = q ? t.ds_q2 + t.nsrc : (float *)t.ds_src_lo + 3;
         }
+    }
+    // overlapped evaluation: the near field (which needs only the sources and their charges)
+    // runs on the second, lower-priority stream beside the far-field chain
+    // P2M -> M2M -> M2L -> L2L, whose small coarse-level launches leave most SMs idle; L2P
+    // follows once both are done. The near field's charges are then stored by their own
+    // launch before the fork instead of by P2M.
+    const bool split = c.opts.fmm_overlap != 0 && c.stream2 != nullptr;
+    NearSets<T> ns;
+    ns.q2 = nq == 2 ? (const T *)t.sq2 : nullptr;
+    ns.F[0] = F;
+    ns.F[1] = F + (nq == 2 ? sstride : 0);
+    ns.pot[0] = c.pot;
+    ns.pot[1] = nq == 2 ? c.pot2 : c.pot;
+    ns.near_only = 0;
+    const int nb = (t.nleaf + 3) / 4;
+    auto near_field = [&](cudaStream_t st) {
+        if constexpr (sizeof(T) == 8) {
+            if (t.ds) {
+                auto k = nq == 2 ? k_l2p_p2p_ds<2> : k_l2p_p2p_ds<1>;
+                k<<<nb, 128, 0, st>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node, (const double *)t.tloc, t.ds_tgt_hi,
+                                      t.ds_tgt_lo, t.ds_src_hi, t.ds_src_lo, t.ds_q2,
+                                      t.ds_q2 ? t.ds_q2 + t.nsrc : nullptr, t.leaf_ijk, t.leaf0, t.leaf_scale,
+                                      t.near_ptr, t.near_leaf, ns);
+            }
+        }
+        if (!t.ds) {
+            auto k = nq == 2 ? k_l2p_p2p<T, 2> : k_l2p_p2p<T, 1>;
+            k<<<nb, 128, 0, st>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node, (const T *)t.tloc, (const T *)t.sloc,
+                                  t.leaf_ijk, t.leaf0, t.leaf_scale, t.near_ptr, t.near_leaf, ns);
+        }
+    };
+    t.ev_split[t.ev_next] = split && prof;
+    if (split) {
+        k_near_charges<T><<<dim3((t.nsrc + 255) / 256, nq), 256, 0, c.stream>>>(t.nsrc, ps[0], ps[1]);
+        for (int k = 0; k < 2; k++) ps[k].qn = nullptr, ps[k].qh = ps[k].ql = nullptr;
+        cudaEventRecord(c.ev_fork, c.stream);
+        cudaStreamWaitEvent(c.stream2, c.ev_fork, 0);
+        ns.near_only = 1;
+        if (prof) cudaEventRecord(t.evn[t.ev_next][0], c.stream2);
+        near_field(c.stream2);
+        if (prof) cudaEventRecord(t.evn[t.ev_next][1], c.stream2);
+        cudaEventRecord(c.ev_join, c.stream2);
+        ns.near_only = 0;
     }
     k_p2m<T><<<dim3((t.nleaf + 3) / 4, nq), 128, 0, c.stream>>>(t.nleaf, t.leaf_src, (const T *)t.sloc, t.leaf0,
                                                                  ps[0], ps[1]);
@@ -1571,27 +1690,12 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq) {
     for (int l = 3; l <= L; l++)
         translate(L2L, t.lev_begin[l + 1] - t.lev_begin[l], t.lev_begin[l], t.tc ? t.tc_l2l[l] : none);
     if (prof) cudaEventRecord(ev[4], c.stream);
-    NearSets<T> ns;
-    ns.q2 = nq == 2 ? (const T *)t.sq2 : nullptr;
-    ns.F[0] = F;
-    ns.F[1] = F + (nq == 2 ? sstride : 0);
-    ns.pot[0] = c.pot;
-    ns.pot[1] = nq == 2 ? c.pot2 : c.pot;
-    const int nb = (t.nleaf + 3) / 4;
-    if constexpr (sizeof(T) == 8) {
-        if (t.ds) {
-            auto k = nq == 2 ? k_l2p_p2p_ds<2> : k_l2p_p2p_ds<1>;
-            k<<<nb, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node, (const double *)t.tloc,
-                                        t.ds_tgt_hi, t.ds_tgt_lo, t.ds_src_hi, t.ds_src_lo, t.ds_q2,
-                                        t.ds_q2 ? t.ds_q2 + t.nsrc : nullptr, t.leaf_ijk, t.leaf0, t.leaf_scale,
-                                        t.near_ptr, t.near_leaf, ns);
-        }
-    }
-    if (!t.ds) {
-        auto k = nq == 2 ? k_l2p_p2p<T, 2> : k_l2p_p2p<T, 1>;
-        k<<<nb, 128, 0, c.stream>>>(t.nleaf, t.leaf_src, t.leaf_tgt, t.tgt_node, (const T *)t.tloc,
-                                    (const T *)t.sloc, t.leaf_ijk, t.leaf0, t.leaf_scale, t.near_ptr, t.near_leaf,
-                                    ns);
+    if (split) {
+        cudaStreamWaitEvent(c.stream, c.ev_join, 0);
+        auto k = nq == 2 ? k_l2p<T, 2> : k_l2p<T, 1>;
+        k<<<nb, 128, 0, c.stream>>>(t.nleaf, t.leaf_tgt, t.tgt_node, (const T *)t.tloc, t.leaf0, t.leaf_scale, ns);
+    } else {
+        near_field(c.stream);
     }
     if (prof) {
         cudaEventRecord(ev[5], c.stream);
@@ -1660,6 +1764,7 @@ int fmm_launches_per_eval(const Ctx &c, int nq) {
     const FmmTree *t = static_cast<const FmmTree *>(c.fmm);
     if (!t) return 0;
     int n = 2;  // P2M, L2P + P2P (both sets in one launch each)
+    if (c.opts.fmm_overlap != 0 && c.stream2) n += 2;  // near-field charges, L2P after the overlapped near field
     // tensor-core and double-single translations: both sets in one launch (the tensor-core
     // form adds one combine launch); the k_translate form launches once per set
     const int per = (t->tc || (!t->fp32 && t->ds)) ? 1 : nq;

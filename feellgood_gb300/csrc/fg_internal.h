@@ -146,7 +146,9 @@ struct MixedArgs {
 
 struct Ctx {
     int device = 0, nsm = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;   // every launch of the context (highest priority)
+    cudaStream_t stream2 = nullptr;  // the FMM near field beside the far field (lowest priority)
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     fg_opts opts{};
     std::string err;
 

@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
             // candidate guess, also the candidate's residual (the referee of the learned guess)
             const bool judge = nref == 0 && a.cand_x != nullptr && !multi;
             {
-                double rr = 0.0, rc = 0.0;
+                double rr = 0.0, rc = 0.0, rx = 0.0;
                 if (!done) {
                     auto row = [&](int i, bool valid, int sub) {
                         double y0 = 0, y1 = 0;
@@ -130,39 +130,46 @@ __global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
                                 a.cand_r[2 * i] = r0;
                                 a.cand_r[2 * i + 1] = r1;
                                 rc += r0 * r0 + r1 * r1;
+                                rx += r0 * a.r64[2 * i] + r1 * a.r64[2 * i + 1];
                             }
                         }
                     };
                     GROUP_ROWS(row)
                 }
-                double v2[2] = {rr, rc};
-                block_store<2>(v2, a.partial, G);
+                double v3[3] = {rr, rc, rx};
+                block_store<3>(v3, a.partial, G);
             }
             if (!grid_sync(a.bar)) goto timeout;
             {
-                double s2[2];
-                range_sum<2>(a.partial, G, sv.b0, sv.b1, s2);
+                double s3[3];
+                range_sum<3>(a.partial, G, sv.b0, sv.b1, s3);
+                double s2 = s3[0];
                 if (judge && !done) {
-                    // the candidate replaces the fallback when its residual is smaller
-                    const bool take = s2[1] < s2[0];
+                    // x = x_prev + t (x_cand - x_prev) with the t in [0, 1] that minimises the
+                    // FP64 residual norm |r_prev + t (r_cand - r_prev)| (the residual is affine in
+                    // t: no further operator application); t > 0 counts as the guess accepted
+                    const double dd = s3[0] + s3[1] - 2.0 * s3[2];
+                    const double t = dd > 0.0 ? fmin(1.0, fmax(0.0, (s3[0] - s3[2]) / dd)) : 0.0;
                     if (blockIdx.x == 0 && threadIdx.x == 0) {
-                        *a.cand_flag = take ? 1 : 0;
-                        a.cand_res2[0] = s2[1];
-                        a.cand_res2[1] = s2[0];
+                        *a.cand_flag = t > 0.0 ? 1 : 0;
+                        a.cand_res2[0] = s3[1];
+                        a.cand_res2[1] = s3[0];
                     }
-                    if (take) {
+                    if (t > 0.0) {
                         SAMPLE_ROWS(i) {
-                            a.x[2 * i] = a.cand_x[2 * i];
-                            a.x[2 * i + 1] = a.cand_x[2 * i + 1];
-                            a.r64[2 * i] = a.cand_r[2 * i];
-                            a.r64[2 * i + 1] = a.cand_r[2 * i + 1];
 #pragma unroll
-                            for (int c = 0; c < 3; c++) a.W64[3 * i + c] = a.cand_W[3 * i + c];
+                            for (int c = 0; c < 2; c++) {
+                                const int k = 2 * i + c;
+                                a.x[k] += t * (a.cand_x[k] - a.x[k]);
+                                a.r64[k] += t * (a.cand_r[k] - a.r64[k]);
+                            }
+#pragma unroll
+                            for (int c = 0; c < 3; c++) a.W64[3 * i + c] += t * (a.cand_W[3 * i + c] - a.W64[3 * i + c]);
                         }
-                        s2[0] = s2[1];
+                        s2 = s3[0] + 2.0 * t * (s3[2] - s3[0]) + t * t * dd;
                     }
                 }
-                if (!done) res = block_once([=] { return sqrt(fabs(s2[0])); });
+                if (!done) res = block_once([=] { return sqrt(fabs(s2)); });
             }
             if (!done) {
                 if (nref == 0) res0 = res;

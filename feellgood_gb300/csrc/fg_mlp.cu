@@ -49,6 +49,7 @@ struct MlpState {
     double *spart = nullptr;                                // its block partials
     int *tc_err = nullptr;                                  // FG_ETIMEDOUT from a tensor-core wait
     double *rc = nullptr;                                   // the candidate's residual (judged in the solver)
+    float *out = nullptr;                                   // the network's outputs [nn][3]
     int nblk_train = 0, nblk_res = 0;
     bool primed = false;   // vprev2 holds a real previous velocity
     bool timed_out = false;  // a tensor-core wait of the last inference expired
@@ -155,17 +156,10 @@ __device__ __forceinline__ void store8(unsigned char *img, int row, int k0, uint
 }
 
 struct MlpTcArgs {
-    int nn;
-    const unsigned char *mag;
-    const double *u0, *heff;
-    const int *Sptr, *Scol;
-    double inv_ms, inv_v0;
-    float *feat;                 // features of every node for the training (nullable)
+    int nn;                      // feature rows
     const __nv_bfloat16 *w;
-    const double *ep, *eq, *vprev, *vprev2, *scale;
-    double *xm, *Wm;             // candidate guess and its tangent vectors
-    const float *xin;            // caller-given feature rows instead of the state (checks)
-    float *yout;                 // with xin: the network's outputs [nn][3]
+    const float *xin;            // feature rows [nn][12]
+    float *yout;                 // the network's outputs [nn][3]
     int *err;                    // FG_ETIMEDOUT after an expired wait
 };
 
@@ -254,18 +248,8 @@ __global__ void __launch_bounds__(TM) k_mlp_infer_tc(MlpTcArgs a) {
         const int i = tile * TM + tid;
         const bool live = i < a.nn;
         float x[NF];
-        if (a.xin) {
 #pragma unroll
-            for (int k = 0; k < NF; k++) x[k] = live ? a.xin[(size_t)i * NF + k] : 0.f;
-        } else if (live) {
-            node_features(i, a.mag, a.u0, a.heff, a.vprev, a.Sptr, a.Scol, a.inv_ms, a.inv_v0, x);
-            if (a.feat)
-#pragma unroll
-                for (int k = 0; k < NF; k++) a.feat[(size_t)i * NF + k] = x[k];
-        } else {
-#pragma unroll
-            for (int k = 0; k < NF; k++) x[k] = 0.f;
-        }
+        for (int k = 0; k < NF; k++) x[k] = live ? a.xin[(size_t)i * NF + k] : 0.f;
         {
             const float x2[8] = {x[8], x[9], x[10], x[11], 0.f, 0.f, 0.f, 0.f};
             store8(A1, tid, 0, SBO_K16, x);
@@ -296,34 +280,10 @@ __global__ void __launch_bounds__(TM) k_mlp_infer_tc(MlpTcArgs a) {
         if (!issue_and_wait(3)) break;
         float o[16];
         drain16(lane_addr, o);
-        const float o0 = o[0] + bias[2 * NH], o1 = o[1] + bias[2 * NH + 1], o2 = o[2] + bias[2 * NH + 2];
-        if (!live) continue;
-        if (a.xin) {
-            a.yout[3 * (size_t)i] = o0;
-            a.yout[3 * (size_t)i + 1] = o1;
-            a.yout[3 * (size_t)i + 2] = o2;
-            continue;
-        }
-        if (!a.mag[i]) {
-            a.xm[2 * i] = a.xm[2 * i + 1] = 0.0;
-            a.Wm[3 * i] = a.Wm[3 * i + 1] = a.Wm[3 * i + 2] = 0.0;
-            continue;
-        }
-        // v = 2 v_prev - v_prev2 + scale * o; x = (v . ep, v . eq) / gamma0
-        const double sc = a.scale[0];
-        const double oo[3] = {o0, o1, o2};
-        double v[3];
+        if (live) {
 #pragma unroll
-        for (int c = 0; c < 3; c++) v[c] = 2.0 * a.vprev[3 * i + c] - a.vprev2[3 * i + c] + sc * oo[c];
-        const double e0 = a.ep[3 * i], e1 = a.ep[3 * i + 1], e2 = a.ep[3 * i + 2];
-        const double q0 = a.eq[3 * i], q1 = a.eq[3 * i + 1], q2 = a.eq[3 * i + 2];
-        const double xp = (v[0] * e0 + v[1] * e1 + v[2] * e2) / FG_GAMMA0;
-        const double xq = (v[0] * q0 + v[1] * q1 + v[2] * q2) / FG_GAMMA0;
-        a.xm[2 * i] = xp;
-        a.xm[2 * i + 1] = xq;
-        a.Wm[3 * i] = xp * e0 + xq * q0;
-        a.Wm[3 * i + 1] = xp * e1 + xq * q1;
-        a.Wm[3 * i + 2] = xp * e2 + xq * q2;
+            for (int c = 0; c < NO; c++) a.yout[NO * (size_t)i + c] = o[c] + bias[2 * NH + c];
+        }
     }
     tc_fence_before();
     __syncthreads();
@@ -331,6 +291,51 @@ __global__ void __launch_bounds__(TM) k_mlp_infer_tc(MlpTcArgs a) {
         tc_fence_after();
         tmem_dealloc(tmem, TC_TMEM_COLS);
     }
+}
+
+// The candidate guess from the network's outputs: the correction of the extrapolation,
+// averaged over the node and its magnetic neighbours (a low-pass filter: the network's
+// per-node errors are uncorrelated from node to node, and rough initial errors are what
+// BiCGSTAB removes slowest), v = 2 v_prev - v_prev2 + scale * mean(o), projected on the new
+// tangent basis: x = (v . ep, v . eq) / gamma0, and its tangent vectors W.
+__global__ void __launch_bounds__(256) k_mlp_candidate(int nn, const unsigned char *__restrict__ mag,
+                                                       const int *__restrict__ Sptr, const int *__restrict__ Scol,
+                                                       const float *__restrict__ o, const double *__restrict__ vprev,
+                                                       const double *__restrict__ vprev2,
+                                                       const double *__restrict__ scale, const double *__restrict__ ep,
+                                                       const double *__restrict__ eq, double *__restrict__ xm,
+                                                       double *__restrict__ Wm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    if (!mag[i]) {
+        xm[2 * i] = xm[2 * i + 1] = 0.0;
+        Wm[3 * i] = Wm[3 * i + 1] = Wm[3 * i + 2] = 0.0;
+        return;
+    }
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+    int cnt = 0;
+    for (int k = Sptr[i]; k < Sptr[i + 1]; k++) {  // the row holds the node itself and its neighbours
+        const int j = Scol[k];
+        if (!mag[j]) continue;
+        s0 += o[3 * (size_t)j];
+        s1 += o[3 * (size_t)j + 1];
+        s2 += o[3 * (size_t)j + 2];
+        cnt++;
+    }
+    const double sc = scale[0] / (double)max(cnt, 1);
+    const double oo[3] = {s0, s1, s2};
+    double v[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) v[c] = 2.0 * vprev[3 * i + c] - vprev2[3 * i + c] + sc * oo[c];
+    const double e0 = ep[3 * i], e1 = ep[3 * i + 1], e2 = ep[3 * i + 2];
+    const double q0 = eq[3 * i], q1 = eq[3 * i + 1], q2 = eq[3 * i + 2];
+    const double xp = (v[0] * e0 + v[1] * e1 + v[2] * e2) / FG_GAMMA0;
+    const double xq = (v[0] * q0 + v[1] * q1 + v[2] * q2) / FG_GAMMA0;
+    xm[2 * i] = xp;
+    xm[2 * i + 1] = xq;
+    Wm[3 * i] = xp * e0 + xq * q0;
+    Wm[3 * i + 1] = xp * e1 + xq * q1;
+    Wm[3 * i + 2] = xp * e2 + xq * q2;
 }
 
 static cudaError_t launch_mlp_infer_tc(Ctx &c, const MlpTcArgs &a) {
@@ -769,6 +774,7 @@ int mlp_create(Ctx &c) {
     if (cudaMalloc(&s->spart, (size_t)s->nblk_res * sizeof(double)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->tc_err, sizeof(int)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->rc, 2 * (size_t)c.nn * sizeof(double)) != cudaSuccess) return FG_ECUDA;
+    if (cudaMalloc(&s->out, 3 * (size_t)c.nn * sizeof(float)) != cudaSuccess) return FG_ECUDA;
     cudaMemset(s->tc_err, 0, sizeof(int));
     {
         const double one = FG_GAMMA0 * c.ms_ref * 1e-3;
@@ -790,7 +796,7 @@ void mlp_free(Ctx &c) {
     MlpState *s = static_cast<MlpState *>(c.mlp);
     if (!s) return;
     void *p[] = {s->master, s->m1, s->m2, s->w, s->feat, s->gpart, s->lpart, s->xm, s->Wm, s->rpart, s->flag,
-                 s->res2, s->vprev2, s->scale, s->spart, s->tc_err, s->rc};
+                 s->res2, s->vprev2, s->scale, s->spart, s->tc_err, s->rc, s->out};
     for (void *q : p)
         if (q) cudaFree(q);
     if (s->hloss) cudaFreeHost(s->hloss);
@@ -817,14 +823,17 @@ cudaError_t mlp_before_solve(Ctx &c, double c0, bool use, bool train) {
         cudaMemcpyAsync(s->vprev2, c.v[0], 3 * (size_t)c.nn * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
         s->primed = true;
     }
+    // features of every node (memory-bound gathers at full occupancy), the network's three
+    // GEMMs on the tensor cores, then the smoothed candidate
+    k_features<<<nb(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.mag, c.u[0], c.heff, c.v[0], c.Sptr, c.Scol,
+                                                      1.0 / c.ms_ref, 1.0 / v0_scale(c), s->feat);
     MlpTcArgs a{};
-    a.nn = c.nn; a.mag = c.mag; a.u0 = c.u[0]; a.heff = c.heff; a.Sptr = c.Sptr; a.Scol = c.Scol;
-    a.inv_ms = 1.0 / c.ms_ref; a.inv_v0 = 1.0 / v0_scale(c); a.feat = train ? s->feat : nullptr;
-    a.w = s->w; a.ep = c.ep; a.eq = c.eq; a.vprev = c.v[0]; a.vprev2 = s->vprev2; a.scale = s->scale;
-    a.xm = s->xm; a.Wm = s->Wm; a.xin = nullptr; a.yout = nullptr; a.err = s->tc_err;
+    a.nn = c.nn; a.w = s->w; a.xin = s->feat; a.yout = s->out; a.err = s->tc_err;
     cudaError_t e = launch_mlp_infer_tc(c, a);
     if (e != cudaSuccess) return e;
-    c.launches += 1;
+    k_mlp_candidate<<<nb(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.mag, c.Sptr, c.Scol, s->out, c.v[0], s->vprev2,
+                                                           s->scale, c.ep, c.eq, s->xm, s->Wm);
+    c.launches += 3;
     if (c.opts.precision == FG_PREC_FP32_REFINE && !c.batch) {
         // the FP32 + refinement solver judges the candidate on its first FP64 residual
         c.cand_x = s->xm;

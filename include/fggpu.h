@@ -126,6 +126,10 @@ typedef struct {
                              potentials are evaluated in full by the FP64 FMM. 0: a full FP32
                              FMM evaluation in every fg_compute_all; 2: a full FP64 FMM
                              evaluation in every fg_compute_all (accuracy studies) */
+    int fmm_overlap;      /* FMM: 1 (default) the near field runs on a second stream of lower
+                             priority concurrently with the far-field translations, then the
+                             local expansions are added (the same arithmetic, results
+                             bit-identical); 0: one stream */
 } fg_opts;
 
 typedef struct {
@@ -373,7 +377,8 @@ int fg_measure_peaks(double out[7]);
 
 /* Device ms of the FMM stages when opts.profile is set, averaged over the evaluations
  * since the previous call (CUDA events around each stage, recorded without any extra
- * synchronisation): [0] P2M, [1] M2M, [2] M2L, [3] L2L, [4] L2P + P2P. */
+ * synchronisation): [0] P2M, [1] M2M, [2] M2L, [3] L2L, [4] L2P + P2P (with
+ * fg_opts.fmm_overlap: the near-field kernel on its own stream, concurrent with [0]-[3]). */
 int fg_fmm_timings(const fg_ctx *ctx, double ms[5]);
 
 /* ---- host-side mesh set-up (no GPU work) ----------------------------------------
