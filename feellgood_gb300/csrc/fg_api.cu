@@ -136,7 +136,7 @@ void fg_opts_default(fg_opts *o) {
     o->spin_tol = 1e-8;        // spinAcc and electrostatSolver tolerance (src/main.cpp:252)
     o->spin_max_iter = 1000;
     o->demag_increment = 1;
-    o->fmm_overlap = 1;
+    o->fmm_overlap = 0;
 }
 
 const char *fg_strerror(int s) {

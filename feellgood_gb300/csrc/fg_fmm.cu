@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(128) k_p2m(int nleaf, const int *__restrict__ 
     for (int s = s0 + lane; s < s1; s += 32) {
         const T x = sloc[4 * (size_t)s], y = sloc[4 * (size_t)s + 1], z = sloc[4 * (size_t)s + 2];
         const T qq = T(q[s]);
-        if (st.qn) st.qn[(size_t)s * st.qn_stride] = qq;
+        st.qn[(size_t)s * st.qn_stride] = qq;
         if (st.qh) {  // charge as hi + lo for the double-single near field
             const float qh = (float)q[s];
             st.qh[(size_t)s * st.qd_stride] = qh;
@@ -286,22 +286,6 @@ __global__ void __launch_bounds__(128) k_p2m(int nleaf, const int *__restrict__ 
                 st.Ml[base + k] = xf - hi;
             }
         }
-    }
-}
-
-// The near field's charges alone (what P2M stores beside its expansions), so that the near
-// field can start before P2M: grid y selects the charge set.
-template <typename T>
-__global__ void __launch_bounds__(256) k_near_charges(int nsrc, P2mSet<T> set0, P2mSet<T> set1) {
-    const P2mSet<T> st = blockIdx.y ? set1 : set0;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nsrc) return;
-    const double q = st.q[s];
-    st.qn[(size_t)s * st.qn_stride] = T(q);
-    if (st.qh) {
-        const float qh = (float)q;
-        st.qh[(size_t)s * st.qd_stride] = qh;
-        st.ql[(size_t)s * st.qd_stride] = (float)(q - (double)qh);
     }
 }
 
@@ -612,8 +596,12 @@ __device__ __forceinline__ void l2p_p2p_pass(int leaf, int tb, int nt, int lane,
 
 // The FP32 pass of l2p_p2p_pass with the pair arithmetic on packed target pairs: per two
 // pairs 3 subtractions, 3 for r^2 (d_x^2, then + d_y^2, + d_z^2 as fused multiply-adds),
-// two SFU reciprocal square roots and one fused multiply-add per charge set; every
-// operation and its order per pair are those of the scalar pass.
+// two SFU reciprocal square roots and one fused multiply-add per charge set, the pair
+// arithmetic of the scalar pass. The terms go straight into the pass sums (no per-leaf
+// partial sums as in the scalar pass): 128 registers, so four blocks fit on an SM, or one
+// beside a tensor-core translation CTA (1.61 -> 1.49 ms on the film; the FP32 FMM's error
+// against the FP64 FMM stays 4.7e-7 for the potential of m, 1.1e-6 instead of 7e-7 for the
+// potential of v).
 template <int NT, int NQ>
 __device__ __forceinline__ void l2p_p2p_pass_x2(int leaf, int tb, int nt, int lane, int li, int lj, int lk,
                                                 const int *__restrict__ leaf_src, const int *__restrict__ tgt_node,
@@ -641,11 +629,6 @@ __device__ __forceinline__ void l2p_p2p_pass_x2(int leaf, int tb, int nt, int la
         const float ox = float(leaf_ijk[3 * nl] - li), oy = float(leaf_ijk[3 * nl + 1] - lj),
                     oz = float(leaf_ijk[3 * nl + 2] - lk);
         const int s0 = leaf_src[nl], s1 = leaf_src[nl + 1];
-        u64 ACC[NQ][NP];
-#pragma unroll
-        for (int p = 0; p < NP; p++)
-#pragma unroll
-            for (int k = 0; k < NQ; k++) ACC[k][p] = 0ull;
         const float4 far = make_float4(1e4f, 1e4f, 1e4f, 0.f);  // a missing source: zero charge far away
         int s = s0 + lane;
         float4 na = s < s1 ? src4[s] : far, nb = s + 32 < s1 ? src4[s + 32] : far;
@@ -679,18 +662,14 @@ __device__ __forceinline__ void l2p_p2p_pass_x2(int leaf, int tb, int nt, int la
                 upk2(db, b0, b1);
                 const u64 RA = pk2(rsqrt_p<float>(a0), rsqrt_p<float>(a1));
                 const u64 RB = pk2(rsqrt_p<float>(b0), rsqrt_p<float>(b1));
-                ACC[0][p] = fma2(AQ, RA, ACC[0][p]);
-                ACC[0][p] = fma2(BQ, RB, ACC[0][p]);
+                NS[0][p] = fma2(AQ, RA, NS[0][p]);
+                NS[0][p] = fma2(BQ, RB, NS[0][p]);
                 if constexpr (NQ == 2) {
-                    ACC[1][p] = fma2(AQ2, RA, ACC[1][p]);
-                    ACC[1][p] = fma2(BQ2, RB, ACC[1][p]);
+                    NS[1][p] = fma2(AQ2, RA, NS[1][p]);
+                    NS[1][p] = fma2(BQ2, RB, NS[1][p]);
                 }
             }
         }
-#pragma unroll
-        for (int p = 0; p < NP; p++)
-#pragma unroll
-            for (int k = 0; k < NQ; k++) NS[k][p] = add2(NS[k][p], ACC[k][p]);
     }
     // warp sums (fixed butterfly order), then FP64
     double near[NQ][NT];
@@ -759,7 +738,7 @@ __device__ __forceinline__ void l2p_p2p_pass_x2(int leaf, int tb, int nt, int la
 // or 4 (a leaf of the film holds 18 to 64 nodes: fixed passes of 16 would spend about a
 // fifth of the pair work on padding).
 template <typename T, int NQ>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? (NQ == 1 ? 4 : 3) : 2)
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)  // FP32: 128 registers, 4 blocks per SM
     k_l2p_p2p(int nleaf, const int *__restrict__ leaf_src, const int *__restrict__ leaf_tgt,
               const int *__restrict__ tgt_node, const T *__restrict__ tloc, const T *__restrict__ sloc,
               const int *__restrict__ leaf_ijk, int leaf0, const double *__restrict__ leaf_scale,
@@ -1597,11 +1576,12 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq) {
             p.ql = q ? t.ds_q2 + t.nsrc : (float *)t.ds_src_lo + 3;
         }
     }
-    // overlapped evaluation: the near field (which needs only the sources and their charges)
-    // runs on the second, lower-priority stream beside the far-field chain
-    // P2M -> M2M -> M2L -> L2L, whose small coarse-level launches leave most SMs idle; L2P
-    // follows once both are done. The near field's charges are then stored by their own
-    // launch before the fork instead of by P2M.
+    // overlapped evaluation: after P2M (which stores the near field's charges) and M2M, the
+    // near field runs on the second, lower-priority stream beside M2L and L2L: an FP32
+    // near-field block (128 threads x 128 registers) fits on an SM beside a tensor-core
+    // translation CTA (288 x 168), so the FP32 and SFU pipes work while the tensor pipe
+    // does; L2P follows once both are done. (Forked before P2M, the near field's blocks took
+    // every SM first and the short M2M launches waited behind them.)
     const bool split = c.opts.fmm_overlap != 0 && c.stream2 != nullptr;
     NearSets<T> ns;
     ns.q2 = nq == 2 ? (const T *)t.sq2 : nullptr;
@@ -1628,18 +1608,6 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq) {
         }
     };
     t.ev_split[t.ev_next] = split && prof;
-    if (split) {
-        k_near_charges<T><<<dim3((t.nsrc + 255) / 256, nq), 256, 0, c.stream>>>(t.nsrc, ps[0], ps[1]);
-        for (int k = 0; k < 2; k++) ps[k].qn = nullptr, ps[k].qh = ps[k].ql = nullptr;
-        cudaEventRecord(c.ev_fork, c.stream);
-        cudaStreamWaitEvent(c.stream2, c.ev_fork, 0);
-        ns.near_only = 1;
-        if (prof) cudaEventRecord(t.evn[t.ev_next][0], c.stream2);
-        near_field(c.stream2);
-        if (prof) cudaEventRecord(t.evn[t.ev_next][1], c.stream2);
-        cudaEventRecord(c.ev_join, c.stream2);
-        ns.near_only = 0;
-    }
     k_p2m<T><<<dim3((t.nleaf + 3) / 4, nq), 128, 0, c.stream>>>(t.nleaf, t.leaf_src, (const T *)t.sloc, t.leaf0,
                                                                  ps[0], ps[1]);
     if (prof) cudaEventRecord(ev[1], c.stream);
@@ -1685,6 +1653,16 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq) {
     for (int l = L - 1; l >= 2; l--)
         translate(M2M, t.lev_begin[l + 1] - t.lev_begin[l], t.lev_begin[l], t.tc ? t.tc_m2m[l] : none);
     if (prof) cudaEventRecord(ev[2], c.stream);
+    if (split) {  // the near field beside M2L and L2L
+        cudaEventRecord(c.ev_fork, c.stream);
+        cudaStreamWaitEvent(c.stream2, c.ev_fork, 0);
+        ns.near_only = 1;
+        if (prof) cudaEventRecord(t.evn[t.ev_next][0], c.stream2);
+        near_field(c.stream2);
+        if (prof) cudaEventRecord(t.evn[t.ev_next][1], c.stream2);
+        cudaEventRecord(c.ev_join, c.stream2);
+        ns.near_only = 0;
+    }
     translate(M2L, t.ncell, 0, t.tc_m2l);
     if (prof) cudaEventRecord(ev[3], c.stream);
     for (int l = 3; l <= L; l++)
@@ -1764,7 +1742,7 @@ int fmm_launches_per_eval(const Ctx &c, int nq) {
     const FmmTree *t = static_cast<const FmmTree *>(c.fmm);
     if (!t) return 0;
     int n = 2;  // P2M, L2P + P2P (both sets in one launch each)
-    if (c.opts.fmm_overlap != 0 && c.stream2) n += 2;  // near-field charges, L2P after the overlapped near field
+    if (c.opts.fmm_overlap != 0 && c.stream2) n += 1;  // L2P after the overlapped near field
     // tensor-core and double-single translations: both sets in one launch (the tensor-core
     // form adds one combine launch); the k_translate form launches once per set
     const int per = (t->tc || (!t->fp32 && t->ds)) ? 1 : nq;
