@@ -752,19 +752,24 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
     }
     CK(cudaEventRecord(c.ev[0], c.stream));
     c.step_open = true;
-    CK(launch_tet(c, dt, Hext));
-    CK(launch_node(c, basis_angle));
-    c.launches += 2;
-    h->last_c0 = prefactor * FG_THETA * dt * FG_GAMMA0;
     const bool use_mlp = c.mlp && mlp_steps(c) >= c.opts.mlp_train_steps;
     const int train_every = std::max(1, c.opts.mlp_train_every);
     // a successful solve of this step trains the guess (features kept from before the solve)
     const bool will_train = !use_mlp || h->solves_since_train + 1 >= train_every;
+    CK(launch_tet(c, dt, Hext));
+    // the node kernel forms the learned guess's features when this step uses or trains it
+    if (c.mlp && (use_mlp || will_train)) c.node_feat = mlp_node_features(c);
+    const cudaError_t en = launch_node(c, basis_angle);
+    c.node_feat.feat = nullptr;
+    CK(en);
+    c.launches += 2;
+    h->last_c0 = prefactor * FG_THETA * dt * FG_GAMMA0;
     if (c.mlp) CK(mlp_before_solve(c, h->last_c0, use_mlp, will_train));
     CK(cudaEventRecord(c.ev[1], c.stream));
     if (c.opts.precision == FG_PREC_FP32_REFINE) {
         const cudaError_t e = launch_mixed(c, dt, prefactor);
         c.cand_x = c.cand_W = nullptr;  // a candidate is judged by one solve only
+        c.cand_o = nullptr;
         CK(e);
     } else {
         CK(launch_bicg64(c, dt, prefactor));

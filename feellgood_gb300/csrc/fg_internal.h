@@ -58,6 +58,14 @@ struct SolveResult {
     int pad;
 };
 
+// The learned guess's per-node features, formed by the node kernel when feat is set:
+// row i = m_i, H_eff,i * inv_ms, v_prev,i * inv_v0, the mean of m over i's neighbours.
+struct NodeFeat {
+    float *feat;  // [nn][12] or nullptr
+    const int *Sptr, *Scol;
+    double inv_ms, inv_v0;
+};
+
 // Per-sample parameters of one step of a batch of independent samples (device copy).
 struct SegPar {
     double dt, prefactor;
@@ -138,10 +146,16 @@ struct MixedArgs {
     // learned initial guess (single system): a candidate x and its tangent vectors beside
     // the fallback in x; the first refinement residual is formed for both and the smaller
     // one wins (cand_flag 1: the candidate), cand_res2 = {|r_cand|^2, |r_fallback|^2}
-    const double *cand_x, *cand_W;
+    double *cand_x, *cand_W;
     double *cand_r;       // the candidate's residual [2 nn]
     int *cand_flag;
     double *cand_res2;
+    // with cand_o set, phase 0 forms the candidate itself (into cand_x / cand_W) from the
+    // network's outputs cand_o [nn][3]: their mean over the node and its magnetic neighbours
+    // times cand_scale, added to the extrapolation 2 v_prev - cand_vprev2 (v_prev = u0's v,
+    // cand_vprev), projected on the new basis
+    const float *cand_o;
+    const double *cand_vprev, *cand_vprev2, *cand_scale;
 };
 
 struct Ctx {
@@ -261,9 +275,12 @@ struct Ctx {
     long long launches = 0;  // kernels launched by this context
     void *mlp = nullptr;     // learned initial guess (fg_mlp.cu)
     // a candidate guess for the next FP32 + refinement solve to judge (set by the learned guess)
-    const double *cand_x = nullptr, *cand_W = nullptr;
+    double *cand_x = nullptr, *cand_W = nullptr;
     double *cand_r = nullptr, *cand_res2 = nullptr;
     int *cand_flag = nullptr;
+    const float *cand_o = nullptr;  // the solver forms the candidate from these network outputs
+    const double *cand_vprev = nullptr, *cand_vprev2 = nullptr, *cand_scale = nullptr;
+    NodeFeat node_feat{nullptr, nullptr, nullptr, 0.0, 0.0};  // features the next node kernel forms
     double *heff = nullptr;  // per-node BE/A (effective field), written when the learned guess is on
 
     // batch of independent samples packed as one block-diagonal system (fg_batch_*)
@@ -368,6 +385,7 @@ int mlp_debug_grad(Ctx &c, int nsamples, const float *hx, const float *hy, float
 int mlp_nparam();
 int mlp_debug_infer(Ctx &c, int n, const float *hx, float *hy);
 bool mlp_take_timeout(Ctx &c);  // a tensor-core wait of the learned guess expired (then cleared)
+NodeFeat mlp_node_features(Ctx &c);  // where the node kernel writes the learned guess's features
 int batch_setup(Ctx &c, const std::vector<int4> &htet, const std::vector<int4> &htri);
 void batch_free(Ctx &c);
 int spin_setup(Ctx &c, const fg_mesh *m, const fg_region *regs, int nreg, const fg_tri_region *tregs, int ntreg,

@@ -431,7 +431,7 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
                          double cr, double sr, double *__restrict__ ep, double *__restrict__ eq,
                          double *__restrict__ Dl, double *__restrict__ rhs, double *__restrict__ x,
                          double *__restrict__ Minv, double *__restrict__ W, double *__restrict__ heff,
-                         const int *__restrict__ node_seg, const SegPar *__restrict__ seg) {
+                         const int *__restrict__ node_seg, const SegPar *__restrict__ seg, NodeFeat nf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
     if (seg) {  // batch: the angle of the node's sample
@@ -498,6 +498,31 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
         heff[3 * i] = be0 * ia;
         heff[3 * i + 1] = be1 * ia;
         heff[3 * i + 2] = be2 * ia;
+    }
+    if (nf.feat) {  // the learned guess's 12 features: m, H_eff / Ms, v_prev / V0, 1-ring mean of m
+        float *f = nf.feat + 12 * (size_t)i;
+        if (!mag[i]) {
+#pragma unroll
+            for (int k = 0; k < 12; k++) f[k] = 0.f;
+        } else {
+            double mb[3] = {0, 0, 0};
+            int deg = 0;
+            for (int k = nf.Sptr[i]; k < nf.Sptr[i + 1]; k++) {
+                const int j = nf.Scol[k];
+                if (j == i) continue;
+                mb[0] += u0[3 * j]; mb[1] += u0[3 * j + 1]; mb[2] += u0[3 * j + 2];
+                deg++;
+            }
+            const double id = deg ? 1.0 / deg : 0.0;
+            const double hb[3] = {be0 * ia, be1 * ia, be2 * ia};
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                f[c] = (float)u[c];
+                f[3 + c] = (float)(hb[c] * nf.inv_ms);
+                f[6 + c] = (float)(v1[3 * i + c] * nf.inv_v0);
+                f[9 + c] = (float)(mb[c] * id);
+            }
+        }
     }
     if (mag[i]) {
         rhs[2 * i] = q[0] * be0 + q[1] * be1 + q[2] * be2;
@@ -1226,7 +1251,7 @@ cudaError_t launch_node(Ctx &c, double angle) {
                                                         c.mag, c.A, c.u[0], c.v[1],
                                                         cr, sr, c.ep, c.eq, c.Dl, c.rhs, c.x, Minv, c.W,
                                                         c.mlp ? c.heff : nullptr, c.node_seg,
-                                                        c.batch ? c.seg_par : nullptr);
+                                                        c.batch ? c.seg_par : nullptr, c.node_feat);
     return cudaGetLastError();
 }
 

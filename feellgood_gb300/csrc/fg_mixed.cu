@@ -75,9 +75,40 @@ __global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
         dt = a.seg[sv.g].dt;
     }
     const float c32 = (float)(c0 * a.scale);
-    // phase 0: FP32 copies of the per-step operator, FP64 tangent vectors of x, |b|^2
+    // phase 0: FP32 copies of the per-step operator, FP64 tangent vectors of x, |b|^2, and
+    // the learned guess's candidate when its network outputs are given
     {
         double bb = 0.0;
+        if (a.cand_o && !multi) {
+            SAMPLE_ROWS(i) {
+                double xp = 0.0, xq = 0.0;
+                if (a.mag[i]) {
+                    // the correction's mean over the node and its magnetic neighbours (the row of
+                    // S holds both): a low-pass filter on the network's per-node errors
+                    float o0 = 0.f, o1 = 0.f, o2 = 0.f;
+                    int cnt = 0;
+                    for (int k = a.Sptr[i]; k < a.Sptr[i + 1]; k++) {
+                        const int j = a.Scol[k];
+                        if (!a.mag[j]) continue;
+                        o0 += a.cand_o[3 * (size_t)j];
+                        o1 += a.cand_o[3 * (size_t)j + 1];
+                        o2 += a.cand_o[3 * (size_t)j + 2];
+                        cnt++;
+                    }
+                    const double sc = a.cand_scale[0] / (double)max(cnt, 1);
+                    const double oo[3] = {o0, o1, o2};
+                    double v[3];
+#pragma unroll
+                    for (int c = 0; c < 3; c++)
+                        v[c] = 2.0 * a.cand_vprev[3 * i + c] - a.cand_vprev2[3 * i + c] + sc * oo[c];
+                    xp = (v[0] * a.ep[3 * i] + v[1] * a.ep[3 * i + 1] + v[2] * a.ep[3 * i + 2]) / FG_GAMMA0;
+                    xq = (v[0] * a.eq[3 * i] + v[1] * a.eq[3 * i + 1] + v[2] * a.eq[3 * i + 2]) / FG_GAMMA0;
+                }
+                a.cand_x[2 * i] = xp;
+                a.cand_x[2 * i + 1] = xq;
+                tangent<double>(i, a.ep, a.eq, xp, xq, a.cand_W);
+            }
+        }
         SAMPLE_ROWS(i) {
             for (int c = 0; c < 3; c++) {
                 a.ep32[3 * i + c] = (float)a.ep[3 * i + c];
@@ -503,6 +534,10 @@ cudaError_t launch_mixed(Ctx &c, double dt, double prefactor) {
     a.cand_r = c.cand_r;
     a.cand_flag = c.cand_flag;
     a.cand_res2 = c.cand_res2;
+    a.cand_o = c.batch ? nullptr : c.cand_o;
+    a.cand_vprev = c.cand_vprev;
+    a.cand_vprev2 = c.cand_vprev2;
+    a.cand_scale = c.cand_scale;
     a.nseg = 1;
     a.seg_node = a.seg_blk = nullptr;
     a.seg = nullptr;

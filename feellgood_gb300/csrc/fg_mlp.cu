@@ -8,12 +8,16 @@
 // The network predicts the correction of the second-order extrapolation
 // v_e = 2 v_prev - v_prev2 (in units of the RMS of that correction over the last solve),
 // so the candidate is v_e + scale * MLP(features), projected on the new tangent basis and
-// divided by gamma0. The reference's guess (previous v on the new basis,
-// src/linear_algebra.cpp:13-24) is the fallback and the referee: the candidate is used only
-// when its FP64 initial residual |b - K x| is smaller than the fallback's (judged inside the
-// FP32 + refinement solver's first FP64 residual pass; by separate kernels on the FP64
-// path). Inference runs the network's three GEMMs on the tensor cores (BF16 operands, FP32
-// accumulation in tensor memory). The network is trained online on (features, solved v)
+// divided by gamma0; the correction is averaged over the node and its magnetic neighbours
+// first (the network's per-node errors are rough, and rough initial errors are what BiCGSTAB
+// removes slowest). The reference's guess (previous v on the new basis,
+// src/linear_algebra.cpp:13-24) is the fallback and the referee: on the FP32 + refinement
+// path the solver forms the candidate in its first phase and, in its first FP64 residual
+// pass, takes the blend of the two guesses with the smallest residual norm; on the FP64 path
+// separate kernels keep the candidate only when its FP64 initial residual is smaller. The
+// node kernel forms the features; inference runs the network's three GEMMs on the tensor
+// cores (BF16 operands, FP32 accumulation in tensor memory). The network is trained online
+// on (features, solved v)
 // pairs with hand-written kernels: BF16 weights (FP32 master copy, Adam), FP32
 // accumulation, deterministic fixed-order reductions.
 #include <cuda_bf16.h>
@@ -61,46 +65,6 @@ struct MlpState {
 
 __device__ __forceinline__ float bf(const __nv_bfloat16 *w, int k) { return __bfloat162float(w[k]); }
 
-// Features of node i (magnetic nodes; others get zeros).
-__device__ __forceinline__ void node_features(int i, const unsigned char *__restrict__ mag,
-                                              const double *__restrict__ u0, const double *__restrict__ heff,
-                                              const double *__restrict__ vprev, const int *__restrict__ Sptr,
-                                              const int *__restrict__ Scol, double inv_ms, double inv_v0,
-                                              float (&f)[NF]) {
-#pragma unroll
-    for (int k = 0; k < NF; k++) f[k] = 0.0f;
-    if (!mag[i]) return;
-    double mb[3] = {0, 0, 0};
-    int deg = 0;
-    for (int k = Sptr[i]; k < Sptr[i + 1]; k++) {
-        const int j = Scol[k];
-        if (j == i) continue;
-        mb[0] += u0[3 * j]; mb[1] += u0[3 * j + 1]; mb[2] += u0[3 * j + 2];
-        deg++;
-    }
-    const double id = deg ? 1.0 / deg : 0.0;
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        f[c] = (float)u0[3 * i + c];
-        f[3 + c] = (float)(heff[3 * i + c] * inv_ms);
-        f[6 + c] = (float)(vprev[3 * i + c] * inv_v0);
-        f[9 + c] = (float)(mb[c] * id);
-    }
-}
-
-// Features of every node, for the training of a step that runs no inference.
-__global__ void k_features(int nn, const unsigned char *__restrict__ mag, const double *__restrict__ u0,
-                           const double *__restrict__ heff, const double *__restrict__ vprev,
-                           const int *__restrict__ Sptr, const int *__restrict__ Scol, double inv_ms,
-                           double inv_v0, float *__restrict__ feat) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nn) return;
-    float f[NF];
-    node_features(i, mag, u0, heff, vprev, Sptr, Scol, inv_ms, inv_v0, f);
-#pragma unroll
-    for (int k = 0; k < NF; k++) feat[(size_t)i * NF + k] = f[k];
-}
-
 // tanh on the SFU (tanh.approx.f32, relative error about 2^-11): the guess only has to be
 // good, the referee below decides on its FP64 residual.
 __device__ __forceinline__ float tanh_sfu(float x) {
@@ -115,7 +79,7 @@ __device__ __forceinline__ float tanh_sfu(float x) {
 //   layer 1  D1[128 x 64] = X[128 x 16] W1^T      (12 features padded to K = 16), 1 MMA
 //   layer 2  D2[128 x 64] = H1[128 x 64] W2^T     4 MMAs of K = 16
 //   layer 3  D3[128 x 16] = H2[128 x 64] W3^T     (3 outputs padded to N = 16), 4 MMAs
-// Thread t of the CTA owns node t of the tile: it forms the node's features, writes its BF16
+// Thread t of the CTA owns node t of the tile: it reads the node's features, writes its BF16
 // row of X, drains its row of D1 / D2 with tcgen05.ld (TMEM lane t), adds the bias, applies
 // tanh and writes its BF16 row of H for the next layer; one thread issues the MMAs.
 // Operands sit in shared memory in the no-swizzle K-major layout of 8-row x 16-byte core
@@ -806,43 +770,46 @@ void mlp_free(Ctx &c) {
 
 static double v0_scale(const Ctx &c) { return FG_GAMMA0 * c.ms_ref; }
 
-// With use != 0 the candidate guess and the decision against the fallback guess already in
-// c.x (writes c.x / c.W when the candidate wins); the features of the current state are
-// stored for the training when train is set (formed inside the inference when it runs).
+// Where the node kernel stores the features of the current state (inference and training).
+NodeFeat mlp_node_features(Ctx &c) {
+    MlpState *s = static_cast<MlpState *>(c.mlp);
+    return NodeFeat{s->feat, c.Sptr, c.Scol, 1.0 / c.ms_ref, 1.0 / v0_scale(c)};
+}
+
+// With use set: the network's outputs on the features this step's node kernel formed, and
+// the candidate guess for the solve to judge (FP32 + refinement: the solver forms and blends
+// it; FP64: formed here and kept by the referee kernels when its residual is smaller).
 cudaError_t mlp_before_solve(Ctx &c, double c0, bool use, bool train) {
     MlpState *s = static_cast<MlpState *>(c.mlp);
-    if (!use) {
-        if (train) {
-            k_features<<<nb(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.mag, c.u[0], c.heff, c.v[1], c.Sptr, c.Scol,
-                                                              1.0 / c.ms_ref, 1.0 / v0_scale(c), s->feat);
-            c.launches += 1;
-        }
-        return cudaGetLastError();
-    }
+    (void)train;
+    if (!use) return cudaSuccess;
     if (!s->primed) {  // no history yet: the extrapolation degenerates to v_prev
         cudaMemcpyAsync(s->vprev2, c.v[0], 3 * (size_t)c.nn * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
         s->primed = true;
     }
-    // features of every node (memory-bound gathers at full occupancy), the network's three
-    // GEMMs on the tensor cores, then the smoothed candidate
-    k_features<<<nb(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.mag, c.u[0], c.heff, c.v[0], c.Sptr, c.Scol,
-                                                      1.0 / c.ms_ref, 1.0 / v0_scale(c), s->feat);
+    // the network's three GEMMs on the tensor cores, on the features the node kernel formed
     MlpTcArgs a{};
     a.nn = c.nn; a.w = s->w; a.xin = s->feat; a.yout = s->out; a.err = s->tc_err;
     cudaError_t e = launch_mlp_infer_tc(c, a);
     if (e != cudaSuccess) return e;
-    k_mlp_candidate<<<nb(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.mag, c.Sptr, c.Scol, s->out, c.v[0], s->vprev2,
-                                                           s->scale, c.ep, c.eq, s->xm, s->Wm);
-    c.launches += 3;
+    c.launches += 1;
     if (c.opts.precision == FG_PREC_FP32_REFINE && !c.batch) {
-        // the FP32 + refinement solver judges the candidate on its first FP64 residual
+        // the FP32 + refinement solver forms the smoothed candidate in its first phase and
+        // judges it on its first FP64 residual
         c.cand_x = s->xm;
         c.cand_W = s->Wm;
         c.cand_r = s->rc;
         c.cand_flag = s->flag;
         c.cand_res2 = s->res2;
+        c.cand_o = s->out;
+        c.cand_vprev = c.v[0];
+        c.cand_vprev2 = s->vprev2;
+        c.cand_scale = s->scale;
         return cudaSuccess;
     }
+    k_mlp_candidate<<<nb(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.mag, c.Sptr, c.Scol, s->out, c.v[0], s->vprev2,
+                                                           s->scale, c.ep, c.eq, s->xm, s->Wm);
+    c.launches += 1;
     k_resid2<<<s->nblk_res, 256, 0, c.stream>>>(c.nn, c.Sptr, c.Scol, c.Sval, c.ep, c.eq, c.A, c.Dl, c.mag, c0,
                                                 c.rhs, s->xm, s->Wm, c.x, c.W, s->rpart);
     k_choose<<<1, 32, 0, c.stream>>>(s->nblk_res, s->rpart, s->flag, s->res2);
