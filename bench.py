@@ -292,6 +292,8 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="film", choices=["film", "batch64", "wire", "platelet", "spin"])
     ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--fp64-batch-steps", type=int, default=10,
+                    help="batch64: timed steps of the FP64 batch (at most --steps)")
     ap.add_argument("--train-steps", type=int, default=None,
                     help="untimed solves that train the learned guess (default 40; 0 with --quick)")
     ap.add_argument("--train-every", type=int, default=4,
@@ -812,7 +814,29 @@ def bench_batch(args):
     fails = int(sum(r["fails"] for r in reps))
     iters = float(np.mean([r["iters"] / args.steps for r in reps]))
     E = b.batch_compute_all(Hext)
+    tree = b.fmm_tree_info()
     b.close()
+    # the octree built with the host's comparison sort instead, for its set-up time
+    t_setup = time.perf_counter()
+    bh = fg.Context(meshes, regs, tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP32_REFINE,
+                    demag=fg.FG_DEMAG_FMM, fmm_tree_host=1)
+    setup_host_s = time.perf_counter() - t_setup
+    tree_host = bh.fmm_tree_info()
+    bh.close()
+
+    # the same batch with the plain FP64 solver and FP64 forest FMM (graph-replayed): the
+    # like-for-like of looping the plain FP64 path over the samples
+    b64 = fg.Context(meshes, regs, tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP64, demag=fg.FG_DEMAG_FMM)
+    b64.set_state(np.concatenate(us))
+    b64.batch_compute_all(Hext, energies=False)
+    k64 = max(1, min(args.steps, args.fp64_batch_steps))
+    b64.batch_run(dt, prefactor(dt, dt), Hext, ang[:1])
+    s64, reps64 = b64.batch_run(dt, prefactor(dt, dt), Hext, ang[args.warmup:args.warmup + k64])
+    ms64 = b64.batch_run_info()[1]
+    fp64_batch = {"value": k64 * BATCH_N / (ms64 * 1e-3), "steps": k64, "ms_per_step": ms64 / k64,
+                  "failed_solves": int(sum(r["fails"] for r in reps64)),
+                  "iters_per_step_mean": float(np.mean([r["iters"] / k64 for r in reps64]))}
+    b64.close()
 
     # looping single contexts over the samples, the same steps: plain FP64 and FP32 + refinement
     loops = {}
@@ -847,6 +871,9 @@ def bench_batch(args):
             "speedup_vs_loop_fp32_refine": value / loops["fp32_refine"],
             "gpu_launches": int(launches), "clocks": clocks,
             "batch_create_wall_s": setup_s,
+            "fmm_setup": {"device_sort": tree, "host_sort": tree_host, "batch_create_wall_s_host_sort": setup_host_s},
+            "fp64_batch_steps_samples_per_s": fp64_batch,
+            "speedup_fp64_batch_vs_loop_plain_fp64": fp64_batch["value"] / loops["plain_fp64"],
             "energy_sample0": [float(x) for x in E[0]],
         }
         print(json.dumps(line), flush=True)

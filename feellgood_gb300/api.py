@@ -61,7 +61,8 @@ class fg_opts(C.Structure):
                 ("mlp_lr", C.c_double), ("fmm_tensor", C.c_int),
                 ("mlp_train_every", C.c_int), ("fmm_native_fp64", C.c_int),
                 ("solver_lpr", C.c_int), ("solver_blocks", C.c_int), ("spin_acc", C.c_int), ("spin_tol", C.c_double),
-                ("spin_max_iter", C.c_int), ("demag_increment", C.c_int), ("fmm_overlap", C.c_int)]
+                ("spin_max_iter", C.c_int), ("demag_increment", C.c_int), ("fmm_overlap", C.c_int),
+                ("fmm_tree_host", C.c_int)]
 
 
 class fg_step_report(C.Structure):
@@ -117,6 +118,7 @@ SIGNATURES = {
     "fg_rng_seed": (None, [C.c_uint]),
     "fg_rng_angle": (C.c_double, []),
     "fg_fmm_timings": (C.c_int, [C.c_void_p, _dp]),
+    "fg_fmm_tree_info": (C.c_int, [C.c_void_p, _dp]),
     "fg_mlp_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _dp]),
     "fg_mlp_debug_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p]),
@@ -602,6 +604,14 @@ class Context:
         ms = np.zeros(5)
         self._check(self.L.fg_fmm_timings(self.h, _dptr(ms)))
         return ms
+
+    def fmm_tree_info(self):
+        """FMM set-up: dict of the whole set-up's wall ms, the octree builds' wall ms, the
+        device ms of the Morton-key radix sort, the depth and the number of trees."""
+        out = np.zeros(5)
+        self._check(self.L.fg_fmm_tree_info(self.h, _dptr(out)))
+        return dict(setup_ms=float(out[0]), tree_ms=float(out[1]), sort_device_ms=float(out[2]),
+                    depth=int(out[3]), trees=int(out[4]))
 
     def timings(self):
         """[elements, solve, demag, energy + evolution, whole step] device ms of the last step."""

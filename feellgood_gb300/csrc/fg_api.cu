@@ -137,6 +137,7 @@ void fg_opts_default(fg_opts *o) {
     o->spin_max_iter = 1000;
     o->demag_increment = 1;
     o->fmm_overlap = 0;
+    o->fmm_tree_host = 0;
 }
 
 const char *fg_strerror(int s) {
@@ -161,10 +162,12 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     Ctx &c = h->c;
     if (opts) c.opts = *opts; else fg_opts_default(&c.opts);
     if (c.batch) {
-        // a batch runs the FP32 + refinement solver and a forest FMM (one tree per sample)
-        if (c.opts.precision != FG_PREC_FP32_REFINE || c.opts.learned_guess ||
-            c.opts.demag == FG_DEMAG_DIRECT) {
-            c.err = "fg_batch_create: a batch needs precision FG_PREC_FP32_REFINE, demag FMM and no learned guess";
+        // a batch runs the FP32 + refinement or the FP64 solver and a forest FMM (one tree
+        // per sample)
+        if ((c.opts.precision != FG_PREC_FP32_REFINE && c.opts.precision != FG_PREC_FP64) ||
+            c.opts.learned_guess || c.opts.demag == FG_DEMAG_DIRECT) {
+            c.err = "fg_batch_create: a batch needs precision FG_PREC_FP32_REFINE or FG_PREC_FP64, demag FMM and "
+                    "no learned guess";
             return FG_EINVAL;
         }
         if (c.opts.spin_acc) {
@@ -1159,6 +1162,23 @@ int fg_solver_info(const fg_ctx *h, int *lanes_per_row, int *blocks) {
 int fg_fmm_timings(const fg_ctx *h, double ms[5]) {
     if (!h || !ms) return FG_EINVAL;
     return fmm_stage_ms(h->c, ms);
+}
+
+int fg_fmm_tree_info(const fg_ctx *h, double out[5]) {
+    if (!h || !out) return FG_EINVAL;
+    const Ctx &c = h->c;
+    int L = 0, nleaf = 0;
+    double a = 0, b = 0;
+    if (fmm_info(c, &L, &nleaf, &a, &b) != FG_OK) {
+        const_cast<Ctx &>(c).err = "fg_fmm_tree_info: the context has no FMM";
+        return FG_EINVAL;
+    }
+    out[0] = c.fmm_setup_ms;
+    out[1] = c.tree_wall_ms;
+    out[2] = c.tree_sort_ms;
+    out[3] = L;
+    out[4] = c.batch ? c.nseg : 1;
+    return FG_OK;
 }
 
 int fg_timings(const fg_ctx *h, double ms[5]) {

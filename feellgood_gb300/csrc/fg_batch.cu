@@ -7,6 +7,9 @@
 //     its own range of blocks, Krylov scalars and stopping test (k_mixed, nseg > 1),
 //   - the demag field is a forest FMM with one octree per sample (fg_fmm.cu),
 //   - energies are reduced per sample over blocks aligned to the samples.
+// The solver is the FP32 body with FP64 refinement (k_mixed, nseg > 1) or, with precision
+// FG_PREC_FP64, the plain FP64 BiCGSTAB (k_bicg64_seg), per sample exactly the iteration of
+// a single context.
 // fg_batch_run uploads a whole schedule of per-step parameters once and replays the step
 // (parameter select, elements, nodes, solve, two demag evaluations, evolution, step
 // counter) as one CUDA graph, so a run needs no host round trip between steps.
@@ -101,7 +104,8 @@ int batch_setup(Ctx &c, const std::vector<int4> &htet, const std::vector<int4> &
 
     // persistent-solver blocks: at least one per sample, the rest spread so that the rows
     // per block are as even as possible (largest rows-per-block first)
-    const int gmax = mixed_max_blocks(c);
+    const bool fp64 = c.opts.precision == FG_PREC_FP64;
+    const int gmax = fp64 ? bicg_seg_max_blocks(c) : mixed_max_blocks(c);
     if (ns > gmax) {
         c.err = "batch: " + std::to_string(ns) + " samples exceed the " + std::to_string(gmax) +
                 " co-resident blocks of one persistent launch";
@@ -133,6 +137,7 @@ int batch_setup(Ctx &c, const std::vector<int4> &htet, const std::vector<int4> &
     for (int g = 0; g < ns; g++) c.h_seg_blk[g + 1] = c.h_seg_blk[g] + nb[g];
     c.seg_grid = c.h_seg_blk[ns];
     BCK(bupload(&c.d_seg_blk, c.h_seg_blk));
+    if (fp64) c.lpr = 1;  // one thread per row: no solver variant to choose
     if (c.partial_len < 8 * c.seg_grid) {
         cudaFree(c.partial);
         c.partial = nullptr;
@@ -203,6 +208,12 @@ static void fill_par(SegPar &P, const fg_sample_step &s) {
 }
 
 
+// The per-step solve of every sample: FP64 BiCGSTAB, or the FP32 body with FP64 refinement.
+static cudaError_t batch_solve(Ctx &c) {
+    if (c.opts.precision == FG_PREC_FP64) return launch_bicg64(c, 1.0, 1.0);
+    return launch_mixed(c, 1.0, 1.0);
+}
+
 // Demag of m (and of v beside it, one FMM evaluation of both charge sets).
 static cudaError_t batch_demag_all(Ctx &c) {
     const int nq = c.opts.first_order ? 1 : 2;
@@ -225,7 +236,7 @@ static cudaError_t run_body(Ctx &c) {
     if ((e = launch_select_params(c)) != cudaSuccess) return e;
     if ((e = launch_tet(c, 1.0, H0)) != cudaSuccess) return e;
     if ((e = launch_node(c, 0.0)) != cudaSuccess) return e;
-    if ((e = launch_mixed(c, 1.0, 1.0)) != cudaSuccess) return e;
+    if ((e = batch_solve(c)) != cudaSuccess) return e;
     if ((e = batch_demag_all(c)) != cudaSuccess) return e;
     const size_t n3 = 3 * sizeof(double) * c.nn, n1 = sizeof(double) * c.nn;
     if ((e = cudaMemcpyAsync(c.u[0], c.u[1], n3, cudaMemcpyDeviceToDevice, c.stream)) != cudaSuccess) return e;
@@ -320,7 +331,7 @@ int fg_batch_step(fg_ctx *h, const fg_sample_step *steps, fg_step_report *reps) 
     CK(cudaEventRecord(c.ev[1], c.stream));
     c.launches += 2;
     c.acc_active = nullptr;
-    CK(launch_mixed(c, 1.0, 1.0));
+    CK(batch_solve(c));
     CK(cudaEventRecord(c.ev[2], c.stream));
     c.launches += 1;
     CK(cudaMemcpyAsync(c.hres, c.dres, sizeof(SolveResult) * ns, cudaMemcpyDeviceToHost, c.stream));

@@ -1062,6 +1062,13 @@ struct SamplePts {
     double c0[3] = {0, 0, 0}, side = 1.0;
 };
 
+// Centre and side of every sample's root cube.
+static std::vector<double4> sample_roots(const std::vector<SamplePts> &S) {
+    std::vector<double4> r(S.size());
+    for (size_t g = 0; g < S.size(); g++) r[g] = make_double4(S[g].c0[0], S[g].c0[1], S[g].c0[2], S[g].side);
+    return r;
+}
+
 static std::vector<SamplePts> split_samples(const Ctx &c) {
     const int nseg = std::max(1, c.nseg);
     std::vector<SamplePts> S(nseg);
@@ -1096,26 +1103,48 @@ int fmm_build(Ctx &c) {
         c.err = "fmm: only expansion order P=9 is built";
         return FG_EINVAL;
     }
+    const auto t_begin = std::chrono::steady_clock::now();
+    c.tree_wall_ms = c.tree_sort_ms = 0.0;
     const std::vector<SamplePts> S = split_samples(c);
     // mean number of sources per occupied leaf at each depth, over all samples
     std::vector<double> occ(11, 0.0);
-    for (const SamplePts &P : S) {
-        const int n10 = 1 << 10;
-        std::vector<uint64_t> keys;
-        keys.reserve(P.src.size());
-        for (int s : P.src) {
-            int ijk[3];
-            for (int d = 0; d < 3; d++)
-                ijk[d] = std::min(n10 - 1, std::max(0, (int)(((c.h_src_xyz[3 * (size_t)s + d] - P.c0[d]) / P.side + 0.5) * n10)));
-            keys.push_back(morton(ijk[0], ijk[1], ijk[2]));
+    {
+        const auto t0 = std::chrono::steady_clock::now();
+        std::vector<std::vector<uint64_t>> keys;
+        if (c.opts.fmm_tree_host) {
+            for (const SamplePts &P : S) {
+                const int n10 = 1 << 10;
+                keys.emplace_back();
+                keys.back().reserve(P.src.size());
+                for (int s : P.src) {
+                    int ijk[3];
+                    for (int d = 0; d < 3; d++)
+                        ijk[d] = std::min(n10 - 1, std::max(0, (int)(((c.h_src_xyz[3 * (size_t)s + d] - P.c0[d]) / P.side + 0.5) * n10)));
+                    keys.back().push_back(morton(ijk[0], ijk[1], ijk[2]));
+                }
+                std::sort(keys.back().begin(), keys.back().end());
+            }
+        } else {
+            // one device sort of all samples' keys (the sample in the bits above the cell's):
+            // the distinct prefixes of the sorted keys are the occupied cells of every sample
+            keys.emplace_back();
+            std::vector<int> idx;
+            int *dseg = nullptr;
+            cudaError_t e = c.h_src_seg.empty() ? cudaSuccess : up(&dseg, c.h_src_seg);
+            if (e == cudaSuccess)
+                e = morton_sort(c, c.nsrc, 10, (int)S.size(), c.src_xyz, dseg, sample_roots(S), nullptr, keys.back(),
+                                idx, &c.tree_sort_ms);
+            if (dseg) cudaFree(dseg);
+            FCK(e);
         }
-        std::sort(keys.begin(), keys.end());
-        for (int l = 2; l <= 10; l++) {
-            const int sh = 3 * (10 - l);
-            uint64_t prev = ~0ull;
-            for (uint64_t k : keys)
-                if ((k >> sh) != prev) { occ[l] += 1; prev = k >> sh; }
-        }
+        for (const auto &K : keys)
+            for (int l = 2; l <= 10; l++) {
+                const int sh = 3 * (10 - l);
+                uint64_t prev = ~0ull;
+                for (uint64_t k : K)
+                    if ((k >> sh) != prev) { occ[l] += 1; prev = k >> sh; }
+            }
+        c.tree_wall_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
     auto closest = [&](double target) {
         int best = 2;
@@ -1145,7 +1174,10 @@ int fmm_build(Ctx &c) {
         t->fp32 = fp32;
         int s = fmm_build_forest(c, cands[k]);
         if (s != FG_OK) return s;
-        if (cands.size() == 1) return FG_OK;
+        if (cands.size() == 1) {
+            c.fmm_setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_begin).count();
+            return FG_OK;
+        }
         // autotune: time two evaluations (of all charge sets, as the steps run them) with
         // the current charges (values do not matter)
         cudaEvent_t a, b;
@@ -1168,7 +1200,9 @@ int fmm_build(Ctx &c) {
     FmmTree *t = new FmmTree();
     c.fmm = t;
     t->fp32 = fp32;
-    return fmm_build_forest(c, bestL);
+    const int s = fmm_build_forest(c, bestL);
+    c.fmm_setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_begin).count();
+    return s;
 }
 
 // Per-sample octree of depth L (host vectors, sample-local indices).
@@ -1180,6 +1214,7 @@ struct TreeH {
 };
 
 static int fmm_build_forest(Ctx &c, int L) {
+    const auto t_tree = std::chrono::steady_clock::now();
     FmmTree *t = static_cast<FmmTree *>(c.fmm);
     const bool fp32 = t->fp32;
     t->L = L;
@@ -1191,18 +1226,37 @@ static int fmm_build_forest(Ctx &c, int L) {
     t->s0 = SP[0].side;
     for (int d = 0; d < 3; d++) t->c0[d] = SP[0].c0[d];
     std::vector<TreeH> T(nseg);
+    if (!c.opts.fmm_tree_host) {
+        // (leaf key, point) pairs of every sample in key order, from the device radix sort of
+        // the sources and of the magnetic nodes
+        const uint64_t cell_mask = (1ull << (3 * L)) - 1ull;
+        std::vector<uint64_t> keys;
+        std::vector<int> idx;
+        int *dseg = nullptr;
+        cudaError_t e = c.h_src_seg.empty() ? cudaSuccess : up(&dseg, c.h_src_seg);
+        if (e == cudaSuccess)
+            e = morton_sort(c, c.nsrc, L, nseg, c.src_xyz, dseg, sample_roots(SP), nullptr, keys, idx, &c.tree_sort_ms);
+        if (dseg) cudaFree(dseg);
+        FCK(e);
+        for (size_t k = 0; k < keys.size(); k++) T[keys[k] >> (3 * L)].sk.push_back({keys[k] & cell_mask, idx[k]});
+        FCK(morton_sort(c, c.nn, L, nseg, c.xyz, c.batch ? c.node_seg : nullptr, sample_roots(SP), c.mag, keys, idx,
+                        &c.tree_sort_ms));
+        for (size_t k = 0; k < keys.size(); k++) T[keys[k] >> (3 * L)].tk.push_back({keys[k] & cell_mask, idx[k]});
+    }
     for (int g = 0; g < nseg; g++) {
         const SamplePts &P = SP[g];
         TreeH &H = T[g];
-        auto cell_of = [&](const double *p) {
-            int ijk[3];
-            for (int d = 0; d < 3; d++) ijk[d] = std::min(nside - 1, std::max(0, (int)(((p[d] - P.c0[d]) / P.side + 0.5) * nside)));
-            return morton(ijk[0], ijk[1], ijk[2]);
-        };
-        for (int s : P.src) H.sk.push_back({cell_of(&c.h_src_xyz[3 * (size_t)s]), s});
-        for (int i : P.tgt) H.tk.push_back({cell_of(&c.h_xyz[3 * (size_t)i]), i});
-        std::sort(H.sk.begin(), H.sk.end());
-        std::sort(H.tk.begin(), H.tk.end());
+        if (c.opts.fmm_tree_host) {
+            auto cell_of = [&](const double *p) {
+                int ijk[3];
+                for (int d = 0; d < 3; d++) ijk[d] = std::min(nside - 1, std::max(0, (int)(((p[d] - P.c0[d]) / P.side + 0.5) * nside)));
+                return morton(ijk[0], ijk[1], ijk[2]);
+            };
+            for (int s : P.src) H.sk.push_back({cell_of(&c.h_src_xyz[3 * (size_t)s]), s});
+            for (int i : P.tgt) H.tk.push_back({cell_of(&c.h_xyz[3 * (size_t)i]), i});
+            std::sort(H.sk.begin(), H.sk.end());
+            std::sort(H.tk.begin(), H.tk.end());
+        }
         std::vector<uint64_t> a, b;
         for (auto &p : H.sk) if (a.empty() || a.back() != p.first) a.push_back(p.first);
         for (auto &p : H.tk) if (b.empty() || b.back() != p.first) b.push_back(p.first);
@@ -1501,6 +1555,7 @@ static int fmm_build_forest(Ctx &c, int L) {
     if (c.opts.verbose)
         fprintf(stderr, "fmm: L=%d trees=%d leaves=%d cells=%d m2l=%zu p2p_pairs=%zu (%s)\n", L, nseg, nleaf, ncell,
                 t->n_m2l, t->n_p2p_pairs, fp32 ? "fp32" : "fp64");
+    c.tree_wall_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_tree).count();
     return FG_OK;
 }
 

@@ -112,6 +112,13 @@ struct BicgArgs {
     double dt;
     const double *u0;
     double *u1, *v1;
+    // batch of independent samples (k_bicg64_seg): sample g owns nodes
+    // [seg_node[g], seg_node[g+1]) and blocks [seg_blk[g], seg_blk[g+1]), its own dt and c0
+    int nseg;
+    const int *seg_node, *seg_blk;
+    const SegPar *seg;
+    SegAcc *acc;          // per-sample accumulation over a run (nullable)
+    const int *step_ctr;  // step index of the run (with acc)
 };
 
 // Arguments of the FP32 inner Krylov solve with FP64 iterative refinement.
@@ -226,6 +233,10 @@ struct Ctx {
     // device: demag
     std::vector<double> h_src_xyz;  // source points (original order), host copy for the FMM tree
     int nseg = 1;                   // independent samples packed in this context
+    // FMM set-up in fg_create: wall time of the whole set-up (tree builds, table uploads, the
+    // depth autotune's evaluations), of the tree builds alone, and device time of the Morton
+    // key and radix-sort kernels
+    double fmm_setup_ms = 0.0, tree_wall_ms = 0.0, tree_sort_ms = 0.0;
     std::vector<int> h_src_seg, h_node_seg;  // sample of every source / node (empty: one sample)
     int *src_dst = nullptr;      // original source index -> storage position (FMM order)
     void *fmm = nullptr;         // FMM tree and buffers (fg_fmm.cu)
@@ -324,6 +335,10 @@ cudaError_t launch_state_diff(Ctx &c);  // dstate = NEXT - CURRENT for u and v
 cudaError_t launch_energy(Ctx &c, const double Hext[3]);
 cudaError_t launch_energy_into(Ctx &c, const double Hext[3], double *partial);
 int bicg_grid_size(Ctx &c, bool mixed);
+cudaError_t morton_sort(Ctx &c, int n, int L, int nseg, const double *xyz, const int *seg,
+                        const std::vector<double4> &roots, const unsigned char *keep, std::vector<uint64_t> &keys,
+                        std::vector<int> &idx, double *dev_ms);
+int bicg_seg_max_blocks(Ctx &c);  // co-resident blocks of the batched FP64 solver
 int mixed_grid_size(Ctx &c);
 int mixed_max_blocks(Ctx &c);
 // Chooses the lanes per row of the mixed solver (opts.solver_lpr, or the fastest of 1, 4, 8

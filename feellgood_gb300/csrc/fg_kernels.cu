@@ -774,6 +774,268 @@ timeout:
     }
 }
 
+// The same FP64 BiCGSTAB for a batch of independent samples (a block-diagonal system):
+// every sample runs the iteration of k_bicg64 with its own scalars, |b|, stopping test and
+// node update (its own dt and c0), exactly as if it were solved alone, on its own range of
+// blocks; a sample that has stopped idles through the remaining grid barriers. The loop
+// ends when no sample is active: an activity flag rides along the first reduction of each
+// pass (slot 1, summed over the whole grid).
+__global__ void __launch_bounds__(256) k_bicg64_seg(BicgArgs a) {
+    const int G = gridDim.x;
+    int g = 0;
+    {
+        int lo = 0, hi = a.nseg - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a.seg_blk[mid] <= (int)blockIdx.x) lo = mid;
+            else hi = mid - 1;
+        }
+        g = lo;
+    }
+    const int r_lo = a.seg_node[g], r_hi = a.seg_node[g + 1];
+    const int b0 = a.seg_blk[g], b1 = a.seg_blk[g + 1];
+    const int stride = (b1 - b0) * blockDim.x;
+    const int i0 = r_lo + (blockIdx.x - b0) * blockDim.x + threadIdx.x;
+    const double c0 = a.seg[g].c0, dt = a.seg[g].dt;
+    {
+        double bb = 0.0, rr = 0.0;
+        for (int i = i0; i < r_hi; i += stride) {
+            double y0, y1;
+            const double xp = a.x[2 * i], xq = a.x[2 * i + 1];
+            apply_row(i, a.Sptr, a.Scol, a.Sval, a.W, a.ep, a.eq, a.A, a.Dl, c0, xp, xq, y0, y1);
+            const bool m = a.mag[i];
+            const double bv0 = m ? a.b[2 * i] : 0.0, bv1 = m ? a.b[2 * i + 1] : 0.0;
+            const double r0 = m ? bv0 - y0 : 0.0, r1 = m ? bv1 - y1 : 0.0;
+            a.r[2 * i] = r0; a.r[2 * i + 1] = r1;
+            a.rt[2 * i] = r0; a.rt[2 * i + 1] = r1;
+            a.p[2 * i] = r0; a.p[2 * i + 1] = r1;
+            bb += bv0 * bv0 + bv1 * bv1;
+            rr += r0 * r0 + r1 * r1;
+        }
+        double v2[2] = {bb, rr};
+        block_store<2>(v2, a.partial, G);
+    }
+    if (!grid_sync(a.bar)) goto timeout;
+    {
+        double s2[2];
+        range_sum<2>(a.partial, G, b0, b1, s2);
+        const double rhsn = sqrt(fabs(s2[0]));
+        const double resmax = a.tol;
+        double rr = s2[1], rtr = s2[1];
+        double rho1 = 0.0, rho2 = 0.0, alpha = 0.0, beta = 0.0, omega = 0.0;
+        int status = -1, nit = 0;
+        double res = sqrt(fabs(rr));
+        const double res0 = res;
+        auto finished = [&](double nr) {
+            res = fabs(nr);
+            if (isnan(res)) {
+                status = 2;
+                return false;
+            }
+            const bool cv = res <= rhsn * resmax;
+            if (cv) status = 0;
+            return cv;
+        };
+        bool act = true;
+        for (;;) {
+            if (act && finished(sqrt(fabs(rr)))) act = false;
+            if (act) {
+                rho1 = rtr;
+                if (nit > 0) {
+                    if (rho2 == 0.0 || omega == 0.0) {
+                        status = 2;
+                        act = false;
+                    } else {
+                        beta = (rho1 / rho2) * (alpha / omega);
+                    }
+                }
+            }
+            if (act)
+                for (int i = i0; i < r_hi; i += stride) {
+                    double p0 = a.p[2 * i], p1 = a.p[2 * i + 1];
+                    if (nit > 0) {
+                        p0 = (p0 - omega * a.v[2 * i]) * beta + a.r[2 * i];
+                        p1 = (p1 - omega * a.v[2 * i + 1]) * beta + a.r[2 * i + 1];
+                        a.p[2 * i] = p0; a.p[2 * i + 1] = p1;
+                    }
+                    const double h0 = a.Minv[2 * i] * p0, h1 = a.Minv[2 * i + 1] * p1;
+                    a.phat[2 * i] = h0; a.phat[2 * i + 1] = h1;
+                    tangent(i, a.ep, a.eq, h0, h1, a.W);
+                }
+            if (!grid_sync(a.bar)) goto timeout;
+            {
+                double vr = 0.0;
+                if (act)
+                    for (int i = i0; i < r_hi; i += stride) {
+                        double y0, y1;
+                        apply_row(i, a.Sptr, a.Scol, a.Sval, a.W, a.ep, a.eq, a.A, a.Dl, c0, a.phat[2 * i],
+                                  a.phat[2 * i + 1], y0, y1);
+                        if (!a.mag[i]) y0 = y1 = 0.0;
+                        a.v[2 * i] = y0; a.v[2 * i + 1] = y1;
+                        vr += y0 * a.rt[2 * i] + y1 * a.rt[2 * i + 1];
+                    }
+                double v2[2] = {vr, (threadIdx.x == 0 && act) ? 1.0 : 0.0};
+                block_store<2>(v2, a.partial, G);
+            }
+            if (!grid_sync(a.bar)) goto timeout;
+            {
+                double s1[1], f[1];
+                range_sum<1>(a.partial, G, b0, b1, s1);
+                grid_sum<1>(a.partial + G, G, f);
+                if (f[0] == 0.0) break;  // every sample has ended
+                if (act) alpha = rho1 / s1[0];
+            }
+            {
+                double ss = 0.0;
+                if (act)
+                    for (int i = i0; i < r_hi; i += stride) {
+                        const double s0 = a.r[2 * i] + (-alpha) * a.v[2 * i];
+                        const double s1 = a.r[2 * i + 1] + (-alpha) * a.v[2 * i + 1];
+                        a.s[2 * i] = s0; a.s[2 * i + 1] = s1;
+                        ss += s0 * s0 + s1 * s1;
+                    }
+                double v1[1] = {ss};
+                block_store<1>(v1, a.partial, G);
+            }
+            if (!grid_sync(a.bar)) goto timeout;
+            {
+                double s1[1];
+                range_sum<1>(a.partial, G, b0, b1, s1);
+                if (act) {
+                    if (finished(sqrt(fabs(s1[0])))) {
+                        for (int i = i0; i < r_hi; i += stride) {
+                            a.x[2 * i] += alpha * a.phat[2 * i];
+                            a.x[2 * i + 1] += alpha * a.phat[2 * i + 1];
+                        }
+                        act = false;
+                    } else if (status == 1 || status == 2) {
+                        act = false;
+                    }
+                }
+            }
+            if (act)
+                for (int i = i0; i < r_hi; i += stride) {
+                    const double h0 = a.Minv[2 * i] * a.s[2 * i], h1 = a.Minv[2 * i + 1] * a.s[2 * i + 1];
+                    a.shat[2 * i] = h0; a.shat[2 * i + 1] = h1;
+                    tangent(i, a.ep, a.eq, h0, h1, a.W);
+                }
+            if (!grid_sync(a.bar)) goto timeout;
+            {
+                double ts = 0.0, tt = 0.0;
+                if (act)
+                    for (int i = i0; i < r_hi; i += stride) {
+                        double y0, y1;
+                        apply_row(i, a.Sptr, a.Scol, a.Sval, a.W, a.ep, a.eq, a.A, a.Dl, c0, a.shat[2 * i],
+                                  a.shat[2 * i + 1], y0, y1);
+                        if (!a.mag[i]) y0 = y1 = 0.0;
+                        a.t[2 * i] = y0; a.t[2 * i + 1] = y1;
+                        ts += y0 * a.s[2 * i] + y1 * a.s[2 * i + 1];
+                        tt += y0 * y0 + y1 * y1;
+                    }
+                double v2[2] = {ts, tt};
+                block_store<2>(v2, a.partial, G);
+            }
+            if (!grid_sync(a.bar)) goto timeout;
+            {
+                double s2b[2];
+                range_sum<2>(a.partial, G, b0, b1, s2b);
+                if (act) omega = s2b[0] / s2b[1];
+            }
+            {
+                double r2 = 0.0, rtr2 = 0.0;
+                if (act)
+                    for (int i = i0; i < r_hi; i += stride) {
+#pragma unroll
+                        for (int c = 0; c < 2; c++) {
+                            const int k = 2 * i + c;
+                            double xv = a.x[k] + alpha * a.phat[k];
+                            xv += omega * a.shat[k];
+                            a.x[k] = xv;
+                            const double rv = a.s[k] - omega * a.t[k];
+                            a.r[k] = rv;
+                            r2 += rv * rv;
+                            rtr2 += a.rt[k] * rv;
+                        }
+                    }
+                double v2[2] = {r2, rtr2};
+                block_store<2>(v2, a.partial, G);
+            }
+            if (!grid_sync(a.bar)) goto timeout;
+            {
+                double s2c[2];
+                range_sum<2>(a.partial, G, b0, b1, s2c);
+                if (act) {
+                    rr = s2c[0];
+                    rtr = s2c[1];
+                    rho2 = rho1;
+                    nit++;
+                    if (nit >= a.maxiter) status = 1;
+                }
+            }
+        }
+        const bool fail = (status == 1 || status == 2 || res > resmax);
+        if (!grid_sync(a.bar)) goto timeout;
+        double v2max = 0.0;
+        if (!fail) {
+            for (int i = i0; i < r_hi; i += stride) {
+                if (!a.mag[i]) continue;
+                const double vp = a.x[2 * i], vq = a.x[2 * i + 1];
+                v2max = fmax(v2max, vp * vp + vq * vq);
+                const double pa = vp * FG_GAMMA0, qb = vq * FG_GAMMA0;
+                double nv[3], nu[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    nv[c] = pa * a.ep[3 * i + c] + qb * a.eq[3 * i + c];
+                    nu[c] = a.u0[3 * i + c] + dt * nv[c];
+                }
+                const double n = sqrt(nu[0] * nu[0] + nu[1] * nu[1] + nu[2] * nu[2]);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    a.v1[3 * i + c] = nv[c];
+                    a.u1[3 * i + c] = nu[c] / n;
+                }
+            }
+        }
+        v2max = dmax_reduce_block(v2max);
+        if (threadIdx.x == 0) {
+            SolveResult *R = a.res + g;
+            atomicMax((unsigned long long *)&R->v2max, (unsigned long long)__double_as_longlong(v2max));
+            if ((int)blockIdx.x == b0) {
+                R->status = status;
+                R->nit = nit;
+                R->fail = fail ? 1 : 0;
+                R->res = res;
+                R->rhsn = rhsn;
+                R->res0 = res0;
+            }
+            if (a.acc) {
+                SegAcc *S = a.acc + g;
+                atomicMax((unsigned long long *)&S->v2max, (unsigned long long)__double_as_longlong(v2max));
+                if ((int)blockIdx.x == b0) {
+                    S->nit_sum += nit;
+                    S->nit_max = max(S->nit_max, nit);
+                    if (fail) {
+                        if (S->fails == 0) S->first_fail = a.step_ctr ? *a.step_ctr : 0;
+                        S->fails++;
+                        S->worst = max(S->worst, status == 1 ? 1 : 2);
+                    }
+                }
+            }
+        }
+        return;
+    }
+timeout:
+    if ((int)blockIdx.x == b0 && threadIdx.x == 0) {
+        a.res[g].timeout = 1;
+        a.res[g].fail = 1;
+        if (a.acc) {
+            if (a.acc[g].fails == 0) a.acc[g].first_fail = a.step_ctr ? *a.step_ctr : 0;
+            a.acc[g].fails++;
+            a.acc[g].worst = 3;
+        }
+    }
+}
+
 // y = K x for inspection (two launches: tangent vectors, then rows).
 __global__ void k_tangent64(int nn, const double *x, const double *ep, const double *eq, double *W) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1255,6 +1517,12 @@ cudaError_t launch_node(Ctx &c, double angle) {
     return cudaGetLastError();
 }
 
+int bicg_seg_max_blocks(Ctx &c) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bicg64_seg, 256, 0);
+    return std::max(1, per_sm) * c.nsm;
+}
+
 int bicg_grid_size(Ctx &c, bool mixed) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bicg64, 256, 0);
@@ -1281,11 +1549,27 @@ cudaError_t launch_bicg64(Ctx &c, double dt, double prefactor) {
     a.partial = c.partial; a.bar = c.bar; a.res = c.dres;
     a.tol = c.opts.tol; a.maxiter = c.opts.max_iter;
     a.dt = dt; a.u0 = c.u[0]; a.u1 = c.u[1]; a.v1 = c.v[1];
+    a.nseg = 1;
+    a.seg_node = a.seg_blk = nullptr;
+    a.seg = nullptr;
+    a.acc = nullptr;
+    a.step_ctr = nullptr;
+    const bool multi = c.batch;
+    if (multi) {
+        a.nseg = c.nseg;
+        a.seg_node = c.d_seg_node;
+        a.seg_blk = c.d_seg_blk;
+        a.seg = c.seg_par;
+        a.acc = c.acc_active;
+        a.step_ctr = c.step_ctr;
+    }
     cudaError_t e = cudaMemsetAsync(c.bar, 0, sizeof(GridBar), c.stream);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(c.dres, 0, sizeof(SolveResult), c.stream);
+    e = cudaMemsetAsync(c.dres, 0, sizeof(SolveResult) * a.nseg, c.stream);
     if (e != cudaSuccess) return e;
     void *args[] = {&a};
+    if (multi)
+        return cudaLaunchCooperativeKernel((void *)k_bicg64_seg, dim3(c.seg_grid), dim3(256), args, 0, c.stream);
     return cudaLaunchCooperativeKernel((void *)k_bicg64, dim3(c.bicg_grid), dim3(256), args, 0, c.stream);
 }
 

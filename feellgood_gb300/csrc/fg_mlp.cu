@@ -41,6 +41,7 @@ constexpr int SB = 128;  // samples per training block
 struct MlpState {
     float *master = nullptr, *m1 = nullptr, *m2 = nullptr;  // FP32 master weights, Adam moments
     __nv_bfloat16 *w = nullptr;                             // BF16 weights used by the kernels
+    unsigned char *wimg = nullptr;                          // their image for the inference
     float *feat = nullptr;                                  // nn x 12
     float *gpart = nullptr;                                 // per-block gradient partials
     float *lpart = nullptr;                                 // per-block loss partials
@@ -119,9 +120,42 @@ __device__ __forceinline__ void store8(unsigned char *img, int row, int k0, uint
     *reinterpret_cast<uint4 *>(img + kmaj(row, k0, sbo)) = q;
 }
 
+// The forward pass's weights as the kernel's shared memory holds them: B1 | B2 | B3 (BF16,
+// K-major core-matrix images, zero padding) | b1, b2, b3 (FP32 values of the BF16 biases).
+// Written once at creation and by every Adam update (k_adam), so that each CTA of the
+// inference copies one contiguous 12.6 KB block with 16-byte loads instead of gathering and
+// re-laying out the parameters itself.
+constexpr int IMG_BYTES = BIAS_OFF - B1_OFF + (NH + NH + NO3) * 4;
+static_assert(IMG_BYTES % 16 == 0 && B1_OFF % 16 == 0, "16-byte copies of the weight image");
+
+// Byte offset of parameter p in the weight image; *bias: stored as FP32 (else BF16).
+__device__ __forceinline__ int img_offset(int p, bool *bias) {
+    *bias = false;
+    if (p < OFF_B1) return kmaj((p - OFF_W1) / NF, (p - OFF_W1) % NF, SBO_K16);
+    if (p < OFF_W2) { *bias = true; return BIAS_OFF - B1_OFF + 4 * (p - OFF_B1); }
+    if (p < OFF_B2) return B2_OFF - B1_OFF + kmaj((p - OFF_W2) / NH, (p - OFF_W2) % NH, SBO_K64);
+    if (p < OFF_W3) { *bias = true; return BIAS_OFF - B1_OFF + 4 * (NH + p - OFF_B2); }
+    if (p < OFF_B3) return B3_OFF - B1_OFF + kmaj((p - OFF_W3) / NH, (p - OFF_W3) % NH, SBO_K64);
+    *bias = true;
+    return BIAS_OFF - B1_OFF + 4 * (2 * NH + p - OFF_B3);
+}
+
+__device__ __forceinline__ void img_store(unsigned char *img, int p, __nv_bfloat16 wb) {
+    bool bias;
+    const int o = img_offset(p, &bias);
+    if (bias) *reinterpret_cast<float *>(img + o) = __bfloat162float(wb);
+    else *reinterpret_cast<__nv_bfloat16 *>(img + o) = wb;
+}
+
+// The image of the BF16 weights w (the padding must be zero already).
+__global__ void k_mlp_pack(const __nv_bfloat16 *__restrict__ w, unsigned char *__restrict__ img) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < NPARAM) img_store(img, p, w[p]);
+}
+
 struct MlpTcArgs {
     int nn;                      // feature rows
-    const __nv_bfloat16 *w;
+    const uint4 *wimg;           // the weight image (IMG_BYTES)
     const float *xin;            // feature rows [nn][12]
     float *yout;                 // the network's outputs [nn][3]
     int *err;                    // FG_ETIMEDOUT after an expired wait
@@ -146,24 +180,12 @@ __global__ void __launch_bounds__(TM) k_mlp_infer_tc(MlpTcArgs a) {
     __shared__ uint32_t tmem_base;
     __shared__ volatile int bail;
     const int tid = threadIdx.x, warp = tid >> 5;
-    // weights and biases (BF16 weights as they are, zero padding)
-    for (int e = tid; e < NH * K1; e += TM) {
-        const int j = e / K1, k = e % K1;
-        *reinterpret_cast<__nv_bfloat16 *>(B1 + kmaj(j, k, SBO_K16)) =
-            k < NF ? a.w[OFF_W1 + j * NF + k] : __float2bfloat16(0.f);
+    // weights and biases: one contiguous copy of the prepared image
+    {
+        uint4 *dst = reinterpret_cast<uint4 *>(B1);
+#pragma unroll 4
+        for (int e = tid; e < IMG_BYTES / 16; e += TM) dst[e] = __ldg(a.wimg + e);
     }
-    for (int e = tid; e < NH * NH; e += TM) {
-        const int j = e / NH, k = e % NH;
-        *reinterpret_cast<__nv_bfloat16 *>(B2 + kmaj(j, k, SBO_K64)) = a.w[OFF_W2 + j * NH + k];
-    }
-    for (int e = tid; e < NO3 * NH; e += TM) {
-        const int j = e / NH, k = e % NH;
-        *reinterpret_cast<__nv_bfloat16 *>(B3 + kmaj(j, k, SBO_K64)) =
-            j < NO ? a.w[OFF_W3 + j * NH + k] : __float2bfloat16(0.f);
-    }
-    for (int e = tid; e < NH + NH + NO3; e += TM)
-        bias[e] = e < NH ? bf(a.w, OFF_B1 + e) : e < 2 * NH ? bf(a.w, OFF_B2 + e - NH)
-                                                             : (e - 2 * NH < NO ? bf(a.w, OFF_B3 + e - 2 * NH) : 0.f);
     if (tid == 0) {
         mbar_init(&bar, 1);
         bail = 0;
@@ -673,8 +695,8 @@ __global__ void k_scale(int G, const double *partial, int nmag, double *scale) {
 
 // Sum the block gradients in block order and apply Adam; refresh the BF16 weights.
 __global__ void k_adam(int nblk, const float *__restrict__ gpart, float *__restrict__ master, float *__restrict__ m1,
-                       float *__restrict__ m2, __nv_bfloat16 *__restrict__ w, float lr, float b1, float b2, float eps,
-                       float bc1, float bc2) {
+                       float *__restrict__ m2, __nv_bfloat16 *__restrict__ w, unsigned char *__restrict__ img, float lr,
+                       float b1, float b2, float eps, float bc1, float bc2) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= NPARAM) return;
     float g = 0.0f;
@@ -686,7 +708,9 @@ __global__ void k_adam(int nblk, const float *__restrict__ gpart, float *__restr
     const float upd = lr * (a / bc1) / (sqrtf(v / bc2) + eps);
     const float nw = master[p] - upd;
     master[p] = nw;
-    w[p] = __float2bfloat16(nw);
+    const __nv_bfloat16 wb = __float2bfloat16(nw);
+    w[p] = wb;
+    img_store(img, p, wb);
 }
 
 // ---------------------------------------------------------------------------------
@@ -724,6 +748,7 @@ int mlp_create(Ctx &c) {
     if (cudaMalloc(&s->m1, NPARAM * sizeof(float)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->m2, NPARAM * sizeof(float)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->w, NPARAM * sizeof(__nv_bfloat16)) != cudaSuccess) return FG_ECUDA;
+    if (cudaMalloc(&s->wimg, IMG_BYTES) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->feat, (size_t)c.nn * NF * sizeof(float)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->gpart, (size_t)s->nblk_train * NPARAM * sizeof(float)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->lpart, (size_t)s->nblk_train * sizeof(float)) != cudaSuccess) return FG_ECUDA;
@@ -748,6 +773,9 @@ int mlp_create(Ctx &c) {
     s->primed = false;
     cudaMemcpy(s->master, w0.data(), NPARAM * sizeof(float), cudaMemcpyHostToDevice);
     cudaMemcpy(s->w, wb.data(), NPARAM * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice);
+    cudaMemset(s->wimg, 0, IMG_BYTES);
+    k_mlp_pack<<<nb(NPARAM, 256), 256, 0, c.stream>>>(s->w, s->wimg);
+    cudaStreamSynchronize(c.stream);
     cudaMemset(s->m1, 0, NPARAM * sizeof(float));
     cudaMemset(s->m2, 0, NPARAM * sizeof(float));
     cudaMemset(s->flag, 0, sizeof(int));
@@ -760,7 +788,7 @@ void mlp_free(Ctx &c) {
     MlpState *s = static_cast<MlpState *>(c.mlp);
     if (!s) return;
     void *p[] = {s->master, s->m1, s->m2, s->w, s->feat, s->gpart, s->lpart, s->xm, s->Wm, s->rpart, s->flag,
-                 s->res2, s->vprev2, s->scale, s->spart, s->tc_err, s->rc, s->out};
+                 s->res2, s->vprev2, s->scale, s->spart, s->tc_err, s->rc, s->out, s->wimg};
     for (void *q : p)
         if (q) cudaFree(q);
     if (s->hloss) cudaFreeHost(s->hloss);
@@ -789,7 +817,7 @@ cudaError_t mlp_before_solve(Ctx &c, double c0, bool use, bool train) {
     }
     // the network's three GEMMs on the tensor cores, on the features the node kernel formed
     MlpTcArgs a{};
-    a.nn = c.nn; a.w = s->w; a.xin = s->feat; a.yout = s->out; a.err = s->tc_err;
+    a.nn = c.nn; a.wimg = reinterpret_cast<const uint4 *>(s->wimg); a.xin = s->feat; a.yout = s->out; a.err = s->tc_err;
     cudaError_t e = launch_mlp_infer_tc(c, a);
     if (e != cudaSuccess) return e;
     c.launches += 1;
@@ -836,7 +864,7 @@ cudaError_t mlp_train(Ctx &c) {
     s->t++;
     const float b1 = 0.9f, b2 = 0.999f;
     const float lr = c.opts.mlp_lr > 0 ? (float)c.opts.mlp_lr : 1e-3f;
-    k_adam<<<nb(NPARAM, 256), 256, 0, c.stream>>>(s->nblk_train, s->gpart, s->master, s->m1, s->m2, s->w, lr, b1, b2,
+    k_adam<<<nb(NPARAM, 256), 256, 0, c.stream>>>(s->nblk_train, s->gpart, s->master, s->m1, s->m2, s->w, s->wimg, lr, b1, b2,
                                                    1e-8f, 1.0f - powf(b1, (float)s->t), 1.0f - powf(b2, (float)s->t));
     cudaMemcpyAsync(s->hloss, s->lpart, s->nblk_train * sizeof(float), cudaMemcpyDeviceToHost, c.stream);
     s->steps++;
@@ -939,7 +967,7 @@ int mlp_debug_infer(Ctx &c, int n, const float *hx, float *hy) {
     }
     cudaMemcpy(dx, hx, sizeof(float) * (size_t)n * NF, cudaMemcpyHostToDevice);
     MlpTcArgs a{};
-    a.nn = n; a.w = s->w; a.xin = dx; a.yout = dy; a.err = s->tc_err;
+    a.nn = n; a.wimg = reinterpret_cast<const uint4 *>(s->wimg); a.xin = dx; a.yout = dy; a.err = s->tc_err;
     cudaError_t e = launch_mlp_infer_tc(c, a);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
     if (e == cudaSuccess) e = cudaMemcpy(hy, dy, sizeof(float) * (size_t)n * NO, cudaMemcpyDeviceToHost);

@@ -131,6 +131,8 @@ typedef struct {
                              added (the same arithmetic, results bit-identical); 0 (default):
                              one stream (on GB300 the near field's blocks crowd out the short
                              translation launches: the film's step is 0.1 ms slower overlapped) */
+    int fmm_tree_host;    /* FMM octree build: 0 (default) Morton keys and their radix sort on the
+                             device; 1 keys and a comparison sort on the host (the same tree) */
 } fg_opts;
 
 typedef struct {
@@ -381,6 +383,12 @@ int fg_measure_peaks(double out[7]);
  * synchronisation): [0] P2M, [1] M2M, [2] M2L, [3] L2L, [4] L2P + P2P (with
  * fg_opts.fmm_overlap: the near-field kernel on its own stream, concurrent with [0]-[3]). */
 int fg_fmm_timings(const fg_ctx *ctx, double ms[5]);
+
+/* FMM set-up of fg_create / fg_batch_create: out[0] wall ms of the whole set-up (octree
+ * builds for every depth the autotune tries, table uploads, the autotune's evaluations),
+ * out[1] wall ms of the octree builds alone, out[2] device ms of the Morton-key and
+ * radix-sort kernels (0 with fg_opts.fmm_tree_host), out[3] octree depth, out[4] trees. */
+int fg_fmm_tree_info(const fg_ctx *ctx, double out[5]);
 
 /* ---- host-side mesh set-up (no GPU work) ----------------------------------------
  * A set-up mesh owned by the library: the fg_mesh fields plus region names (index 0 is

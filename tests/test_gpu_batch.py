@@ -47,8 +47,8 @@ def _singles(ms, us):
     return cs
 
 
-def _batch(ms, us):
-    b = fg.Context(ms, cases.regions(alpha=0.1), **OPTS)
+def _batch(ms, us, **over):
+    b = fg.Context(ms, cases.regions(alpha=0.1), **dict(OPTS, **over))
     b.set_state(np.concatenate(us))
     b.batch_compute_all(None, energies=False)
     return b
@@ -108,18 +108,19 @@ def test_batch_of_one_is_the_single_path():
     np.testing.assert_array_equal(b.get_state(1)["v"], c.get_state(1)["v"])
 
 
-def test_batch_run_graph_equals_stepwise():
+@pytest.mark.parametrize("precision", [fg.FG_PREC_FP32_REFINE, fg.FG_PREC_FP64])
+def test_batch_run_graph_equals_stepwise(precision):
     ms, us = _samples()
     nsteps = 5
     rng = np.random.default_rng(3)
     angles = rng.uniform(0, 2 * np.pi, (nsteps, len(ms)))
-    a = _batch(ms, us)
+    a = _batch(ms, us, precision=precision)
     s, reps = a.batch_run(1e-14, 1.0, H, angles)
     assert s == fg.FG_OK
     graph, ms_dev = a.batch_run_info()
     print(f"batch run: graph replay {graph}, {ms_dev:.3f} ms for {nsteps} steps")
     assert ms_dev > 0
-    b = _batch(ms, us)
+    b = _batch(ms, us, precision=precision)
     iters = np.zeros(len(ms), dtype=int)
     for k in range(nsteps):
         s, rr = b.batch_step(1e-14, 1.0, H, angles[k])
@@ -158,3 +159,83 @@ def test_batch_solver_lanes_per_row(lpr):
         ref.batch_compute_all(None, energies=False)
         b.batch_compute_all(None, energies=False)
 
+
+
+def test_fp64_batch_steps_like_single_fp64_contexts_and_the_oracle():
+    """precision FG_PREC_FP64 in a batch: the plain FP64 BiCGSTAB per sample (k_bicg64_seg,
+    the iteration of bicg_dir, src/algebra/bicg.h:163-234, with each sample's own scalars and
+    stopping test) and the FP64 forest FMM. Three steps against single FP64 contexts (same
+    iteration counts; v within 1e-9 relative: only the order of partial sums and of the
+    translations' groups differs), and the first step of every sample against the oracle's
+    FP64 step from the same state and potentials (v within 1e-8 relative at tolerance 1e-10)."""
+    ms, us = _samples()
+    opts = dict(precision=fg.FG_PREC_FP64, demag=fg.FG_DEMAG_FMM, fmm_leaf=-3, tol=1e-10)
+    b = fg.Context(ms, cases.regions(alpha=0.1), **opts)
+    b.set_state(np.concatenate(us))
+    b.batch_compute_all(None, energies=False)
+    off = b.node_offsets
+    st0 = b.get_state(0)
+    singles = []
+    for g, (m, u) in enumerate(zip(ms, us)):
+        c = fg.Context(m, cases.regions(alpha=0.1), **opts)
+        c.set_state(u, st0["v"][off[g]:off[g + 1]], st0["phi"][off[g]:off[g + 1]], st0["phiv"][off[g]:off[g + 1]])
+        singles.append(c)
+    dt, pref = 1e-14, 1.0
+    angles = np.array([0.3, 1.1, 2.0])
+    for it in range(3):
+        s, reps = b.batch_step(dt, pref, H, angles + it)
+        assert s == fg.FG_OK
+        vb = b.get_state(1)["v"]
+        if it == 0:
+            for g, m in enumerate(ms):
+                o = fgo.Oracle(m, cases.oracle_regions(alpha=0.1))
+                o.set_solver(1e-10, 500)
+                sl = slice(off[g], off[g + 1])
+                o.set_state(st0["u"][sl], st0["v"][sl], st0["phi"][sl], st0["phiv"][sl])
+                o.base_projection(float(angles[g]))
+                ro = o.step(dt, pref, H[g])
+                assert not ro["fail"]
+                assert _rel(vb[sl], o.get_state(1)["v"]) < 1e-8
+        for g, c in enumerate(singles):
+            r = c.step(dt, pref, H[g], angles[g] + it)
+            assert r["status"] == fg.FG_OK
+            assert reps[g]["iters"] == r["iters"], (g, reps[g], r)
+            assert reps[g]["refinements"] == 0
+            assert _rel(vb[off[g]:off[g + 1]], c.get_state(1)["v"]) < 1e-9
+            assert reps[g]["res"] <= 1e-10 * reps[g]["rhsn"]
+        b.batch_compute_all(None, energies=False)
+        for c in singles:
+            c.compute_all(np.zeros(3))
+    for c in singles:
+        c.close()
+    b.close()
+
+
+@pytest.mark.parametrize("batch", [False, True])
+def test_device_tree_build_equals_host_tree_build(batch):
+    """The octree from the device Morton-key radix sort (fg_opts.fmm_tree_host 0) is the
+    octree of the host's comparison sort: the same depth from the occupancy count (the depth
+    whose mean sources per leaf is closest to 300), and bit-identical potentials (the same
+    tables in the same order)."""
+    ms, us = _samples()
+    mesh = ms if batch else cases.cuboid(24, 20, 10)
+    u = np.concatenate(us) if batch else cases.perturbed_state(mesh["xyz"], seed=5, sigma=0.2)
+    phi, info = [], []
+    for host in (1, 0):
+        opts = dict(OPTS, fmm_leaf=300, fmm_tree_host=host)  # depth from the occupancy count
+        c = fg.Context(mesh, cases.regions(alpha=0.1), **opts)
+        c.set_state(u)
+        if batch:
+            c.batch_compute_all(None, energies=False)
+        else:
+            c.compute_all(np.zeros(3))
+        st = c.get_state(0)
+        phi.append((st["phi"], st["phiv"]))
+        info.append(c.fmm_tree_info())
+        c.close()
+    print(f"octree set-up, host sort: {info[0]}; device sort: {info[1]}")
+    assert info[0]["depth"] == info[1]["depth"]
+    assert info[0]["trees"] == info[1]["trees"] == (len(ms) if batch else 1)
+    assert info[0]["sort_device_ms"] == 0.0 and info[1]["sort_device_ms"] > 0.0
+    for a, b in zip(phi[0], phi[1]):
+        np.testing.assert_array_equal(a, b)
