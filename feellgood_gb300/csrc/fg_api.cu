@@ -780,6 +780,7 @@ int fg_step(fg_ctx *h, double dt, double prefactor, const double Hext[3], double
     c.launches += 1;
     CK(cudaEventRecord(c.ev[2], c.stream));
     CK(cudaMemcpyAsync(c.hres, c.dres, sizeof(SolveResult), cudaMemcpyDeviceToHost, c.stream));
+    if (c.mlp) CK(mlp_before_sync(c));
     CK(cudaStreamSynchronize(c.stream));
     cudaEventElapsedTime(&c.ms[0], c.ev[0], c.ev[1]);
     cudaEventElapsedTime(&c.ms[1], c.ev[1], c.ev[2]);

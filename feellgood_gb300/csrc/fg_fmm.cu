@@ -289,6 +289,123 @@ __global__ void __launch_bounds__(128) k_p2m(int nleaf, const int *__restrict__ 
     }
 }
 
+// The same harmonics restricted to the columns M0..M1 (the diagonal recurrence still runs
+// from m = 0): f(n, m, re, im) for M0 <= m <= M1 only, with the values and the order of
+// operations of ups_cols.
+template <typename T, int M, int M0, int M1, typename Fn>
+__device__ __forceinline__ void ups_col_r(T x, T y, T z, T r2, T &dre, T &dim, Fn &f) {
+    if constexpr (M > 0) {
+        const T s = T(1) / T(2 * M);
+        const T nre = (x * dre - y * dim) * s, nim = (x * dim + y * dre) * s;
+        dre = nre;
+        dim = nim;
+    }
+    if constexpr (M >= M0) {
+        f(M, M, dre, dim);
+        if constexpr (M + 1 <= FMM_P) {
+            T p2re = dre, p2im = dim;
+            T p1re = z * dre, p1im = z * dim;
+            f(M + 1, M, p1re, p1im);
+#pragma unroll
+            for (int n = M + 2; n <= FMM_P; n++) {
+                const T a = T(2 * n - 1), b = T(1) / T((n + M) * (n - M));
+                const T cre = (a * z * p1re - r2 * p2re) * b, cim = (a * z * p1im - r2 * p2im) * b;
+                f(n, M, cre, cim);
+                p2re = p1re; p2im = p1im;
+                p1re = cre; p1im = cim;
+            }
+        }
+    }
+    if constexpr (M < M1) ups_col_r<T, M + 1, M0, M1>(x, y, z, r2, dre, dim, f);
+}
+
+// Reals of harmonic column m (n = m..P; real and imaginary parts for m > 0).
+__host__ __device__ constexpr int col_reals(int m) { return m == 0 ? FMM_P + 1 : 2 * (FMM_P + 1 - m); }
+// Index of (n, m, part) among the reals of the columns M0.. (column-major).
+__host__ __device__ constexpr int lidx(int M0, int n, int m, int part) {
+    int k = 0;
+    for (int c = M0; c < m; c++) k += col_reals(c);
+    return k + (m == 0 ? n : 2 * (n - m) + part);
+}
+
+// One pass of k_p2m2 over the columns M0..M1 of the NS charge sets of a leaf's sources.
+template <int NS, int M0, int M1>
+__device__ __forceinline__ void p2m2_pass(int lane, int s0, int s1, const float *__restrict__ sloc, size_t base,
+                                          const P2mSet<float> &a, const P2mSet<float> &b) {
+    constexpr int NPR = lidx(M0, FMM_P, M1, 1) + 1;
+    float acc0[NPR], acc1[NS == 2 ? NPR : 1];
+#pragma unroll
+    for (int k = 0; k < NPR; k++) acc0[k] = 0.f;
+#pragma unroll
+    for (int k = 0; k < (NS == 2 ? NPR : 1); k++) acc1[k] = 0.f;
+    for (int s = s0 + lane; s < s1; s += 32) {
+        const float x = sloc[4 * (size_t)s], y = sloc[4 * (size_t)s + 1], z = sloc[4 * (size_t)s + 2];
+        const float qa = float(a.q[s]), qb = NS == 2 ? float(b.q[s]) : 0.f;
+        if constexpr (M0 == 0) {  // the charges for the near field, once
+            a.qn[(size_t)s * a.qn_stride] = qa;
+            if constexpr (NS == 2) b.qn[(size_t)s * b.qn_stride] = qb;
+        }
+        const float r2 = x * x + y * y + z * z;
+        float dre = 1, dim = 0;
+        auto f = [&](int n, int m, float re, float im) {
+            const int k = lidx(M0, n, m, 0);
+            acc0[k] += qa * re;
+            if constexpr (NS == 2) acc1[k] += qb * re;
+            if (m) {
+                acc0[k + 1] -= qa * im;
+                if constexpr (NS == 2) acc1[k + 1] -= qb * im;
+            }
+        };
+        ups_col_r<float, 0, M0, M1>(x, y, z, r2, dre, dim, f);
+    }
+    auto put = [&](const P2mSet<float> &st, int g, float v) {
+        st.M[base + g] = v;
+        if (st.Mh) {  // split for the tensor-core translations: hi = tf32(x), lo = x - hi
+            const float hi = __uint_as_float((__float_as_uint(v) + 0x1000u) & 0xFFFFE000u);
+            st.Mh[base + g] = hi;
+            st.Ml[base + g] = v - hi;
+        }
+    };
+#pragma unroll
+    for (int m = M0; m <= M1; m++)
+#pragma unroll
+        for (int n = m; n <= FMM_P; n++)
+#pragma unroll
+            for (int part = 0; part < (m ? 2 : 1); part++) {
+                const int k = lidx(M0, n, m, part), g = ridx(n, m, part);
+                float v0 = acc0[k], v1 = NS == 2 ? acc1[NS == 2 ? k : 0] : 0.f;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    v0 += __shfl_xor_sync(0xffffffffu, v0, o);
+                    if constexpr (NS == 2) v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+                }
+                if ((g & 31) == lane) {
+                    put(a, g, v0);
+                    if constexpr (NS == 2) put(b, g, v1);
+                }
+            }
+}
+
+// P2M of the FP32 path, the NS charge sets in one pass over the sources: the harmonics of a
+// source are formed once for both sets (k_p2m forms them once per set), in three passes over
+// the harmonic columns (0-2, 3-5, 6-9: 88, 72 and 40 register accumulators for two sets)
+// that repeat the cheap diagonal recurrence. Each coefficient sums the terms of k_p2m in the
+// same order; one set (fg_demag) and two (fg_compute_all) run the same code, so a set's
+// expansion does not depend on whether the other is evaluated beside it.
+template <int NS>
+__global__ void __launch_bounds__(128) k_p2m2(int nleaf, const int *__restrict__ leaf_src,
+                                              const float *__restrict__ sloc, int leaf0, P2mSet<float> set0,
+                                              P2mSet<float> set1) {
+    const int lane = threadIdx.x & 31;
+    const int leaf = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (leaf >= nleaf) return;
+    const int s0 = leaf_src[leaf], s1 = leaf_src[leaf + 1];
+    const size_t base = (size_t)(leaf0 + leaf) * NR;
+    p2m2_pass<NS, 0, 2>(lane, s0, s1, sloc, base, set0, set1);
+    p2m2_pass<NS, 3, 5>(lane, s0, s1, sloc, base, set0, set1);
+    p2m2_pass<NS, 6, FMM_P>(lane, s0, s1, sloc, base, set0, set1);
+}
+
 // Batched translation out[c] (+)= sum_code Op[code] in[tab[c][code]] for TB output cells
 // per block. 160 threads: 10 row groups (10 rows each) x 16 column groups (CT cells each).
 template <typename T>
@@ -1663,8 +1780,13 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq) {
         }
     };
     t.ev_split[t.ev_next] = split && prof;
-    k_p2m<T><<<dim3((t.nleaf + 3) / 4, nq), 128, 0, c.stream>>>(t.nleaf, t.leaf_src, (const T *)t.sloc, t.leaf0,
-                                                                 ps[0], ps[1]);
+    if constexpr (sizeof(T) == 4) {
+        (nq == 2 ? k_p2m2<2> : k_p2m2<1>)<<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(
+            t.nleaf, t.leaf_src, (const float *)t.sloc, t.leaf0, ps[0], ps[1]);
+    } else {
+        k_p2m<T><<<dim3((t.nleaf + 3) / 4, nq), 128, 0, c.stream>>>(t.nleaf, t.leaf_src, (const T *)t.sloc, t.leaf0,
+                                                                     ps[0], ps[1]);
+    }
     if (prof) cudaEventRecord(ev[1], c.stream);
     // out (+)= sum_code Op[code] in[tab[cell][code]] over n output cells from out0; the
     // tensor-core form reads the inputs' hi/lo split and writes the outputs' split

@@ -59,10 +59,10 @@ struct SolveResult {
 };
 
 // The learned guess's per-node features, formed by the node kernel when feat is set:
-// row i = m_i, H_eff,i * inv_ms, v_prev,i * inv_v0, the mean of m over i's neighbours.
+// row i = m_i, H_eff,i * inv_ms, v_prev,i * inv_v0 (features 0..8; the mean of m over i's
+// neighbours, 9..11, is added from these rows by the inference or by k_feat_ring).
 struct NodeFeat {
     float *feat;  // [nn][12] or nullptr
-    const int *Sptr, *Scol;
     double inv_ms, inv_v0;
 };
 
@@ -291,7 +291,7 @@ struct Ctx {
     int *cand_flag = nullptr;
     const float *cand_o = nullptr;  // the solver forms the candidate from these network outputs
     const double *cand_vprev = nullptr, *cand_vprev2 = nullptr, *cand_scale = nullptr;
-    NodeFeat node_feat{nullptr, nullptr, nullptr, 0.0, 0.0};  // features the next node kernel forms
+    NodeFeat node_feat{nullptr, 0.0, 0.0};  // features the next node kernel forms
     double *heff = nullptr;  // per-node BE/A (effective field), written when the learned guess is on
 
     // batch of independent samples packed as one block-diagonal system (fg_batch_*)
@@ -392,6 +392,7 @@ int mlp_create(Ctx &c);
 void mlp_free(Ctx &c);
 cudaError_t mlp_before_solve(Ctx &c, double c0, bool use, bool train);
 cudaError_t mlp_train(Ctx &c);
+cudaError_t mlp_before_sync(Ctx &c);
 void mlp_after_sync(Ctx &c, int *accepted, double *res0_mlp, double *res0_prev, double *loss);
 long long mlp_steps(const Ctx &c);
 cudaError_t mlp_before_evolution(Ctx &c);

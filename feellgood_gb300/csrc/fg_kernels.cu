@@ -499,28 +499,19 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
         heff[3 * i + 1] = be1 * ia;
         heff[3 * i + 2] = be2 * ia;
     }
-    if (nf.feat) {  // the learned guess's 12 features: m, H_eff / Ms, v_prev / V0, 1-ring mean of m
+    if (nf.feat) {  // the learned guess's per-node features: m, H_eff / Ms, v_prev / V0 (the
+                    // 1-ring mean of m, features 9..11, is formed in FP32 from these rows later)
         float *f = nf.feat + 12 * (size_t)i;
         if (!mag[i]) {
 #pragma unroll
             for (int k = 0; k < 12; k++) f[k] = 0.f;
         } else {
-            double mb[3] = {0, 0, 0};
-            int deg = 0;
-            for (int k = nf.Sptr[i]; k < nf.Sptr[i + 1]; k++) {
-                const int j = nf.Scol[k];
-                if (j == i) continue;
-                mb[0] += u0[3 * j]; mb[1] += u0[3 * j + 1]; mb[2] += u0[3 * j + 2];
-                deg++;
-            }
-            const double id = deg ? 1.0 / deg : 0.0;
             const double hb[3] = {be0 * ia, be1 * ia, be2 * ia};
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 f[c] = (float)u[c];
                 f[3 + c] = (float)(hb[c] * nf.inv_ms);
                 f[6 + c] = (float)(v1[3 * i + c] * nf.inv_v0);
-                f[9 + c] = (float)(mb[c] * id);
             }
         }
     }

@@ -249,32 +249,57 @@ __global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
                 double rho1 = 0.0, rho2 = 0.0, alpha = 0.0, beta = 0.0, omega = 0.0;
                 int it = 0;
                 bool act = !done;
+                // Four grid barriers per iteration: the update x += alpha phat + omega shat,
+                // r = s - omega t of a full iteration is carried into the first phase of the
+                // next pass (pending), and its |r|^2 and (rt . r) come from the recurrence
+                // |s - omega t|^2 = |s|^2 - 2 omega (t . s) + omega^2 |t|^2,
+                // rt . (s - omega t) = rt . s - omega (rt . t) on the partial sums of the t phase.
+                bool pending = false;
                 for (;;) {
-                    if (act && !(rr > target2 && nit < a.maxiter)) act = false;
-                    if (act) {
+                    bool cont = act && rr > target2 && nit < a.maxiter;
+                    if (cont) {
                         rho1 = rtr;
                         if (it > 0) {
-                            if (rho2 == 0.0 || omega == 0.0) act = false;
+                            if (rho2 == 0.0 || omega == 0.0) cont = false;
                             else beta = block_once([=] { return (rho1 / rho2) * (alpha / omega); });
                         }
                     }
-                    if (!multi && !act) break;
-                    if (act) {
-                        const float fb = (float)beta, fo = (float)omega;
+                    if (pending || cont) {
+                        const float fa = (float)alpha, fo = (float)omega, fb = (float)beta;
+                        const bool upd = pending, go = cont, later = it > 0;
                         SAMPLE_ROWS(i) {
-                            float p0 = a.p[2 * i], p1 = a.p[2 * i + 1];
-                            if (it > 0) {
-                                p0 = a.r[2 * i] + fb * (p0 - fo * a.v[2 * i]);
-                                p1 = a.r[2 * i + 1] + fb * (p1 - fo * a.v[2 * i + 1]);
-                                a.p[2 * i] = p0;
-                                a.p[2 * i + 1] = p1;
+                            float rv[2];
+#pragma unroll
+                            for (int c = 0; c < 2; c++) {
+                                const int k = 2 * i + c;
+                                if (upd) {
+                                    a.d[k] += fa * a.phat[k] + fo * a.shat[k];
+                                    if (go) {
+                                        rv[c] = a.s[k] - fo * a.t[k];
+                                        a.r[k] = rv[c];
+                                    }
+                                } else if (go) {
+                                    rv[c] = a.r[k];
+                                }
                             }
-                            const float h0 = a.Minv32[2 * i] * p0, h1 = a.Minv32[2 * i + 1] * p1;
-                            a.phat[2 * i] = h0;
-                            a.phat[2 * i + 1] = h1;
-                            tangent<float>(i, a.ep32, a.eq32, h0, h1, a.W32);
+                            if (go) {
+                                float p0 = a.p[2 * i], p1 = a.p[2 * i + 1];
+                                if (later) {
+                                    p0 = rv[0] + fb * (p0 - fo * a.v[2 * i]);
+                                    p1 = rv[1] + fb * (p1 - fo * a.v[2 * i + 1]);
+                                    a.p[2 * i] = p0;
+                                    a.p[2 * i + 1] = p1;
+                                }
+                                const float h0 = a.Minv32[2 * i] * p0, h1 = a.Minv32[2 * i + 1] * p1;
+                                a.phat[2 * i] = h0;
+                                a.phat[2 * i + 1] = h1;
+                                tangent<float>(i, a.ep32, a.eq32, h0, h1, a.W32);
+                            }
                         }
                     }
+                    pending = false;
+                    act = cont;
+                    if (!multi && !act) break;
                     if (!grid_sync(a.bar)) goto timeout;
                     {
                         float vr = 0.0f;
@@ -326,10 +351,12 @@ __global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
                         block_store_f<1>(v1, a.partial, G);
                     }
                     if (!grid_sync(a.bar)) goto timeout;
+                    double ssum = 0.0;
                     {
                         double s1c[1];
                         range_sum<1>(a.partial, G, sv.b0, sv.b1, s1c);
-                        if (act && s1c[0] <= target2) {
+                        ssum = s1c[0];
+                        if (act && ssum <= target2) {
                             const float fa = (float)alpha;
                             SAMPLE_ROWS(i) {
                                 a.d[2 * i] += fa * a.phat[2 * i];
@@ -342,7 +369,7 @@ __global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
                     }
                     if (!multi && !act) break;
                     {
-                        float ts = 0.0f, tt = 0.0f;
+                        float ts = 0.0f, tt = 0.0f, rts = 0.0f, rtt = 0.0f;
                         if (act) {
                             auto row = [&](int i, bool valid, int sub) {
                                 float y0 = 0, y1 = 0;
@@ -353,50 +380,31 @@ __global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
                                     if (!a.mag[i]) y0 = y1 = 0.0f;
                                     a.t[2 * i] = y0;
                                     a.t[2 * i + 1] = y1;
-                                    ts += y0 * a.s[2 * i] + y1 * a.s[2 * i + 1];
+                                    const float s0 = a.s[2 * i], s1 = a.s[2 * i + 1];
+                                    const float q0 = a.rt[2 * i], q1 = a.rt[2 * i + 1];
+                                    ts += y0 * s0 + y1 * s1;
                                     tt += y0 * y0 + y1 * y1;
+                                    rts += q0 * s0 + q1 * s1;
+                                    rtt += q0 * y0 + q1 * y1;
                                 }
                             };
                             GROUP_ROWS(row)
                         }
-                        float v2[2] = {ts, tt};
-                        block_store_f<2>(v2, a.partial, G);
+                        float v4[4] = {ts, tt, rts, rtt};
+                        block_store_f<4>(v4, a.partial, G);
                     }
                     if (!grid_sync(a.bar)) goto timeout;
                     {
-                        double s2b[2];
-                        range_sum<2>(a.partial, G, sv.b0, sv.b1, s2b);
-                        if (act) omega = block_once([=] { return s2b[0] / s2b[1]; });
-                    }
-                    {
-                        float r2 = 0.0f, rtr2 = 0.0f;
+                        double s4[4];
+                        range_sum<4>(a.partial, G, sv.b0, sv.b1, s4);
                         if (act) {
-                            const float fa = (float)alpha, fo = (float)omega;
-                            SAMPLE_ROWS(i) {
-#pragma unroll
-                                for (int c = 0; c < 2; c++) {
-                                    const int k = 2 * i + c;
-                                    a.d[k] += fa * a.phat[k] + fo * a.shat[k];
-                                    const float rv = a.s[k] - fo * a.t[k];
-                                    a.r[k] = rv;
-                                    r2 += rv * rv;
-                                    rtr2 += a.rt[k] * rv;
-                                }
-                            }
-                        }
-                        float v2[2] = {r2, rtr2};
-                        block_store_f<2>(v2, a.partial, G);
-                    }
-                    if (!grid_sync(a.bar)) goto timeout;
-                    {
-                        double s2c[2];
-                        range_sum<2>(a.partial, G, sv.b0, sv.b1, s2c);
-                        if (act) {
-                            rr = s2c[0];
-                            rtr = s2c[1];
+                            omega = block_once([=] { return s4[0] / s4[1]; });
+                            rr = fmax(0.0, ssum - 2.0 * omega * s4[0] + omega * omega * s4[1]);
+                            rtr = s4[2] - omega * s4[3];
                             rho2 = rho1;
                             it++;
                             nit++;
+                            pending = true;
                         }
                     }
                 }

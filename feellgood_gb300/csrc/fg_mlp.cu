@@ -15,8 +15,10 @@
 // path the solver forms the candidate in its first phase and, in its first FP64 residual
 // pass, takes the blend of the two guesses with the smallest residual norm; on the FP64 path
 // separate kernels keep the candidate only when its FP64 initial residual is smaller. The
-// node kernel forms the features; inference runs the network's three GEMMs on the tensor
-// cores (BF16 operands, FP32 accumulation in tensor memory). The network is trained online
+// node kernel forms each node's own features; the inference adds the 1-ring mean of m from
+// the neighbours' rows (FP32 sums, so that the FP64 node kernel gathers nothing more) and
+// runs the network's three GEMMs on the tensor cores (BF16 operands, FP32 accumulation in
+// tensor memory). The network is trained online
 // on (features, solved v)
 // pairs with hand-written kernels: BF16 weights (FP32 master copy, Adam), FP32
 // accumulation, deterministic fixed-order reductions.
@@ -25,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <vector>
 
 #include "fg_device.cuh"
@@ -37,6 +40,13 @@ constexpr int NF = 12, NH = 64, NO = 3;
 constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NH * NF, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH,
               OFF_W3 = OFF_B2 + NH, OFF_B3 = OFF_W3 + NO * NH, NPARAM = OFF_B3 + NO;
 constexpr int SB = 128;  // samples per training block
+
+// The per-step results read back at the step's one host synchronisation (one copy).
+struct MlpFlags {
+    int tc_err;      // FG_ETIMEDOUT from a tensor-core wait
+    int flag;        // the candidate guess was taken (blend weight > 0)
+    double res2[2];  // |r_cand|^2, |r_fallback|^2 of the first FP64 residual
+};
 
 struct MlpState {
     float *master = nullptr, *m1 = nullptr, *m2 = nullptr;  // FP32 master weights, Adam moments
@@ -62,6 +72,7 @@ struct MlpState {
     long long steps = 0;   // training steps done
     double loss = 0.0;
     float *hloss = nullptr;  // pinned
+    MlpFlags *dflags = nullptr, *hflags = nullptr;  // device, pinned copy (flag, res2, tc_err point into dflags)
 };
 
 __device__ __forceinline__ float bf(const __nv_bfloat16 *w, int k) { return __bfloat162float(w[k]); }
@@ -80,7 +91,8 @@ __device__ __forceinline__ float tanh_sfu(float x) {
 //   layer 1  D1[128 x 64] = X[128 x 16] W1^T      (12 features padded to K = 16), 1 MMA
 //   layer 2  D2[128 x 64] = H1[128 x 64] W2^T     4 MMAs of K = 16
 //   layer 3  D3[128 x 16] = H2[128 x 64] W3^T     (3 outputs padded to N = 16), 4 MMAs
-// Thread t of the CTA owns node t of the tile: it reads the node's features, writes its BF16
+// Thread t of the CTA owns node t of the tile: it reads the node's features (forming the
+// 1-ring mean of m from its neighbours' rows in FP32), writes its BF16
 // row of X, drains its row of D1 / D2 with tcgen05.ld (TMEM lane t), adds the bias, applies
 // tanh and writes its BF16 row of H for the next layer; one thread issues the MMAs.
 // Operands sit in shared memory in the no-swizzle K-major layout of 8-row x 16-byte core
@@ -156,10 +168,44 @@ __global__ void k_mlp_pack(const __nv_bfloat16 *__restrict__ w, unsigned char *_
 struct MlpTcArgs {
     int nn;                      // feature rows
     const uint4 *wimg;           // the weight image (IMG_BYTES)
-    const float *xin;            // feature rows [nn][12]
+    float *xin;                  // feature rows [nn][12]
+    // with Sptr set, features 9..11 of a row are formed here: the mean of features 0..2 (m)
+    // over the node's neighbours in the stiffness pattern (written back when ring_out is set)
+    const int *Sptr, *Scol;
+    int ring_out;
     float *yout;                 // the network's outputs [nn][3]
     int *err;                    // FG_ETIMEDOUT after an expired wait
 };
+
+// Features 9..11 of node i: the mean of m (features 0..2, FP32) over i's neighbours in the
+// stiffness pattern (the nodes sharing a magnetic tetrahedron with i; zero rows elsewhere).
+__device__ __forceinline__ void ring_mean(int i, const int *__restrict__ Sptr, const int *__restrict__ Scol,
+                                          const float *feat, float *mean) {
+    float m0 = 0.f, m1 = 0.f, m2 = 0.f;
+    int deg = 0;
+    for (int k = Sptr[i]; k < Sptr[i + 1]; k++) {
+        const int j = Scol[k];
+        if (j == i) continue;
+        m0 += feat[NF * (size_t)j];
+        m1 += feat[NF * (size_t)j + 1];
+        m2 += feat[NF * (size_t)j + 2];
+        deg++;
+    }
+    const float id = deg ? 1.0f / (float)deg : 0.0f;
+    mean[0] = m0 * id;
+    mean[1] = m1 * id;
+    mean[2] = m2 * id;
+}
+
+// Features 9..11 of every node (steps that train the network without using it).
+__global__ void k_feat_ring(int nn, const int *__restrict__ Sptr, const int *__restrict__ Scol, float *feat) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    float m[3];
+    ring_mean(i, Sptr, Scol, feat, m);
+#pragma unroll
+    for (int c = 0; c < 3; c++) feat[NF * (size_t)i + 9 + c] = m[c];
+}
 
 // Drains 16 TMEM columns of this thread's lane (row) into v[0..15].
 __device__ __forceinline__ void drain16(uint32_t taddr, float *v) {
@@ -235,7 +281,14 @@ __global__ void __launch_bounds__(TM) k_mlp_infer_tc(MlpTcArgs a) {
         const bool live = i < a.nn;
         float x[NF];
 #pragma unroll
-        for (int k = 0; k < NF; k++) x[k] = live ? a.xin[(size_t)i * NF + k] : 0.f;
+        for (int k = 0; k < NF; k++) x[k] = live && (k < 9 || !a.Sptr) ? a.xin[(size_t)i * NF + k] : 0.f;
+        if (a.Sptr && live) {
+            ring_mean(i, a.Sptr, a.Scol, a.xin, x + 9);
+            if (a.ring_out) {
+#pragma unroll
+                for (int c = 0; c < 3; c++) a.xin[(size_t)i * NF + 9 + c] = x[9 + c];
+            }
+        }
         {
             const float x2[8] = {x[8], x[9], x[10], x[11], 0.f, 0.f, 0.f, 0.f};
             store8(A1, tid, 0, SBO_K16, x);
@@ -755,13 +808,17 @@ int mlp_create(Ctx &c) {
     if (cudaMalloc(&s->xm, 2 * (size_t)c.nn * sizeof(double)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->Wm, 3 * (size_t)c.nn * sizeof(double)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->rpart, 2 * (size_t)s->nblk_res * sizeof(double)) != cudaSuccess) return FG_ECUDA;
-    if (cudaMalloc(&s->flag, sizeof(int)) != cudaSuccess) return FG_ECUDA;
-    if (cudaMalloc(&s->res2, 2 * sizeof(double)) != cudaSuccess) return FG_ECUDA;
+    if (cudaMalloc(&s->dflags, sizeof(MlpFlags)) != cudaSuccess) return FG_ECUDA;
+    if (cudaMallocHost(&s->hflags, sizeof(MlpFlags)) != cudaSuccess) return FG_ECUDA;
+    cudaMemset(s->dflags, 0, sizeof(MlpFlags));
+    std::memset(s->hflags, 0, sizeof(MlpFlags));
+    s->flag = &s->dflags->flag;
+    s->res2 = s->dflags->res2;
+    s->tc_err = &s->dflags->tc_err;
     if (cudaMallocHost(&s->hloss, (size_t)s->nblk_train * sizeof(float)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->vprev2, 3 * (size_t)c.nn * sizeof(double)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->scale, sizeof(double)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->spart, (size_t)s->nblk_res * sizeof(double)) != cudaSuccess) return FG_ECUDA;
-    if (cudaMalloc(&s->tc_err, sizeof(int)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->rc, 2 * (size_t)c.nn * sizeof(double)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->out, 3 * (size_t)c.nn * sizeof(float)) != cudaSuccess) return FG_ECUDA;
     cudaMemset(s->tc_err, 0, sizeof(int));
@@ -787,11 +844,12 @@ int mlp_create(Ctx &c) {
 void mlp_free(Ctx &c) {
     MlpState *s = static_cast<MlpState *>(c.mlp);
     if (!s) return;
-    void *p[] = {s->master, s->m1, s->m2, s->w, s->feat, s->gpart, s->lpart, s->xm, s->Wm, s->rpart, s->flag,
-                 s->res2, s->vprev2, s->scale, s->spart, s->tc_err, s->rc, s->out, s->wimg};
+    void *p[] = {s->master, s->m1, s->m2, s->w, s->feat, s->gpart, s->lpart, s->xm, s->Wm, s->rpart, s->dflags,
+                 s->vprev2, s->scale, s->spart, s->rc, s->out, s->wimg};
     for (void *q : p)
         if (q) cudaFree(q);
     if (s->hloss) cudaFreeHost(s->hloss);
+    if (s->hflags) cudaFreeHost(s->hflags);
     delete s;
     c.mlp = nullptr;
 }
@@ -801,7 +859,7 @@ static double v0_scale(const Ctx &c) { return FG_GAMMA0 * c.ms_ref; }
 // Where the node kernel stores the features of the current state (inference and training).
 NodeFeat mlp_node_features(Ctx &c) {
     MlpState *s = static_cast<MlpState *>(c.mlp);
-    return NodeFeat{s->feat, c.Sptr, c.Scol, 1.0 / c.ms_ref, 1.0 / v0_scale(c)};
+    return NodeFeat{s->feat, 1.0 / c.ms_ref, 1.0 / v0_scale(c)};
 }
 
 // With use set: the network's outputs on the features this step's node kernel formed, and
@@ -809,8 +867,12 @@ NodeFeat mlp_node_features(Ctx &c) {
 // it; FP64: formed here and kept by the referee kernels when its residual is smaller).
 cudaError_t mlp_before_solve(Ctx &c, double c0, bool use, bool train) {
     MlpState *s = static_cast<MlpState *>(c.mlp);
-    (void)train;
-    if (!use) return cudaSuccess;
+    if (!use) {
+        if (!train) return cudaSuccess;
+        k_feat_ring<<<nb(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.Sptr, c.Scol, s->feat);
+        c.launches += 1;
+        return cudaGetLastError();
+    }
     if (!s->primed) {  // no history yet: the extrapolation degenerates to v_prev
         cudaMemcpyAsync(s->vprev2, c.v[0], 3 * (size_t)c.nn * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
         s->primed = true;
@@ -818,6 +880,7 @@ cudaError_t mlp_before_solve(Ctx &c, double c0, bool use, bool train) {
     // the network's three GEMMs on the tensor cores, on the features the node kernel formed
     MlpTcArgs a{};
     a.nn = c.nn; a.wimg = reinterpret_cast<const uint4 *>(s->wimg); a.xin = s->feat; a.yout = s->out; a.err = s->tc_err;
+    a.Sptr = c.Sptr; a.Scol = c.Scol; a.ring_out = train ? 1 : 0;
     cudaError_t e = launch_mlp_infer_tc(c, a);
     if (e != cudaSuccess) return e;
     c.launches += 1;
@@ -879,21 +942,23 @@ void mlp_after_sync(Ctx &c, int *accepted, double *res0_mlp, double *res0_prev, 
     for (int b = 0; b < s->nblk_train; b++) l += s->hloss[b];
     s->loss = l / (s->nblk_train * SB * NO);
     if (loss) *loss = s->loss;
-    int terr = 0;
-    cudaMemcpy(&terr, s->tc_err, sizeof(int), cudaMemcpyDeviceToHost);
-    if (terr) {
+    const MlpFlags &f = *s->hflags;  // copied by mlp_before_sync
+    if (f.tc_err) {
         s->timed_out = true;
-        cudaMemset(s->tc_err, 0, sizeof(int));
+        cudaMemsetAsync(s->tc_err, 0, sizeof(int), c.stream);
     }
     if (accepted) {
-        int f = 0;
-        double r2[2] = {0, 0};
-        cudaMemcpy(&f, s->flag, sizeof(int), cudaMemcpyDeviceToHost);
-        cudaMemcpy(r2, s->res2, 2 * sizeof(double), cudaMemcpyDeviceToHost);
-        *accepted = f;
-        *res0_mlp = std::sqrt(r2[0]);
-        *res0_prev = std::sqrt(r2[1]);
+        *accepted = f.flag;
+        *res0_mlp = std::sqrt(f.res2[0]);
+        *res0_prev = std::sqrt(f.res2[1]);
     }
+}
+
+// Enqueues the copy of this step's flags that mlp_after_sync reads after the step's sync.
+cudaError_t mlp_before_sync(Ctx &c) {
+    MlpState *s = static_cast<MlpState *>(c.mlp);
+    if (!s) return cudaSuccess;
+    return cudaMemcpyAsync(s->hflags, s->dflags, sizeof(MlpFlags), cudaMemcpyDeviceToHost, c.stream);
 }
 
 // Gradient of the mean-squared loss for caller-given samples (nblk*SB of them, device
@@ -968,6 +1033,8 @@ int mlp_debug_infer(Ctx &c, int n, const float *hx, float *hy) {
     cudaMemcpy(dx, hx, sizeof(float) * (size_t)n * NF, cudaMemcpyHostToDevice);
     MlpTcArgs a{};
     a.nn = n; a.wimg = reinterpret_cast<const uint4 *>(s->wimg); a.xin = dx; a.yout = dy; a.err = s->tc_err;
+    a.Sptr = a.Scol = nullptr;  // the caller's rows are complete
+    a.ring_out = 0;
     cudaError_t e = launch_mlp_infer_tc(c, a);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
     if (e == cudaSuccess) e = cudaMemcpy(hy, dy, sizeof(float) * (size_t)n * NO, cudaMemcpyDeviceToHost);
