@@ -465,6 +465,12 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     CK(upload(&c.Sval, Sval));
     CK(upload(&c.A, A));
     {
+        std::vector<double> ainv(A.size(), 0.0);
+        for (size_t i = 0; i < A.size(); i++)
+            if (mag[i]) ainv[i] = 1.0 / A[i];
+        CK(upload(&c.Ainv, ainv));
+    }
+    {
         std::vector<float> s32(Sval.begin(), Sval.end()), a32(A.size());
         const double sc = 1.0 / c.mean_A;
         for (size_t i = 0; i < A.size(); i++) a32[i] = (float)(A[i] * sc);
@@ -530,7 +536,6 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     CK(dalloc(&c.epart, 7 * (size_t)c.epart_blocks));
     CK(cudaMallocHost((void **)&c.hepart, 7 * sizeof(double) * c.epart_blocks));
     if (c.opts.learned_guess) {
-        CK(dalloc(&c.heff, 3 * (size_t)nn));
         int sm = mlp_create(c);
         if (sm != FG_OK) {
             c.err = "fg_create: learned-guess buffers";
@@ -660,7 +665,7 @@ void fg_destroy(fg_ctx *h) {
     Ctx &c = h->c;
     if (c.stream) cudaStreamSynchronize(c.stream);
     void *ptrs[] = {c.xyz, c.tet, c.da, c.detJ, c.treg, c.regs, c.mag, c.inc_ptr, c.inc, c.Sptr, c.Scol, c.Sval,
-                    c.Sval32, c.A, c.A32, c.tri, c.tri_c, c.tinc_ptr, c.tinc, c.src_xyz, c.mag_nodes, c.u[0], c.u[1],
+                    c.Sval32, c.A, c.Ainv, c.A32, c.tri, c.tri_c, c.tinc_ptr, c.tinc, c.src_xyz, c.mag_nodes, c.u[0], c.u[1],
                     c.v[0], c.v[1], c.phi[0], c.phi[1], c.phiv[0], c.phiv[1], c.ep, c.eq, c.ep32, c.eq32, c.Dl32,
                     c.slot, c.Dl, c.rhs, c.x, c.bv, c.W, c.fv, c.partial, c.bar, c.dres, c.src_q, c.tri_slot,
                     c.pot, c.epart, c.src_dst, c.src_q2, c.tri_slot2, c.pot2, c.tri_be, c.hsp, c.da_ds, c.J_ds, c.state_ds,
@@ -673,7 +678,6 @@ void fg_destroy(fg_ctx *h) {
     spin_free(c);
     recenter_free(c);
     batch_free(c);
-    if (c.heff) cudaFree(c.heff);
     if (c.hres) cudaFreeHost(c.hres);
     if (c.hflag) cudaFreeHost(c.hflag);
     if (c.hepart) cudaFreeHost(c.hepart);

@@ -202,6 +202,7 @@ struct Ctx {
     float *Sval32 = nullptr;
     int nnzS = 0;
     double *A = nullptr;        // lumped mass per node
+    double *Ainv = nullptr;     // 1 / A on the magnetic nodes, 0 elsewhere
     float *A32 = nullptr;
     int4 *tri = nullptr;        // magnetic triangles: 3 nodes + index
     DevTri *tri_c = nullptr;
@@ -292,7 +293,6 @@ struct Ctx {
     const float *cand_o = nullptr;  // the solver forms the candidate from these network outputs
     const double *cand_vprev = nullptr, *cand_vprev2 = nullptr, *cand_scale = nullptr;
     NodeFeat node_feat{nullptr, 0.0, 0.0};  // features the next node kernel forms
-    double *heff = nullptr;  // per-node BE/A (effective field), written when the learned guess is on
 
     // batch of independent samples packed as one block-diagonal system (fg_batch_*)
     bool batch = false;

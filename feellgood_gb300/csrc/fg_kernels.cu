@@ -427,10 +427,10 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
                          const double4 *__restrict__ slot, int slot_ds, const int *__restrict__ tinc_ptr,
                          const int *__restrict__ tinc, const double *__restrict__ tri_be,
                          const unsigned char *__restrict__ mag,
-                         const double *__restrict__ A, const double *__restrict__ u0, const double *__restrict__ v1,
+                         const double *__restrict__ Ainv, const double *__restrict__ u0, const double *__restrict__ v1,
                          double cr, double sr, double *__restrict__ ep, double *__restrict__ eq,
                          double *__restrict__ Dl, double *__restrict__ rhs, double *__restrict__ x,
-                         double *__restrict__ Minv, double *__restrict__ W, double *__restrict__ heff,
+                         double *__restrict__ Minv, double *__restrict__ W,
                          const int *__restrict__ node_seg, const SegPar *__restrict__ seg, NodeFeat nf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
@@ -493,12 +493,7 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
             be0 += b[0]; be1 += b[1]; be2 += b[2];
         }
     Dl[i] = dl;
-    const double ia = mag[i] ? 1.0 / A[i] : 0.0;
-    if (heff) {  // effective field BE_i / A_i, a feature of the learned guess
-        heff[3 * i] = be0 * ia;
-        heff[3 * i + 1] = be1 * ia;
-        heff[3 * i + 2] = be2 * ia;
-    }
+    const double ia = Ainv[i];  // 1 / A_i (0 off the magnetic nodes), formed once per mesh
     if (nf.feat) {  // the learned guess's per-node features: m, H_eff / Ms, v_prev / V0 (the
                     // 1-ring mean of m, features 9..11, is formed in FP32 from these rows later)
         float *f = nf.feat + 12 * (size_t)i;
@@ -1501,9 +1496,9 @@ cudaError_t launch_node(Ctx &c, double angle) {
     double *Minv = bv + 8 * n2;
     k_node64<<<nblocks(c.nn, 256), 256, 0, c.stream>>>(c.nn, c.inc_ptr, c.inc, c.slot, use_elem_ds(c) ? 1 : 0,
                                                         c.tinc_ptr, c.tinc, c.tri_be,
-                                                        c.mag, c.A, c.u[0], c.v[1],
+                                                        c.mag, c.Ainv, c.u[0], c.v[1],
                                                         cr, sr, c.ep, c.eq, c.Dl, c.rhs, c.x, Minv, c.W,
-                                                        c.mlp ? c.heff : nullptr, c.node_seg,
+                                                        c.node_seg,
                                                         c.batch ? c.seg_par : nullptr, c.node_feat);
     return cudaGetLastError();
 }

@@ -96,8 +96,9 @@ __device__ __forceinline__ float tanh_sfu(float x) {
 // row of X, drains its row of D1 / D2 with tcgen05.ld (TMEM lane t), adds the bias, applies
 // tanh and writes its BF16 row of H for the next layer; one thread issues the MMAs.
 // Operands sit in shared memory in the no-swizzle K-major layout of 8-row x 16-byte core
-// matrices (LBO 128 bytes along K; SBO = bytes of one 8-row group). TMEM: D1 and D3 in
-// columns 0..63, D2 in 64..127.
+// matrices (LBO 128 bytes along K; SBO = bytes of one 8-row group). TMEM: 64 columns, D1,
+// D2 and D3 in turn (each is drained before the next layer's MMAs are issued), so that six
+// CTAs (the shared-memory limit) fit on an SM.
 constexpr int TM = 128;        // nodes per tile
 constexpr int K1 = 16;         // layer-1 K (features padded)
 constexpr int NO3 = 16;        // layer-3 N (outputs padded)
@@ -110,7 +111,7 @@ constexpr int B2_OFF = B1_OFF + B1_BYTES, B2_BYTES = NH * NH * 2;   // 8 KB
 constexpr int B3_OFF = B2_OFF + B2_BYTES, B3_BYTES = NO3 * NH * 2;  // 2 KB
 constexpr int BIAS_OFF = B3_OFF + B3_BYTES;                         // b1, b2, b3 as FP32
 constexpr int TC_SMEM = BIAS_OFF + (NH + NH + NO3) * 4 + 1024;      // + alignment slack
-constexpr int TC_TMEM_COLS = 128;
+constexpr int TC_TMEM_COLS = 64;
 
 // Byte offset of element (row, k) in a K-major image whose 8-row groups are sbo bytes apart.
 __device__ __forceinline__ int kmaj(int row, int k, uint32_t sbo) {
@@ -183,12 +184,16 @@ __device__ __forceinline__ void ring_mean(int i, const int *__restrict__ Sptr, c
                                           const float *feat, float *mean) {
     float m0 = 0.f, m1 = 0.f, m2 = 0.f;
     int deg = 0;
-    for (int k = Sptr[i]; k < Sptr[i + 1]; k++) {
+    const int k0 = Sptr[i], k1 = Sptr[i + 1];
+#pragma unroll 4
+    for (int k = k0; k < k1; k++) {
         const int j = Scol[k];
         if (j == i) continue;
-        m0 += feat[NF * (size_t)j];
-        m1 += feat[NF * (size_t)j + 1];
-        m2 += feat[NF * (size_t)j + 2];
+        // m_j and one more feature as one 16-byte load (rows are 48 bytes)
+        const float4 f = *reinterpret_cast<const float4 *>(feat + NF * (size_t)j);
+        m0 += f.x;
+        m1 += f.y;
+        m2 += f.z;
         deg++;
     }
     const float id = deg ? 1.0f / (float)deg : 0.0f;
@@ -258,7 +263,7 @@ __global__ void __launch_bounds__(TM) k_mlp_infer_tc(MlpTcArgs a) {
                 mma_bf16(tmem, sdesc_kmajor(sA1, TC_LBO, SBO_K16), sdesc_kmajor(sB1, TC_LBO, SBO_K16),
                          idesc_bf16(TM, NH), 0u);
             } else {
-                const uint32_t d = layer == 2 ? tmem + NH : tmem;
+                const uint32_t d = tmem;
                 const uint32_t sB = layer == 2 ? sB2 : sB3;
                 const uint32_t id = idesc_bf16(TM, layer == 2 ? NH : NO3);
 #pragma unroll
@@ -280,8 +285,14 @@ __global__ void __launch_bounds__(TM) k_mlp_infer_tc(MlpTcArgs a) {
         const int i = tile * TM + tid;
         const bool live = i < a.nn;
         float x[NF];
+        {
+            // the row as three 16-byte loads (features 9..11 are replaced below when Sptr is set)
+            const float4 *row = reinterpret_cast<const float4 *>(a.xin + (size_t)(live ? i : 0) * NF);
+            const float4 r0 = row[0], r1 = row[1], r2 = row[2];
+            const float v[NF] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
 #pragma unroll
-        for (int k = 0; k < NF; k++) x[k] = live && (k < 9 || !a.Sptr) ? a.xin[(size_t)i * NF + k] : 0.f;
+            for (int k = 0; k < NF; k++) x[k] = live ? v[k] : 0.f;
+        }
         if (a.Sptr && live) {
             ring_mean(i, a.Sptr, a.Scol, a.xin, x + 9);
             if (a.ring_out) {
@@ -310,7 +321,7 @@ __global__ void __launch_bounds__(TM) k_mlp_infer_tc(MlpTcArgs a) {
 #pragma unroll
         for (int c = 0; c < NH / 16; c++) {
             float v[16];
-            drain16(lane_addr + NH + 16 * c, v);
+            drain16(lane_addr + 16 * c, v);
 #pragma unroll
             for (int k = 0; k < 16; k++) v[k] = tanh_sfu(v[k] + bias[NH + 16 * c + k]);
             store8(A2, tid, 16 * c, SBO_K64, v);
@@ -385,7 +396,7 @@ static cudaError_t launch_mlp_infer_tc(Ctx &c, const MlpTcArgs &a) {
         attr_set = true;
     }
     const int ntiles = (a.nn + TM - 1) / TM;
-    const int grid = std::max(1, std::min(ntiles, 4 * c.nsm));  // 4 CTAs of 128 TMEM columns per SM
+    const int grid = std::max(1, std::min(ntiles, 6 * c.nsm));  // 6 CTAs of 64 TMEM columns per SM
     k_mlp_infer_tc<<<grid, TM, TC_SMEM, c.stream>>>(a);
     return cudaGetLastError();
 }
