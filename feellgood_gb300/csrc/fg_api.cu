@@ -555,7 +555,18 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     }
     c.dinc = demag == FG_DEMAG_FMM && c.opts.precision == FG_PREC_FP32_REFINE && c.opts.demag_increment != 0 &&
             !c.batch;
-    if (c.dinc) CK(dalloc(&c.dstate, 6 * (size_t)c.nn));
+    if (c.dinc) {
+        // the change of the field in FP32 and the FP32 charges of the incremental evaluation:
+        // FP32 copies of da and of -Ms detJ per magnetic tet (the FP64 charge arithmetic would
+        // keep GB300's 1/64-rate FP64 pipe busy for the whole charge pass)
+        CK(dalloc(&c.dstate32, 6 * (size_t)c.nn));
+        std::vector<float> da32(da.begin(), da.end()), cq32(c.nmt);
+        for (int k = 0; k < c.nmt; k++) cq32[k] = (float)(-hreg[htreg[k]].Ms * detJ[k]);
+        CK(upload(&c.da32, da32));
+        CK(upload(&c.cq32, cq32));
+        CK(dalloc(&c.src_qf, std::max(1, c.nsrc)));
+        if (c.src_q2) CK(dalloc(&c.src_q2f, std::max(1, c.nsrc)));
+    }
     CK(cudaDeviceSynchronize());
     return FG_OK;
 }
@@ -669,7 +680,7 @@ void fg_destroy(fg_ctx *h) {
                     c.v[0], c.v[1], c.phi[0], c.phi[1], c.phiv[0], c.phiv[1], c.ep, c.eq, c.ep32, c.eq32, c.Dl32,
                     c.slot, c.Dl, c.rhs, c.x, c.bv, c.W, c.fv, c.partial, c.bar, c.dres, c.src_q, c.tri_slot,
                     c.pot, c.epart, c.src_dst, c.src_q2, c.tri_slot2, c.pot2, c.tri_be, c.hsp, c.da_ds, c.J_ds, c.state_ds,
-                    c.dstate};
+                    c.dstate32, c.da32, c.cq32, c.src_qf, c.src_q2f};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     fmm64_free(c);
@@ -888,10 +899,11 @@ static int demag_increment(fg_ctx *h) {
     const bool valid = c.dinc_valid[0] && (nq == 1 || c.dinc_valid[1]) && c.opts.demag_increment != 2;
     if (valid) {
         CK(launch_state_diff(c));
-        const double *du = c.dstate, *dv = c.dstate + 3 * (size_t)c.nn;
-        if (nq == 2) CK(launch_charges_pair(c, du, dv));
-        else CK(launch_charges(c, du));
-        CK(fmm_eval(c, nq));
+        CK(launch_charges32(c, nq));
+        c.charges32 = true;  // the FP32 FMM reads the FP32 charges of the change
+        const cudaError_t se = fmm_eval(c, nq);
+        c.charges32 = false;
+        CK(se);
         CK(launch_phi_final(c, c.phi[1], 0, c.phi[0]));
         if (nq == 2) CK(launch_phi_final(c, c.phiv[1], 1, c.phiv[0]));
         c.launches += 2 + nq + fmm_launches_per_eval(c, nq);

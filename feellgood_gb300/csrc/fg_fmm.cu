@@ -237,6 +237,7 @@ __device__ __forceinline__ void ups_cols(T x, T y, T z, Fn &&f) {
 template <typename T>
 struct P2mSet {
     const double *q;        // charges (storage order)
+    const float *qf;        // FP32 charges read instead of q (FP32 path, incremental demag), or nullptr
     T *M;                   // expansions of this set
     float *Mh, *Ml;         // their split (tensor-core translations) or nullptr
     T *qn;                  // charge for the near field, element s at qn[s * qn_stride]
@@ -340,7 +341,8 @@ __device__ __forceinline__ void p2m2_pass(int lane, int s0, int s1, const float 
     for (int k = 0; k < (NS == 2 ? NPR : 1); k++) acc1[k] = 0.f;
     for (int s = s0 + lane; s < s1; s += 32) {
         const float x = sloc[4 * (size_t)s], y = sloc[4 * (size_t)s + 1], z = sloc[4 * (size_t)s + 2];
-        const float qa = float(a.q[s]), qb = NS == 2 ? float(b.q[s]) : 0.f;
+        const float qa = a.qf ? a.qf[s] : float(a.q[s]);
+        const float qb = NS == 2 ? (b.qf ? b.qf[s] : float(b.q[s])) : 0.f;
         if constexpr (M0 == 0) {  // the charges for the near field, once
             a.qn[(size_t)s * a.qn_stride] = qa;
             if constexpr (NS == 2) b.qn[(size_t)s * b.qn_stride] = qb;
@@ -1736,6 +1738,7 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq) {
         const int q = k < nq ? k : 0;
         P2mSet<T> &p = ps[k];
         p.q = q ? c.src_q2 : c.src_q;
+        p.qf = (sizeof(T) == 4 && c.charges32) ? (q ? c.src_q2f : c.src_qf) : nullptr;
         p.M = M + q * sstride;
         p.Mh = tc ? t.Mh + q * sstride : nullptr;
         p.Ml = tc ? t.Ml + q * sstride : nullptr;

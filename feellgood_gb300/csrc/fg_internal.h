@@ -269,7 +269,10 @@ struct Ctx {
     // the field), the FP32 FMM acting on the change only, the sum kept in FP64
     bool dinc = false;
     bool dinc_valid[2] = {false, false};  // phi / phiv of CURRENT are the potentials of u / v
-    double *dstate = nullptr;            // NEXT - CURRENT: u [3 nn], then v [3 nn]
+    float *dstate32 = nullptr;           // NEXT - CURRENT in FP32: u [3 nn], then v [3 nn]
+    float *da32 = nullptr, *cq32 = nullptr;  // FP32 da [12][nmt] and -Ms detJ [nmt] (incremental demag)
+    float *src_qf = nullptr, *src_q2f = nullptr;  // FP32 charges of the change (FMM leaf order)
+    bool charges32 = false;              // the FMM evaluation reads src_qf / src_q2f
     void *fmm64 = nullptr;               // FP64 tree at the FP32 tree's depth, built on first use
     double *epart = nullptr;     // energy partials
     double *hepart = nullptr;    // pinned
@@ -331,7 +334,8 @@ cudaError_t launch_charges_pair(Ctx &c, const double *m, const double *v);  // s
 cudaError_t launch_p2p_direct(Ctx &c);
 // phi_out = base + (pot + corr) / (4 pi) (base nullptr: no base)
 cudaError_t launch_phi_final(Ctx &c, double *phi_out, int set = 0, const double *base = nullptr);
-cudaError_t launch_state_diff(Ctx &c);  // dstate = NEXT - CURRENT for u and v
+cudaError_t launch_state_diff(Ctx &c);  // dstate32 = NEXT - CURRENT for u and v (FP32)
+cudaError_t launch_charges32(Ctx &c, int nq);  // FP32 charges of dstate32 (incremental demag)
 cudaError_t launch_energy(Ctx &c, const double Hext[3]);
 cudaError_t launch_energy_into(Ctx &c, const double Hext[3], double *partial);
 int bicg_grid_size(Ctx &c, bool mixed);

@@ -29,6 +29,7 @@ namespace fg {
 
 __constant__ double c_ta[4][5];   // tet shape functions at Gauss points (src/tetra.h:50-80)
 __constant__ double c_tpds[5];
+__constant__ float c_tpds32[5];  // the same weights in FP32 (charges of the incremental demag)
 __constant__ double c_cw[4][5];   // c_ta[i][g] * c_tpds[g]: weight of vertex i at Gauss point g per unit detJ
 __constant__ double c_cws[4];     // sum_g c_cw[i][g]
 __constant__ double c_tps;        // sum_g c_tpds[g]
@@ -1105,6 +1106,71 @@ __global__ void k_charges(int nmt, int nft, const int4 *__restrict__ tet, const 
     }
 }
 
+// The charges of the change of the field (incremental demag of the FP32 path) in FP32:
+// the volume charges from FP32 copies of da and of -Ms detJ (k_charges' formula, FP32
+// arithmetic: the FP32 FMM reads FP32 charges), written as FP32 in the FMM's leaf order;
+// the triangles (few) in FP64 as in k_charges, their charges stored as FP32 and their
+// self-correction terms as FP64 for k_phi_final.
+template <int NPI, int NPF, int NQ>
+__global__ void k_charges32(int nmt, int nft, const int4 *__restrict__ tet, const float *__restrict__ da32,
+                            const float *__restrict__ cq32, const int4 *__restrict__ tri,
+                            const DevTri *__restrict__ tc, const float *__restrict__ m0, const float *__restrict__ m1,
+                            const int *__restrict__ dst, float *__restrict__ q0, float *__restrict__ q1,
+                            double *__restrict__ ts0, double *__restrict__ ts1) {
+    const float *mm[2] = {m0, m1};
+    float *qq[2] = {q0, q1};
+    double *ts[2] = {ts0, ts1};
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nmt) {
+        const int4 I = tet[k];
+        const int ind[4] = {I.x, I.y, I.z, I.w};
+        float d[4][3];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) d[i][c] = da32[(3 * i + c) * (size_t)nmt + k];
+        const float cq = cq32[k];
+#pragma unroll
+        for (int f = 0; f < NQ; f++) {
+            float dud = 0.f;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const float *pm = mm[f] + 3 * (size_t)ind[i];
+                dud += pm[0] * d[i][0] + pm[1] * d[i][1] + pm[2] * d[i][2];
+            }
+#pragma unroll
+            for (int g = 0; g < NPI; g++) {
+                const size_t s = (size_t)k * NPI + g;
+                qq[f][dst[s]] = cq * c_tpds32[g] * dud;
+            }
+        }
+    } else if (k < nmt + nft) {
+        const int f = k - nmt;
+        const int4 I = tri[f];
+        const int ind[3] = {I.x, I.y, I.z};
+        const DevTri &T = tc[f];
+#pragma unroll
+        for (int h = 0; h < NQ; h++) {
+            double sn[3];
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                const float *pm = mm[h] + 3 * (size_t)ind[i];
+                sn[i] = (double)pm[0] * T.n[0] + (double)pm[1] * T.n[1] + (double)pm[2] * T.n[2];
+            }
+#pragma unroll
+            for (int g = 0; g < NPF; g++) {
+                const double un = c_fa[0][g] * sn[0] + c_fa[1][g] * sn[1] + c_fa[2][g] * sn[2];
+                const size_t sidx = (size_t)nmt * NPI + (size_t)f * NPF + g;
+                qq[h][dst[sidx]] = (T.dMs != 0.0) ? (float)(T.dMs * T.w[g] * un) : 0.f;
+            }
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+                ts[h][3 * (size_t)f + i] =
+                    T.dMs * (T.beta[3 * i] * sn[0] + T.beta[3 * i + 1] * sn[1] + T.beta[3 * i + 2] * sn[2]);
+        }
+    }
+}
+
 // Exact FP64 direct sum pot_i = sum_s q_s / |x_i - y_s| over all sources, tiled through
 // shared memory (one thread per magnetic node).
 __global__ void __launch_bounds__(256) k_p2p_direct64(int nt, const int *__restrict__ tnode,
@@ -1154,11 +1220,11 @@ __global__ void k_phi_final(int nt, const int *__restrict__ tnode, const int *__
 
 // d = NEXT - CURRENT of u (first 3 nn) and of v (next 3 nn).
 __global__ void k_state_diff(size_t n3, const double *__restrict__ u1, const double *__restrict__ u0,
-                             const double *__restrict__ v1, const double *__restrict__ v0, double *__restrict__ d) {
+                             const double *__restrict__ v1, const double *__restrict__ v0, float *__restrict__ d) {
     const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (k >= n3) return;
-    d[k] = u1[k] - u0[k];
-    d[n3 + k] = v1[k] - v0[k];
+    d[k] = (float)(u1[k] - u0[k]);
+    d[n3 + k] = (float)(v1[k] - v0[k]);
 }
 
 // ---------------------------------------------------------------------------------
@@ -1436,6 +1502,11 @@ void upload_rules(bool one_point) {
     }
     cudaMemcpyToSymbol(c_ta, ta, sizeof(ta));
     cudaMemcpyToSymbol(c_tpds, tp, sizeof(tp));
+    {
+        float tp32[5];
+        for (int j = 0; j < 5; j++) tp32[j] = (float)tp[j];
+        cudaMemcpyToSymbol(c_tpds32, tp32, sizeof(tp32));
+    }
     double cw[4][5] = {}, cws[4] = {}, tps = 0.0;
     for (int j = 0; j < 5; j++) tps += tp[j];
     for (int i = 0; i < 4; i++)
@@ -1612,9 +1683,37 @@ cudaError_t launch_phi_final(Ctx &c, double *phi_out, int set, const double *bas
 }
 
 cudaError_t launch_state_diff(Ctx &c) {
-    if (!c.dstate) return cudaErrorInvalidValue;
+    if (!c.dstate32) return cudaErrorInvalidValue;
     const size_t n3 = 3 * (size_t)c.nn;
-    k_state_diff<<<(unsigned)((n3 + 255) / 256), 256, 0, c.stream>>>(n3, c.u[1], c.u[0], c.v[1], c.v[0], c.dstate);
+    k_state_diff<<<(unsigned)((n3 + 255) / 256), 256, 0, c.stream>>>(n3, c.u[1], c.u[0], c.v[1], c.v[0], c.dstate32);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_charges32(Ctx &c, int nq) {
+    const int n = c.nmt + c.nft;
+    if (n == 0) return cudaSuccess;
+    if (!c.dstate32 || !c.src_qf || !c.src_dst || (nq == 2 && (!c.src_q2f || !c.tri_slot2)))
+        return cudaErrorInvalidValue;
+    const float *du = c.dstate32, *dv = c.dstate32 + 3 * (size_t)c.nn;
+    if (nq == 2) {
+        if (c.npi_t == 5)
+            k_charges32<5, 4, 2><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da32, c.cq32, c.tri,
+                                                                         c.tri_c, du, dv, c.src_dst, c.src_qf,
+                                                                         c.src_q2f, c.tri_slot, c.tri_slot2);
+        else
+            k_charges32<1, 1, 2><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da32, c.cq32, c.tri,
+                                                                         c.tri_c, du, dv, c.src_dst, c.src_qf,
+                                                                         c.src_q2f, c.tri_slot, c.tri_slot2);
+    } else {
+        if (c.npi_t == 5)
+            k_charges32<5, 4, 1><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da32, c.cq32, c.tri,
+                                                                         c.tri_c, du, du, c.src_dst, c.src_qf,
+                                                                         c.src_qf, c.tri_slot, c.tri_slot);
+        else
+            k_charges32<1, 1, 1><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da32, c.cq32, c.tri,
+                                                                         c.tri_c, du, du, c.src_dst, c.src_qf,
+                                                                         c.src_qf, c.tri_slot, c.tri_slot);
+    }
     return cudaGetLastError();
 }
 
