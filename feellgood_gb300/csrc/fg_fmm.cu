@@ -34,6 +34,7 @@
 #include <queue>
 #include <vector>
 
+#include "fg_ds.cuh"
 #include "fg_f32x2.cuh"
 #include "fg_internal.h"
 
@@ -406,6 +407,134 @@ __global__ void __launch_bounds__(128) k_p2m2(int nleaf, const int *__restrict__
     p2m2_pass<NS, 0, 2>(lane, s0, s1, sloc, base, set0, set1);
     p2m2_pass<NS, 3, 5>(lane, s0, s1, sloc, base, set0, set1);
     p2m2_pass<NS, 6, FMM_P>(lane, s0, s1, sloc, base, set0, set1);
+}
+
+// ---- P2M of the FP64 path in double-single arithmetic -------------------------------
+// The harmonics and the accumulation of k_p2m's FP64 form on the FP32 pipes (GB300's FP64
+// pipe, 2 DFMA per clock and SM, made the FP64 P2M 9.9 ms of the film's FP64 evaluation):
+// the recurrences of ups_cols with every operation a double-single one (about 48 bits), the
+// coordinates as the normalised pair of their stored hi + lo parts, the charge split once.
+
+__device__ __forceinline__ dsf dsc(double x) {  // a double constant as a double-single pair
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+
+template <int M, int M0, int M1, typename Fn>
+__device__ __forceinline__ void ups_col_ds(dsf x, dsf y, dsf z, dsf r2, dsf &dre, dsf &dim, Fn &f) {
+    if constexpr (M > 0) {
+        const dsf s = dsc(1.0 / (2 * M));
+        const dsf nre = ds_mul(ds_sub(ds_mul(x, dre), ds_mul(y, dim)), s);
+        const dsf nim = ds_mul(ds_add(ds_mul(x, dim), ds_mul(y, dre)), s);
+        dre = nre;
+        dim = nim;
+    }
+    if constexpr (M >= M0) {
+        f(M, M, dre, dim);
+        if constexpr (M + 1 <= FMM_P) {
+            dsf p2re = dre, p2im = dim;
+            dsf p1re = ds_mul(z, dre), p1im = ds_mul(z, dim);
+            f(M + 1, M, p1re, p1im);
+#pragma unroll
+            for (int n = M + 2; n <= FMM_P; n++) {
+                const dsf az = ds_mul(dsf{(float)(2 * n - 1), 0.f}, z);
+                const dsf b = dsc(1.0 / ((n + M) * (n - M)));
+                const dsf cre = ds_mul(ds_sub(ds_mul(az, p1re), ds_mul(r2, p2re)), b);
+                const dsf cim = ds_mul(ds_sub(ds_mul(az, p1im), ds_mul(r2, p2im)), b);
+                f(n, M, cre, cim);
+                p2re = p1re; p2im = p1im;
+                p1re = cre; p1im = cim;
+            }
+        }
+    }
+    if constexpr (M < M1) ups_col_ds<M + 1, M0, M1>(x, y, z, r2, dre, dim, f);
+}
+
+template <int NS, int M0, int M1>
+__device__ __forceinline__ void p2m_ds_pass(int lane, int s0, int s1, const float4 *__restrict__ shi,
+                                            const float4 *__restrict__ slo, size_t base, const P2mSet<double> &a,
+                                            const P2mSet<double> &b) {
+    constexpr int NPR = lidx(M0, FMM_P, M1, 1) + 1;
+    dsf acc0[NPR], acc1[NS == 2 ? NPR : 1];
+#pragma unroll
+    for (int k = 0; k < NPR; k++) acc0[k] = dsf{0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < (NS == 2 ? NPR : 1); k++) acc1[k] = dsf{0.f, 0.f};
+    for (int s = s0 + lane; s < s1; s += 32) {
+        const float4 h = shi[s], l = slo[s];
+        const dsf x = ds_two_sum_f(h.x, l.x), y = ds_two_sum_f(h.y, l.y), z = ds_two_sum_f(h.z, l.z);
+        const double qa_d = a.q[s], qb_d = NS == 2 ? b.q[s] : 0.0;
+        const dsf qa = dsc(qa_d), qb = dsc(qb_d);
+        if constexpr (M0 == 0) {  // the charges for the near field, as k_p2m stores them
+            a.qn[(size_t)s * a.qn_stride] = qa_d;
+            if (a.qh) {
+                a.qh[(size_t)s * a.qd_stride] = qa.h;
+                a.ql[(size_t)s * a.qd_stride] = (float)(qa_d - (double)qa.h);
+            }
+            if constexpr (NS == 2) {
+                b.qn[(size_t)s * b.qn_stride] = qb_d;
+                if (b.qh) {
+                    b.qh[(size_t)s * b.qd_stride] = qb.h;
+                    b.ql[(size_t)s * b.qd_stride] = (float)(qb_d - (double)qb.h);
+                }
+            }
+        }
+        const dsf r2 = ds_add(ds_add(ds_mul(x, x), ds_mul(y, y)), ds_mul(z, z));
+        dsf dre = {1.f, 0.f}, dim = {0.f, 0.f};
+        auto f = [&](int n, int m, dsf re, dsf im) {
+            const int k = lidx(M0, n, m, 0);
+            acc0[k] = ds_add(acc0[k], ds_mul(qa, re));
+            if constexpr (NS == 2) acc1[k] = ds_add(acc1[k], ds_mul(qb, re));
+            if (m) {
+                acc0[k + 1] = ds_sub(acc0[k + 1], ds_mul(qa, im));
+                if constexpr (NS == 2) acc1[k + 1] = ds_sub(acc1[k + 1], ds_mul(qb, im));
+            }
+        };
+        ups_col_ds<0, M0, M1>(x, y, z, r2, dre, dim, f);
+    }
+    auto red = [&](dsf v) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v = ds_add(v, dsf{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)});
+        return v;
+    };
+#pragma unroll
+    for (int m = M0; m <= M1; m++)
+#pragma unroll
+        for (int n = m; n <= FMM_P; n++)
+#pragma unroll
+            for (int part = 0; part < (m ? 2 : 1); part++) {
+                const int k = lidx(M0, n, m, part), g = ridx(n, m, part);
+                const dsf v0 = red(acc0[k]);
+                dsf v1 = {0.f, 0.f};
+                if constexpr (NS == 2) v1 = red(acc1[k]);
+                if ((g & 31) == lane) {
+                    a.M[base + g] = ds_to(v0);
+                    if constexpr (NS == 2) b.M[base + g] = ds_to(v1);
+                }
+            }
+}
+
+// One warp per leaf, the NS charge sets in one pass over the sources (the FP64 tree's
+// sources as hi/lo float4 pairs): the harmonics of a source are formed once for both sets,
+// in six passes over the harmonic columns (0, 1, 2, 3, 4-5, 6-9: at most 22 reals, 88 floats
+// of accumulators for two sets); one set and two run the same code, so a set's expansion
+// does not depend on whether the other is evaluated beside it.
+template <int NS>
+__global__ void __launch_bounds__(128) k_p2m_ds(int nleaf, const int *__restrict__ leaf_src,
+                                                const float4 *__restrict__ shi, const float4 *__restrict__ slo,
+                                                int leaf0, P2mSet<double> set0, P2mSet<double> set1) {
+    const int lane = threadIdx.x & 31;
+    const int leaf = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (leaf >= nleaf) return;
+    const int s0 = leaf_src[leaf], s1 = leaf_src[leaf + 1];
+    const size_t base = (size_t)(leaf0 + leaf) * NR;
+    p2m_ds_pass<NS, 0, 0>(lane, s0, s1, shi, slo, base, set0, set1);
+    p2m_ds_pass<NS, 1, 1>(lane, s0, s1, shi, slo, base, set0, set1);
+    p2m_ds_pass<NS, 2, 2>(lane, s0, s1, shi, slo, base, set0, set1);
+    p2m_ds_pass<NS, 3, 3>(lane, s0, s1, shi, slo, base, set0, set1);
+    p2m_ds_pass<NS, 4, 5>(lane, s0, s1, shi, slo, base, set0, set1);
+    p2m_ds_pass<NS, 6, FMM_P>(lane, s0, s1, shi, slo, base, set0, set1);
 }
 
 // Batched translation out[c] (+)= sum_code Op[code] in[tab[c][code]] for TB output cells
@@ -1786,6 +1915,9 @@ static cudaError_t fmm_eval_t(Ctx &c, FmmTree &t, int nq) {
     if constexpr (sizeof(T) == 4) {
         (nq == 2 ? k_p2m2<2> : k_p2m2<1>)<<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(
             t.nleaf, t.leaf_src, (const float *)t.sloc, t.leaf0, ps[0], ps[1]);
+    } else if (t.ds) {
+        (nq == 2 ? k_p2m_ds<2> : k_p2m_ds<1>)<<<(t.nleaf + 3) / 4, 128, 0, c.stream>>>(
+            t.nleaf, t.leaf_src, (const float4 *)t.ds_src_hi, (const float4 *)t.ds_src_lo, t.leaf0, ps[0], ps[1]);
     } else {
         k_p2m<T><<<dim3((t.nleaf + 3) / 4, nq), 128, 0, c.stream>>>(t.nleaf, t.leaf_src, (const T *)t.sloc, t.leaf0,
                                                                      ps[0], ps[1]);

@@ -101,9 +101,9 @@ typedef struct {
                              0 on the CUDA cores */
     int mlp_train_every;  /* learned guess: after the first mlp_train_steps solves, train on every
                              n-th successful solve only (1, the default: on every one) */
-    int fmm_native_fp64;  /* FP64 FMM: 0 (default) near field and translations in double-single
-                             arithmetic on the FP32 pipes (relative error ~1e-13); 1 both on
-                             the FP64 pipe */
+    int fmm_native_fp64;  /* FP64 FMM: 0 (default) P2M, near field and translations in
+                             double-single arithmetic on the FP32 pipes (relative error
+                             ~1e-13); 1 all three on the FP64 pipe */
     int solver_lpr;       /* FP32 + refinement solver: lanes sharing one row of the operator
                              (1 thread per row, 4, 8); 0 (default): the fastest, timed on the
                              first step */

@@ -94,8 +94,8 @@ def test_tensor_core_split_precision():
 
 @pytest.mark.parametrize("shape,leaf", [((12, 12, 12), -3), ((40, 40, 3), -4)])
 def test_double_single_near_field(shape, leaf):
-    """The FP64 path's near field and translations in double-single arithmetic on the FP32
-    pipes against the same FMM on the FP64 pipe (same tree): FP64-level agreement."""
+    """The FP64 path's P2M, near field and translations in double-single arithmetic on the
+    FP32 pipes against the same FMM on the FP64 pipe (same tree): FP64-level agreement."""
     m = cases.cuboid(*shape)
     u = cases.perturbed_state(m["xyz"], seed=9, sigma=0.3)
     v = cases.tangent_field(u, seed=10)
