@@ -838,6 +838,28 @@ def bench_batch(args):
                   "iters_per_step_mean": float(np.mean([r["iters"] / k64 for r in reps64]))}
     b64.close()
 
+    # the same batch with the learned guess (one network for all samples): trained on the first
+    # steps by fg_batch_step, then graph-replayed with the network frozen
+    bl = fg.Context(meshes, regs, tol=TOL, max_iter=MAXITER, precision=fg.FG_PREC_FP32_REFINE,
+                    demag=fg.FG_DEMAG_FMM, learned_guess=1, mlp_train_steps=30, mlp_train_every=1)
+    bl.set_state(np.concatenate(us))
+    bl.batch_compute_all(Hext, energies=False)
+    acc = []
+    for k in range(30 + 2):
+        _, rr = bl.batch_step(dt, prefactor(dt, dt), Hext, ang[k % len(ang)])
+        if k >= 30:
+            acc += [r["guess_accepted"] for r in rr]
+        bl.batch_compute_all(Hext, energies=False)
+    kl = max(1, min(args.steps, 100))
+    bl.batch_run(dt, prefactor(dt, dt), Hext, ang[:1])
+    sl, repl = bl.batch_run(dt, prefactor(dt, dt), Hext, ang[args.warmup:args.warmup + kl])
+    msl = bl.batch_run_info()[1]
+    learned_batch = {"value": kl * BATCH_N / (msl * 1e-3), "steps": kl, "ms_per_step": msl / kl,
+                     "train_steps": 30, "accepted_frac_after_training": float(np.mean(acc)) if acc else None,
+                     "failed_solves": int(sum(r["fails"] for r in repl)),
+                     "iters_per_step_mean": float(np.mean([r["iters"] / kl for r in repl]))}
+    bl.close()
+
     # looping single contexts over the samples, the same steps: plain FP64 and FP32 + refinement
     loops = {}
     for name, prec in (("plain_fp64", fg.FG_PREC_FP64), ("fp32_refine", fg.FG_PREC_FP32_REFINE)):
@@ -873,6 +895,7 @@ def bench_batch(args):
             "batch_create_wall_s": setup_s,
             "fmm_setup": {"device_sort": tree, "host_sort": tree_host, "batch_create_wall_s_host_sort": setup_host_s},
             "fp64_batch_steps_samples_per_s": fp64_batch,
+            "learned_guess_batch_steps_samples_per_s": learned_batch,
             "speedup_fp64_batch_vs_loop_plain_fp64": fp64_batch["value"] / loops["plain_fp64"],
             "energy_sample0": [float(x) for x in E[0]],
         }

@@ -163,11 +163,12 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     if (opts) c.opts = *opts; else fg_opts_default(&c.opts);
     if (c.batch) {
         // a batch runs the FP32 + refinement or the FP64 solver and a forest FMM (one tree
-        // per sample)
+        // per sample); the learned guess (one network for all samples, judged per sample
+        // inside the FP32 + refinement solver) with the FP32 + refinement solver only
         if ((c.opts.precision != FG_PREC_FP32_REFINE && c.opts.precision != FG_PREC_FP64) ||
-            c.opts.learned_guess || c.opts.demag == FG_DEMAG_DIRECT) {
-            c.err = "fg_batch_create: a batch needs precision FG_PREC_FP32_REFINE or FG_PREC_FP64, demag FMM and "
-                    "no learned guess";
+            (c.opts.learned_guess && c.opts.precision != FG_PREC_FP32_REFINE) || c.opts.demag == FG_DEMAG_DIRECT) {
+            c.err = "fg_batch_create: a batch needs precision FG_PREC_FP32_REFINE (with or without the learned guess) "
+                    "or FG_PREC_FP64, and demag FMM";
             return FG_EINVAL;
         }
         if (c.opts.spin_acc) {

@@ -9,7 +9,10 @@
 //   - energies are reduced per sample over blocks aligned to the samples.
 // The solver is the FP32 body with FP64 refinement (k_mixed, nseg > 1) or, with precision
 // FG_PREC_FP64, the plain FP64 BiCGSTAB (k_bicg64_seg), per sample exactly the iteration of
-// a single context.
+// a single context. With the learned guess (FP32 + refinement) one network serves all
+// samples: fg_batch_step trains it on the batch's solutions as fg_step does, the solver
+// forms and judges its candidate per sample, and fg_batch_run replays its inference with
+// the network frozen.
 // fg_batch_run uploads a whole schedule of per-step parameters once and replays the step
 // (parameter select, elements, nodes, solve, two demag evaluations, evolution, step
 // counter) as one CUDA graph, so a run needs no host round trip between steps.
@@ -229,15 +232,28 @@ static int demag_launches(const Ctx &c) {
     return 1 + nq + fmm_launches_per_eval(c, nq);
 }
 
+// Whether a step uses the learned guess (after its training solves; the network of a batch is
+// trained by fg_batch_step and frozen inside fg_batch_run).
+static bool batch_use_mlp(const Ctx &c) { return c.mlp && mlp_steps(c) >= c.opts.mlp_train_steps; }
+
 // Stream-ordered body of one step of a run (the graph is a capture of exactly this).
 static cudaError_t run_body(Ctx &c) {
     const double H0[3] = {0, 0, 0};
+    const bool use = batch_use_mlp(c);
     cudaError_t e;
     if ((e = launch_select_params(c)) != cudaSuccess) return e;
     if ((e = launch_tet(c, 1.0, H0)) != cudaSuccess) return e;
-    if ((e = launch_node(c, 0.0)) != cudaSuccess) return e;
-    if ((e = batch_solve(c)) != cudaSuccess) return e;
+    if (use) c.node_feat = mlp_node_features(c);
+    e = launch_node(c, 0.0);
+    c.node_feat.feat = nullptr;
+    if (e != cudaSuccess) return e;
+    if (use && (e = mlp_before_solve(c, 0.0, true, false)) != cudaSuccess) return e;
+    e = batch_solve(c);
+    c.cand_x = c.cand_W = nullptr;  // a candidate is judged by one solve only
+    c.cand_o = nullptr;
+    if (e != cudaSuccess) return e;
     if ((e = batch_demag_all(c)) != cudaSuccess) return e;
+    if (use && (e = mlp_before_evolution(c)) != cudaSuccess) return e;
     const size_t n3 = 3 * sizeof(double) * c.nn, n1 = sizeof(double) * c.nn;
     if ((e = cudaMemcpyAsync(c.u[0], c.u[1], n3, cudaMemcpyDeviceToDevice, c.stream)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(c.v[0], c.v[1], n3, cudaMemcpyDeviceToDevice, c.stream)) != cudaSuccess) return e;
@@ -248,7 +264,7 @@ static cudaError_t run_body(Ctx &c) {
 }
 
 static int body_launches(const Ctx &c) {
-    return 5 + demag_launches(c);
+    return 5 + demag_launches(c) + (batch_use_mlp(c) ? 1 : 0);
 }
 
 static void try_capture(Ctx &c) {
@@ -261,6 +277,7 @@ static void try_capture(Ctx &c) {
         else e = (eb != cudaSuccess) ? eb : (ee != cudaSuccess ? ee : cudaErrorUnknown);
         if (g) cudaGraphDestroy(g);
     }
+    c.graph_mlp = batch_use_mlp(c);
     if (e != cudaSuccess || !c.graph) {
         if (c.graph) cudaGraphExecDestroy(c.graph);
         c.graph = nullptr;
@@ -326,15 +343,30 @@ int fg_batch_step(fg_ctx *h, const fg_sample_step *steps, fg_step_report *reps) 
     }
     CK(cudaEventRecord(c.ev[0], c.stream));
     c.step_open = true;
+    // the learned guess as in fg_step: one network for all samples, trained on the batch's
+    // solutions, its candidate judged per sample inside the solver
+    const bool use_mlp = batch_use_mlp(c);
+    const int train_every = std::max(1, c.opts.mlp_train_every);
+    const bool will_train = c.mlp && (!use_mlp || h->solves_since_train + 1 >= train_every);
     CK(launch_tet(c, 1.0, H0));
-    CK(launch_node(c, 0.0));
-    CK(cudaEventRecord(c.ev[1], c.stream));
+    if (c.mlp && (use_mlp || will_train)) c.node_feat = mlp_node_features(c);
+    const cudaError_t en = launch_node(c, 0.0);
+    c.node_feat.feat = nullptr;
+    CK(en);
     c.launches += 2;
+    if (c.mlp) CK(mlp_before_solve(c, 0.0, use_mlp, will_train));
+    CK(cudaEventRecord(c.ev[1], c.stream));
     c.acc_active = nullptr;
-    CK(batch_solve(c));
+    {
+        const cudaError_t e = batch_solve(c);
+        c.cand_x = c.cand_W = nullptr;
+        c.cand_o = nullptr;
+        CK(e);
+    }
     CK(cudaEventRecord(c.ev[2], c.stream));
     c.launches += 1;
     CK(cudaMemcpyAsync(c.hres, c.dres, sizeof(SolveResult) * ns, cudaMemcpyDeviceToHost, c.stream));
+    if (c.mlp) CK(mlp_before_sync(c));
     CK(cudaStreamSynchronize(c.stream));
     cudaEventElapsedTime(&c.ms[0], c.ev[0], c.ev[1]);
     cudaEventElapsedTime(&c.ms[1], c.ev[1], c.ev[2]);
@@ -354,6 +386,28 @@ int fg_batch_step(fg_ctx *h, const fg_sample_step *steps, fg_step_report *reps) 
             p.rhsn = r.rhsn;
             p.res0 = r.res0;
             p.res0_fallback = r.res0;
+            if (use_mlp) {
+                double r0m = 0.0, r0p = 0.0;
+                mlp_sample_flags(c, g, &p.guess_accepted, &r0m, &r0p);
+                p.res0_fallback = r0p;
+            }
+        }
+    }
+    if (c.mlp) {
+        double r0m = 0.0, r0p = 0.0;
+        mlp_after_sync(c, nullptr, &r0m, &r0p, nullptr);  // the training loss and the timeout flag
+        if (mlp_take_timeout(c)) {
+            worst = FG_ETIMEDOUT;
+            c.err = "learned guess: a tensor-core pipeline wait timed out";
+            return worst;
+        }
+        // train on this step's solutions of every sample (asynchronous)
+        if (worst == FG_OK) {
+            ++h->solves_since_train;
+            if (will_train) {
+                h->solves_since_train = 0;
+                CK(mlp_train(c));
+            }
         }
     }
     if (worst == FG_ETIMEDOUT) c.err = "persistent solver: grid barrier timed out";
@@ -380,6 +434,7 @@ int fg_batch_compute_all(fg_ctx *h, const double *Hext, double *energies) {
         CK(cudaMemcpyAsync(c.hseg_energy, c.seg_energy, 7 * sizeof(double) * ns, cudaMemcpyDeviceToHost, c.stream));
     }
     const size_t n3 = 3 * sizeof(double) * c.nn, n1 = sizeof(double) * c.nn;
+    if (c.mlp) CK(mlp_before_evolution(c));  // v_prev2 of the learned guess's extrapolation
     CK(cudaMemcpyAsync(c.u[0], c.u[1], n3, cudaMemcpyDeviceToDevice, c.stream));
     CK(cudaMemcpyAsync(c.v[0], c.v[1], n3, cudaMemcpyDeviceToDevice, c.stream));
     CK(cudaMemcpyAsync(c.phi[0], c.phi[1], n1, cudaMemcpyDeviceToDevice, c.stream));
@@ -443,6 +498,11 @@ int fg_batch_run(fg_ctx *h, int n_steps, const fg_sample_step *steps, fg_batch_r
         CK(mixed_autotune(c, 1.0, 1.0, 0.0));
     }
     c.acc_active = c.seg_acc;
+    if (c.graph_state == 1 && c.graph_mlp != batch_use_mlp(c)) {  // the network became usable: recapture
+        cudaGraphExecDestroy(c.graph);
+        c.graph = nullptr;
+        c.graph_state = 0;
+    }
     if (c.graph_state == 0) try_capture(c);
     CK(cudaEventRecord(c.ev[6], c.stream));
     for (int k = 0; k < n_steps; k++) {

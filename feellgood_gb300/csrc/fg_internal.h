@@ -319,6 +319,7 @@ struct Ctx {
     cudaGraphExec_t graph = nullptr;                    // captured step + compute_all of a run
     int graph_state = 0;                                // 0 not tried, 1 captured, -1 capture refused
     bool run_graph = false;                             // the last run replayed the graph
+    bool graph_mlp = false;                             // the captured step runs the learned guess's inference
     float run_ms = 0.f;                                 // device time of the last run
 };
 
@@ -396,6 +397,7 @@ int mlp_create(Ctx &c);
 void mlp_free(Ctx &c);
 cudaError_t mlp_before_solve(Ctx &c, double c0, bool use, bool train);
 cudaError_t mlp_train(Ctx &c);
+void mlp_sample_flags(const Ctx &c, int g, int *accepted, double *res0_mlp, double *res0_prev);
 cudaError_t mlp_before_sync(Ctx &c);
 void mlp_after_sync(Ctx &c, int *accepted, double *res0_mlp, double *res0_prev, double *loss);
 long long mlp_steps(const Ctx &c);

@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
     // the learned guess's candidate when its network outputs are given
     {
         double bb = 0.0;
-        if (a.cand_o && !multi) {
+        if (a.cand_o) {
             SAMPLE_ROWS(i) {
                 double xp = 0.0, xq = 0.0;
                 if (a.mag[i]) {
@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
         for (;;) {
             // refinement residual r64 = b - K x (FP64, masked); on the first pass with a
             // candidate guess, also the candidate's residual (the referee of the learned guess)
-            const bool judge = nref == 0 && a.cand_x != nullptr && !multi;
+            const bool judge = nref == 0 && a.cand_x != nullptr;
             {
                 double rr = 0.0, rc = 0.0, rx = 0.0;
                 if (!done) {
@@ -181,10 +181,10 @@ __global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
                     // t: no further operator application); t > 0 counts as the guess accepted
                     const double dd = s3[0] + s3[1] - 2.0 * s3[2];
                     const double t = dd > 0.0 ? fmin(1.0, fmax(0.0, (s3[0] - s3[2]) / dd)) : 0.0;
-                    if (blockIdx.x == 0 && threadIdx.x == 0) {
-                        *a.cand_flag = t > 0.0 ? 1 : 0;
-                        a.cand_res2[0] = s3[1];
-                        a.cand_res2[1] = s3[0];
+                    if (blockIdx.x == sv.b0 && threadIdx.x == 0) {  // per sample in a batch
+                        a.cand_flag[sv.g] = t > 0.0 ? 1 : 0;
+                        a.cand_res2[2 * sv.g] = s3[1];
+                        a.cand_res2[2 * sv.g + 1] = s3[0];
                     }
                     if (t > 0.0) {
                         SAMPLE_ROWS(i) {
@@ -537,12 +537,12 @@ cudaError_t launch_mixed(Ctx &c, double dt, double prefactor) {
     a.maxiter = c.opts.max_iter; a.refine_max = c.opts.refine_max;
     a.dt = dt; a.u0 = c.u[0]; a.u1 = c.u[1]; a.v1 = c.v[1];
     a.scale = 1.0 / c.mean_A;
-    a.cand_x = c.batch ? nullptr : c.cand_x;
+    a.cand_x = c.cand_x;
     a.cand_W = c.cand_W;
     a.cand_r = c.cand_r;
     a.cand_flag = c.cand_flag;
     a.cand_res2 = c.cand_res2;
-    a.cand_o = c.batch ? nullptr : c.cand_o;
+    a.cand_o = c.cand_o;
     a.cand_vprev = c.cand_vprev;
     a.cand_vprev2 = c.cand_vprev2;
     a.cand_scale = c.cand_scale;

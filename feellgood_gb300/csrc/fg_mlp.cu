@@ -41,11 +41,18 @@ constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NH * NF, OFF_W2 = OFF_B1 + NH, OFF_B
               OFF_W3 = OFF_B2 + NH, OFF_B3 = OFF_W3 + NO * NH, NPARAM = OFF_B3 + NO;
 constexpr int SB = 128;  // samples per training block
 
-// The per-step results read back at the step's one host synchronisation (one copy).
-struct MlpFlags {
-    int tc_err;      // FG_ETIMEDOUT from a tensor-core wait
-    int flag;        // the candidate guess was taken (blend weight > 0)
-    double res2[2];  // |r_cand|^2, |r_fallback|^2 of the first FP64 residual
+// The per-step results read back at the step's one host synchronisation (one copy), for
+// each of the nflag systems (the samples of a batch): one block of
+//   int tc_err (FG_ETIMEDOUT from a tensor-core wait), int pad,
+//   int flag[nflag] (the candidate guess was taken: blend weight > 0), padded to 8 bytes,
+//   double res2[2 nflag] (|r_cand|^2, |r_fallback|^2 of the first FP64 residual).
+struct MlpFlagsLayout {
+    size_t flag_off, res2_off, bytes;
+    explicit MlpFlagsLayout(int n) {
+        flag_off = 8;
+        res2_off = flag_off + 8 * (((size_t)n + 1) / 2);
+        bytes = res2_off + 16 * (size_t)n;
+    }
 };
 
 struct MlpState {
@@ -72,7 +79,8 @@ struct MlpState {
     long long steps = 0;   // training steps done
     double loss = 0.0;
     float *hloss = nullptr;  // pinned
-    MlpFlags *dflags = nullptr, *hflags = nullptr;  // device, pinned copy (flag, res2, tc_err point into dflags)
+    unsigned char *dflags = nullptr, *hflags = nullptr;  // device, pinned copy (flag, res2, tc_err point into dflags)
+    int nflag = 1;                                         // systems: 1, or the samples of a batch
 };
 
 __device__ __forceinline__ float bf(const __nv_bfloat16 *w, int k) { return __bfloat162float(w[k]); }
@@ -819,13 +827,17 @@ int mlp_create(Ctx &c) {
     if (cudaMalloc(&s->xm, 2 * (size_t)c.nn * sizeof(double)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->Wm, 3 * (size_t)c.nn * sizeof(double)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->rpart, 2 * (size_t)s->nblk_res * sizeof(double)) != cudaSuccess) return FG_ECUDA;
-    if (cudaMalloc(&s->dflags, sizeof(MlpFlags)) != cudaSuccess) return FG_ECUDA;
-    if (cudaMallocHost(&s->hflags, sizeof(MlpFlags)) != cudaSuccess) return FG_ECUDA;
-    cudaMemset(s->dflags, 0, sizeof(MlpFlags));
-    std::memset(s->hflags, 0, sizeof(MlpFlags));
-    s->flag = &s->dflags->flag;
-    s->res2 = s->dflags->res2;
-    s->tc_err = &s->dflags->tc_err;
+    s->nflag = c.batch ? std::max(1, c.nseg) : 1;
+    {
+        const MlpFlagsLayout lay(s->nflag);
+        if (cudaMalloc(&s->dflags, lay.bytes) != cudaSuccess) return FG_ECUDA;
+        if (cudaMallocHost(&s->hflags, lay.bytes) != cudaSuccess) return FG_ECUDA;
+        cudaMemset(s->dflags, 0, lay.bytes);
+        std::memset(s->hflags, 0, lay.bytes);
+        s->tc_err = reinterpret_cast<int *>(s->dflags);
+        s->flag = reinterpret_cast<int *>(s->dflags + lay.flag_off);
+        s->res2 = reinterpret_cast<double *>(s->dflags + lay.res2_off);
+    }
     if (cudaMallocHost(&s->hloss, (size_t)s->nblk_train * sizeof(float)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->vprev2, 3 * (size_t)c.nn * sizeof(double)) != cudaSuccess) return FG_ECUDA;
     if (cudaMalloc(&s->scale, sizeof(double)) != cudaSuccess) return FG_ECUDA;
@@ -895,7 +907,7 @@ cudaError_t mlp_before_solve(Ctx &c, double c0, bool use, bool train) {
     cudaError_t e = launch_mlp_infer_tc(c, a);
     if (e != cudaSuccess) return e;
     c.launches += 1;
-    if (c.opts.precision == FG_PREC_FP32_REFINE && !c.batch) {
+    if (c.opts.precision == FG_PREC_FP32_REFINE) {
         // the FP32 + refinement solver forms the smoothed candidate in its first phase and
         // judges it on its first FP64 residual
         c.cand_x = s->xm;
@@ -953,23 +965,31 @@ void mlp_after_sync(Ctx &c, int *accepted, double *res0_mlp, double *res0_prev, 
     for (int b = 0; b < s->nblk_train; b++) l += s->hloss[b];
     s->loss = l / (s->nblk_train * SB * NO);
     if (loss) *loss = s->loss;
-    const MlpFlags &f = *s->hflags;  // copied by mlp_before_sync
-    if (f.tc_err) {
+    if (*reinterpret_cast<const int *>(s->hflags)) {  // copied by mlp_before_sync
         s->timed_out = true;
         cudaMemsetAsync(s->tc_err, 0, sizeof(int), c.stream);
     }
-    if (accepted) {
-        *accepted = f.flag;
-        *res0_mlp = std::sqrt(f.res2[0]);
-        *res0_prev = std::sqrt(f.res2[1]);
-    }
+    if (accepted) mlp_sample_flags(c, 0, accepted, res0_mlp, res0_prev);
+}
+
+// The learned guess's result for system g of the last step (0: a single context; a sample of
+// a batch), from the copy read at the step's sync.
+void mlp_sample_flags(const Ctx &c, int g, int *accepted, double *res0_mlp, double *res0_prev) {
+    const MlpState *s = static_cast<const MlpState *>(c.mlp);
+    if (!s || g < 0 || g >= s->nflag) return;
+    const MlpFlagsLayout lay(s->nflag);
+    const int *flag = reinterpret_cast<const int *>(s->hflags + lay.flag_off);
+    const double *res2 = reinterpret_cast<const double *>(s->hflags + lay.res2_off);
+    *accepted = flag[g];
+    *res0_mlp = std::sqrt(res2[2 * g]);
+    *res0_prev = std::sqrt(res2[2 * g + 1]);
 }
 
 // Enqueues the copy of this step's flags that mlp_after_sync reads after the step's sync.
 cudaError_t mlp_before_sync(Ctx &c) {
     MlpState *s = static_cast<MlpState *>(c.mlp);
     if (!s) return cudaSuccess;
-    return cudaMemcpyAsync(s->hflags, s->dflags, sizeof(MlpFlags), cudaMemcpyDeviceToHost, c.stream);
+    return cudaMemcpyAsync(s->hflags, s->dflags, MlpFlagsLayout(s->nflag).bytes, cudaMemcpyDeviceToHost, c.stream);
 }
 
 // Gradient of the mean-squared loss for caller-given samples (nblk*SB of them, device

@@ -239,3 +239,42 @@ def test_device_tree_build_equals_host_tree_build(batch):
     assert info[0]["sort_device_ms"] == 0.0 and info[1]["sort_device_ms"] > 0.0
     for a, b in zip(phi[0], phi[1]):
         np.testing.assert_array_equal(a, b)
+
+
+def test_batch_learned_guess():
+    """The learned guess inside a batch (FP32 + refinement): one network for all samples,
+    trained by fg_batch_step on the batch's solutions (src/linear_algebra.cpp:13-24 is the
+    fallback), its candidate formed and judged per sample inside the solver. After the
+    training solves: every sample converges to the tolerance, the judged initial residual is
+    never above the fallback's, the candidate is taken, and the states agree with the same
+    batch stepped with the previous-step guess to the solver's tolerance; a graph-replayed
+    run with the frozen network does the same."""
+    ms, us = _samples()
+    ntrain, nuse = 30, 4
+    b = _batch(ms, us, learned_guess=1, mlp_train_steps=ntrain, mlp_train_every=1)
+    p = _batch(ms, us)
+    rng = np.random.default_rng(21)
+    accepted = 0
+    for k in range(ntrain + nuse):
+        angles = rng.uniform(0, 2 * np.pi, len(ms))
+        s1, rb = b.batch_step(1e-14, 1.0, H, angles)
+        s2, rp = p.batch_step(1e-14, 1.0, H, angles)
+        assert s1 == fg.FG_OK and s2 == fg.FG_OK
+        if k >= ntrain:
+            for r in rb:
+                assert r["res"] <= 1e-9 * r["rhsn"]
+                assert r["res0"] <= r["res0_fallback"] * (1 + 1e-12)
+                accepted += r["guess_accepted"]
+            assert _rel(b.get_state(1)["v"], p.get_state(1)["v"]) < 1e-6
+        b.batch_compute_all(None, energies=False)
+        p.batch_compute_all(None, energies=False)
+    assert accepted > 0
+    angles = rng.uniform(0, 2 * np.pi, (3, len(ms)))
+    s1, rb = b.batch_run(1e-14, 1.0, H, angles)
+    s2, rp = p.batch_run(1e-14, 1.0, H, angles)
+    assert s1 == fg.FG_OK and s2 == fg.FG_OK
+    assert all(r["fails"] == 0 for r in rb)
+    assert b.batch_run_info()[0]
+    assert _rel(b.get_state(0)["u"], p.get_state(0)["u"]) < 1e-6
+    b.close()
+    p.close()
