@@ -1265,10 +1265,21 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
 #pragma unroll
         for (int i = 0; i < 4; i++) cw[i] = ds_from(c_cws[i]);
         const dsf Hd[3] = {ds_from(Hx), ds_from(Hy), ds_from(Hz)};
+        // the region's constants as double-single pairs, formed again only when the region
+        // changes (their FP64 -> pair conversions run on the 1/64-rate FP64 pipe)
+        int rlast = -1;
+        dsf rA = {0.f, 0.f}, rD = {0.f, 0.f}, rZ = {0.f, 0.f};
         for (int k = t0; k < t1; k += stride) {
             const int4 I = tet[k];
             const int ind[4] = {I.x, I.y, I.z, I.w};
-            const DevRegion &R = regs[treg[k]];
+            const int rg = treg[k];
+            if (rg != rlast) {
+                const DevRegion &R = regs[rg];
+                rA = ds_from(R.A);
+                rD = ds_from(-0.5 * FG_MU0 * R.Ms);
+                rZ = ds_from(-FG_MU0 * R.Ms);
+                rlast = rg;
+            }
             dsf un[4][3], ph[4], d[4][3];
 #pragma unroll
             for (int i = 0; i < 4; i++) {
@@ -1304,10 +1315,9 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
                 for (int c = 0; c < 3; c++) su[c] = ds_fma(aw, un[i][c], su[c]);
                 sp = ds_fma(aw, ph[i], sp);
             }
-            dacc[0] = ds_fma(ds_mul(ds_from(R.A), ds_mul(J, tp)), dens, dacc[0]);
-            dacc[2] = ds_fma(ds_mul(ds_from(-0.5 * FG_MU0 * R.Ms), div), sp, dacc[2]);
-            dacc[3] = ds_fma(ds_from(-FG_MU0 * R.Ms),
-                             ds_fma(su[2], Hd[2], ds_fma(su[1], Hd[1], ds_mul(su[0], Hd[0]))), dacc[3]);
+            dacc[0] = ds_fma(ds_mul(rA, ds_mul(J, tp)), dens, dacc[0]);
+            dacc[2] = ds_fma(ds_mul(rD, div), sp, dacc[2]);
+            dacc[3] = ds_fma(rZ, ds_fma(su[2], Hd[2], ds_fma(su[1], Hd[1], ds_mul(su[0], Hd[0]))), dacc[3]);
             dacc[4] = ds_add(dacc[4], su[0]);
             dacc[5] = ds_add(dacc[5], su[1]);
             dacc[6] = ds_add(dacc[6], su[2]);
