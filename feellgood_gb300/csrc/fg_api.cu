@@ -484,6 +484,23 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     CK(upload(&c.tinc, tinc));
     bool surf_aniso = false;
     for (const DevTri &T : htc) surf_aniso = surf_aniso || T.Ks != 0.0;
+    if (c.elem_ds && !surf_aniso && c.nft > 0) {
+        // the double-single energies' triangle constants: normal and 0.5 mu0 dMs times each
+        // Gauss weight as (hi, lo) pairs, four float4 per triangle
+        auto split = [](double x, float &h, float &l) {
+            h = (float)x;
+            l = (float)(x - (double)h);
+        };
+        std::vector<float4> tds(4 * (size_t)c.nft, make_float4(0.f, 0.f, 0.f, 0.f));
+        for (int f = 0; f < c.nft; f++) {
+            const DevTri &T = htc[f];
+            float v[16] = {0};
+            for (int k = 0; k < 3; k++) split(T.n[k], v[2 * k], v[2 * k + 1]);
+            for (int g = 0; g < 4; g++) split(0.5 * FG_MU0 * T.dMs * T.w[g], v[6 + 2 * g], v[7 + 2 * g]);
+            for (int q = 0; q < 4; q++) tds[4 * (size_t)f + q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        }
+        CK(upload(&c.tri_ds, tds));
+    }
     if (surf_aniso && c.nft > 0) {
         CK(dalloc(&c.tri_be, 9 * (size_t)c.nft));
         CK(cudaMemset(c.tri_be, 0, 9 * sizeof(double) * c.nft));
@@ -681,7 +698,7 @@ void fg_destroy(fg_ctx *h) {
                     c.v[0], c.v[1], c.phi[0], c.phi[1], c.phiv[0], c.phiv[1], c.ep, c.eq, c.ep32, c.eq32, c.Dl32,
                     c.slot, c.Dl, c.rhs, c.x, c.bv, c.W, c.fv, c.partial, c.bar, c.dres, c.src_q, c.tri_slot,
                     c.pot, c.epart, c.src_dst, c.src_q2, c.tri_slot2, c.pot2, c.tri_be, c.hsp, c.da_ds, c.J_ds, c.state_ds,
-                    c.dstate32, c.da32, c.cq32, c.src_qf, c.src_q2f};
+                    c.dstate32, c.da32, c.cq32, c.src_qf, c.src_q2f, c.tri_ds};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     fmm64_free(c);

@@ -262,6 +262,7 @@ struct Ctx {
     // per-step double-single copies of u, phi, phiv of CURRENT
     bool elem_ds = false;
     float2 *da_ds = nullptr, *J_ds = nullptr, *state_ds = nullptr;
+    float4 *tri_ds = nullptr;  // energies: per triangle normal and 0.5 mu0 dMs w_g as double-single pairs
     double *pot = nullptr;       // nn
     double *pot2 = nullptr;      // nn, potential of src_q2
     // incremental demag of the FP32 + refinement path (fg_opts.demag_increment): NEXT's

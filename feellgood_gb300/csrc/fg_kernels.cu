@@ -34,6 +34,7 @@ __constant__ double c_cw[4][5];   // c_ta[i][g] * c_tpds[g]: weight of vertex i 
 __constant__ double c_cws[4];     // sum_g c_cw[i][g]
 __constant__ double c_tps;        // sum_g c_tpds[g]
 __constant__ double c_fa[3][4];   // triangle rule (src/triangle.h:42-64)
+__constant__ float2 c_fa_ds[3][4];  // the same weights as double-single pairs
 __constant__ double c_fpds[4];
 
 // ---------------------------------------------------------------------------------
@@ -1242,7 +1243,7 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
                                                 const double *__restrict__ segH, const double *__restrict__ hsp,
                                                 double amp, const float2 *__restrict__ da_ds,
                                                 const float2 *__restrict__ J_ds, const float2 *__restrict__ st_ds,
-                                                int nn_ds) {
+                                                int nn_ds, const float4 *__restrict__ tri_ds) {
     double acc[7] = {0, 0, 0, 0, 0, 0, 0};
     // isotropic form in double-single (FP32 + refinement path): state of NEXT and geometry as
     // double-single pairs, the Jacobian scaled by 2^DS_SLOT_SCALE; per-thread double-single sums
@@ -1325,6 +1326,48 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
 #pragma unroll
         for (int q = 0; q < 7; q++) acc[q] += std::ldexp(ds_to(dacc[q]), -DS_SLOT_SCALE);
         t1 = t0;  // the FP64 tet loop below has nothing left to do
+        if (tri_ds) {
+            // the surface demag term of the triangles (no surface anisotropy) in double-single:
+            // per triangle the normal and the Gauss weights times 0.5 mu0 dMs as pairs
+            dsf dtri = {0.f, 0.f};
+            for (int f = f0; f < f1; f += stride) {
+                const int4 I = tri[f];
+                const int ind[3] = {I.x, I.y, I.z};
+                const float4 *q = tri_ds + 4 * (size_t)f;
+                const float4 q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
+                const dsf n[3] = {{q0.x, q0.y}, {q0.z, q0.w}, {q1.x, q1.y}};
+                const dsf wq[4] = {{q1.z, q1.w}, {q2.x, q2.y}, {q2.z, q2.w}, {q3.x, q3.y}};
+                dsf un[3][3], ph[3];
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const float2 a = uds[3 * (size_t)ind[i] + c];
+                        un[i][c] = {a.x, a.y};
+                    }
+                    const float2 pp = pds[ind[i]];
+                    ph[i] = {pp.x, pp.y};
+                }
+                dsf dm = {0.f, 0.f};
+#pragma unroll
+                for (int g = 0; g < NPF; g++) {
+                    dsf U[3], pg = {0.f, 0.f};
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        U[c] = {0.f, 0.f};
+#pragma unroll
+                        for (int i = 0; i < 3; i++) U[c] = ds_fma(dsf{c_fa_ds[i][g].x, c_fa_ds[i][g].y}, un[i][c], U[c]);
+                    }
+#pragma unroll
+                    for (int i = 0; i < 3; i++) pg = ds_fma(dsf{c_fa_ds[i][g].x, c_fa_ds[i][g].y}, ph[i], pg);
+                    const dsf un_n = ds_fma(U[2], n[2], ds_fma(U[1], n[1], ds_mul(U[0], n[0])));
+                    dm = ds_fma(ds_mul(un_n, pg), wq[g], dm);
+                }
+                dtri = ds_add(dtri, dm);
+            }
+            acc[2] += ds_to(dtri);
+            f1 = f0;  // the FP64 triangle loop below has nothing left to do
+        }
     }
     for (int k = t0; k < t1; k += stride) {
         const int4 I = tet[k];
@@ -1529,6 +1572,15 @@ void upload_rules(bool one_point) {
     cudaMemcpyToSymbol(c_tps, &tps, sizeof(tps));
     upload_rules_ds(ta, tp);
     cudaMemcpyToSymbol(c_fa, fa, sizeof(fa));
+    {
+        float2 fad[3][4];
+        for (int i = 0; i < 3; i++)
+            for (int g = 0; g < 4; g++) {
+                const float h = (float)fa[i][g];
+                fad[i][g] = make_float2(h, (float)(fa[i][g] - (double)h));
+            }
+        cudaMemcpyToSymbol(c_fa_ds, fad, sizeof(fad));
+    }
     cudaMemcpyToSymbol(c_fpds, fp, sizeof(fp));
 }
 
@@ -1747,11 +1799,13 @@ cudaError_t launch_energy_into(Ctx &c, const double H[3], double *partial) {
     if (c.npi_t == 5)
         (energy_iso(c) ? k_energy<5, 4, true> : k_energy<5, 4, false>)<<<G, 256, 0, c.stream>>>(
             c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c, c.u[1], c.phi[1], H[0], H[1], H[2],
-            partial, nullptr, nullptr, nullptr, c.hsp, c.field_amp, dda, c.J_ds, c.state_ds, c.nn);
+            partial, nullptr, nullptr, nullptr, c.hsp, c.field_amp, dda, c.J_ds, c.state_ds, c.nn,
+            dsp ? c.tri_ds : nullptr);
     else
         (energy_iso(c) ? k_energy<1, 1, true> : k_energy<1, 1, false>)<<<G, 256, 0, c.stream>>>(
             c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c, c.u[1], c.phi[1], H[0], H[1], H[2],
-            partial, nullptr, nullptr, nullptr, c.hsp, c.field_amp, dda, c.J_ds, c.state_ds, c.nn);
+            partial, nullptr, nullptr, nullptr, c.hsp, c.field_amp, dda, c.J_ds, c.state_ds, c.nn,
+            dsp ? c.tri_ds : nullptr);
     return cudaGetLastError();
 }
 
@@ -1763,12 +1817,12 @@ cudaError_t launch_energy_seg(Ctx &c) {
         (c.aniso ? k_energy<5, 4, false> : k_energy<5, 4, true>)<<<G, 256, 0, c.stream>>>(
             c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
                                                  c.u[1], c.phi[1], H0[0], H0[1], H0[2], c.seg_epart, c.eblk_rng,
-                                                 c.eblk_seg, c.seg_H, nullptr, 0.0, nullptr, nullptr, nullptr, 0);
+                                                 c.eblk_seg, c.seg_H, nullptr, 0.0, nullptr, nullptr, nullptr, 0, nullptr);
     else
         (c.aniso ? k_energy<1, 1, false> : k_energy<1, 1, true>)<<<G, 256, 0, c.stream>>>(
             c.nmt, c.nft, c.tet, c.da, c.detJ, c.treg, c.regs, c.tri, c.tri_c,
                                                  c.u[1], c.phi[1], H0[0], H0[1], H0[2], c.seg_epart, c.eblk_rng,
-                                                 c.eblk_seg, c.seg_H, nullptr, 0.0, nullptr, nullptr, nullptr, 0);
+                                                 c.eblk_seg, c.seg_H, nullptr, 0.0, nullptr, nullptr, nullptr, 0, nullptr);
     k_seg_energy_sum<<<c.nseg, 32, 0, c.stream>>>(G, c.d_seg_eblk, c.seg_epart, c.seg_energy);
     return cudaGetLastError();
 }
