@@ -451,8 +451,9 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
         e[0] = (m == 0) - u[m] * u[0];
         e[1] = (m == 1) - u[m] * u[1];
         e[2] = (m == 2) - u[m] * u[2];
-        // one reciprocal instead of three divisions (GB300's FP64 pipe is 1/64 rate)
-        const double in = 1.0 / sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+        // one reciprocal square root instead of a square root and three divisions (GB300's
+        // FP64 pipe is 1/64 rate); the norm is exact to a few ulp either way
+        const double in = rsqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
         e[0] *= in; e[1] *= in; e[2] *= in;
         q[0] = u[1] * e[2] - u[2] * e[1];
         q[1] = u[2] * e[0] - u[0] * e[2];

@@ -397,34 +397,65 @@ __global__ void __launch_bounds__(256, 4) k_spin_mixed(SpinArgs a) {
                 grid_sum<1>(a.partial, G, s1i);
                 double rr = s1i[0], rtr = s1i[0];
                 double rho1 = 0.0, rho2 = 0.0, alpha = 0.0, beta = 0.0, omega = 0.0;
+                // four grid barriers per iteration, as k_mixed: the update d += alpha phat +
+                // omega shat, r = s - omega t of a full iteration is carried into the first phase
+                // of the next pass, and |r|^2, rt . r come from the recurrence on the partial
+                // sums of the t phase
+                bool pending = false;
                 for (int it = 0;; it++) {
-                    if (!(rr > target2 && nit < a.maxiter)) break;
-                    rho1 = rtr;
-                    if (it > 0) {
-                        if (rho2 == 0.0 || omega == 0.0) break;
-                        beta = block_once([=] { return (rho1 / rho2) * (alpha / omega); });
-                    }
-                    {
-                        const float fb = (float)beta, fo = (float)omega;
-                        float4 *__restrict__ P = reinterpret_cast<float4 *>(a.fp);
-                        float4 *__restrict__ PH = reinterpret_cast<float4 *>(a.fphat);
-                        const float4 *__restrict__ R = reinterpret_cast<const float4 *>(a.fr);
-                        const float4 *__restrict__ V = reinterpret_cast<const float4 *>(a.fv);
-                        const float4 *__restrict__ D = reinterpret_cast<const float4 *>(a.dinv3);
-                        for (int q = i0; q < a.n4; q += stride) {
-                            float4 pv = P[q];
-                            if (it > 0) {
-                                const float4 r = R[q], v = V[q];
-                                pv.x = r.x + fb * (pv.x - fo * v.x);
-                                pv.y = r.y + fb * (pv.y - fo * v.y);
-                                pv.z = r.z + fb * (pv.z - fo * v.z);
-                                pv.w = r.w + fb * (pv.w - fo * v.w);
-                                P[q] = pv;
-                            }
-                            const float4 d = D[q];
-                            PH[q] = make_float4(d.x * pv.x, d.y * pv.y, d.z * pv.z, d.w * pv.w);
+                    bool cont = rr > target2 && nit < a.maxiter;
+                    if (cont) {
+                        rho1 = rtr;
+                        if (it > 0) {
+                            if (rho2 == 0.0 || omega == 0.0) cont = false;
+                            else beta = block_once([=] { return (rho1 / rho2) * (alpha / omega); });
                         }
                     }
+                    if (pending || cont) {
+                        const float fa = (float)alpha, fb = (float)beta, fo = (float)omega;
+                        const bool upd = pending, go = cont, later = it > 0;
+                        float4 *__restrict__ P = reinterpret_cast<float4 *>(a.fp);
+                        float4 *__restrict__ PH = reinterpret_cast<float4 *>(a.fphat);
+                        float4 *__restrict__ R4 = reinterpret_cast<float4 *>(a.fr);
+                        float4 *__restrict__ D4 = reinterpret_cast<float4 *>(a.fd);
+                        const float4 *__restrict__ V = reinterpret_cast<const float4 *>(a.fv);
+                        const float4 *__restrict__ SH = reinterpret_cast<const float4 *>(a.fshat);
+                        const float4 *__restrict__ S4 = reinterpret_cast<const float4 *>(a.fs);
+                        const float4 *__restrict__ T4 = reinterpret_cast<const float4 *>(a.ft);
+                        const float4 *__restrict__ D = reinterpret_cast<const float4 *>(a.dinv3);
+                        for (int q = i0; q < a.n4; q += stride) {
+                            float4 rv = make_float4(0.f, 0.f, 0.f, 0.f);
+                            if (upd) {
+                                float4 d = D4[q];
+                                const float4 h = PH[q], g = SH[q];
+                                d.x += fa * h.x + fo * g.x; d.y += fa * h.y + fo * g.y;
+                                d.z += fa * h.z + fo * g.z; d.w += fa * h.w + fo * g.w;
+                                D4[q] = d;
+                                if (go) {
+                                    const float4 sv = S4[q], t = T4[q];
+                                    rv = make_float4(sv.x - fo * t.x, sv.y - fo * t.y, sv.z - fo * t.z, sv.w - fo * t.w);
+                                    R4[q] = rv;
+                                }
+                            } else if (go) {
+                                rv = R4[q];
+                            }
+                            if (go) {
+                                float4 pv = P[q];
+                                if (later) {
+                                    const float4 v = V[q];
+                                    pv.x = rv.x + fb * (pv.x - fo * v.x);
+                                    pv.y = rv.y + fb * (pv.y - fo * v.y);
+                                    pv.z = rv.z + fb * (pv.z - fo * v.z);
+                                    pv.w = rv.w + fb * (pv.w - fo * v.w);
+                                    P[q] = pv;
+                                }
+                                const float4 d = D[q];
+                                PH[q] = make_float4(d.x * pv.x, d.y * pv.y, d.z * pv.z, d.w * pv.w);
+                            }
+                        }
+                    }
+                    pending = false;
+                    if (!cont) break;
                     if (!grid_sync(a.bar)) goto timeout;
                     {
                         float vr = 0.0f;
@@ -449,6 +480,7 @@ __global__ void __launch_bounds__(256, 4) k_spin_mixed(SpinArgs a) {
                         grid_sum<1>(a.partial, G, s1b);
                         alpha = block_once([=] { return rho1 / s1b[0]; });
                     }
+                    double ssum = 0.0;
                     {
                         float ss = 0.0f;
                         const float fa = (float)alpha;
@@ -471,7 +503,8 @@ __global__ void __launch_bounds__(256, 4) k_spin_mixed(SpinArgs a) {
                     {
                         double s1c[1];
                         grid_sum<1>(a.partial, G, s1c);
-                        if (s1c[0] <= target2) {
+                        ssum = s1c[0];
+                        if (ssum <= target2) {
                             const float fa = (float)alpha;
                             float4 *__restrict__ D4 = reinterpret_cast<float4 *>(a.fd);
                             const float4 *__restrict__ PH = reinterpret_cast<const float4 *>(a.fphat);
@@ -486,7 +519,7 @@ __global__ void __launch_bounds__(256, 4) k_spin_mixed(SpinArgs a) {
                         }
                     }
                     {
-                        float ts = 0.0f, tt = 0.0f;
+                        float ts = 0.0f, tt = 0.0f, rts = 0.0f, rtt = 0.0f;
                         auto row = [&](int i, bool valid, int sub) {
                             float y[3];
                             spin_row<float, SPIN_LPR>(valid, i, sub, a.ptr, a.col, a.A32, a.cc32, a.m32, a.dir,
@@ -494,56 +527,34 @@ __global__ void __launch_bounds__(256, 4) k_spin_mixed(SpinArgs a) {
                             if (!valid || sub != 0) return;
 #pragma unroll
                             for (int c = 0; c < 3; c++) {
+                                const float sv = a.fs[3 * i + c], rt = a.frt[3 * i + c];
                                 a.ft[3 * i + c] = y[c];
-                                ts += y[c] * a.fs[3 * i + c];
+                                ts += y[c] * sv;
                                 tt += y[c] * y[c];
+                                rts += rt * sv;
+                                rtt += rt * y[c];
                             }
                         };
                         SPIN_ROWS(row)
-                        float v2[2] = {ts, tt};
-                        block_store_f<2>(v2, a.partial, G);
+                        float v4[4] = {ts, tt, rts, rtt};
+                        block_store_f<4>(v4, a.partial, G);
                     }
                     if (!grid_sync(a.bar)) goto timeout;
                     {
-                        double s2[2];
-                        grid_sum<2>(a.partial, G, s2);
-                        omega = block_once([=] { return s2[0] / s2[1]; });
-                    }
-                    {
-                        float r2 = 0.0f, rtr2 = 0.0f;
-                        const float fa = (float)alpha, fo = (float)omega;
-                        float4 *__restrict__ D4 = reinterpret_cast<float4 *>(a.fd);
-                        float4 *__restrict__ R4 = reinterpret_cast<float4 *>(a.fr);
-                        const float4 *__restrict__ PH = reinterpret_cast<const float4 *>(a.fphat);
-                        const float4 *__restrict__ SH = reinterpret_cast<const float4 *>(a.fshat);
-                        const float4 *__restrict__ S4 = reinterpret_cast<const float4 *>(a.fs);
-                        const float4 *__restrict__ T4 = reinterpret_cast<const float4 *>(a.ft);
-                        const float4 *__restrict__ RT = reinterpret_cast<const float4 *>(a.frt);
-                        for (int q = i0; q < a.n4; q += stride) {
-                            float4 d = D4[q];
-                            const float4 h = PH[q], g = SH[q], sv = S4[q], t = T4[q], rt = RT[q];
-                            d.x += fa * h.x + fo * g.x; d.y += fa * h.y + fo * g.y;
-                            d.z += fa * h.z + fo * g.z; d.w += fa * h.w + fo * g.w;
-                            D4[q] = d;
-                            const float4 rv = make_float4(sv.x - fo * t.x, sv.y - fo * t.y, sv.z - fo * t.z, sv.w - fo * t.w);
-                            R4[q] = rv;
-                            r2 += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
-                            rtr2 += rt.x * rv.x + rt.y * rv.y + rt.z * rv.z + rt.w * rv.w;
-                        }
-                        float v2[2] = {r2, rtr2};
-                        block_store_f<2>(v2, a.partial, G);
-                    }
-                    if (!grid_sync(a.bar)) goto timeout;
-                    {
-                        double s2c[2];
-                        grid_sum<2>(a.partial, G, s2c);
-                        rr = s2c[0];
-                        rtr = s2c[1];
+                        double s4[4];
+                        grid_sum<4>(a.partial, G, s4);
+                        omega = block_once([=] { return s4[0] / s4[1]; });
+                        rr = fmax(0.0, ssum - 2.0 * omega * s4[0] + omega * omega * s4[1]);
+                        rtr = s4[2] - omega * s4[3];
                     }
                     rho2 = rho1;
                     nit++;
+                    pending = true;
                 }
             }
+            // the last pass's updates of d (float4 elements) are read below per element by other
+            // threads
+            if (!grid_sync(a.bar)) goto timeout;
             // x += scale |r| d (FP64); the next residual gathers x across the grid
             {
                 const double f = a.scale * res;
@@ -948,7 +959,7 @@ int spin_setup(Ctx &c, const fg_mesh *m, const fg_region *regs, int nreg, const 
     int bps = S->mixed ? 4 : 2;
     if (const char *env = std::getenv("FG_SPIN_BLOCKS_PER_SM")) bps = std::max(1, std::atoi(env));
     S->grid = std::max(1, std::min(std::min(std::max(1, per_sm), bps) * c.nsm, (nn + 255) / 256));
-    if (cudaMalloc(&S->partial, 3 * sizeof(double) * std::max(1024, S->grid)) != cudaSuccess) return FG_ECUDA;
+    if (cudaMalloc(&S->partial, 4 * sizeof(double) * std::max(1024, S->grid)) != cudaSuccess) return FG_ECUDA;
     c.spin_s = S->out;
     return FG_OK;
 }
