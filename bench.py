@@ -697,8 +697,10 @@ def bench_learned_workload(args):
 
 def bench_spin(args):
     """The film with the spin-accumulation coupling: current injected through the x = 400 nm
-    face (jn = 1e5 A/m^2, polarisation along y: Hst of the order of Ms, so that the fixed
-    dt = 5e-14 s stays stable), the x = 0 face grounded (V = 0, s = 0);
+    face (jn = 1e3 A/m^2, polarisation along y; the spin field enters the next step's element
+    integrals explicitly, and at the fixed dt = 5e-14 s a current of 1e5 A/m^2 made the
+    velocity grow tenfold per step, while 1e3 keeps the run stable), the x = 0 face grounded
+    (V = 0, s = 0);
     permalloy-like transport parameters (sigma 5e6 S/m, N0 1e47, P 0.5, l_sd 1 nm, l_sf 5 nm).
     FP32 body + FP64 refinement with the previous-step guess, with and without the coupling,
     same state and angles; the spin solve (FP64 BiCGSTAB over 3 x 242k unknowns) runs in
@@ -715,7 +717,7 @@ def bench_spin(args):
     mesh = dict(mesh, tri_reg=reg)
     sp = dict(sigma=5e6, dens_state=1e47, P=0.5, lsd=1e-9, lsf=5e-9)
     regs = [dict(Ae=1e-11, Ms=795774.7, alpha=0.5, **sp), dict(Ae=AE, Ms=MS, alpha=ALPHA, **sp)]
-    bc = [dict(), dict(), dict(V=0.0, s=(0, 0, 0)), dict(jn=1e5, uP=(0, 1, 0))]
+    bc = [dict(), dict(), dict(V=0.0, s=(0, 0, 0)), dict(jn=1e3, uP=(0, 1, 0))]
     u0 = initial_state(mesh)
     H = np.zeros(3)
     fg.rng_seed(SEED)
