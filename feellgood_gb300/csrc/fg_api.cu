@@ -229,6 +229,13 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
         for (int k = 0; k < 3; k++) {
             d.uk[k] = g.uk[k]; d.ex[k] = g.ex[k]; d.ey[k] = g.ey[k]; d.ez[k] = g.ez[k];
         }
+        auto pair = [](double x) {
+            const float h = (float)x;
+            return make_float2(h, (float)(x - (double)h));
+        };
+        d.A_ds = pair(g.Ae);
+        d.edm_ds = pair(-0.5 * FG_MU0 * g.Ms);
+        d.ez_ds = pair(-FG_MU0 * g.Ms);
     }
     // magnetic tetrahedra and nodes (src/mesh.h:115-131)
     std::vector<unsigned char> mag(nn, 0);
@@ -584,6 +591,18 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
         CK(upload(&c.cq32, cq32));
         CK(dalloc(&c.src_qf, std::max(1, c.nsrc)));
         if (c.src_q2) CK(dalloc(&c.src_q2f, std::max(1, c.nsrc)));
+        if (c.nft > 0) {
+            std::vector<float4> t32(4 * (size_t)c.nft);
+            for (int f = 0; f < c.nft; f++) {
+                const DevTri &T = htc[f];
+                float v[16];
+                for (int k = 0; k < 3; k++) v[k] = (float)T.n[k];
+                for (int g = 0; g < 4; g++) v[3 + g] = (float)(T.dMs * T.w[g]);
+                for (int k = 0; k < 9; k++) v[7 + k] = (float)(T.dMs * T.beta[k]);
+                for (int q = 0; q < 4; q++) t32[4 * (size_t)f + q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            }
+            CK(upload(&c.tri32, t32));
+        }
     }
     CK(cudaDeviceSynchronize());
     return FG_OK;
@@ -698,7 +717,7 @@ void fg_destroy(fg_ctx *h) {
                     c.v[0], c.v[1], c.phi[0], c.phi[1], c.phiv[0], c.phiv[1], c.ep, c.eq, c.ep32, c.eq32, c.Dl32,
                     c.slot, c.Dl, c.rhs, c.x, c.bv, c.W, c.fv, c.partial, c.bar, c.dres, c.src_q, c.tri_slot,
                     c.pot, c.epart, c.src_dst, c.src_q2, c.tri_slot2, c.pot2, c.tri_be, c.hsp, c.da_ds, c.J_ds, c.state_ds,
-                    c.dstate32, c.da32, c.cq32, c.src_qf, c.src_q2f, c.tri_ds};
+                    c.dstate32, c.da32, c.cq32, c.src_qf, c.src_q2f, c.tri_ds, c.tri32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     fmm64_free(c);

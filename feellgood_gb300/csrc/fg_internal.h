@@ -23,6 +23,7 @@ struct DevRegion {
     double uk[3], ex[3], ey[3], ez[3];
     double hst;  // spin accumulation: Hst = hst * s at the Gauss points (0 without the coupling)
     float2 Abis_ds, alpha_ds;  // double-single copies for the double-single element kernel
+    float2 A_ds, edm_ds, ez_ds;  // double-single A, -mu0 Ms / 2 and -mu0 Ms for the energies
 };
 
 // The double-single element slots are scaled by 2^DS_SLOT_SCALE (the Jacobian is scaled on
@@ -273,6 +274,7 @@ struct Ctx {
     float *dstate32 = nullptr;           // NEXT - CURRENT in FP32: u [3 nn], then v [3 nn]
     float *da32 = nullptr, *cq32 = nullptr;  // FP32 da [12][nmt] and -Ms detJ [nmt] (incremental demag)
     float *src_qf = nullptr, *src_q2f = nullptr;  // FP32 charges of the change (FMM leaf order)
+    float4 *tri32 = nullptr;  // per triangle n, dMs w_g, dMs beta in FP32 (charges of the change)
     bool charges32 = false;              // the FMM evaluation reads src_qf / src_q2f
     void *fmm64 = nullptr;               // FP64 tree at the FP32 tree's depth, built on first use
     double *epart = nullptr;     // energy partials

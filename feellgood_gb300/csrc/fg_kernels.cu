@@ -35,6 +35,7 @@ __constant__ double c_cws[4];     // sum_g c_cw[i][g]
 __constant__ double c_tps;        // sum_g c_tpds[g]
 __constant__ double c_fa[3][4];   // triangle rule (src/triangle.h:42-64)
 __constant__ float2 c_fa_ds[3][4];  // the same weights as double-single pairs
+__constant__ float c_fa32[3][4];    // and in FP32 (charges of the incremental demag)
 __constant__ double c_fpds[4];
 
 // ---------------------------------------------------------------------------------
@@ -1116,7 +1117,7 @@ __global__ void k_charges(int nmt, int nft, const int4 *__restrict__ tet, const 
 template <int NPI, int NPF, int NQ>
 __global__ void k_charges32(int nmt, int nft, const int4 *__restrict__ tet, const float *__restrict__ da32,
                             const float *__restrict__ cq32, const int4 *__restrict__ tri,
-                            const DevTri *__restrict__ tc, const float *__restrict__ m0, const float *__restrict__ m1,
+                            const float4 *__restrict__ tc32, const float *__restrict__ m0, const float *__restrict__ m1,
                             const int *__restrict__ dst, float *__restrict__ q0, float *__restrict__ q1,
                             double *__restrict__ ts0, double *__restrict__ ts1) {
     const float *mm[2] = {m0, m1};
@@ -1147,28 +1148,32 @@ __global__ void k_charges32(int nmt, int nft, const int4 *__restrict__ tet, cons
             }
         }
     } else if (k < nmt + nft) {
+        // per triangle in FP32 from constants formed on the host: n, dMs w_g, dMs beta
         const int f = k - nmt;
         const int4 I = tri[f];
         const int ind[3] = {I.x, I.y, I.z};
-        const DevTri &T = tc[f];
+        const float4 *T = tc32 + 4 * (size_t)f;
+        const float4 t0 = T[0], t1 = T[1], t2 = T[2], t3 = T[3];
+        const float n[3] = {t0.x, t0.y, t0.z};
+        const float wq[4] = {t0.w, t1.x, t1.y, t1.z};
+        const float be[9] = {t1.w, t2.x, t2.y, t2.z, t2.w, t3.x, t3.y, t3.z, t3.w};
 #pragma unroll
         for (int h = 0; h < NQ; h++) {
-            double sn[3];
+            float sn[3];
 #pragma unroll
             for (int i = 0; i < 3; i++) {
                 const float *pm = mm[h] + 3 * (size_t)ind[i];
-                sn[i] = (double)pm[0] * T.n[0] + (double)pm[1] * T.n[1] + (double)pm[2] * T.n[2];
+                sn[i] = pm[0] * n[0] + pm[1] * n[1] + pm[2] * n[2];
             }
 #pragma unroll
             for (int g = 0; g < NPF; g++) {
-                const double un = c_fa[0][g] * sn[0] + c_fa[1][g] * sn[1] + c_fa[2][g] * sn[2];
+                const float un = c_fa32[0][g] * sn[0] + c_fa32[1][g] * sn[1] + c_fa32[2][g] * sn[2];
                 const size_t sidx = (size_t)nmt * NPI + (size_t)f * NPF + g;
-                qq[h][dst[sidx]] = (T.dMs != 0.0) ? (float)(T.dMs * T.w[g] * un) : 0.f;
+                qq[h][dst[sidx]] = wq[g] * un;
             }
 #pragma unroll
             for (int i = 0; i < 3; i++)
-                ts[h][3 * (size_t)f + i] =
-                    T.dMs * (T.beta[3 * i] * sn[0] + T.beta[3 * i + 1] * sn[1] + T.beta[3 * i + 2] * sn[2]);
+                ts[h][3 * (size_t)f + i] = (double)(be[3 * i] * sn[0] + be[3 * i + 1] * sn[1] + be[3 * i + 2] * sn[2]);
         }
     }
 }
@@ -1267,21 +1272,13 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
 #pragma unroll
         for (int i = 0; i < 4; i++) cw[i] = ds_from(c_cws[i]);
         const dsf Hd[3] = {ds_from(Hx), ds_from(Hy), ds_from(Hz)};
-        // the region's constants as double-single pairs, formed again only when the region
-        // changes (their FP64 -> pair conversions run on the 1/64-rate FP64 pipe)
-        int rlast = -1;
-        dsf rA = {0.f, 0.f}, rD = {0.f, 0.f}, rZ = {0.f, 0.f};
         for (int k = t0; k < t1; k += stride) {
             const int4 I = tet[k];
             const int ind[4] = {I.x, I.y, I.z, I.w};
-            const int rg = treg[k];
-            if (rg != rlast) {
-                const DevRegion &R = regs[rg];
-                rA = ds_from(R.A);
-                rD = ds_from(-0.5 * FG_MU0 * R.Ms);
-                rZ = ds_from(-FG_MU0 * R.Ms);
-                rlast = rg;
-            }
+            // the region's constants as double-single pairs formed on the host (forming them
+            // here would put FP64 conversions on the 1/64-rate FP64 pipe for every tet)
+            const DevRegion &R = regs[treg[k]];
+            const dsf rA = {R.A_ds.x, R.A_ds.y}, rD = {R.edm_ds.x, R.edm_ds.y}, rZ = {R.ez_ds.x, R.ez_ds.y};
             dsf un[4][3], ph[4], d[4][3];
 #pragma unroll
             for (int i = 0; i < 4; i++) {
@@ -1581,6 +1578,10 @@ void upload_rules(bool one_point) {
                 fad[i][g] = make_float2(h, (float)(fa[i][g] - (double)h));
             }
         cudaMemcpyToSymbol(c_fa_ds, fad, sizeof(fad));
+        float fa32[3][4];
+        for (int i = 0; i < 3; i++)
+            for (int g = 0; g < 4; g++) fa32[i][g] = (float)fa[i][g];
+        cudaMemcpyToSymbol(c_fa32, fa32, sizeof(fa32));
     }
     cudaMemcpyToSymbol(c_fpds, fp, sizeof(fp));
 }
@@ -1755,26 +1756,26 @@ cudaError_t launch_state_diff(Ctx &c) {
 cudaError_t launch_charges32(Ctx &c, int nq) {
     const int n = c.nmt + c.nft;
     if (n == 0) return cudaSuccess;
-    if (!c.dstate32 || !c.src_qf || !c.src_dst || (nq == 2 && (!c.src_q2f || !c.tri_slot2)))
+    if (!c.dstate32 || !c.src_qf || !c.src_dst || (c.nft > 0 && !c.tri32) || (nq == 2 && (!c.src_q2f || !c.tri_slot2)))
         return cudaErrorInvalidValue;
     const float *du = c.dstate32, *dv = c.dstate32 + 3 * (size_t)c.nn;
     if (nq == 2) {
         if (c.npi_t == 5)
             k_charges32<5, 4, 2><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da32, c.cq32, c.tri,
-                                                                         c.tri_c, du, dv, c.src_dst, c.src_qf,
+                                                                         c.tri32, du, dv, c.src_dst, c.src_qf,
                                                                          c.src_q2f, c.tri_slot, c.tri_slot2);
         else
             k_charges32<1, 1, 2><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da32, c.cq32, c.tri,
-                                                                         c.tri_c, du, dv, c.src_dst, c.src_qf,
+                                                                         c.tri32, du, dv, c.src_dst, c.src_qf,
                                                                          c.src_q2f, c.tri_slot, c.tri_slot2);
     } else {
         if (c.npi_t == 5)
             k_charges32<5, 4, 1><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da32, c.cq32, c.tri,
-                                                                         c.tri_c, du, du, c.src_dst, c.src_qf,
+                                                                         c.tri32, du, du, c.src_dst, c.src_qf,
                                                                          c.src_qf, c.tri_slot, c.tri_slot);
         else
             k_charges32<1, 1, 1><<<nblocks(n, 128), 128, 0, c.stream>>>(c.nmt, c.nft, c.tet, c.da32, c.cq32, c.tri,
-                                                                         c.tri_c, du, du, c.src_dst, c.src_qf,
+                                                                         c.tri32, du, du, c.src_dst, c.src_qf,
                                                                          c.src_qf, c.tri_slot, c.tri_slot);
     }
     return cudaGetLastError();
