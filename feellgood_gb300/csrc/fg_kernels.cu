@@ -33,6 +33,7 @@ __constant__ float c_tpds32[5];  // the same weights in FP32 (charges of the inc
 __constant__ double c_cw[4][5];   // c_ta[i][g] * c_tpds[g]: weight of vertex i at Gauss point g per unit detJ
 __constant__ double c_cws[4];     // sum_g c_cw[i][g]
 __constant__ double c_tps;        // sum_g c_tpds[g]
+__constant__ float2 c_cws_dsp[4], c_tps_dsp;  // the same as double-single pairs (energies)
 __constant__ double c_fa[3][4];   // triangle rule (src/triangle.h:42-64)
 __constant__ float2 c_fa_ds[3][4];  // the same weights as double-single pairs
 __constant__ float c_fa32[3][4];    // and in FP32 (charges of the incremental demag)
@@ -1267,11 +1268,22 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
         Hx = h[0]; Hy = h[1]; Hz = h[2];
     }
     if (dsp) {
+        // every constant as a double-single pair formed once (host, or one thread per block):
+        // per-thread FP64 set-up and FP64 block sums would keep the 1/64-rate FP64 pipe busy
+        // longer than the tets of a thread take on the FP32 pipes
         const float2 *uds = st_ds, *pds = st_ds + 3 * (size_t)nn_ds;
-        dsf cw[4], tp = ds_from(c_tps);
+        __shared__ dsf Hsh[3];
+        if (threadIdx.x == 0) {
+            Hsh[0] = ds_from(Hx);
+            Hsh[1] = ds_from(Hy);
+            Hsh[2] = ds_from(Hz);
+        }
+        __syncthreads();
+        dsf cw[4];
+        const dsf tp = {c_tps_dsp.x, c_tps_dsp.y};
 #pragma unroll
-        for (int i = 0; i < 4; i++) cw[i] = ds_from(c_cws[i]);
-        const dsf Hd[3] = {ds_from(Hx), ds_from(Hy), ds_from(Hz)};
+        for (int i = 0; i < 4; i++) cw[i] = {c_cws_dsp[i].x, c_cws_dsp[i].y};
+        const dsf Hd[3] = {Hsh[0], Hsh[1], Hsh[2]};
         for (int k = t0; k < t1; k += stride) {
             const int4 I = tet[k];
             const int ind[4] = {I.x, I.y, I.z, I.w};
@@ -1321,13 +1333,11 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
             dacc[5] = ds_add(dacc[5], su[1]);
             dacc[6] = ds_add(dacc[6], su[2]);
         }
-#pragma unroll
-        for (int q = 0; q < 7; q++) acc[q] += std::ldexp(ds_to(dacc[q]), -DS_SLOT_SCALE);
         t1 = t0;  // the FP64 tet loop below has nothing left to do
+        dsf dtri = {0.f, 0.f};
         if (tri_ds) {
             // the surface demag term of the triangles (no surface anisotropy) in double-single:
             // per triangle the normal and the Gauss weights times 0.5 mu0 dMs as pairs
-            dsf dtri = {0.f, 0.f};
             for (int f = f0; f < f1; f += stride) {
                 const int4 I = tri[f];
                 const int ind[3] = {I.x, I.y, I.z};
@@ -1363,8 +1373,39 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
                 }
                 dtri = ds_add(dtri, dm);
             }
-            acc[2] += ds_to(dtri);
             f1 = f0;  // the FP64 triangle loop below has nothing left to do
+        }
+        // block sums in double-single (warp shuffles of both words, then the warps' sums in a
+        // fixed order), converted to FP64 once per block; the FP64 triangle loop's sums (with
+        // surface anisotropy) follow in acc
+        __shared__ dsf wsum[8][32];
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        dsf v8[8] = {dacc[0], dacc[1], dacc[2], dacc[3], dacc[4], dacc[5], dacc[6], dtri};
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                v8[q] = ds_add(v8[q], dsf{__shfl_xor_sync(0xffffffffu, v8[q].h, o),
+                                          __shfl_xor_sync(0xffffffffu, v8[q].l, o)});
+            if (lane == 0) wsum[q][warp] = v8[q];
+        }
+        __syncthreads();
+        if (threadIdx.x < 8) {
+            dsf t = {0.f, 0.f};
+            for (int w = 0; w < nw; w++) t = ds_add(t, wsum[threadIdx.x][w]);
+            wsum[threadIdx.x][0] = t;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int q = 0; q < 7; q++) acc[q] += std::ldexp(ds_to(wsum[q][0]), -DS_SLOT_SCALE);
+            acc[2] += ds_to(wsum[7][0]);
+        }
+        if (tri_ds) {  // no FP64 triangle loop (uniform over the block): thread 0 holds the sums
+            if (threadIdx.x == 0)
+#pragma unroll
+                for (int q = 0; q < 7; q++) partial[q * gridDim.x + blockIdx.x] = acc[q];
+            return;
         }
     }
     for (int k = t0; k < t1; k += stride) {
@@ -1568,6 +1609,17 @@ void upload_rules(bool one_point) {
     cudaMemcpyToSymbol(c_cw, cw, sizeof(cw));
     cudaMemcpyToSymbol(c_cws, cws, sizeof(cws));
     cudaMemcpyToSymbol(c_tps, &tps, sizeof(tps));
+    {
+        auto pair = [](double x) {
+            const float h = (float)x;
+            return make_float2(h, (float)(x - (double)h));
+        };
+        float2 cwd[4];
+        for (int i = 0; i < 4; i++) cwd[i] = pair(cws[i]);
+        const float2 tpd = pair(tps);
+        cudaMemcpyToSymbol(c_cws_dsp, cwd, sizeof(cwd));
+        cudaMemcpyToSymbol(c_tps_dsp, &tpd, sizeof(tpd));
+    }
     upload_rules_ds(ta, tp);
     cudaMemcpyToSymbol(c_fa, fa, sizeof(fa));
     {
