@@ -208,6 +208,13 @@ static void fill_par(SegPar &P, const fg_sample_step &s) {
     P.cr = std::cos(s.basis_angle);
     P.sr = std::sin(s.basis_angle);
     P.c0 = s.prefactor * FG_THETA * s.dt * FG_GAMMA0;
+    auto pair = [](double x) {
+        const float h = (float)x;
+        return make_float2(h, (float)(x - (double)h));
+    };
+    for (int k = 0; k < 3; k++) P.H_ds[k] = pair(s.Hext[k]);
+    P.rdt_ds = pair(FG_GAMMA0 * s.dt);
+    P.kv_ds = pair(FG_THETA * s.dt);
 }
 
 

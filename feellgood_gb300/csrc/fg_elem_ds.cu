@@ -55,18 +55,13 @@ __global__ void __launch_bounds__(128) k_tet_ds(int nmt, const int4 *__restrict_
                                                 const SegPar *__restrict__ seg) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nmt) return;
-    if (seg) {  // batch: the tet's sample carries dt and the applied field
+    if (seg) {  // batch: the tet's sample carries dt and the applied field (pairs formed on the host)
         const SegPar &P = seg[tet_seg[t]];
-        dsf v = ds_from(P.H[0]);
-        Hx2 = make_float2(v.h, v.l);
-        v = ds_from(P.H[1]);
-        Hy2 = make_float2(v.h, v.l);
-        v = ds_from(P.H[2]);
-        Hz2 = make_float2(v.h, v.l);
-        v = ds_from(FG_GAMMA0 * P.dt);
-        rdt2 = make_float2(v.h, v.l);
-        v = ds_from(FG_THETA * P.dt);
-        kv2 = make_float2(v.h, v.l);
+        Hx2 = P.H_ds[0];
+        Hy2 = P.H_ds[1];
+        Hz2 = P.H_ds[2];
+        rdt2 = P.rdt_ds;
+        kv2 = P.kv_ds;
     }
     const int4 I = tet[t];
     const int ind[4] = {I.x, I.y, I.z, I.w};

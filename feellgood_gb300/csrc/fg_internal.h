@@ -73,6 +73,9 @@ struct SegPar {
     double H[3];    // applied field, A/m
     double cr, sr;  // cos / sin of the basis rotation angle of Node::setBasis
     double c0;      // prefactor * theta * dt * gamma0
+    // double-single pairs for the double-single element kernel, formed on the host: H,
+    // gamma0 dt and theta dt
+    float2 H_ds[3], rdt_ds, kv_ds;
 };
 
 // Per-sample results accumulated over a multi-step batch run.
