@@ -29,6 +29,8 @@ struct DevRegion {
 // The double-single element slots are scaled by 2^DS_SLOT_SCALE (the Jacobian is scaled on
 // the host) so that their low words stay normal FP32 numbers.
 constexpr int DS_SLOT_SCALE = 70;
+constexpr double DS_SLOT_INV = 0x1p-70;  // 2^-DS_SLOT_SCALE: the scale undone by an exact product
+static_assert(DS_SLOT_SCALE == 70 && DS_SLOT_INV * 0x1p70 == 1.0, "DS_SLOT_INV is 2^-DS_SLOT_SCALE");
 
 // Gauss rules of the tets (5 points, or 1) and triangles (4 points, or 1): shape functions
 // a_i(g) and weights per unit Jacobian (src/tetra.h:27-81, src/triangle.h:43-66).

@@ -482,10 +482,10 @@ __global__ void k_node64(int nn, const int *__restrict__ inc_ptr, const int *__r
             a2 = ds_add(a2, {h.z, l.z});
             a3 = ds_add(a3, {h.w, l.w});
         }
-        dl = std::ldexp(ds_to(a0), -DS_SLOT_SCALE);
-        be0 = std::ldexp(ds_to(a1), -DS_SLOT_SCALE);
-        be1 = std::ldexp(ds_to(a2), -DS_SLOT_SCALE);
-        be2 = std::ldexp(ds_to(a3), -DS_SLOT_SCALE);
+        dl = ds_to(a0) * DS_SLOT_INV;  // exact: a product by a power of two
+        be0 = ds_to(a1) * DS_SLOT_INV;
+        be1 = ds_to(a2) * DS_SLOT_INV;
+        be2 = ds_to(a3) * DS_SLOT_INV;
     } else {
         for (int k = inc_ptr[i]; k < inc_ptr[i + 1]; k++) {
             const double4 s = slot[inc[k]];
@@ -1398,7 +1398,7 @@ __global__ void __launch_bounds__(256) k_energy(int nmt, int nft, const int4 *__
         __syncthreads();
         if (threadIdx.x == 0) {
 #pragma unroll
-            for (int q = 0; q < 7; q++) acc[q] += std::ldexp(ds_to(wsum[q][0]), -DS_SLOT_SCALE);
+            for (int q = 0; q < 7; q++) acc[q] += ds_to(wsum[q][0]) * DS_SLOT_INV;
             acc[2] += ds_to(wsum[7][0]);
         }
         if (tri_ds) {  // no FP64 triangle loop (uniform over the block): thread 0 holds the sums
