@@ -62,7 +62,7 @@ class fg_opts(C.Structure):
                 ("mlp_train_every", C.c_int), ("fmm_native_fp64", C.c_int),
                 ("solver_lpr", C.c_int), ("solver_blocks", C.c_int), ("spin_acc", C.c_int), ("spin_tol", C.c_double),
                 ("spin_max_iter", C.c_int), ("demag_increment", C.c_int), ("fmm_overlap", C.c_int),
-                ("fmm_tree_host", C.c_int)]
+                ("fmm_tree_host", C.c_int), ("solver_threads", C.c_int)]
 
 
 class fg_step_report(C.Structure):
@@ -209,7 +209,7 @@ def rng_seed(seed):
 
 class fg_checkpoint_shape(C.Structure):
     _fields_ = [("n_nodes", C.c_int), ("n_mag_tets", C.c_int), ("precision", C.c_int), ("solver_lpr", C.c_int),
-                ("solver_blocks", C.c_int), ("fmm_depth", C.c_int)]
+                ("solver_blocks", C.c_int), ("fmm_depth", C.c_int), ("solver_threads", C.c_int)]
 
 
 class fg_checkpoint_meta(C.Structure):

@@ -138,6 +138,7 @@ void fg_opts_default(fg_opts *o) {
     o->demag_increment = 1;
     o->fmm_overlap = 0;
     o->fmm_tree_host = 0;
+    o->solver_threads = 0;
 }
 
 const char *fg_strerror(int s) {
@@ -177,6 +178,10 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
         }
         c.opts.demag = FG_DEMAG_FMM;
         c.opts.profile = 0;
+    }
+    if (c.opts.solver_threads != 0 && c.opts.solver_threads != 256 && c.opts.solver_threads != 512) {
+        c.err = "fg_create: solver_threads must be 0, 256 or 512";
+        return FG_EINVAL;
     }
     if (!m || !regs || nreg <= 0 || m->n_nodes <= 0 || m->n_tets <= 0 || !m->xyz || !m->tet4 || !m->tet_region) {
         c.err = "fg_create: missing mesh or region data";

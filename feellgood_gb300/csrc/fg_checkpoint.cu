@@ -3,7 +3,8 @@
 //
 // File layout (little-endian, fields written one by one, no padding):
 //   "FGGPUCK1" | u32 version | i32 n_nodes, n_mag_tets, precision, solver_lpr,
-//   solver_blocks, fmm_depth | meta: f64 t0, t, dt, dt_soft_max | i64 steps,
+//   solver_blocks, fmm_depth, solver_threads (version 2; version 1 ends at fmm_depth) |
+//   meta: f64 t0, t, dt, dt_soft_max | i64 steps,
 //   output_index | u32 rng_seed | i64 rng_draws | f64 E[4] | f64 u[3n], v[3n], phi[n],
 //   phiv[n] (CURRENT, node order of the set-up mesh) | u64 FNV-1a of all preceding bytes
 #include <cstdint>
@@ -21,7 +22,7 @@ int fmm_info(const Ctx &c, int *L, int *nleaf, double *n_m2l, double *n_p2p);
 namespace {
 
 constexpr char MAGIC[8] = {'F', 'G', 'G', 'P', 'U', 'C', 'K', '1'};
-constexpr uint32_t VERSION = 1;
+constexpr uint32_t VERSION = 2;  // 2: solver_threads after fmm_depth (1 is still read)
 
 struct Writer {
     std::vector<unsigned char> buf;
@@ -68,6 +69,7 @@ void put_header(Writer &w, const fg_checkpoint_shape &s, const fg_checkpoint_met
     w.put(VERSION);
     w.put<int32_t>(s.n_nodes); w.put<int32_t>(s.n_mag_tets); w.put<int32_t>(s.precision);
     w.put<int32_t>(s.solver_lpr); w.put<int32_t>(s.solver_blocks); w.put<int32_t>(s.fmm_depth);
+    w.put<int32_t>(s.solver_threads);
     w.put(m.t0); w.put(m.t); w.put(m.dt); w.put(m.dt_soft_max);
     w.put<int64_t>(m.steps); w.put<int64_t>(m.output_index);
     w.put<uint32_t>(m.rng_seed); w.put<int64_t>(m.rng_draws);
@@ -92,9 +94,12 @@ int get_header(const std::string &path, std::vector<unsigned char> &buf, Reader 
     if (fnv1a(buf.data(), buf.size() - 8) != stored) return FG_EIO;
     char magic[8];
     r.get_bytes(magic, 8);
-    if (std::memcmp(magic, MAGIC, 8) != 0 || r.get<uint32_t>() != VERSION) return FG_EIO;
+    if (std::memcmp(magic, MAGIC, 8) != 0) return FG_EIO;
+    const uint32_t version = r.get<uint32_t>();
+    if (version != 1 && version != VERSION) return FG_EIO;
     s.n_nodes = r.get<int32_t>(); s.n_mag_tets = r.get<int32_t>(); s.precision = r.get<int32_t>();
     s.solver_lpr = r.get<int32_t>(); s.solver_blocks = r.get<int32_t>(); s.fmm_depth = r.get<int32_t>();
+    s.solver_threads = version >= 2 ? r.get<int32_t>() : 0;
     m.t0 = r.get<double>(); m.t = r.get<double>(); m.dt = r.get<double>(); m.dt_soft_max = r.get<double>();
     m.steps = r.get<int64_t>(); m.output_index = r.get<int64_t>();
     m.rng_seed = r.get<uint32_t>(); m.rng_draws = r.get<int64_t>();
@@ -120,6 +125,7 @@ int fg_checkpoint_save(fg_ctx *h, const char *path, const fg_checkpoint_meta *me
     if (c.opts.precision == FG_PREC_FP32_REFINE) {
         s.solver_lpr = c.lpr;
         s.solver_blocks = c.mixed_grid;
+        s.solver_threads = c.mixed_threads;
     }
     if (c.fmm) {
         int L = 0, nl = 0;

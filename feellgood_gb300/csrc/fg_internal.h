@@ -289,6 +289,7 @@ struct Ctx {
     // persistent-kernel launch shapes
     int bicg_grid = 0, bicg_block = 256;
     int mixed_grid = 0;
+    int mixed_threads = 256;  // threads per block of the single-system solver (256 or 512)
     int lpr = 0;  // lanes per row of the mixed solver's operator applications (0: not chosen yet)
 
     // timings

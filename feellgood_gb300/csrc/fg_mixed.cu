@@ -62,8 +62,11 @@ __device__ __forceinline__ SegView seg_view(const MixedArgs &a) {
         body(i_, i_ < sv.hi, (int)threadIdx.x % LPR);                                                   \
     }
 
+// Blocks of 256 threads (two per SM at 128 registers) or 512 (one per SM: twice the warps of
+// a 256-thread block to hide the operator's gathers, with the same number of blocks meeting at
+// each grid barrier); every block-level reduction works for either size.
 template <int LPR>
-__global__ void __launch_bounds__(256, 2) k_mixed(MixedArgs a) {
+__global__ void __launch_bounds__(512, 1) k_mixed(MixedArgs a) {
     const int G = gridDim.x;
     const SegView sv = seg_view(a);
     const int rstride = (sv.b1 - sv.b0) * blockDim.x;
@@ -568,7 +571,7 @@ cudaError_t launch_mixed(Ctx &c, double dt, double prefactor) {
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(256);
+    cfg.blockDim = dim3(c.batch ? 256 : c.mixed_threads);
     cfg.stream = c.stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
@@ -604,11 +607,29 @@ cudaError_t launch_barrier_timeout_probe(Ctx &c, int *out) {
     return cudaLaunchKernelEx(&cfg, k_barrier_timeout_probe, c.bar, out);
 }
 
+// Co-resident blocks per SM of the variant with LPR lanes per row at the given block size.
+static int mixed_blocks_per_sm(int lpr, int threads) {
+    int n = 0;
+    if (lpr == 8) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mixed<8>, threads, 0);
+    else if (lpr == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mixed<4>, threads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mixed<1>, threads, 0);
+    return n;
+}
+
 cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle) {
     if (c.lpr > 0) return cudaSuccess;
     if (c.opts.solver_lpr == 1 || c.opts.solver_lpr == 4 || c.opts.solver_lpr == 8) {
         c.lpr = c.opts.solver_lpr;
         if (c.opts.solver_blocks > 0 && !c.batch) c.mixed_grid = std::min(c.opts.solver_blocks, c.mixed_grid);
+        if (c.opts.solver_threads == 512 && !c.batch) {
+            const int per_sm = mixed_blocks_per_sm(c.lpr, 512);
+            if (per_sm < 1) {
+                c.err = "solver_threads 512: a block of 512 threads does not fit on an SM";
+                return cudaErrorInvalidConfiguration;
+            }
+            c.mixed_threads = 512;
+            c.mixed_grid = std::min(c.mixed_grid, per_sm * c.nsm);  // all blocks co-resident
+        }
         return cudaSuccess;
     }
     const int cand[3] = {1, 4, 8};
@@ -626,19 +647,25 @@ cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle) {
     if ((e = cudaMemcpyAsync(keep_v, c.v[1], n3, cudaMemcpyDeviceToDevice, c.stream)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(keep_u, c.u[1], n3, cudaMemcpyDeviceToDevice, c.stream)) != cudaSuccess) return e;
     double best = 1e300;
-    int bestv = 1, bestg = c.mixed_grid;
+    int bestv = 1, bestg = c.mixed_grid, bestt = 256;
     std::vector<SolveResult> res(c.batch ? c.nseg : 1);
-    // grid sizes of the single-system solver: all co-resident blocks, or 2 or 1 per SM (fewer
-    // blocks make each grid barrier cheaper; a batch keeps its per-sample block ranges)
-    std::vector<int> grids{c.mixed_grid};
-    if (!c.batch)
+    // launch shapes of the single-system solver: all co-resident blocks of 256 threads, or 2 or
+    // 1 per SM (fewer blocks make each grid barrier cheaper), and one block of 512 threads per
+    // SM (as few blocks, twice the warps); a batch keeps its per-sample block ranges
+    std::vector<int2> shapes{make_int2(c.mixed_grid, 256)};
+    if (!c.batch) {
         for (int g : {2 * c.nsm, c.nsm})
-            if (g < c.mixed_grid) grids.push_back(g);
+            if (g < c.mixed_grid) shapes.push_back(make_int2(g, 256));
+        if (c.nsm <= c.mixed_grid) shapes.push_back(make_int2(c.nsm, 512));
+    }
     const int gmax = c.mixed_grid;
-    for (int vi = 0; vi < 3 * (int)grids.size(); vi++) {
+    for (int vi = 0; vi < 3 * (int)shapes.size(); vi++) {
         const int v = cand[vi % 3];
+        const int2 sh = shapes[vi / 3];
+        if (sh.y == 512 && mixed_blocks_per_sm(v, 512) < 1) continue;  // does not fit: not a candidate
         c.lpr = v;
-        c.mixed_grid = grids[vi / 3];
+        c.mixed_grid = sh.x;
+        c.mixed_threads = sh.y;
         for (int rep = 0; rep < 2; rep++) {  // the first run of each variant warms it up
             if ((e = launch_node(c, angle)) != cudaSuccess) break;
             cudaEventRecord(e0, c.stream);
@@ -654,6 +681,7 @@ cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle) {
                 best = ms / it;
                 bestv = v;
                 bestg = c.mixed_grid;
+                bestt = c.mixed_threads;
             }
         }
         if (e != cudaSuccess) break;
@@ -666,7 +694,10 @@ cudaError_t mixed_autotune(Ctx &c, double dt, double prefactor, double angle) {
     c.acc_active = acc;
     c.lpr = bestv;
     c.mixed_grid = e == cudaSuccess ? bestg : gmax;
-    if (c.opts.verbose) fprintf(stderr, "mixed solver: %d lane(s) per row, %d blocks\n", bestv, c.mixed_grid);
+    c.mixed_threads = e == cudaSuccess ? bestt : 256;
+    if (c.opts.verbose)
+        fprintf(stderr, "mixed solver: %d lane(s) per row, %d blocks of %d threads\n", bestv, c.mixed_grid,
+                c.mixed_threads);
     return e;
 }
 

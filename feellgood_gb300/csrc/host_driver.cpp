@@ -249,10 +249,12 @@ int run_impl(Run &R, const char *settings_path, unsigned int seed, int verbose, 
     fg_opts_default(&o);
     o.solver_lpr = S.solver_lpr;
     o.solver_blocks = S.solver_blocks;
+    o.solver_threads = S.solver_threads;
     if (S.fmm_depth > 0) o.fmm_leaf = -S.fmm_depth;
     if (resume) {
         o.solver_lpr = ck.solver_lpr;
         o.solver_blocks = ck.solver_blocks;
+        o.solver_threads = ck.solver_threads;
         if (ck.fmm_depth > 0) o.fmm_leaf = -ck.fmm_depth;
     }
     o.tol = S.tol;

@@ -449,6 +449,7 @@ void apply_yaml(Settings &S, const std::shared_ptr<YNode> &y) {
         };
         count("solver_lanes_per_row", S.solver_lpr);
         count("solver_blocks", S.solver_blocks);
+        count("solver_threads", S.solver_threads);
         count("fmm_depth", S.fmm_depth);
     }
 }

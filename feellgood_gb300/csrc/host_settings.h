@@ -74,6 +74,7 @@ struct Settings {
     double recenter_threshold = 0.1;
     int checkpoint_every = 0;    // write <out_dir>/<sim_name>.ckpt after every n-th output row
     int solver_lpr = 0, solver_blocks = 0, fmm_depth = 0;  // fixed solver / FMM choices (0: timed)
+    int solver_threads = 0;                                 // threads per solver block (0: 256)
     std::string resume_file;     // continue the run of this checkpoint
     void finish();
 };

@@ -108,9 +108,9 @@ typedef struct {
                              (1 thread per row, 4, 8); 0 (default): the fastest, timed on the
                              first step */
     int solver_blocks;    /* FP32 + refinement solver with solver_lpr set: persistent blocks
-                             (0: all co-resident blocks). Fixing both (and fmm_leaf = -depth)
-                             makes runs repeat bit for bit: the timed choices decide the
-                             order of the solver's reductions */
+                             (0: all co-resident blocks). Fixing both, solver_threads (and
+                             fmm_leaf = -depth) makes runs repeat bit for bit: the timed
+                             choices decide the order of the solver's reductions */
     int spin_acc;         /* 1: spin accumulation coupling (spin_accumulation.enable): the
                              electrostatic potential is solved once, the spin accumulation s
                              in every fg_compute_all, and its field Hst enters the next
@@ -133,6 +133,10 @@ typedef struct {
                              translation launches: the film's step is 0.1 ms slower overlapped) */
     int fmm_tree_host;    /* FMM octree build: 0 (default) Morton keys and their radix sort on the
                              device; 1 keys and a comparison sort on the host (the same tree) */
+    int solver_threads;   /* FP32 + refinement solver with solver_lpr set: threads per persistent
+                             block, 256 or 512 (one block per SM: twice the warps to hide the
+                             operator's gathers, the same number of grid-barrier participants);
+                             0: 256 */
 } fg_opts;
 
 typedef struct {
@@ -230,8 +234,9 @@ int fg_set_drift(fg_ctx *ctx, int direction, double vdrift);
  * keeps u and phi to 7 digits and loses v and phiv, src/save.cpp:164-186). The file holds the
  * CURRENT state (u, v, phi, phiv in FP64), the caller's run metadata below, and the choices
  * that fix the order of the solver's and the FMM's arithmetic (solver lanes per row and
- * blocks, FMM depth), so that a run resumed from it with those choices (fg_opts.solver_lpr,
- * solver_blocks, fmm_leaf = -depth) repeats the uninterrupted run bit for bit (the learned
+ * blocks and threads, FMM depth), so that a run resumed from it with those choices
+ * (fg_opts.solver_lpr, solver_blocks, solver_threads, fmm_leaf = -depth) repeats the
+ * uninterrupted run bit for bit (the learned
  * guess's network is not saved: with it the resumed run agrees to the solver tolerance).
  * Binary, little-endian, with an FNV-1a checksum; fg_checkpoint_peek reads the header
  * without a context. Call fg_checkpoint_save after fg_compute_all. */
@@ -247,6 +252,7 @@ typedef struct {
 typedef struct {
     int n_nodes, n_mag_tets, precision;
     int solver_lpr, solver_blocks, fmm_depth; /* 0 where not used */
+    int solver_threads;                       /* 0 where not used (and in version-1 files) */
 } fg_checkpoint_shape;
 int fg_checkpoint_save(fg_ctx *ctx, const char *path, const fg_checkpoint_meta *meta);
 int fg_checkpoint_peek(const char *path, fg_checkpoint_shape *shape, fg_checkpoint_meta *meta);

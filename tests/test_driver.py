@@ -165,7 +165,7 @@ def test_checkpoint_resume_is_bitwise(tmp_path, golden_dir, gpu):
     rep = fg.run(tmp_path / "rest.json", seed=12345)  # the checkpoint's seed and stream position win
     assert abs(rep["t"] - total) < 1e-20
     fixed = dict(solver_lanes_per_row=head["solver_lpr"], solver_blocks=head["solver_blocks"],
-                 fmm_depth=head["fmm_depth"])
+                 solver_threads=head["solver_threads"], fmm_depth=head["fmm_depth"])
     full = dict(st, gpu=dict(gpu, **fixed), outputs=dict(st["outputs"], file_basename="full", final_time=total,
                                                         evol_columns=cols))
     (tmp_path / "full.json").write_text(json.dumps(full))

@@ -182,6 +182,28 @@ def test_mixed_precision_solve(tol):
     assert np.max(np.abs(np.linalg.norm(sg["u"], axis=1) - 1.0)) < 1e-14
 
 
+@pytest.mark.parametrize("lpr,threads", [(1, 256), (1, 512), (4, 512), (8, 512)])
+def test_mixed_solver_block_shapes(lpr, threads):
+    """The FP32 + refinement solver with 256- or 512-thread persistent blocks (one of 512 per
+    SM: the same kernel, its reductions over 16 warps) on a mesh that spreads over many blocks:
+    the same FP64 stopping test, and v within the tolerance's reach of the FP64 solver's."""
+    tol = 1e-10
+    m = cases.cuboid(40, 40, 10)
+    u = cases.perturbed_state(m["xyz"], seed=21, sigma=0.3)
+    v = cases.tangent_field(u, seed=22)
+    H = np.array([0.0, 0.0, 0.02])
+    phi0 = np.zeros(len(u))
+    out = {}
+    for prec, kw in ((fg.FG_PREC_FP64, {}), (fg.FG_PREC_FP32_REFINE, dict(solver_lpr=lpr, solver_threads=threads))):
+        c = fg.Context(m, cases.regions(), tol=tol, max_iter=5000, precision=prec, demag=fg.FG_DEMAG_DIRECT, **kw)
+        c.set_state(u, v, phi0, phi0)  # the same (zero) potentials for both solvers
+        r = c.step(DT, 1.0, H, 0.3)
+        assert r["status"] == fg.FG_OK and r["res"] <= tol * r["rhsn"]
+        out[prec] = c.get_state(1)["v"]
+        c.close()
+    assert _rel(out[fg.FG_PREC_FP32_REFINE], out[fg.FG_PREC_FP64]) <= 50 * tol
+
+
 @pytest.mark.parametrize("one_point", [False, True])
 def test_surface_anisotropy(one_point):
     """Tri::integrales (src/triangle.cpp:6-36): the surface anisotropy of the magnetic

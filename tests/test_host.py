@@ -80,13 +80,16 @@ def test_missing_mesh_file():
     assert e.value.status == fg.api.FG_EIO
 
 
-def _checkpoint_bytes(n=4, nmt=2, meta=None):
-    """A checkpoint in the documented layout (fg_checkpoint.cu): header, meta, state, FNV-1a."""
+def _checkpoint_bytes(n=4, nmt=2, meta=None, version=1):
+    """A checkpoint in the documented layout (fg_checkpoint.cu): header, meta, state, FNV-1a.
+    Version 2 adds the solver's threads per block after the FMM depth."""
     import struct
     m = dict(t0=0.0, t=1.5e-12, dt=2e-14, dt_soft_max=3e-14, steps=75, output_index=4, rng_seed=9, rng_draws=80,
              E=[1.0, 2.0, -3.0, 4.0])
     m.update(meta or {})
-    b = b"FGGPUCK1" + struct.pack("<I6i", 1, n, nmt, 1, 4, 304, 6)
+    b = b"FGGPUCK1" + struct.pack("<I6i", version, n, nmt, 1, 4, 304, 6)
+    if version >= 2:
+        b += struct.pack("<i", 512)
     b += struct.pack("<4d", m["t0"], m["t"], m["dt"], m["dt_soft_max"])
     b += struct.pack("<qqIq", m["steps"], m["output_index"], m["rng_seed"], m["rng_draws"])
     b += struct.pack("<4d", *m["E"])
@@ -105,6 +108,7 @@ def test_checkpoint_header_and_checksum(tmp_path):
     h = fg.checkpoint_peek(p)
     assert (h["n_nodes"], h["n_mag_tets"], h["precision"], h["solver_lpr"], h["solver_blocks"], h["fmm_depth"]) == \
         (4, 2, 1, 4, 304, 6)
+    assert h["solver_threads"] == 0  # a version-1 file has no block size (256 threads)
     for k in ("t0", "t", "dt", "dt_soft_max", "steps", "output_index", "rng_seed", "rng_draws", "E"):
         assert h[k] == m[k], k
     bad = bytearray(raw)
@@ -113,5 +117,21 @@ def test_checkpoint_header_and_checksum(tmp_path):
     with pytest.raises(fg.FgError):
         fg.checkpoint_peek(p)
     p.write_bytes(raw[:-9])
+    with pytest.raises(fg.FgError):
+        fg.checkpoint_peek(p)
+
+
+def test_checkpoint_version2_header(tmp_path):
+    """Version 2 of the layout carries the solver's threads per block after the FMM depth; a
+    version the library does not know is rejected."""
+    raw, m = _checkpoint_bytes(version=2)
+    p = tmp_path / "b.ckpt"
+    p.write_bytes(raw)
+    h = fg.checkpoint_peek(p)
+    assert (h["solver_lpr"], h["solver_blocks"], h["fmm_depth"], h["solver_threads"]) == (4, 304, 6, 512)
+    for k in ("t", "steps", "rng_draws", "E"):
+        assert h[k] == m[k], k
+    raw3, _ = _checkpoint_bytes(version=3)
+    p.write_bytes(raw3)
     with pytest.raises(fg.FgError):
         fg.checkpoint_peek(p)
