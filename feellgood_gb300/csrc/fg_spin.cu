@@ -312,7 +312,9 @@ timeout:
 //                 in FP64 once per block, to the relative target max(inner_tol,
 //                 0.3 tol |b| / |r|);
 //   x += scale |r| d in FP64.
-__global__ void __launch_bounds__(256, 4) k_spin_mixed(SpinArgs a) {
+// Launched as four blocks of 256 threads per SM or one of 1024 (the same 32 warps per SM, a
+// quarter of the blocks meeting at each grid barrier); every reduction works for either size.
+__global__ void __launch_bounds__(1024, 1) k_spin_mixed(SpinArgs a) {
     const int G = gridDim.x, nn = a.nn;
     const int stride = G * blockDim.x, i0 = blockIdx.x * blockDim.x + threadIdx.x;
     const int gstride = G * (int)blockDim.x / SPIN_LPR;
@@ -670,7 +672,7 @@ int cg_dir(const std::vector<int> &ptr, const std::vector<int> &col, const std::
 }
 
 struct SpinState {
-    int nn = 0, grid = 0;
+    int nn = 0, grid = 0, threads = 256;  // persistent blocks and their threads
     int *ptr = nullptr, *col = nullptr;
     double *A = nullptr, *dinv = nullptr, *cc = nullptr, *G = nullptr, *L = nullptr, *xd = nullptr;
     unsigned char *dir = nullptr;
@@ -948,17 +950,28 @@ int spin_setup(Ctx &c, const fg_mesh *m, const fg_region *regs, int nreg, const 
             return FG_ECUDA;
         }
     }
+    // block size: 256 threads for the FP64 kernel; the FP32 body one block of 1024 per SM, the
+    // warps of four 256-thread blocks with a quarter of the blocks at each grid barrier
+    // (measured on the 1.2M-tet film: 68 against 72 us per iteration); FG_SPIN_THREADS=256
+    // selects four blocks of 256
+    if (S->mixed) S->threads = 1024;
+    if (const char *env = std::getenv("FG_SPIN_THREADS"))
+        if (std::atoi(env) == 256) S->threads = 256;
     int per_sm = 0, per_sm_mixed = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spin_bicg, 256, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_mixed, k_spin_mixed, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_mixed, k_spin_mixed, S->threads, 0);
     if (S->mixed) per_sm = per_sm_mixed;
+    if (per_sm < 1 && S->threads != 256) {  // a 1024-thread block does not fit: back to 256
+        S->threads = 256;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spin_mixed, 256, 0);
+    }
     // blocks per SM: the FP64 kernel runs best with two (fewer blocks make each grid barrier
     // cheaper), the FP32 body with four (its latency-bound sweeps want the warps; measured
     // 77 against 93 us per iteration on the 1.2M-tet film); FG_SPIN_BLOCKS_PER_SM overrides
     // it (up to the kernel's occupancy)
     int bps = S->mixed ? 4 : 2;
     if (const char *env = std::getenv("FG_SPIN_BLOCKS_PER_SM")) bps = std::max(1, std::atoi(env));
-    S->grid = std::max(1, std::min(std::min(std::max(1, per_sm), bps) * c.nsm, (nn + 255) / 256));
+    S->grid = std::max(1, std::min(std::min(std::max(1, per_sm), bps) * c.nsm, (nn + S->threads - 1) / S->threads));
     if (cudaMalloc(&S->partial, 4 * sizeof(double) * std::max(1024, S->grid)) != cudaSuccess) return FG_ECUDA;
     c.spin_s = S->out;
     return FG_OK;
@@ -1007,7 +1020,7 @@ cudaError_t launch_spin(Ctx &c) {
     if (e != cudaSuccess) return e;
     void *args[] = {&a};
     return cudaLaunchCooperativeKernel(S->mixed ? (void *)k_spin_mixed : (void *)k_spin_bicg, dim3(S->grid),
-                                       dim3(256), args, 0, c.stream);
+                                       dim3(S->mixed ? S->threads : 256), args, 0, c.stream);
 }
 
 int spin_info(const Ctx &c, int *status, int *iters, double *V, int *v_iters) {
