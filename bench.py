@@ -703,8 +703,8 @@ def bench_spin(args):
     (V = 0, s = 0);
     permalloy-like transport parameters (sigma 5e6 S/m, N0 1e47, P 0.5, l_sd 1 nm, l_sf 5 nm).
     FP32 body + FP64 refinement with the previous-step guess, with and without the coupling,
-    same state and angles; the spin solve (FP64 BiCGSTAB over 3 x 242k unknowns) runs in
-    every compute_all."""
+    same state and angles; the spin solve (FP32 BiCGSTAB body with FP64 refinement over
+    3 x 242k unknowns) runs in every compute_all."""
     import __graft_entry__
     __graft_entry__.build_product()
     import feellgood_gb300 as fg
@@ -762,6 +762,7 @@ def bench_spin(args):
             "warmup": args.warmup, "ms_per_step": out["spin"]["ms_per_step"], "higher_is_better": True,
             "dtype": "f32+f64", "data": "synthetic (seeded smoothed random film state)",
             "config": {"workload": " ".join(bench_spin.__doc__.split())}, "detail": out,
+            "clocks": out["spin"]["clocks"],
             "spin_cost_ms_per_step": out["spin"]["ms_per_step"] - out["no_spin"]["ms_per_step"]}
     print(json.dumps(line), flush=True)
 
