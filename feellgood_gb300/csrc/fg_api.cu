@@ -452,12 +452,12 @@ static int create_impl(fg_ctx *h, const fg_mesh *m, const fg_region *regs, int n
     CK(upload(&c.tet, htet));
     CK(upload(&c.da, da));
     CK(upload(&c.detJ, detJ));
-    // double-single element integrals for the FP32 + refinement path without anisotropy
-    // (FG_DS_ELEMENTS=0 in the environment keeps the FP64 kernel, for comparisons)
+    // double-single element integrals for the FP32 + refinement path without anisotropy, with
+    // or without the spin coupling (FG_DS_ELEMENTS=0 in the environment keeps the FP64 kernel,
+    // for comparisons)
     {
         const char *env = std::getenv("FG_DS_ELEMENTS");
-        c.elem_ds = c.opts.precision == FG_PREC_FP32_REFINE && !c.aniso && !c.opts.spin_acc &&
-                    !(env && env[0] == '0');
+        c.elem_ds = c.opts.precision == FG_PREC_FP32_REFINE && !c.aniso && !(env && env[0] == '0');
     }
     if (c.elem_ds) {
         const int s = elem_ds_setup(c, da, detJ);

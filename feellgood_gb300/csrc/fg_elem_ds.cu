@@ -7,8 +7,9 @@
 // tet volumes ~1e-27 keep their low words normal in FP32); the node kernel sums them in
 // double-single and converts each node's sums to FP64 once. The assembled system then
 // agrees with the FP64 path's to ~1e-14 relative, far below the solver tolerance. Used when
-// there is no anisotropy, space field or spin accumulation (those keep the FP64 kernels);
-// batches read each tet's dt and field from its sample.
+// there is no anisotropy or space field (those keep the FP64 kernels), with the spin
+// accumulation's Hst terms (src/tetra.cpp:248-303) in the same arithmetic when the coupling
+// is on; batches read each tet's dt and field from its sample.
 #include <cmath>
 
 #include "fg_ds.cuh"
@@ -29,10 +30,12 @@ __device__ __forceinline__ dsf ld2(const float2 *p, size_t k) {
 }
 __device__ __forceinline__ dsf cs(float2 v) { return {v.x, v.y}; }
 
-// CURRENT u, phi, phiv of every node as double-single (read by ~24 tets each)
+// CURRENT u, phi, phiv of every node as double-single (read by ~24 tets each); with s0 set
+// also the spin accumulation s and the velocity v of CURRENT (the spin coupling's terms)
 __global__ void k_state_ds(int nn, const double *__restrict__ u0, const double *__restrict__ phi0,
                            const double *__restrict__ phiv0, float2 *__restrict__ uds, float2 *__restrict__ phids,
-                           float2 *__restrict__ phivds) {
+                           float2 *__restrict__ phivds, const double *__restrict__ s0, const double *__restrict__ v0,
+                           float2 *__restrict__ sds, float2 *__restrict__ vds) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
 #pragma unroll
@@ -43,16 +46,28 @@ __global__ void k_state_ds(int nn, const double *__restrict__ u0, const double *
     const dsf p = ds_from(phi0[i]), q = ds_from(phiv0[i]);
     phids[i] = make_float2(p.h, p.l);
     phivds[i] = make_float2(q.h, q.l);
+    if (s0) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const dsf a = ds_from(s0[3 * (size_t)i + c]), b = ds_from(v0[3 * (size_t)i + c]);
+            sds[3 * (size_t)i + c] = make_float2(a.h, a.l);
+            vds[3 * (size_t)i + c] = make_float2(b.h, b.l);
+        }
+    }
 }
 
-template <int NPI>
+// SPIN: the spin coupling (single contexts only): Hst(g) = hst sum_i a_i(g) s_i adds U(g).Hst(g)
+// to uHeff(g) and sum_g w_g a_i(g) (Hst(g) - (Hst(g).U(g)) s_dt V(g)) to BE_i, s_dt = theta dt
+// gamma0 (sdt2), from the double-single s and v of CURRENT (sds, vds).
+template <int NPI, bool SPIN>
 __global__ void __launch_bounds__(128) k_tet_ds(int nmt, const int4 *__restrict__ tet, const float2 *__restrict__ da,
                                                 const float2 *__restrict__ Js, const int *__restrict__ treg,
                                                 const DevRegion *__restrict__ regs, const float2 *__restrict__ uds,
                                                 const float2 *__restrict__ phids, const float2 *__restrict__ phivds,
                                                 float2 Hx2, float2 Hy2, float2 Hz2, float2 rdt2, float2 kv2,
                                                 float4 *__restrict__ slot, const int *__restrict__ tet_seg,
-                                                const SegPar *__restrict__ seg) {
+                                                const SegPar *__restrict__ seg, const float2 *__restrict__ sds,
+                                                const float2 *__restrict__ vds, float2 sdt2) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nmt) return;
     if (seg) {  // batch: the tet's sample carries dt and the applied field (pairs formed on the host)
@@ -110,11 +125,48 @@ __global__ void __launch_bounds__(128) k_tet_ds(int nmt, const int4 *__restrict_
     const dsf hx = ds_neg(ds_mul(Abis, gradsq));
     const dsf one = {1.f, 0.f};
     dsf contrib[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    // spin coupling: hst s and v at the vertices, and the per-vertex sums of its BE term
+    const bool spin = SPIN && (R.hst_ds.x != 0.f || R.hst_ds.y != 0.f);
+    dsf sn[4][3], vn[4][3], sw[4][3];
+    if constexpr (SPIN) {
+        const dsf hst = cs(R.hst_ds);
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                sw[i][c] = {0.f, 0.f};
+                sn[i][c] = spin ? ds_mul(hst, ld2(sds, 3 * (size_t)ind[i] + c)) : dsf{0.f, 0.f};
+                vn[i][c] = spin ? ld2(vds, 3 * (size_t)ind[i] + c) : dsf{0.f, 0.f};
+            }
+    }
+    const dsf sdt = {sdt2.x, sdt2.y};
 #pragma unroll
     for (int g = 0; g < NPI; g++) {
         dsf h = hx;
 #pragma unroll
         for (int i = 0; i < 4; i++) h = ds_fma(cs(c_ta_ds[i][g]), uh[i], h);
+        if constexpr (SPIN) {
+            if (spin) {
+                const dsf t0 = cs(c_ta_ds[0][g]), t1 = cs(c_ta_ds[1][g]), t2 = cs(c_ta_ds[2][g]),
+                          t3 = cs(c_ta_ds[3][g]);
+                dsf U[3], Hs[3], Vg[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    U[c] = ds_fma(t3, un[3][c], ds_fma(t2, un[2][c], ds_fma(t1, un[1][c], ds_mul(t0, un[0][c]))));
+                    Hs[c] = ds_fma(sn[3][c], t3, ds_fma(sn[2][c], t2, ds_fma(sn[1][c], t1, ds_mul(sn[0][c], t0))));
+                    Vg[c] = ds_fma(t3, vn[3][c], ds_fma(t2, vn[2][c], ds_fma(t1, vn[1][c], ds_mul(t0, vn[0][c]))));
+                }
+                const dsf hu = ds_fma(Hs[2], U[2], ds_fma(Hs[1], U[1], ds_mul(Hs[0], U[0])));
+                h = ds_add(h, hu);
+                const dsf hs = ds_mul(hu, sdt);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const dsf e = ds_sub(Hs[c], ds_mul(hs, Vg[c]));
+#pragma unroll
+                    for (int i = 0; i < 4; i++) sw[i][c] = ds_fma(cs(c_cw_ds[i][g]), e, sw[i][c]);
+                }
+            }
+        }
         dsf a;
         if (h.h > 0.f) {
             a = ds_fma(half_rdt, ds_gt(h, M) ? M : h, alpha);
@@ -136,6 +188,9 @@ __global__ void __launch_bounds__(128) k_tet_ds(int nmt, const int4 *__restrict_
         for (int c = 0; c < 3; c++) {
             const dsf ex = ds_fma(d[i][2], dU[2][c], ds_fma(d[i][1], dU[1][c], ds_mul(d[i][0], dU[0][c])));
             BE[c] = ds_fma(nva, ex, ds_mul(aw, H[c]));
+            if constexpr (SPIN) {
+                if (spin) BE[c] = ds_fma(J, sw[i][c], BE[c]);
+            }
         }
         const dsf ct = ds_mul(J, contrib[i]);
         slot[2 * (4 * (size_t)t + i)] = make_float4(ct.h, BE[0].h, BE[1].h, BE[2].h);
@@ -178,7 +233,7 @@ int elem_ds_setup(Ctx &c, const std::vector<double> &da, const std::vector<doubl
     for (size_t k = 0; k < n; k++) jj[k] = split(std::ldexp(detJ[k], DS_SLOT_SCALE));
     if (cudaMalloc(&c.da_ds, sizeof(float2) * std::max<size_t>(1, dd.size())) != cudaSuccess ||
         cudaMalloc(&c.J_ds, sizeof(float2) * std::max<size_t>(1, n)) != cudaSuccess ||
-        cudaMalloc(&c.state_ds, sizeof(float2) * 5 * std::max(1, c.nn)) != cudaSuccess)
+        cudaMalloc(&c.state_ds, sizeof(float2) * (c.opts.spin_acc ? 11 : 5) * std::max(1, c.nn)) != cudaSuccess)
         return FG_ECUDA;
     if (cudaMemcpy(c.da_ds, dd.data(), sizeof(float2) * dd.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(c.J_ds, jj.data(), sizeof(float2) * n, cudaMemcpyHostToDevice) != cudaSuccess)
@@ -188,25 +243,35 @@ int elem_ds_setup(Ctx &c, const std::vector<double> &da, const std::vector<doubl
 
 cudaError_t launch_state_ds(Ctx &c, const double *u, const double *phi, const double *phiv) {
     float2 *uds = c.state_ds, *phids = uds + 3 * (size_t)c.nn, *phivds = phids + c.nn;
-    k_state_ds<<<(c.nn + 255) / 256, 256, 0, c.stream>>>(c.nn, u, phi, phiv, uds, phids, phivds);
+    k_state_ds<<<(c.nn + 255) / 256, 256, 0, c.stream>>>(c.nn, u, phi, phiv, uds, phids, phivds, nullptr, nullptr,
+                                                          nullptr, nullptr);
     return cudaGetLastError();
 }
 
 cudaError_t launch_tet_ds(Ctx &c, double dt, const double H[3]) {
     if (c.nmt == 0) return cudaSuccess;
     float2 *uds = c.state_ds, *phids = uds + 3 * (size_t)c.nn, *phivds = phids + c.nn;
-    cudaError_t e = launch_state_ds(c, c.u[0], c.phi[0], c.phiv[0]);
+    // with the spin coupling the buffer also holds s and v of CURRENT (allocated for it)
+    const bool spin = c.spin_s != nullptr;
+    float2 *sds = phivds + c.nn, *vds = sds + 3 * (size_t)c.nn;
+    cudaError_t e;
+    if (spin) {
+        k_state_ds<<<(c.nn + 255) / 256, 256, 0, c.stream>>>(c.nn, c.u[0], c.phi[0], c.phiv[0], uds, phids, phivds,
+                                                              c.spin_s, c.v[0], sds, vds);
+        e = cudaGetLastError();
+    } else {
+        e = launch_state_ds(c, c.u[0], c.phi[0], c.phiv[0]);
+    }
     if (e != cudaSuccess) return e;
     const float2 hx = split(H[0]), hy = split(H[1]), hz = split(H[2]);
-    const float2 rdt = split(FG_GAMMA0 * dt), kv = split(FG_THETA * dt);
+    const float2 rdt = split(FG_GAMMA0 * dt), kv = split(FG_THETA * dt), sdt = split(FG_THETA * dt * FG_GAMMA0);
     float4 *slot = reinterpret_cast<float4 *>(c.slot);
     const int b = 128, g = (c.nmt + b - 1) / b;
-    if (c.npi_t == 5)
-        k_tet_ds<5><<<g, b, 0, c.stream>>>(c.nmt, c.tet, c.da_ds, c.J_ds, c.treg, c.regs, uds, phids, phivds, hx, hy,
-                                          hz, rdt, kv, slot, c.tet_seg, c.batch ? c.seg_par : nullptr);
-    else
-        k_tet_ds<1><<<g, b, 0, c.stream>>>(c.nmt, c.tet, c.da_ds, c.J_ds, c.treg, c.regs, uds, phids, phivds, hx, hy,
-                                          hz, rdt, kv, slot, c.tet_seg, c.batch ? c.seg_par : nullptr);
+    auto k = c.npi_t == 5 ? (spin ? k_tet_ds<5, true> : k_tet_ds<5, false>)
+                          : (spin ? k_tet_ds<1, true> : k_tet_ds<1, false>);
+    k<<<g, b, 0, c.stream>>>(c.nmt, c.tet, c.da_ds, c.J_ds, c.treg, c.regs, uds, phids, phivds, hx, hy, hz, rdt, kv,
+                             slot, c.tet_seg, c.batch ? c.seg_par : nullptr, spin ? sds : nullptr,
+                             spin ? vds : nullptr, sdt);
     return cudaGetLastError();
 }
 

@@ -24,6 +24,7 @@ struct DevRegion {
     double hst;  // spin accumulation: Hst = hst * s at the Gauss points (0 without the coupling)
     float2 Abis_ds, alpha_ds;  // double-single copies for the double-single element kernel
     float2 A_ds, edm_ds, ez_ds;  // double-single A, -mu0 Ms / 2 and -mu0 Ms for the energies
+    float2 hst_ds;               // double-single hst
 };
 
 // The double-single element slots are scaled by 2^DS_SLOT_SCALE (the Jacobian is scaled on
@@ -430,7 +431,7 @@ void upload_rules_ds(const double ta[4][5], const double tp[5]);
 cudaError_t launch_tet_ds(Ctx &c, double dt, const double H[3]);
 cudaError_t launch_state_ds(Ctx &c, const double *u, const double *phi, const double *phiv);
 inline bool drift_on(const Ctx &c) { return c.drift_dir >= 0 && c.drift_v != 0.0; }
-inline bool use_elem_ds(const Ctx &c) { return c.elem_ds && !c.hsp && !c.spin_s && !drift_on(c); }
+inline bool use_elem_ds(const Ctx &c) { return c.elem_ds && !c.hsp && !drift_on(c); }
 void recenter_free(Ctx &c);
 cudaError_t launch_select_params(Ctx &c);
 cudaError_t launch_advance(Ctx &c);

@@ -1639,7 +1639,7 @@ void upload_rules(bool one_point) {
 }
 
 cudaError_t launch_tet(Ctx &c, double dt, const double H[3]) {
-    if (use_elem_ds(c)) {  // FP32 + refinement, isotropic, no space field / spin / batch
+    if (use_elem_ds(c)) {  // FP32 + refinement, isotropic, no space field or drift (spin coupling included)
         if (c.tri_be && c.nft > 0) {
             if (c.npi_f == 4) k_tri_aniso<4><<<nblocks(c.nft, 128), 128, 0, c.stream>>>(c.nft, c.tri, c.tri_c, c.u[0], c.tri_be);
             else k_tri_aniso<1><<<nblocks(c.nft, 128), 128, 0, c.stream>>>(c.nft, c.tri, c.tri_c, c.u[0], c.tri_be);

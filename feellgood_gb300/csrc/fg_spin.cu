@@ -905,6 +905,8 @@ int spin_setup(Ctx &c, const fg_mesh *m, const fg_region *regs, int nreg, const 
         if (p.Ms > 0 && p.lsd != 0.0 && p.dens_state != 0.0) {
             const double D0 = 2.0 * p.sigma / (CHARGE_ELECTRON * CHARGE_ELECTRON * p.dens_state);
             hreg[r].hst = D0 / (p.lsd * p.lsd * FG_GAMMA0 * p.Ms);
+            const float hh = (float)hreg[r].hst;
+            hreg[r].hst_ds = make_float2(hh, (float)(hreg[r].hst - (double)hh));
         }
     }
     // device

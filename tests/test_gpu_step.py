@@ -385,6 +385,44 @@ def test_spin_accumulation_fp32_refine(spin_tol):
         assert _rel(c.debug_system()[0], o.export_system()[3]) <= 1e-9
 
 
+def test_double_single_elements_with_spin(monkeypatch):
+    """With the spin coupling the FP32 + refinement path keeps its double-single element
+    integrals, the Hst terms of Tet::integrales (src/tetra.cpp:248-303) included: on the same
+    state, potentials and s, the assembled RHS and operator agree with those of the FP64
+    element kernel (FG_DS_ELEMENTS=0) to 1e-12, while the coupling moves the RHS by far
+    more than that."""
+    m, regs_o, regs_g, tregs_o, bc = _spin_case()
+    u = cases.perturbed_state(m["xyz"], seed=45)
+    v = cases.tangent_field(u, seed=46)
+    H = np.array([1e4, 2e4, -3e4])
+    angle, pref = 0.3, fgo.prefactor(DT, DTMAX)
+    xs = np.random.default_rng(47).normal(size=(2, 2 * len(m["xyz"])))
+    out = {}
+    for name, env, spin in (("ds", None, 1), ("fp64", "0", 1), ("no_spin", None, 0)):
+        if env is None:
+            monkeypatch.delenv("FG_DS_ELEMENTS", raising=False)
+        else:
+            monkeypatch.setenv("FG_DS_ELEMENTS", env)
+        c = fg.Context(m, regs_g, bc, tol=1e-6, max_iter=5000, spin_acc=spin, spin_tol=1e-12, spin_max_iter=5000,
+                       precision=fg.FG_PREC_FP32_REFINE)
+        c.set_state(u, v)
+        c.compute_all(H)
+        if spin:
+            assert c.spin_info()["status"] == fg.FG_OK
+        c.step(DT, pref, H, angle)
+        out[name] = (c.debug_system()[0], [c.debug_apply(x) for x in xs])
+        c.close()
+    monkeypatch.delenv("FG_DS_ELEMENTS", raising=False)
+    rd, ad = out["ds"]
+    r64, a64 = out["fp64"]
+    print("ds vs FP64 elements with spin: rhs %.2e, operator %.2e; spin's share of the rhs %.2e"
+          % (_rel(rd, r64), max(_rel(a, b) for a, b in zip(ad, a64)), _rel(r64, out["no_spin"][0])))
+    assert _rel(rd, r64) <= 1e-12
+    for a, b in zip(ad, a64):
+        assert _rel(a, b) <= 1e-12
+    assert _rel(r64, out["no_spin"][0]) >= 1e-6
+
+
 def test_spin_boundary_conditions_checked():
     """A spin-accumulation context without exactly one jn surface, one V surface and one s
     surface is refused (the reference's checkBoundaryConditions exit)."""
