@@ -93,6 +93,11 @@ def test_settings_errors(tmp_path):
     p.write_text("mesh:\n  filename: a.msh\n  volume_regions:\n    v: {Ms: 1}\ninitial_magnetization: [sin(x), 0, 1]\n")
     with pytest.raises(fg.FgError):
         fg.settings_dump(p)
+    for key in ("solver_threads", "solver_blocks", "checkpoint_every"):  # counts >= 0
+        p.write_text("mesh:\n  filename: a.msh\n  volume_regions:\n    v: {Ms: 1}\ngpu: {%s: -1}\n" % key)
+        with pytest.raises(fg.FgError) as e:
+            fg.settings_dump(p)
+        assert key in str(e.value)
 
 
 def _last_row(path):

@@ -27,6 +27,23 @@ def test_library_exports_every_declared_symbol():
     assert len(names) >= 20
 
 
+def test_opts_mirror_matches_the_c_layout():
+    """The ctypes mirror of fg_opts has the C struct's size and field offsets: fg_opts_default
+    (host code) writes every field of a buffer larger than the mirror, leaves the bytes after
+    it alone, and the mirror reads the documented defaults at its field offsets, the last
+    field included."""
+    import ctypes as C
+    n = C.sizeof(fg.api.fg_opts)
+    raw = (C.c_ubyte * (n + 64))(*([0xA5] * (n + 64)))
+    fg.fg_lib().fg_opts_default(C.cast(raw, C.POINTER(fg.api.fg_opts)))
+    assert all(b == 0xA5 for b in raw[n:]), "fg_opts is larger in C than its mirror"
+    o = fg.api.fg_opts.from_buffer(raw)
+    assert (o.tol, o.max_iter, o.precision, o.refine_max, o.inner_tol) == (1e-6, 700, fg.FG_PREC_FP64, 20, 1e-5)
+    assert (o.mlp_train_steps, o.mlp_batch, o.mlp_lr, o.fmm_tensor, o.mlp_train_every) == (20, 16384, 1e-3, 1, 1)
+    assert (o.spin_tol, o.spin_max_iter, o.demag_increment) == (1e-8, 1000, 1)
+    assert (o.fmm_overlap, o.fmm_tree_host, o.solver_threads) == (0, 0, 0)
+
+
 def _same(a, b, keys=("xyz", "tets", "tet_reg", "tris", "tri_reg", "dMs")):
     for k in keys:
         assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), k
